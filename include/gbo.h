@@ -1,0 +1,168 @@
+/*
+ * gbo.h -- C ABI of the GB300-native NonhydrostaticModel time-stepping library
+ * (libgb300ocean.so).
+ *
+ * The library replaces the device side of Oceananigans.jl's
+ * `time_step!(model::NonhydrostaticModel{<:RungeKutta3TimeStepper}, Δt)`
+ * for RectilinearGrid / ImmersedBoundaryGrid(GridFittedBottom) models with
+ * Periodic x and y and Bounded (or Flat) z.  A host binding (Julia `ccall`,
+ * Python `ctypes`) keeps the reference's model API -- construction, `set!`,
+ * `time_step!`, `run!` -- and calls only these entry points.
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, enums.  No CUDA or torch types.
+ *   - Every entry point returns GBO_OK (0) or a negative GBO_ERR_* code and
+ *     never aborts; gbo_last_error() gives the message.  This mirrors the
+ *     reference throwing ArgumentError at construction
+ *     (src/Models/NonhydrostaticModels/nonhydrostatic_model.jl:150-175).
+ *   - Arrays crossing the boundary hold interior points only, column-major
+ *     with x fastest (Julia layout): index i + Nx*(j + Ny*k), 0-based.
+ *     w carries Nz+1 vertical faces on Bounded z (Face location,
+ *     src/Grids/grid_utils.jl:74-80); all other fields carry Nz levels.
+ *   - A handle is not thread-safe; distinct handles may be driven from
+ *     distinct host threads.  Work is issued on one CUDA stream per handle.
+ */
+#ifndef GBO_H
+#define GBO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GBO_OK                 0
+#define GBO_ERR_INVALID       -1  /* invalid argument or unsupported configuration */
+#define GBO_ERR_CUDA          -2  /* a CUDA runtime call failed */
+#define GBO_ERR_NAN           -3  /* NaN / Inf detected in the prognostic state */
+#define GBO_ERR_NOT_CONVERGED -4  /* iterative pressure solver hit maxiter */
+#define GBO_ERR_TIMEOUT       -5  /* a bounded device-side wait ran out */
+#define GBO_ERR_NO_DEVICE     -6  /* no CUDA device visible */
+#define GBO_ERR_STATE         -7  /* call out of order (e.g. stepping before set) */
+
+/* ---- enums --------------------------------------------------------------- */
+enum gbo_topology   { GBO_FLAT = 0, GBO_PERIODIC = 1, GBO_BOUNDED = 2 };
+enum gbo_float_type { GBO_FLOAT32 = 4, GBO_FLOAT64 = 8 };
+enum gbo_advection  { GBO_ADVECTION_NONE = 0, GBO_ADVECTION_CENTERED2 = 2, GBO_ADVECTION_WENO5 = 5 };
+enum gbo_closure    { GBO_CLOSURE_NONE = 0, GBO_CLOSURE_SMAGORINSKY_LILLY = 1,
+                      GBO_CLOSURE_AMD = 2 };
+enum gbo_solver     { GBO_SOLVER_FFT = 0, GBO_SOLVER_FOURIER_TRIDIAGONAL = 1,
+                      GBO_SOLVER_CONJUGATE_GRADIENT = 2 };
+enum gbo_precond    { GBO_PRECOND_FFT = 0, GBO_PRECOND_NONE = 1, GBO_PRECOND_LEARNED = 2 };
+
+/* field identifiers for set/get */
+#define GBO_FIELD_U      0
+#define GBO_FIELD_V      1
+#define GBO_FIELD_W      2
+#define GBO_FIELD_TRACER 3        /* tracer n is GBO_FIELD_TRACER + n */
+#define GBO_FIELD_PNHS   100      /* nonhydrostatic pressure (model.pressures.pNHS) */
+#define GBO_FIELD_PHY    101      /* hydrostatic pressure anomaly (model.pressures.pHY′) */
+#define GBO_FIELD_NU     102      /* eddy viscosity νₑ (closure_fields.νₑ) */
+#define GBO_FIELD_KAPPA  103      /* AMD tracer diffusivity κₑ of tracer 0 */
+
+#define GBO_MAX_TRACERS 4
+
+/* Grid: replaces RectilinearGrid(size, x, y, z, topology) and
+ * ImmersedBoundaryGrid(grid, GridFittedBottom(h))
+ * (src/Grids/rectilinear_grid.jl:266-305; src/ImmersedBoundaries/grid_fitted_bottom.jl:17). */
+typedef struct gbo_grid_desc {
+    int32_t size[3];          /* Nx, Ny, Nz (Nz = 1 with topology[2] == GBO_FLAT) */
+    int32_t topology[3];      /* x, y must be GBO_PERIODIC; z GBO_BOUNDED or GBO_FLAT */
+    double  x[2], y[2], z[2]; /* domain extents (z ignored when z_faces != NULL) */
+    const double* z_faces;    /* NULL: regular z; else Nz+1 increasing face positions */
+    const double* bottom_height; /* NULL: no immersed boundary; else Nx*Ny bottom heights h(x,y) */
+    int32_t float_type;       /* GBO_FLOAT32 or GBO_FLOAT64 */
+} gbo_grid_desc;
+
+/* Model physics: replaces NonhydrostaticModel(grid; advection, closure, buoyancy,
+ * coriolis, tracers, boundary_conditions, pressure_solver)
+ * (src/Models/NonhydrostaticModels/nonhydrostatic_model.jl:124-313). */
+typedef struct gbo_model_desc {
+    int32_t advection;               /* gbo_advection */
+    int32_t closure;                 /* gbo_closure */
+    double  closure_C;               /* Smagorinsky C (0.16) or AMD C (1/3) */
+    double  closure_Cb;              /* Lilly reduction factor Cb (1.0); unused by AMD */
+    double  closure_Pr;              /* turbulent Prandtl number for all tracers (1.0) */
+    int32_t ntracers;                /* 0..GBO_MAX_TRACERS */
+    int32_t buoyancy_tracer;         /* 1: tracer 0 is the BuoyancyTracer `b`; 0: no buoyancy */
+    int32_t has_coriolis;            /* 1: FPlane(f) with the EnstrophyConserving scheme */
+    double  coriolis_f;
+    double  tracer_flux_top[GBO_MAX_TRACERS];    /* FluxBoundaryCondition values (top) */
+    double  tracer_flux_bottom[GBO_MAX_TRACERS]; /* FluxBoundaryCondition values (bottom) */
+    int32_t pressure_solver;         /* gbo_solver */
+    int32_t preconditioner;          /* gbo_precond, CG only */
+    double  cg_reltol;               /* 0 -> sqrt(eps(FT)) as the reference defaults */
+    double  cg_abstol;               /* 0 -> sqrt(eps(FT)) */
+    int32_t cg_maxiter;              /* 0 -> Nx*Ny*Nz */
+} gbo_model_desc;
+
+typedef struct gbo_model gbo_model;
+
+/* Fill *d with the reference's defaults: WENO5, no closure, no tracers, FFT solver. */
+void gbo_model_desc_default(gbo_model_desc* d);
+
+/* Construct a model on the current CUDA device.
+ * Replaces NonhydrostaticModel(grid; ...) (nonhydrostatic_model.jl:124). */
+int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out);
+
+/* Release all device memory held by the model. */
+void gbo_model_destroy(gbo_model* m);
+
+/* Copy interior values of one field from host memory (dtype GBO_FLOAT32/64).
+ * Replaces set!(field, array) (src/Fields/set!.jl:46-70) for one field. */
+int gbo_set_field(gbo_model* m, int32_t field, const void* host, int32_t dtype, int64_t count);
+
+/* Finish `set!(model; kwargs...)`: mask immersed cells, update the state and,
+ * if enforce_incompressibility, project the velocities onto the divergence-free
+ * space (compute_pressure_correction!(model, 1) + make_pressure_correction!)
+ * and update again (src/Models/NonhydrostaticModels/set_nonhydrostatic_model.jl:39-74). */
+int gbo_set_finalize(gbo_model* m, int32_t enforce_incompressibility);
+
+/* Copy interior values of one field to host memory (dtype GBO_FLOAT32/64). */
+int gbo_get_field(gbo_model* m, int32_t field, void* host, int32_t dtype, int64_t count);
+
+/* Number of interior values of `field` (for sizing host buffers). */
+int64_t gbo_field_count(const gbo_model* m, int32_t field);
+
+/* Device pointer and element count of a field (zero-copy access for a host binding's
+ * unsafe_wrap / torch view).  The element type is the model's float type. */
+int gbo_field_device_pointer(gbo_model* m, int32_t field, void** dptr, int64_t* count);
+
+/* Advance nsteps RK3 time steps of size dt.
+ * Replaces time_step!(model::AbstractModel{<:RungeKutta3TimeStepper}, Δt)
+ * (src/TimeSteppers/runge_kutta_3.jl:103-168) with the NonhydrostaticModel substep
+ * (src/Models/NonhydrostaticModels/nonhydrostatic_rk3_substep.jl:31-63). */
+int gbo_time_step(gbo_model* m, double dt, int32_t nsteps);
+
+/* Clock (model.clock.time, model.clock.iteration; src/TimeSteppers/clock.jl). */
+int gbo_clock(const gbo_model* m, double* time, int64_t* iteration);
+
+/* Block until all work issued for the model has finished; returns the first
+ * deferred device error (NaN flag, solver non-convergence, CUDA error). */
+int gbo_synchronize(gbo_model* m);
+
+/* Iterations taken by the last conjugate-gradient pressure solve (0 for direct solvers). */
+int32_t gbo_last_solver_iterations(const gbo_model* m);
+
+/* Message describing the last error on this handle (or a global message if m is NULL). */
+const char* gbo_last_error(const gbo_model* m);
+
+/* Library version string. */
+const char* gbo_version(void);
+
+/* ---- standalone Poisson solve ---------------------------------------------
+ * Solve ∇²ϕ = rhs with the model's pressure solver on device buffers holding
+ * Nx*Ny*Nz interior values of the model's float type.
+ * Replaces solve!(ϕ, solver::FFTBasedPoissonSolver / FourierTridiagonalPoissonSolver, b)
+ * (src/Solvers/fft_based_poisson_solver.jl:94-124;
+ *  src/Solvers/fourier_tridiagonal_poisson_solver.jl:231-260)
+ * and, for the CG solver, solve!(x, ::ConjugateGradientPoissonSolver, rhs)
+ * (src/Solvers/conjugate_gradient_poisson_solver.jl; the rhs there is V·div). */
+int gbo_poisson_solve_device(gbo_model* m, void* phi_device, const void* rhs_device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBO_H */

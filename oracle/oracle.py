@@ -1,0 +1,178 @@
+"""ctypes harness for the FP64 CPU oracle (ocean_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.  The oracle is a
+C++ restatement of Oceananigans.jl's NonhydrostaticModel RK3 step; see the
+header of ocean_oracle.cpp for what it follows and how it is pinned.
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "ocean_oracle.cpp")
+
+GBO_FLAT, GBO_PERIODIC, GBO_BOUNDED = 0, 1, 2
+GBO_FLOAT32, GBO_FLOAT64 = 4, 8
+MAX_TRACERS = 4
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_int32 * 3), ("topology", ctypes.c_int32 * 3),
+                ("x", ctypes.c_double * 2), ("y", ctypes.c_double * 2), ("z", ctypes.c_double * 2),
+                ("z_faces", ctypes.POINTER(ctypes.c_double)),
+                ("bottom_height", ctypes.POINTER(ctypes.c_double)),
+                ("float_type", ctypes.c_int32)]
+
+
+class ModelDesc(ctypes.Structure):
+    _fields_ = [("advection", ctypes.c_int32), ("closure", ctypes.c_int32),
+                ("closure_C", ctypes.c_double), ("closure_Cb", ctypes.c_double), ("closure_Pr", ctypes.c_double),
+                ("ntracers", ctypes.c_int32), ("buoyancy_tracer", ctypes.c_int32),
+                ("has_coriolis", ctypes.c_int32), ("coriolis_f", ctypes.c_double),
+                ("tracer_flux_top", ctypes.c_double * MAX_TRACERS),
+                ("tracer_flux_bottom", ctypes.c_double * MAX_TRACERS),
+                ("pressure_solver", ctypes.c_int32), ("preconditioner", ctypes.c_int32),
+                ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32)]
+
+
+def build(force=False):
+    """Compile the oracle with g++ (OpenMP) into oracle/_build/liboracle.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp", SRC]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc)]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.orc_set_field.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_int64]
+        L.orc_get_field.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_int64]
+        L.orc_set_finalize.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_time_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.orc_poisson_solve.argtypes = [ctypes.c_void_p, dp, dp]
+        L.orc_z_spacings.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int]
+        L.orc_weno5.restype = ctypes.c_double
+        L.orc_weno5.argtypes = [dp, ctypes.c_int]
+        L.orc_clock.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_int64)]
+        L.orc_last_cg_iterations.argtypes = [ctypes.c_void_p]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+FIELD_IDS = {"u": 0, "v": 1, "w": 2, "p": 100, "pHY": 101, "nu": 102, "kappa": 103}
+
+
+class OracleModel:
+    """FP64 oracle of NonhydrostaticModel with the same descriptors as the CUDA library."""
+
+    def __init__(self, grid_desc, model_desc, tracers=()):
+        self._keep = grid_desc._keep if hasattr(grid_desc, "_keep") else None
+        self.grid = grid_desc
+        self.desc = model_desc
+        self.tracers = tuple(tracers)
+        self.h = lib().orc_create(ctypes.byref(grid_desc), ctypes.byref(model_desc))
+        Nx, Ny, Nz = grid_desc.size
+        self.flat = grid_desc.topology[2] == GBO_FLAT
+        self.shape = (Nx, Ny, 1 if self.flat else Nz)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def _fid(self, name):
+        if name in FIELD_IDS:
+            return FIELD_IDS[name]
+        return 3 + self.tracers.index(name)
+
+    def field_shape(self, name):
+        Nx, Ny, Nz = self.shape
+        if name == "w" and not self.flat:
+            return (Nx, Ny, Nz + 1)
+        return (Nx, Ny, Nz)
+
+    def set(self, **fields):
+        for name, val in fields.items():
+            shp = self.field_shape(name)
+            a = np.asfortranarray(np.broadcast_to(np.asarray(val, dtype=np.float64), shp))
+            flat = np.ascontiguousarray(a.ravel(order="F"))
+            rc = lib().orc_set_field(self.h, self._fid(name), _dptr(flat), flat.size)
+            if rc:
+                raise ValueError("oracle set failed for %s" % name)
+
+    def finalize_set(self, enforce_incompressibility=True):
+        return lib().orc_set_finalize(self.h, int(enforce_incompressibility))
+
+    def get(self, name):
+        shp = self.field_shape(name)
+        out = np.zeros(int(np.prod(shp)), dtype=np.float64)
+        rc = lib().orc_get_field(self.h, self._fid(name), _dptr(out), out.size)
+        if rc:
+            raise ValueError("oracle get failed for %s" % name)
+        return out.reshape(shp, order="F")
+
+    def time_step(self, dt, nsteps=1):
+        return lib().orc_time_step(self.h, float(dt), int(nsteps))
+
+    def clock(self):
+        t = ctypes.c_double()
+        it = ctypes.c_int64()
+        lib().orc_clock(self.h, ctypes.byref(t), ctypes.byref(it))
+        return t.value, it.value
+
+    def poisson_solve(self, rhs):
+        rhs = np.asfortranarray(np.asarray(rhs, dtype=np.float64).reshape(self.shape, order="F"))
+        flat = np.ascontiguousarray(rhs.ravel(order="F"))
+        out = np.zeros_like(flat)
+        lib().orc_poisson_solve(self.h, _dptr(out), _dptr(flat))
+        return out.reshape(self.shape, order="F")
+
+    def z_spacings(self):
+        Nz = self.shape[2]
+        H = 0 if self.flat else (4 if self.grid.bottom_height else 3)
+        n = Nz + 2 * H + 1
+        dzc = np.zeros(n)
+        dzf = np.zeros(n)
+        lib().orc_z_spacings(self.h, _dptr(dzc), _dptr(dzf), n)
+        return dzc, dzf
+
+    def last_cg_iterations(self):
+        return lib().orc_last_cg_iterations(self.h)
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def max_threads():
+    return lib().orc_max_threads()
+
+
+def weno5(stencil, left=True):
+    s = np.ascontiguousarray(np.asarray(stencil, dtype=np.float64))
+    return lib().orc_weno5(_dptr(s), int(bool(left)))

@@ -1,0 +1,94 @@
+// gbo_common.cuh -- shared device-side definitions for the GB300 NonhydrostaticModel kernels.
+//
+// Data layout in HBM: every field stores interior points only, x fastest,
+// index i + Nx*(j + Ny*k) with 0-based (i, j, k).  Halo points are never
+// stored: the kernels synthesise them at load time with the semantics of the
+// reference's halo fills (src/BoundaryConditions/fill_halo_regions*.jl):
+//   * x and y are Periodic: indices wrap;
+//   * Center-in-z fields on Bounded z (u, v, tracers, νₑ, κₑ, pHY′, p) carry a
+//     no-flux halo of ONE mirrored layer (fill_halo_regions_flux.jl:9-27);
+//     deeper halo layers are never written by the reference and read as zero;
+//   * w (Face in z) stores faces k = 0..Nz-1; the bottom face k = 0 and the
+//     top face k = Nz are impenetrable and always zero
+//     (fill_halo_regions_normal_flow.jl:2-7); faces outside read as zero.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gbo_coeffs.h"
+
+#define GBO_HD __host__ __device__ __forceinline__
+#define GBO_D __device__ __forceinline__
+
+template <typename FT>
+struct Cx {
+    FT re, im;
+};
+template <typename FT> GBO_HD Cx<FT> cx(FT a, FT b) { return Cx<FT>{a, b}; }
+template <typename FT> GBO_HD Cx<FT> operator+(Cx<FT> a, Cx<FT> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename FT> GBO_HD Cx<FT> operator-(Cx<FT> a, Cx<FT> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename FT> GBO_HD Cx<FT> operator*(Cx<FT> a, Cx<FT> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename FT> GBO_HD Cx<FT> operator*(FT s, Cx<FT> a) { return {s * a.re, s * a.im}; }
+template <typename FT> GBO_HD Cx<FT> conj(Cx<FT> a) { return {a.re, -a.im}; }
+
+// Grid description visible to kernels.  Vertical spacings are tables indexed
+// by the reference's 1-based level kr in [1-Hz, Nz+Hz+1] at position kr + zoff.
+template <typename FT>
+struct GridP {
+    int Nx, Ny, Nz;
+    int flatz;        // 1: topology (Periodic, Periodic, Flat)
+    int zoff;
+    FT dx, dy;        // uniform horizontal spacings
+    FT rdx, rdy;      // 1/Δx, 1/Δy evaluated in FT (Δx⁻¹ operators)
+    const FT* dzc;    // Δzᵃᵃᶜ(kr)
+    const FT* dzf;    // Δzᵃᵃᶠ(kr)
+    const FT* rdzc;   // 1/Δzᵃᵃᶜ(kr)
+    const FT* rdzf;   // 1/Δzᵃᵃᶠ(kr)
+    // immersed boundary: per-column index of the first active cell (0 = none immersed)
+    const int* kbot;  // Nx*Ny entries or nullptr
+};
+
+GBO_D int wrapi(int i, int N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
+
+template <typename FT>
+GBO_D FT ldg(const FT* p) { return __ldg(p); }
+
+// Accessor for a Center-in-z field.
+template <typename FT>
+struct CFld {
+    const FT* __restrict__ a;
+    int Nx, Ny, Nz, flatz;
+    GBO_D FT operator()(int i, int j, int k) const {
+        i = wrapi(i, Nx);
+        j = wrapi(j, Ny);
+        if (flatz) return ldg(a + i + (size_t)Nx * j);
+        if (k < -1 || k > Nz) return FT(0);
+        k = k < 0 ? 0 : (k >= Nz ? Nz - 1 : k);
+        return ldg(a + i + (size_t)Nx * (j + (size_t)Ny * k));
+    }
+};
+
+// Accessor for w (Face in z): faces 0..Nz-1 stored, face 0 and Nz are walls.
+template <typename FT>
+struct WFld {
+    const FT* __restrict__ a;
+    int Nx, Ny, Nz;
+    GBO_D FT operator()(int i, int j, int k) const {
+        if (k <= 0 || k >= Nz) return FT(0);
+        i = wrapi(i, Nx);
+        j = wrapi(j, Ny);
+        return ldg(a + i + (size_t)Nx * (j + (size_t)Ny * k));
+    }
+};
+
+template <typename FT>
+GBO_D CFld<FT> cfld(const FT* a, const GridP<FT>& g) { return CFld<FT>{a, g.Nx, g.Ny, g.Nz, g.flatz}; }
+template <typename FT>
+GBO_D WFld<FT> wfld(const FT* a, const GridP<FT>& g) { return WFld<FT>{a, g.Nx, g.Ny, g.Nz}; }
+
+// Device-side error flags (bit mask) read back by the host after a step.
+#define GBO_FLAG_NAN     1u
+#define GBO_FLAG_TIMEOUT 2u

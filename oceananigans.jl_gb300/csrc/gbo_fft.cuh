@@ -1,0 +1,350 @@
+// gbo_fft.cuh -- shared-memory batched FFT engine and the Poisson pass kernels.
+//
+// The reference solves ∇²ϕ = b by eigenfunction expansion
+// (src/Solvers/fft_based_poisson_solver.jl:94-124): DCT-II in Bounded
+// directions (REDFT10 on the CPU, a permuted complex FFT + twiddles on the GPU,
+// discrete_transforms.jl:108-182, index_permutations.jl:18-90), FFTs in Periodic
+// ones, ϕ̂ = -b̂/(λx+λy+λz) with the zero mode set to zero, then the inverse
+// transforms.  That is a C2C transform over a complex copy of the whole field
+// with ~8 separate permute / twiddle / copy launches.  Here the field stays real
+// until the x pass, which produces the Hermitian half spectrum directly:
+//   Z pass   real -> real   DCT-II along z (Makhoul reordering, two columns per complex line)
+//   X pass   real -> complex  R2C along x (half-length complex FFT + split)
+//   Y pass   complex in place: FFT along y, divide by the eigenvalues, inverse FFT
+//   X⁻¹, Z⁻¹ the inverses.
+// All 1-D transforms run in shared memory (Stockham autosort, radix 4/2/3/5),
+// one block per batch of lines with coalesced loads along the contiguous axis.
+// Forward transforms are unnormalised; the whole normalisation is applied once
+// in the Y pass (or in the Thomas kernel for the Fourier-tridiagonal solver).
+#pragma once
+#include "gbo_common.cuh"
+
+#define GBO_MAX_RADICES 16
+
+struct FFTPlan1D {
+    int n;
+    int nrad;
+    int rad[GBO_MAX_RADICES];
+};
+
+// y = DFT over each of L lines of length n held in A (scratch B); returns the buffer
+// holding the result.  sign = -1 forward, +1 inverse (unnormalised).
+// tw[m] = exp(-2πi m / n), m = 0..n-1.
+template <typename FT>
+__device__ Cx<FT>* block_fft(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* __restrict__ tw) {
+    const int n = pl.n;
+    int Ns = 1;
+    for (int s = 0; s < pl.nrad; ++s) {
+        const int R = pl.rad[s];
+        const int nR = n / R;
+        const int twstep = n / (Ns * R);
+        for (int t = threadIdx.x; t < L * nR; t += blockDim.x) {
+            const int line = t / nR;
+            const int jj = t - line * nR;
+            const int kk = jj % Ns;
+            const Cx<FT>* x = A + line * n;
+            Cx<FT>* y = B + line * n;
+            Cx<FT> v[5];
+            for (int r = 0; r < R; ++r) {
+                Cx<FT> a = x[jj + r * nR];
+                if (r > 0 && kk > 0) {
+                    Cx<FT> wv = tw[(kk * r * twstep) % n];
+                    if (sign > 0) wv.im = -wv.im;
+                    a = a * wv;
+                }
+                v[r] = a;
+            }
+            Cx<FT> V[5];
+            if (R == 2) {
+                V[0] = v[0] + v[1];
+                V[1] = v[0] - v[1];
+            } else if (R == 4) {
+                Cx<FT> s02 = v[0] + v[2], d02 = v[0] - v[2], s13 = v[1] + v[3], d13 = v[1] - v[3];
+                // multiply d13 by -i (forward) or +i (inverse)
+                Cx<FT> jd13 = sign < 0 ? cx(d13.im, -d13.re) : cx(-d13.im, d13.re);
+                V[0] = s02 + s13;
+                V[1] = d02 + jd13;
+                V[2] = s02 - s13;
+                V[3] = d02 - jd13;
+            } else {
+                // generic small DFT with roots of unity taken from the table
+                for (int q = 0; q < R; ++q) {
+                    Cx<FT> acc = v[0];
+                    for (int r = 1; r < R; ++r) {
+                        Cx<FT> wv = tw[((q * r) % R) * nR];
+                        if (sign > 0) wv.im = -wv.im;
+                        acc = acc + v[r] * wv;
+                    }
+                    V[q] = acc;
+                }
+            }
+            const int idxD = (jj / Ns) * Ns * R + kk;
+            for (int q = 0; q < R; ++q) y[idxD + q * Ns] = V[q];
+        }
+        __syncthreads();
+        Cx<FT>* tmp = A;
+        A = B;
+        B = tmp;
+        Ns *= R;
+    }
+    return A;
+}
+
+// Makhoul reordering: the element x(k) of a length-N real sequence goes to v[dest(k)]
+// (index_permutations.jl:18-20 restated: even samples first, odd samples reversed).
+GBO_D int makhoul_dest(int k, int N) { return (k & 1) ? N - 1 - (k >> 1) : (k >> 1); }
+
+struct PoissonTables;  // host side
+
+template <typename FT>
+struct PassP {
+    int Nx, Ny, Nz, Nh;        // Nh = Nx/2 + 1
+    FT* rb;                    // real buffer Nx*Ny*Nz
+    Cx<FT>* cb;                // complex buffer Nh*Ny*Nz
+    FFTPlan1D px_half, py, pz; // plans for lengths Nx/2, Ny, Nz
+    const Cx<FT>* tw_xh;       // n = Nx/2
+    const Cx<FT>* tw_x;        // n = Nx (real-FFT split twiddles)
+    const Cx<FT>* tw_y;        // n = Ny
+    const Cx<FT>* tw_z;        // n = Nz
+    const Cx<FT>* tq_z;        // exp(-iπk/(2Nz)), k = 0..Nz-1
+    const FT* lx;              // eigenvalues λx (Nh entries used)
+    const FT* ly;
+    const FT* lz;
+    FT scale;                  // 1/(Nx Ny Nz) or 1/(Nx Ny)
+    int has_z;                 // Bounded z with a DCT pass
+};
+
+// ---------------------------------------------------------------------------
+// Z pass: DCT-II (forward) / its inverse along z, in place on the real buffer.
+// Block: ZT consecutive x columns at one y, all Nz levels.
+// ---------------------------------------------------------------------------
+template <typename FT>
+__global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
+    extern __shared__ unsigned char smem_raw[];
+    const int N = P.Nz;
+    const int L = ZT / 2;
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    Cx<FT>* B = A + L * N;
+    const int j = blockIdx.y;
+    const int i0 = blockIdx.x * ZT;
+    const size_t plane = (size_t)P.Nx * P.Ny;
+    FT* col0 = P.rb + i0 + (size_t)P.Nx * j;
+    if (!inverse) {
+        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+            int c = t % ZT, k = t / ZT;
+            FT x = (i0 + c < P.Nx) ? col0[c + plane * k] : FT(0);
+            Cx<FT>& d = A[(c >> 1) * N + makhoul_dest(k, N)];
+            if (c & 1) d.im = x; else d.re = x;
+        }
+        __syncthreads();
+        Cx<FT>* R = block_fft<FT>(A, B, L, P.pz, -1, P.tw_z);
+        Cx<FT>* O = (R == A) ? B : A;
+        FT* out = reinterpret_cast<FT*>(O);  // ZT x N reals staged for coalesced stores
+        for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
+            int l = t / N, k = t - l * N;
+            Cx<FT> Zk = R[l * N + k], Zn = R[l * N + (k == 0 ? 0 : N - k)];
+            Cx<FT> w = P.tq_z[k];
+            Cx<FT> s = Zk + conj(Zn), d = Zk - conj(Zn);
+            Cx<FT> ws = w * s, wd = w * d;
+            out[(2 * l) + ZT * k] = ws.re;       // X_a[k] = Re(ω^k (Z_k + Z*_{N-k}))
+            out[(2 * l + 1) + ZT * k] = wd.im;   // X_b[k] = Im(ω^k (Z_k - Z*_{N-k}))
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+            int c = t % ZT, k = t / ZT;
+            if (i0 + c < P.Nx) col0[c + plane * k] = out[c + ZT * k];
+        }
+    } else {
+        FT* in = reinterpret_cast<FT*>(B);
+        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+            int c = t % ZT, k = t / ZT;
+            in[c + ZT * k] = (i0 + c < P.Nx) ? col0[c + plane * k] : FT(0);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
+            int l = t / N, k = t - l * N;
+            FT Xa = in[2 * l + ZT * k], Xb = in[2 * l + 1 + ZT * k];
+            FT Xan = k == 0 ? FT(0) : in[2 * l + ZT * (N - k)];
+            FT Xbn = k == 0 ? FT(0) : in[2 * l + 1 + ZT * (N - k)];
+            Cx<FT> w = conj(P.tq_z[k]);
+            // V_a = ω^{-k}(X_a[k] - i X_a[N-k]) / 2 ; V_b likewise ; Z = V_a + i V_b
+            Cx<FT> Va = FT(0.5) * (w * cx(Xa, -Xan));
+            Cx<FT> Vb = FT(0.5) * (w * cx(Xb, -Xbn));
+            A[l * N + k] = cx(Va.re - Vb.im, Va.im + Vb.re);
+        }
+        __syncthreads();
+        Cx<FT>* R = block_fft<FT>(A, B, L, P.pz, +1, P.tw_z);
+        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+            int c = t % ZT, k = t / ZT;
+            Cx<FT> z = R[(c >> 1) * N + makhoul_dest(k, N)];
+            if (i0 + c < P.Nx) col0[c + plane * k] = (c & 1) ? z.im : z.re;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// X pass: real FFT along x through a half-length complex FFT.
+// Forward: rb (Nx reals per line) -> cb (Nh = Nx/2+1 complex per line).
+// Inverse: cb -> rb.  Block: XL lines (consecutive (j, k) pairs).
+// ---------------------------------------------------------------------------
+template <typename FT>
+__global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
+    extern __shared__ unsigned char smem_raw[];
+    const int M = P.Nx / 2, Nh = P.Nh;
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    Cx<FT>* B = A + XL * M;
+    const int nlines = P.Ny * P.Nz;
+    const int line0 = blockIdx.x * XL;
+    const int L = min(XL, nlines - line0);
+    if (!inverse) {
+        const FT* src = P.rb + (size_t)line0 * P.Nx;
+        FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
+        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) As[t] = src[t];
+        __syncthreads();
+        Cx<FT>* R = block_fft<FT>(A, B, L, P.px_half, -1, P.tw_xh);
+        Cx<FT>* dst = P.cb + (size_t)line0 * Nh;
+        for (int t = threadIdx.x; t < L * Nh; t += blockDim.x) {
+            int l = t / Nh, k = t - l * Nh;
+            Cx<FT> Zk = R[l * M + (k == M ? 0 : k)];
+            Cx<FT> Zn = R[l * M + (k == 0 ? 0 : M - k)];
+            Cx<FT> e = FT(0.5) * (Zk + conj(Zn));
+            Cx<FT> d = FT(0.5) * (Zk - conj(Zn));
+            Cx<FT> o = cx(d.im, -d.re);  // (Z_k - Z*_{M-k}) / (2i)
+            Cx<FT> w = P.tw_x[k == M ? 0 : k];
+            if (k == M) w = cx(FT(-1), FT(0));
+            dst[t] = e + w * o;
+        }
+    } else {
+        const Cx<FT>* src = P.cb + (size_t)line0 * Nh;
+        for (int t = threadIdx.x; t < L * M; t += blockDim.x) {
+            int l = t / M, k = t - l * M;
+            Cx<FT> Xk = src[l * Nh + k], Xn = src[l * Nh + (M - k)];
+            Cx<FT> e = Xk + conj(Xn);
+            Cx<FT> w = conj(P.tw_x[k]);
+            Cx<FT> o = w * (Xk - conj(Xn));
+            A[l * M + k] = cx(e.re - o.im, e.im + o.re);  // e + i o
+        }
+        __syncthreads();
+        Cx<FT>* R = block_fft<FT>(A, B, L, P.px_half, +1, P.tw_xh);
+        FT* dst = P.rb + (size_t)line0 * P.Nx;
+        const FT* Rs = reinterpret_cast<const FT*>(R);
+        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) dst[t] = Rs[t];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Y pass for the FFT solver: FFT along y, ϕ̂ = -b̂ / (λx + λy + λz) (zero mode 0),
+// inverse FFT along y.  Block: YT consecutive kx at one kz, all Ny.
+// mode: 0 = forward+divide+inverse, 1 = forward only, 2 = inverse only.
+// ---------------------------------------------------------------------------
+template <typename FT>
+__global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
+    extern __shared__ unsigned char smem_raw[];
+    const int N = P.Ny, Nh = P.Nh;
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    Cx<FT>* B = A + YT * N;
+    const int kz = blockIdx.y;
+    const int kx0 = blockIdx.x * YT;
+    Cx<FT>* base = P.cb + kx0 + (size_t)Nh * N * kz;
+    for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
+        int c = t % YT, ky = t / YT;
+        A[c * N + ky] = (kx0 + c < Nh) ? base[c + (size_t)Nh * ky] : cx(FT(0), FT(0));
+    }
+    __syncthreads();
+    Cx<FT>* R = A;
+    if (mode != 2) R = block_fft<FT>(A, B, YT, P.py, -1, P.tw_y);
+    if (mode == 0) {
+        for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
+            int c = t / N, ky = t - c * N;
+            int kx = kx0 + c;
+            if (kx < Nh) {
+                FT lam = (P.lx[kx] + P.ly[ky]) + (P.has_z ? P.lz[kz] : FT(0));
+                Cx<FT> b = R[t];
+                Cx<FT> phi = (kx == 0 && ky == 0 && kz == 0) ? cx(FT(0), FT(0))
+                                                             : cx(-b.re / lam, -b.im / lam);
+                R[t] = P.scale * phi;
+            }
+        }
+        __syncthreads();
+    }
+    if (mode != 1) {
+        Cx<FT>* O = (R == A) ? B : A;
+        R = block_fft<FT>(R, O, YT, P.py, +1, P.tw_y);
+    }
+    for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
+        int c = t % YT, ky = t / YT;
+        if (kx0 + c < Nh) base[c + (size_t)Nh * ky] = R[c * N + ky];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched Thomas sweep along z in FP64 for the Fourier-tridiagonal solver
+// (fourier_tridiagonal_poisson_solver.jl:199-229; batched_tridiagonal_solver.jl:217-243):
+//   D_k ϕ_k + ϕ_{k-1}/Δzᶠ_k + ϕ_{k+1}/Δzᶠ_{k+1} = Δzᶜ_k b̂_k,
+//   D_1 = -1/Δzᶠ_2 - Δzᶜ_1 (λx+λy), D_N = -1/Δzᶠ_N - Δzᶜ_N (λx+λy),
+//   D_k = -(1/Δzᶠ_{k+1} + 1/Δzᶠ_k) - Δzᶜ_k (λx+λy).
+// The forward update is elided where |β| ≤ 10 eps (the singular (0,0) mode);
+// the (0,0) column then has its vertical mean removed, which is the reference's
+// `ϕ .- mean(ϕ)` applied in spectral space.  One thread per (kx, ky) column.
+// ---------------------------------------------------------------------------
+struct ThomasP {
+    int Nh, Ny, Nz;
+    const double* rdzf;   // 1/Δzᶠ(kr), indexed kr + zoff
+    const double* dzc;    // Δzᶜ(kr)
+    int zoff;
+    const double* lx;     // λx, λy in FP64
+    const double* ly;
+    double scale;         // 1/(Nx Ny)
+};
+
+template <typename FT>
+__global__ void k_thomas_z(PassP<FT> P, ThomasP T, int TC) {
+    extern __shared__ unsigned char smem_raw[];
+    double* pre = reinterpret_cast<double*>(smem_raw);  // [Nz][TC]
+    double* pim = pre + (size_t)T.Nz * TC;
+    double* tt = pim + (size_t)T.Nz * TC;
+    const int c = threadIdx.x;
+    const int kx = blockIdx.x * TC + c;
+    const int ky = blockIdx.y;
+    if (kx >= T.Nh) return;
+    const size_t stride = (size_t)T.Nh * T.Ny;
+    Cx<FT>* col = P.cb + kx + (size_t)T.Nh * ky;
+    const double lam = T.lx[kx] + T.ly[ky];
+    const int Nz = T.Nz;
+    auto D = [&](int kr) {
+        if (kr == 1) return -T.rdzf[2 + T.zoff] - T.dzc[1 + T.zoff] * lam;
+        if (kr == Nz) return -T.rdzf[Nz + T.zoff] - T.dzc[Nz + T.zoff] * lam;
+        return -(T.rdzf[kr + 1 + T.zoff] + T.rdzf[kr + T.zoff]) - T.dzc[kr + T.zoff] * lam;
+    };
+    auto off = [&](int q) { return T.rdzf[q + 1 + T.zoff]; };
+    const double tiny = 10 * 2.220446049250313e-16;
+    double beta = D(1);
+    Cx<FT> f1 = col[0];
+    pre[c] = (double)f1.re / beta;
+    pim[c] = (double)f1.im / beta;
+    for (int kr = 2; kr <= Nz; ++kr) {
+        double a = off(kr - 1);
+        double t = a / beta;
+        tt[(kr - 1) * TC + c] = t;
+        beta = D(kr) - a * t;
+        Cx<FT> fk = col[stride * (kr - 1)];
+        double sre = ((double)fk.re - a * pre[(kr - 2) * TC + c]) / beta;
+        double sim = ((double)fk.im - a * pim[(kr - 2) * TC + c]) / beta;
+        bool dd = fabs(beta) > tiny;
+        pre[(kr - 1) * TC + c] = dd ? sre : 0.0;
+        pim[(kr - 1) * TC + c] = dd ? sim : 0.0;
+    }
+    for (int kr = Nz - 1; kr >= 1; --kr) {
+        double t = tt[kr * TC + c];
+        pre[(kr - 1) * TC + c] -= t * pre[kr * TC + c];
+        pim[(kr - 1) * TC + c] -= t * pim[kr * TC + c];
+    }
+    double mre = 0, mim = 0;
+    if (kx == 0 && ky == 0) {
+        for (int k = 0; k < Nz; ++k) { mre += pre[k * TC + c]; mim += pim[k * TC + c]; }
+        mre /= Nz;
+        mim /= Nz;
+    }
+    for (int k = 0; k < Nz; ++k)
+        col[stride * k] = cx((FT)((pre[k * TC + c] - mre) * T.scale), (FT)((pim[k * TC + c] - mim) * T.scale));
+}

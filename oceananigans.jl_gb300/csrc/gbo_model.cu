@@ -1,0 +1,822 @@
+// gbo_model.cu -- model lifecycle, RK3 orchestration and the C ABI of libgb300ocean.so.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbo.h"
+#include "gbo_fft.cuh"
+#include "gbo_step.cuh"
+
+// ===========================================================================
+// Pressure source and projection kernels
+// ===========================================================================
+enum { SRC_FFT = 0, SRC_FT = 1, SRC_CG = 2 };
+
+// rhs = divᶜᶜᶜ(u*) (solve_for_pressure.jl:12-50): × Δzᶜ for the Fourier-tridiagonal
+// solver, × Vᶜᶜᶜ for CG.
+template <typename FT>
+__global__ void k_source(GridP<FT> g, const FT* __restrict__ u, const FT* __restrict__ v, const FT* __restrict__ w,
+                         FT* __restrict__ rhs, int mode) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= g.Nx || j >= g.Ny) return;
+    CFld<FT> U = cfld(u, g), V = cfld(v, g);
+    WFld<FT> W = wfld(w, g);
+    Met<FT> M(g);
+    FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
+    FT div = M.rVc(k) * ((Ax * U(i + 1, j, k) - Ax * U(i, j, k)) + (Ay * V(i, j + 1, k) - Ay * V(i, j, k)) +
+                         (g.flatz ? FT(0) : (Az * W(i, j, k + 1) - Az * W(i, j, k))));
+    bool active = true;
+    if (g.kbot) active = k >= g.kbot[i + (size_t)g.Nx * j];
+    FT r = active ? div : FT(0);
+    if (mode == SRC_FT) r = (active ? M.dzc(k) : FT(0)) * div;
+    if (mode == SRC_CG) r = r * (Az * M.dzc(k));
+    rhs[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = r;
+}
+
+// u = u* - ∂x(pΔτ), ... (pressure_correction.jl:67-73), p = pΔτ / max(eps, Δτ)
+// (:102-104), and the tracer predictor copied to the state.  In place is allowed
+// (every point reads only its own u*).
+template <typename FT>
+__global__ void k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws, const FT* __restrict__ phi,
+                          FT* u, FT* v, FT* w, FT* __restrict__ p, FT rdtau, FT phi_shift) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= g.Nx || j >= g.Ny) return;
+    CFld<FT> P = cfld(phi, g);
+    Met<FT> M(g);
+    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+    FT pc = P(i, j, k) - phi_shift;
+    u[idx] = us[idx] - (pc - (P(i - 1, j, k) - phi_shift)) * g.rdx;
+    v[idx] = vs[idx] - (pc - (P(i, j - 1, k) - phi_shift)) * g.rdy;
+    if (!g.flatz) w[idx] = ws[idx] - (pc - (P(i, j, k - 1) - phi_shift)) * M.rdzf(k);
+    p[idx] = pc * rdtau;
+}
+
+template <typename FT>
+__global__ void k_scale_dzc(GridP<FT> g, FT* __restrict__ a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= g.Nx || j >= g.Ny) return;
+    a[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] *= Met<FT>(g).dzc(k);
+}
+
+template <typename FT>
+__global__ void k_copy(const FT* __restrict__ a, FT* __restrict__ b, size_t n) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; t < n; t += stride) b[t] = a[t];
+}
+
+template <typename FT>
+__global__ void k_nan_check(const FT* __restrict__ a, size_t n, unsigned int* flags) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (; t < n; t += stride) bad |= !isfinite(a[t]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flags, GBO_FLAG_NAN);
+}
+
+// ===========================================================================
+// Host helpers
+// ===========================================================================
+namespace {
+
+thread_local std::string g_last_error = "";
+
+struct CudaError {
+    cudaError_t e;
+    const char* what;
+};
+
+#define GBO_CUDA(call)                                                  \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) throw CudaError{e_, #call};              \
+    } while (0)
+
+struct InvalidArg {
+    std::string msg;
+};
+
+// FFT radix plan: radix-4 stages, then 2, 3, 5.  Returns false if n has other factors.
+bool make_plan(int n, FFTPlan1D& p) {
+    p.n = n;
+    p.nrad = 0;
+    int m = n;
+    while (m % 4 == 0 && p.nrad < GBO_MAX_RADICES) { p.rad[p.nrad++] = 4; m /= 4; }
+    for (int r : {2, 3, 5})
+        while (m % r == 0 && p.nrad < GBO_MAX_RADICES) { p.rad[p.nrad++] = r; m /= r; }
+    return m == 1 && n >= 1;
+}
+
+// Vertical grid following generate_coordinate (src/Grids/grid_generation.jl:34-176),
+// evaluated in the working precision FT.  Tables cover kr in [1-H, Nz+H+1].
+template <typename FT>
+struct ZGrid {
+    int Nz = 1, H = 3, zoff = 0;
+    FT Lz = 1;
+    std::vector<FT> dzc, dzf, zc, zf;
+    bool flat = false;
+    FT at(const std::vector<FT>& a, int kr) const { return a[kr + zoff]; }
+};
+
+template <typename FT>
+ZGrid<FT> make_zgrid(int Nz, int H, bool flat, const double* faces, double z0, double z1) {
+    ZGrid<FT> Z;
+    Z.Nz = Nz;
+    Z.H = H;
+    Z.flat = flat;
+    const int kmin = 1 - H, kmax = Nz + H + 1;
+    Z.zoff = -kmin;
+    const int len = kmax - kmin + 1;
+    Z.dzc.assign(len, FT(1));
+    Z.dzf.assign(len, FT(1));
+    Z.zc.assign(len, FT(0));
+    Z.zf.assign(len, FT(0));
+    if (flat) return Z;
+    if (!faces) {
+        // regular: Δ = FT(L/N), faces F₋ + (k-1)Δ (grid_generation.jl:124-156)
+        double L = z1 - z0;
+        FT d = FT(L / Nz);
+        Z.Lz = FT(L);
+        for (int k = kmin; k <= kmax; ++k) {
+            Z.dzc[k + Z.zoff] = d;
+            Z.dzf[k + Z.zoff] = d;
+            Z.zf[k + Z.zoff] = FT(z0 + (k - 1) * (L / Nz));
+            Z.zc[k + Z.zoff] = FT(z0 + (k - 0.5) * (L / Nz));
+        }
+        return Z;
+    }
+    std::vector<FT> Fi(Nz + 1);
+    for (int i = 0; i <= Nz; ++i) Fi[i] = FT(faces[i]);
+    Z.Lz = Fi[Nz] - Fi[0];
+    std::vector<FT> dlow(H), dup(H);
+    for (int i = 1; i <= H; ++i) dlow[i - 1] = Fi[Nz + 1 - H + i - 1] - Fi[Nz + 1 - H + i - 2];
+    for (int i = 1; i <= H; ++i) dup[i - 1] = Fi[i] - Fi[i - 1];
+    std::vector<FT> dplus(dup.rbegin(), dup.rend());
+    std::vector<FT> F;
+    for (int i = 1; i <= H; ++i) {
+        FT s = 0;
+        for (int q = i; q <= H; ++q) s += dlow[q - 1];
+        F.push_back(Fi[0] - s);
+    }
+    for (FT f : Fi) F.push_back(f);
+    std::vector<FT> Fp;
+    for (int i = 1; i <= H; ++i) {
+        FT s = 0;
+        for (int q = i; q <= H; ++q) s += dplus[q - 1];
+        Fp.push_back(Fi[Nz] + s);
+    }
+    std::reverse(Fp.begin(), Fp.end());
+    for (FT f : Fp) F.push_back(f);
+    const int TC = Nz + 2 * H, TF = Nz + 1 + 2 * H;
+    std::vector<FT> C(TC), Df, Dc(TF - 1);
+    for (int i = 0; i < TC; ++i) C[i] = (F[i + 1] + F[i]) / FT(2);
+    for (int i = 1; i < TC; ++i) Df.push_back(C[i] - C[i - 1]);
+    for (int i = 0; i < TF - 1; ++i) Dc[i] = F[i + 1] - F[i];
+    std::vector<FT> Dff;
+    Dff.push_back(Df.front());
+    for (FT d : Df) Dff.push_back(d);
+    Dff.push_back(Df.back());
+    for (int i = (int)Dff.size() - 1; i >= 1; --i) Dff[i] = Dff[i - 1];
+    for (int k = kmin; k <= kmax; ++k) {
+        int pc = k + H - 1, pf = k + H;
+        if (pc >= 0 && pc < (int)Dc.size()) Z.dzc[k + Z.zoff] = Dc[pc];
+        if (pf >= 0 && pf < (int)Dff.size()) Z.dzf[k + Z.zoff] = Dff[pf];
+        if (pc >= 0 && pc < TF) Z.zf[k + Z.zoff] = F[pc];
+        if (pc >= 0 && pc < TC) Z.zc[k + Z.zoff] = C[pc];
+    }
+    return Z;
+}
+
+template <typename FT>
+std::vector<Cx<FT>> twiddles(int n, double frac = 1.0) {
+    // exp(-2πi m frac / n), m = 0..n-1, evaluated in double on the host
+    std::vector<Cx<FT>> t(n);
+    for (int m = 0; m < n; ++m) {
+        double a = -2.0 * M_PI * frac * (double)m / (double)n;
+        t[m] = Cx<FT>{FT(std::cos(a)), FT(std::sin(a))};
+    }
+    return t;
+}
+
+// Poisson eigenvalues (src/Solvers/poisson_eigenvalues.jl:8-23), computed in FP64
+double eig_periodic(int i1, int N, double L) { double s = 2 * std::sin((i1 - 1) * M_PI / N) / (L / N); return s * s; }
+double eig_bounded(int i1, int N, double L) { double s = 2 * std::sin((i1 - 1) * M_PI / (2 * N)) / (L / N); return s * s; }
+
+}  // namespace
+
+// ===========================================================================
+// Model
+// ===========================================================================
+struct gbo_model {
+    virtual ~gbo_model() {}
+    std::string err;
+    int dtype = GBO_FLOAT64;
+    gbo_grid_desc grid{};
+    gbo_model_desc desc{};
+    int Nx = 0, Ny = 0, Nz = 0;
+    bool flat = false;
+    double time = 0;
+    int64_t iteration = 0;
+    int last_iters = 0;
+    int device = 0;
+    virtual int set_field(int field, const void* host, int dtype, int64_t count) = 0;
+    virtual int get_field(int field, void* host, int dtype, int64_t count) = 0;
+    virtual int set_finalize(int enforce) = 0;
+    virtual int step(double dt, int nsteps) = 0;
+    virtual int sync() = 0;
+    virtual int device_pointer(int field, void** p, int64_t* n) = 0;
+    virtual int poisson_device(void* phi, const void* rhs) = 0;
+    int64_t count(int field) const {
+        int64_t plane = (int64_t)Nx * Ny;
+        if (field == GBO_FIELD_W) return flat ? plane : plane * (Nz + 1);
+        return plane * Nz;
+    }
+};
+
+namespace {
+
+template <typename FT>
+struct DBuf {
+    FT* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        n = count;
+        GBO_CUDA(cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(FT)));
+        GBO_CUDA(cudaMemset(p, 0, std::max<size_t>(1, count) * sizeof(FT)));
+    }
+    void free_() {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+    template <typename T>
+    void upload(const std::vector<T>& h) {
+        alloc(h.size());
+        GBO_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+};
+
+template <typename FT>
+struct ModelImpl : gbo_model {
+    using C = Cx<FT>;
+    cudaStream_t stream = nullptr;
+    int ntr = 0;
+    bool has_phy = false;
+    size_t N = 0;  // Nx*Ny*Nz
+    // state and work arrays
+    DBuf<FT> u, v, w, us, vs, ws, Gu, Gv, Gw, nu, phy, p;
+    std::vector<DBuf<FT>> c, cs, Gc, kap;
+    // grid tables
+    DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf;
+    DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64;
+    DBuf<int> t_kbot;
+    ZGrid<FT> Z;
+    GridP<FT> gp{};
+    // Poisson solver
+    DBuf<FT> rb, lx, ly, lz;
+    DBuf<C> cb, tw_xh, tw_x, tw_y, tw_z, tq_z;
+    PassP<FT> pp{};
+    ThomasP tp{};
+    int ZT = 32, XL = 8, YT = 16, TC = 16;
+    size_t smem_z = 0, smem_x = 0, smem_y = 0, smem_t = 0;
+    // flags
+    unsigned int* d_flags = nullptr;
+    unsigned int* h_flags = nullptr;
+    // graph of one time step (per dt)
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = -1;
+    bool use_graph = true;
+
+    ~ModelImpl() override {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz})
+            b->free_();
+        for (auto* vec : {&c, &cs, &Gc, &kap})
+            for (auto& b : *vec) b.free_();
+        t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_kbot.free_();
+        for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
+        if (d_flags) cudaFree(d_flags);
+        if (h_flags) cudaFreeHost(h_flags);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void init(const gbo_grid_desc* gd, const gbo_model_desc* md) {
+        grid = *gd;
+        grid.z_faces = nullptr;
+        grid.bottom_height = nullptr;
+        desc = *md;
+        dtype = sizeof(FT) == 4 ? GBO_FLOAT32 : GBO_FLOAT64;
+        Nx = gd->size[0];
+        Ny = gd->size[1];
+        flat = gd->topology[2] == GBO_FLAT;
+        Nz = flat ? 1 : gd->size[2];
+        ntr = md->ntracers;
+        has_phy = !flat && md->buoyancy_tracer && ntr > 0;
+        N = (size_t)Nx * Ny * Nz;
+        GBO_CUDA(cudaGetDevice(&device));
+        GBO_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        // grid tables
+        const int H = gd->bottom_height ? 4 : 3;
+        Z = make_zgrid<FT>(Nz, H, flat, gd->z_faces, gd->z[0], gd->z[1]);
+        std::vector<FT> rdzc(Z.dzc.size()), rdzf(Z.dzf.size());
+        std::vector<double> rdzf64(Z.dzf.size()), dzc64(Z.dzc.size());
+        for (size_t q = 0; q < Z.dzc.size(); ++q) {
+            rdzc[q] = FT(1) / Z.dzc[q];
+            rdzf[q] = FT(1) / Z.dzf[q];
+            rdzf64[q] = 1.0 / (double)Z.dzf[q];
+            dzc64[q] = (double)Z.dzc[q];
+        }
+        t_dzc.upload(Z.dzc); t_dzf.upload(Z.dzf); t_rdzc.upload(rdzc); t_rdzf.upload(rdzf);
+        t_rdzf64.upload(rdzf64); t_dzc64.upload(dzc64);
+        double Lx = gd->x[1] - gd->x[0], Ly = gd->y[1] - gd->y[0];
+        gp.Nx = Nx; gp.Ny = Ny; gp.Nz = Nz; gp.flatz = flat; gp.zoff = Z.zoff;
+        gp.dx = FT(Lx / Nx); gp.dy = FT(Ly / Ny);
+        gp.rdx = FT(1) / gp.dx; gp.rdy = FT(1) / gp.dy;
+        gp.dzc = t_dzc.p; gp.dzf = t_dzf.p; gp.rdzc = t_rdzc.p; gp.rdzf = t_rdzf.p;
+        gp.kbot = nullptr;
+        if (gd->bottom_height) {
+            // GridFittedBottom: a cell is immersed iff its centre lies at or below the bottom
+            // (grid_fitted_bottom.jl:118-158); kbot = index of the first active level.
+            std::vector<int> kb((size_t)Nx * Ny);
+            for (size_t q = 0; q < kb.size(); ++q) {
+                double h = gd->bottom_height[q];
+                int first = 0;
+                for (int k = 0; k < Nz; ++k)
+                    if ((double)Z.at(Z.zc, k + 1) <= h) first = k + 1;
+                kb[q] = first;
+            }
+            t_kbot.upload(kb);
+            gp.kbot = t_kbot.p;
+        }
+        // fields
+        for (DBuf<FT>* b : {&u, &v, &us, &vs, &Gu, &Gv, &p, &rb}) b->alloc(N);
+        if (!flat) { w.alloc(N); ws.alloc(N); Gw.alloc(N); }
+        if (md->closure != GBO_CLOSURE_NONE) nu.alloc(N);
+        if (has_phy) phy.alloc(N);
+        c.resize(ntr); cs.resize(ntr); Gc.resize(ntr);
+        for (int n = 0; n < ntr; ++n) { c[n].alloc(N); cs[n].alloc(N); Gc[n].alloc(N); }
+        if (md->closure == GBO_CLOSURE_AMD) {
+            kap.resize(ntr);
+            for (int n = 0; n < ntr; ++n) kap[n].alloc(N);
+        }
+        GBO_CUDA(cudaMalloc(&d_flags, sizeof(unsigned int)));
+        GBO_CUDA(cudaMemset(d_flags, 0, sizeof(unsigned int)));
+        GBO_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned int)));
+        init_poisson(Lx, Ly);
+    }
+
+    void init_poisson(double Lx, double Ly) {
+        const int Nh = Nx / 2 + 1;
+        pp.Nx = Nx; pp.Ny = Ny; pp.Nz = Nz; pp.Nh = Nh;
+        if (!make_plan(Nx / 2, pp.px_half) || !make_plan(Ny, pp.py) || !make_plan(Nz, pp.pz))
+            throw InvalidArg{"grid sizes must factor into 2, 3 and 5 for the spectral Poisson solvers"};
+        cb.alloc((size_t)Nh * Ny * Nz);
+        pp.rb = rb.p;
+        pp.cb = cb.p;
+        tw_xh.upload(twiddles<FT>(Nx / 2));
+        tw_x.upload(twiddles<FT>(Nx));
+        tw_y.upload(twiddles<FT>(Ny));
+        tw_z.upload(twiddles<FT>(Nz));
+        tq_z.upload(twiddles<FT>(Nz, 0.25));  // exp(-iπk/(2Nz))
+        pp.tw_xh = tw_xh.p; pp.tw_x = tw_x.p; pp.tw_y = tw_y.p; pp.tw_z = tw_z.p; pp.tq_z = tq_z.p;
+        const double Lxf = (double)FT(Lx), Lyf = (double)FT(Ly), Lzf = (double)Z.Lz;
+        std::vector<FT> hx(Nh), hy(Ny), hz(Nz);
+        std::vector<double> hx64(Nh), hy64(Ny);
+        for (int q = 0; q < Nh; ++q) { hx64[q] = eig_periodic(q + 1, Nx, Lxf); hx[q] = FT(hx64[q]); }
+        for (int q = 0; q < Ny; ++q) { hy64[q] = eig_periodic(q + 1, Ny, Lyf); hy[q] = FT(hy64[q]); }
+        for (int q = 0; q < Nz; ++q) hz[q] = flat ? FT(0) : FT(eig_bounded(q + 1, Nz, Lzf));
+        lx.upload(hx); ly.upload(hy); lz.upload(hz);
+        t_lx64.upload(hx64); t_ly64.upload(hy64);
+        pp.lx = lx.p; pp.ly = ly.p; pp.lz = lz.p;
+        pp.has_z = !flat;
+        pp.scale = flat ? FT(1.0 / ((double)Nx * Ny)) : FT(1.0 / ((double)Nx * Ny * Nz));
+        tp.Nh = Nh; tp.Ny = Ny; tp.Nz = Nz;
+        tp.rdzf = t_rdzf64.p; tp.dzc = t_dzc64.p; tp.zoff = Z.zoff;
+        tp.lx = t_lx64.p; tp.ly = t_ly64.p;
+        tp.scale = 1.0 / ((double)Nx * Ny);
+        // shared-memory tiles: keep each block at or below ~100 KB
+        const size_t cs_ = sizeof(C), lim = 100 * 1024;
+        ZT = 32;
+        while (ZT > 2 && (size_t)ZT * Nz * cs_ > lim) ZT /= 2;
+        smem_z = (size_t)ZT * Nz * cs_;
+        XL = 8;
+        while (XL > 1 && (size_t)2 * XL * (Nx / 2) * cs_ > lim) XL /= 2;
+        smem_x = (size_t)2 * XL * (Nx / 2) * cs_;
+        YT = 16;
+        while (YT > 1 && (size_t)2 * YT * Ny * cs_ > lim) YT /= 2;
+        smem_y = (size_t)2 * YT * Ny * cs_;
+        TC = 32;
+        while (TC > 1 && (size_t)3 * Nz * TC * sizeof(double) > lim) TC /= 2;
+        smem_t = (size_t)3 * Nz * TC * sizeof(double);
+        GBO_CUDA(cudaFuncSetAttribute(k_dct_z<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_z, 1)));
+        GBO_CUDA(cudaFuncSetAttribute(k_rfft_x<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_x, 1)));
+        GBO_CUDA(cudaFuncSetAttribute(k_fft_y<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_y, 1)));
+        GBO_CUDA(cudaFuncSetAttribute(k_thomas_z<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_t, 1)));
+    }
+
+    // ------------------------------------------------------------------
+    dim3 blk() const { return dim3(32, 8, 1); }
+    dim3 grd() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, Nz); }
+
+    void check_launch() { GBO_CUDA(cudaGetLastError()); }
+
+    StepP<FT> params() {
+        StepP<FT> P{};
+        P.g = gp;
+        P.u = u.p; P.v = v.p; P.w = flat ? nullptr : w.p;
+        P.nu = nu.p; P.phy = phy.p;
+        P.b = (desc.buoyancy_tracer && ntr > 0) ? c[0].p : nullptr;
+        P.uo = us.p; P.vo = vs.p; P.wo = flat ? nullptr : ws.p;
+        P.Gu = Gu.p; P.Gv = Gv.p; P.Gw = flat ? nullptr : Gw.p;
+        P.f = FT(desc.coriolis_f);
+        P.has_cor = desc.has_coriolis;
+        P.has_phy = has_phy;
+        P.closure = desc.closure;
+        P.buoyancy = desc.buoyancy_tracer && ntr > 0;
+        P.Pr = FT(desc.closure_Pr);
+        P.C = FT(desc.closure_C);
+        P.Cb = FT(desc.closure_Cb);
+        return P;
+    }
+
+    // Spectral solve of ∇²ϕ = rb in place (rb holds the source on entry, ϕ on exit).
+    void poisson_solve() {
+        const int Nh = Nx / 2 + 1;
+        if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
+            k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
+            check_launch();
+            k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 1, YT);
+            check_launch();
+            k_thomas_z<FT><<<dim3((Nh + TC - 1) / TC, Ny), TC, smem_t, stream>>>(pp, tp, TC);
+            check_launch();
+            k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 2, YT);
+            check_launch();
+            k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
+            check_launch();
+            return;
+        }
+        if (!flat) {
+            k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 0, ZT);
+            check_launch();
+        }
+        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
+        check_launch();
+        k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 0, YT);
+        check_launch();
+        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
+        check_launch();
+        if (!flat) {
+            k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 1, ZT);
+            check_launch();
+        }
+    }
+
+    // compute_pressure_correction! + make_pressure_correction! on the predictor (us, vs, ws)
+    // writing the state (u, v, w) and p; in == out is allowed.
+    void project(const FT* ui, const FT* vi, const FT* wi, double dtau) {
+        int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
+        k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
+        check_launch();
+        poisson_solve();
+        const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+        FT rdtau = FT(1) / FT(std::max(eps, dtau));
+        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0));
+        check_launch();
+    }
+
+    // One RK3 stage: Gⁿ from the current state, predictor, projection.
+    void stage(double dt, double gamma, double zeta, bool first) {
+        StepP<FT> P = params();
+        P.dt = FT(dt);
+        P.gamma = FT(gamma);
+        P.zeta = FT(zeta);
+        P.first = first;
+        if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
+            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(P, nu.p);
+            check_launch();
+        } else if (desc.closure == GBO_CLOSURE_AMD) {
+            StepP<FT> Q = P;
+            Q.c = ntr > 0 ? c[0].p : nullptr;
+            k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
+            check_launch();
+            for (int n = 1; n < ntr; ++n) {
+                Q.c = c[n].p;
+                // viscosity recomputed identically; only κₑ of tracer n is new
+                k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, kap[n].p);
+                check_launch();
+            }
+        }
+        if (has_phy) {
+            k_hydrostatic<FT><<<dim3((Nx + 31) / 32, (Ny + 7) / 8), blk(), 0, stream>>>(P, phy.p);
+            check_launch();
+        }
+        k_momentum<FT><<<grd(), blk(), 0, stream>>>(P);
+        check_launch();
+        for (int n = 0; n < ntr; ++n) {
+            StepP<FT> Q = P;
+            Q.c = c[n].p;
+            Q.co = cs[n].p;
+            Q.Gc = Gc[n].p;
+            Q.kap = kap.empty() ? nullptr : kap[n].p;
+            Q.flux_top = FT(desc.tracer_flux_top[n]);
+            Q.flux_bot = FT(desc.tracer_flux_bottom[n]);
+            k_tracer<FT><<<grd(), blk(), 0, stream>>>(Q);
+            check_launch();
+        }
+        // Δτ = Δt γ (first stage) or Δt (γ + ζ) with γ, ζ in the working precision
+        // (nonhydrostatic_rk3_substep.jl:34-36; runge_kutta_3.jl:186-187)
+        double dtau = first ? (double)FT(dt * (double)FT(gamma)) : (double)FT(dt * (double)(FT(gamma) + FT(zeta)));
+        project(us.p, vs.p, flat ? nullptr : ws.p, dtau);
+        for (int n = 0; n < ntr; ++n) {
+            k_copy<FT><<<std::min<size_t>((N + 255) / 256, 4096), 256, 0, stream>>>(cs[n].p, c[n].p, N);
+            check_launch();
+        }
+    }
+
+    void full_step(double dt) {
+        using K = GboCoeffs<double>;
+        stage(dt, K::rk3_gamma1, 0.0, true);
+        stage(dt, K::rk3_gamma2, K::rk3_zeta2, false);
+        stage(dt, K::rk3_gamma3, K::rk3_zeta3, false);
+    }
+
+    int step(double dt, int nsteps) override {
+        if (nsteps <= 0) return GBO_OK;
+        if (use_graph) {
+            if (!graph || graph_dt != dt) {
+                if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
+                cudaGraph_t gph;
+                GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                full_step(dt);
+                GBO_CUDA(cudaStreamEndCapture(stream, &gph));
+                GBO_CUDA(cudaGraphInstantiate(&graph, gph, 0));
+                GBO_CUDA(cudaGraphDestroy(gph));
+                graph_dt = dt;
+            }
+            for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
+        } else {
+            for (int s = 0; s < nsteps; ++s) full_step(dt);
+        }
+        for (int s = 0; s < nsteps; ++s) {
+            // clock: tⁿ⁺¹ = tⁿ + Δt computed a priori (runge_kutta_3.jl:122,160-161)
+            time = time + dt;
+            iteration += 1;
+        }
+        k_nan_check<FT><<<std::min<size_t>((N + 255) / 256, 1024), 256, 0, stream>>>(u.p, N, d_flags);
+        check_launch();
+        return sync();
+    }
+
+    int sync() override {
+        GBO_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        if (*h_flags & GBO_FLAG_NAN) {
+            err = "NaN or Inf found in the prognostic state";
+            GBO_CUDA(cudaMemset(d_flags, 0, sizeof(unsigned int)));
+            return GBO_ERR_NAN;
+        }
+        return GBO_OK;
+    }
+
+    FT* field_ptr(int field) {
+        if (field == GBO_FIELD_U) return u.p;
+        if (field == GBO_FIELD_V) return v.p;
+        if (field == GBO_FIELD_W) return flat ? nullptr : w.p;
+        if (field >= GBO_FIELD_TRACER && field < GBO_FIELD_TRACER + ntr) return c[field - GBO_FIELD_TRACER].p;
+        if (field == GBO_FIELD_PNHS) return p.p;
+        if (field == GBO_FIELD_PHY) return has_phy ? phy.p : nullptr;
+        if (field == GBO_FIELD_NU) return nu.p;
+        if (field == GBO_FIELD_KAPPA) return kap.empty() ? nullptr : kap[0].p;
+        return nullptr;
+    }
+
+    // Interior transfer with type conversion; w carries Nz+1 faces at the boundary.
+    int set_field(int field, const void* host, int dt_, int64_t count) override {
+        FT* d = field_ptr(field);
+        if (field == GBO_FIELD_W && flat) { err = "w does not exist on a Flat-z grid"; return GBO_ERR_INVALID; }
+        if (!d) { err = "unknown field id"; return GBO_ERR_INVALID; }
+        if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
+        std::vector<FT> h(N);
+        for (size_t q = 0; q < N; ++q)
+            h[q] = dt_ == GBO_FLOAT32 ? FT(static_cast<const float*>(host)[q]) : FT(static_cast<const double*>(host)[q]);
+        if (field == GBO_FIELD_W)  // impenetrable walls: the bottom face is zero (set! + fill_halo_regions!)
+            for (size_t q = 0; q < (size_t)Nx * Ny; ++q) h[q] = FT(0);
+        GBO_CUDA(cudaMemcpyAsync(d, h.data(), N * sizeof(FT), cudaMemcpyHostToDevice, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        return GBO_OK;
+    }
+
+    int get_field(int field, void* host, int dt_, int64_t count) override {
+        FT* d = field_ptr(field);
+        if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
+        std::vector<FT> h(N, FT(0));
+        if (d) {
+            GBO_CUDA(cudaMemcpyAsync(h.data(), d, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
+        } else if (field != GBO_FIELD_W) {
+            err = "field not present in this model";
+            return GBO_ERR_INVALID;
+        }
+        const size_t total = (size_t)count;
+        for (size_t q = 0; q < total; ++q) {
+            FT x = q < N ? h[q] : FT(0);  // the top w face (index Nz) is the wall
+            if (dt_ == GBO_FLOAT32) static_cast<float*>(host)[q] = (float)x;
+            else static_cast<double*>(host)[q] = (double)x;
+        }
+        return GBO_OK;
+    }
+
+    int set_finalize(int enforce) override {
+        if (enforce) project(u.p, v.p, flat ? nullptr : w.p, 1.0);
+        return sync();
+    }
+
+    int device_pointer(int field, void** ptr, int64_t* n) override {
+        FT* d = field_ptr(field);
+        if (!d) { err = "field not present in this model"; return GBO_ERR_INVALID; }
+        *ptr = d;
+        *n = (int64_t)N;
+        return GBO_OK;
+    }
+
+    int poisson_device(void* phi, const void* rhs) override {
+        GBO_CUDA(cudaMemcpyAsync(rb.p, rhs, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+        if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
+            // set_source_term!: b ← b Δzᶜ (fourier_tridiagonal_poisson_solver.jl:268-290)
+            k_scale_dzc<FT><<<grd(), blk(), 0, stream>>>(gp, rb.p);
+            check_launch();
+        }
+        poisson_solve();
+        GBO_CUDA(cudaMemcpyAsync(phi, rb.p, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+        return sync();
+    }
+};
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+namespace {
+
+template <class F>
+int guarded(gbo_model* m, F&& f) {
+    try {
+        return f();
+    } catch (const CudaError& e) {
+        std::string msg = std::string("CUDA error in ") + e.what + ": " + cudaGetErrorString(e.e);
+        if (m) m->err = msg;
+        g_last_error = msg;
+        return GBO_ERR_CUDA;
+    } catch (const InvalidArg& e) {
+        if (m) m->err = e.msg;
+        g_last_error = e.msg;
+        return GBO_ERR_INVALID;
+    } catch (const std::exception& e) {
+        if (m) m->err = e.what();
+        g_last_error = e.what();
+        return GBO_ERR_INVALID;
+    }
+}
+
+std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
+    if (!g || !d) return "null descriptor";
+    if (g->topology[0] != GBO_PERIODIC || g->topology[1] != GBO_PERIODIC)
+        return "x and y must be Periodic";
+    if (g->topology[2] != GBO_BOUNDED && g->topology[2] != GBO_FLAT) return "z must be Bounded or Flat";
+    if (g->float_type != GBO_FLOAT32 && g->float_type != GBO_FLOAT64) return "float_type must be GBO_FLOAT32 or GBO_FLOAT64";
+    int nz = g->topology[2] == GBO_FLAT ? 1 : g->size[2];
+    if (g->size[0] < 8 || g->size[1] < 8 || nz < 1) return "Nx and Ny must be at least 8";
+    if (g->size[0] % 2) return "Nx must be even";
+    if (g->topology[2] == GBO_BOUNDED && nz < 6) return "Nz must be at least 6 on a Bounded z";
+    if (g->x[1] <= g->x[0] || g->y[1] <= g->y[0]) return "x and y extents must be increasing";
+    if (g->topology[2] == GBO_BOUNDED && !g->z_faces && g->z[1] <= g->z[0]) return "z extent must be increasing";
+    if (g->z_faces)
+        for (int k = 0; k < nz; ++k)
+            if (!(g->z_faces[k + 1] > g->z_faces[k])) return "z_faces must be increasing";
+    if (d->advection != GBO_ADVECTION_WENO5) return "only WENO(order=5) advection is implemented";
+    if (d->closure < 0 || d->closure > 2) return "unknown closure";
+    if (d->ntracers < 0 || d->ntracers > GBO_MAX_TRACERS) return "ntracers out of range";
+    if (d->buoyancy_tracer && d->ntracers < 1) return "BuoyancyTracer requires tracer b (tracer 0)";
+    if (d->pressure_solver == GBO_SOLVER_FFT && g->z_faces) return "FFTBasedPoissonSolver requires a regular grid";
+    if (d->pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL && g->topology[2] != GBO_BOUNDED)
+        return "FourierTridiagonalPoissonSolver requires Bounded z";
+    if (d->pressure_solver < 0 || d->pressure_solver > 1) return "pressure_solver not available";
+    if (g->bottom_height) return "ImmersedBoundaryGrid requires the conjugate-gradient solver";
+    return "";
+}
+
+}  // namespace
+
+extern "C" {
+
+void gbo_model_desc_default(gbo_model_desc* d) {
+    std::memset(d, 0, sizeof(*d));
+    d->advection = GBO_ADVECTION_WENO5;
+    d->closure = GBO_CLOSURE_NONE;
+    d->closure_C = 0.16;
+    d->closure_Cb = 1.0;
+    d->closure_Pr = 1.0;
+    d->pressure_solver = GBO_SOLVER_FFT;
+    d->preconditioner = GBO_PRECOND_FFT;
+}
+
+int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out) {
+    if (!out) { g_last_error = "null output handle"; return GBO_ERR_INVALID; }
+    *out = nullptr;
+    std::string why = validate(grid, desc);
+    if (!why.empty()) { g_last_error = why; return GBO_ERR_INVALID; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        g_last_error = "no CUDA device visible";
+        return GBO_ERR_NO_DEVICE;
+    }
+    gbo_model* m = nullptr;
+    int rc = guarded(nullptr, [&]() {
+        if (grid->float_type == GBO_FLOAT32) {
+            auto* mm = new ModelImpl<float>();
+            m = mm;
+            mm->init(grid, desc);
+        } else {
+            auto* mm = new ModelImpl<double>();
+            m = mm;
+            mm->init(grid, desc);
+        }
+        return GBO_OK;
+    });
+    if (rc != GBO_OK) {
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return GBO_OK;
+}
+
+void gbo_model_destroy(gbo_model* m) { delete m; }
+
+int gbo_set_field(gbo_model* m, int32_t field, const void* host, int32_t dtype, int64_t count) {
+    if (!m || !host) return GBO_ERR_INVALID;
+    if (dtype != GBO_FLOAT32 && dtype != GBO_FLOAT64) { m->err = "dtype must be GBO_FLOAT32 or GBO_FLOAT64"; return GBO_ERR_INVALID; }
+    return guarded(m, [&]() { return m->set_field(field, host, dtype, count); });
+}
+
+int gbo_set_finalize(gbo_model* m, int32_t enforce) {
+    if (!m) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->set_finalize(enforce); });
+}
+
+int gbo_get_field(gbo_model* m, int32_t field, void* host, int32_t dtype, int64_t count) {
+    if (!m || !host) return GBO_ERR_INVALID;
+    if (dtype != GBO_FLOAT32 && dtype != GBO_FLOAT64) { m->err = "dtype must be GBO_FLOAT32 or GBO_FLOAT64"; return GBO_ERR_INVALID; }
+    return guarded(m, [&]() { return m->get_field(field, host, dtype, count); });
+}
+
+int64_t gbo_field_count(const gbo_model* m, int32_t field) { return m ? m->count(field) : -1; }
+
+int gbo_field_device_pointer(gbo_model* m, int32_t field, void** dptr, int64_t* count) {
+    if (!m || !dptr || !count) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->device_pointer(field, dptr, count); });
+}
+
+int gbo_time_step(gbo_model* m, double dt, int32_t nsteps) {
+    if (!m) return GBO_ERR_INVALID;
+    if (!(dt > 0) || !std::isfinite(dt)) { m->err = "dt must be positive and finite"; return GBO_ERR_INVALID; }
+    return guarded(m, [&]() { return m->step(dt, nsteps); });
+}
+
+int gbo_clock(const gbo_model* m, double* time, int64_t* iteration) {
+    if (!m) return GBO_ERR_INVALID;
+    if (time) *time = m->time;
+    if (iteration) *iteration = m->iteration;
+    return GBO_OK;
+}
+
+int gbo_synchronize(gbo_model* m) {
+    if (!m) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->sync(); });
+}
+
+int32_t gbo_last_solver_iterations(const gbo_model* m) { return m ? m->last_iters : 0; }
+
+const char* gbo_last_error(const gbo_model* m) {
+    if (m && !m->err.empty()) return m->err.c_str();
+    return g_last_error.c_str();
+}
+
+const char* gbo_version(void) { return "gb300ocean 0.1.0 (sm_103a)"; }
+
+int gbo_poisson_solve_device(gbo_model* m, void* phi, const void* rhs) {
+    if (!m || !phi || !rhs) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->poisson_device(phi, rhs); });
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// gbo_weno.cuh -- WENO5 / WENO3 / centered reconstructions on device.
+//
+// Z-WENO of order 5 with the buffer hierarchy WENO5 -> WENO3 -> Centered(2)
+// used near Bounded walls, as Oceananigans' WENO() builds it
+// (src/Advection/weno_reconstruction.jl:107-140):
+//   * stencils S_r (left / right biased) ... weno_interpolants.jl:515-562
+//   * smoothness β_r with integer coefficients ... weno_interpolants.jl:169-174,196-213;
+//     in single precision every stencil is shifted by its centre value before
+//     β is formed (weno_interpolants.jl:268-281) to avoid cancellation
+//   * τ = |β₀ - β_{N-1}|, α_r = C★_r (1 + (τ/(β_r + ε))²), ω = α/Σα
+//     (weno_interpolants.jl:296-328), ε the single-precision literal 1e-8
+//   * ψ̂ = Σ ω_r p_r with p_r the order-N reconstruction of stencil r.
+// Reconstruction weights come from gbo_coeffs.h (generated, exact rationals).
+#pragma once
+#include "gbo_common.cuh"
+
+template <typename FT> struct IsF32 { static constexpr bool value = false; };
+template <> struct IsF32<float> { static constexpr bool value = true; };
+
+// Division used in the WENO weights.  FP64 keeps IEEE division (the reference's
+// CPU semantics, the parity target); FP32 uses the fast reciprocal as the
+// reference's GPU backend does (ext/OceananigansCUDAExt.jl:147-171).
+GBO_D double weno_div(double a, double b) { return a / b; }
+GBO_D float weno_div(float a, float b) { return __fdividef(a, b); }
+
+template <typename FT>
+GBO_D FT beta3(FT p0, FT p1, FT p2, int s) {
+    if (IsF32<FT>::value) {
+        FT c = p1;
+        p0 -= c; p1 -= c; p2 -= c;
+        // p1 is exactly zero after the shift
+    }
+    FT b;
+    if (s == 0)
+        b = p0 * (FT(10) * p0 + FT(-31) * p1 + FT(11) * p2) + p1 * (FT(25) * p1 + FT(-19) * p2) + p2 * p2 * FT(4);
+    else if (s == 1)
+        b = p0 * (FT(4) * p0 + FT(-13) * p1 + FT(5) * p2) + p1 * (FT(13) * p1 + FT(-13) * p2) + p2 * p2 * FT(4);
+    else
+        b = p0 * (FT(4) * p0 + FT(-19) * p1 + FT(11) * p2) + p1 * (FT(25) * p1 + FT(-31) * p2) + p2 * p2 * FT(10);
+    return b;
+}
+
+// WENO5 biased reconstruction at a face; S[0..5] = ψ at face offsets -3..+2.
+template <typename FT>
+GBO_D FT weno5(const FT S[6], bool left) {
+    using K = GboCoeffs<FT>;
+    FT a0, a1, a2, b0, b1, b2, c0, c1, c2;  // stencils P0=(a), P1=(b), P2=(c)
+    if (left) {
+        a0 = S[2]; a1 = S[3]; a2 = S[4];
+        b0 = S[1]; b1 = S[2]; b2 = S[3];
+        c0 = S[0]; c1 = S[1]; c2 = S[2];
+    } else {
+        a0 = S[3]; a1 = S[2]; a2 = S[1];
+        b0 = S[4]; b1 = S[3]; b2 = S[2];
+        c0 = S[5]; c1 = S[4]; c2 = S[3];
+    }
+    FT be0 = beta3(a0, a1, a2, 0), be1 = beta3(b0, b1, b2, 1), be2 = beta3(c0, c1, c2, 2);
+    FT tau = fabs(be0 - be2);
+    FT q0 = weno_div(tau, be0 + K::eps), q1 = weno_div(tau, be1 + K::eps), q2 = weno_div(tau, be2 + K::eps);
+    FT al0 = K::weno3_cstar[0] * (FT(1) + q0 * q0);
+    FT al1 = K::weno3_cstar[1] * (FT(1) + q1 * q1);
+    FT al2 = K::weno3_cstar[2] * (FT(1) + q2 * q2);
+    FT inv = weno_div(FT(1), (al0 + al1) + al2);
+    FT p0 = (K::weno3_p0[0] * a0 + K::weno3_p0[1] * a1) + K::weno3_p0[2] * a2;
+    FT p1 = (K::weno3_p1[0] * b0 + K::weno3_p1[1] * b1) + K::weno3_p1[2] * b2;
+    FT p2 = (K::weno3_p2[0] * c0 + K::weno3_p2[1] * c1) + K::weno3_p2[2] * c2;
+    return (al0 * inv) * p0 + (al1 * inv) * p1 + (al2 * inv) * p2;
+}
+
+// WENO3 biased reconstruction at a face; S[0..3] = ψ at face offsets -2..+1.
+template <typename FT>
+GBO_D FT weno3(const FT S[4], bool left) {
+    using K = GboCoeffs<FT>;
+    FT a0, a1, b0, b1;
+    if (left) { a0 = S[1]; a1 = S[2]; b0 = S[0]; b1 = S[1]; }
+    else      { a0 = S[2]; a1 = S[1]; b0 = S[3]; b1 = S[2]; }
+    FT sa0 = a0, sa1 = a1, sb0 = b0, sb1 = b1;
+    if (IsF32<FT>::value) { sa0 -= a1; sa1 = FT(0); sb0 -= b1; sb1 = FT(0); }
+    FT be0 = sa0 * (FT(1) * sa0 + FT(-2) * sa1) + sa1 * sa1 * FT(1);
+    FT be1 = sb0 * (FT(1) * sb0 + FT(-2) * sb1) + sb1 * sb1 * FT(1);
+    FT tau = fabs(be0 - be1);
+    FT q0 = weno_div(tau, be0 + K::eps), q1 = weno_div(tau, be1 + K::eps);
+    FT al0 = K::weno2_cstar[0] * (FT(1) + q0 * q0);
+    FT al1 = K::weno2_cstar[1] * (FT(1) + q1 * q1);
+    FT inv = weno_div(FT(1), al0 + al1);
+    FT p0 = K::weno2_p0[0] * a0 + K::weno2_p0[1] * a1;
+    FT p1 = K::weno2_p1[0] * b0 + K::weno2_p1[1] * b1;
+    return (al0 * inv) * p0 + (al1 * inv) * p1;
+}
+
+template <typename FT>
+GBO_D FT cen4(FT q0, FT q1, FT q2, FT q3) {  // offsets -2, -1, 0, +1
+    using K = GboCoeffs<FT>;
+    return K::c4[0] * q0 + K::c4[1] * q1 + K::c4[2] * q2 + K::c4[3] * q3;
+}
+template <typename FT>
+GBO_D FT cen2(FT qm, FT q0) {  // offsets -1, 0
+    using K = GboCoeffs<FT>;
+    return K::c2[0] * qm + K::c2[1] * q0;
+}
+
+// Buffer-scheme selection in Bounded z (topologically_conditional_interpolation.jl:52-58),
+// kr = 1-based level, N = Nz.  Returns 3 (WENO5 / C4), 2 (WENO3) or 1 (C2).
+GBO_D int zlev_biased_face(int kr, int N) {
+    if (kr >= 4 && kr <= N - 2) return 3;
+    if (kr >= 3 && kr <= N - 1) return 2;
+    return 1;
+}
+GBO_D int zlev_biased_center(int kr, int N) {
+    if (kr >= 3 && kr <= N - 2) return 3;
+    if (kr >= 2 && kr <= N - 1) return 2;
+    return 1;
+}
+GBO_D int zlev_symm_face(int kr, int N) { return (kr >= 4 && kr <= N - 2) ? 3 : 1; }
+GBO_D int zlev_symm_center(int kr, int N) { return (kr >= 3 && kr <= N - 2) ? 3 : 1; }
+
+// Biased reconstruction with level selection; q(o) gives ψ at face offset o.
+template <typename FT, class Q>
+GBO_D FT biased(Q q, bool left, int level) {
+    if (level == 3) {
+        FT S[6];
+#pragma unroll
+        for (int o = -3; o <= 2; ++o) S[o + 3] = q(o);
+        return weno5<FT>(S, left);
+    }
+    if (level == 2) {
+        FT S[4];
+#pragma unroll
+        for (int o = -2; o <= 1; ++o) S[o + 2] = q(o);
+        return weno3<FT>(S, left);
+    }
+    return cen2<FT>(q(-1), q(0));
+}
+template <typename FT, class Q>
+GBO_D FT symm(Q q, int level) {
+    if (level == 3) return cen4<FT>(q(-2), q(-1), q(0), q(1));
+    return cen2<FT>(q(-1), q(0));
+}

@@ -1,0 +1,14 @@
+"""oceananigans_gb300: GB300-native NonhydrostaticModel time stepping behind a C ABI.
+
+The compute path is libgb300ocean.so (hand-written sm_103a CUDA); this package
+is the host-side mirror of the reference's model API.
+"""
+from .api import (  # noqa: F401
+    Periodic, Bounded, Flat,
+    RectilinearGrid, ImmersedBoundaryGrid, GridFittedBottom,
+    WENO, SmagorinskyLilly, AnisotropicMinimumDissipation, BuoyancyTracer, FPlane,
+    FluxBoundaryCondition, FieldBoundaryConditions,
+    FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver,
+    NonhydrostaticModel, Simulation, set_, time_step_, run_,
+)
+from ._lib import GboError, NaNError, NotConvergedError, load  # noqa: F401

@@ -1,0 +1,388 @@
+"""Host-side mirror of the reference's NonhydrostaticModel API over the C ABI.
+
+Names and argument meanings follow Oceananigans.jl:
+  RectilinearGrid(size, x, y, z, topology)        src/Grids/rectilinear_grid.jl:266
+  ImmersedBoundaryGrid(grid, GridFittedBottom(h)) src/ImmersedBoundaries/immersed_boundary_grid.jl:46
+  NonhydrostaticModel(grid; advection, closure, buoyancy, coriolis, tracers,
+                      boundary_conditions, pressure_solver)
+                                                  src/Models/NonhydrostaticModels/nonhydrostatic_model.jl:124
+  set!(model; u=..., b=...)                       set_nonhydrostatic_model.jl:39   -> set_
+  time_step!(model, Δt)                           src/TimeSteppers/runge_kutta_3.jl:103 -> time_step_
+  Simulation(model; Δt, stop_time), run!(sim)     src/Simulations/simulation.jl:12, run.jl:151 -> run_
+A trailing underscore stands for Julia's `!`.  Errors mirror the reference:
+invalid configurations raise ValueError (ArgumentError there).
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib as L
+
+Periodic, Bounded, Flat = "Periodic", "Bounded", "Flat"
+_TOPO = {Periodic: L.GBO_PERIODIC, Bounded: L.GBO_BOUNDED, Flat: L.GBO_FLAT}
+
+
+# ---------------------------------------------------------------------------
+# Grids
+# ---------------------------------------------------------------------------
+class RectilinearGrid:
+    """RectilinearGrid(size, x, y, z, topology, float_type).
+
+    `z` is an extent tuple (regular spacing) or a callable / array of Nz+1
+    increasing face positions (stretched), as in the reference.
+    """
+
+    def __init__(self, size, x=(0.0, 1.0), y=(0.0, 1.0), z=(-1.0, 0.0),
+                 topology=(Periodic, Periodic, Bounded), float_type=np.float64, halo=None):
+        topology = tuple(topology)
+        if topology[0] != Periodic or topology[1] != Periodic:
+            raise ValueError("only Periodic x and y topologies are supported")
+        if topology[2] not in (Bounded, Flat):
+            raise ValueError("z topology must be Bounded or Flat")
+        size = tuple(int(s) for s in size)
+        if topology[2] == Flat and len(size) == 2:
+            size = size + (1,)
+        self.Nx, self.Ny, self.Nz = size
+        self.topology = topology
+        self.x = tuple(float(a) for a in x)
+        self.y = tuple(float(a) for a in y)
+        self.float_type = np.dtype(float_type).type
+        self.z_faces = None
+        if topology[2] == Flat:
+            self.Nz = 1
+            self.z = (0.0, 1.0)
+        elif callable(z):
+            self.z_faces = np.array([z(k) for k in range(1, self.Nz + 2)], dtype=np.float64)
+            self.z = (float(self.z_faces[0]), float(self.z_faces[-1]))
+        elif np.ndim(z) == 1 and len(z) == self.Nz + 1:
+            self.z_faces = np.asarray(z, dtype=np.float64).copy()
+            self.z = (float(self.z_faces[0]), float(self.z_faces[-1]))
+        else:
+            self.z = tuple(float(a) for a in z)
+        if self.z_faces is not None and not np.all(np.diff(self.z_faces) > 0):
+            raise ValueError("The elements of z must be increasing!")
+        self.bottom_height = None
+
+    @property
+    def Lx(self):
+        return self.x[1] - self.x[0]
+
+    @property
+    def Ly(self):
+        return self.y[1] - self.y[0]
+
+    @property
+    def Lz(self):
+        return self.z[1] - self.z[0]
+
+    def size(self):
+        return (self.Nx, self.Ny, self.Nz)
+
+    def nodes(self):
+        """Cell-centre coordinates (xᶜ, yᶜ, zᶜ)."""
+        xc = self.x[0] + (np.arange(self.Nx) + 0.5) * self.Lx / self.Nx
+        yc = self.y[0] + (np.arange(self.Ny) + 0.5) * self.Ly / self.Ny
+        if self.z_faces is not None:
+            zc = 0.5 * (self.z_faces[1:] + self.z_faces[:-1])
+        else:
+            zc = self.z[0] + (np.arange(self.Nz) + 0.5) * self.Lz / self.Nz
+        return xc, yc, zc
+
+    def descriptor(self):
+        d = L.GridDesc()
+        d.size[:] = (self.Nx, self.Ny, self.Nz)
+        d.topology[:] = tuple(_TOPO[t] for t in self.topology)
+        d.x[:] = self.x
+        d.y[:] = self.y
+        d.z[:] = self.z
+        keep = []
+        if self.z_faces is not None:
+            zf = np.ascontiguousarray(self.z_faces, dtype=np.float64)
+            keep.append(zf)
+            d.z_faces = zf.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        if self.bottom_height is not None:
+            h = np.ascontiguousarray(np.asarray(self.bottom_height, dtype=np.float64).ravel(order="F"))
+            keep.append(h)
+            d.bottom_height = h.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.float_type = L.GBO_FLOAT32 if self.float_type == np.float32 else L.GBO_FLOAT64
+        d._keep = keep
+        return d
+
+
+class GridFittedBottom:
+    """GridFittedBottom(h) with h an (Nx, Ny) array or a callable h(x, y)."""
+
+    def __init__(self, bottom_height):
+        self.bottom_height = bottom_height
+
+
+class ImmersedBoundaryGrid(RectilinearGrid):
+    def __init__(self, grid, boundary):
+        self.__dict__.update(grid.__dict__)
+        self.underlying_grid = grid
+        h = boundary.bottom_height
+        if callable(h):
+            xc, yc, _ = grid.nodes()
+            X, Y = np.meshgrid(xc, yc, indexing="ij")
+            h = np.vectorize(h)(X, Y)
+        self.bottom_height = np.asarray(h, dtype=np.float64).reshape(grid.Nx, grid.Ny)
+
+
+# ---------------------------------------------------------------------------
+# Physics options
+# ---------------------------------------------------------------------------
+class WENO:
+    def __init__(self, order=5):
+        if order != 5:
+            raise ValueError("only WENO(order=5) is implemented on GB300")
+        self.order = order
+
+
+class SmagorinskyLilly:
+    def __init__(self, C=0.16, Cb=1.0, Pr=1.0):
+        self.C, self.Cb, self.Pr = float(C), float(Cb), float(Pr)
+
+
+class AnisotropicMinimumDissipation:
+    def __init__(self, C=1.0 / 3.0):
+        self.C = float(C)
+
+
+class BuoyancyTracer:
+    pass
+
+
+class FPlane:
+    def __init__(self, f):
+        self.f = float(f)
+
+
+class FluxBoundaryCondition:
+    def __init__(self, value):
+        self.value = float(value)
+
+
+class FieldBoundaryConditions:
+    def __init__(self, top=None, bottom=None):
+        self.top = top
+        self.bottom = bottom
+
+
+class FFTBasedPoissonSolver:
+    kind = L.GBO_SOLVER_FFT
+
+
+class FourierTridiagonalPoissonSolver:
+    kind = L.GBO_SOLVER_FOURIER_TRIDIAGONAL
+
+
+class ConjugateGradientPoissonSolver:
+    kind = L.GBO_SOLVER_CONJUGATE_GRADIENT
+
+    def __init__(self, reltol=0.0, abstol=0.0, maxiter=0, preconditioner="fft"):
+        self.reltol, self.abstol, self.maxiter = reltol, abstol, maxiter
+        self.preconditioner = {"fft": L.GBO_PRECOND_FFT, None: L.GBO_PRECOND_NONE,
+                               "learned": L.GBO_PRECOND_LEARNED}[preconditioner]
+
+
+def _grid_is_regular(grid):
+    return grid.z_faces is None
+
+
+def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis=None, tracers=(),
+                     boundary_conditions=None, pressure_solver=None, timestepper="RungeKutta3"):
+    """Translate NonhydrostaticModel keyword arguments into the C ABI's gbo_model_desc.
+
+    Follows the reference constructor's choices: default advection WENO(), the
+    pressure solver picked from the grid (nonhydrostatic_pressure_solver,
+    src/Models/NonhydrostaticModels/NonhydrostaticModels.jl:30-76), and
+    ArgumentError-style failures raised as ValueError.
+    """
+    if timestepper != "RungeKutta3":
+        raise ValueError("timestepper = :%s is not supported; use :RungeKutta3" % timestepper)
+    advection = advection if advection is not None else WENO()
+    if not isinstance(advection, WENO):
+        raise ValueError("advection must be WENO(order=5)")
+    if isinstance(tracers, str):
+        tracers = (tracers,)
+    tracers = tuple(tracers)
+    if isinstance(buoyancy, BuoyancyTracer):
+        if "b" not in tracers:
+            raise ValueError("BuoyancyTracer requires a tracer named b")
+        tracers = ("b",) + tuple(t for t in tracers if t != "b")
+    d = L.ModelDesc()
+    L.load().gbo_model_desc_default(ctypes.byref(d))
+    d.advection = L.GBO_ADVECTION_WENO5
+    if isinstance(closure, SmagorinskyLilly):
+        d.closure = L.GBO_CLOSURE_SMAGORINSKY_LILLY
+        d.closure_C, d.closure_Cb, d.closure_Pr = closure.C, closure.Cb, closure.Pr
+    elif isinstance(closure, AnisotropicMinimumDissipation):
+        d.closure = L.GBO_CLOSURE_AMD
+        d.closure_C = closure.C
+    elif closure is not None:
+        raise ValueError("unsupported closure %r" % (closure,))
+    d.ntracers = len(tracers)
+    d.buoyancy_tracer = int(isinstance(buoyancy, BuoyancyTracer))
+    if isinstance(coriolis, FPlane):
+        d.has_coriolis = 1
+        d.coriolis_f = coriolis.f
+    for name, bcs in (boundary_conditions or {}).items():
+        if name not in tracers:
+            raise ValueError("boundary conditions are supported on tracers only (got %s)" % name)
+        n = tracers.index(name)
+        if bcs.top is not None:
+            d.tracer_flux_top[n] = bcs.top.value
+        if bcs.bottom is not None:
+            d.tracer_flux_bottom[n] = bcs.bottom.value
+    if pressure_solver is None:
+        if grid.bottom_height is not None:
+            pressure_solver = ConjugateGradientPoissonSolver()
+        elif _grid_is_regular(grid):
+            pressure_solver = FFTBasedPoissonSolver()
+        else:
+            pressure_solver = FourierTridiagonalPoissonSolver()
+    d.pressure_solver = pressure_solver.kind
+    if isinstance(pressure_solver, ConjugateGradientPoissonSolver):
+        d.preconditioner = pressure_solver.preconditioner
+        d.cg_reltol, d.cg_abstol, d.cg_maxiter = pressure_solver.reltol, pressure_solver.abstol, pressure_solver.maxiter
+    return d, tracers
+
+
+# ---------------------------------------------------------------------------
+# Model
+# ---------------------------------------------------------------------------
+class NonhydrostaticModel:
+    """NonhydrostaticModel(grid; advection, closure, buoyancy, coriolis, tracers,
+    boundary_conditions, pressure_solver) on one GB300.  State lives on the device.
+    """
+
+    def __init__(self, grid, advection=None, closure=None, buoyancy=None, coriolis=None, tracers=(),
+                 boundary_conditions=None, pressure_solver=None, timestepper="RungeKutta3"):
+        d, self.tracers = model_descriptor(grid, advection=advection, closure=closure, buoyancy=buoyancy,
+                                           coriolis=coriolis, tracers=tracers,
+                                           boundary_conditions=boundary_conditions,
+                                           pressure_solver=pressure_solver, timestepper=timestepper)
+        self.grid = grid
+        self.desc = d
+        self._gdesc = grid.descriptor()
+        h = ctypes.c_void_p()
+        lib = L.load()
+        rc = lib.gbo_model_create(ctypes.byref(self._gdesc), ctypes.byref(d), ctypes.byref(h))
+        if rc == L.GBO_ERR_INVALID:
+            raise ValueError(lib.gbo_last_error(None).decode())
+        L.check(rc)
+        self._h = h
+        self.dtype = grid.float_type
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.load().gbo_model_destroy(h)
+            self._h = None
+
+    # -- field access --------------------------------------------------------
+    def _fid(self, name):
+        ids = {"u": L.GBO_FIELD_U, "v": L.GBO_FIELD_V, "w": L.GBO_FIELD_W, "p": L.GBO_FIELD_PNHS,
+               "pNHS": L.GBO_FIELD_PNHS, "pHY": L.GBO_FIELD_PHY, "pHY′": L.GBO_FIELD_PHY,
+               "nu": L.GBO_FIELD_NU, "νₑ": L.GBO_FIELD_NU, "kappa": L.GBO_FIELD_KAPPA}
+        if name in ids:
+            return ids[name]
+        if name in self.tracers:
+            return L.GBO_FIELD_TRACER + self.tracers.index(name)
+        raise ValueError("name %s not found in model.velocities or model.tracers." % name)
+
+    def field_shape(self, name):
+        g = self.grid
+        if name == "w" and g.topology[2] == Bounded:
+            return (g.Nx, g.Ny, g.Nz + 1)
+        return (g.Nx, g.Ny, g.Nz)
+
+    def set_field(self, name, value):
+        shp = self.field_shape(name)
+        if callable(value):
+            value = self._evaluate(name, value)
+        a = np.broadcast_to(np.asarray(value, dtype=np.float64), shp)
+        flat = np.ascontiguousarray(np.asfortranarray(a).ravel(order="F"))
+        L.check(L.load().gbo_set_field(self._h, self._fid(name), flat.ctypes.data, L.GBO_FLOAT64, flat.size), self._h)
+
+    def _evaluate(self, name, fn):
+        g = self.grid
+        xc, yc, zc = g.nodes()
+        xf = g.x[0] + np.arange(g.Nx) * g.Lx / g.Nx
+        yf = g.y[0] + np.arange(g.Ny) * g.Ly / g.Ny
+        xs = xf if name == "u" else xc
+        ys = yf if name == "v" else yc
+        if name == "w" and g.topology[2] == Bounded:
+            zs = g.z_faces if g.z_faces is not None else g.z[0] + np.arange(g.Nz + 1) * g.Lz / g.Nz
+        else:
+            zs = zc
+        X, Y, Zz = np.meshgrid(xs, ys, zs, indexing="ij")
+        return np.vectorize(fn)(X, Y, Zz)
+
+    def get(self, name, dtype=np.float64):
+        shp = self.field_shape(name)
+        out = np.zeros(int(np.prod(shp)), dtype=dtype)
+        code = L.GBO_FLOAT32 if np.dtype(dtype) == np.float32 else L.GBO_FLOAT64
+        L.check(L.load().gbo_get_field(self._h, self._fid(name), out.ctypes.data, code, out.size), self._h)
+        return out.reshape(shp, order="F")
+
+    @property
+    def clock(self):
+        t = ctypes.c_double()
+        it = ctypes.c_int64()
+        L.load().gbo_clock(self._h, ctypes.byref(t), ctypes.byref(it))
+        return t.value, it.value
+
+    def device_pointer(self, name):
+        p = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        L.check(L.load().gbo_field_device_pointer(self._h, self._fid(name), ctypes.byref(p), ctypes.byref(n)), self._h)
+        return p.value, n.value
+
+    def poisson_solve_device(self, phi_ptr, rhs_ptr):
+        L.check(L.load().gbo_poisson_solve_device(self._h, ctypes.c_void_p(phi_ptr), ctypes.c_void_p(rhs_ptr)), self._h)
+
+    @property
+    def solver_iterations(self):
+        return L.load().gbo_last_solver_iterations(self._h)
+
+
+def set_(model, enforce_incompressibility=True, **fields):
+    """set!(model; enforce_incompressibility=true, kwargs...)."""
+    for name, value in fields.items():
+        model.set_field(name, value)
+    L.check(L.load().gbo_set_finalize(model._h, int(bool(enforce_incompressibility))), model._h)
+
+
+def time_step_(model, dt, nsteps=1):
+    """time_step!(model, Δt) (nsteps times; one CUDA-graph launch per step)."""
+    L.check(L.load().gbo_time_step(model._h, float(dt), int(nsteps)), model._h)
+
+
+class Simulation:
+    """Simulation(model; Δt, stop_time, stop_iteration) (src/Simulations/simulation.jl:12)."""
+
+    def __init__(self, model, dt, stop_time=math.inf, stop_iteration=math.inf, callbacks=()):
+        self.model = model
+        self.dt = float(dt)
+        self.stop_time = stop_time
+        self.stop_iteration = stop_iteration
+        self.callbacks = list(callbacks)
+
+
+def run_(sim, chunk=None):
+    """run!(sim): step until stop_time / stop_iteration; callbacks run between chunks."""
+    m = sim.model
+    while True:
+        t, it = m.clock
+        if it >= sim.stop_iteration or t >= sim.stop_time - 1e-12 * max(1.0, abs(sim.stop_time)):
+            break
+        n_time = math.ceil((sim.stop_time - t) / sim.dt - 1e-9) if math.isfinite(sim.stop_time) else 1 << 30
+        n_iter = sim.stop_iteration - it if math.isfinite(sim.stop_iteration) else 1 << 30
+        n = int(min(n_time, n_iter, chunk or (1 << 30)))
+        if n <= 0:
+            break
+        time_step_(m, sim.dt, n)
+        for cb in sim.callbacks:
+            cb(sim)

@@ -1,0 +1,97 @@
+"""The C ABI library loads and exports every entry point declared in include/gbo.h;
+argument validation runs without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oceananigans_gb300 as og
+from oceananigans_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "gbo.h")).read()
+    return sorted(set(re.findall(r"\b(gbo_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_symbols_exported_and_bound():
+    lib = L.load()
+    syms = declared_symbols()
+    assert syms, "no declarations found"
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(L.SIGNATURES) == syms
+
+
+def test_struct_layout_matches_header(tmp_path):
+    # compile a probe against include/gbo.h and compare sizes/offsets with the ctypes mirror
+    src = tmp_path / "probe.c"
+    src.write_text('''#include <stdio.h>
+#include <stddef.h>
+#include "gbo.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(gbo_grid_desc), offsetof(gbo_grid_desc, z_faces),
+         offsetof(gbo_grid_desc, float_type), sizeof(gbo_model_desc), offsetof(gbo_model_desc, pressure_solver),
+         offsetof(gbo_model_desc, cg_maxiter));
+  return 0; }
+''')
+    exe = tmp_path / "probe"
+    import subprocess
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
+    want = [ctypes.sizeof(L.GridDesc), L.GridDesc.z_faces.offset, L.GridDesc.float_type.offset,
+            ctypes.sizeof(L.ModelDesc), L.ModelDesc.pressure_solver.offset, L.ModelDesc.cg_maxiter.offset]
+    assert got == want
+
+
+def test_version_and_defaults():
+    lib = L.load()
+    assert b"sm_103a" in lib.gbo_version()
+    d = L.ModelDesc()
+    lib.gbo_model_desc_default(ctypes.byref(d))
+    assert d.advection == L.GBO_ADVECTION_WENO5 and d.closure_C == 0.16 and d.pressure_solver == L.GBO_SOLVER_FFT
+
+
+def test_invalid_extent_rejected_before_device():
+    with pytest.raises(ValueError, match="increasing"):
+        _create(og.RectilinearGrid(size=(16, 16, 8), x=(1, 0), z=(-1, 0)))
+
+
+def _create(grid, **kw):
+    d, _ = og.api.model_descriptor(grid, **kw)
+    g = grid.descriptor()
+    h = ctypes.c_void_p()
+    rc = L.load().gbo_model_create(ctypes.byref(g), ctypes.byref(d), ctypes.byref(h))
+    if rc == L.GBO_ERR_INVALID:
+        raise ValueError(L.load().gbo_last_error(None).decode())
+    return rc
+
+
+def test_validation_messages():
+    grid = og.RectilinearGrid(size=(16, 16, 8), z=(-1, 0))
+    with pytest.raises(ValueError, match="WENO"):
+        og.WENO(order=7)
+    with pytest.raises(ValueError, match="Periodic"):
+        og.RectilinearGrid(size=(16, 16, 8), topology=("Bounded", "Periodic", "Bounded"))
+    with pytest.raises(ValueError, match="BuoyancyTracer"):
+        og.api.model_descriptor(grid, buoyancy=og.BuoyancyTracer(), tracers=("c",))
+    stretched = og.RectilinearGrid(size=(16, 16, 8), z=np.linspace(-1, 0, 9) ** 3)
+    with pytest.raises(ValueError, match="regular"):
+        _create(stretched, pressure_solver=og.FFTBasedPoissonSolver())
+    with pytest.raises(ValueError, match="factor"):
+        pass_through = og.RectilinearGrid(size=(14, 16, 8), z=(-1, 0))
+        rc = _create(pass_through)
+        if rc == L.GBO_ERR_NO_DEVICE:
+            raise ValueError("factor check needs a device")
+
+
+def test_no_device_is_reported_cleanly():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    grid = og.RectilinearGrid(size=(16, 16, 8), z=(-1, 0))
+    assert _create(grid) == L.GBO_ERR_NO_DEVICE

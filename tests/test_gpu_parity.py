@@ -1,0 +1,94 @@
+"""GPU parity against the FP64 CPU oracle, through the C ABI.
+
+Tolerances: FP64 paths must match within 1e-12 relative L2 per field after one
+step and 1e-8 after 100 steps (the path's stated bar); FP32 paths state their
+error against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import cases
+import oceananigans_gb300 as og
+
+pytestmark = pytest.mark.gpu
+
+
+def compare(model, ref, names, tol):
+    errs = {}
+    for n in names:
+        errs[n] = cases.rel_l2(model.get(n), ref.get(n))
+    bad = {n: e for n, e in errs.items() if not e <= tol}
+    assert not bad, "relative L2 above %.1e: %s (all: %s)" % (tol, bad, errs)
+    return errs
+
+
+def test_projection_2d():
+    c = cases.turbulence_2d(64)
+    m, r = c.start_gpu(), c.start_oracle()
+    compare(m, r, ("u", "v", "p"), 1e-12)
+
+
+def test_turbulence_2d_one_and_100_steps():
+    c = cases.turbulence_2d(64)
+    m, r = c.start_gpu(), c.start_oracle()
+    og.time_step_(m, 0.01)
+    r.time_step(0.01)
+    compare(m, r, ("u", "v", "p"), 1e-12)
+    og.time_step_(m, 0.01, 99)
+    r.time_step(0.01, 99)
+    compare(m, r, ("u", "v", "p"), 1e-8)
+    assert m.clock[1] == 100
+
+
+@pytest.mark.parametrize("closure", ["smagorinsky", "amd", None])
+def test_convection_3d_fp64(closure):
+    c = cases.convection_3d((32, 24, 16), closure=closure, N2=1e-7, U0=2e-2)
+    m, r = c.start_gpu(), c.start_oracle()
+    compare(m, r, ("u", "v", "w", "b", "p"), 1e-12)
+    og.time_step_(m, 2.0)
+    r.time_step(2.0)
+    names = ("u", "v", "w", "b", "p", "pHY") + (("nu",) if closure else ())
+    compare(m, r, names, 1e-12)
+    og.time_step_(m, 2.0, 19)
+    r.time_step(2.0, 19)
+    compare(m, r, names, 1e-8)
+
+
+def test_stretched_amd_fourier_tridiagonal_fp64():
+    c = cases.convection_3d((32, 32, 24), closure="amd", stretched=True, N2=1e-7, U0=2e-2)
+    m, r = c.start_gpu(), c.start_oracle()
+    compare(m, r, ("u", "v", "w", "b", "p"), 1e-12)
+    og.time_step_(m, 1.0)
+    r.time_step(1.0)
+    compare(m, r, ("u", "v", "w", "b", "p", "nu", "kappa"), 1e-12)
+    og.time_step_(m, 1.0, 9)
+    r.time_step(1.0, 9)
+    compare(m, r, ("u", "v", "w", "b", "p"), 1e-8)
+
+
+def test_convection_fp32_against_fp64_oracle():
+    c64 = cases.convection_3d((32, 32, 16), closure="smagorinsky", N2=1e-7, U0=2e-2)
+    c32 = cases.convection_3d((32, 32, 16), closure="smagorinsky", N2=1e-7, U0=2e-2, float_type=np.float32)
+    m, r = c32.start_gpu(), c64.start_oracle()
+    og.time_step_(m, 2.0, 10)
+    r.time_step(2.0, 10)
+    # FP32 state against the FP64 oracle after 10 steps (stated FP32 error bar)
+    errs = compare(m, r, ("u", "v", "w", "b"), 1e-4)
+    print("fp32 vs fp64 oracle after 10 steps:", errs)
+
+
+def test_poisson_solvers_against_oracle():
+    torch = pytest.importorskip("torch")
+    for stretched in (False, True):
+        c = cases.convection_3d((32, 24, 20), stretched=stretched)
+        m = c.gpu_model()
+        r = c.oracle_model()
+        rng = np.random.default_rng(3)
+        b = rng.standard_normal((32, 24, 20))
+        b -= b.mean()
+        rhs = torch.tensor(b.ravel(order="F"), dtype=torch.float64, device="cuda")
+        phi = torch.empty_like(rhs)
+        m.poisson_solve_device(phi.data_ptr(), rhs.data_ptr())
+        got = phi.cpu().numpy().reshape(b.shape, order="F")
+        want = r.poisson_solve(b)
+        assert cases.rel_l2(got, want) < 1e-12

@@ -161,6 +161,25 @@ const char* gbo_version(void);
  * (src/Solvers/conjugate_gradient_poisson_solver.jl; the rhs there is V·div). */
 int gbo_poisson_solve_device(gbo_model* m, void* phi_device, const void* rhs_device);
 
+/* ---- instrumentation -----------------------------------------------------
+ * No reference counterpart: the reference measures with external profilers
+ * (benchmarking/, nsys in CI).  These expose what a benchmark harness needs to
+ * time the library on the stream it launches on. */
+
+/* The cudaStream_t (as void*) on which all of the model's work is issued. */
+int gbo_model_stream(gbo_model* m, void** stream);
+
+/* Cumulative number of CUDA kernels launched for this model (graph replays count
+ * every kernel they contain). */
+int64_t gbo_kernel_launches(const gbo_model* m);
+
+/* Run nsteps time steps launching kernels one by one with CUDA events around each
+ * kernel group; writes the mean duration per launch (ms) of group g into ms[g] for
+ * g < min(nmax, gbo_kernel_group_count()).  Advances the model like gbo_time_step. */
+int gbo_kernel_timings(gbo_model* m, double dt, int32_t nsteps, double* ms, int32_t nmax);
+int32_t gbo_kernel_group_count(void);
+const char* gbo_kernel_group_name(int32_t g);
+
 #ifdef __cplusplus
 }
 #endif

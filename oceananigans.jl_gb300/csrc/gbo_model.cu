@@ -235,12 +235,21 @@ struct gbo_model {
     virtual int sync() = 0;
     virtual int device_pointer(int field, void** p, int64_t* n) = 0;
     virtual int poisson_device(void* phi, const void* rhs) = 0;
+    virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
+    virtual void* stream_ptr() = 0;
+    virtual int64_t launch_count() const = 0;
     int64_t count(int field) const {
         int64_t plane = (int64_t)Nx * Ny;
         if (field == GBO_FIELD_W) return flat ? plane : plane * (Nz + 1);
         return plane * Nz;
     }
 };
+
+enum { G_MOMENTUM = 0, G_TRACER, G_CLOSURE, G_HYDROSTATIC, G_SOURCE, G_DCT_Z, G_FFT_X, G_FFT_Y, G_THOMAS,
+       G_CORRECT, G_COPY, G_NAN, GROUPS };
+const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", "k_hydrostatic", "k_source",
+                                         "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
+                                         "k_nan_check"};
 
 namespace {
 
@@ -303,6 +312,8 @@ struct ModelImpl : gbo_model {
             for (auto& b : *vec) b.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_kbot.free_();
         for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
         if (d_flags) cudaFree(d_flags);
         if (h_flags) cudaFreeHost(h_flags);
         if (stream) cudaStreamDestroy(stream);
@@ -426,7 +437,31 @@ struct ModelImpl : gbo_model {
     dim3 blk() const { return dim3(32, 8, 1); }
     dim3 grd() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, Nz); }
 
-    void check_launch() { GBO_CUDA(cudaGetLastError()); }
+    // kernel accounting: group of the next launch, launches per captured step,
+    // optional per-group CUDA events (timing mode)
+    int64_t launches = 0, graph_launches_per_step = 0;
+    bool timing = false;
+    int cur_group = 0;
+    std::vector<double> group_ms = std::vector<double>(GROUPS, 0.0);
+    std::vector<int64_t> group_n = std::vector<int64_t>(GROUPS, 0);
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    void pre(int group) {
+        cur_group = group;
+        if (timing) GBO_CUDA(cudaEventRecord(ev0, stream));
+    }
+    void check_launch() {
+        GBO_CUDA(cudaGetLastError());
+        launches += 1;
+        if (timing) {
+            GBO_CUDA(cudaEventRecord(ev1, stream));
+            GBO_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0;
+            GBO_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            group_ms[cur_group] += ms;
+            group_n[cur_group] += 1;
+        }
+    }
 
     StepP<FT> params() {
         StepP<FT> P{};
@@ -451,29 +486,41 @@ struct ModelImpl : gbo_model {
     void poisson_solve() {
         const int Nh = Nx / 2 + 1;
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
-            k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
+            pre(G_FFT_X);
+            pre(G_FFT_X);
+        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
             check_launch();
+            pre(G_FFT_Y);
             k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 1, YT);
             check_launch();
+            pre(G_THOMAS);
             k_thomas_z<FT><<<dim3((Nh + TC - 1) / TC, Ny), TC, smem_t, stream>>>(pp, tp, TC);
             check_launch();
+            pre(G_FFT_Y);
             k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 2, YT);
             check_launch();
-            k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
+            pre(G_FFT_X);
+            pre(G_FFT_X);
+        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
             check_launch();
             return;
         }
         if (!flat) {
+            pre(G_DCT_Z);
             k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 0, ZT);
             check_launch();
         }
+        pre(G_FFT_X);
         k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
         check_launch();
+        pre(G_FFT_Y);
         k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 0, YT);
         check_launch();
+        pre(G_FFT_X);
         k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
         check_launch();
         if (!flat) {
+            pre(G_DCT_Z);
             k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 1, ZT);
             check_launch();
         }
@@ -483,13 +530,45 @@ struct ModelImpl : gbo_model {
     // writing the state (u, v, w) and p; in == out is allowed.
     void project(const FT* ui, const FT* vi, const FT* wi, double dtau) {
         int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
+        pre(G_SOURCE);
         k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
         check_launch();
         poisson_solve();
         const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
         FT rdtau = FT(1) / FT(std::max(eps, dtau));
+        pre(G_CORRECT);
         k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0));
         check_launch();
+    }
+
+    // Closure fields and the hydrostatic pressure anomaly of the current state: the part
+    // of update_state! (update_nonhydrostatic_model_state.jl:64-83) that the next stage's
+    // tendencies read.  Run after every projection, as the reference does.
+    void auxiliaries() {
+        StepP<FT> P = params();
+        if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
+            pre(G_CLOSURE);
+            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(P, nu.p);
+            check_launch();
+        } else if (desc.closure == GBO_CLOSURE_AMD) {
+            StepP<FT> Q = P;
+            Q.c = ntr > 0 ? c[0].p : nullptr;
+            pre(G_CLOSURE);
+            k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
+            check_launch();
+            for (int n = 1; n < ntr; ++n) {
+                Q.c = c[n].p;
+                // viscosity recomputed identically; only κₑ of tracer n is new
+                pre(G_CLOSURE);
+                k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, kap[n].p);
+                check_launch();
+            }
+        }
+        if (has_phy) {
+            pre(G_HYDROSTATIC);
+            k_hydrostatic<FT><<<dim3((Nx + 31) / 32, (Ny + 7) / 8), blk(), 0, stream>>>(P, phy.p);
+            check_launch();
+        }
     }
 
     // One RK3 stage: Gⁿ from the current state, predictor, projection.
@@ -499,25 +578,7 @@ struct ModelImpl : gbo_model {
         P.gamma = FT(gamma);
         P.zeta = FT(zeta);
         P.first = first;
-        if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
-            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(P, nu.p);
-            check_launch();
-        } else if (desc.closure == GBO_CLOSURE_AMD) {
-            StepP<FT> Q = P;
-            Q.c = ntr > 0 ? c[0].p : nullptr;
-            k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
-            check_launch();
-            for (int n = 1; n < ntr; ++n) {
-                Q.c = c[n].p;
-                // viscosity recomputed identically; only κₑ of tracer n is new
-                k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, kap[n].p);
-                check_launch();
-            }
-        }
-        if (has_phy) {
-            k_hydrostatic<FT><<<dim3((Nx + 31) / 32, (Ny + 7) / 8), blk(), 0, stream>>>(P, phy.p);
-            check_launch();
-        }
+        pre(G_MOMENTUM);
         k_momentum<FT><<<grd(), blk(), 0, stream>>>(P);
         check_launch();
         for (int n = 0; n < ntr; ++n) {
@@ -528,6 +589,7 @@ struct ModelImpl : gbo_model {
             Q.kap = kap.empty() ? nullptr : kap[n].p;
             Q.flux_top = FT(desc.tracer_flux_top[n]);
             Q.flux_bot = FT(desc.tracer_flux_bottom[n]);
+            pre(G_TRACER);
             k_tracer<FT><<<grd(), blk(), 0, stream>>>(Q);
             check_launch();
         }
@@ -536,9 +598,11 @@ struct ModelImpl : gbo_model {
         double dtau = first ? (double)FT(dt * (double)FT(gamma)) : (double)FT(dt * (double)(FT(gamma) + FT(zeta)));
         project(us.p, vs.p, flat ? nullptr : ws.p, dtau);
         for (int n = 0; n < ntr; ++n) {
+            pre(G_COPY);
             k_copy<FT><<<std::min<size_t>((N + 255) / 256, 4096), 256, 0, stream>>>(cs[n].p, c[n].p, N);
             check_launch();
         }
+        auxiliaries();
     }
 
     void full_step(double dt) {
@@ -555,13 +619,17 @@ struct ModelImpl : gbo_model {
                 if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
                 cudaGraph_t gph;
                 GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                int64_t before = launches;
                 full_step(dt);
+                graph_launches_per_step = launches - before;
+                launches = before;
                 GBO_CUDA(cudaStreamEndCapture(stream, &gph));
                 GBO_CUDA(cudaGraphInstantiate(&graph, gph, 0));
                 GBO_CUDA(cudaGraphDestroy(gph));
                 graph_dt = dt;
             }
             for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
+            launches += graph_launches_per_step * nsteps;
         } else {
             for (int s = 0; s < nsteps; ++s) full_step(dt);
         }
@@ -570,10 +638,34 @@ struct ModelImpl : gbo_model {
             time = time + dt;
             iteration += 1;
         }
+        pre(G_NAN);
         k_nan_check<FT><<<std::min<size_t>((N + 255) / 256, 1024), 256, 0, stream>>>(u.p, N, d_flags);
         check_launch();
         return sync();
     }
+
+    int timed_steps(double dt, int nsteps, double* ms, int nmax) override {
+        if (!ev0) { GBO_CUDA(cudaEventCreate(&ev0)); GBO_CUDA(cudaEventCreate(&ev1)); }
+        std::fill(group_ms.begin(), group_ms.end(), 0.0);
+        std::fill(group_n.begin(), group_n.end(), 0);
+        timing = true;
+        try {
+            for (int s = 0; s < nsteps; ++s) {
+                full_step(dt);
+                time += dt;
+                iteration += 1;
+            }
+        } catch (...) {
+            timing = false;
+            throw;
+        }
+        timing = false;
+        for (int g = 0; g < std::min(nmax, (int)GROUPS); ++g) ms[g] = group_n[g] ? group_ms[g] / group_n[g] : 0.0;
+        return sync();
+    }
+
+    void* stream_ptr() override { return (void*)stream; }
+    int64_t launch_count() const override { return launches; }
 
     int sync() override {
         GBO_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
@@ -604,12 +696,18 @@ struct ModelImpl : gbo_model {
         if (field == GBO_FIELD_W && flat) { err = "w does not exist on a Flat-z grid"; return GBO_ERR_INVALID; }
         if (!d) { err = "unknown field id"; return GBO_ERR_INVALID; }
         if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
-        std::vector<FT> h(N);
-        for (size_t q = 0; q < N; ++q)
-            h[q] = dt_ == GBO_FLOAT32 ? FT(static_cast<const float*>(host)[q]) : FT(static_cast<const double*>(host)[q]);
+        const bool same = (dt_ == GBO_FLOAT32) == (sizeof(FT) == 4);
+        if (same) {
+            GBO_CUDA(cudaMemcpyAsync(d, host, N * sizeof(FT), cudaMemcpyHostToDevice, stream));
+        } else {
+            std::vector<FT> h(N);
+            for (size_t q = 0; q < N; ++q)
+                h[q] = dt_ == GBO_FLOAT32 ? FT(static_cast<const float*>(host)[q]) : FT(static_cast<const double*>(host)[q]);
+            GBO_CUDA(cudaMemcpyAsync(d, h.data(), N * sizeof(FT), cudaMemcpyHostToDevice, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
+        }
         if (field == GBO_FIELD_W)  // impenetrable walls: the bottom face is zero (set! + fill_halo_regions!)
-            for (size_t q = 0; q < (size_t)Nx * Ny; ++q) h[q] = FT(0);
-        GBO_CUDA(cudaMemcpyAsync(d, h.data(), N * sizeof(FT), cudaMemcpyHostToDevice, stream));
+            GBO_CUDA(cudaMemsetAsync(d, 0, (size_t)Nx * Ny * sizeof(FT), stream));
         GBO_CUDA(cudaStreamSynchronize(stream));
         return GBO_OK;
     }
@@ -617,6 +715,13 @@ struct ModelImpl : gbo_model {
     int get_field(int field, void* host, int dt_, int64_t count) override {
         FT* d = field_ptr(field);
         if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
+        const bool same = (dt_ == GBO_FLOAT32) == (sizeof(FT) == 4);
+        if (d && same) {
+            GBO_CUDA(cudaMemcpyAsync(host, d, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
+            if ((size_t)count > N) std::memset(static_cast<char*>(host) + N * sizeof(FT), 0, ((size_t)count - N) * sizeof(FT));
+            return GBO_OK;
+        }
         std::vector<FT> h(N, FT(0));
         if (d) {
             GBO_CUDA(cudaMemcpyAsync(h.data(), d, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
@@ -636,6 +741,7 @@ struct ModelImpl : gbo_model {
 
     int set_finalize(int enforce) override {
         if (enforce) project(u.p, v.p, flat ? nullptr : w.p, 1.0);
+        auxiliaries();
         return sync();
     }
 
@@ -651,6 +757,7 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaMemcpyAsync(rb.p, rhs, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
             // set_source_term!: b ← b Δzᶜ (fourier_tridiagonal_poisson_solver.jl:268-290)
+            pre(G_SOURCE);
             k_scale_dzc<FT><<<grd(), blk(), 0, stream>>>(gp, rb.p);
             check_launch();
         }
@@ -813,6 +920,24 @@ const char* gbo_last_error(const gbo_model* m) {
 }
 
 const char* gbo_version(void) { return "gb300ocean 0.1.0 (sm_103a)"; }
+
+int gbo_model_stream(gbo_model* m, void** stream) {
+    if (!m || !stream) return GBO_ERR_INVALID;
+    *stream = m->stream_ptr();
+    return GBO_OK;
+}
+
+int64_t gbo_kernel_launches(const gbo_model* m) { return m ? m->launch_count() : -1; }
+
+int gbo_kernel_timings(gbo_model* m, double dt, int32_t nsteps, double* ms, int32_t nmax) {
+    if (!m || !ms) return GBO_ERR_INVALID;
+    if (!(dt > 0) || !std::isfinite(dt)) { m->err = "dt must be positive and finite"; return GBO_ERR_INVALID; }
+    return guarded(m, [&]() { return m->timed_steps(dt, nsteps, ms, nmax); });
+}
+
+int32_t gbo_kernel_group_count(void) { return GROUPS; }
+
+const char* gbo_kernel_group_name(int32_t g) { return (g >= 0 && g < GROUPS) ? GROUP_NAMES[g] : ""; }
 
 int gbo_poisson_solve_device(gbo_model* m, void* phi, const void* rhs) {
     if (!m || !phi || !rhs) return GBO_ERR_INVALID;

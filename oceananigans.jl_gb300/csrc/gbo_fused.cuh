@@ -1,0 +1,597 @@
+// gbo_fused.cuh -- column-marching fused momentum tendency + RK3 predictor kernel.
+//
+// Same arithmetic as k_momentum (gbo_step.cuh), organised for the GPU:
+//   * a 32 x 8 block owns a tile of (i, j) columns and marches upward over a
+//     chunk of levels k;
+//   * x / y stencils (halo 3) are read from shared-memory planes that the block
+//     loads once per level (periodic wrap and the z-halo rules applied at load);
+//   * z stencils come from per-thread register windows that slide with k;
+//   * every face flux is evaluated once: a thread computes the fluxes through
+//     the west, south and top faces of its control volumes, exchanges west and
+//     south values with its neighbours through shared memory, and carries the
+//     top value to the next level as the bottom value.
+// The extra faces on the tile's east column and north row are evaluated by
+// warps 0 and 1 after their own work.
+#pragma once
+#include "gbo_step.cuh"
+
+namespace fused {
+
+constexpr int TX = 32, TY = 8, H = 3;
+constexpr int PX = TX + 2 * H, PY = TY + 2 * H, PS = PX * PY;
+constexpr int NT = TX * TY;
+
+GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + H); }
+
+// exchange quantities (west-face values live in WX[q][ty][tx], tx = 0..TX;
+// south-face values in SY[q][ty][tx], ty = 0..TY)
+enum { A_UU = 0, A_UV, A_UW, C_11, C_12, C_13, A_CX, Q_CX, NWX };   // west faces
+enum { A_VU = 0, A_VV, A_VW, C_22, C_12N, C_23, A_CY, Q_CY, NSY };  // south faces
+
+template <typename FT>
+struct Smem {
+    FT U[2][PS], V[2][PS], W[2][PS];  // u, v at levels k-1, k; w at faces k, k+1
+    FT NU[3][PS];                      // νₑ at k-1, k, k+1
+    FT PH[PS];                         // pHY′ at k
+    FT CC[PS];                         // tracer at k
+    FT KP[2][PS];                      // AMD tracer diffusivity κₑ at k, k+1
+    FT WX[NWX][TY][TX + 1];
+    FT SY[NSY][TY + 1][TX];
+};
+
+// Load one plane of a Center-in-z field (level k) with halo H into smem.
+template <typename FT>
+GBO_D void load_plane_c(FT* dst, const FT* src, const GridP<FT>& g, int i0, int j0, int k, int tid) {
+    CFld<FT> f = cfld(src, g);
+    for (int e = tid; e < PS; e += NT) {
+        int px = e % PX, py = e / PX;
+        dst[e] = f(i0 + px - H, j0 + py - H, k);
+    }
+}
+template <typename FT>
+GBO_D void load_plane_w(FT* dst, const FT* src, const GridP<FT>& g, int i0, int j0, int k, int tid) {
+    WFld<FT> f = wfld(src, g);
+    for (int e = tid; e < PS; e += NT) {
+        int px = e % PX, py = e / PX;
+        dst[e] = f(i0 + px - H, j0 + py - H, k);
+    }
+}
+
+// Advective momentum flux through a face: ũ from four area-weighted velocities
+// (Centered(4)), ψ reconstructed by WENO5 from six values.
+template <typename FT>
+GBO_D FT flux_c4_w5(FT a0, FT a1, FT a2, FT a3, const FT* S) {
+    FT ut = cen4<FT>(a0, a1, a2, a3);
+    return ut * weno5<FT>(S, bias_left(ut));
+}
+
+// Per-thread column state: register windows of u, v (levels k-3..k+3) and
+// w (faces k-2..k+3), plus the values carried from the level below.
+template <typename FT>
+struct Col {
+    FT uc[7], vc[7], wc[6];
+    FT fWu, fWv, fWw;     // advective fluxes through the bottom faces (u, v at face k; w at centre k-1)
+    FT t13, t23, t33;     // closure fluxes τ13(k), τ23(k) at face k and τ33 at centre k-1
+    FT cc[7];             // tracer window (levels k-3..k+3)
+    FT fWc, qzc;          // tracer advective / diffusive fluxes through the bottom face k
+};
+
+}  // namespace fused
+
+// TR: also advance one tracer (P.c -> P.co, P.Gc) in the same march.
+template <typename FT, bool TR>
+__global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk) {
+    using namespace fused;
+    extern __shared__ unsigned char smem_raw[];
+    Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
+    const GridP<FT>& g = P.g;
+    Met<FT> M(g);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int i = i0 + tx, j = j0 + ty;
+    const int kb = blockIdx.z * kchunk, ke = min(g.Nz, kb + kchunk);
+    const bool closure = P.closure != CL_NONE;
+    const bool inside = (i < g.Nx) && (j < g.Ny);
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Ng = cfld(P.nu, g);
+    WFld<FT> Wg = wfld(P.w, g);
+    const int Nz = g.Nz;
+    const FT Az = M.Az();
+    const size_t plane = (size_t)g.Nx * g.Ny;
+
+    // ---- prologue: planes and windows for the first level kb ----
+    int cu = 0;  // ring slot of level k for U/V (k-1 in 1-cu); W: slot of face k in cw, k+1 in 1-cw
+    load_plane_c(s.U[1 - cu], P.u, g, i0, j0, kb - 1, tid);
+    load_plane_c(s.V[1 - cu], P.v, g, i0, j0, kb - 1, tid);
+    load_plane_c(s.U[cu], P.u, g, i0, j0, kb, tid);
+    load_plane_c(s.V[cu], P.v, g, i0, j0, kb, tid);
+    int cw = 0;
+    load_plane_w(s.W[cw], P.w, g, i0, j0, kb, tid);
+    int cn = 0;  // NU slots: cn = k-1, (cn+1)%3 = k, (cn+2)%3 = k+1
+    if (closure) {
+        load_plane_c(s.NU[cn], P.nu, g, i0, j0, kb - 1, tid);
+        load_plane_c(s.NU[(cn + 1) % 3], P.nu, g, i0, j0, kb, tid);
+    }
+    Col<FT> c;
+    {
+        const int ii = i % g.Nx, jj = j % g.Ny;
+#pragma unroll
+        for (int o = 0; o < 7; ++o) {
+            c.uc[o] = Ug(ii, jj, kb - 3 + o);
+            c.vc[o] = Vg(ii, jj, kb - 3 + o);
+        }
+#pragma unroll
+        for (int o = 0; o < 6; ++o) c.wc[o] = Wg(ii, jj, kb - 2 + o);
+        if (TR) {
+            CFld<FT> Cg = cfld(P.c, g);
+#pragma unroll
+            for (int o = 0; o < 7; ++o) c.cc[o] = Cg(ii, jj, kb - 3 + o);
+        }
+    }
+    const bool amd = P.closure == CL_AMD;
+    int ck = 0;  // KP slot of level k (k+1 in 1-ck)
+    if (TR && amd) load_plane_c(s.KP[ck], P.kap, g, i0, j0, kb, tid);
+    __syncthreads();
+    // bottom fluxes at level kb (faces kb / centre kb-1), from planes (w at kb) and windows
+    {
+        const FT* Wk = s.W[cw];
+        // F_Wu(i, j, kb): w̃ = C4(Az w(i-2..i+1, kb)), ψ = u(kb-3..kb+2)
+        {
+            FT wt = cen4<FT>(Az * Wk[pidx(tx - 2, ty)], Az * Wk[pidx(tx - 1, ty)], Az * Wk[pidx(tx, ty)], Az * Wk[pidx(tx + 1, ty)]);
+            auto q = [&](int o) { return c.uc[3 + o]; };
+            c.fWu = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(kb + 1, Nz));
+        }
+        {
+            FT wt = cen4<FT>(Az * Wk[pidx(tx, ty - 2)], Az * Wk[pidx(tx, ty - 1)], Az * Wk[pidx(tx, ty)], Az * Wk[pidx(tx, ty + 1)]);
+            auto q = [&](int o) { return c.vc[3 + o]; };
+            c.fWv = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(kb + 1, Nz));
+        }
+        // F_Ww at centre kb-1: reconstructions at face kb from w(kb-3..kb+2) -> window index o+2
+        {
+            const int kc = kb - 1;
+            FT wm3 = Wg(i % g.Nx, j % g.Ny, kb - 3);
+            auto qs = [&](int o) { return Az * (o == -3 ? wm3 : c.wc[2 + o]); };
+            FT wt = symm<FT>(qs, zlev_symm_center(kc + 1, Nz));
+            auto qb = [&](int o) { return o == -3 ? wm3 : c.wc[2 + o]; };
+            c.fWw = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(kc + 1, Nz));
+        }
+        if (closure) {
+            const FT* Nm = s.NU[cn];
+            const FT* Nk = s.NU[(cn + 1) % 3];
+            // τ13 at (i, kb): -2 ν_fcf S13, S13 = ½(∂z u + ∂x w)
+            FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(tx - 1, ty)] + Nm[pidx(tx, ty)]) + FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]));
+            FT dzu = (c.uc[3] - c.uc[2]) * M.rdzf(kb);
+            FT dxw = (Wk[pidx(tx, ty)] - Wk[pidx(tx - 1, ty)]) * g.rdx;
+            c.t13 = FT(-2) * (nfcf * (FT(0.5) * (dzu + dxw)));
+            FT ncff = FT(0.5) * (FT(0.5) * (Nm[pidx(tx, ty - 1)] + Nm[pidx(tx, ty)]) + FT(0.5) * (Nk[pidx(tx, ty - 1)] + Nk[pidx(tx, ty)]));
+            FT dzv = (c.vc[3] - c.vc[2]) * M.rdzf(kb);
+            FT dyw = (Wk[pidx(tx, ty)] - Wk[pidx(tx, ty - 1)]) * g.rdy;
+            c.t23 = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
+            // τ33 at centre kb-1: -2 ν(kb-1) (w(kb) - w(kb-1)) / Δzᶜ(kb-1)
+            c.t33 = FT(-2) * (Nm[pidx(tx, ty)] * ((c.wc[2] - c.wc[1]) * M.rdzc(kb - 1)));
+        }
+        if (TR) {
+            // tracer flux through face kb: Az w(kb) ψ(kb), diffusive -κᶜᶜᶠ ∂z c
+            FT wk = c.wc[2];
+            auto q = [&](int o) { return c.cc[3 + o]; };
+            c.fWc = Az * wk * biased<FT>(q, bias_left(wk), zlev_biased_face(kb + 1, Nz));
+            c.qzc = FT(0);
+            if (closure) {
+                FT km, kk;
+                if (amd) {
+                    CFld<FT> Kg = cfld(P.kap, g);
+                    km = Kg(i % g.Nx, j % g.Ny, kb - 1);
+                    kk = s.KP[ck][pidx(tx, ty)];
+                } else {
+                    km = s.NU[cn][pidx(tx, ty)];
+                    kk = s.NU[(cn + 1) % 3][pidx(tx, ty)];
+                }
+                FT kz = amd ? FT(0.5) * (km + kk) : FT(0.5) * (km + kk) / P.Pr;
+                c.qzc = -kz * ((c.cc[3] - c.cc[2]) * M.rdzf(kb));
+            }
+        }
+    }
+
+    for (int k = kb; k < ke; ++k) {
+        // ---- load the planes new at this level: w(k+1), ν(k+1), pHY(k) ----
+        __syncthreads();
+        load_plane_w(s.W[1 - cw], P.w, g, i0, j0, k + 1, tid);
+        if (closure) load_plane_c(s.NU[(cn + 2) % 3], P.nu, g, i0, j0, k + 1, tid);
+        if (P.has_phy) load_plane_c(s.PH, P.phy, g, i0, j0, k, tid);
+        if (TR) load_plane_c(s.CC, P.c, g, i0, j0, k, tid);
+        if (TR && amd) load_plane_c(s.KP[1 - ck], P.kap, g, i0, j0, k + 1, tid);
+        __syncthreads();
+        const FT* Uk = s.U[cu];
+        const FT* Um = s.U[1 - cu];
+        const FT* Vk = s.V[cu];
+        const FT* Vm = s.V[1 - cu];
+        const FT* Wk = s.W[cw];
+        const FT* Wp = s.W[1 - cw];
+        const FT* Nm = s.NU[cn];
+        const FT* Nk = s.NU[(cn + 1) % 3];
+        const FT* Np = s.NU[(cn + 2) % 3];
+        const FT Ax = M.Ax(k), Ay = M.Ay(k);
+
+        // ---- west / south face quantities of this thread (and the tile edges) ----
+        auto west = [&](int x, int y, bool own) {
+            // F_Uu at centre i-1: ũ = C4(Ax u(i-2..i+1)), ψ = u(i-3..i+2)
+            FT S[6];
+#pragma unroll
+            for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x - 3 + o, y)];
+            s.WX[A_UU][y][x] = flux_c4_w5<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4], S);
+            // F_Uv at (f,f,c): ũ = C4(Ax u(i, j-2..j+1)), ψ = v(i-3..i+2, j)
+#pragma unroll
+            for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x - 3 + o, y)];
+            s.WX[A_UV][y][x] = flux_c4_w5<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)], S);
+            // F_Uw at (f,c,f) level k: ũ = symm_z(Ax u(i, k-2..k+1)), ψ = w(i-3..i+2, k)
+            {
+                FT uz[4];
+                if (own) {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
+                } else {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) uz[o] = Ug(i0 + x, j0 + y, k - 2 + o);
+                }
+                auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
+                FT ut = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+#pragma unroll
+                for (int o = 0; o < 6; ++o) S[o] = Wk[pidx(x - 3 + o, y)];
+                s.WX[A_UW][y][x] = ut * weno5<FT>(S, bias_left(ut));
+            }
+            if (closure) {
+                // τ11 at centre i-1, τ12 at (i, j), τ13 at (i, k)
+                FT s11 = (Uk[pidx(x, y)] - Uk[pidx(x - 1, y)]) * g.rdx;
+                s.WX[C_11][y][x] = FT(-2) * (Nk[pidx(x - 1, y)] * s11);
+                FT nffc = FT(0.5) * (FT(0.5) * (Nk[pidx(x - 1, y - 1)] + Nk[pidx(x, y - 1)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
+                FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
+                FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
+                s.WX[C_12][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
+                if (own) {
+                    s.WX[C_13][y][x] = c.t13;
+                } else {
+                    FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(x - 1, y)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
+                    FT dzu = (Uk[pidx(x, y)] - Um[pidx(x, y)]) * M.rdzf(k);
+                    FT dxw = (Wk[pidx(x, y)] - Wk[pidx(x - 1, y)]) * g.rdx;
+                    s.WX[C_13][y][x] = FT(-2) * (nfcf * (FT(0.5) * (dzu + dxw)));
+                }
+            }
+            if (TR) {
+                // F_cx = Ax u(i) ψ(i),  q_x = -κᶠᶜᶜ ∂x c
+                FT ut = Uk[pidx(x, y)];
+#pragma unroll
+                for (int o = 0; o < 6; ++o) S[o] = s.CC[pidx(x - 3 + o, y)];
+                s.WX[A_CX][y][x] = Ax * ut * weno5<FT>(S, bias_left(ut));
+                if (closure) {
+                    const FT* K = amd ? s.KP[ck] : Nk;
+                    FT kx = amd ? FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) / P.Pr;
+                    s.WX[Q_CX][y][x] = -kx * ((s.CC[pidx(x, y)] - s.CC[pidx(x - 1, y)]) * g.rdx);
+                }
+            }
+        };
+        auto south = [&](int x, int y, bool own) {
+            FT S[6];
+            // F_Vu at (f,f,c): ṽ = C4(Ay v(i-2..i+1, j)), ψ = u(i, j-3..j+2)
+#pragma unroll
+            for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x, y - 3 + o)];
+            s.SY[A_VU][y][x] = flux_c4_w5<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)], S);
+            // F_Vv at centre j-1: ṽ = C4(Ay v(j-2..j+1)), ψ = v(j-3..j+2)
+#pragma unroll
+            for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x, y - 3 + o)];
+            s.SY[A_VV][y][x] = flux_c4_w5<FT>(Ay * S[1], Ay * S[2], Ay * S[3], Ay * S[4], S);
+            // F_Vw at (c,f,f) level k
+            {
+                FT vz[4];
+                if (own) {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
+                } else {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) vz[o] = Vg(i0 + x, j0 + y, k - 2 + o);
+                }
+                auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
+                FT vt = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+#pragma unroll
+                for (int o = 0; o < 6; ++o) S[o] = Wk[pidx(x, y - 3 + o)];
+                s.SY[A_VW][y][x] = vt * weno5<FT>(S, bias_left(vt));
+            }
+            if (closure) {
+                FT s22 = (Vk[pidx(x, y)] - Vk[pidx(x, y - 1)]) * g.rdy;
+                s.SY[C_22][y][x] = FT(-2) * (Nk[pidx(x, y - 1)] * s22);
+                FT nffc = FT(0.5) * (FT(0.5) * (Nk[pidx(x - 1, y - 1)] + Nk[pidx(x, y - 1)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
+                FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
+                FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
+                s.SY[C_12N][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
+                if (own) {
+                    s.SY[C_23][y][x] = c.t23;
+                } else {
+                    FT ncff = FT(0.5) * (FT(0.5) * (Nm[pidx(x, y - 1)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x, y - 1)] + Nk[pidx(x, y)]));
+                    FT dzv = (Vk[pidx(x, y)] - Vm[pidx(x, y)]) * M.rdzf(k);
+                    FT dyw = (Wk[pidx(x, y)] - Wk[pidx(x, y - 1)]) * g.rdy;
+                    s.SY[C_23][y][x] = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
+                }
+            }
+            if (TR) {
+                FT vt = Vk[pidx(x, y)];
+#pragma unroll
+                for (int o = 0; o < 6; ++o) S[o] = s.CC[pidx(x, y - 3 + o)];
+                s.SY[A_CY][y][x] = Ay * vt * weno5<FT>(S, bias_left(vt));
+                if (closure) {
+                    const FT* K = amd ? s.KP[ck] : Nk;
+                    FT ky = amd ? FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) / P.Pr;
+                    s.SY[Q_CY][y][x] = -ky * ((s.CC[pidx(x, y)] - s.CC[pidx(x, y - 1)]) * g.rdy);
+                }
+            }
+        };
+        west(tx, ty, true);
+        south(tx, ty, true);
+        if (ty == 0 && tx < TY) west(TX, tx, false);   // east column of the tile
+        if (ty == 1) south(tx, TY, false);             // north row of the tile
+
+        // ---- top-face quantities (carried to the next level) ----
+        FT fWu_t, fWv_t, fWw_t, t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);
+        {
+            FT wt = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
+            auto q = [&](int o) { return c.uc[4 + o]; };
+            fWu_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+        }
+        {
+            FT wt = cen4<FT>(Az * Wp[pidx(tx, ty - 2)], Az * Wp[pidx(tx, ty - 1)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx, ty + 1)]);
+            auto q = [&](int o) { return c.vc[4 + o]; };
+            fWv_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+        }
+        {
+            // F_Ww at centre k: face k+1 reconstructions from w(k-2..k+3) = wc[0..5]
+            auto qs = [&](int o) { return Az * c.wc[3 + o]; };
+            FT wt = symm<FT>(qs, zlev_symm_center(k + 1, Nz));
+            auto qb = [&](int o) { return c.wc[3 + o]; };
+            fWw_t = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, Nz));
+        }
+        if (closure) {
+            FT nfcf = FT(0.5) * (FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx - 1, ty)] + Np[pidx(tx, ty)]));
+            FT dzu = (c.uc[4] - c.uc[3]) * M.rdzf(k + 1);
+            FT dxw = (Wp[pidx(tx, ty)] - Wp[pidx(tx - 1, ty)]) * g.rdx;
+            t13_t = FT(-2) * (nfcf * (FT(0.5) * (dzu + dxw)));
+            FT ncff = FT(0.5) * (FT(0.5) * (Nk[pidx(tx, ty - 1)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx, ty - 1)] + Np[pidx(tx, ty)]));
+            FT dzv = (c.vc[4] - c.vc[3]) * M.rdzf(k + 1);
+            FT dyw = (Wp[pidx(tx, ty)] - Wp[pidx(tx, ty - 1)]) * g.rdy;
+            t23_t = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
+            t33_t = FT(-2) * (Nk[pidx(tx, ty)] * ((c.wc[3] - c.wc[2]) * M.rdzc(k)));
+        }
+        FT fWc_t = FT(0), qzc_t = FT(0);
+        if (TR) {
+            FT wt = c.wc[3];  // w at face k+1
+            auto q = [&](int o) { return c.cc[4 + o]; };
+            fWc_t = Az * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+            if (closure) {
+                FT kk = amd ? s.KP[ck][pidx(tx, ty)] : Nk[pidx(tx, ty)];
+                FT kp = amd ? s.KP[1 - ck][pidx(tx, ty)] : Np[pidx(tx, ty)];
+                FT kz = amd ? FT(0.5) * (kk + kp) : FT(0.5) * (kk + kp) / P.Pr;
+                qzc_t = -kz * ((c.cc[4] - c.cc[3]) * M.rdzf(k + 1));
+            }
+        }
+        __syncthreads();
+
+        // ---- tendencies and predictor ----
+        if (inside) {
+            const size_t idx = i + (size_t)g.Nx * j + plane * k;
+            const FT rVc = M.rVc(k);
+            // u
+            {
+                FT dx_ = s.WX[A_UU][ty][tx + 1] - s.WX[A_UU][ty][tx];
+                FT dy_ = s.SY[A_VU][ty + 1][tx] - s.SY[A_VU][ty][tx];
+                FT dz_ = g.flatz ? FT(0) : (fWu_t - c.fWu);
+                FT G = -(rVc * (dx_ + dy_ + dz_));
+                if (P.has_cor) {
+                    FT ixy = FT(0.5) * (FT(0.5) * (Ay * Vk[pidx(tx - 1, ty)] + Ay * Vk[pidx(tx, ty)]) +
+                                        FT(0.5) * (Ay * Vk[pidx(tx - 1, ty + 1)] + Ay * Vk[pidx(tx, ty + 1)]));
+                    FT xfu = -P.f * ixy * (FT(1) / Ay);
+                    G = G - xfu;
+                }
+                if (P.has_phy) G = G - (s.PH[pidx(tx, ty)] - s.PH[pidx(tx - 1, ty)]) * g.rdx;
+                if (closure) {
+                    FT cdx = Ax * s.WX[C_11][ty][tx + 1] - Ax * s.WX[C_11][ty][tx];
+                    FT cdy = Ay * s.SY[C_12N][ty + 1][tx] - Ay * s.SY[C_12N][ty][tx];
+                    FT cdz = g.flatz ? FT(0) : (Az * t13_t - Az * c.t13);
+                    G = G - rVc * (cdx + cdy + cdz);
+                }
+                FT Gm = P.first ? FT(0) : P.Gu[idx];
+                P.Gu[idx] = G;
+                P.uo[idx] = rk3_update(Uk[pidx(tx, ty)], G, Gm, P);
+            }
+            // v
+            {
+                FT dx_ = s.WX[A_UV][ty][tx + 1] - s.WX[A_UV][ty][tx];
+                FT dy_ = s.SY[A_VV][ty + 1][tx] - s.SY[A_VV][ty][tx];
+                FT dz_ = g.flatz ? FT(0) : (fWv_t - c.fWv);
+                FT G = -(rVc * (dx_ + dy_ + dz_));
+                if (P.has_cor) {
+                    FT ixy = FT(0.5) * (FT(0.5) * (Ax * Uk[pidx(tx, ty - 1)] + Ax * Uk[pidx(tx + 1, ty - 1)]) +
+                                        FT(0.5) * (Ax * Uk[pidx(tx, ty)] + Ax * Uk[pidx(tx + 1, ty)]));
+                    FT yfu = P.f * ixy * (FT(1) / Ax);
+                    G = G - yfu;
+                }
+                if (P.has_phy) G = G - (s.PH[pidx(tx, ty)] - s.PH[pidx(tx, ty - 1)]) * g.rdy;
+                if (closure) {
+                    FT cdx = Ax * s.WX[C_12][ty][tx + 1] - Ax * s.WX[C_12][ty][tx];
+                    FT cdy = Ay * s.SY[C_22][ty + 1][tx] - Ay * s.SY[C_22][ty][tx];
+                    FT cdz = g.flatz ? FT(0) : (Az * t23_t - Az * c.t23);
+                    G = G - rVc * (cdx + cdy + cdz);
+                }
+                FT Gm = P.first ? FT(0) : P.Gv[idx];
+                P.Gv[idx] = G;
+                P.vo[idx] = rk3_update(Vk[pidx(tx, ty)], G, Gm, P);
+            }
+            // w (face k; k = 0 is the wall)
+            if (!g.flatz) {
+                if (k == 0) {
+                    P.wo[idx] = FT(0);
+                } else {
+                    FT dx_ = s.WX[A_UW][ty][tx + 1] - s.WX[A_UW][ty][tx];
+                    FT dy_ = s.SY[A_VW][ty + 1][tx] - s.SY[A_VW][ty][tx];
+                    FT dz_ = fWw_t - c.fWw;
+                    FT rVf = M.rVf(k);
+                    FT G = -(rVf * (dx_ + dy_ + dz_));
+                    if (closure) {
+                        FT Axf = M.Axf(k), Ayf = M.Ayf(k);
+                        FT cdx = Axf * s.WX[C_13][ty][tx + 1] - Axf * s.WX[C_13][ty][tx];
+                        FT cdy = Ayf * s.SY[C_23][ty + 1][tx] - Ayf * s.SY[C_23][ty][tx];
+                        FT cdz = Az * t33_t - Az * c.t33;
+                        G = G - rVf * (cdx + cdy + cdz);
+                    }
+                    FT Gm = P.first ? FT(0) : P.Gw[idx];
+                    P.Gw[idx] = G;
+                    P.wo[idx] = rk3_update(Wk[pidx(tx, ty)], G, Gm, P);
+                }
+            }
+        }
+
+        if (TR && inside) {
+            const size_t idx = i + (size_t)g.Nx * j + plane * k;
+            const FT rVc = M.rVc(k);
+            FT dx_ = s.WX[A_CX][ty][tx + 1] - s.WX[A_CX][ty][tx];
+            FT dy_ = s.SY[A_CY][ty + 1][tx] - s.SY[A_CY][ty][tx];
+            FT dz_ = g.flatz ? FT(0) : (fWc_t - c.fWc);
+            FT G = -(rVc * (dx_ + dy_ + dz_));
+            if (closure) {
+                FT cdx = Ax * s.WX[Q_CX][ty][tx + 1] - Ax * s.WX[Q_CX][ty][tx];
+                FT cdy = Ay * s.SY[Q_CY][ty + 1][tx] - Ay * s.SY[Q_CY][ty][tx];
+                FT cdz = g.flatz ? FT(0) : (Az * qzc_t - Az * c.qzc);
+                G = G - rVc * (cdx + cdy + cdz);
+            }
+            if (!g.flatz) {
+                if (k == Nz - 1 && P.flux_top != FT(0)) G -= P.flux_top * Az / (Az * M.dzc(k));
+                if (k == 0 && P.flux_bot != FT(0)) G += P.flux_bot * Az / (Az * M.dzc(k));
+            }
+            FT Gm = P.first ? FT(0) : P.Gc[idx];
+            P.Gc[idx] = G;
+            P.co[idx] = rk3_update(s.CC[pidx(tx, ty)], G, Gm, P);
+        }
+
+        // ---- advance: carry top -> bottom, slide windows and rotate plane slots ----
+        c.fWu = fWu_t; c.fWv = fWv_t; c.fWw = fWw_t;
+        c.t13 = t13_t; c.t23 = t23_t; c.t33 = t33_t;
+        c.fWc = fWc_t; c.qzc = qzc_t;
+        {
+            const int ii = i % g.Nx, jj = j % g.Ny;
+#pragma unroll
+            for (int o = 0; o < 6; ++o) { c.uc[o] = c.uc[o + 1]; c.vc[o] = c.vc[o + 1]; }
+            c.uc[6] = Ug(ii, jj, k + 4);
+            c.vc[6] = Vg(ii, jj, k + 4);
+#pragma unroll
+            for (int o = 0; o < 5; ++o) c.wc[o] = c.wc[o + 1];
+            c.wc[5] = Wg(ii, jj, k + 4);
+            if (TR) {
+                CFld<FT> Cg = cfld(P.c, g);
+#pragma unroll
+                for (int o = 0; o < 6; ++o) c.cc[o] = c.cc[o + 1];
+                c.cc[6] = Cg(ii, jj, k + 4);
+            }
+        }
+        __syncthreads();
+        // u, v at level k+1 into the slot of level k-1
+        if (k + 1 < ke) {
+            load_plane_c(s.U[1 - cu], P.u, g, i0, j0, k + 1, tid);
+            load_plane_c(s.V[1 - cu], P.v, g, i0, j0, k + 1, tid);
+        }
+        cu = 1 - cu;
+        cw = 1 - cw;
+        cn = (cn + 1) % 3;
+        ck = 1 - ck;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Smagorinsky-Lilly νₑ on a shared-memory tile: the block stages u, v, w, b on a
+// (32+2) x (8+2) x (KT+2) box once (halo synthesis at load) and every thread
+// evaluates the closure for KT levels of its column from shared memory.
+// Arithmetic identical to k_smagorinsky (gbo_kernels.cuh).
+// ---------------------------------------------------------------------------
+namespace smag {
+constexpr int TX = 32, TY = 8, KT = 4;
+constexpr int BX = TX + 2, BY = TY + 2, BZ = KT + 2, BS = BX * BY * BZ;
+GBO_D int bidx(int x, int y, int z) { return ((z + 1) * BY + (y + 1)) * BX + (x + 1); }
+template <typename FT>
+struct Smem {
+    FT u[BS], v[BS], w[BS], b[BS];
+};
+}  // namespace smag
+
+template <typename FT>
+__global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __restrict__ nu_out) {
+    using namespace smag;
+    extern __shared__ unsigned char smem_raw[];
+    Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
+    const GridP<FT>& g = P.g;
+    Met<FT> M(g);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Bg = cfld(P.b, g);
+    WFld<FT> Wg = wfld(P.w, g);
+    const bool buoy = P.buoyancy && !g.flatz;
+    for (int e = tid; e < BS; e += TX * TY) {
+        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
+        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
+        s.u[e] = Ug(gi, gj, gk);
+        s.v[e] = Vg(gi, gj, gk);
+        s.w[e] = Wg(gi, gj, gk);
+        s.b[e] = buoy ? Bg(gi, gj, gk) : FT(0);
+    }
+    __syncthreads();
+    const int i = i0 + tx, j = j0 + ty;
+    if (i >= g.Nx || j >= g.Ny) return;
+    for (int z = 0; z < KT; ++z) {
+        const int k = k0 + z;
+        if (k >= g.Nz) break;
+        auto U = [&](int x, int y, int zz) { return s.u[bidx(x, y, zz)]; };
+        auto V = [&](int x, int y, int zz) { return s.v[bidx(x, y, zz)]; };
+        auto W = [&](int x, int y, int zz) { return s.w[bidx(x, y, zz)]; };
+        // strain components at the staggered points around the cell (velocity_tracer_gradients.jl)
+        auto S12 = [&](int x, int y) {
+            FT dyu = (U(x, y, z) - U(x, y - 1, z)) * g.rdy;
+            FT dxv = (V(x, y, z) - V(x - 1, y, z)) * g.rdx;
+            return FT(0.5) * (dyu + dxv);
+        };
+        auto S13 = [&](int x, int zz) {
+            if (g.flatz) return FT(0);
+            FT dzu = (U(x, ty, zz) - U(x, ty, zz - 1)) * M.rdzf(k0 + zz);
+            FT dxw = (W(x, ty, zz) - W(x - 1, ty, zz)) * g.rdx;
+            return FT(0.5) * (dzu + dxw);
+        };
+        auto S23 = [&](int y, int zz) {
+            if (g.flatz) return FT(0);
+            FT dzv = (V(tx, y, zz) - V(tx, y, zz - 1)) * M.rdzf(k0 + zz);
+            FT dyw = (W(tx, y, zz) - W(tx, y - 1, zz)) * g.rdy;
+            return FT(0.5) * (dzv + dyw);
+        };
+        auto sq = [](FT x) { return x * x; };
+        FT s11 = (U(tx + 1, ty, z) - U(tx, ty, z)) * g.rdx;
+        FT s22 = (V(tx, ty + 1, z) - V(tx, ty, z)) * g.rdy;
+        FT s33 = g.flatz ? FT(0) : (W(tx, ty, z + 1) - W(tx, ty, z)) * M.rdzc(k);
+        FT tr = s11 * s11 + s22 * s22 + s33 * s33;
+        FT ixy = FT(0.5) * (FT(0.5) * (sq(S12(tx, ty)) + sq(S12(tx + 1, ty))) + FT(0.5) * (sq(S12(tx, ty + 1)) + sq(S12(tx + 1, ty + 1))));
+        FT ixz, iyz;
+        if (g.flatz) {
+            ixz = FT(0);
+            iyz = FT(0);
+        } else {
+            ixz = FT(0.5) * (FT(0.5) * (sq(S13(tx, z)) + sq(S13(tx + 1, z))) + FT(0.5) * (sq(S13(tx, z + 1)) + sq(S13(tx + 1, z + 1))));
+            iyz = FT(0.5) * (FT(0.5) * (sq(S23(ty, z)) + sq(S23(ty + 1, z))) + FT(0.5) * (sq(S23(ty, z + 1)) + sq(S23(ty + 1, z + 1))));
+        }
+        FT Sig2 = tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
+        FT D3 = g.dx * g.dy * M.dzc(k);
+        FT Df = cbrt(D3);
+        FT N2 = FT(0);
+        if (buoy) {
+            FT b1 = (s.b[bidx(tx, ty, z)] - s.b[bidx(tx, ty, z - 1)]) * M.rdzf(k);
+            FT b2 = (s.b[bidx(tx, ty, z + 1)] - s.b[bidx(tx, ty, z)]) * M.rdzf(k + 1);
+            N2 = FT(0.5) * (b1 + b2);
+        }
+        FT N2p = fmax(FT(0), N2);
+        FT r = P.Cb * N2p / Sig2;
+        FT mn = isnan(r) ? r : fmin(FT(1), r);
+        FT vs2 = FT(1) - mn;
+        FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
+        FT cs2 = vs * (P.C * P.C);
+        nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * (Df * Df) * sqrt(FT(2) * Sig2);
+    }
+}

@@ -8,7 +8,7 @@
 
 #include "../../include/gbo.h"
 #include "gbo_fft.cuh"
-#include "gbo_step.cuh"
+#include "gbo_fused.cuh"
 
 // ===========================================================================
 // Pressure source and projection kernels
@@ -295,6 +295,7 @@ struct ModelImpl : gbo_model {
     PassP<FT> pp{};
     ThomasP tp{};
     int ZT = 32, XL = 8, YT = 16, TC = 16;
+    int kchunk = 16;  // levels marched per block by the fused momentum kernel
     size_t smem_z = 0, smem_x = 0, smem_y = 0, smem_t = 0;
     // flags
     unsigned int* d_flags = nullptr;
@@ -427,6 +428,10 @@ struct ModelImpl : gbo_model {
         TC = 32;
         while (TC > 1 && (size_t)3 * Nz * TC * sizeof(double) > lim) TC /= 2;
         smem_t = (size_t)3 * Nz * TC * sizeof(double);
+        GBO_CUDA(cudaFuncSetAttribute(k_momentum_fused<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(fused::Smem<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_momentum_fused<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(fused::Smem<FT>)));
+        kchunk = flat ? 1 : std::min(16, Nz);
         GBO_CUDA(cudaFuncSetAttribute(k_dct_z<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_z, 1)));
         GBO_CUDA(cudaFuncSetAttribute(k_rfft_x<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_x, 1)));
         GBO_CUDA(cudaFuncSetAttribute(k_fft_y<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_y, 1)));
@@ -548,7 +553,8 @@ struct ModelImpl : gbo_model {
         StepP<FT> P = params();
         if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
             pre(G_CLOSURE);
-            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(P, nu.p);
+            k_smagorinsky_tiled<FT><<<dim3((Nx + smag::TX - 1) / smag::TX, (Ny + smag::TY - 1) / smag::TY, (Nz + smag::KT - 1) / smag::KT),
+                                      dim3(smag::TX, smag::TY), sizeof(smag::Smem<FT>), stream>>>(P, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;
@@ -578,10 +584,26 @@ struct ModelImpl : gbo_model {
         P.gamma = FT(gamma);
         P.zeta = FT(zeta);
         P.first = first;
-        pre(G_MOMENTUM);
-        k_momentum<FT><<<grd(), blk(), 0, stream>>>(P);
-        check_launch();
-        for (int n = 0; n < ntr; ++n) {
+        // momentum and tracer 0 in one march; further tracers use the per-point tracer kernel
+        StepP<FT> M0 = P;
+        const dim3 fgrid((Nx + fused::TX - 1) / fused::TX, (Ny + fused::TY - 1) / fused::TY, (Nz + kchunk - 1) / kchunk);
+        const dim3 fblock(fused::TX, fused::TY);
+        if (ntr > 0) {
+            M0.c = c[0].p;
+            M0.co = cs[0].p;
+            M0.Gc = Gc[0].p;
+            M0.kap = kap.empty() ? nullptr : kap[0].p;
+            M0.flux_top = FT(desc.tracer_flux_top[0]);
+            M0.flux_bot = FT(desc.tracer_flux_bottom[0]);
+            pre(G_MOMENTUM);
+            k_momentum_fused<FT, true><<<fgrid, fblock, sizeof(fused::Smem<FT>), stream>>>(M0, kchunk);
+            check_launch();
+        } else {
+            pre(G_MOMENTUM);
+            k_momentum_fused<FT, false><<<fgrid, fblock, sizeof(fused::Smem<FT>), stream>>>(M0, kchunk);
+            check_launch();
+        }
+        for (int n = 1; n < ntr; ++n) {
             StepP<FT> Q = P;
             Q.c = c[n].p;
             Q.co = cs[n].p;

@@ -168,8 +168,9 @@ def algorithmic_bytes(group, size, s, closure=True, ntr=1):
     """Algorithmic bytes per launch (compulsory reads + writes of whole fields)."""
     N = float(np.prod(size))
     per = {
-        # u,v,w (+νₑ, pHY′) read, U* and Gⁿ written; G⁻ read on 2 of 3 stages
-        "k_momentum": (3 + (1 if closure else 0) + 1) + 3 + 3 + 3 * 2.0 / 3,
+        # fused momentum + tracer 0: u,v,w,c (+νₑ, pHY′) read, U*, c*, Gⁿ written;
+        # G⁻ read on 2 of 3 stages
+        "k_momentum": (3 + ntr + (1 if closure else 0) + 1) + (3 + ntr) * 2 + (3 + ntr) * 2.0 / 3,
         "k_tracer": (3 + 1 + (1 if closure else 0)) + 2 + 2.0 / 3,
         "k_closure": 4 + 1,
         "k_hydrostatic": 2,

@@ -90,6 +90,104 @@ __device__ Cx<FT>* block_fft(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, i
     return A;
 }
 
+
+// Compile-time-length variant of block_fft: the radix sequence, spans and
+// twiddle strides are constants, so the index arithmetic reduces to shifts,
+// multiplies and masks and the stage loop unrolls.
+struct CPlan {
+    int nrad;
+    int rad[GBO_MAX_RADICES];
+};
+__host__ __device__ constexpr CPlan cplan(int n) {
+    CPlan p{0, {}};
+    int m = n;
+    while (m % 4 == 0) { p.rad[p.nrad++] = 4; m /= 4; }
+    while (m % 2 == 0) { p.rad[p.nrad++] = 2; m /= 2; }
+    while (m % 3 == 0) { p.rad[p.nrad++] = 3; m /= 3; }
+    while (m % 5 == 0) { p.rad[p.nrad++] = 5; m /= 5; }
+    return p;
+}
+
+template <typename FT, int N, int R, int NS>
+__device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* __restrict__ B, int L, int sign,
+                                          const Cx<FT>* __restrict__ tw) {
+    constexpr int NR = N / R;
+    constexpr int TWS = N / (NS * R);
+    for (int t = threadIdx.x; t < L * NR; t += blockDim.x) {
+        const int line = t / NR;
+        const int jj = t - line * NR;
+        const int kk = jj % NS;
+        const Cx<FT>* x = A + line * N;
+        Cx<FT>* y = B + line * N;
+        Cx<FT> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            Cx<FT> a = x[jj + r * NR];
+            if (r > 0) {
+                Cx<FT> wv = tw[kk * r * TWS];
+                if (sign > 0) wv.im = -wv.im;
+                a = a * wv;
+            }
+            v[r] = a;
+        }
+        Cx<FT> V[R];
+        if (R == 2) {
+            V[0] = v[0] + v[1];
+            V[1] = v[0] - v[1];
+        } else if (R == 4) {
+            Cx<FT> s02 = v[0] + v[2], d02 = v[0] - v[2], s13 = v[1] + v[3], d13 = v[1] - v[3];
+            Cx<FT> jd13 = sign < 0 ? cx(d13.im, -d13.re) : cx(-d13.im, d13.re);
+            V[0] = s02 + s13;
+            V[1] = d02 + jd13;
+            V[2] = s02 - s13;
+            V[3] = d02 - jd13;
+        } else {
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                Cx<FT> acc = v[0];
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    Cx<FT> wv = tw[((q * r) % R) * NR];
+                    if (sign > 0) wv.im = -wv.im;
+                    acc = acc + v[r] * wv;
+                }
+                V[q] = acc;
+            }
+        }
+        const int idxD = (jj / NS) * NS * R + kk;
+#pragma unroll
+        for (int q = 0; q < R; ++q) y[idxD + q * NS] = V[q];
+    }
+    __syncthreads();
+}
+
+template <typename FT, int N, int S, int NS>
+struct FFTStages {
+    static __device__ __forceinline__ Cx<FT>* run(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
+        constexpr CPlan p = cplan(N);
+        if constexpr (S >= p.nrad) {
+            return A;
+        } else {
+            constexpr int R = p.rad[S];
+            fft_stage<FT, N, R, NS>(A, B, L, sign, tw);
+            return FFTStages<FT, N, S + 1, NS * R>::run(B, A, L, sign, tw);
+        }
+    }
+};
+
+template <typename FT, int N>
+__device__ __forceinline__ Cx<FT>* block_fft_n(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
+    return FFTStages<FT, N, 0, 1>::run(A, B, L, sign, tw);
+}
+
+// Dispatch helper: a kernel template parameter NC (0 = runtime length) selects
+// the compile-time engine when the length matches.
+template <typename FT, int NC>
+__device__ __forceinline__ Cx<FT>* fft_any(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* tw) {
+    if constexpr (NC > 0) return block_fft_n<FT, NC>(A, B, L, sign, tw);
+    else return block_fft<FT>(A, B, L, pl, sign, tw);
+}
+
 // Makhoul reordering: the element x(k) of a length-N real sequence goes to v[dest(k)]
 // (index_permutations.jl:18-20 restated: even samples first, odd samples reversed).
 GBO_D int makhoul_dest(int k, int N) { return (k & 1) ? N - 1 - (k >> 1) : (k >> 1); }
@@ -118,7 +216,7 @@ struct PassP {
 // Z pass: DCT-II (forward) / its inverse along z, in place on the real buffer.
 // Block: ZT consecutive x columns at one y, all Nz levels.
 // ---------------------------------------------------------------------------
-template <typename FT>
+template <typename FT, int NC>
 __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
     extern __shared__ unsigned char smem_raw[];
     const int N = P.Nz;
@@ -137,7 +235,7 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
             if (c & 1) d.im = x; else d.re = x;
         }
         __syncthreads();
-        Cx<FT>* R = block_fft<FT>(A, B, L, P.pz, -1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.pz, -1, P.tw_z);
         Cx<FT>* O = (R == A) ? B : A;
         FT* out = reinterpret_cast<FT*>(O);  // ZT x N reals staged for coalesced stores
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
@@ -173,7 +271,7 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
             A[l * N + k] = cx(Va.re - Vb.im, Va.im + Vb.re);
         }
         __syncthreads();
-        Cx<FT>* R = block_fft<FT>(A, B, L, P.pz, +1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.pz, +1, P.tw_z);
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
             int c = t % ZT, k = t / ZT;
             Cx<FT> z = R[(c >> 1) * N + makhoul_dest(k, N)];
@@ -187,7 +285,7 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
 // Forward: rb (Nx reals per line) -> cb (Nh = Nx/2+1 complex per line).
 // Inverse: cb -> rb.  Block: XL lines (consecutive (j, k) pairs).
 // ---------------------------------------------------------------------------
-template <typename FT>
+template <typename FT, int NC>
 __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
     extern __shared__ unsigned char smem_raw[];
     const int M = P.Nx / 2, Nh = P.Nh;
@@ -201,7 +299,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
         FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) As[t] = src[t];
         __syncthreads();
-        Cx<FT>* R = block_fft<FT>(A, B, L, P.px_half, -1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.px_half, -1, P.tw_xh);
         Cx<FT>* dst = P.cb + (size_t)line0 * Nh;
         for (int t = threadIdx.x; t < L * Nh; t += blockDim.x) {
             int l = t / Nh, k = t - l * Nh;
@@ -225,7 +323,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
             A[l * M + k] = cx(e.re - o.im, e.im + o.re);  // e + i o
         }
         __syncthreads();
-        Cx<FT>* R = block_fft<FT>(A, B, L, P.px_half, +1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.px_half, +1, P.tw_xh);
         FT* dst = P.rb + (size_t)line0 * P.Nx;
         const FT* Rs = reinterpret_cast<const FT*>(R);
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) dst[t] = Rs[t];
@@ -237,7 +335,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
 // inverse FFT along y.  Block: YT consecutive kx at one kz, all Ny.
 // mode: 0 = forward+divide+inverse, 1 = forward only, 2 = inverse only.
 // ---------------------------------------------------------------------------
-template <typename FT>
+template <typename FT, int NC>
 __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     extern __shared__ unsigned char smem_raw[];
     const int N = P.Ny, Nh = P.Nh;
@@ -252,7 +350,7 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     }
     __syncthreads();
     Cx<FT>* R = A;
-    if (mode != 2) R = block_fft<FT>(A, B, YT, P.py, -1, P.tw_y);
+    if (mode != 2) R = fft_any<FT, NC>(A, B, YT, P.py, -1, P.tw_y);
     if (mode == 0) {
         for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
             int c = t / N, ky = t - c * N;
@@ -269,7 +367,7 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     }
     if (mode != 1) {
         Cx<FT>* O = (R == A) ? B : A;
-        R = block_fft<FT>(R, O, YT, P.py, +1, P.tw_y);
+        R = fft_any<FT, NC>(R, O, YT, P.py, +1, P.tw_y);
     }
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
         int c = t % YT, ky = t / YT;
@@ -348,3 +446,13 @@ __global__ void k_thomas_z(PassP<FT> P, ThomasP T, int TC) {
     for (int k = 0; k < Nz; ++k)
         col[stride * k] = cx((FT)((pre[k * TC + c] - mre) * T.scale), (FT)((pim[k * TC + c] - mim) * T.scale));
 }
+
+// ---------------------------------------------------------------------------
+// Host-side launchers (instantiated in gbo_fft.cu): pick the compile-time
+// engine for the common lengths and the runtime engine otherwise.
+// ---------------------------------------------------------------------------
+template <typename FT> void launch_dct_z(const PassP<FT>& P, int inverse, int ZT, size_t smem, cudaStream_t st);
+template <typename FT> void launch_rfft_x(const PassP<FT>& P, int inverse, int XL, size_t smem, cudaStream_t st);
+template <typename FT> void launch_fft_y(const PassP<FT>& P, int mode, int YT, size_t smem, cudaStream_t st);
+template <typename FT> void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, int TC, size_t smem, cudaStream_t st);
+template <typename FT> cudaError_t fft_set_smem(size_t smem_z, size_t smem_x, size_t smem_y, size_t smem_t);

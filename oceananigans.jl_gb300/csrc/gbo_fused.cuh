@@ -20,6 +20,7 @@ namespace fused {
 constexpr int TX = 32, TY = 8, H = 3;
 constexpr int PX = TX + 2 * H, PY = TY + 2 * H, PS = PX * PY;
 constexpr int NT = TX * TY;
+constexpr int EPT = (PS + NT - 1) / NT;  // plane elements loaded per thread
 
 GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + H); }
 
@@ -28,57 +29,90 @@ GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + H); }
 enum { A_UU = 0, A_UV, A_UW, C_11, C_12, C_13, A_CX, Q_CX, NWX };   // west faces
 enum { A_VU = 0, A_VV, A_VW, C_22, C_12N, C_23, A_CY, Q_CY, NSY };  // south faces
 
+// Plane rings: a level's plane stays in its slot while it is in use and the
+// next level's planes are prefetched asynchronously into the free slots.
 template <typename FT>
 struct Smem {
-    FT U[2][PS], V[2][PS], W[2][PS];  // u, v at levels k-1, k; w at faces k, k+1
-    FT NU[3][PS];                      // νₑ at k-1, k, k+1
-    FT PH[PS];                         // pHY′ at k
-    FT CC[PS];                         // tracer at k
-    FT KP[2][PS];                      // AMD tracer diffusivity κₑ at k, k+1
+    FT U[3][PS], V[3][PS], W[3][PS];  // u, v: levels k-1, k (+k+1 in flight); w: faces k, k+1 (+k+2)
+    FT NU[4][PS];                      // νₑ: k-1, k, k+1 (+k+2)
+    FT PH[2][PS];                      // pHY′: k (+k+1)
+    FT CC[2][PS];                      // tracer: k (+k+1)
+    FT KP[3][PS];                      // AMD κₑ: k, k+1 (+k+2)
     FT WX[NWX][TY][TX + 1];
     FT SY[NSY][TY + 1][TX];
 };
 
-// Load one plane of a Center-in-z field (level k) with halo H into smem.
+// Asynchronous 4/8-byte global -> shared copy; src_bytes = 0 writes zero.
 template <typename FT>
-GBO_D void load_plane_c(FT* dst, const FT* src, const GridP<FT>& g, int i0, int j0, int k, int tid) {
-    CFld<FT> f = cfld(src, g);
-    for (int e = tid; e < PS; e += NT) {
-        int px = e % PX, py = e / PX;
-        dst[e] = f(i0 + px - H, j0 + py - H, k);
-    }
+GBO_D void cp_async(FT* dst, const FT* src, bool zero) {
+    unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(FT) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(zero ? 0 : 4));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(zero ? 0 : 8));
 }
+GBO_D void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+GBO_D void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Per-thread plane-load plan: offsets (within one z-level) of the wrapped
+// (i, j) points this thread copies; identical for every level.
+struct PlanePlan {
+    int off[EPT];
+    int n;
+};
 template <typename FT>
-GBO_D void load_plane_w(FT* dst, const FT* src, const GridP<FT>& g, int i0, int j0, int k, int tid) {
-    WFld<FT> f = wfld(src, g);
-    for (int e = tid; e < PS; e += NT) {
-        int px = e % PX, py = e / PX;
-        dst[e] = f(i0 + px - H, j0 + py - H, k);
+GBO_D PlanePlan make_plan(const GridP<FT>& g, int i0, int j0, int tid) {
+    PlanePlan p;
+    p.n = 0;
+#pragma unroll
+    for (int m = 0; m < EPT; ++m) {
+        int e = tid + m * NT;
+        p.off[m] = 0;
+        if (e < PS) {
+            int px = e % PX, py = e / PX;
+            int gi = wrapi(i0 + px - H, g.Nx), gj = wrapi(j0 + py - H, g.Ny);
+            p.off[m] = gi + g.Nx * gj;
+            p.n = m + 1;
+        }
     }
+    return p;
+}
+// Level to read for a Center-in-z field at level k (mirror one halo layer; -1 = zero)
+GBO_D int zsrc_c(int k, int Nz, int flatz) {
+    if (flatz) return 0;
+    if (k < -1 || k > Nz) return -1;
+    return k < 0 ? 0 : (k >= Nz ? Nz - 1 : k);
+}
+// Level for w at face k (walls and beyond read zero)
+GBO_D int zsrc_w(int k, int Nz) { return (k <= 0 || k >= Nz) ? -1 : k; }
+
+template <typename FT>
+GBO_D void issue_plane(FT* dst, const FT* src, int zl, size_t plane, const PlanePlan& pp, int tid) {
+    const FT* base = src + (zl < 0 ? 0 : (size_t)zl * plane);
+#pragma unroll
+    for (int m = 0; m < EPT; ++m)
+        if (m < pp.n) cp_async(dst + tid + m * NT, base + pp.off[m], zl < 0);
 }
 
-// Advective momentum flux through a face: ũ from four area-weighted velocities
-// (Centered(4)), ψ reconstructed by WENO5 from six values.
 template <typename FT>
 GBO_D FT flux_c4_w5(FT a0, FT a1, FT a2, FT a3, const FT* S) {
     FT ut = cen4<FT>(a0, a1, a2, a3);
     return ut * weno5<FT>(S, bias_left(ut));
 }
 
-// Per-thread column state: register windows of u, v (levels k-3..k+3) and
-// w (faces k-2..k+3), plus the values carried from the level below.
 template <typename FT>
 struct Col {
     FT uc[7], vc[7], wc[6];
-    FT fWu, fWv, fWw;     // advective fluxes through the bottom faces (u, v at face k; w at centre k-1)
-    FT t13, t23, t33;     // closure fluxes τ13(k), τ23(k) at face k and τ33 at centre k-1
-    FT cc[7];             // tracer window (levels k-3..k+3)
-    FT fWc, qzc;          // tracer advective / diffusive fluxes through the bottom face k
+    FT fWu, fWv, fWw;
+    FT t13, t23, t33;
+    FT cc[7];
+    FT fWc, qzc;
 };
 
 }  // namespace fused
 
-// TR: also advance one tracer (P.c -> P.co, P.Gc) in the same march.
+// Column-marching fused kernel (see the file header).  TR: also advance one tracer
+// (P.c -> P.co, P.Gc) in the same march.
 template <typename FT, bool TR>
 __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk) {
     using namespace fused;
@@ -91,50 +125,60 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
     const int i = i0 + tx, j = j0 + ty;
     const int kb = blockIdx.z * kchunk, ke = min(g.Nz, kb + kchunk);
     const bool closure = P.closure != CL_NONE;
+    const bool amd = P.closure == CL_AMD;
     const bool inside = (i < g.Nx) && (j < g.Ny);
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Ng = cfld(P.nu, g);
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g);
     WFld<FT> Wg = wfld(P.w, g);
-    const int Nz = g.Nz;
+    const int Nz = g.Nz, fz = g.flatz;
     const FT Az = M.Az();
     const size_t plane = (size_t)g.Nx * g.Ny;
+    const PlanePlan pp = make_plan(g, i0, j0, tid);
+    const int ii = i % g.Nx, jj = j % g.Ny;
 
-    // ---- prologue: planes and windows for the first level kb ----
-    int cu = 0;  // ring slot of level k for U/V (k-1 in 1-cu); W: slot of face k in cw, k+1 in 1-cw
-    load_plane_c(s.U[1 - cu], P.u, g, i0, j0, kb - 1, tid);
-    load_plane_c(s.V[1 - cu], P.v, g, i0, j0, kb - 1, tid);
-    load_plane_c(s.U[cu], P.u, g, i0, j0, kb, tid);
-    load_plane_c(s.V[cu], P.v, g, i0, j0, kb, tid);
-    int cw = 0;
-    load_plane_w(s.W[cw], P.w, g, i0, j0, kb, tid);
-    int cn = 0;  // NU slots: cn = k-1, (cn+1)%3 = k, (cn+2)%3 = k+1
+    // ring slots: U/V slot of level k = k mod 3, W slot of face k = k mod 3,
+    // NU slot of level k = k mod 4, PH/CC slot = k mod 2, KP slot = k mod 3
+    auto m3 = [](int k) { return ((k % 3) + 3) % 3; };
+    auto m4 = [](int k) { return ((k % 4) + 4) % 4; };
+    auto m2 = [](int k) { return k & 1; };
+
+    // ---- prologue: planes for level kb ----
+    issue_plane(s.U[m3(kb - 1)], P.u, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
+    issue_plane(s.V[m3(kb - 1)], P.v, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
+    issue_plane(s.U[m3(kb)], P.u, zsrc_c(kb, Nz, fz), plane, pp, tid);
+    issue_plane(s.V[m3(kb)], P.v, zsrc_c(kb, Nz, fz), plane, pp, tid);
+    if (!fz) {
+        issue_plane(s.W[m3(kb)], P.w, zsrc_w(kb, Nz), plane, pp, tid);
+        issue_plane(s.W[m3(kb + 1)], P.w, zsrc_w(kb + 1, Nz), plane, pp, tid);
+    }
     if (closure) {
-        load_plane_c(s.NU[cn], P.nu, g, i0, j0, kb - 1, tid);
-        load_plane_c(s.NU[(cn + 1) % 3], P.nu, g, i0, j0, kb, tid);
+        issue_plane(s.NU[m4(kb - 1)], P.nu, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
+        issue_plane(s.NU[m4(kb)], P.nu, zsrc_c(kb, Nz, fz), plane, pp, tid);
+        issue_plane(s.NU[m4(kb + 1)], P.nu, zsrc_c(kb + 1, Nz, fz), plane, pp, tid);
     }
+    if (P.has_phy) issue_plane(s.PH[m2(kb)], P.phy, zsrc_c(kb, Nz, fz), plane, pp, tid);
+    if (TR) issue_plane(s.CC[m2(kb)], P.c, zsrc_c(kb, Nz, fz), plane, pp, tid);
+    if (TR && amd) {
+        issue_plane(s.KP[m3(kb)], P.kap, zsrc_c(kb, Nz, fz), plane, pp, tid);
+        issue_plane(s.KP[m3(kb + 1)], P.kap, zsrc_c(kb + 1, Nz, fz), plane, pp, tid);
+    }
+    cp_async_commit();
     Col<FT> c;
-    {
-        const int ii = i % g.Nx, jj = j % g.Ny;
 #pragma unroll
-        for (int o = 0; o < 7; ++o) {
-            c.uc[o] = Ug(ii, jj, kb - 3 + o);
-            c.vc[o] = Vg(ii, jj, kb - 3 + o);
-        }
-#pragma unroll
-        for (int o = 0; o < 6; ++o) c.wc[o] = Wg(ii, jj, kb - 2 + o);
-        if (TR) {
-            CFld<FT> Cg = cfld(P.c, g);
-#pragma unroll
-            for (int o = 0; o < 7; ++o) c.cc[o] = Cg(ii, jj, kb - 3 + o);
-        }
+    for (int o = 0; o < 7; ++o) {
+        c.uc[o] = Ug(ii, jj, kb - 3 + o);
+        c.vc[o] = Vg(ii, jj, kb - 3 + o);
+        if (TR) c.cc[o] = Cg(ii, jj, kb - 3 + o);
     }
-    const bool amd = P.closure == CL_AMD;
-    int ck = 0;  // KP slot of level k (k+1 in 1-ck)
-    if (TR && amd) load_plane_c(s.KP[ck], P.kap, g, i0, j0, kb, tid);
+#pragma unroll
+    for (int o = 0; o < 6; ++o) c.wc[o] = Wg(ii, jj, kb - 2 + o);
+    const FT wm3 = Wg(ii, jj, kb - 3);
+    FT km_amd = FT(0);
+    if (TR && amd) km_amd = cfld(P.kap, g)(ii, jj, kb - 1);
+    cp_async_wait_all();
     __syncthreads();
-    // bottom fluxes at level kb (faces kb / centre kb-1), from planes (w at kb) and windows
+    // bottom fluxes at level kb (faces kb / centre kb-1)
     {
-        const FT* Wk = s.W[cw];
-        // F_Wu(i, j, kb): w̃ = C4(Az w(i-2..i+1, kb)), ψ = u(kb-3..kb+2)
+        const FT* Wk = s.W[m3(kb)];
         {
             FT wt = cen4<FT>(Az * Wk[pidx(tx - 2, ty)], Az * Wk[pidx(tx - 1, ty)], Az * Wk[pidx(tx, ty)], Az * Wk[pidx(tx + 1, ty)]);
             auto q = [&](int o) { return c.uc[3 + o]; };
@@ -145,19 +189,17 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
             auto q = [&](int o) { return c.vc[3 + o]; };
             c.fWv = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(kb + 1, Nz));
         }
-        // F_Ww at centre kb-1: reconstructions at face kb from w(kb-3..kb+2) -> window index o+2
         {
             const int kc = kb - 1;
-            FT wm3 = Wg(i % g.Nx, j % g.Ny, kb - 3);
             auto qs = [&](int o) { return Az * (o == -3 ? wm3 : c.wc[2 + o]); };
             FT wt = symm<FT>(qs, zlev_symm_center(kc + 1, Nz));
             auto qb = [&](int o) { return o == -3 ? wm3 : c.wc[2 + o]; };
             c.fWw = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(kc + 1, Nz));
         }
+        c.t13 = c.t23 = c.t33 = FT(0);
         if (closure) {
-            const FT* Nm = s.NU[cn];
-            const FT* Nk = s.NU[(cn + 1) % 3];
-            // τ13 at (i, kb): -2 ν_fcf S13, S13 = ½(∂z u + ∂x w)
+            const FT* Nm = s.NU[m4(kb - 1)];
+            const FT* Nk = s.NU[m4(kb)];
             FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(tx - 1, ty)] + Nm[pidx(tx, ty)]) + FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]));
             FT dzu = (c.uc[3] - c.uc[2]) * M.rdzf(kb);
             FT dxw = (Wk[pidx(tx, ty)] - Wk[pidx(tx - 1, ty)]) * g.rdx;
@@ -166,25 +208,16 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
             FT dzv = (c.vc[3] - c.vc[2]) * M.rdzf(kb);
             FT dyw = (Wk[pidx(tx, ty)] - Wk[pidx(tx, ty - 1)]) * g.rdy;
             c.t23 = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
-            // τ33 at centre kb-1: -2 ν(kb-1) (w(kb) - w(kb-1)) / Δzᶜ(kb-1)
             c.t33 = FT(-2) * (Nm[pidx(tx, ty)] * ((c.wc[2] - c.wc[1]) * M.rdzc(kb - 1)));
         }
         if (TR) {
-            // tracer flux through face kb: Az w(kb) ψ(kb), diffusive -κᶜᶜᶠ ∂z c
             FT wk = c.wc[2];
             auto q = [&](int o) { return c.cc[3 + o]; };
             c.fWc = Az * wk * biased<FT>(q, bias_left(wk), zlev_biased_face(kb + 1, Nz));
             c.qzc = FT(0);
             if (closure) {
-                FT km, kk;
-                if (amd) {
-                    CFld<FT> Kg = cfld(P.kap, g);
-                    km = Kg(i % g.Nx, j % g.Ny, kb - 1);
-                    kk = s.KP[ck][pidx(tx, ty)];
-                } else {
-                    km = s.NU[cn][pidx(tx, ty)];
-                    kk = s.NU[(cn + 1) % 3][pidx(tx, ty)];
-                }
+                FT km = amd ? km_amd : s.NU[m4(kb - 1)][pidx(tx, ty)];
+                FT kk = amd ? s.KP[m3(kb)][pidx(tx, ty)] : s.NU[m4(kb)][pidx(tx, ty)];
                 FT kz = amd ? FT(0.5) * (km + kk) : FT(0.5) * (km + kk) / P.Pr;
                 c.qzc = -kz * ((c.cc[3] - c.cc[2]) * M.rdzf(kb));
             }
@@ -192,38 +225,54 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
     }
 
     for (int k = kb; k < ke; ++k) {
-        // ---- load the planes new at this level: w(k+1), ν(k+1), pHY(k) ----
-        __syncthreads();
-        load_plane_w(s.W[1 - cw], P.w, g, i0, j0, k + 1, tid);
-        if (closure) load_plane_c(s.NU[(cn + 2) % 3], P.nu, g, i0, j0, k + 1, tid);
-        if (P.has_phy) load_plane_c(s.PH, P.phy, g, i0, j0, k, tid);
-        if (TR) load_plane_c(s.CC, P.c, g, i0, j0, k, tid);
-        if (TR && amd) load_plane_c(s.KP[1 - ck], P.kap, g, i0, j0, k + 1, tid);
-        __syncthreads();
-        const FT* Uk = s.U[cu];
-        const FT* Um = s.U[1 - cu];
-        const FT* Vk = s.V[cu];
-        const FT* Vm = s.V[1 - cu];
-        const FT* Wk = s.W[cw];
-        const FT* Wp = s.W[1 - cw];
-        const FT* Nm = s.NU[cn];
-        const FT* Nk = s.NU[(cn + 1) % 3];
-        const FT* Np = s.NU[(cn + 2) % 3];
+        // ---- prefetch the planes first needed at level k+1 (free ring slots) ----
+        const int kn = k + 1;
+        if (kn < ke) {
+            issue_plane(s.U[m3(kn)], P.u, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            issue_plane(s.V[m3(kn)], P.v, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            if (!fz) issue_plane(s.W[m3(kn + 1)], P.w, zsrc_w(kn + 1, Nz), plane, pp, tid);
+            if (closure) issue_plane(s.NU[m4(kn + 1)], P.nu, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
+            if (P.has_phy) issue_plane(s.PH[m2(kn)], P.phy, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            if (TR) issue_plane(s.CC[m2(kn)], P.c, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            if (TR && amd) issue_plane(s.KP[m3(kn + 1)], P.kap, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
+        }
+        cp_async_commit();
+        // ---- early loads: window tops for the next level, G⁻ of this level ----
+        const FT un = Ug(ii, jj, k + 4), vn = Vg(ii, jj, k + 4), wn = Wg(ii, jj, k + 4);
+        const FT cnext = TR ? Cg(ii, jj, k + 4) : FT(0);
+        const size_t idx = ii + (size_t)g.Nx * jj + plane * k;
+        FT Gum = FT(0), Gvm = FT(0), Gwm = FT(0), Gcm = FT(0);
+        if (!P.first && inside) {
+            Gum = P.Gu[idx];
+            Gvm = P.Gv[idx];
+            if (!fz && k > 0) Gwm = P.Gw[idx];
+            if (TR) Gcm = P.Gc[idx];
+        }
+        const FT* Uk = s.U[m3(k)];
+        const FT* Um = s.U[m3(k - 1)];
+        const FT* Vk = s.V[m3(k)];
+        const FT* Vm = s.V[m3(k - 1)];
+        const FT* Wk = s.W[m3(k)];
+        const FT* Wp = s.W[m3(k + 1)];
+        const FT* Nm = s.NU[m4(k - 1)];
+        const FT* Nk = s.NU[m4(k)];
+        const FT* Np = s.NU[m4(k + 1)];
+        const FT* PHk = s.PH[m2(k)];
+        const FT* CCk = s.CC[m2(k)];
+        const FT* Kk = s.KP[m3(k)];
+        const FT* Kp = s.KP[m3(k + 1)];
         const FT Ax = M.Ax(k), Ay = M.Ay(k);
 
         // ---- west / south face quantities of this thread (and the tile edges) ----
         auto west = [&](int x, int y, bool own) {
-            // F_Uu at centre i-1: ũ = C4(Ax u(i-2..i+1)), ψ = u(i-3..i+2)
             FT S[6];
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x - 3 + o, y)];
             s.WX[A_UU][y][x] = flux_c4_w5<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4], S);
-            // F_Uv at (f,f,c): ũ = C4(Ax u(i, j-2..j+1)), ψ = v(i-3..i+2, j)
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x - 3 + o, y)];
             s.WX[A_UV][y][x] = flux_c4_w5<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)], S);
-            // F_Uw at (f,c,f) level k: ũ = symm_z(Ax u(i, k-2..k+1)), ψ = w(i-3..i+2, k)
-            {
+            if (!fz) {
                 FT uz[4];
                 if (own) {
 #pragma unroll
@@ -239,7 +288,6 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 s.WX[A_UW][y][x] = ut * weno5<FT>(S, bias_left(ut));
             }
             if (closure) {
-                // τ11 at centre i-1, τ12 at (i, j), τ13 at (i, k)
                 FT s11 = (Uk[pidx(x, y)] - Uk[pidx(x - 1, y)]) * g.rdx;
                 s.WX[C_11][y][x] = FT(-2) * (Nk[pidx(x - 1, y)] * s11);
                 FT nffc = FT(0.5) * (FT(0.5) * (Nk[pidx(x - 1, y - 1)] + Nk[pidx(x, y - 1)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
@@ -248,7 +296,7 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 s.WX[C_12][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
                 if (own) {
                     s.WX[C_13][y][x] = c.t13;
-                } else {
+                } else if (!fz) {
                     FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(x - 1, y)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
                     FT dzu = (Uk[pidx(x, y)] - Um[pidx(x, y)]) * M.rdzf(k);
                     FT dxw = (Wk[pidx(x, y)] - Wk[pidx(x - 1, y)]) * g.rdx;
@@ -256,30 +304,26 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 }
             }
             if (TR) {
-                // F_cx = Ax u(i) ψ(i),  q_x = -κᶠᶜᶜ ∂x c
                 FT ut = Uk[pidx(x, y)];
 #pragma unroll
-                for (int o = 0; o < 6; ++o) S[o] = s.CC[pidx(x - 3 + o, y)];
+                for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x - 3 + o, y)];
                 s.WX[A_CX][y][x] = Ax * ut * weno5<FT>(S, bias_left(ut));
                 if (closure) {
-                    const FT* K = amd ? s.KP[ck] : Nk;
+                    const FT* K = amd ? Kk : Nk;
                     FT kx = amd ? FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) / P.Pr;
-                    s.WX[Q_CX][y][x] = -kx * ((s.CC[pidx(x, y)] - s.CC[pidx(x - 1, y)]) * g.rdx);
+                    s.WX[Q_CX][y][x] = -kx * ((CCk[pidx(x, y)] - CCk[pidx(x - 1, y)]) * g.rdx);
                 }
             }
         };
         auto south = [&](int x, int y, bool own) {
             FT S[6];
-            // F_Vu at (f,f,c): ṽ = C4(Ay v(i-2..i+1, j)), ψ = u(i, j-3..j+2)
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x, y - 3 + o)];
             s.SY[A_VU][y][x] = flux_c4_w5<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)], S);
-            // F_Vv at centre j-1: ṽ = C4(Ay v(j-2..j+1)), ψ = v(j-3..j+2)
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x, y - 3 + o)];
             s.SY[A_VV][y][x] = flux_c4_w5<FT>(Ay * S[1], Ay * S[2], Ay * S[3], Ay * S[4], S);
-            // F_Vw at (c,f,f) level k
-            {
+            if (!fz) {
                 FT vz[4];
                 if (own) {
 #pragma unroll
@@ -303,7 +347,7 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 s.SY[C_12N][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
                 if (own) {
                     s.SY[C_23][y][x] = c.t23;
-                } else {
+                } else if (!fz) {
                     FT ncff = FT(0.5) * (FT(0.5) * (Nm[pidx(x, y - 1)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x, y - 1)] + Nk[pidx(x, y)]));
                     FT dzv = (Vk[pidx(x, y)] - Vm[pidx(x, y)]) * M.rdzf(k);
                     FT dyw = (Wk[pidx(x, y)] - Wk[pidx(x, y - 1)]) * g.rdy;
@@ -313,12 +357,12 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
             if (TR) {
                 FT vt = Vk[pidx(x, y)];
 #pragma unroll
-                for (int o = 0; o < 6; ++o) S[o] = s.CC[pidx(x, y - 3 + o)];
+                for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x, y - 3 + o)];
                 s.SY[A_CY][y][x] = Ay * vt * weno5<FT>(S, bias_left(vt));
                 if (closure) {
-                    const FT* K = amd ? s.KP[ck] : Nk;
+                    const FT* K = amd ? Kk : Nk;
                     FT ky = amd ? FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) / P.Pr;
-                    s.SY[Q_CY][y][x] = -ky * ((s.CC[pidx(x, y)] - s.CC[pidx(x, y - 1)]) * g.rdy);
+                    s.SY[Q_CY][y][x] = -ky * ((CCk[pidx(x, y)] - CCk[pidx(x, y - 1)]) * g.rdy);
                 }
             }
         };
@@ -328,58 +372,57 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
         if (ty == 1) south(tx, TY, false);             // north row of the tile
 
         // ---- top-face quantities (carried to the next level) ----
-        FT fWu_t, fWv_t, fWw_t, t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);
-        {
-            FT wt = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
-            auto q = [&](int o) { return c.uc[4 + o]; };
-            fWu_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
-        }
-        {
-            FT wt = cen4<FT>(Az * Wp[pidx(tx, ty - 2)], Az * Wp[pidx(tx, ty - 1)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx, ty + 1)]);
-            auto q = [&](int o) { return c.vc[4 + o]; };
-            fWv_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
-        }
-        {
-            // F_Ww at centre k: face k+1 reconstructions from w(k-2..k+3) = wc[0..5]
-            auto qs = [&](int o) { return Az * c.wc[3 + o]; };
-            FT wt = symm<FT>(qs, zlev_symm_center(k + 1, Nz));
-            auto qb = [&](int o) { return c.wc[3 + o]; };
-            fWw_t = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, Nz));
-        }
-        if (closure) {
-            FT nfcf = FT(0.5) * (FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx - 1, ty)] + Np[pidx(tx, ty)]));
-            FT dzu = (c.uc[4] - c.uc[3]) * M.rdzf(k + 1);
-            FT dxw = (Wp[pidx(tx, ty)] - Wp[pidx(tx - 1, ty)]) * g.rdx;
-            t13_t = FT(-2) * (nfcf * (FT(0.5) * (dzu + dxw)));
-            FT ncff = FT(0.5) * (FT(0.5) * (Nk[pidx(tx, ty - 1)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx, ty - 1)] + Np[pidx(tx, ty)]));
-            FT dzv = (c.vc[4] - c.vc[3]) * M.rdzf(k + 1);
-            FT dyw = (Wp[pidx(tx, ty)] - Wp[pidx(tx, ty - 1)]) * g.rdy;
-            t23_t = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
-            t33_t = FT(-2) * (Nk[pidx(tx, ty)] * ((c.wc[3] - c.wc[2]) * M.rdzc(k)));
-        }
+        FT fWu_t = FT(0), fWv_t = FT(0), fWw_t = FT(0), t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);
         FT fWc_t = FT(0), qzc_t = FT(0);
-        if (TR) {
-            FT wt = c.wc[3];  // w at face k+1
-            auto q = [&](int o) { return c.cc[4 + o]; };
-            fWc_t = Az * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+        if (!fz) {
+            {
+                FT wt = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
+                auto q = [&](int o) { return c.uc[4 + o]; };
+                fWu_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+            }
+            {
+                FT wt = cen4<FT>(Az * Wp[pidx(tx, ty - 2)], Az * Wp[pidx(tx, ty - 1)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx, ty + 1)]);
+                auto q = [&](int o) { return c.vc[4 + o]; };
+                fWv_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+            }
+            {
+                auto qs = [&](int o) { return Az * c.wc[3 + o]; };
+                FT wt = symm<FT>(qs, zlev_symm_center(k + 1, Nz));
+                auto qb = [&](int o) { return c.wc[3 + o]; };
+                fWw_t = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, Nz));
+            }
             if (closure) {
-                FT kk = amd ? s.KP[ck][pidx(tx, ty)] : Nk[pidx(tx, ty)];
-                FT kp = amd ? s.KP[1 - ck][pidx(tx, ty)] : Np[pidx(tx, ty)];
-                FT kz = amd ? FT(0.5) * (kk + kp) : FT(0.5) * (kk + kp) / P.Pr;
-                qzc_t = -kz * ((c.cc[4] - c.cc[3]) * M.rdzf(k + 1));
+                FT nfcf = FT(0.5) * (FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx - 1, ty)] + Np[pidx(tx, ty)]));
+                FT dzu = (c.uc[4] - c.uc[3]) * M.rdzf(k + 1);
+                FT dxw = (Wp[pidx(tx, ty)] - Wp[pidx(tx - 1, ty)]) * g.rdx;
+                t13_t = FT(-2) * (nfcf * (FT(0.5) * (dzu + dxw)));
+                FT ncff = FT(0.5) * (FT(0.5) * (Nk[pidx(tx, ty - 1)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx, ty - 1)] + Np[pidx(tx, ty)]));
+                FT dzv = (c.vc[4] - c.vc[3]) * M.rdzf(k + 1);
+                FT dyw = (Wp[pidx(tx, ty)] - Wp[pidx(tx, ty - 1)]) * g.rdy;
+                t23_t = FT(-2) * (ncff * (FT(0.5) * (dzv + dyw)));
+                t33_t = FT(-2) * (Nk[pidx(tx, ty)] * ((c.wc[3] - c.wc[2]) * M.rdzc(k)));
+            }
+            if (TR) {
+                FT wt = c.wc[3];
+                auto q = [&](int o) { return c.cc[4 + o]; };
+                fWc_t = Az * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+                if (closure) {
+                    FT kk = amd ? Kk[pidx(tx, ty)] : Nk[pidx(tx, ty)];
+                    FT kp = amd ? Kp[pidx(tx, ty)] : Np[pidx(tx, ty)];
+                    FT kz = amd ? FT(0.5) * (kk + kp) : FT(0.5) * (kk + kp) / P.Pr;
+                    qzc_t = -kz * ((c.cc[4] - c.cc[3]) * M.rdzf(k + 1));
+                }
             }
         }
         __syncthreads();
 
         // ---- tendencies and predictor ----
         if (inside) {
-            const size_t idx = i + (size_t)g.Nx * j + plane * k;
             const FT rVc = M.rVc(k);
-            // u
             {
                 FT dx_ = s.WX[A_UU][ty][tx + 1] - s.WX[A_UU][ty][tx];
                 FT dy_ = s.SY[A_VU][ty + 1][tx] - s.SY[A_VU][ty][tx];
-                FT dz_ = g.flatz ? FT(0) : (fWu_t - c.fWu);
+                FT dz_ = fz ? FT(0) : (fWu_t - c.fWu);
                 FT G = -(rVc * (dx_ + dy_ + dz_));
                 if (P.has_cor) {
                     FT ixy = FT(0.5) * (FT(0.5) * (Ay * Vk[pidx(tx - 1, ty)] + Ay * Vk[pidx(tx, ty)]) +
@@ -387,22 +430,20 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                     FT xfu = -P.f * ixy * (FT(1) / Ay);
                     G = G - xfu;
                 }
-                if (P.has_phy) G = G - (s.PH[pidx(tx, ty)] - s.PH[pidx(tx - 1, ty)]) * g.rdx;
+                if (P.has_phy) G = G - (PHk[pidx(tx, ty)] - PHk[pidx(tx - 1, ty)]) * g.rdx;
                 if (closure) {
                     FT cdx = Ax * s.WX[C_11][ty][tx + 1] - Ax * s.WX[C_11][ty][tx];
                     FT cdy = Ay * s.SY[C_12N][ty + 1][tx] - Ay * s.SY[C_12N][ty][tx];
-                    FT cdz = g.flatz ? FT(0) : (Az * t13_t - Az * c.t13);
+                    FT cdz = fz ? FT(0) : (Az * t13_t - Az * c.t13);
                     G = G - rVc * (cdx + cdy + cdz);
                 }
-                FT Gm = P.first ? FT(0) : P.Gu[idx];
                 P.Gu[idx] = G;
-                P.uo[idx] = rk3_update(Uk[pidx(tx, ty)], G, Gm, P);
+                P.uo[idx] = rk3_update(Uk[pidx(tx, ty)], G, Gum, P);
             }
-            // v
             {
                 FT dx_ = s.WX[A_UV][ty][tx + 1] - s.WX[A_UV][ty][tx];
                 FT dy_ = s.SY[A_VV][ty + 1][tx] - s.SY[A_VV][ty][tx];
-                FT dz_ = g.flatz ? FT(0) : (fWv_t - c.fWv);
+                FT dz_ = fz ? FT(0) : (fWv_t - c.fWv);
                 FT G = -(rVc * (dx_ + dy_ + dz_));
                 if (P.has_cor) {
                     FT ixy = FT(0.5) * (FT(0.5) * (Ax * Uk[pidx(tx, ty - 1)] + Ax * Uk[pidx(tx + 1, ty - 1)]) +
@@ -410,19 +451,17 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                     FT yfu = P.f * ixy * (FT(1) / Ax);
                     G = G - yfu;
                 }
-                if (P.has_phy) G = G - (s.PH[pidx(tx, ty)] - s.PH[pidx(tx, ty - 1)]) * g.rdy;
+                if (P.has_phy) G = G - (PHk[pidx(tx, ty)] - PHk[pidx(tx, ty - 1)]) * g.rdy;
                 if (closure) {
                     FT cdx = Ax * s.WX[C_12][ty][tx + 1] - Ax * s.WX[C_12][ty][tx];
                     FT cdy = Ay * s.SY[C_22][ty + 1][tx] - Ay * s.SY[C_22][ty][tx];
-                    FT cdz = g.flatz ? FT(0) : (Az * t23_t - Az * c.t23);
+                    FT cdz = fz ? FT(0) : (Az * t23_t - Az * c.t23);
                     G = G - rVc * (cdx + cdy + cdz);
                 }
-                FT Gm = P.first ? FT(0) : P.Gv[idx];
                 P.Gv[idx] = G;
-                P.vo[idx] = rk3_update(Vk[pidx(tx, ty)], G, Gm, P);
+                P.vo[idx] = rk3_update(Vk[pidx(tx, ty)], G, Gvm, P);
             }
-            // w (face k; k = 0 is the wall)
-            if (!g.flatz) {
+            if (!fz) {
                 if (k == 0) {
                     P.wo[idx] = FT(0);
                 } else {
@@ -438,65 +477,48 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                         FT cdz = Az * t33_t - Az * c.t33;
                         G = G - rVf * (cdx + cdy + cdz);
                     }
-                    FT Gm = P.first ? FT(0) : P.Gw[idx];
                     P.Gw[idx] = G;
-                    P.wo[idx] = rk3_update(Wk[pidx(tx, ty)], G, Gm, P);
+                    P.wo[idx] = rk3_update(Wk[pidx(tx, ty)], G, Gwm, P);
                 }
             }
+            if (TR) {
+                FT dx_ = s.WX[A_CX][ty][tx + 1] - s.WX[A_CX][ty][tx];
+                FT dy_ = s.SY[A_CY][ty + 1][tx] - s.SY[A_CY][ty][tx];
+                FT dz_ = fz ? FT(0) : (fWc_t - c.fWc);
+                FT G = -(rVc * (dx_ + dy_ + dz_));
+                if (closure) {
+                    FT cdx = Ax * s.WX[Q_CX][ty][tx + 1] - Ax * s.WX[Q_CX][ty][tx];
+                    FT cdy = Ay * s.SY[Q_CY][ty + 1][tx] - Ay * s.SY[Q_CY][ty][tx];
+                    FT cdz = fz ? FT(0) : (Az * qzc_t - Az * c.qzc);
+                    G = G - rVc * (cdx + cdy + cdz);
+                }
+                if (!fz) {
+                    if (k == Nz - 1 && P.flux_top != FT(0)) G -= P.flux_top * Az / (Az * M.dzc(k));
+                    if (k == 0 && P.flux_bot != FT(0)) G += P.flux_bot * Az / (Az * M.dzc(k));
+                }
+                P.Gc[idx] = G;
+                P.co[idx] = rk3_update(CCk[pidx(tx, ty)], G, Gcm, P);
+            }
         }
 
-        if (TR && inside) {
-            const size_t idx = i + (size_t)g.Nx * j + plane * k;
-            const FT rVc = M.rVc(k);
-            FT dx_ = s.WX[A_CX][ty][tx + 1] - s.WX[A_CX][ty][tx];
-            FT dy_ = s.SY[A_CY][ty + 1][tx] - s.SY[A_CY][ty][tx];
-            FT dz_ = g.flatz ? FT(0) : (fWc_t - c.fWc);
-            FT G = -(rVc * (dx_ + dy_ + dz_));
-            if (closure) {
-                FT cdx = Ax * s.WX[Q_CX][ty][tx + 1] - Ax * s.WX[Q_CX][ty][tx];
-                FT cdy = Ay * s.SY[Q_CY][ty + 1][tx] - Ay * s.SY[Q_CY][ty][tx];
-                FT cdz = g.flatz ? FT(0) : (Az * qzc_t - Az * c.qzc);
-                G = G - rVc * (cdx + cdy + cdz);
-            }
-            if (!g.flatz) {
-                if (k == Nz - 1 && P.flux_top != FT(0)) G -= P.flux_top * Az / (Az * M.dzc(k));
-                if (k == 0 && P.flux_bot != FT(0)) G += P.flux_bot * Az / (Az * M.dzc(k));
-            }
-            FT Gm = P.first ? FT(0) : P.Gc[idx];
-            P.Gc[idx] = G;
-            P.co[idx] = rk3_update(s.CC[pidx(tx, ty)], G, Gm, P);
-        }
-
-        // ---- advance: carry top -> bottom, slide windows and rotate plane slots ----
+        // ---- advance: carry top -> bottom, slide the windows ----
         c.fWu = fWu_t; c.fWv = fWv_t; c.fWw = fWw_t;
         c.t13 = t13_t; c.t23 = t23_t; c.t33 = t33_t;
         c.fWc = fWc_t; c.qzc = qzc_t;
-        {
-            const int ii = i % g.Nx, jj = j % g.Ny;
 #pragma unroll
-            for (int o = 0; o < 6; ++o) { c.uc[o] = c.uc[o + 1]; c.vc[o] = c.vc[o + 1]; }
-            c.uc[6] = Ug(ii, jj, k + 4);
-            c.vc[6] = Vg(ii, jj, k + 4);
+        for (int o = 0; o < 6; ++o) { c.uc[o] = c.uc[o + 1]; c.vc[o] = c.vc[o + 1]; }
+        c.uc[6] = un;
+        c.vc[6] = vn;
 #pragma unroll
-            for (int o = 0; o < 5; ++o) c.wc[o] = c.wc[o + 1];
-            c.wc[5] = Wg(ii, jj, k + 4);
-            if (TR) {
-                CFld<FT> Cg = cfld(P.c, g);
+        for (int o = 0; o < 5; ++o) c.wc[o] = c.wc[o + 1];
+        c.wc[5] = wn;
+        if (TR) {
 #pragma unroll
-                for (int o = 0; o < 6; ++o) c.cc[o] = c.cc[o + 1];
-                c.cc[6] = Cg(ii, jj, k + 4);
-            }
+            for (int o = 0; o < 6; ++o) c.cc[o] = c.cc[o + 1];
+            c.cc[6] = cnext;
         }
+        cp_async_wait_all();
         __syncthreads();
-        // u, v at level k+1 into the slot of level k-1
-        if (k + 1 < ke) {
-            load_plane_c(s.U[1 - cu], P.u, g, i0, j0, k + 1, tid);
-            load_plane_c(s.V[1 - cu], P.v, g, i0, j0, k + 1, tid);
-        }
-        cu = 1 - cu;
-        cw = 1 - cw;
-        cn = (cn + 1) % 3;
-        ck = 1 - ck;
     }
 }
 

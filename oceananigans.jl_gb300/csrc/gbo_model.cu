@@ -432,10 +432,7 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         GBO_CUDA(cudaFuncSetAttribute(k_momentum_fused<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(fused::Smem<FT>)));
         kchunk = flat ? 1 : std::min(16, Nz);
-        GBO_CUDA(cudaFuncSetAttribute(k_dct_z<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_z, 1)));
-        GBO_CUDA(cudaFuncSetAttribute(k_rfft_x<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_x, 1)));
-        GBO_CUDA(cudaFuncSetAttribute(k_fft_y<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_y, 1)));
-        GBO_CUDA(cudaFuncSetAttribute(k_thomas_z<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_t, 1)));
+        GBO_CUDA(fft_set_smem<FT>(smem_z, smem_x, smem_y, smem_t));
     }
 
     // ------------------------------------------------------------------
@@ -493,40 +490,40 @@ struct ModelImpl : gbo_model {
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
             pre(G_FFT_X);
             pre(G_FFT_X);
-        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
+        launch_rfft_x<FT>(pp, 0, XL, smem_x, stream);
             check_launch();
             pre(G_FFT_Y);
-            k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 1, YT);
+            launch_fft_y<FT>(pp, 1, YT, smem_y, stream);
             check_launch();
             pre(G_THOMAS);
-            k_thomas_z<FT><<<dim3((Nh + TC - 1) / TC, Ny), TC, smem_t, stream>>>(pp, tp, TC);
+            launch_thomas_z<FT>(pp, tp, TC, smem_t, stream);
             check_launch();
             pre(G_FFT_Y);
-            k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 2, YT);
+            launch_fft_y<FT>(pp, 2, YT, smem_y, stream);
             check_launch();
             pre(G_FFT_X);
             pre(G_FFT_X);
-        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
+        launch_rfft_x<FT>(pp, 1, XL, smem_x, stream);
             check_launch();
             return;
         }
         if (!flat) {
             pre(G_DCT_Z);
-            k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 0, ZT);
+            launch_dct_z<FT>(pp, 0, ZT, smem_z, stream);
             check_launch();
         }
         pre(G_FFT_X);
-        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 0, XL);
+        launch_rfft_x<FT>(pp, 0, XL, smem_x, stream);
         check_launch();
         pre(G_FFT_Y);
-        k_fft_y<FT><<<dim3((Nh + YT - 1) / YT, Nz), 256, smem_y, stream>>>(pp, 0, YT);
+        launch_fft_y<FT>(pp, 0, YT, smem_y, stream);
         check_launch();
         pre(G_FFT_X);
-        k_rfft_x<FT><<<(Ny * Nz + XL - 1) / XL, 256, smem_x, stream>>>(pp, 1, XL);
+        launch_rfft_x<FT>(pp, 1, XL, smem_x, stream);
         check_launch();
         if (!flat) {
             pre(G_DCT_Z);
-            k_dct_z<FT><<<dim3((Nx + ZT - 1) / ZT, Ny), 256, smem_z, stream>>>(pp, 1, ZT);
+            launch_dct_z<FT>(pp, 1, ZT, smem_z, stream);
             check_launch();
         }
     }

@@ -31,22 +31,25 @@ struct FFTPlan1D {
 // holding the result.  sign = -1 forward, +1 inverse (unnormalised).
 // tw[m] = exp(-2πi m / n), m = 0..n-1.
 template <typename FT>
-__device__ Cx<FT>* block_fft(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* __restrict__ tw) {
+__device__ Cx<FT>* block_fft(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* __restrict__ tw,
+                             bool il = false) {
     const int n = pl.n;
     int Ns = 1;
     for (int s = 0; s < pl.nrad; ++s) {
         const int R = pl.rad[s];
         const int nR = n / R;
         const int twstep = n / (Ns * R);
+        // element (line, m) lives at line*n + m, or at m*L + line when interleaved
+        const int es = il ? L : 1;
         for (int t = threadIdx.x; t < L * nR; t += blockDim.x) {
-            const int line = t / nR;
-            const int jj = t - line * nR;
+            const int line = il ? t % L : t / nR;
+            const int jj = il ? t / L : t - line * nR;
             const int kk = jj % Ns;
-            const Cx<FT>* x = A + line * n;
-            Cx<FT>* y = B + line * n;
+            const Cx<FT>* x = A + (il ? line : line * n);
+            Cx<FT>* y = B + (il ? line : line * n);
             Cx<FT> v[5];
             for (int r = 0; r < R; ++r) {
-                Cx<FT> a = x[jj + r * nR];
+                Cx<FT> a = x[(jj + r * nR) * es];
                 if (r > 0 && kk > 0) {
                     Cx<FT> wv = tw[(kk * r * twstep) % n];
                     if (sign > 0) wv.im = -wv.im;
@@ -79,7 +82,7 @@ __device__ Cx<FT>* block_fft(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, i
                 }
             }
             const int idxD = (jj / Ns) * Ns * R + kk;
-            for (int q = 0; q < R; ++q) y[idxD + q * Ns] = V[q];
+            for (int q = 0; q < R; ++q) y[(idxD + q * Ns) * es] = V[q];
         }
         __syncthreads();
         Cx<FT>* tmp = A;
@@ -108,21 +111,22 @@ __host__ __device__ constexpr CPlan cplan(int n) {
     return p;
 }
 
-template <typename FT, int N, int R, int NS>
+template <typename FT, int N, int R, int NS, bool IL>
 __device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* __restrict__ B, int L, int sign,
                                           const Cx<FT>* __restrict__ tw) {
     constexpr int NR = N / R;
     constexpr int TWS = N / (NS * R);
+    const int es = IL ? L : 1;
     for (int t = threadIdx.x; t < L * NR; t += blockDim.x) {
-        const int line = t / NR;
-        const int jj = t - line * NR;
+        const int line = IL ? t % L : t / NR;
+        const int jj = IL ? t / L : t - line * NR;
         const int kk = jj % NS;
-        const Cx<FT>* x = A + line * N;
-        Cx<FT>* y = B + line * N;
+        const Cx<FT>* x = A + (IL ? line : line * N);
+        Cx<FT>* y = B + (IL ? line : line * N);
         Cx<FT> v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            Cx<FT> a = x[jj + r * NR];
+            Cx<FT> a = x[(jj + r * NR) * es];
             if (r > 0) {
                 Cx<FT> wv = tw[kk * r * TWS];
                 if (sign > 0) wv.im = -wv.im;
@@ -156,12 +160,12 @@ __device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* 
         }
         const int idxD = (jj / NS) * NS * R + kk;
 #pragma unroll
-        for (int q = 0; q < R; ++q) y[idxD + q * NS] = V[q];
+        for (int q = 0; q < R; ++q) y[(idxD + q * NS) * es] = V[q];
     }
     __syncthreads();
 }
 
-template <typename FT, int N, int S, int NS>
+template <typename FT, int N, int S, int NS, bool IL>
 struct FFTStages {
     static __device__ __forceinline__ Cx<FT>* run(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
         constexpr CPlan p = cplan(N);
@@ -169,23 +173,25 @@ struct FFTStages {
             return A;
         } else {
             constexpr int R = p.rad[S];
-            fft_stage<FT, N, R, NS>(A, B, L, sign, tw);
-            return FFTStages<FT, N, S + 1, NS * R>::run(B, A, L, sign, tw);
+            fft_stage<FT, N, R, NS, IL>(A, B, L, sign, tw);
+            return FFTStages<FT, N, S + 1, NS * R, IL>::run(B, A, L, sign, tw);
         }
     }
 };
 
-template <typename FT, int N>
+template <typename FT, int N, bool IL>
 __device__ __forceinline__ Cx<FT>* block_fft_n(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
-    return FFTStages<FT, N, 0, 1>::run(A, B, L, sign, tw);
+    return FFTStages<FT, N, 0, 1, IL>::run(A, B, L, sign, tw);
 }
 
 // Dispatch helper: a kernel template parameter NC (0 = runtime length) selects
-// the compile-time engine when the length matches.
-template <typename FT, int NC>
+// the compile-time engine when the length matches.  IL: interleaved line layout
+// (element (line, m) at m*L + line), used where a block's lines are columns of a
+// strided axis so that loads, scatters and butterflies are bank-conflict free.
+template <typename FT, int NC, bool IL>
 __device__ __forceinline__ Cx<FT>* fft_any(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* tw) {
-    if constexpr (NC > 0) return block_fft_n<FT, NC>(A, B, L, sign, tw);
-    else return block_fft<FT>(A, B, L, pl, sign, tw);
+    if constexpr (NC > 0) return block_fft_n<FT, NC, IL>(A, B, L, sign, tw);
+    else return block_fft<FT>(A, B, L, pl, sign, tw, IL);
 }
 
 // Makhoul reordering: the element x(k) of a length-N real sequence goes to v[dest(k)]
@@ -231,16 +237,16 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
             int c = t % ZT, k = t / ZT;
             FT x = (i0 + c < P.Nx) ? col0[c + plane * k] : FT(0);
-            Cx<FT>& d = A[(c >> 1) * N + makhoul_dest(k, N)];
+            Cx<FT>& d = A[makhoul_dest(k, N) * L + (c >> 1)];
             if (c & 1) d.im = x; else d.re = x;
         }
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.pz, -1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, -1, P.tw_z);
         Cx<FT>* O = (R == A) ? B : A;
         FT* out = reinterpret_cast<FT*>(O);  // ZT x N reals staged for coalesced stores
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
-            int l = t / N, k = t - l * N;
-            Cx<FT> Zk = R[l * N + k], Zn = R[l * N + (k == 0 ? 0 : N - k)];
+            int l = t % L, k = t / L;
+            Cx<FT> Zk = R[k * L + l], Zn = R[(k == 0 ? 0 : N - k) * L + l];
             Cx<FT> w = P.tq_z[k];
             Cx<FT> s = Zk + conj(Zn), d = Zk - conj(Zn);
             Cx<FT> ws = w * s, wd = w * d;
@@ -260,7 +266,7 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
         }
         __syncthreads();
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
-            int l = t / N, k = t - l * N;
+            int l = t % L, k = t / L;
             FT Xa = in[2 * l + ZT * k], Xb = in[2 * l + 1 + ZT * k];
             FT Xan = k == 0 ? FT(0) : in[2 * l + ZT * (N - k)];
             FT Xbn = k == 0 ? FT(0) : in[2 * l + 1 + ZT * (N - k)];
@@ -268,13 +274,13 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
             // V_a = ω^{-k}(X_a[k] - i X_a[N-k]) / 2 ; V_b likewise ; Z = V_a + i V_b
             Cx<FT> Va = FT(0.5) * (w * cx(Xa, -Xan));
             Cx<FT> Vb = FT(0.5) * (w * cx(Xb, -Xbn));
-            A[l * N + k] = cx(Va.re - Vb.im, Va.im + Vb.re);
+            A[k * L + l] = cx(Va.re - Vb.im, Va.im + Vb.re);
         }
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.pz, +1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, +1, P.tw_z);
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
             int c = t % ZT, k = t / ZT;
-            Cx<FT> z = R[(c >> 1) * N + makhoul_dest(k, N)];
+            Cx<FT> z = R[makhoul_dest(k, N) * L + (c >> 1)];
             if (i0 + c < P.Nx) col0[c + plane * k] = (c & 1) ? z.im : z.re;
         }
     }
@@ -299,7 +305,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
         FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) As[t] = src[t];
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.px_half, -1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, -1, P.tw_xh);
         Cx<FT>* dst = P.cb + (size_t)line0 * Nh;
         for (int t = threadIdx.x; t < L * Nh; t += blockDim.x) {
             int l = t / Nh, k = t - l * Nh;
@@ -323,7 +329,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
             A[l * M + k] = cx(e.re - o.im, e.im + o.re);  // e + i o
         }
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC>(A, B, L, P.px_half, +1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, +1, P.tw_xh);
         FT* dst = P.rb + (size_t)line0 * P.Nx;
         const FT* Rs = reinterpret_cast<const FT*>(R);
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) dst[t] = Rs[t];
@@ -346,14 +352,14 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     Cx<FT>* base = P.cb + kx0 + (size_t)Nh * N * kz;
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
         int c = t % YT, ky = t / YT;
-        A[c * N + ky] = (kx0 + c < Nh) ? base[c + (size_t)Nh * ky] : cx(FT(0), FT(0));
+        A[ky * YT + c] = (kx0 + c < Nh) ? base[c + (size_t)Nh * ky] : cx(FT(0), FT(0));
     }
     __syncthreads();
     Cx<FT>* R = A;
-    if (mode != 2) R = fft_any<FT, NC>(A, B, YT, P.py, -1, P.tw_y);
+    if (mode != 2) R = fft_any<FT, NC, true>(A, B, YT, P.py, -1, P.tw_y);
     if (mode == 0) {
         for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
-            int c = t / N, ky = t - c * N;
+            int c = t % YT, ky = t / YT;
             int kx = kx0 + c;
             if (kx < Nh) {
                 FT lam = (P.lx[kx] + P.ly[ky]) + (P.has_z ? P.lz[kz] : FT(0));
@@ -367,11 +373,11 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     }
     if (mode != 1) {
         Cx<FT>* O = (R == A) ? B : A;
-        R = fft_any<FT, NC>(R, O, YT, P.py, +1, P.tw_y);
+        R = fft_any<FT, NC, true>(R, O, YT, P.py, +1, P.tw_y);
     }
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
         int c = t % YT, ky = t / YT;
-        if (kx0 + c < Nh) base[c + (size_t)Nh * ky] = R[c * N + ky];
+        if (kx0 + c < Nh) base[c + (size_t)Nh * ky] = R[ky * YT + c];
     }
 }
 

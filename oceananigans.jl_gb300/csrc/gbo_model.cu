@@ -486,7 +486,6 @@ struct ModelImpl : gbo_model {
 
     // Spectral solve of ∇²ϕ = rb in place (rb holds the source on entry, ϕ on exit).
     void poisson_solve() {
-        const int Nh = Nx / 2 + 1;
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
             pre(G_FFT_X);
             pre(G_FFT_X);

@@ -52,10 +52,31 @@ __global__ void k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws,
     Met<FT> M(g);
     const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
     FT pc = P(i, j, k) - phi_shift;
-    u[idx] = us[idx] - (pc - (P(i - 1, j, k) - phi_shift)) * g.rdx;
-    v[idx] = vs[idx] - (pc - (P(i, j - 1, k) - phi_shift)) * g.rdy;
-    if (!g.flatz) w[idx] = ws[idx] - (pc - (P(i, j, k - 1) - phi_shift)) * M.rdzf(k);
+    // ∂ operators are conditional on an immersed grid (conditional_differences.jl:15-43)
+    FT dx_ = cond_zero(g, i - 1, j, k, i, j, k) ? FT(0) : (pc - (P(i - 1, j, k) - phi_shift));
+    FT dy_ = cond_zero(g, i, j - 1, k, i, j, k) ? FT(0) : (pc - (P(i, j - 1, k) - phi_shift));
+    u[idx] = us[idx] - dx_ * g.rdx;
+    v[idx] = vs[idx] - dy_ * g.rdy;
+    if (!g.flatz) {
+        FT dz_ = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (pc - (P(i, j, k - 1) - phi_shift));
+        w[idx] = ws[idx] - dz_ * M.rdzf(k);
+    }
     p[idx] = pc * rdtau;
+}
+
+// mask_immersed_field! (mask_immersed_field.jl:65-77): zero on the immersed periphery
+// of each field's location.  which: bit 0 u, bit 1 v, bit 2 w, bit 3 tracer c.
+template <typename FT>
+__global__ void k_mask(GridP<FT> g, FT* u, FT* v, FT* w, FT* c, int which) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= g.Nx || j >= g.Ny) return;
+    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+    if ((which & 1) && imm_periph(g, i, j, k, true, false, false)) u[idx] = FT(0);
+    if ((which & 2) && imm_periph(g, i, j, k, false, true, false)) v[idx] = FT(0);
+    if ((which & 4) && !g.flatz && imm_periph(g, i, j, k, false, false, true)) w[idx] = FT(0);
+    if ((which & 8) && imm_periph(g, i, j, k, false, false, false)) c[idx] = FT(0);
 }
 
 template <typename FT>
@@ -81,6 +102,160 @@ __global__ void k_nan_check(const FT* __restrict__ a, size_t n, unsigned int* fl
     bool bad = false;
     for (; t < n; t += stride) bad |= !isfinite(a[t]);
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flags, GBO_FLAG_NAN);
+}
+
+
+// ===========================================================================
+// Conjugate-gradient Poisson solver on an immersed grid
+// (src/Solvers/conjugate_gradient_poisson_solver.jl:38-211;
+//  src/Solvers/conjugate_gradient_solver.jl:177-284).  Dot products and norms
+// accumulate in FP64; scalars live in device memory (CGS slots below).
+// ===========================================================================
+// scalar slots: ρ of even / odd iterations, p·q, Σx and Σr over active cells, ‖V⁻¹r‖², active cells
+enum { CG_RHO0 = 0, CG_RHO1, CG_PQ, CG_SX, CG_SR, CG_NORM2, CG_NACT, CG_NSLOTS };
+
+GBO_D double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+// block-reduce one or two doubles and add them to device scalars
+GBO_D void block_add(double a, double* da, double b = 0.0, double* db = nullptr) {
+    __shared__ double sa[32], sb[32];
+    int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+    int wid = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+    int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) { sa[wid] = a; sb[wid] = b; }
+    __syncthreads();
+    if (wid == 0) {
+        a = lane < nw ? sa[lane] : 0.0;
+        b = lane < nw ? sb[lane] : 0.0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (lane == 0) {
+            atomicAdd(da, a);
+            if (db) atomicAdd(db, b);
+        }
+    }
+}
+
+// q = V∇²x with differences set to zero across faces touching immersed cells
+// (_symmetric_laplacian_operator!, conjugate_gradient_poisson_solver.jl:62-79 with
+// conditional_differences.jl:15-43).  Optionally accumulates Σ p·q.
+template <typename FT>
+__global__ void k_cg_laplacian(GridP<FT> g, const FT* __restrict__ x, FT* __restrict__ q, double* dot_pq) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    double acc = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        CFld<FT> X = cfld(x, g);
+        Met<FT> M(g);
+        FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
+        auto fx = [&](int ii) { return cond_zero(g, ii - 1, j, k, ii, j, k) ? FT(0) : Ax * ((X(ii, j, k) - X(ii - 1, j, k)) * g.rdx); };
+        auto fy = [&](int jj) { return cond_zero(g, i, jj - 1, k, i, jj, k) ? FT(0) : Ay * ((X(i, jj, k) - X(i, jj - 1, k)) * g.rdy); };
+        auto fz = [&](int kk) {
+            if (g.flatz) return FT(0);
+            return cond_zero(g, i, j, kk - 1, i, j, kk) ? FT(0) : Az * ((X(i, j, kk) - X(i, j, kk - 1)) * M.rdzf(kk));
+        };
+        FT val = (fx(i + 1) - fx(i)) + (fy(j + 1) - fy(j)) + (fz(k + 1) - fz(k));
+        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        q[idx] = val;
+        if (dot_pq) acc = (double)x[idx] * (double)val;
+    }
+    if (dot_pq) block_add(acc, dot_pq);
+}
+
+// elementwise helpers over N values (1-D grid-stride)
+template <typename FT>
+__global__ void k_cg_init(const FT* __restrict__ b, const FT* __restrict__ q, FT* __restrict__ r, size_t n) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) r[t] = b[t] - q[t];
+}
+template <typename FT>
+__global__ void k_cg_scale(const FT* __restrict__ a, FT* __restrict__ out, FT s, size_t n) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) out[t] = a[t] * s;
+}
+// ‖V⁻¹ r‖² (VolumeInverseNorm) and the preconditioner right-hand side V⁻¹ r, times
+// Δzᶜ for the Fourier-tridiagonal preconditioner (its solve! applies set_source_term!,
+// fourier_tridiagonal_poisson_solver.jl:231-281)
+template <typename FT>
+__global__ void k_cg_vinv(GridP<FT> g, const FT* __restrict__ r, FT* __restrict__ out, double* norm2, int dz_scale) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    double acc = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        Met<FT> M(g);
+        FT s = r[idx] * M.rVc(k);
+        if (out) out[idx] = dz_scale ? s * M.dzc(k) : s;
+        acc = (double)s * (double)s;
+    }
+    if (norm2) block_add(acc, norm2);
+}
+template <typename FT>
+__global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, size_t n, double* out) {
+    double acc = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        acc += (double)a[t] * (double)b[t];
+    block_add(acc, out);
+}
+// p = z (first iteration) or z + (ρ/ρ_prev) p (conjugate_gradient_solver.jl:246-263)
+template <typename FT>
+__global__ void k_cg_update_p(const FT* __restrict__ z, FT* __restrict__ p, const double* rho, const double* rho_prev,
+                              int first, size_t n) {
+    const FT beta = first ? FT(0) : FT(*rho / *rho_prev);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        p[t] = first ? z[t] : z[t] + beta * p[t];
+}
+// x += α p, r -= α q with α = ρ / (p·q); accumulates the active-cell sums of x and r
+template <typename FT>
+__global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, const FT* __restrict__ p,
+                               const FT* __restrict__ q, const double* rho, double* s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    double ax = 0.0, ar = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        const FT alpha = FT(*rho / s[CG_PQ]);
+        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        FT xv = x[idx] + alpha * p[idx];
+        FT rv = r[idx] - alpha * q[idx];
+        x[idx] = xv;
+        r[idx] = rv;
+        if (!inactive_cell(g, i, j, k)) { ax = xv; ar = rv; }
+    }
+    block_add(ax, s + CG_SX, ar, s + CG_SR);
+}
+// zero-mean gauge over active cells, immersed cells zeroed (enforce_zero_mean_gauge!,
+// conjugate_gradient_poisson_solver.jl:81-96); accumulates ‖V⁻¹ r‖²
+template <typename FT>
+__global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, double* s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    double acc = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        const FT mx = FT(s[CG_SX] / s[CG_NACT]), mr = FT(s[CG_SR] / s[CG_NACT]);
+        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        const FT act = inactive_cell(g, i, j, k) ? FT(0) : FT(1);
+        x[idx] = (x[idx] - mx) * act;
+        FT rv = (r[idx] - mr) * act;
+        r[idx] = rv;
+        FT sv = rv * Met<FT>(g).rVc(k);
+        acc = (double)sv * (double)sv;
+    }
+    block_add(acc, s + CG_NORM2);
+}
+// number of active cells (for the gauge means)
+template <typename FT>
+__global__ void k_cg_count(GridP<FT> g, double* s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    double a = (i < g.Nx && j < g.Ny && !inactive_cell(g, i, j, k)) ? 1.0 : 0.0;
+    block_add(a, s + CG_NACT);
 }
 
 // ===========================================================================
@@ -246,10 +421,10 @@ struct gbo_model {
 };
 
 enum { G_MOMENTUM = 0, G_TRACER, G_CLOSURE, G_HYDROSTATIC, G_SOURCE, G_DCT_Z, G_FFT_X, G_FFT_Y, G_THOMAS,
-       G_CORRECT, G_COPY, G_NAN, GROUPS };
+       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, GROUPS };
 const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", "k_hydrostatic", "k_source",
                                          "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
-                                         "k_nan_check"};
+                                         "k_nan_check", "k_mask", "k_cg"};
 
 namespace {
 
@@ -292,6 +467,13 @@ struct ModelImpl : gbo_model {
     // Poisson solver
     DBuf<FT> rb, lx, ly, lz;
     DBuf<C> cb, tw_xh, tw_x, tw_y, tw_z, tq_z;
+    // immersed boundary and conjugate-gradient solver
+    bool ibg = false, cg = false;
+    int precond_solver = GBO_SOLVER_FFT;  // spectral solver of the underlying grid
+    DBuf<FT> cg_b, cg_r, cg_q, cg_d, cg_x;
+    DBuf<double> cg_s;
+    double* h_cgs = nullptr;
+    int cg_status = GBO_OK;
     PassP<FT> pp{};
     ThomasP tp{};
     int ZT = 32, XL = 8, YT = 16, TC = 16;
@@ -307,8 +489,11 @@ struct ModelImpl : gbo_model {
 
     ~ModelImpl() override {
         if (graph) cudaGraphExecDestroy(graph);
-        for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz})
+        for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz,
+                            &cg_b, &cg_r, &cg_q, &cg_d, &cg_x})
             b->free_();
+        cg_s.free_();
+        if (h_cgs) cudaFreeHost(h_cgs);
         for (auto* vec : {&c, &cs, &Gc, &kap})
             for (auto& b : *vec) b.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_kbot.free_();
@@ -367,7 +552,12 @@ struct ModelImpl : gbo_model {
             }
             t_kbot.upload(kb);
             gp.kbot = t_kbot.p;
+            ibg = true;
         }
+        cg = md->pressure_solver == GBO_SOLVER_CONJUGATE_GRADIENT;
+        // the FFT preconditioner is the spectral solver of the underlying grid
+        // (conjugate_gradient_poisson_solver.jl:141-147): Fourier-tridiagonal when z is stretched
+        precond_solver = gd->z_faces ? GBO_SOLVER_FOURIER_TRIDIAGONAL : GBO_SOLVER_FFT;
         // fields
         for (DBuf<FT>* b : {&u, &v, &us, &vs, &Gu, &Gv, &p, &rb}) b->alloc(N);
         if (!flat) { w.alloc(N); ws.alloc(N); Gw.alloc(N); }
@@ -383,6 +573,16 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaMemset(d_flags, 0, sizeof(unsigned int)));
         GBO_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned int)));
         init_poisson(Lx, Ly);
+        if (cg) {
+            for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_x}) b->alloc(N);
+            cg_s.alloc(CG_NSLOTS);
+            GBO_CUDA(cudaMallocHost(&h_cgs, CG_NSLOTS * sizeof(double)));
+            k_cg_count<FT><<<grd(), blk(), 0, stream>>>(gp, cg_s.p);
+            GBO_CUDA(cudaGetLastError());
+            GBO_CUDA(cudaStreamSynchronize(stream));
+            // the iteration count decides on the host after each iteration: no graph
+            use_graph = false;
+        }
     }
 
     void init_poisson(double Lx, double Ly) {
@@ -484,12 +684,12 @@ struct ModelImpl : gbo_model {
         return P;
     }
 
-    // Spectral solve of ∇²ϕ = rb in place (rb holds the source on entry, ϕ on exit).
-    void poisson_solve() {
-        if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
+    // Spectral solve of ∇²ϕ = rb in place (rb holds the source on entry, ϕ on exit)
+    // with the FFT or the Fourier-tridiagonal solver.
+    void poisson_solve(int solver) {
+        if (solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
             pre(G_FFT_X);
-            pre(G_FFT_X);
-        launch_rfft_x<FT>(pp, 0, XL, smem_x, stream);
+            launch_rfft_x<FT>(pp, 0, XL, smem_x, stream);
             check_launch();
             pre(G_FFT_Y);
             launch_fft_y<FT>(pp, 1, YT, smem_y, stream);
@@ -501,8 +701,7 @@ struct ModelImpl : gbo_model {
             launch_fft_y<FT>(pp, 2, YT, smem_y, stream);
             check_launch();
             pre(G_FFT_X);
-            pre(G_FFT_X);
-        launch_rfft_x<FT>(pp, 1, XL, smem_x, stream);
+            launch_rfft_x<FT>(pp, 1, XL, smem_x, stream);
             check_launch();
             return;
         }
@@ -529,17 +728,107 @@ struct ModelImpl : gbo_model {
 
     // compute_pressure_correction! + make_pressure_correction! on the predictor (us, vs, ws)
     // writing the state (u, v, w) and p; in == out is allowed.
-    void project(const FT* ui, const FT* vi, const FT* wi, double dtau) {
-        int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
-        pre(G_SOURCE);
-        k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
-        check_launch();
-        poisson_solve();
+    void project(FT* ui, FT* vi, FT* wi, double dtau) {
         const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+        if (ibg) {  // mask_immersed_field! on the velocities (pressure_correction.jl:9)
+            pre(G_MASK);
+            k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, nullptr, flat ? 3 : 7);
+            check_launch();
+        }
+        const FT* phi = rb.p;
+        if (cg) {
+            cg_status = cg_solve(ui, vi, wi, std::max(eps, dtau) * (std::isfinite(dtau) ? 1.0 : 0.0));
+            phi = cg_x.p;
+        } else {
+            int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
+            pre(G_SOURCE);
+            k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
+            check_launch();
+            poisson_solve(desc.pressure_solver);
+        }
         FT rdtau = FT(1) / FT(std::max(eps, dtau));
         pre(G_CORRECT);
-        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0));
+        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, phi, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0));
         check_launch();
+    }
+
+    // Preconditioned conjugate gradient for V∇²x = V·div u* with x₀ = p·Δτ
+    // (solve_for_pressure.jl:52-72; conjugate_gradient_solver.jl:177-284).  Each
+    // iteration reads ‖V⁻¹r‖ back to the host for the stopping test.
+    int cg_solve(const FT* ui, const FT* vi, const FT* wi, double dtp) {
+        const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
+        pre(G_CG);
+        k_cg_scale<FT><<<lin, 256, 0, stream>>>(p.p, cg_x.p, FT(dtp), N);
+        check_launch();
+        pre(G_SOURCE);
+        k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, cg_b.p, SRC_CG);
+        check_launch();
+        return cg_iterate();
+    }
+
+    // solve!(x, ::ConjugateGradientSolver, b) on x = cg_x, b = cg_b
+    int cg_iterate() {
+        const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+        const double rel = desc.cg_reltol > 0 ? desc.cg_reltol : std::sqrt(eps);
+        const double abs_ = desc.cg_abstol > 0 ? desc.cg_abstol : std::sqrt(eps);
+        const int64_t maxiter = desc.cg_maxiter > 0 ? desc.cg_maxiter : (int64_t)N;
+        const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
+        double* s = cg_s.p;
+        auto read_norm = [&]() {
+            GBO_CUDA(cudaMemcpyAsync(h_cgs, s, CG_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
+            return std::sqrt(h_cgs[CG_NORM2]);
+        };
+        pre(G_CG);
+        k_cg_laplacian<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_q.p, nullptr);
+        check_launch();
+        pre(G_CG);
+        k_cg_init<FT><<<lin, 256, 0, stream>>>(cg_b.p, cg_q.p, cg_r.p, N);
+        check_launch();
+        GBO_CUDA(cudaMemsetAsync(s + CG_NORM2, 0, sizeof(double), stream));
+        pre(G_CG);
+        k_cg_vinv<FT><<<grd(), blk(), 0, stream>>>(gp, cg_r.p, nullptr, s + CG_NORM2, 0);
+        check_launch();
+        double norm = read_norm();
+        const double tol = std::max(rel * norm, abs_);
+        int64_t it = 0;
+        while (it < maxiter && norm > tol) {
+            const FT* z = cg_r.p;
+            if (desc.preconditioner == GBO_PRECOND_FFT) {
+                pre(G_CG);
+                k_cg_vinv<FT><<<grd(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, nullptr, precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL);
+                check_launch();
+                poisson_solve(precond_solver);
+                z = rb.p;
+            }
+            double* rho = s + ((it & 1) ? CG_RHO1 : CG_RHO0);
+            double* rho_prev = s + ((it & 1) ? CG_RHO0 : CG_RHO1);
+            GBO_CUDA(cudaMemsetAsync(rho, 0, sizeof(double), stream));
+            GBO_CUDA(cudaMemsetAsync(s + CG_PQ, 0, (CG_NORM2 - CG_PQ + 1) * sizeof(double), stream));
+            pre(G_CG);
+            k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, rho);
+            check_launch();
+            pre(G_CG);
+            k_cg_update_p<FT><<<lin, 256, 0, stream>>>(z, cg_d.p, rho, rho_prev, it == 0, N);
+            check_launch();
+            pre(G_CG);
+            k_cg_laplacian<FT><<<grd(), blk(), 0, stream>>>(gp, cg_d.p, cg_q.p, s + CG_PQ);
+            check_launch();
+            pre(G_CG);
+            k_cg_update_xr<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_q.p, rho, s);
+            check_launch();
+            pre(G_CG);
+            k_cg_gauge<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, s);
+            check_launch();
+            norm = read_norm();
+            ++it;
+        }
+        last_iters = (int)it;
+        if (it >= maxiter && norm > tol) {
+            err = "conjugate-gradient Poisson solver did not reach its tolerance within maxiter iterations";
+            return GBO_ERR_NOT_CONVERGED;
+        }
+        return GBO_OK;
     }
 
     // Closure fields and the hydrostatic pressure anomaly of the current state: the part
@@ -584,7 +873,14 @@ struct ModelImpl : gbo_model {
         StepP<FT> M0 = P;
         const dim3 fgrid((Nx + fused::TX - 1) / fused::TX, (Ny + fused::TY - 1) / fused::TY, (Nz + kchunk - 1) / kchunk);
         const dim3 fblock(fused::TX, fused::TY);
-        if (ntr > 0) {
+        int tracer0 = 1;
+        if (ibg) {
+            // the column-marching kernel has no immersed-boundary logic: per-point kernels
+            pre(G_MOMENTUM);
+            k_momentum<FT><<<grd(), blk(), 0, stream>>>(P);
+            check_launch();
+            tracer0 = 0;
+        } else if (ntr > 0) {
             M0.c = c[0].p;
             M0.co = cs[0].p;
             M0.Gc = Gc[0].p;
@@ -599,7 +895,7 @@ struct ModelImpl : gbo_model {
             k_momentum_fused<FT, false><<<fgrid, fblock, sizeof(fused::Smem<FT>), stream>>>(M0, kchunk);
             check_launch();
         }
-        for (int n = 1; n < ntr; ++n) {
+        for (int n = tracer0; n < ntr; ++n) {
             StepP<FT> Q = P;
             Q.c = c[n].p;
             Q.co = cs[n].p;
@@ -620,7 +916,18 @@ struct ModelImpl : gbo_model {
             k_copy<FT><<<std::min<size_t>((N + 255) / 256, 4096), 256, 0, stream>>>(cs[n].p, c[n].p, N);
             check_launch();
         }
+        mask_tracers();
         auxiliaries();
+    }
+
+    // mask_immersed_field!(model.tracers) (update_nonhydrostatic_model_state.jl:25)
+    void mask_tracers() {
+        if (!ibg) return;
+        for (int n = 0; n < ntr; ++n) {
+            pre(G_MASK);
+            k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, nullptr, nullptr, nullptr, c[n].p, 8);
+            check_launch();
+        }
     }
 
     void full_step(double dt) {
@@ -632,6 +939,7 @@ struct ModelImpl : gbo_model {
 
     int step(double dt, int nsteps) override {
         if (nsteps <= 0) return GBO_OK;
+        cg_status = GBO_OK;
         if (use_graph) {
             if (!graph || graph_dt != dt) {
                 if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
@@ -649,7 +957,12 @@ struct ModelImpl : gbo_model {
             for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
             launches += graph_launches_per_step * nsteps;
         } else {
-            for (int s = 0; s < nsteps; ++s) full_step(dt);
+            int worst = GBO_OK;
+            for (int s = 0; s < nsteps; ++s) {
+                full_step(dt);
+                if (cg_status != GBO_OK) worst = cg_status;
+            }
+            cg_status = worst;
         }
         for (int s = 0; s < nsteps; ++s) {
             // clock: tⁿ⁺¹ = tⁿ + Δt computed a priori (runge_kutta_3.jl:122,160-161)
@@ -659,7 +972,8 @@ struct ModelImpl : gbo_model {
         pre(G_NAN);
         k_nan_check<FT><<<std::min<size_t>((N + 255) / 256, 1024), 256, 0, stream>>>(u.p, N, d_flags);
         check_launch();
-        return sync();
+        int rc = sync();
+        return rc != GBO_OK ? rc : cg_status;
     }
 
     int timed_steps(double dt, int nsteps, double* ms, int nmax) override {
@@ -758,9 +1072,18 @@ struct ModelImpl : gbo_model {
     }
 
     int set_finalize(int enforce) override {
+        // set_nonhydrostatic_model.jl:59-73: mask tracers and velocities, then project
+        cg_status = GBO_OK;
+        mask_tracers();
+        if (ibg) {
+            pre(G_MASK);
+            k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, u.p, v.p, flat ? nullptr : w.p, nullptr, flat ? 3 : 7);
+            check_launch();
+        }
         if (enforce) project(u.p, v.p, flat ? nullptr : w.p, 1.0);
         auxiliaries();
-        return sync();
+        int rc = sync();
+        return rc != GBO_OK ? rc : cg_status;
     }
 
     int device_pointer(int field, void** ptr, int64_t* n) override {
@@ -772,6 +1095,15 @@ struct ModelImpl : gbo_model {
     }
 
     int poisson_device(void* phi, const void* rhs) override {
+        if (cg) {
+            // V∇²ϕ = rhs by preconditioned CG from the initial guess in ϕ
+            GBO_CUDA(cudaMemcpyAsync(cg_x.p, phi, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+            GBO_CUDA(cudaMemcpyAsync(cg_b.p, rhs, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+            int st = cg_iterate();
+            GBO_CUDA(cudaMemcpyAsync(phi, cg_x.p, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+            int rc = sync();
+            return rc != GBO_OK ? rc : st;
+        }
         GBO_CUDA(cudaMemcpyAsync(rb.p, rhs, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
             // set_source_term!: b ← b Δzᶜ (fourier_tridiagonal_poisson_solver.jl:268-290)
@@ -779,7 +1111,7 @@ struct ModelImpl : gbo_model {
             k_scale_dzc<FT><<<grd(), blk(), 0, stream>>>(gp, rb.p);
             check_launch();
         }
-        poisson_solve();
+        poisson_solve(desc.pressure_solver);
         GBO_CUDA(cudaMemcpyAsync(phi, rb.p, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
         return sync();
     }
@@ -834,8 +1166,18 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
     if (d->pressure_solver == GBO_SOLVER_FFT && g->z_faces) return "FFTBasedPoissonSolver requires a regular grid";
     if (d->pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL && g->topology[2] != GBO_BOUNDED)
         return "FourierTridiagonalPoissonSolver requires Bounded z";
-    if (d->pressure_solver < 0 || d->pressure_solver > 1) return "pressure_solver not available";
-    if (g->bottom_height) return "ImmersedBoundaryGrid requires the conjugate-gradient solver";
+    if (d->pressure_solver < 0 || d->pressure_solver > 2) return "pressure_solver not available";
+    if (d->pressure_solver == GBO_SOLVER_CONJUGATE_GRADIENT) {
+        if (d->preconditioner == GBO_PRECOND_LEARNED) return "the learned preconditioner is not available";
+        if (d->preconditioner < 0 || d->preconditioner > 1) return "unknown preconditioner";
+        if (d->cg_reltol < 0 || d->cg_abstol < 0 || d->cg_maxiter < 0) return "CG tolerances and maxiter must be non-negative";
+    }
+    if (g->bottom_height) {
+        if (g->topology[2] != GBO_BOUNDED) return "GridFittedBottom requires Bounded z";
+        if (d->closure != GBO_CLOSURE_NONE) return "turbulence closures on an ImmersedBoundaryGrid are not implemented";
+        for (int q = 0; q < g->size[0] * g->size[1]; ++q)
+            if (std::isnan(g->bottom_height[q])) return "bottom_height must not be NaN";
+    }
     return "";
 }
 

@@ -39,12 +39,13 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         FT G = -(M.rVc(k) * (dx_ + dy_ + dz_));
         if (P.has_cor) {
             FT Ay = M.Ay(k);
-            FT ixy = FT(0.5) * (FT(0.5) * (Ay * F.v(i - 1, j, k) + Ay * F.v(i, j, k)) +
-                                FT(0.5) * (Ay * F.v(i - 1, j + 1, k) + Ay * F.v(i, j + 1, k)));
+            // masked_Ay_qᶜᶠᶜ: zero on the immersed periphery (coriolis_schemes.jl:55-58)
+            auto AyV = [&](int ii, int jj) { return imm_periph(g, ii, jj, k, false, true, false) ? FT(0) : Ay * F.v(ii, jj, k); };
+            FT ixy = FT(0.5) * (FT(0.5) * (AyV(i - 1, j) + AyV(i, j)) + FT(0.5) * (AyV(i - 1, j + 1) + AyV(i, j + 1)));
             FT xfu = -P.f * ixy * (FT(1) / Ay);
             G = G - xfu;
         }
-        if (P.has_phy) G = G - (F.phy(i, j, k) - F.phy(i - 1, j, k)) * g.rdx;
+        if (P.has_phy) G = G - (cond_zero(g, i - 1, j, k, i, j, k) ? FT(0) : (F.phy(i, j, k) - F.phy(i - 1, j, k))) * g.rdx;
         if (closure) {
             FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
             FT cdx = Ax * S.tau_ux(i, j, k) - Ax * S.tau_ux(i - 1, j, k);
@@ -64,12 +65,12 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         FT G = -(M.rVc(k) * (dx_ + dy_ + dz_));
         if (P.has_cor) {
             FT Ax = M.Ax(k);
-            FT ixy = FT(0.5) * (FT(0.5) * (Ax * F.u(i, j - 1, k) + Ax * F.u(i + 1, j - 1, k)) +
-                                FT(0.5) * (Ax * F.u(i, j, k) + Ax * F.u(i + 1, j, k)));
+            auto AxU = [&](int ii, int jj) { return imm_periph(g, ii, jj, k, true, false, false) ? FT(0) : Ax * F.u(ii, jj, k); };
+            FT ixy = FT(0.5) * (FT(0.5) * (AxU(i, j - 1) + AxU(i + 1, j - 1)) + FT(0.5) * (AxU(i, j) + AxU(i + 1, j)));
             FT yfu = P.f * ixy * (FT(1) / Ax);
             G = G - yfu;
         }
-        if (P.has_phy) G = G - (F.phy(i, j, k) - F.phy(i, j - 1, k)) * g.rdy;
+        if (P.has_phy) G = G - (cond_zero(g, i, j - 1, k, i, j, k) ? FT(0) : (F.phy(i, j, k) - F.phy(i, j - 1, k))) * g.rdy;
         if (closure) {
             FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
             FT cdx = Ax * (FT(-2) * (S.nu_ffc(i + 1, j, k) * S.S12(i + 1, j, k))) - Ax * (FT(-2) * (S.nu_ffc(i, j, k) * S.S12(i, j, k)));
@@ -117,24 +118,25 @@ __global__ void __launch_bounds__(256) k_tracer(StepP<FT> P) {
     Met<FT> M(g);
     const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
 
+    // reconstruction levels: WENO5 away from immersed nodes (and the Bounded-z buffers)
+    auto lev = [&](int d, int ii, int jj, int kk) {
+        if (g.kbot) return ibg_level(g, d, ii, jj, kk, true);
+        return d == 2 ? zlev_biased_face(kk + 1, g.Nz) : 3;
+    };
     auto Fx = [&](int ii) {
         FT ut = u(ii, j, k);
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = c(ii - 3 + o, j, k);
-        return M.Ax(k) * ut * weno5<FT>(S, bias_left(ut));
+        auto q = [&](int o) { return c(ii + o, j, k); };
+        return M.Ax(k) * ut * biased<FT>(q, bias_left(ut), lev(0, ii, j, k));
     };
     auto Fy = [&](int jj) {
         FT vt = v(i, jj, k);
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = c(i, jj - 3 + o, k);
-        return M.Ay(k) * vt * weno5<FT>(S, bias_left(vt));
+        auto q = [&](int o) { return c(i, jj + o, k); };
+        return M.Ay(k) * vt * biased<FT>(q, bias_left(vt), lev(1, i, jj, k));
     };
     auto Fz = [&](int kk) {
         FT wt = w(i, j, kk);
         auto q = [&](int o) { return c(i, j, kk + o); };
-        return M.Az() * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(kk + 1, g.Nz));
+        return M.Az() * wt * biased<FT>(q, bias_left(wt), lev(2, i, j, kk));
     };
     FT dx_ = Fx(i + 1) - Fx(i);
     FT dy_ = Fy(j + 1) - Fy(j);

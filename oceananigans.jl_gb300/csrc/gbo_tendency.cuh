@@ -35,6 +35,61 @@ struct Met {
     GBO_D FT rVf(int k) const { return FT(1) / (Az() * dzf(k)); }
 };
 
+// ---------------------------------------------------------------------------
+// Immersed boundary (GridFittedBottom): a cell is immersed when its centre is at or
+// below the bottom (grid_fitted_bottom.jl:150-158); kbot[i + Nx j] is the number of
+// immersed cells of the column.  Predicates follow src/Grids/inactive_node.jl and
+// src/ImmersedBoundaries/immersed_boundary_interface.jl.
+// ---------------------------------------------------------------------------
+template <typename FT>
+GBO_D bool imm_cell(const GridP<FT>& g, int i, int j, int k) {
+    if (!g.kbot || k < 0 || k >= g.Nz) return false;
+    return k < __ldg(g.kbot + wrapi(i, g.Nx) + (size_t)g.Nx * wrapi(j, g.Ny));
+}
+template <typename FT>
+GBO_D bool inactive_cell(const GridP<FT>& g, int i, int j, int k) {
+    return (!g.flatz && (k < 0 || k >= g.Nz)) || imm_cell(g, i, j, k);
+}
+// immersed_peripheral_node at a location with Face flags (fx, fy, fz)
+template <typename FT>
+GBO_D bool imm_periph(const GridP<FT>& g, int i, int j, int k, bool fx, bool fy, bool fz) {
+    if (!g.kbot) return false;
+    bool any_imm = false, any_out = false;
+    for (int a = 0; a <= (fx ? 1 : 0); ++a)
+        for (int b = 0; b <= (fy ? 1 : 0); ++b)
+            for (int c = 0; c <= (fz ? 1 : 0); ++c) {
+                int kk = k - c;
+                bool out = !g.flatz && (kk < 0 || kk >= g.Nz);
+                any_out |= out;
+                any_imm |= (!out) && imm_cell(g, i - a, j - b, kk);
+            }
+    return any_imm && !any_out;
+}
+// Reconstruction level near immersed nodes (immersed_advective_fluxes.jl:114-214): 3 (WENO5 /
+// Centered 4), 2 (WENO3) or 1 (Centered 2); d = direction, loc_face = Face location of the
+// interpolation index.  Out-of-domain cells count as inactive, which reproduces the wall
+// buffer rules exactly.
+template <typename FT>
+GBO_D int ibg_level(const GridP<FT>& g, int d, int i, int j, int k, bool loc_face) {
+    for (int B = 3; B >= 2; --B) {
+        int lo = loc_face ? -B : -B + 1, hi = loc_face ? B - 1 : B;
+        bool near = false;
+        for (int o = lo; o <= hi; ++o) {
+            int ii = i + (d == 0 ? o : 0), jj = j + (d == 1 ? o : 0), kk = k + (d == 2 ? o : 0);
+            bool inact = inactive_cell(g, ii, jj, kk);
+            if (!loc_face) inact = inact && inactive_cell(g, ii - (d == 0), jj - (d == 1), kk - (d == 2));
+            near |= inact;
+        }
+        if (!near) return B;
+    }
+    return 1;
+}
+// immersed-aware ∂ mask: a difference across a face is zero when either cell is immersed
+template <typename FT>
+GBO_D bool cond_zero(const GridP<FT>& g, int i0, int j0, int k0, int i1, int j1, int k1) {
+    return g.kbot && (imm_cell(g, i0, j0, k0) || imm_cell(g, i1, j1, k1));
+}
+
 GBO_D bool bias_left(float u) { return u > 0.f; }
 GBO_D bool bias_left(double u) { return u > 0.0; }
 
@@ -49,80 +104,94 @@ struct MomentumFluxes {
     GBO_D MomentumFluxes(const GridP<FT>& gg, const Fields<FT>& ff) : g(gg), F(ff), M(gg) {}
 
     // Uu at (c,c,c)
+    // levels of horizontal reconstructions (always WENO5 / C4 away from immersed nodes)
+    GBO_D int hl(int d, int i, int j, int k, bool face) const { return g.kbot ? ibg_level(g, d, i, j, k, face) : 3; }
+    GBO_D int hs(int d, int i, int j, int k, bool face) const { return hl(d, i, j, k, face) == 3 ? 3 : 1; }
+    GBO_D int zb(int i, int j, int k, bool face) const {
+        return g.kbot ? ibg_level(g, 2, i, j, k, face) : (face ? zlev_biased_face(k + 1, g.Nz) : zlev_biased_center(k + 1, g.Nz));
+    }
+    GBO_D int zs(int i, int j, int k, bool face) const {
+        return g.kbot ? (ibg_level(g, 2, i, j, k, face) == 3 ? 3 : 1) : (face ? zlev_symm_face(k + 1, g.Nz) : zlev_symm_center(k + 1, g.Nz));
+    }
+    GBO_D bool zero(int i, int j, int k, bool fx, bool fy, bool fz) const { return imm_periph(g, i, j, k, fx, fy, fz); }
+
     GBO_D FT Uu(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, false, false, false)) return FT(0);
         FT Ax = M.Ax(k);
-        FT ut = cen4<FT>(Ax * F.u(i - 1, j, k), Ax * F.u(i, j, k), Ax * F.u(i + 1, j, k), Ax * F.u(i + 2, j, k));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.u(i - 2 + o, j, k);
-        return ut * weno5<FT>(S, bias_left(ut));
+        auto qs = [&](int o) { return Ax * F.u(i + 1 + o, j, k); };
+        FT ut = symm<FT>(qs, hs(0, i, j, k, false));
+        auto qb = [&](int o) { return F.u(i + 1 + o, j, k); };
+        return ut * biased<FT>(qb, bias_left(ut), hl(0, i, j, k, false));
     }
     // Vu at (f,f,c)
     GBO_D FT Vu(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, true, true, false)) return FT(0);
         FT Ay = M.Ay(k);
-        FT vt = cen4<FT>(Ay * F.v(i - 2, j, k), Ay * F.v(i - 1, j, k), Ay * F.v(i, j, k), Ay * F.v(i + 1, j, k));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.u(i, j - 3 + o, k);
-        return vt * weno5<FT>(S, bias_left(vt));
+        auto qs = [&](int o) { return Ay * F.v(i + o, j, k); };
+        FT vt = symm<FT>(qs, hs(0, i, j, k, true));
+        auto qb = [&](int o) { return F.u(i, j + o, k); };
+        return vt * biased<FT>(qb, bias_left(vt), hl(1, i, j, k, true));
     }
     // Wu at (f,c,f)
     GBO_D FT Wu(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, true, false, true)) return FT(0);
         FT Az = M.Az();
-        FT wt = cen4<FT>(Az * F.w(i - 2, j, k), Az * F.w(i - 1, j, k), Az * F.w(i, j, k), Az * F.w(i + 1, j, k));
+        auto qs = [&](int o) { return Az * F.w(i + o, j, k); };
+        FT wt = symm<FT>(qs, hs(0, i, j, k, true));
         auto q = [&](int o) { return F.u(i, j, k + o); };
-        return wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 1, g.Nz));
+        return wt * biased<FT>(q, bias_left(wt), zb(i, j, k, true));
     }
     // Uv at (f,f,c)
     GBO_D FT Uv(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, true, true, false)) return FT(0);
         FT Ax = M.Ax(k);
-        FT ut = cen4<FT>(Ax * F.u(i, j - 2, k), Ax * F.u(i, j - 1, k), Ax * F.u(i, j, k), Ax * F.u(i, j + 1, k));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.v(i - 3 + o, j, k);
-        return ut * weno5<FT>(S, bias_left(ut));
+        auto qs = [&](int o) { return Ax * F.u(i, j + o, k); };
+        FT ut = symm<FT>(qs, hs(1, i, j, k, true));
+        auto qb = [&](int o) { return F.v(i + o, j, k); };
+        return ut * biased<FT>(qb, bias_left(ut), hl(0, i, j, k, true));
     }
     // Vv at (c,c,c)
     GBO_D FT Vv(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, false, false, false)) return FT(0);
         FT Ay = M.Ay(k);
-        FT vt = cen4<FT>(Ay * F.v(i, j - 1, k), Ay * F.v(i, j, k), Ay * F.v(i, j + 1, k), Ay * F.v(i, j + 2, k));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.v(i, j - 2 + o, k);
-        return vt * weno5<FT>(S, bias_left(vt));
+        auto qs = [&](int o) { return Ay * F.v(i, j + 1 + o, k); };
+        FT vt = symm<FT>(qs, hs(1, i, j, k, false));
+        auto qb = [&](int o) { return F.v(i, j + 1 + o, k); };
+        return vt * biased<FT>(qb, bias_left(vt), hl(1, i, j, k, false));
     }
     // Wv at (c,f,f)
     GBO_D FT Wv(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, false, true, true)) return FT(0);
         FT Az = M.Az();
-        FT wt = cen4<FT>(Az * F.w(i, j - 2, k), Az * F.w(i, j - 1, k), Az * F.w(i, j, k), Az * F.w(i, j + 1, k));
+        auto qs = [&](int o) { return Az * F.w(i, j + o, k); };
+        FT wt = symm<FT>(qs, hs(1, i, j, k, true));
         auto q = [&](int o) { return F.v(i, j, k + o); };
-        return wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 1, g.Nz));
+        return wt * biased<FT>(q, bias_left(wt), zb(i, j, k, true));
     }
     // Uw at (f,c,f)
     GBO_D FT Uw(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, true, false, true)) return FT(0);
         auto qs = [&](int o) { return M.Ax(k + o) * F.u(i, j, k + o); };
-        FT ut = symm<FT>(qs, zlev_symm_face(k + 1, g.Nz));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.w(i - 3 + o, j, k);
-        return ut * weno5<FT>(S, bias_left(ut));
+        FT ut = symm<FT>(qs, zs(i, j, k, true));
+        auto qb = [&](int o) { return F.w(i + o, j, k); };
+        return ut * biased<FT>(qb, bias_left(ut), hl(0, i, j, k, true));
     }
     // Vw at (c,f,f)
     GBO_D FT Vw(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, false, true, true)) return FT(0);
         auto qs = [&](int o) { return M.Ay(k + o) * F.v(i, j, k + o); };
-        FT vt = symm<FT>(qs, zlev_symm_face(k + 1, g.Nz));
-        FT S[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) S[o] = F.w(i, j - 3 + o, k);
-        return vt * weno5<FT>(S, bias_left(vt));
+        FT vt = symm<FT>(qs, zs(i, j, k, true));
+        auto qb = [&](int o) { return F.w(i, j + o, k); };
+        return vt * biased<FT>(qb, bias_left(vt), hl(1, i, j, k, true));
     }
     // Ww at (c,c,c) level k: reconstructions at face k+1 with centre conditions
     GBO_D FT Ww(int i, int j, int k) const {
+        if (g.kbot && zero(i, j, k, false, false, false)) return FT(0);
         FT Az = M.Az();
         auto qs = [&](int o) { return Az * F.w(i, j, k + 1 + o); };
-        FT wt = symm<FT>(qs, zlev_symm_center(k + 1, g.Nz));
+        FT wt = symm<FT>(qs, zs(i, j, k, false));
         auto qb = [&](int o) { return F.w(i, j, k + 1 + o); };
-        return wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, g.Nz));
+        return wt * biased<FT>(qb, bias_left(wt), zb(i, j, k, false));
     }
 };
 

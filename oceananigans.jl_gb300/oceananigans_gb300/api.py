@@ -14,6 +14,7 @@ invalid configurations raise ValueError (ArgumentError there).
 """
 import ctypes
 import math
+import warnings
 
 import numpy as np
 
@@ -237,8 +238,13 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
             d.tracer_flux_bottom[n] = bcs.bottom.value
     if pressure_solver is None:
         if grid.bottom_height is not None:
-            pressure_solver = ConjugateGradientPoissonSolver()
-        elif _grid_is_regular(grid):
+            # nonhydrostatic_pressure_solver(arch, ibg::IBGWithFFT, ...) (NonhydrostaticModels.jl:54-73):
+            # the spectral solver of the underlying grid, with a warning
+            warnings.warn("The FFT-based pressure_solver for NonhydrostaticModels on ImmersedBoundaryGrid is "
+                          "approximate and will probably produce velocity fields that are divergent adjacent to "
+                          "the immersed boundary; pass pressure_solver=ConjugateGradientPoissonSolver() for the "
+                          "iterative solver.")
+        if _grid_is_regular(grid):
             pressure_solver = FFTBasedPoissonSolver()
         else:
             pressure_solver = FourierTridiagonalPoissonSolver()

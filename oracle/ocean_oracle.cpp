@@ -19,6 +19,7 @@
 // the golden fixtures and analytic tests under tests/ (the Julia reference
 // cannot run in this environment; see the oracle tests' docstrings).
 #include <cmath>
+#include <cstdlib>
 #include <complex>
 #include <cstdint>
 #include <cstring>
@@ -76,6 +77,7 @@ struct Grid {
     std::vector<double> dzc_, dzf_, zf_, zc_;
     int zoff = 0;  // vector index = k + zoff
     bool immersed = false;
+    bool stretched = false;  // z faces given explicitly
     std::vector<double> zb;  // numerical bottom height per (i,j) incl. halos, (Nx+2H)*(Ny+2H)
 
     double dzC(int k) const { return dzc_[k + zoff]; }
@@ -188,7 +190,7 @@ struct Model {
     std::vector<cplx> ft_storage;
     int last_cg_iters = 0;
     // CG work arrays
-    Field cg_r, cg_p, cg_q, cg_z, cg_rhs;
+    Field cg_r, cg_p, cg_q, cg_z, cg_rhs, cg_x;
 
     int nfields() const { return 3 + ntr; }
     Field& fld(int n) { return n == 0 ? u : n == 1 ? v : n == 2 ? w : c[n - 3]; }
@@ -396,6 +398,52 @@ inline bool imm_periph_fcc(const Grid& g, int i, int j, int k) {
     return (a != b) || (a && b);  // peripheral or inactive
 }
 
+// Immersed cell strictly inside the domain (immersed_inactive_node of a Center node)
+inline bool imm_in(const Grid& g, int i, int j, int k) {
+    if (!g.immersed) return false;
+    if (!g.flatz && (k < 1 || k > g.Nz)) return false;
+    return immersed_cell(g, i, j, k);
+}
+// immersed_peripheral_node for the flux / velocity locations: a node is on the immersed
+// periphery when one of its adjacent cells is immersed and none is outside the domain
+// (immersed_boundary_interface.jl:49-63, inactive_node.jl:140-160).  fx, fy, fz = Face flags.
+inline bool imm_periph(const Grid& g, int i, int j, int k, bool fx, bool fy, bool fz) {
+    if (!g.immersed) return false;
+    bool any_imm = false, any_out = false;
+    for (int a = 0; a <= (fx ? 1 : 0); ++a)
+        for (int b = 0; b <= (fy ? 1 : 0); ++b)
+            for (int c = 0; c <= (fz ? 1 : 0); ++c) {
+                int kk = k - c;
+                bool out = !g.flatz && (kk < 1 || kk > g.Nz);
+                any_out |= out;
+                any_imm |= (!out) && immersed_cell(g, i - a, j - b, kk);
+            }
+    return any_imm && !any_out;
+}
+// inactive_node of the stencil nodes used by the immersed-aware reconstruction
+// (immersed_advective_fluxes.jl:114-152): Center nodes are inactive cells; Face nodes
+// are inactive when both adjacent cells are.
+inline bool inactive_c(const Grid& g, int i, int j, int k) { return inactive_cell(g, i, j, k); }
+// Level of a reconstruction of order 5 in direction d at index n (the face or centre index
+// passed to the interpolation, loc_face = Face location) on an immersed grid: WENO5 / WENO3 /
+// second order depending on whether the buffer's stencil nodes are all active.
+int ibg_level(const Grid& g, int d, int i, int j, int k, bool loc_face) {
+    auto node_inactive = [&](int off) {
+        int ii = i + (d == 0 ? off : 0), jj = j + (d == 1 ? off : 0), kk = k + (d == 2 ? off : 0);
+        if (loc_face) return inactive_c(g, ii, jj, kk);  // flipped to Center
+        // flipped to Face: both cells adjacent in direction d inactive
+        int ip = ii - (d == 0), jp = jj - (d == 1), kp = kk - (d == 2);
+        return inactive_c(g, ii, jj, kk) && inactive_c(g, ip, jp, kp);
+    };
+    for (int B = 3; B >= 2; --B) {
+        int lo = loc_face ? -B : -B + 1, hi = loc_face ? B - 1 : B;
+        bool near = false;
+        for (int o = lo; o <= hi && !near; ++o) near = node_inactive(o);
+        if (!near) return B;
+    }
+    return 1;
+}
+
 // ---------------------------------------------------------------------------
 // Tendencies (src/Models/NonhydrostaticModels/nonhydrostatic_tendency_kernel_functions.jl:71-302)
 // ---------------------------------------------------------------------------
@@ -427,92 +475,95 @@ struct Ctx {
     // Symmetric interpolation levels: 3 -> C4, 1 -> C2
     // ---- momentum advection ----
     // Flux Uu at (c,c,c) index (i,j,k): advective_momentum_flux_Uu (upwind_biased_advective_fluxes.jl:23-29)
+    // level of a horizontal (periodic) reconstruction: WENO5 unless near an immersed node
+    int hl(int d, int i, int j, int k, bool face) const { return g.immersed ? ibg_level(g, d, i, j, k, face) : 3; }
+    int zl_b(int k, bool face) const { return g.immersed ? ibg_level(g, 2, 0, 0, k, face) : zlevel_biased(k, Nz, face); }
+    int zl_s(int k, bool face) const { return g.immersed ? ibg_level(g, 2, 0, 0, k, face) : zlevel_symm(k, Nz, face); }
+    int zlb(int i, int j, int k, bool face) const { return g.immersed ? ibg_level(g, 2, i, j, k, face) : zlevel_biased(k, Nz, face); }
+    int zls(int i, int j, int k, bool face) const { return g.immersed ? (ibg_level(g, 2, i, j, k, face) == 3 ? 3 : 1) : zlevel_symm(k, Nz, face); }
+    int hls(int d, int i, int j, int k, bool face) const { return hl(d, i, j, k, face) == 3 ? 3 : 1; }
+
     double F_Uu(int i, int j, int k) const {
+        if (imm_periph(g, i, j, k, false, false, false)) return 0.0;
         const Field& U = m.u;
         double ut;
-        if (weno) {
-            auto q = [&](int o) { return M.Ax_c(k) * U(i + 1 + o, j, k); };
-            ut = symm_interp(q, 3);
-        } else {
-            ut = c2(M.Ax_c(k) * U(i, j, k), M.Ax_c(k) * U(i + 1, j, k));
-        }
+        // _symmetric_interpolate_xᶜᵃᵃ(i) and _biased_interpolate_xᶜᵃᵃ(i): Center location in x
+        auto q = [&](int o) { return M.Ax_c(k) * U(i + 1 + o, j, k); };
+        ut = symm_interp(q, hls(0, i, j, k, false));
         auto qb = [&](int o) { return U(i + 1 + o, j, k); };
-        double ur = weno ? biased_interp(qb, bias_left(ut), 3) : c2(qb(-1), qb(0));
+        double ur = biased_interp(qb, bias_left(ut), hl(0, i, j, k, false));
         return ut * ur;
     }
     // Vu at (f,f,c): ṽ = sym_x face i of Ay v; uᴿ = biased_y face j of u
     double F_Vu(int i, int j, int k) const {
-        double vt;
-        if (weno) { auto q = [&](int o) { return M.Ay_c(k) * m.v(i + o, j, k); }; vt = symm_interp(q, 3); }
-        else vt = c2(M.Ay_c(k) * m.v(i - 1, j, k), M.Ay_c(k) * m.v(i, j, k));
+        if (imm_periph(g, i, j, k, true, true, false)) return 0.0;
+        auto q = [&](int o) { return M.Ay_c(k) * m.v(i + o, j, k); };
+        double vt = symm_interp(q, hls(0, i, j, k, true));
         auto qb = [&](int o) { return m.u(i, j + o, k); };
-        double ur = weno ? biased_interp(qb, bias_left(vt), 3) : c2(qb(-1), qb(0));
+        double ur = biased_interp(qb, bias_left(vt), hl(1, i, j, k, true));
         return vt * ur;
     }
     // Wu at (f,c,f)
     double F_Wu(int i, int j, int k) const {
-        double wt;
-        if (weno) { auto q = [&](int o) { return M.Az() * m.w(i + o, j, k); }; wt = symm_interp(q, 3); }
-        else wt = c2(M.Az() * m.w(i - 1, j, k), M.Az() * m.w(i, j, k));
+        if (imm_periph(g, i, j, k, true, false, true)) return 0.0;
+        auto q = [&](int o) { return M.Az() * m.w(i + o, j, k); };
+        double wt = symm_interp(q, hls(0, i, j, k, true));
         auto qb = [&](int o) { return m.u(i, j, k + o); };
-        int lev = weno ? zlevel_biased(k, Nz, true) : 1;
-        double ur = biased_interp(qb, bias_left(wt), lev);
+        double ur = biased_interp(qb, bias_left(wt), zlb(i, j, k, true));
         return wt * ur;
     }
     // Uv at (f,f,c): ũ = sym_y face j of Ax u; vᴿ = biased_x face i of v
     double F_Uv(int i, int j, int k) const {
-        double ut;
-        if (weno) { auto q = [&](int o) { return M.Ax_c(k) * m.u(i, j + o, k); }; ut = symm_interp(q, 3); }
-        else ut = c2(M.Ax_c(k) * m.u(i, j - 1, k), M.Ax_c(k) * m.u(i, j, k));
+        if (imm_periph(g, i, j, k, true, true, false)) return 0.0;
+        auto q = [&](int o) { return M.Ax_c(k) * m.u(i, j + o, k); };
+        double ut = symm_interp(q, hls(1, i, j, k, true));
         auto qb = [&](int o) { return m.v(i + o, j, k); };
-        double vr = weno ? biased_interp(qb, bias_left(ut), 3) : c2(qb(-1), qb(0));
+        double vr = biased_interp(qb, bias_left(ut), hl(0, i, j, k, true));
         return ut * vr;
     }
     // Vv at (c,c,c)
     double F_Vv(int i, int j, int k) const {
-        double vt;
-        if (weno) { auto q = [&](int o) { return M.Ay_c(k) * m.v(i, j + 1 + o, k); }; vt = symm_interp(q, 3); }
-        else vt = c2(M.Ay_c(k) * m.v(i, j, k), M.Ay_c(k) * m.v(i, j + 1, k));
+        if (imm_periph(g, i, j, k, false, false, false)) return 0.0;
+        auto q = [&](int o) { return M.Ay_c(k) * m.v(i, j + 1 + o, k); };
+        double vt = symm_interp(q, hls(1, i, j, k, false));
         auto qb = [&](int o) { return m.v(i, j + 1 + o, k); };
-        double vr = weno ? biased_interp(qb, bias_left(vt), 3) : c2(qb(-1), qb(0));
+        double vr = biased_interp(qb, bias_left(vt), hl(1, i, j, k, false));
         return vt * vr;
     }
     // Wv at (c,f,f)
     double F_Wv(int i, int j, int k) const {
-        double wt;
-        if (weno) { auto q = [&](int o) { return M.Az() * m.w(i, j + o, k); }; wt = symm_interp(q, 3); }
-        else wt = c2(M.Az() * m.w(i, j - 1, k), M.Az() * m.w(i, j, k));
+        if (imm_periph(g, i, j, k, false, true, true)) return 0.0;
+        auto q = [&](int o) { return M.Az() * m.w(i, j + o, k); };
+        double wt = symm_interp(q, hls(1, i, j, k, true));
         auto qb = [&](int o) { return m.v(i, j, k + o); };
-        int lev = weno ? zlevel_biased(k, Nz, true) : 1;
-        double vr = biased_interp(qb, bias_left(wt), lev);
+        double vr = biased_interp(qb, bias_left(wt), zlb(i, j, k, true));
         return wt * vr;
     }
     // Uw at (f,c,f): ũ = sym_z face k of Ax u (Ax at centers k+o); wᴿ = biased_x face i of w
     double F_Uw(int i, int j, int k) const {
-        int lev = weno ? zlevel_symm(k, Nz, true) : 1;
+        if (imm_periph(g, i, j, k, true, false, true)) return 0.0;
         auto q = [&](int o) { return M.Ax_c(k + o) * m.u(i, j, k + o); };
-        double ut = symm_interp(q, lev);
+        double ut = symm_interp(q, zls(i, j, k, true));
         auto qb = [&](int o) { return m.w(i + o, j, k); };
-        double wr = weno ? biased_interp(qb, bias_left(ut), 3) : c2(qb(-1), qb(0));
+        double wr = biased_interp(qb, bias_left(ut), hl(0, i, j, k, true));
         return ut * wr;
     }
     // Vw at (c,f,f)
     double F_Vw(int i, int j, int k) const {
-        int lev = weno ? zlevel_symm(k, Nz, true) : 1;
+        if (imm_periph(g, i, j, k, false, true, true)) return 0.0;
         auto q = [&](int o) { return M.Ay_c(k + o) * m.v(i, j, k + o); };
-        double vt = symm_interp(q, lev);
+        double vt = symm_interp(q, zls(i, j, k, true));
         auto qb = [&](int o) { return m.w(i, j + o, k); };
-        double wr = weno ? biased_interp(qb, bias_left(vt), 3) : c2(qb(-1), qb(0));
+        double wr = biased_interp(qb, bias_left(vt), hl(1, i, j, k, true));
         return vt * wr;
     }
     // Ww at (c,c,c) index k: sym/biased at face k+1 with center conditions
     double F_Ww(int i, int j, int k) const {
-        int levs = weno ? zlevel_symm(k, Nz, false) : 1;
+        if (imm_periph(g, i, j, k, false, false, false)) return 0.0;
         auto q = [&](int o) { return M.Az() * m.w(i, j, k + 1 + o); };
-        double wt = symm_interp(q, levs);
-        int levb = weno ? zlevel_biased(k, Nz, false) : 1;
+        double wt = symm_interp(q, zls(i, j, k, false));
         auto qb = [&](int o) { return m.w(i, j, k + 1 + o); };
-        double wr = biased_interp(qb, bias_left(wt), levb);
+        double wr = biased_interp(qb, bias_left(wt), zlb(i, j, k, false));
         return wt * wr;
     }
 
@@ -520,20 +571,19 @@ struct Ctx {
     double F_cx(const Field& cc, int i, int j, int k) const {
         double ut = m.u(i, j, k);
         auto qb = [&](int o) { return cc(i + o, j, k); };
-        double cr = weno ? biased_interp(qb, bias_left(ut), 3) : c2(qb(-1), qb(0));
+        double cr = biased_interp(qb, bias_left(ut), hl(0, i, j, k, true));
         return M.Ax_c(k) * ut * cr;
     }
     double F_cy(const Field& cc, int i, int j, int k) const {
         double vt = m.v(i, j, k);
         auto qb = [&](int o) { return cc(i, j + o, k); };
-        double cr = weno ? biased_interp(qb, bias_left(vt), 3) : c2(qb(-1), qb(0));
+        double cr = biased_interp(qb, bias_left(vt), hl(1, i, j, k, true));
         return M.Ay_c(k) * vt * cr;
     }
     double F_cz(const Field& cc, int i, int j, int k) const {
         double wt = m.w(i, j, k);
         auto qb = [&](int o) { return cc(i, j, k + o); };
-        int lev = weno ? zlevel_biased(k, Nz, true) : 1;
-        double cr = biased_interp(qb, bias_left(wt), lev);
+        double cr = biased_interp(qb, bias_left(wt), zlb(i, j, k, true));
         return M.Az() * wt * cr;
     }
 
@@ -610,12 +660,14 @@ struct Ctx {
         double G = -adv;
         if (m.desc.has_coriolis) {
             double f = m.desc.coriolis_f;
-            auto AyV = [&](int ii, int jj) { return M.Ay_c(k) * m.v(ii, jj, k); };
+            // masked_Ay_qᶜᶠᶜ: zero on the immersed periphery (coriolis_schemes.jl:55-58)
+            auto AyV = [&](int ii, int jj) { return imm_periph(g, ii, jj, k, false, true, false) ? 0.0 : M.Ay_c(k) * m.v(ii, jj, k); };
             double ixy = 0.5 * (0.5 * (AyV(i - 1, j) + AyV(i, j)) + 0.5 * (AyV(i - 1, j + 1) + AyV(i, j + 1)));
             double xfu = -f * ixy * (1 / M.Ay_c(k));
             G = G - xfu;
         }
-        if (m.has_phy) G = G - (m.phy(i, j, k) - m.phy(i - 1, j, k)) * (1 / g.dx);
+        // ∂xᶠᶜᶜ is conditional on an immersed grid (conditional_differences.jl:15-43)
+        if (m.has_phy) G = G - ((imm_in(g, i - 1, j, k) || imm_in(g, i, j, k)) ? 0.0 : (m.phy(i, j, k) - m.phy(i - 1, j, k))) * (1 / g.dx);
         if (closure_on()) {
             double dx_ = M.Ax_c(k) * tau_ux(i, j, k) - M.Ax_c(k) * tau_ux(i - 1, j, k);
             double dy_ = M.Ay_c(k) * tau_uy(i, j + 1, k) - M.Ay_c(k) * tau_uy(i, j, k);
@@ -635,12 +687,12 @@ struct Ctx {
         double G = -adv;
         if (m.desc.has_coriolis) {
             double f = m.desc.coriolis_f;
-            auto AxU = [&](int ii, int jj) { return M.Ax_c(k) * m.u(ii, jj, k); };
+            auto AxU = [&](int ii, int jj) { return imm_periph(g, ii, jj, k, true, false, false) ? 0.0 : M.Ax_c(k) * m.u(ii, jj, k); };
             double ixy = 0.5 * (0.5 * (AxU(i, j - 1) + AxU(i + 1, j - 1)) + 0.5 * (AxU(i, j) + AxU(i + 1, j)));
             double yfu = f * ixy * (1 / M.Ax_c(k));
             G = G - yfu;
         }
-        if (m.has_phy) G = G - (m.phy(i, j, k) - m.phy(i, j - 1, k)) * (1 / g.dy);
+        if (m.has_phy) G = G - ((imm_in(g, i, j - 1, k) || imm_in(g, i, j, k)) ? 0.0 : (m.phy(i, j, k) - m.phy(i, j - 1, k))) * (1 / g.dy);
         if (closure_on()) {
             double dx_ = M.Ax_c(k) * (-2 * (nu_ffc(i + 1, j, k) * S12(i + 1, j, k))) - M.Ax_c(k) * (-2 * (nu_ffc(i, j, k) * S12(i, j, k)));
             double dy_ = M.Ay_c(k) * tau_vy(i, j, k) - M.Ay_c(k) * tau_vy(i, j - 1, k);
@@ -1046,16 +1098,15 @@ void update_phy(Model& m) {
     fill_halos(m, m.phy, 0);
 }
 
-void mask_immersed(Model& m, Field& f, bool wface) {
+// _mask_immersed_field!: zero where immersed_peripheral_node holds at the field's location
+// (mask_immersed_field.jl:65-77).  loc: 0 = (c,c,c), 1 = u (f,c,c), 2 = v (c,f,c), 3 = w (c,c,f)
+void mask_immersed(Model& m, Field& f, int loc) {
     const Grid& g = m.g;
     if (!g.immersed) return;
-    // _mask_immersed_field! zeroes values on the immersed periphery / inactive nodes
-    for (int k = 1; k <= g.Nz + (wface ? 1 : 0); ++k)
+    for (int k = 1; k <= g.Nz + (loc == 3 ? 1 : 0); ++k)
         for (int j = 1; j <= g.Ny; ++j)
-            for (int i = 1; i <= g.Nx; ++i) {
-                bool inactive = wface ? (imm(g, i, j, k) || imm(g, i, j, k - 1)) : imm(g, i, j, k);
-                if (inactive) f.at(i, j, k) = 0.0;
-            }
+            for (int i = 1; i <= g.Nx; ++i)
+                if (imm_periph(g, i, j, k, loc == 1, loc == 2, loc == 3)) f.at(i, j, k) = 0.0;
 }
 
 void compute_tendencies(Model& m) {
@@ -1074,7 +1125,7 @@ void compute_tendencies(Model& m) {
 
 // update_state! (update_nonhydrostatic_model_state.jl:22-62)
 void update_state(Model& m) {
-    for (int n = 0; n < m.ntr; ++n) mask_immersed(m, m.c[n], false);
+    for (int n = 0; n < m.ntr; ++n) mask_immersed(m, m.c[n], 0);
     fill_halos(m, m.u, 0);
     fill_halos(m, m.v, 0);
     fill_halos(m, m.w, 1, /*normal_flow=*/false);
@@ -1108,9 +1159,9 @@ int pressure_correction(Model& m, double dtau) {
     const Grid& g = m.g;
     const int Nx = g.Nx, Ny = g.Ny, Nz = g.Nz;
     Met M(g);
-    mask_immersed(m, m.u, false);
-    mask_immersed(m, m.v, false);
-    mask_immersed(m, m.w, true);
+    mask_immersed(m, m.u, 1);
+    mask_immersed(m, m.v, 2);
+    mask_immersed(m, m.w, 3);
     fill_halos(m, m.u, 0);
     fill_halos(m, m.v, 0);
     fill_halos(m, m.w, 1, true);
@@ -1144,9 +1195,15 @@ int pressure_correction(Model& m, double dtau) {
     for (int k = 1; k <= Nz; ++k)
         for (int j = 1; j <= Ny; ++j)
             for (int i = 1; i <= Nx; ++i) {
-                m.u.at(i, j, k) -= (m.p(i, j, k) - m.p(i - 1, j, k)) * (1 / g.dx);
-                m.v.at(i, j, k) -= (m.p(i, j, k) - m.p(i, j - 1, k)) * (1 / g.dy);
-                if (!g.flatz) m.w.at(i, j, k) -= (m.p(i, j, k) - m.p(i, j, k - 1)) * (1 / g.dzF(k));
+                // ∂ operators are conditional on an immersed grid (conditional_differences.jl:15-43)
+                double dx_ = (imm_in(g, i - 1, j, k) || imm_in(g, i, j, k)) ? 0.0 : (m.p(i, j, k) - m.p(i - 1, j, k));
+                double dy_ = (imm_in(g, i, j - 1, k) || imm_in(g, i, j, k)) ? 0.0 : (m.p(i, j, k) - m.p(i, j - 1, k));
+                m.u.at(i, j, k) -= dx_ * (1 / g.dx);
+                m.v.at(i, j, k) -= dy_ * (1 / g.dy);
+                if (!g.flatz) {
+                    double dz_ = (imm_in(g, i, j, k - 1) || imm_in(g, i, j, k)) ? 0.0 : (m.p(i, j, k) - m.p(i, j, k - 1));
+                    m.w.at(i, j, k) -= dz_ * (1 / g.dzF(k));
+                }
             }
     double dtp = std::max(2.220446049250313e-16, dtau);
     for (int k = 1; k <= Nz; ++k)
@@ -1261,7 +1318,10 @@ double vin_norm(const Model& m, const Field& r) {
     return std::sqrt(s);
 }
 
-// FFT preconditioner: z = FFTsolve_underlying(V⁻¹ r)
+// FFT preconditioner: z = solve(V⁻¹ r) with the spectral solver of the underlying grid
+// (conjugate_gradient_poisson_solver.jl:141-147,170-211): FFT on a regular grid,
+// Fourier-tridiagonal on a stretched one, whose solve! multiplies the source by Δzᶜ
+// (set_source_term!, fourier_tridiagonal_poisson_solver.jl:231-281)
 void precondition_fft(Model& m, Field& z, const Field& r) {
     const Grid& g = m.g;
     Met M(g);
@@ -1269,16 +1329,33 @@ void precondition_fft(Model& m, Field& z, const Field& r) {
     std::vector<double> rhs((size_t)Nx * Ny * Nz), phi;
     for (int k = 1; k <= Nz; ++k)
         for (int j = 1; j <= Ny; ++j)
-            for (int i = 1; i <= Nx; ++i) rhs[(i - 1) + (size_t)Nx * ((j - 1) + (size_t)Ny * (k - 1))] = r(i, j, k) * (1 / M.Vc(k));
-    fft_poisson(g, phi, rhs);
+            for (int i = 1; i <= Nx; ++i) {
+                double s = r(i, j, k) * (1 / M.Vc(k));
+                if (g.stretched) s *= g.dzC(k);
+                rhs[(i - 1) + (size_t)Nx * ((j - 1) + (size_t)Ny * (k - 1))] = s;
+            }
+    if (g.stretched) ft_poisson(m, phi, rhs);
+    else fft_poisson(g, phi, rhs);
     for (int k = 1; k <= Nz; ++k)
         for (int j = 1; j <= Ny; ++j)
             for (int i = 1; i <= Nx; ++i) z.at(i, j, k) = phi[(i - 1) + (size_t)Nx * ((j - 1) + (size_t)Ny * (k - 1))];
 }
 
+// mean over the cells that are not immersed (immersed_reductions.jl: NotImmersed condition)
+double active_mean(const Model& m, const Field& a) {
+    const Grid& g = m.g;
+    double s = 0;
+    long n = 0;
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i)
+                if (!inactive_cell(g, i, j, k)) { s += a(i, j, k); ++n; }
+    return n ? s / n : 0.0;
+}
+
 void gauge(Model& m, Field& x, Field& r) {
     const Grid& g = m.g;
-    double mx = field_mean(m, x), mr = field_mean(m, r);
+    double mx = active_mean(m, x), mr = active_mean(m, r);
     for (int k = 1; k <= g.Nz; ++k)
         for (int j = 1; j <= g.Ny; ++j)
             for (int i = 1; i <= g.Nx; ++i) {
@@ -1304,7 +1381,9 @@ int cg_solve(Model& m, Field& x, const Field& b) {
     double tol = std::max(rel * vin_norm(m, r), abs_);
     int it = 0;
     double rho_prev = 0;
+    static const bool trace = std::getenv("GBO_ORACLE_CG_TRACE") != nullptr;
     while (it < maxiter && vin_norm(m, r) > tol) {
+        if (trace && (it < 50 || it % 500 == 0)) std::fprintf(stderr, "cg %d |V^-1 r| = %.6e (tol %.3e)\n", it, vin_norm(m, r), tol);
         if (m.desc.preconditioner == GBO_PRECOND_NONE) z.d = r.d;
         else precondition_fft(m, z, r);
         double rho = field_dot(m, z, r);
@@ -1368,6 +1447,7 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
         g.zoff = 4;
     } else if (gd->z_faces) {
         build_stretched_z(g, gd->z_faces);
+        g.stretched = true;
     } else {
         build_regular_z(g, gd->z[0], gd->z[1]);
     }
@@ -1457,10 +1537,10 @@ int orc_get_field(void* h, int id, double* out, int64_t n) {
 // Rest of set!(model; ...) (set_nonhydrostatic_model.jl:59-73)
 int orc_set_finalize(void* h, int enforce) {
     Model* m = static_cast<Model*>(h);
-    for (int n = 0; n < m->ntr; ++n) mask_immersed(*m, m->c[n], false);
-    mask_immersed(*m, m->u, false);
-    mask_immersed(*m, m->v, false);
-    mask_immersed(*m, m->w, true);
+    for (int n = 0; n < m->ntr; ++n) mask_immersed(*m, m->c[n], 0);
+    mask_immersed(*m, m->u, 1);
+    mask_immersed(*m, m->v, 2);
+    mask_immersed(*m, m->w, 3);
     update_state(*m);
     int rc = 0;
     if (enforce) {
@@ -1493,6 +1573,24 @@ int orc_poisson_solve(void* h, double* phi, const double* rhs) {
     const Grid& g = m->g;
     const size_t N = (size_t)g.Nx * g.Ny * g.Nz;
     std::vector<double> b(rhs, rhs + N), out;
+    if (m->desc.pressure_solver == GBO_SOLVER_CONJUGATE_GRADIENT) {
+        // solve!(x, ::ConjugateGradientSolver, b): V∇²ϕ = rhs from the initial guess in ϕ
+        Field& x = m->cg_x;
+        x.init(g.Nx, g.Ny, g.Nz, g.H, g.Hz);
+        Field& bb = m->cg_rhs;
+        for (int k = 1; k <= g.Nz; ++k)
+            for (int j = 1; j <= g.Ny; ++j)
+                for (int i = 1; i <= g.Nx; ++i) {
+                    size_t q = (i - 1) + (size_t)g.Nx * ((j - 1) + (size_t)g.Ny * (k - 1));
+                    x.at(i, j, k) = phi[q];
+                    bb.at(i, j, k) = rhs[q];
+                }
+        int rc = cg_solve(*m, x, bb);
+        for (int k = 1; k <= g.Nz; ++k)
+            for (int j = 1; j <= g.Ny; ++j)
+                for (int i = 1; i <= g.Nx; ++i) phi[(i - 1) + (size_t)g.Nx * ((j - 1) + (size_t)g.Ny * (k - 1))] = x(i, j, k);
+        return rc;
+    }
     if (m->desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL) {
         for (int k = 1; k <= g.Nz; ++k)
             for (size_t n = 0; n < (size_t)g.Nx * g.Ny; ++n) b[n + (size_t)g.Nx * g.Ny * (k - 1)] *= g.dzC(k);

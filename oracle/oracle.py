@@ -126,7 +126,7 @@ class OracleModel:
                 raise ValueError("oracle set failed for %s" % name)
 
     def finalize_set(self, enforce_incompressibility=True):
-        return lib().orc_set_finalize(self.h, int(enforce_incompressibility))
+        return _checked(lib().orc_set_finalize(self.h, int(enforce_incompressibility)))
 
     def get(self, name):
         shp = self.field_shape(name)
@@ -137,7 +137,7 @@ class OracleModel:
         return out.reshape(shp, order="F")
 
     def time_step(self, dt, nsteps=1):
-        return lib().orc_time_step(self.h, float(dt), int(nsteps))
+        return _checked(lib().orc_time_step(self.h, float(dt), int(nsteps)))
 
     def clock(self):
         t = ctypes.c_double()
@@ -149,7 +149,7 @@ class OracleModel:
         rhs = np.asfortranarray(np.asarray(rhs, dtype=np.float64).reshape(self.shape, order="F"))
         flat = np.ascontiguousarray(rhs.ravel(order="F"))
         out = np.zeros_like(flat)
-        lib().orc_poisson_solve(self.h, _dptr(out), _dptr(flat))
+        _checked(lib().orc_poisson_solve(self.h, _dptr(out), _dptr(flat)))
         return out.reshape(self.shape, order="F")
 
     def z_spacings(self):
@@ -163,6 +163,18 @@ class OracleModel:
 
     def last_cg_iterations(self):
         return lib().orc_last_cg_iterations(self.h)
+
+
+class OracleNotConverged(RuntimeError):
+    pass
+
+
+def _checked(rc):
+    if rc == -4:
+        raise OracleNotConverged("oracle conjugate-gradient solve hit maxiter")
+    if rc != 0:
+        raise RuntimeError("oracle call failed with status %d" % rc)
+    return rc
 
 
 def set_threads(n):

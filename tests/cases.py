@@ -83,3 +83,65 @@ def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0
             "b": b}
     return Case(grid, init, advection=og.WENO(), closure=cl, buoyancy=og.BuoyancyTracer(),
                 coriolis=og.FPlane(f) if f else None, tracers=("b",), boundary_conditions=bcs)
+
+
+def seamount(N=(32, 32, 16), float_type=np.float64, seed=0, solver="cg", reltol=0.0, abstol=0.0,
+             height=1200.0, width=800.0, N2=1e-6, U=0.1, noise=1e-3, stretched=False):
+    """Seamount on an ImmersedBoundaryGrid(GridFittedBottom): x, y in [-5, 5] km, z in [-2, 0] km,
+    h = -2000 + height exp(-(x² + y²) / (2 width²)), b = N² z, u = U + noise, v, w = noise."""
+    Nx, Ny, Nz = N
+    if stretched:
+        zf = np.array([-2000.0 * (1 - np.tanh(1.5 * (k / Nz)) / np.tanh(1.5)) for k in range(Nz + 1)])
+        z = zf
+    else:
+        z = (-2000.0, 0.0)
+    under = og.RectilinearGrid(size=N, x=(-5000.0, 5000.0), y=(-5000.0, 5000.0), z=z,
+                               topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    grid = og.ImmersedBoundaryGrid(under, og.GridFittedBottom(
+        lambda x, y: -2000.0 + height * np.exp(-(x * x + y * y) / (2 * width * width))))
+    if solver == "cg":
+        ps = og.ConjugateGradientPoissonSolver(reltol=reltol, abstol=abstol)
+    elif solver == "cg-none":
+        ps = og.ConjugateGradientPoissonSolver(reltol=reltol, abstol=abstol, preconditioner=None)
+    elif solver == "fft":
+        ps = og.FourierTridiagonalPoissonSolver() if stretched else og.FFTBasedPoissonSolver()
+    else:
+        raise ValueError(solver)
+    rng = np.random.default_rng(seed)
+    _, _, zc = under.nodes()
+    init = {"u": U + noise * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "v": noise * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "w": noise * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
+            "b": N2 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz))}
+    return Case(grid, init, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
+                pressure_solver=ps)
+
+
+def immersed_mask(grid):
+    """Boolean (Nx, Ny, Nz) array: cell centre at or below the bottom height."""
+    _, _, zc = grid.nodes()
+    return zc[None, None, :] <= grid.bottom_height[:, :, None]
+
+
+def conditional_laplacian(grid, x, dzc, dzf):
+    """V∇²x with differences zeroed across faces that touch an immersed cell or a wall,
+    restated in numpy (ImmersedBoundaries/conditional_differences.jl:15-43).  dzc: the Nz
+    cell thicknesses Δzᶜ; dzf: the Nz+1 centre-to-centre spacings Δzᶠ at the faces."""
+    Nx, Ny, Nz = x.shape
+    imm = immersed_mask(grid)
+    dx, dy = grid.Lx / Nx, grid.Ly / Ny
+    Ax = dy * dzc[None, None, :]
+    Ay = dx * dzc[None, None, :]
+    Az = dx * dy
+    fx = np.where(imm | np.roll(imm, 1, 0), 0.0, Ax * (x - np.roll(x, 1, 0)) / dx)  # west faces
+    fy = np.where(imm | np.roll(imm, 1, 1), 0.0, Ay * (x - np.roll(x, 1, 1)) / dy)
+    fz = np.zeros((Nx, Ny, Nz + 1))
+    both = imm[:, :, 1:] | imm[:, :, :-1]
+    fz[:, :, 1:-1] = np.where(both, 0.0, Az * (x[:, :, 1:] - x[:, :, :-1]) / dzf[None, None, 1:-1])
+    return (np.roll(fx, -1, 0) - fx) + (np.roll(fy, -1, 1) - fy) + (fz[:, :, 1:] - fz[:, :, :-1])
+
+
+def interior_spacings(ref, Nz, H=4):
+    """Δzᶜ of cells 1..Nz and Δzᶠ of faces 1..Nz+1 from an oracle model (halo H)."""
+    dzc, dzf = ref.z_spacings()
+    return dzc[H:H + Nz], dzf[H:H + Nz + 1]

@@ -161,6 +161,38 @@ const char* gbo_version(void);
  * (src/Solvers/conjugate_gradient_poisson_solver.jl; the rhs there is V·div). */
 int gbo_poisson_solve_device(gbo_model* m, void* phi_device, const void* rhs_device);
 
+/* ---- allocation-free FFT Poisson solve --------------------------------------
+ * No counterpart in the reference: Oceananigans allocates the FFT solver's work
+ * arrays when FFTBasedPoissonSolver(grid) is built, and gbo_poisson_solve_device
+ * uses the work arrays gbo_model_create allocated.  This entry point solves
+ * ∇²ϕ = rhs on a regular RectilinearGrid (Periodic x, y; Bounded or Flat z;
+ * z_faces and bottom_height NULL) with the FFT-based solver and allocates no
+ * memory: its work space is one static device array of
+ * GBO_STATIC_SCRATCH_BYTES (32 MiB) in the library, and ϕ itself is the real
+ * work buffer.  It is for callers that cannot allocate device memory at solve
+ * time: a host whose device memory belongs to another allocator (a CUDA.jl or
+ * PyTorch caching pool that already holds the free memory, where a cudaMalloc
+ * from the library would fail or fragment the pool), and a caller with work in
+ * flight on other streams, where cudaMalloc / cudaFree could synchronize the
+ * device and stall that work.
+ *   - phi_device, rhs_device: Nx*Ny*Nz interior values of grid->float_type
+ *     (x fastest); phi may equal rhs (in place).  rhs is not modified otherwise.
+ *   - cuda_stream: the cudaStream_t (as void*) the work is issued on; NULL is the
+ *     default stream.  The call returns once the work is enqueued.
+ *   - Grids whose work space exceeds GBO_STATIC_SCRATCH_BYTES are rejected with
+ *     GBO_ERR_INVALID and a message giving the bytes needed (FP32: about
+ *     Nx/2*Ny*Nz*8 bytes, e.g. up to 256x256x64; FP64: twice that, e.g. 128^3).
+ *   - The first call on each device does the set-up (it looks up the static
+ *     array's device address with that device current); make that first call
+ *     before any stream capture.
+ *   - The scratch is one array per device shared by all callers: calls that
+ *     overlap in time (other streams, other threads) race on it and must be
+ *     serialized by the caller.  Nothing in it has to start at zero; every
+ *     value a call reads was written earlier in the same call. */
+#define GBO_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int gbo_poisson_solve_fft_static(const gbo_grid_desc* grid, void* phi_device, const void* rhs_device,
+                                 void* cuda_stream);
+
 /* ---- instrumentation -----------------------------------------------------
  * No reference counterpart: the reference measures with external profilers
  * (benchmarking/, nsys in CI).  These expose what a benchmark harness needs to

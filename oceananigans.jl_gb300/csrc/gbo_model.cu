@@ -1183,6 +1183,9 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
 
 }  // namespace
 
+// Message for gbo_last_error(NULL) from entry points in other translation units.
+void gbo_record_error(const char* msg) { g_last_error = msg; }
+
 extern "C" {
 
 void gbo_model_desc_default(gbo_model_desc* d) {

@@ -82,6 +82,7 @@ SIGNATURES = {
     "gbo_last_error": (ctypes.c_char_p, [_vp]),
     "gbo_version": (ctypes.c_char_p, []),
     "gbo_poisson_solve_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "gbo_poisson_solve_fft_static": (ctypes.c_int, [ctypes.POINTER(GridDesc), _vp, _vp, _vp]),
     "gbo_model_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "gbo_kernel_launches": (ctypes.c_int64, [_vp]),
     "gbo_kernel_timings": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_int32]),

@@ -8,7 +8,7 @@ PKG_ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libgb300ocean.so")
-SOURCES = ["gbo_model.cu", "gbo_fft.cu"]
+SOURCES = ["gbo_model.cu", "gbo_fft.cu", "gbo_static_poisson.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

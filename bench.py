@@ -155,6 +155,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch from an ncu
+# capture of this workload; the capture, its command and the algorithmic bytes of the
+# same launch are in the named profile.
+PROFILED_TRAFFIC = {
+    ("k_momentum", (256, 256, 128), "f32"): {
+        "traffic": 426.7e6,
+        "traffic_launch": "one RK3 stage-1 launch (algorithmic bytes of that launch 469.8e6; stages 2-3 also read G-)",
+        "traffic_profile": "profiles/k_momentum_fused_free_convection_256x256x128_f32.md",
+        "issue_active_frac": 0.578,
+        "dram_throughput_frac": 0.053,
+    },
+}
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -283,6 +297,9 @@ def main():
     roofline = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": ab}
+    prof = PROFILED_TRAFFIC.get((top, tuple(size), args.dtype))
+    if prof:
+        roofline.update(prof)
     for n, k in kernels.items():
         b = algorithmic_bytes(n, size, s)
         k["achieved_gbs"] = b / (k["ms_per_launch"] / 1e3) / 1e9 if b else None

@@ -15,6 +15,12 @@
 #pragma once
 #include "gbo_step.cuh"
 
+// Resident blocks per SM the FP32 kernel is compiled for (registers are capped so
+// that this many 256-thread blocks fit).
+#ifndef GBO_FUSED_MIN_BLOCKS
+#define GBO_FUSED_MIN_BLOCKS 3
+#endif
+
 namespace fused {
 
 constexpr int TX = 32, TY = 8, H = 3;
@@ -37,10 +43,16 @@ struct Smem {
     FT NU[4][PS];                      // νₑ: k-1, k, k+1 (+k+2)
     FT PH[2][PS];                      // pHY′: k (+k+1)
     FT CC[2][PS];                      // tracer: k (+k+1)
-    FT KP[3][PS];                      // AMD κₑ: k, k+1 (+k+2)
     FT WX[NWX][TY][TX + 1];
     FT SY[NSY][TY + 1][TX];
+    FT KP[3][PS];                      // AMD κₑ: k, k+1 (+k+2); last, so that other closures
+                                       // launch without it (smem_bytes)
 };
+// Dynamic shared memory of a launch: the κₑ ring only with AMD.
+template <typename FT>
+constexpr size_t smem_bytes(bool amd) {
+    return amd ? sizeof(Smem<FT>) : sizeof(Smem<FT>) - sizeof(FT) * 3 * PS;
+}
 
 // Asynchronous 4/8-byte global -> shared copy; src_bytes = 0 writes zero.
 template <typename FT>
@@ -113,8 +125,8 @@ struct Col {
 
 // Column-marching fused kernel (see the file header).  TR: also advance one tracer
 // (P.c -> P.co, P.Gc) in the same march.
-template <typename FT, bool TR>
-__global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk) {
+template <typename FT, bool TR, int CLK>
+__global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 1) k_momentum_fused(StepP<FT> P, int kchunk) {
     using namespace fused;
     extern __shared__ unsigned char smem_raw[];
     Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
@@ -124,8 +136,8 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
     const int i = i0 + tx, j = j0 + ty;
     const int kb = blockIdx.z * kchunk, ke = min(g.Nz, kb + kchunk);
-    const bool closure = P.closure != CL_NONE;
-    const bool amd = P.closure == CL_AMD;
+    constexpr bool closure = CLK != CL_NONE;
+    constexpr bool amd = CLK == CL_AMD;
     const bool inside = (i < g.Nx) && (j < g.Ny);
     CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g);
     WFld<FT> Wg = wfld(P.w, g);
@@ -137,8 +149,9 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
 
     // ring slots: U/V slot of level k = k mod 3, W slot of face k = k mod 3,
     // NU slot of level k = k mod 4, PH/CC slot = k mod 2, KP slot = k mod 3
+    // (m3 only in the prologue; the loop tracks k mod 3 in r3)
     auto m3 = [](int k) { return ((k % 3) + 3) % 3; };
-    auto m4 = [](int k) { return ((k % 4) + 4) % 4; };
+    auto m4 = [](int k) { return k & 3; };
     auto m2 = [](int k) { return k & 1; };
 
     // ---- prologue: planes for level kb ----
@@ -217,24 +230,28 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
             c.qzc = FT(0);
             if (closure) {
                 FT km = amd ? km_amd : s.NU[m4(kb - 1)][pidx(tx, ty)];
-                FT kk = amd ? s.KP[m3(kb)][pidx(tx, ty)] : s.NU[m4(kb)][pidx(tx, ty)];
+                const FT* Kb = amd ? s.KP[m3(kb)] : s.NU[m4(kb)];  // pick the plane, then load
+                FT kk = Kb[pidx(tx, ty)];
                 FT kz = amd ? FT(0.5) * (km + kk) : FT(0.5) * (km + kk) / P.Pr;
                 c.qzc = -kz * ((c.cc[3] - c.cc[2]) * M.rdzf(kb));
             }
         }
     }
 
+    int r3 = m3(kb);
     for (int k = kb; k < ke; ++k) {
+        // ring slots of levels k-1, k, k+1 (and k+2, which shares the slot of k-1)
+        const int s3k = r3, s3p = r3 == 2 ? 0 : r3 + 1, s3m = r3 == 0 ? 2 : r3 - 1;
         // ---- prefetch the planes first needed at level k+1 (free ring slots) ----
         const int kn = k + 1;
         if (kn < ke) {
-            issue_plane(s.U[m3(kn)], P.u, zsrc_c(kn, Nz, fz), plane, pp, tid);
-            issue_plane(s.V[m3(kn)], P.v, zsrc_c(kn, Nz, fz), plane, pp, tid);
-            if (!fz) issue_plane(s.W[m3(kn + 1)], P.w, zsrc_w(kn + 1, Nz), plane, pp, tid);
+            issue_plane(s.U[s3p], P.u, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            issue_plane(s.V[s3p], P.v, zsrc_c(kn, Nz, fz), plane, pp, tid);
+            if (!fz) issue_plane(s.W[s3m], P.w, zsrc_w(kn + 1, Nz), plane, pp, tid);
             if (closure) issue_plane(s.NU[m4(kn + 1)], P.nu, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
             if (P.has_phy) issue_plane(s.PH[m2(kn)], P.phy, zsrc_c(kn, Nz, fz), plane, pp, tid);
             if (TR) issue_plane(s.CC[m2(kn)], P.c, zsrc_c(kn, Nz, fz), plane, pp, tid);
-            if (TR && amd) issue_plane(s.KP[m3(kn + 1)], P.kap, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
+            if (TR && amd) issue_plane(s.KP[s3m], P.kap, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
         }
         cp_async_commit();
         // ---- early loads: window tops for the next level, G⁻ of this level ----
@@ -248,19 +265,19 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
             if (!fz && k > 0) Gwm = P.Gw[idx];
             if (TR) Gcm = P.Gc[idx];
         }
-        const FT* Uk = s.U[m3(k)];
-        const FT* Um = s.U[m3(k - 1)];
-        const FT* Vk = s.V[m3(k)];
-        const FT* Vm = s.V[m3(k - 1)];
-        const FT* Wk = s.W[m3(k)];
-        const FT* Wp = s.W[m3(k + 1)];
+        const FT* Uk = s.U[s3k];
+        const FT* Um = s.U[s3m];
+        const FT* Vk = s.V[s3k];
+        const FT* Vm = s.V[s3m];
+        const FT* Wk = s.W[s3k];
+        const FT* Wp = s.W[s3p];
         const FT* Nm = s.NU[m4(k - 1)];
         const FT* Nk = s.NU[m4(k)];
         const FT* Np = s.NU[m4(k + 1)];
         const FT* PHk = s.PH[m2(k)];
         const FT* CCk = s.CC[m2(k)];
-        const FT* Kk = s.KP[m3(k)];
-        const FT* Kp = s.KP[m3(k + 1)];
+        const FT* Kk = s.KP[s3k];
+        const FT* Kp = s.KP[s3p];
         const FT Ax = M.Ax(k), Ay = M.Ay(k);
 
         // ---- west / south face quantities of this thread (and the tile edges) ----
@@ -366,10 +383,14 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 }
             }
         };
-        west(tx, ty, true);
-        south(tx, ty, true);
-        if (ty == 0 && tx < TY) west(TX, tx, false);   // east column of the tile
-        if (ty == 1) south(tx, TY, false);             // north row of the tile
+        // pass 0: the faces of this thread's cells; pass 1: the tile's east column
+        // (warp 0, lanes < TY) and north row (warp 1).  One code copy serves both.
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool own = pass == 0;
+            if (own || (ty == 0 && tx < TY)) west(own ? tx : TX, own ? ty : tx, own);
+            if (own || ty == 1) south(tx, own ? ty : TY, own);
+        }
 
         // ---- top-face quantities (carried to the next level) ----
         FT fWu_t = FT(0), fWv_t = FT(0), fWw_t = FT(0), t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);
@@ -407,8 +428,10 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
                 auto q = [&](int o) { return c.cc[4 + o]; };
                 fWc_t = Az * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
                 if (closure) {
-                    FT kk = amd ? Kk[pidx(tx, ty)] : Nk[pidx(tx, ty)];
-                    FT kp = amd ? Kp[pidx(tx, ty)] : Np[pidx(tx, ty)];
+                    const FT* K0 = amd ? Kk : Nk;
+                    const FT* K1 = amd ? Kp : Np;
+                    FT kk = K0[pidx(tx, ty)];
+                    FT kp = K1[pidx(tx, ty)];
                     FT kz = amd ? FT(0.5) * (kk + kp) : FT(0.5) * (kk + kp) / P.Pr;
                     qzc_t = -kz * ((c.cc[4] - c.cc[3]) * M.rdzf(k + 1));
                 }
@@ -519,6 +542,7 @@ __global__ void __launch_bounds__(256) k_momentum_fused(StepP<FT> P, int kchunk)
         }
         cp_async_wait_all();
         __syncthreads();
+        r3 = s3p;
     }
 }
 

@@ -426,6 +426,27 @@ const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", 
                                          "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
                                          "k_nan_check", "k_mask", "k_cg"};
 
+// The fused momentum kernel is compiled per closure kind; these pick the instance.
+template <typename FT, bool TR>
+void launch_fused(int closure, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk) {
+    const size_t smem = fused::smem_bytes<FT>(closure == CL_AMD);
+    if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk);
+    else if (closure == CL_AMD) k_momentum_fused<FT, TR, CL_AMD><<<grid, block, smem, st>>>(P, kchunk);
+    else k_momentum_fused<FT, TR, CL_NONE><<<grid, block, smem, st>>>(P, kchunk);
+}
+template <typename FT>
+cudaError_t fused_set_smem() {
+    const int b = (int)sizeof(fused::Smem<FT>);
+    cudaError_t e = cudaSuccess;
+    for (const void* f : {(const void*)k_momentum_fused<FT, true, CL_NONE>, (const void*)k_momentum_fused<FT, true, CL_SMAG>,
+                          (const void*)k_momentum_fused<FT, true, CL_AMD>, (const void*)k_momentum_fused<FT, false, CL_NONE>,
+                          (const void*)k_momentum_fused<FT, false, CL_SMAG>, (const void*)k_momentum_fused<FT, false, CL_AMD>}) {
+        cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        if (r != cudaSuccess) e = r;
+    }
+    return e;
+}
+
 namespace {
 
 template <typename FT>
@@ -628,9 +649,8 @@ struct ModelImpl : gbo_model {
         TC = 32;
         while (TC > 1 && (size_t)3 * Nz * TC * sizeof(double) > lim) TC /= 2;
         smem_t = (size_t)3 * Nz * TC * sizeof(double);
-        GBO_CUDA(cudaFuncSetAttribute(k_momentum_fused<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(fused::Smem<FT>)));
+        GBO_CUDA(fused_set_smem<FT>());
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
-        GBO_CUDA(cudaFuncSetAttribute(k_momentum_fused<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(fused::Smem<FT>)));
         kchunk = flat ? 1 : std::min(16, Nz);
         GBO_CUDA(fft_set_smem<FT>(smem_z, smem_x, smem_y, smem_t));
     }
@@ -888,11 +908,11 @@ struct ModelImpl : gbo_model {
             M0.flux_top = FT(desc.tracer_flux_top[0]);
             M0.flux_bot = FT(desc.tracer_flux_bottom[0]);
             pre(G_MOMENTUM);
-            k_momentum_fused<FT, true><<<fgrid, fblock, sizeof(fused::Smem<FT>), stream>>>(M0, kchunk);
+            launch_fused<FT, true>(desc.closure, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         } else {
             pre(G_MOMENTUM);
-            k_momentum_fused<FT, false><<<fgrid, fblock, sizeof(fused::Smem<FT>), stream>>>(M0, kchunk);
+            launch_fused<FT, false>(desc.closure, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         }
         for (int n = tracer0; n < ntr; ++n) {

@@ -26,9 +26,11 @@ GBO_D float weno_div(float a, float b) { return __fdividef(a, b); }
 template <typename FT>
 GBO_D FT beta3(FT p0, FT p1, FT p2, int s) {
     if (IsF32<FT>::value) {
+        // shift by the stencil centre; p1 - p1 is exactly +0 for finite values, so the
+        // terms in p1 vanish without changing any bit of β
         FT c = p1;
-        p0 -= c; p1 -= c; p2 -= c;
-        // p1 is exactly zero after the shift
+        p0 -= c; p2 -= c;
+        p1 = FT(0);
     }
     FT b;
     if (s == 0)

@@ -10,6 +10,8 @@ BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libgb300ocean.so")
 SOURCES = ["gbo_model.cu", "gbo_fft.cu", "gbo_static_poisson.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc options, e.g. GBO_NVCC_EXTRA="-DGBO_FUSED_MIN_BLOCKS=4" for a tuning build
+EXTRA = os.environ.get("GBO_NVCC_EXTRA", "").split()
 
 
 def _stale(target, deps):
@@ -29,7 +31,7 @@ def build(force=False, verbose=False):
     procs = []
     for src in SOURCES:
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *EXTRA, "-c",
                os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))

@@ -1,13 +1,27 @@
 """Benchmark: NonhydrostaticModel RK3 cell-updates/s on one GB300 (replicas for N > 1).
 
-Workload: 3-D free convection, 256×256×128 RectilinearGrid over x, y ∈ [0, 512] m,
-z ∈ [-256, 0] m, (Periodic, Periodic, Bounded); BuoyancyTracer b = N² z + 1e-8
-noise (N² = 1e-5 s⁻²), velocities 1e-3 U[-1, 1] (seeded), surface buoyancy flux
-1e-8 m² s⁻³, WENO5, SmagorinskyLilly, FPlane(f = 1e-4), FFT/DCT pressure solver,
-Δt = 2 s, FP32.  A "step" is one full RK3 time step (three substeps with their
-pressure projections) of the whole grid.
+Default workload (the headline): 3-D free convection, 256×256×128 RectilinearGrid
+over x, y ∈ [0, 512] m, z ∈ [-256, 0] m, (Periodic, Periodic, Bounded);
+BuoyancyTracer b = N² z + 1e-8 noise (N² = 1e-5 s⁻²), velocities 1e-3 U[-1, 1]
+(seeded), surface buoyancy flux 1e-8 m² s⁻³, WENO5, SmagorinskyLilly,
+FPlane(f = 1e-4), FFT/DCT pressure solver, Δt = 2 s, FP32.  A "step" is one full
+RK3 time step (three substeps with their pressure projections) of the whole grid.
+
+Other workloads (--workload), each with seeded synthetic inputs of the stated
+shapes and distributions:
+  turbulence2d    128×128 (Periodic, Periodic, Flat), u, v ~ U[-1, 1] projected,
+                  WENO5, FP64, Δt = 0.01
+  stretched_amd   512×512×256 with faces z_k = -256(1 - tanh(2(1 - k/256))/tanh 2),
+                  AnisotropicMinimumDissipation, FourierTridiagonalPoissonSolver
+                  (FP64 Thomas sweep), FP32 state, Δt = 1 s
+  seamount        256×256×128 ImmersedBoundaryGrid(GridFittedBottom) over
+                  x, y ∈ [-5, 5] km, z ∈ [-2, 0] km, h = -2000 + 1200 exp(-r²/(2·800²)),
+                  N² = 1e-6, u = 0.1 + 1e-3 noise, FFT-preconditioned CG to a 1e-8
+                  relative residual (FP64 dot products), FP32 state; also reports the
+                  Poisson-solve time of held-out right-hand sides
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                       [--workload NAME] [--size NX NY NZ] [--dtype f32|f64]
 """
 import argparse
 import ctypes
@@ -24,8 +38,6 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "oceananigans.jl_gb300"))
 
-SIZE = (256, 256, 128)
-DT = 2.0
 METRIC = "cell_updates_per_s"
 UNIT = "cell-updates/s"
 
@@ -36,17 +48,22 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--size", type=int, nargs=3, default=list(SIZE))
-    p.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    p.add_argument("--workload", default="convection", choices=sorted(WORKLOADS))
+    p.add_argument("--size", type=int, nargs=3, default=None)
+    p.add_argument("--dtype", default=None, choices=["f32", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
-    return p.parse_args()
+    a = p.parse_args()
+    w = WORKLOADS[a.workload]
+    a.size = tuple(a.size) if a.size else w["size"]
+    a.dtype = a.dtype or w["dtype"]
+    return a
 
 
-def workload(size, float_type):
+def _convection(size, float_type):
     import oceananigans_gb300 as og
     Nx, Ny, Nz = size
-    grid = og.RectilinearGrid(size=size, x=(0, 512.0), y=(0, 512.0), z=(-256.0, 0.0),
+    grid = og.RectilinearGrid(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=(-256.0, 0.0),
                               topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
     physics = dict(advection=og.WENO(), closure=og.SmagorinskyLilly(), buoyancy=og.BuoyancyTracer(),
                    coriolis=og.FPlane(1e-4), tracers=("b",),
@@ -60,28 +77,96 @@ def workload(size, float_type):
     return grid, physics, init
 
 
-def config_dict(size, dtype, n):
-    return {"workload": "free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft" % tuple(size),
-            "grid": list(size), "dt_s": DT, "float": dtype, "parallelism": "replicas%d" % n,
-            "l2_policy": "inputs larger than L2 (state + work arrays ≈ 20 fields × %.0f MB)" %
-                         (np.prod(size) * (4 if dtype == "f32" else 8) / 1e6)}
+def _turbulence2d(size, float_type):
+    import oceananigans_gb300 as og
+    Nx, Ny = size[0], size[1]
+    grid = og.RectilinearGrid(size=(Nx, Ny), x=(0, 2 * np.pi), y=(0, 2 * np.pi),
+                              topology=("Periodic", "Periodic", "Flat"), float_type=float_type)
+    rng = np.random.default_rng(2024)
+    init = {"u": rng.uniform(-1, 1, (Nx, Ny, 1)), "v": rng.uniform(-1, 1, (Nx, Ny, 1))}
+    return grid, dict(advection=og.WENO()), init
+
+
+def _stretched_amd(size, float_type):
+    import oceananigans_gb300 as og
+    Nx, Ny, Nz = size
+    # faces -256 (1 - tanh(2 (1 - k/Nz)) / tanh 2), k = 0..Nz, in increasing order (finest at the surface)
+    zf = np.sort([-256.0 * (1 - np.tanh(2 * (1 - k / Nz)) / np.tanh(2)) for k in range(Nz + 1)])
+    grid = og.RectilinearGrid(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=zf,
+                              topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    physics = dict(advection=og.WENO(), closure=og.AnisotropicMinimumDissipation(), buoyancy=og.BuoyancyTracer(),
+                   coriolis=og.FPlane(1e-4), tracers=("b",),
+                   boundary_conditions={"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(1e-8))},
+                   pressure_solver=og.FourierTridiagonalPoissonSolver())
+    rng = np.random.default_rng(2024)
+    _, _, zc = grid.nodes()
+    init = {"u": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
+            "b": 1e-5 * zc[None, None, :] + 1e-8 * rng.standard_normal((Nx, Ny, Nz))}
+    return grid, physics, init
+
+
+def _seamount(size, float_type):
+    import oceananigans_gb300 as og
+    Nx, Ny, Nz = size
+    under = og.RectilinearGrid(size=size, x=(-5000.0, 5000.0), y=(-5000.0, 5000.0), z=(-2000.0, 0.0),
+                               topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    grid = og.ImmersedBoundaryGrid(under, og.GridFittedBottom(
+        lambda x, y: -2000.0 + 1200.0 * np.exp(-(x * x + y * y) / (2 * 800.0 ** 2))))
+    physics = dict(advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
+                   pressure_solver=og.ConjugateGradientPoissonSolver(reltol=1e-8, abstol=1e-30))
+    rng = np.random.default_rng(2024)
+    _, _, zc = under.nodes()
+    init = {"u": 0.1 + 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
+            "b": 1e-6 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz))}
+    return grid, physics, init
+
+
+WORKLOADS = {
+    "convection": dict(build=_convection, size=(256, 256, 128), dtype="f32", dt=2.0, cpu_size=(128, 128, 128),
+                       name="free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft"),
+    "turbulence2d": dict(build=_turbulence2d, size=(128, 128, 1), dtype="f64", dt=0.01, cpu_size=(128, 128, 1),
+                         name="turbulence2d_%dx%dx%d_weno5_fft"),
+    "stretched_amd": dict(build=_stretched_amd, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),
+                          name="stretched_convection_%dx%dx%d_weno5_amd_fourier_tridiagonal"),
+    "seamount": dict(build=_seamount, size=(256, 256, 128), dtype="f32", dt=20.0, cpu_size=(64, 64, 128),
+                     name="seamount_ibg_%dx%dx%d_weno5_fft_pcg"),
+}
+
+
+def workload(name, size, float_type):
+    return WORKLOADS[name]["build"](size, float_type)
+
+
+def config_dict(args, n):
+    w = WORKLOADS[args.workload]
+    size = args.size
+    s = 4 if args.dtype == "f32" else 8
+    return {"workload": w["name"] % tuple(size), "grid": list(size), "dt_s": w["dt"], "float": args.dtype,
+            "parallelism": "replicas%d" % n,
+            "l2_policy": "inputs larger than L2 (state + work arrays ≈ 20 fields × %.0f MB)" % (np.prod(size) * s / 1e6)
+            if np.prod(size) * s * 20 > 129e6 else "state fits in L2 (small 2-D case; no flush between steps)"}
 
 
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 C++/OpenMP oracle (a restatement of the reference; the
 # Julia reference cannot run on this machine)
 # ---------------------------------------------------------------------------
-def cpu_sample(steps_budget_s=20.0, size=None):
+def cpu_sample(name, steps_budget_s=20.0):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from oceananigans_gb300.api import model_descriptor
     oracle.build()
     nthreads = os.cpu_count() or 1
     oracle.set_threads(nthreads)
-    # bounded sample: the same per-cell work on a 128×128×128 sub-grid of the workload
-    size = size or (128, 128, 128)
-    grid, physics, init = workload(size, np.float64)
-    grid.x, grid.y = (0, 512.0 * size[0] / SIZE[0]), (0, 512.0 * size[1] / SIZE[1])
+    # bounded sample: the same per-cell work (same spacings and physics) on a smaller grid
+    w = WORKLOADS[name]
+    size = w["cpu_size"]
+    dt = w["dt"]
+    grid, physics, init = workload(name, size, np.float64)
     d = grid.descriptor()
     g = oracle.GridDesc()
     for f, _ in oracle.GridDesc._fields_:
@@ -93,11 +178,11 @@ def cpu_sample(steps_budget_s=20.0, size=None):
     ref = oracle.OracleModel(g, m, tracers=tracers)
     ref.set(**init)
     ref.finalize_set(True)
-    ref.time_step(DT, 1)  # warm-up
+    ref.time_step(dt, 1)  # warm-up
     t0 = time.perf_counter()
     n = 0
     while True:
-        ref.time_step(DT, 1)
+        ref.time_step(dt, 1)
         n += 1
         if time.perf_counter() - t0 > steps_budget_s or n >= 5:
             break
@@ -178,20 +263,27 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def algorithmic_bytes(group, size, s, closure=True, ntr=1):
-    """Algorithmic bytes per launch (compulsory reads + writes of whole fields)."""
+def algorithmic_bytes(group, size, s, ntr=1, closure="smagorinsky", has_phy=True, fused=True):
+    """Algorithmic bytes per launch: compulsory reads + writes of whole fields, G⁻ read
+    on 2 of the 3 RK3 stages."""
     N = float(np.prod(size))
+    nu = 1 if closure else 0
+    kap = 1 if closure == "amd" else 0
+    spec = 2 * (1 + 2.0 / size[0])  # half spectrum in and out (complex, Nx/2+1 of Nx)
+    if fused:  # momentum + tracer 0 in one march
+        mom = (3 + 1 + nu + kap + (1 if has_phy else 0)) + (3 + 1) * 2 + (3 + 1) * 2.0 / 3
+    else:      # per-point momentum kernel; tracers separately
+        mom = (3 + nu + (1 if has_phy else 0)) + 3 * 2 + 3 * 2.0 / 3
     per = {
-        # fused momentum + tracer 0: u,v,w,c (+νₑ, pHY′) read, U*, c*, Gⁿ written;
-        # G⁻ read on 2 of 3 stages
-        "k_momentum": (3 + ntr + (1 if closure else 0) + 1) + (3 + ntr) * 2 + (3 + ntr) * 2.0 / 3,
-        "k_tracer": (3 + 1 + (1 if closure else 0)) + 2 + 2.0 / 3,
-        "k_closure": 4 + 1,
+        "k_momentum": mom,
+        "k_tracer": (3 + 1 + nu) + 2 + 2.0 / 3,
+        "k_closure": 4 + 1 + kap,
         "k_hydrostatic": 2,
         "k_source": 4,
         "k_dct_z": 2,
-        "k_rfft_x": 2 * (1 + 2.0 / size[0]),
-        "k_fft_y": 2 * (1 + 2.0 / size[0]),
+        "k_rfft_x": spec,
+        "k_fft_y": spec,
+        "k_thomas_z": spec,
         "k_correct": 8,
         "k_copy": 2,
         "k_nan_check": 1,
@@ -210,18 +302,59 @@ def run_reference(args):
         pass
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        cpu = cpu_sample(steps_budget_s=max(2.0, 60.0 / max(1, args.steps)))
+        cpu = cpu_sample(args.workload, steps_budget_s=max(2.0, 60.0 / max(1, args.steps)))
         samples.append(cpu["value"])
     value = statistics.median(samples)
     cpu["value"] = value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * np.prod(size) / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": config_dict(size, "f64", args.gpus),
+            "data": "synthetic (seeded)", "config": config_dict(args, args.gpus),
             "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference arm = FP64 CPU restatement of the reference's algorithm (Julia is not installed); "
                     "wall %.1f s" % (time.perf_counter() - t_all)}
     print(json.dumps(line), flush=True)
+
+
+def held_out_solves(model, grid, torch, stream, ft, n=50):
+    """Time CG Poisson solves (to the model's tolerance) of held-out right-hand sides:
+    V·div of the model's current velocity plus seeded perturbations, masked to the
+    active cells with zero active mean, as the pressure correction builds them."""
+    u, v, w = model.get("u"), model.get("v"), model.get("w")
+    Nx, Ny, Nz = u.shape
+    dx, dy = grid.Lx / Nx, grid.Ly / Ny
+    _, _, zc = grid.nodes()
+    dz = grid.Lz / Nz
+    imm = zc[None, None, :] <= grid.bottom_height[:, :, None]
+    rng = np.random.default_rng(7)
+    tdt = torch.float32 if ft == np.float32 else torch.float64
+    phi = torch.zeros(Nx * Ny * Nz, dtype=tdt, device="cuda")
+    rhs = []
+    for _ in range(n):
+        du = u + 1e-3 * rng.standard_normal(u.shape)
+        dv = v + 1e-3 * rng.standard_normal(v.shape)
+        dw = w + 1e-3 * rng.standard_normal(w.shape)
+        dw[:, :, 0] = dw[:, :, -1] = 0
+        div = (np.roll(du, -1, 0) - du) / dx + (np.roll(dv, -1, 1) - dv) / dy + (dw[:, :, 1:] - dw[:, :, :-1]) / dz
+        b = div * (dx * dy * dz)
+        b[imm] = 0
+        b[~imm] -= b[~imm].mean()
+        rhs.append(torch.tensor(b.ravel(order="F"), dtype=tdt, device="cuda"))
+    times, iters = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for r in rhs:
+        phi.zero_()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        model.poisson_solve_device(phi.data_ptr(), r.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        iters.append(model.solver_iterations)
+    return {"solves": n, "ms_mean": float(np.mean(times)), "ms_median": float(np.median(times)),
+            "iterations_mean": float(np.mean(iters)), "ms_per_iteration": float(np.sum(times) / max(1, np.sum(iters))),
+            "preconditioner": "fft", "reltol": 1e-8,
+            "path": "gbo_poisson_solve_device from a zero initial guess (host reads the stop flag each iteration)"}
 
 
 def main():
@@ -243,12 +376,20 @@ def main():
     size = tuple(args.size)
     ft = np.float32 if args.dtype == "f32" else np.float64
     s = 4 if ft == np.float32 else 8
-    grid, physics, init = workload(size, ft)
+    DT = WORKLOADS[args.workload]["dt"]
+    grid, physics, init = workload(args.workload, size, ft)
     model = og.NonhydrostaticModel(grid, **physics)
     og.set_(model, **init)
     sp = ctypes.c_void_p()
     lib.gbo_model_stream(model._h, ctypes.byref(sp))
     stream = torch.cuda.ExternalStream(sp.value)
+    closure = {type(None): None}.get(type(physics.get("closure")), None)
+    cl = physics.get("closure")
+    closure = None if cl is None else ("amd" if isinstance(cl, og.AnisotropicMinimumDissipation) else "smagorinsky")
+    ntr = len(physics.get("tracers", ()))
+    has_phy = ntr > 0 and grid.topology[2] == "Bounded" and physics.get("buoyancy") is not None
+    fused = grid.bottom_height is None
+    ab_kw = dict(ntr=ntr, closure=closure, has_phy=has_phy, fused=fused)
 
     og.time_step_(model, DT, args.warmup)
 
@@ -274,25 +415,26 @@ def main():
     cells = float(np.prod(size))
     value = cells * args.steps * world / elapsed
 
-    # per-kernel durations from an instrumented pass on the same stream
+    # per-kernel durations from an instrumented pass on the same stream: every launch
+    # bracketed by CUDA events, launched one by one
     ng = lib.gbo_kernel_group_count()
     ms = (ctypes.c_double * ng)()
+    cnt = (ctypes.c_int64 * ng)()
     nt = 2
     L.check(lib.gbo_kernel_timings(model._h, DT, nt, ms, ng), model._h)
+    L.check(lib.gbo_kernel_timing_counts(model._h, cnt, ng), model._h)
     names = [lib.gbo_kernel_group_name(g).decode() for g in range(ng)]
-    per_step_launches = {"k_momentum": 3, "k_tracer": 3, "k_closure": 3, "k_hydrostatic": 3, "k_source": 3,
-                         "k_dct_z": 6, "k_rfft_x": 6, "k_fft_y": 3, "k_correct": 3, "k_copy": 3}
     kernels = {}
     for g, n in enumerate(names):
-        if ms[g] > 0:
-            kernels[n] = {"ms_per_launch": ms[g], "launches_per_step": per_step_launches.get(n, 0),
-                          "ms_per_step": ms[g] * per_step_launches.get(n, 0)}
+        if ms[g] > 0 and n != "k_nan_check":
+            per_step = cnt[g] / nt
+            kernels[n] = {"ms_per_launch": ms[g], "launches_per_step": per_step, "ms_per_step": ms[g] * per_step}
     tot = sum(k["ms_per_step"] for k in kernels.values()) or 1.0
     for k in kernels.values():
         k["share"] = k["ms_per_step"] / tot
     top = max(kernels, key=lambda n: kernels[n]["ms_per_step"])
     peak, peak_kind = measured_peak()
-    ab = algorithmic_bytes(top, size, s)
+    ab = algorithmic_bytes(top, size, s, **ab_kw)
     achieved = ab / (kernels[top]["ms_per_launch"] / 1e3) / 1e9
     roofline = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
@@ -301,12 +443,13 @@ def main():
     if prof:
         roofline.update(prof)
     for n, k in kernels.items():
-        b = algorithmic_bytes(n, size, s)
+        b = algorithmic_bytes(n, size, s, **ab_kw)
         k["achieved_gbs"] = b / (k["ms_per_launch"] / 1e3) / 1e9 if b else None
 
     # end to end through the C ABI with host buffers: upload the state, step, download
     e2e = None
-    fields = ["u", "v", "w", "b"] if args.e2e_steps > 0 else []
+    prognostic = ["u", "v"] + (["w"] if grid.topology[2] != "Flat" else []) + list(physics.get("tracers", ()))
+    fields = prognostic if args.e2e_steps > 0 else []
     host = {}
     for n in fields:
         shp = model.field_shape(n)
@@ -333,17 +476,23 @@ def main():
     if fields:
         e2e = {"value": cells * args.e2e_steps * world / e2e_el, "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-               "path": "gbo_set_field x4 (pinned host) + gbo_time_step(1) + gbo_get_field x4"}
+               "path": "gbo_set_field x%d (pinned host) + gbo_time_step(1) + gbo_get_field x%d" % (len(fields), len(fields))}
+
+    poisson = None
+    if isinstance(physics.get("pressure_solver"), og.ConjugateGradientPoissonSolver):
+        poisson = held_out_solves(model, grid, torch, stream, ft, n=50)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_sample()
+        cpu = cpu_sample(args.workload)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded numpy PCG64)",
-                "config": config_dict(size, args.dtype, world), "clocks": clk.summary(), "e2e": e2e,
+                "config": config_dict(args, world), "clocks": clk.summary(), "e2e": e2e,
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "kernels": kernels}
+        if poisson:
+            line["poisson_solve"] = poisson
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -62,6 +62,10 @@ enum gbo_precond    { GBO_PRECOND_FFT = 0, GBO_PRECOND_NONE = 1, GBO_PRECOND_LEA
 #define GBO_FIELD_KAPPA  103      /* AMD tracer diffusivity κₑ of tracer 0 */
 
 #define GBO_MAX_TRACERS 4
+/* Upper bound on conjugate-gradient iterations per pressure solve (the reference's
+ * default maxiter is the number of cells; the device loop also stops here and
+ * reports GBO_ERR_NOT_CONVERGED, so a stagnating solve ends in bounded time). */
+#define GBO_CG_MAX_ITERATIONS 20000
 
 /* Grid: replaces RectilinearGrid(size, x, y, z, topology) and
  * ImmersedBoundaryGrid(grid, GridFittedBottom(h))
@@ -210,6 +214,8 @@ int64_t gbo_kernel_launches(const gbo_model* m);
  * g < min(nmax, gbo_kernel_group_count()).  Advances the model like gbo_time_step. */
 int gbo_kernel_timings(gbo_model* m, double dt, int32_t nsteps, double* ms, int32_t nmax);
 int32_t gbo_kernel_group_count(void);
+/* Launches of each kernel group in the last gbo_kernel_timings pass (all its steps). */
+int gbo_kernel_timing_counts(const gbo_model* m, int64_t* n, int32_t nmax);
 const char* gbo_kernel_group_name(int32_t g);
 
 #ifdef __cplusplus

@@ -8,6 +8,7 @@
 
 #include "../../include/gbo.h"
 #include "gbo_fft.cuh"
+#include "gbo_cg.cuh"
 #include "gbo_fused.cuh"
 
 // ===========================================================================
@@ -104,159 +105,6 @@ __global__ void k_nan_check(const FT* __restrict__ a, size_t n, unsigned int* fl
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flags, GBO_FLAG_NAN);
 }
 
-
-// ===========================================================================
-// Conjugate-gradient Poisson solver on an immersed grid
-// (src/Solvers/conjugate_gradient_poisson_solver.jl:38-211;
-//  src/Solvers/conjugate_gradient_solver.jl:177-284).  Dot products and norms
-// accumulate in FP64; scalars live in device memory (CGS slots below).
-// ===========================================================================
-// scalar slots: ρ of even / odd iterations, p·q, Σx and Σr over active cells, ‖V⁻¹r‖², active cells
-enum { CG_RHO0 = 0, CG_RHO1, CG_PQ, CG_SX, CG_SR, CG_NORM2, CG_NACT, CG_NSLOTS };
-
-GBO_D double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-// block-reduce one or two doubles and add them to device scalars
-GBO_D void block_add(double a, double* da, double b = 0.0, double* db = nullptr) {
-    __shared__ double sa[32], sb[32];
-    int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
-    int wid = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
-    int nw = (blockDim.x * blockDim.y + 31) >> 5;
-    a = warp_sum(a);
-    b = warp_sum(b);
-    if (lane == 0) { sa[wid] = a; sb[wid] = b; }
-    __syncthreads();
-    if (wid == 0) {
-        a = lane < nw ? sa[lane] : 0.0;
-        b = lane < nw ? sb[lane] : 0.0;
-        a = warp_sum(a);
-        b = warp_sum(b);
-        if (lane == 0) {
-            atomicAdd(da, a);
-            if (db) atomicAdd(db, b);
-        }
-    }
-}
-
-// q = V∇²x with differences set to zero across faces touching immersed cells
-// (_symmetric_laplacian_operator!, conjugate_gradient_poisson_solver.jl:62-79 with
-// conditional_differences.jl:15-43).  Optionally accumulates Σ p·q.
-template <typename FT>
-__global__ void k_cg_laplacian(GridP<FT> g, const FT* __restrict__ x, FT* __restrict__ q, double* dot_pq) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    double acc = 0.0;
-    if (i < g.Nx && j < g.Ny) {
-        CFld<FT> X = cfld(x, g);
-        Met<FT> M(g);
-        FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
-        auto fx = [&](int ii) { return cond_zero(g, ii - 1, j, k, ii, j, k) ? FT(0) : Ax * ((X(ii, j, k) - X(ii - 1, j, k)) * g.rdx); };
-        auto fy = [&](int jj) { return cond_zero(g, i, jj - 1, k, i, jj, k) ? FT(0) : Ay * ((X(i, jj, k) - X(i, jj - 1, k)) * g.rdy); };
-        auto fz = [&](int kk) {
-            if (g.flatz) return FT(0);
-            return cond_zero(g, i, j, kk - 1, i, j, kk) ? FT(0) : Az * ((X(i, j, kk) - X(i, j, kk - 1)) * M.rdzf(kk));
-        };
-        FT val = (fx(i + 1) - fx(i)) + (fy(j + 1) - fy(j)) + (fz(k + 1) - fz(k));
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        q[idx] = val;
-        if (dot_pq) acc = (double)x[idx] * (double)val;
-    }
-    if (dot_pq) block_add(acc, dot_pq);
-}
-
-// elementwise helpers over N values (1-D grid-stride)
-template <typename FT>
-__global__ void k_cg_init(const FT* __restrict__ b, const FT* __restrict__ q, FT* __restrict__ r, size_t n) {
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) r[t] = b[t] - q[t];
-}
-template <typename FT>
-__global__ void k_cg_scale(const FT* __restrict__ a, FT* __restrict__ out, FT s, size_t n) {
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) out[t] = a[t] * s;
-}
-// ‖V⁻¹ r‖² (VolumeInverseNorm) and the preconditioner right-hand side V⁻¹ r, times
-// Δzᶜ for the Fourier-tridiagonal preconditioner (its solve! applies set_source_term!,
-// fourier_tridiagonal_poisson_solver.jl:231-281)
-template <typename FT>
-__global__ void k_cg_vinv(GridP<FT> g, const FT* __restrict__ r, FT* __restrict__ out, double* norm2, int dz_scale) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    double acc = 0.0;
-    if (i < g.Nx && j < g.Ny) {
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        Met<FT> M(g);
-        FT s = r[idx] * M.rVc(k);
-        if (out) out[idx] = dz_scale ? s * M.dzc(k) : s;
-        acc = (double)s * (double)s;
-    }
-    if (norm2) block_add(acc, norm2);
-}
-template <typename FT>
-__global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, size_t n, double* out) {
-    double acc = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-        acc += (double)a[t] * (double)b[t];
-    block_add(acc, out);
-}
-// p = z (first iteration) or z + (ρ/ρ_prev) p (conjugate_gradient_solver.jl:246-263)
-template <typename FT>
-__global__ void k_cg_update_p(const FT* __restrict__ z, FT* __restrict__ p, const double* rho, const double* rho_prev,
-                              int first, size_t n) {
-    const FT beta = first ? FT(0) : FT(*rho / *rho_prev);
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-        p[t] = first ? z[t] : z[t] + beta * p[t];
-}
-// x += α p, r -= α q with α = ρ / (p·q); accumulates the active-cell sums of x and r
-template <typename FT>
-__global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, const FT* __restrict__ p,
-                               const FT* __restrict__ q, const double* rho, double* s) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    double ax = 0.0, ar = 0.0;
-    if (i < g.Nx && j < g.Ny) {
-        const FT alpha = FT(*rho / s[CG_PQ]);
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        FT xv = x[idx] + alpha * p[idx];
-        FT rv = r[idx] - alpha * q[idx];
-        x[idx] = xv;
-        r[idx] = rv;
-        if (!inactive_cell(g, i, j, k)) { ax = xv; ar = rv; }
-    }
-    block_add(ax, s + CG_SX, ar, s + CG_SR);
-}
-// zero-mean gauge over active cells, immersed cells zeroed (enforce_zero_mean_gauge!,
-// conjugate_gradient_poisson_solver.jl:81-96); accumulates ‖V⁻¹ r‖²
-template <typename FT>
-__global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, double* s) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    double acc = 0.0;
-    if (i < g.Nx && j < g.Ny) {
-        const FT mx = FT(s[CG_SX] / s[CG_NACT]), mr = FT(s[CG_SR] / s[CG_NACT]);
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        const FT act = inactive_cell(g, i, j, k) ? FT(0) : FT(1);
-        x[idx] = (x[idx] - mx) * act;
-        FT rv = (r[idx] - mr) * act;
-        r[idx] = rv;
-        FT sv = rv * Met<FT>(g).rVc(k);
-        acc = (double)sv * (double)sv;
-    }
-    block_add(acc, s + CG_NORM2);
-}
-// number of active cells (for the gauge means)
-template <typename FT>
-__global__ void k_cg_count(GridP<FT> g, double* s) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    double a = (i < g.Nx && j < g.Ny && !inactive_cell(g, i, j, k)) ? 1.0 : 0.0;
-    block_add(a, s + CG_NACT);
-}
 
 // ===========================================================================
 // Host helpers
@@ -411,6 +259,7 @@ struct gbo_model {
     virtual int device_pointer(int field, void** p, int64_t* n) = 0;
     virtual int poisson_device(void* phi, const void* rhs) = 0;
     virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
+    virtual int timing_counts(int64_t* n, int nmax) const = 0;
     virtual void* stream_ptr() = 0;
     virtual int64_t launch_count() const = 0;
     int64_t count(int field) const {
@@ -495,6 +344,9 @@ struct ModelImpl : gbo_model {
     DBuf<double> cg_s;
     double* h_cgs = nullptr;
     int cg_status = GBO_OK;
+    cudaStream_t body_stream = nullptr;  // captures the CG loop body into a conditional node
+    int64_t body_launches = 0;           // kernels per CG iteration
+    double iters_seen = 0;               // CG_ITERS already accounted in `launches`
     PassP<FT> pp{};
     ThomasP tp{};
     int ZT = 32, XL = 8, YT = 16, TC = 16;
@@ -515,6 +367,7 @@ struct ModelImpl : gbo_model {
             b->free_();
         cg_s.free_();
         if (h_cgs) cudaFreeHost(h_cgs);
+        if (body_stream) cudaStreamDestroy(body_stream);
         for (auto* vec : {&c, &cs, &Gc, &kap})
             for (auto& b : *vec) b.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_kbot.free_();
@@ -598,11 +451,10 @@ struct ModelImpl : gbo_model {
             for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_x}) b->alloc(N);
             cg_s.alloc(CG_NSLOTS);
             GBO_CUDA(cudaMallocHost(&h_cgs, CG_NSLOTS * sizeof(double)));
-            k_cg_count<FT><<<grd(), blk(), 0, stream>>>(gp, cg_s.p);
+            GBO_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
+            k_cg_count<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_s.p);
             GBO_CUDA(cudaGetLastError());
             GBO_CUDA(cudaStreamSynchronize(stream));
-            // the iteration count decides on the host after each iteration: no graph
-            use_graph = false;
         }
     }
 
@@ -658,6 +510,7 @@ struct ModelImpl : gbo_model {
     // ------------------------------------------------------------------
     dim3 blk() const { return dim3(32, 8, 1); }
     dim3 grd() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, Nz); }
+    dim3 cg_grid() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, std::min(Nz, CG_ZSLICES)); }
 
     // kernel accounting: group of the next launch, launches per captured step,
     // optional per-group CUDA events (timing mode)
@@ -786,65 +639,131 @@ struct ModelImpl : gbo_model {
         return cg_iterate();
     }
 
+    // One CG iteration (iterate!, conjugate_gradient_solver.jl:202-235) and the stopping
+    // test; rb holds the preconditioner's right-hand side on entry.
+    void cg_body(double maxiter, cudaGraphConditionalHandle h, int use_handle) {
+        const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
+        const bool pc = desc.preconditioner == GBO_PRECOND_FFT;
+        const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
+        double* s = cg_s.p;
+        const FT* z = cg_r.p;
+        if (pc) {
+            poisson_solve(precond_solver);
+            z = rb.p;
+        }
+        pre(G_CG);
+        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s);
+        check_launch();
+        pre(G_CG);
+        k_cg_update_p<FT><<<lin, 256, 0, stream>>>(z, cg_d.p, s, N);
+        check_launch();
+        pre(G_CG);
+        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_d.p, cg_q.p, s);
+        check_launch();
+        pre(G_CG);
+        k_cg_update_xr<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_q.p, s);
+        check_launch();
+        pre(G_CG);
+        k_cg_gauge<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, pc ? rb.p : nullptr, s, dzs);
+        check_launch();
+        pre(G_CG);
+        k_cg_check<<<1, 1, 0, stream>>>(s, maxiter, h, use_handle);
+        check_launch();
+    }
+
+    void read_cg_scalars() {
+        GBO_CUDA(cudaMemcpyAsync(h_cgs, cg_s.p, CG_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));
+    }
+
     // solve!(x, ::ConjugateGradientSolver, b) on x = cg_x, b = cg_b
+    // (conjugate_gradient_solver.jl:177-197).  Under stream capture the loop becomes a
+    // conditional WHILE node whose body is captured on body_stream; otherwise the host
+    // reads the stop flag after each iteration.  Non-convergence is reported through
+    // CG_FAIL when the step (or solve) is synchronised.
     int cg_iterate() {
         const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
         const double rel = desc.cg_reltol > 0 ? desc.cg_reltol : std::sqrt(eps);
         const double abs_ = desc.cg_abstol > 0 ? desc.cg_abstol : std::sqrt(eps);
-        const int64_t maxiter = desc.cg_maxiter > 0 ? desc.cg_maxiter : (int64_t)N;
+        // maxiter defaults to the number of cells as in the reference; the device loop is
+        // additionally capped so that a stagnating solve ends in bounded time
+        const double maxiter = std::min((double)GBO_CG_MAX_ITERATIONS,
+                                        desc.cg_maxiter > 0 ? (double)desc.cg_maxiter : (double)N);
         const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
+        const bool pc = desc.preconditioner == GBO_PRECOND_FFT;
+        const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
         double* s = cg_s.p;
-        auto read_norm = [&]() {
-            GBO_CUDA(cudaMemcpyAsync(h_cgs, s, CG_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, stream));
-            GBO_CUDA(cudaStreamSynchronize(stream));
-            return std::sqrt(h_cgs[CG_NORM2]);
-        };
         pre(G_CG);
-        k_cg_laplacian<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_q.p, nullptr);
+        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_q.p, nullptr);
         check_launch();
         pre(G_CG);
         k_cg_init<FT><<<lin, 256, 0, stream>>>(cg_b.p, cg_q.p, cg_r.p, N);
         check_launch();
-        GBO_CUDA(cudaMemsetAsync(s + CG_NORM2, 0, sizeof(double), stream));
         pre(G_CG);
-        k_cg_vinv<FT><<<grd(), blk(), 0, stream>>>(gp, cg_r.p, nullptr, s + CG_NORM2, 0);
+        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, pc ? rb.p : nullptr, s, dzs);
         check_launch();
-        double norm = read_norm();
-        const double tol = std::max(rel * norm, abs_);
-        int64_t it = 0;
-        while (it < maxiter && norm > tol) {
-            const FT* z = cg_r.p;
-            if (desc.preconditioner == GBO_PRECOND_FFT) {
-                pre(G_CG);
-                k_cg_vinv<FT><<<grd(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, nullptr, precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL);
-                check_launch();
-                poisson_solve(precond_solver);
-                z = rb.p;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        GBO_CUDA(cudaStreamIsCapturing(stream, &cs));
+        if (cs == cudaStreamCaptureStatusActive) {
+            cudaGraph_t g = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            GBO_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+            cudaGraphConditionalHandle h;
+            GBO_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+            pre(G_CG);
+            k_cg_begin<<<1, 1, 0, stream>>>(s, rel, abs_, maxiter, h, 1);
+            check_launch();
+            GBO_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            GBO_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            GBO_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+            GBO_CUDA(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            struct Swap {  // launches go to `stream`: point it at the body stream meanwhile
+                cudaStream_t& a; cudaStream_t& b;
+                Swap(cudaStream_t& x, cudaStream_t& y) : a(x), b(y) { std::swap(a, b); }
+                ~Swap() { std::swap(a, b); }
+            };
+            const int64_t before = launches;
+            {
+                Swap sw(stream, body_stream);
+                cg_body(maxiter, h, 1);
             }
-            double* rho = s + ((it & 1) ? CG_RHO1 : CG_RHO0);
-            double* rho_prev = s + ((it & 1) ? CG_RHO0 : CG_RHO1);
-            GBO_CUDA(cudaMemsetAsync(rho, 0, sizeof(double), stream));
-            GBO_CUDA(cudaMemsetAsync(s + CG_PQ, 0, (CG_NORM2 - CG_PQ + 1) * sizeof(double), stream));
-            pre(G_CG);
-            k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, rho);
-            check_launch();
-            pre(G_CG);
-            k_cg_update_p<FT><<<lin, 256, 0, stream>>>(z, cg_d.p, rho, rho_prev, it == 0, N);
-            check_launch();
-            pre(G_CG);
-            k_cg_laplacian<FT><<<grd(), blk(), 0, stream>>>(gp, cg_d.p, cg_q.p, s + CG_PQ);
-            check_launch();
-            pre(G_CG);
-            k_cg_update_xr<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_q.p, rho, s);
-            check_launch();
-            pre(G_CG);
-            k_cg_gauge<FT><<<grd(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, s);
-            check_launch();
-            norm = read_norm();
-            ++it;
+            body_launches = launches - before;
+            launches = before;  // counted per executed iteration after the step
+            cudaGraph_t captured = nullptr;
+            GBO_CUDA(cudaStreamEndCapture(body_stream, &captured));
+            // the body must end with k_cg_check, the only node that can end the loop
+            size_t nodes = 0;
+            GBO_CUDA(cudaGraphGetNodes(body, nullptr, &nodes));
+            if ((int64_t)nodes != body_launches || body_launches < 2)
+                throw CudaError{cudaErrorInvalidValue, "CG loop body capture"};
+            return GBO_OK;
         }
-        last_iters = (int)it;
-        if (it >= maxiter && norm > tol) {
+        pre(G_CG);
+        k_cg_begin<<<1, 1, 0, stream>>>(s, rel, abs_, maxiter, 0, 0);
+        check_launch();
+        read_cg_scalars();
+        while (h_cgs[CG_CONT] != 0.0) {
+            cg_body(maxiter, 0, 0);
+            read_cg_scalars();
+        }
+        iters_seen = h_cgs[CG_ITERS];
+        last_iters = (int)h_cgs[CG_IT];
+        return cg_outcome();
+    }
+
+    // CG_FAIL (sticky) -> status; clears it
+    int cg_outcome() {
+        if (h_cgs[CG_FAIL] != 0.0) {
+            GBO_CUDA(cudaMemsetAsync(cg_s.p + CG_FAIL, 0, sizeof(double), stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
             err = "conjugate-gradient Poisson solver did not reach its tolerance within maxiter iterations";
             return GBO_ERR_NOT_CONVERGED;
         }
@@ -993,7 +912,20 @@ struct ModelImpl : gbo_model {
         k_nan_check<FT><<<std::min<size_t>((N + 255) / 256, 1024), 256, 0, stream>>>(u.p, N, d_flags);
         check_launch();
         int rc = sync();
+        if (cg) {  // iterations run inside the graph: account for them now
+            read_cg_scalars();
+            launches += body_launches * (int64_t)(h_cgs[CG_ITERS] - iters_seen);
+            iters_seen = h_cgs[CG_ITERS];
+            last_iters = (int)h_cgs[CG_IT];
+            int st = cg_outcome();
+            if (st != GBO_OK) cg_status = st;
+        }
         return rc != GBO_OK ? rc : cg_status;
+    }
+
+    int timing_counts(int64_t* n, int nmax) const override {
+        for (int g = 0; g < std::min(nmax, (int)GROUPS); ++g) n[g] = group_n[g];
+        return GBO_OK;
     }
 
     int timed_steps(double dt, int nsteps, double* ms, int nmax) override {
@@ -1319,6 +1251,11 @@ int gbo_kernel_timings(gbo_model* m, double dt, int32_t nsteps, double* ms, int3
 }
 
 int32_t gbo_kernel_group_count(void) { return GROUPS; }
+
+int gbo_kernel_timing_counts(const gbo_model* m, int64_t* n, int32_t nmax) {
+    if (!m || !n || nmax < 0) return GBO_ERR_INVALID;
+    return m->timing_counts(n, nmax);
+}
 
 const char* gbo_kernel_group_name(int32_t g) { return (g >= 0 && g < GROUPS) ? GROUP_NAMES[g] : ""; }
 

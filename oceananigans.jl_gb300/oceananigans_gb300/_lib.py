@@ -87,6 +87,7 @@ SIGNATURES = {
     "gbo_kernel_launches": (ctypes.c_int64, [_vp]),
     "gbo_kernel_timings": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_int32]),
     "gbo_kernel_group_count": (ctypes.c_int32, []),
+    "gbo_kernel_timing_counts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]),
     "gbo_kernel_group_name": (ctypes.c_char_p, [ctypes.c_int32]),
 }
 

@@ -38,12 +38,13 @@ void launch_fft_y(const PassP<FT>& P, int mode, int YT, size_t smem, cudaStream_
 }
 
 template <typename FT>
-void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, int TC, size_t smem, cudaStream_t st) {
-    k_thomas_z<FT><<<dim3((T.Nh + TC - 1) / TC, T.Ny), TC, smem, st>>>(P, T, TC);
+void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, cudaStream_t st) {
+    const size_t ncol = (size_t)T.Nh * T.Ny;
+    k_thomas_z<FT><<<(unsigned)((ncol + 127) / 128), 128, 0, st>>>(P, T);
 }
 
 template <typename FT>
-cudaError_t fft_set_smem(size_t sz, size_t sx, size_t sy, size_t stt) {
+cudaError_t fft_set_smem(size_t sz, size_t sx, size_t sy) {
     cudaError_t e = cudaSuccess;
     auto set = [&](const void* f, size_t b) {
         cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(b, 1));
@@ -55,7 +56,6 @@ cudaError_t fft_set_smem(size_t sz, size_t sx, size_t sy, size_t stt) {
     set((const void*)k_dct_z<FT, 0>, sz);
     set((const void*)k_rfft_x<FT, 0>, sx);
     set((const void*)k_fft_y<FT, 0>, sy);
-    set((const void*)k_thomas_z<FT>, stt);
     return e;
 }
 
@@ -63,7 +63,7 @@ cudaError_t fft_set_smem(size_t sz, size_t sx, size_t sy, size_t stt) {
     template void launch_dct_z<FT>(const PassP<FT>&, int, int, size_t, cudaStream_t);             \
     template void launch_rfft_x<FT>(const PassP<FT>&, int, int, size_t, cudaStream_t);            \
     template void launch_fft_y<FT>(const PassP<FT>&, int, int, size_t, cudaStream_t);             \
-    template void launch_thomas_z<FT>(const PassP<FT>&, const ThomasP&, int, size_t, cudaStream_t); \
-    template cudaError_t fft_set_smem<FT>(size_t, size_t, size_t, size_t);
+    template void launch_thomas_z<FT>(const PassP<FT>&, const ThomasP&, cudaStream_t);                  \
+    template cudaError_t fft_set_smem<FT>(size_t, size_t, size_t);
 INST(float)
 INST(double)

@@ -389,7 +389,15 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
 //   D_k = -(1/Δzᶠ_{k+1} + 1/Δzᶠ_k) - Δzᶜ_k (λx+λy).
 // The forward update is elided where |β| ≤ 10 eps (the singular (0,0) mode);
 // the (0,0) column then has its vertical mean removed, which is the reference's
-// `ϕ .- mean(ϕ)` applied in spectral space.  One thread per (kx, ky) column.
+// `ϕ .- mean(ϕ)` applied in spectral space.
+//
+// One thread per (kx, ky) column; a plane of the half spectrum is Nh·Ny
+// consecutive columns, so thread c of a level reads and writes column c of that
+// plane and every access is coalesced.  The forward sweep keeps its FP64
+// intermediates (the eliminated right-hand side and the ratios t_k) in a global
+// scratch laid out [level][column] (3·Nz·Nh·Ny doubles), which the backward sweep
+// reads in reverse: the sweep streams at HBM speed with full occupancy instead of
+// holding whole columns in shared memory.
 // ---------------------------------------------------------------------------
 struct ThomasP {
     int Nh, Ny, Nz;
@@ -399,22 +407,21 @@ struct ThomasP {
     const double* lx;     // λx, λy in FP64
     const double* ly;
     double scale;         // 1/(Nx Ny)
+    double* ws;           // scratch: 3 arrays of Nz * Nh * Ny doubles (re, im, t)
 };
 
 template <typename FT>
-__global__ void k_thomas_z(PassP<FT> P, ThomasP T, int TC) {
-    extern __shared__ unsigned char smem_raw[];
-    double* pre = reinterpret_cast<double*>(smem_raw);  // [Nz][TC]
-    double* pim = pre + (size_t)T.Nz * TC;
-    double* tt = pim + (size_t)T.Nz * TC;
-    const int c = threadIdx.x;
-    const int kx = blockIdx.x * TC + c;
-    const int ky = blockIdx.y;
-    if (kx >= T.Nh) return;
-    const size_t stride = (size_t)T.Nh * T.Ny;
-    Cx<FT>* col = P.cb + kx + (size_t)T.Nh * ky;
-    const double lam = T.lx[kx] + T.ly[ky];
+__global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
+    const size_t ncol = (size_t)T.Nh * T.Ny;
+    const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const int kx = (int)(c % T.Nh), ky = (int)(c / T.Nh);
     const int Nz = T.Nz;
+    double* wre = T.ws;
+    double* wim = T.ws + ncol * Nz;
+    double* wt = T.ws + 2 * ncol * Nz;
+    Cx<FT>* col = P.cb + c;
+    const double lam = T.lx[kx] + T.ly[ky];
     auto D = [&](int kr) {
         if (kr == 1) return -T.rdzf[2 + T.zoff] - T.dzc[1 + T.zoff] * lam;
         if (kr == Nz) return -T.rdzf[Nz + T.zoff] - T.dzc[Nz + T.zoff] * lam;
@@ -424,33 +431,43 @@ __global__ void k_thomas_z(PassP<FT> P, ThomasP T, int TC) {
     const double tiny = 10 * 2.220446049250313e-16;
     double beta = D(1);
     Cx<FT> f1 = col[0];
-    pre[c] = (double)f1.re / beta;
-    pim[c] = (double)f1.im / beta;
+    double pre = (double)f1.re / beta, pim = (double)f1.im / beta;
+    wre[c] = pre;
+    wim[c] = pim;
     for (int kr = 2; kr <= Nz; ++kr) {
-        double a = off(kr - 1);
-        double t = a / beta;
-        tt[(kr - 1) * TC + c] = t;
+        const double a = off(kr - 1);
+        const double t = a / beta;
+        const size_t at = c + ncol * (kr - 1);
+        wt[at] = t;
         beta = D(kr) - a * t;
-        Cx<FT> fk = col[stride * (kr - 1)];
-        double sre = ((double)fk.re - a * pre[(kr - 2) * TC + c]) / beta;
-        double sim = ((double)fk.im - a * pim[(kr - 2) * TC + c]) / beta;
-        bool dd = fabs(beta) > tiny;
-        pre[(kr - 1) * TC + c] = dd ? sre : 0.0;
-        pim[(kr - 1) * TC + c] = dd ? sim : 0.0;
+        const Cx<FT> fk = col[ncol * (kr - 1)];
+        const double sre = ((double)fk.re - a * pre) / beta;
+        const double sim = ((double)fk.im - a * pim) / beta;
+        const bool dd = fabs(beta) > tiny;
+        pre = dd ? sre : 0.0;
+        pim = dd ? sim : 0.0;
+        wre[at] = pre;
+        wim[at] = pim;
     }
+    // backward substitution; the (0,0) column keeps its solution for the mean
+    const bool mean_col = kx == 0 && ky == 0;
+    col[ncol * (Nz - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
     for (int kr = Nz - 1; kr >= 1; --kr) {
-        double t = tt[kr * TC + c];
-        pre[(kr - 1) * TC + c] -= t * pre[kr * TC + c];
-        pim[(kr - 1) * TC + c] -= t * pim[kr * TC + c];
+        const size_t at = c + ncol * (kr - 1);
+        const double t = wt[c + ncol * kr];
+        pre = wre[at] - t * pre;
+        pim = wim[at] - t * pim;
+        if (mean_col) { wre[at] = pre; wim[at] = pim; }
+        col[ncol * (kr - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
     }
-    double mre = 0, mim = 0;
-    if (kx == 0 && ky == 0) {
-        for (int k = 0; k < Nz; ++k) { mre += pre[k * TC + c]; mim += pim[k * TC + c]; }
+    if (mean_col) {
+        double mre = 0, mim = 0;
+        for (int k = 0; k < Nz; ++k) { mre += wre[c + ncol * k]; mim += wim[c + ncol * k]; }
         mre /= Nz;
         mim /= Nz;
+        for (int k = 0; k < Nz; ++k)
+            col[ncol * k] = cx((FT)((wre[c + ncol * k] - mre) * T.scale), (FT)((wim[c + ncol * k] - mim) * T.scale));
     }
-    for (int k = 0; k < Nz; ++k)
-        col[stride * k] = cx((FT)((pre[k * TC + c] - mre) * T.scale), (FT)((pim[k * TC + c] - mim) * T.scale));
 }
 
 // ---------------------------------------------------------------------------
@@ -460,5 +477,5 @@ __global__ void k_thomas_z(PassP<FT> P, ThomasP T, int TC) {
 template <typename FT> void launch_dct_z(const PassP<FT>& P, int inverse, int ZT, size_t smem, cudaStream_t st);
 template <typename FT> void launch_rfft_x(const PassP<FT>& P, int inverse, int XL, size_t smem, cudaStream_t st);
 template <typename FT> void launch_fft_y(const PassP<FT>& P, int mode, int YT, size_t smem, cudaStream_t st);
-template <typename FT> void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, int TC, size_t smem, cudaStream_t st);
-template <typename FT> cudaError_t fft_set_smem(size_t smem_z, size_t smem_x, size_t smem_y, size_t smem_t);
+template <typename FT> void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, cudaStream_t st);
+template <typename FT> cudaError_t fft_set_smem(size_t smem_z, size_t smem_x, size_t smem_y);

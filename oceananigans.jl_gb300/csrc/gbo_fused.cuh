@@ -641,3 +641,54 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
         nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * (Df * Df) * sqrt(FT(2) * Sig2);
     }
 }
+
+// ---------------------------------------------------------------------------
+// Anisotropic minimum dissipation νₑ (and κₑ of one tracer) on the same shared-
+// memory tile as k_smagorinsky_tiled: u, v, w and the tracer are staged once on a
+// (32+2) x (8+2) x (KT+2) box (halo synthesis at load) and amd_point (the
+// arithmetic of k_amd) reads them through tile accessors with global indices.
+// ---------------------------------------------------------------------------
+namespace smag {
+template <typename FT>
+struct TileFld {  // global (i, j, k) -> tile cell of the block at (i0, j0, k0)
+    const FT* a;
+    int i0, j0, k0;
+    GBO_D FT operator()(int i, int j, int k) const { return a[bidx(i - i0, j - j0, k - k0)]; }
+};
+template <typename FT>
+struct TileFields {
+    TileFld<FT> u, v, nu, phy, w;
+};
+}  // namespace smag
+
+template <typename FT>
+__global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
+    using namespace smag;
+    extern __shared__ unsigned char smem_raw[];
+    Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
+    const GridP<FT>& g = P.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g);
+    WFld<FT> Wg = wfld(P.w, g);
+    const bool has_c = P.c != nullptr;
+    for (int e = tid; e < BS; e += TX * TY) {
+        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
+        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
+        s.u[e] = Ug(gi, gj, gk);
+        s.v[e] = Vg(gi, gj, gk);
+        s.w[e] = Wg(gi, gj, gk);
+        s.b[e] = has_c ? Cg(gi, gj, gk) : FT(0);
+    }
+    __syncthreads();
+    const int i = i0 + tx, j = j0 + ty;
+    if (i >= g.Nx || j >= g.Ny) return;
+    const TileFld<FT> tu{s.u, i0, j0, k0}, tv{s.v, i0, j0, k0}, tw{s.w, i0, j0, k0}, tc{s.b, i0, j0, k0};
+    const TileFields<FT> F{tu, tv, tu, tu, tw};
+    const StrainT<FT, TileFields<FT>> S(g, F);
+    for (int z = 0; z < KT; ++z) {
+        const int k = k0 + z;
+        if (k >= g.Nz) break;
+        amd_point<FT>(P, g, S, tc, has_c, i, j, k, i + (size_t)g.Nx * (j + (size_t)g.Ny * k), nu_out, kap_out);
+    }
+}

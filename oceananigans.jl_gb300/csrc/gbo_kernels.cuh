@@ -75,12 +75,12 @@ __global__ void k_smagorinsky(StepP<FT> P, FT* __restrict__ nu_out) {
 // normalised gradients velocity_tracer_gradients.jl:120-250).  Filter widths are
 // twice the cell-centre spacings at the evaluation index, as the reference uses.
 // ---------------------------------------------------------------------------
-template <typename FT>
+template <typename FT, class ST = Strain<FT>>
 struct AMD {
     const GridP<FT>& g;
-    const Strain<FT>& S;
+    const ST& S;
     Met<FT> M;
-    GBO_D AMD(const GridP<FT>& gg, const Strain<FT>& s) : g(gg), S(s), M(gg) {}
+    GBO_D AMD(const GridP<FT>& gg, const ST& s) : g(gg), S(s), M(gg) {}
     GBO_D FT Dfx() const { return FT(2) * g.dx; }
     GBO_D FT Dfy() const { return FT(2) * g.dy; }
     GBO_D FT Dfz(int k) const { return FT(2) * M.dzc(k); }
@@ -102,16 +102,11 @@ struct AMD {
 #define GBO_IY(f) (FT(0.5) * ((f)(i, j, k) + (f)(i, j + 1, k)))
 #define GBO_IZ(f) (FT(0.5) * ((f)(i, j, k) + (f)(i, j, k + 1)))
 
-template <typename FT>
-__global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
-    const GridP<FT>& g = P.g;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    if (i >= g.Nx || j >= g.Ny) return;
-    Fields<FT> F{cfld(P.u, g), cfld(P.v, g), cfld(P.nu, g), cfld(P.phy, g), wfld(P.w, g)};
-    Strain<FT> S(g, F);
-    AMD<FT> A(g, S);
+// νₑ and (with a tracer accessor c) κₑ at one cell from strain S and tracer c.
+template <typename FT, class ST, class CF>
+GBO_D void amd_point(const StepP<FT>& P, const GridP<FT>& g, const ST& S, const CF& c, bool has_c, int i, int j, int k,
+                     size_t idx, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
+    AMD<FT, ST> A(g, S);
     Met<FT> M(g);
     auto sq = [](FT x) { return x * x; };
     auto dxv2 = [&](int a, int b, int c) { return sq(A.n_dxv(a, b, c)); };
@@ -120,7 +115,6 @@ __global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap
     auto dzu2 = [&](int a, int b, int c) { return sq(A.n_dzu(a, b, c)); };
     auto dyw2 = [&](int a, int b, int c) { return sq(A.n_dyw(a, b, c)); };
     auto dzv2 = [&](int a, int b, int c) { return sq(A.n_dzv(a, b, c)); };
-    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
     FT S11 = S.S11(i, j, k), S22 = S.S22(i, j, k), S33 = S.S33(i, j, k);
     FT q = sq(S11) + sq(S22) + sq(S33) + GBO_IXY(dxv2) + GBO_IXY(dyu2) + GBO_IXZ(dxw2) + GBO_IXZ(dzu2) +
            GBO_IYZ(dyw2) + GBO_IYZ(dzv2);
@@ -152,8 +146,7 @@ __global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap
         nsgs = -P.C * d2 * (r - FT(0)) / q;
     }
     nu_out[idx] = fmax(FT(0), nsgs);
-    if (kap_out && P.c) {
-        CFld<FT> c = cfld(P.c, g);
+    if (kap_out && has_c) {
         auto n_dxc = [&](int a, int b, int cc) { return A.Dfx() * ((c(a, b, cc) - c(a - 1, b, cc)) * g.rdx); };
         auto n_dyc = [&](int a, int b, int cc) { return A.Dfy() * ((c(a, b, cc) - c(a, b - 1, cc)) * g.rdy); };
         auto n_dzc = [&](int a, int b, int cc) { return A.Dfz(cc) * ((c(a, b, cc) - c(a, b, cc - 1)) * M.rdzf(cc)); };
@@ -180,6 +173,19 @@ __global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap
         }
         kap_out[idx] = fmax(FT(0), ksgs);
     }
+}
+
+template <typename FT>
+__global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
+    const GridP<FT>& g = P.g;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= g.Nx || j >= g.Ny) return;
+    Fields<FT> F{cfld(P.u, g), cfld(P.v, g), cfld(P.nu, g), cfld(P.phy, g), wfld(P.w, g)};
+    Strain<FT> S(g, F);
+    CFld<FT> c = cfld(P.c, g);
+    amd_point<FT>(P, g, S, c, P.c != nullptr, i, j, k, i + (size_t)g.Nx * (j + (size_t)g.Ny * k), nu_out, kap_out);
 }
 
 // ---------------------------------------------------------------------------

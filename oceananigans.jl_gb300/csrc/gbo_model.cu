@@ -330,7 +330,7 @@ struct ModelImpl : gbo_model {
     std::vector<DBuf<FT>> c, cs, Gc, kap;
     // grid tables
     DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf;
-    DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64;
+    DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64, t_ws;
     DBuf<int> t_kbot;
     ZGrid<FT> Z;
     GridP<FT> gp{};
@@ -349,9 +349,9 @@ struct ModelImpl : gbo_model {
     double iters_seen = 0;               // CG_ITERS already accounted in `launches`
     PassP<FT> pp{};
     ThomasP tp{};
-    int ZT = 32, XL = 8, YT = 16, TC = 16;
+    int ZT = 32, XL = 8, YT = 16;
     int kchunk = 16;  // levels marched per block by the fused momentum kernel
-    size_t smem_z = 0, smem_x = 0, smem_y = 0, smem_t = 0;
+    size_t smem_z = 0, smem_x = 0, smem_y = 0;
     // flags
     unsigned int* d_flags = nullptr;
     unsigned int* h_flags = nullptr;
@@ -370,7 +370,7 @@ struct ModelImpl : gbo_model {
         if (body_stream) cudaStreamDestroy(body_stream);
         for (auto* vec : {&c, &cs, &Gc, &kap})
             for (auto& b : *vec) b.free_();
-        t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_kbot.free_();
+        t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_ws.free_(); t_kbot.free_();
         for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -487,6 +487,13 @@ struct ModelImpl : gbo_model {
         tp.rdzf = t_rdzf64.p; tp.dzc = t_dzc64.p; tp.zoff = Z.zoff;
         tp.lx = t_lx64.p; tp.ly = t_ly64.p;
         tp.scale = 1.0 / ((double)Nx * Ny);
+        // FP64 work space of the Thomas sweep, for models that use the Fourier-tridiagonal solver
+        // (as the pressure solver or as the CG preconditioner on a stretched grid)
+        if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ||
+            (desc.pressure_solver == GBO_SOLVER_CONJUGATE_GRADIENT && precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL)) {
+            t_ws.alloc((size_t)3 * Nz * Nh * Ny);
+            tp.ws = t_ws.p;
+        }
         // shared-memory tiles: keep each block at or below ~100 KB
         const size_t cs_ = sizeof(C), lim = 100 * 1024;
         ZT = 32;
@@ -498,13 +505,11 @@ struct ModelImpl : gbo_model {
         YT = 16;
         while (YT > 1 && (size_t)2 * YT * Ny * cs_ > lim) YT /= 2;
         smem_y = (size_t)2 * YT * Ny * cs_;
-        TC = 32;
-        while (TC > 1 && (size_t)3 * Nz * TC * sizeof(double) > lim) TC /= 2;
-        smem_t = (size_t)3 * Nz * TC * sizeof(double);
         GBO_CUDA(fused_set_smem<FT>());
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         kchunk = flat ? 1 : std::min(16, Nz);
-        GBO_CUDA(fft_set_smem<FT>(smem_z, smem_x, smem_y, smem_t));
+        GBO_CUDA(fft_set_smem<FT>(smem_z, smem_x, smem_y));
     }
 
     // ------------------------------------------------------------------
@@ -568,7 +573,7 @@ struct ModelImpl : gbo_model {
             launch_fft_y<FT>(pp, 1, YT, smem_y, stream);
             check_launch();
             pre(G_THOMAS);
-            launch_thomas_z<FT>(pp, tp, TC, smem_t, stream);
+            launch_thomas_z<FT>(pp, tp, stream);
             check_launch();
             pre(G_FFT_Y);
             launch_fft_y<FT>(pp, 2, YT, smem_y, stream);
@@ -775,22 +780,23 @@ struct ModelImpl : gbo_model {
     // tendencies read.  Run after every projection, as the reference does.
     void auxiliaries() {
         StepP<FT> P = params();
+        const dim3 sgrid((Nx + smag::TX - 1) / smag::TX, (Ny + smag::TY - 1) / smag::TY, (Nz + smag::KT - 1) / smag::KT);
+        const dim3 sblock(smag::TX, smag::TY);
         if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
             pre(G_CLOSURE);
-            k_smagorinsky_tiled<FT><<<dim3((Nx + smag::TX - 1) / smag::TX, (Ny + smag::TY - 1) / smag::TY, (Nz + smag::KT - 1) / smag::KT),
-                                      dim3(smag::TX, smag::TY), sizeof(smag::Smem<FT>), stream>>>(P, nu.p);
+            k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(P, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;
             Q.c = ntr > 0 ? c[0].p : nullptr;
             pre(G_CLOSURE);
-            k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
+            k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
             check_launch();
             for (int n = 1; n < ntr; ++n) {
                 Q.c = c[n].p;
                 // viscosity recomputed identically; only κₑ of tracer n is new
                 pre(G_CLOSURE);
-                k_amd<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p, kap[n].p);
+                k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, kap[n].p);
                 check_launch();
             }
         }

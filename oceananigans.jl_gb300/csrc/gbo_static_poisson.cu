@@ -192,7 +192,7 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
                     (long long)std::max({smem_z, smem_x, smem_y}), optin);
     // Raise (never lower) the pass kernels' dynamic shared-memory limit: the kernels are
     // shared with models, which set their own, smaller limits when they are created.
-    rc = fft_set_smem<FT>(optin, optin, optin, optin);
+    rc = fft_set_smem<FT>(optin, optin, optin);
     if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaFuncSetAttribute failed (error %lld)", (long long)rc);
 
     if (phi != rhs) {

@@ -199,12 +199,14 @@ struct MomentumFluxes {
 // Closure: strain components and eddy-viscosity interpolations
 // (velocity_tracer_gradients.jl:1-60; abstract_scalar_diffusivity_closure.jl:330-366)
 // ---------------------------------------------------------------------------
-template <typename FT>
-struct Strain {
+// FL supplies u, v, w, nu accessors taking global indices: the global-memory Fields
+// (halos synthesised at load) or a shared-memory tile.
+template <typename FT, class FL = Fields<FT>>
+struct StrainT {
     const GridP<FT>& g;
-    const Fields<FT>& F;
+    const FL& F;
     Met<FT> M;
-    GBO_D Strain(const GridP<FT>& gg, const Fields<FT>& ff) : g(gg), F(ff), M(gg) {}
+    GBO_D StrainT(const GridP<FT>& gg, const FL& ff) : g(gg), F(ff), M(gg) {}
     GBO_D FT S11(int i, int j, int k) const { return (F.u(i + 1, j, k) - F.u(i, j, k)) * g.rdx; }
     GBO_D FT S22(int i, int j, int k) const { return (F.v(i, j + 1, k) - F.v(i, j, k)) * g.rdy; }
     GBO_D FT S33(int i, int j, int k) const { return g.flatz ? FT(0) : (F.w(i, j, k + 1) - F.w(i, j, k)) * M.rdzc(k); }
@@ -236,3 +238,5 @@ struct Strain {
     GBO_D FT tau_vz(int i, int j, int k) const { return FT(-2) * (nu_cff(i, j, k) * S23(i, j, k)); }
     GBO_D FT tau_wz(int i, int j, int k) const { return FT(-2) * (F.nu(i, j, k) * S33(i, j, k)); }
 };
+template <typename FT>
+using Strain = StrainT<FT>;

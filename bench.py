@@ -125,6 +125,30 @@ def _seamount(size, float_type):
     return grid, physics, init
 
 
+def ensemble_specs(n=64, float_type=np.float32, seed=2025):
+    """Members of the ensemble workload: Nx = Ny from {64, 96, 128}, Nz from {32, 48, 64},
+    N² log-uniform on [1e-6, 1e-4] s⁻², surface flux uniform on [1e-9, 1e-7] m² s⁻³."""
+    import oceananigans_gb300 as og
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        Nh = int(rng.choice([64, 96, 128]))
+        Nz = int(rng.choice([32, 48, 64]))
+        N2 = float(10 ** rng.uniform(-6, -4))
+        flux = float(rng.uniform(1e-9, 1e-7))
+        grid = og.RectilinearGrid(size=(Nh, Nh, Nz), x=(0, 2.0 * Nh), y=(0, 2.0 * Nh), z=(-2.0 * Nz, 0.0),
+                                  topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+        physics = dict(advection=og.WENO(), closure=og.SmagorinskyLilly(), buoyancy=og.BuoyancyTracer(),
+                       tracers=("b",),
+                       boundary_conditions={"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(flux))})
+        _, _, zc = grid.nodes()
+        init = {"u": 1e-3 * rng.uniform(-1, 1, (Nh, Nh, Nz)), "v": 1e-3 * rng.uniform(-1, 1, (Nh, Nh, Nz)),
+                "w": 1e-3 * rng.uniform(-1, 1, (Nh, Nh, Nz + 1)),
+                "b": N2 * zc[None, None, :] + 1e-8 * rng.standard_normal((Nh, Nh, Nz))}
+        specs.append((grid, physics, init))
+    return specs
+
+
 WORKLOADS = {
     "convection": dict(build=_convection, size=(256, 256, 128), dtype="f32", dt=2.0, cpu_size=(128, 128, 128),
                        name="free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft"),
@@ -132,6 +156,8 @@ WORKLOADS = {
                          name="turbulence2d_%dx%dx%d_weno5_fft"),
     "stretched_amd": dict(build=_stretched_amd, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),
                           name="stretched_convection_%dx%dx%d_weno5_amd_fourier_tridiagonal"),
+    "ensemble": dict(build=None, size=(0, 0, 0), dtype="f32", dt=1.0, cpu_size=(128, 128, 128),
+                     name="ensemble_64_members_convection_smagorinsky_fft"),
     "seamount": dict(build=_seamount, size=(256, 256, 128), dtype="f32", dt=20.0, cpu_size=(64, 64, 128),
                      name="seamount_ibg_%dx%dx%d_weno5_fft_pcg"),
 }
@@ -141,8 +167,17 @@ def workload(name, size, float_type):
     return WORKLOADS[name]["build"](size, float_type)
 
 
+def workload_cells(args):
+    if args.workload == "ensemble":
+        return float(sum(np.prod(g.size()) for g, _, _ in ensemble_specs()))
+    return float(np.prod(args.size))
+
+
 def config_dict(args, n):
     w = WORKLOADS[args.workload]
+    if args.workload == "ensemble":
+        return {"workload": w["name"], "members": 64, "dt_s": w["dt"], "float": args.dtype,
+                "parallelism": "replicas%d" % n}
     size = args.size
     s = 4 if args.dtype == "f32" else 8
     return {"workload": w["name"] % tuple(size), "grid": list(size), "dt_s": w["dt"], "float": args.dtype,
@@ -166,7 +201,8 @@ def cpu_sample(name, steps_budget_s=20.0):
     w = WORKLOADS[name]
     size = w["cpu_size"]
     dt = w["dt"]
-    grid, physics, init = workload(name, size, np.float64)
+    # the ensemble's members carry the convection physics
+    grid, physics, init = workload("convection" if name == "ensemble" else name, size, np.float64)
     d = grid.descriptor()
     g = oracle.GridDesc()
     for f, _ in oracle.GridDesc._fields_:
@@ -307,7 +343,7 @@ def run_reference(args):
     value = statistics.median(samples)
     cpu["value"] = value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * np.prod(size) / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * workload_cells(args) / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "config": config_dict(args, args.gpus),
             "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -357,6 +393,109 @@ def held_out_solves(model, grid, torch, stream, ft, n=50):
             "path": "gbo_poisson_solve_device from a zero initial guess (host reads the stop flag each iteration)"}
 
 
+def run_ensemble(args, torch, og, L, lib, local):
+    """64 uneven members advanced by one graph launch per step, against the same
+    members stepped one after another (each with its own step graph)."""
+    ft = np.float32 if args.dtype == "f32" else np.float64
+    dt = WORKLOADS["ensemble"]["dt"]
+    specs = ensemble_specs(64, ft)
+    ens = og.Ensemble([(g, p) for g, p, _ in specs])
+    for mm, (_, _, init) in zip(ens.members, specs):
+        og.set_(mm, **init)
+    cells = float(sum(np.prod(g.size()) for g, _, _ in specs))
+    sp = ctypes.c_void_p()
+    lib.gbo_ensemble_stream(ens._h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    ens.time_step(dt, args.warmup)
+    launches0 = sum(lib.gbo_kernel_launches(mm._h) for mm in ens.members)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        ens.time_step(dt, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    launches = sum(lib.gbo_kernel_launches(mm._h) for mm in ens.members) - launches0
+    value = cells * args.steps / elapsed
+    # the same members one after another (separate models, each its own graph per step)
+    singles = []
+    for g, p, init in specs:
+        s = og.NonhydrostaticModel(g, **p)
+        og.set_(s, **init)
+        og.time_step_(s, dt, 1)
+        singles.append(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in singles:
+        og.time_step_(s, dt, args.steps)
+    torch.cuda.synchronize()
+    seq = cells * args.steps / (time.perf_counter() - t0)
+    del singles
+    # per-kernel timings and the roofline on the largest member
+    big = max(range(len(specs)), key=lambda i: np.prod(specs[i][0].size()))
+    g, p, _ = specs[big]
+    mm = ens.members[big]
+    ng = lib.gbo_kernel_group_count()
+    ms = (ctypes.c_double * ng)()
+    cnt = (ctypes.c_int64 * ng)()
+    L.check(lib.gbo_kernel_timings(mm._h, dt, 2, ms, ng), mm._h)
+    L.check(lib.gbo_kernel_timing_counts(mm._h, cnt, ng), mm._h)
+    s_ = 4 if ft == np.float32 else 8
+    kernels = {}
+    for gi in range(ng):
+        n = lib.gbo_kernel_group_name(gi).decode()
+        if ms[gi] > 0 and n != "k_nan_check":
+            b = algorithmic_bytes(n, g.size(), s_)
+            kernels[n] = {"ms_per_launch": ms[gi], "launches_per_step": cnt[gi] / 2, "ms_per_step": ms[gi] * cnt[gi] / 2,
+                          "achieved_gbs": b / (ms[gi] / 1e3) / 1e9 if b else None}
+    top = max(kernels, key=lambda n: kernels[n]["ms_per_step"])
+    peak, peak_kind = measured_peak()
+    ab = algorithmic_bytes(top, g.size(), s_)
+    achieved = ab / (kernels[top]["ms_per_launch"] / 1e3) / 1e9
+    roofline = {"kernel": top, "member_grid": list(g.size()), "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": ab}
+    # end to end: upload every member's prognostic fields, one ensemble step, download
+    code = L.GBO_FLOAT32 if ft == np.float32 else L.GBO_FLOAT64
+    host = []
+    for mm in ens.members:
+        for n in ("u", "v", "w", "b"):
+            t = torch.empty(int(np.prod(mm.field_shape(n))), dtype=torch.float32 if ft == np.float32 else torch.float64,
+                            pin_memory=True)
+            L.check(lib.gbo_get_field(mm._h, mm._fid(n), t.data_ptr(), code, t.numel()), mm._h)
+            host.append((mm, n, t))
+    nbytes = sum(t.numel() * t.element_size() for _, _, t in host)
+    e2e = None
+    if args.e2e_steps > 0:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            for mm, n, t in host:
+                L.check(lib.gbo_set_field(mm._h, mm._fid(n), t.data_ptr(), code, t.numel()), mm._h)
+            ens.time_step(dt, 1)
+            for mm, n, t in host:
+                L.check(lib.gbo_get_field(mm._h, mm._fid(n), t.data_ptr(), code, t.numel()), mm._h)
+        e2e = {"value": cells * args.e2e_steps / (time.perf_counter() - t0), "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "path": "gbo_set_field + gbo_ensemble_time_step(1) + gbo_get_field for all 64 members"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_sample("convection", steps_budget_s=20.0)
+        cpu["sample"] = "ensemble members share the convection physics; " + cpu["sample"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded numpy PCG64)",
+            "config": {"workload": WORKLOADS["ensemble"]["name"], "members": len(specs), "cells": int(cells),
+                       "dt_s": dt, "float": args.dtype, "parallelism": "replicas1",
+                       "l2_policy": "inputs larger than L2 (%.0f MB of state)" % (cells * 20 * s_ / 1e6)},
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+            "cpu_baseline": cpu, "kernels": kernels,
+            "sequential": {"value": seq, "unit": UNIT, "speedup_of_batched": value / seq,
+                           "path": "the same 64 models stepped one after another"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -373,6 +512,10 @@ def main():
     import oceananigans_gb300 as og
     from oceananigans_gb300 import _lib as L
     lib = og.load()
+    if args.workload == "ensemble":
+        if rank == 0:
+            run_ensemble(args, torch, og, L, lib, local)
+        return
     size = tuple(args.size)
     ft = np.float32 if args.dtype == "f32" else np.float64
     s = 4 if ft == np.float32 else 8

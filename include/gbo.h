@@ -165,6 +165,26 @@ const char* gbo_version(void);
  * (src/Solvers/conjugate_gradient_poisson_solver.jl; the rhs there is V·div). */
 int gbo_poisson_solve_device(gbo_model* m, void* phi_device, const void* rhs_device);
 
+/* ---- ensembles ---------------------------------------------------------------
+ * No counterpart in the reference, which advances models one at a time.  An
+ * ensemble owns n independent models (each created as by gbo_model_create from
+ * grids[i], descs[i]; sizes and physics may differ) and advances all of them with
+ * one CUDA graph launch per step: every member's step is a parallel branch of the
+ * graph, so small members share the GPU instead of running back to back.
+ * Members are ordinary handles for gbo_set_field / gbo_set_finalize /
+ * gbo_get_field / gbo_clock; they belong to the ensemble (never pass them to
+ * gbo_model_destroy) and are stepped only through gbo_ensemble_time_step. */
+typedef struct gbo_ensemble gbo_ensemble;
+int gbo_ensemble_create(int32_t n, const gbo_grid_desc* grids, const gbo_model_desc* descs, gbo_ensemble** out);
+void gbo_ensemble_destroy(gbo_ensemble* e);
+int32_t gbo_ensemble_size(const gbo_ensemble* e);
+gbo_model* gbo_ensemble_member(gbo_ensemble* e, int32_t i);
+/* The cudaStream_t (as void*) on which the ensemble graph is launched (instrumentation). */
+int gbo_ensemble_stream(gbo_ensemble* e, void** stream);
+/* Advance every member by nsteps steps of dt; returns the first member error (NaN,
+ * CG non-convergence) after all members finished, with gbo_last_error(NULL) naming it. */
+int gbo_ensemble_time_step(gbo_ensemble* e, double dt, int32_t nsteps);
+
 /* ---- allocation-free FFT Poisson solve --------------------------------------
  * No counterpart in the reference: Oceananigans allocates the FFT solver's work
  * arrays when FFTBasedPoissonSolver(grid) is built, and gbo_poisson_solve_device

@@ -434,13 +434,13 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
     double pre = (double)f1.re / beta, pim = (double)f1.im / beta;
     wre[c] = pre;
     wim[c] = pim;
-    for (int kr = 2; kr <= Nz; ++kr) {
+    // forward elimination of level kr (1-based) with right-hand side fk
+    auto forward = [&](int kr, Cx<FT> fk) {
         const double a = off(kr - 1);
         const double t = a / beta;
         const size_t at = c + ncol * (kr - 1);
         wt[at] = t;
         beta = D(kr) - a * t;
-        const Cx<FT> fk = col[ncol * (kr - 1)];
         const double sre = ((double)fk.re - a * pre) / beta;
         const double sim = ((double)fk.im - a * pim) / beta;
         const bool dd = fabs(beta) > tiny;
@@ -448,18 +448,40 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
         pim = dd ? sim : 0.0;
         wre[at] = pre;
         wim[at] = pim;
+    };
+    // the loads of four levels are issued together (they do not depend on the recurrence)
+    int kr = 2;
+    for (; kr + 3 <= Nz; kr += 4) {
+        Cx<FT> f[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) f[q] = col[ncol * (kr - 1 + q)];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) forward(kr + q, f[q]);
     }
+    for (; kr <= Nz; ++kr) forward(kr, col[ncol * (kr - 1)]);
     // backward substitution; the (0,0) column keeps its solution for the mean
     const bool mean_col = kx == 0 && ky == 0;
     col[ncol * (Nz - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
-    for (int kr = Nz - 1; kr >= 1; --kr) {
-        const size_t at = c + ncol * (kr - 1);
-        const double t = wt[c + ncol * kr];
-        pre = wre[at] - t * pre;
-        pim = wim[at] - t * pim;
+    auto backward = [&](int kq, double r, double i, double t) {
+        pre = r - t * pre;
+        pim = i - t * pim;
+        const size_t at = c + ncol * (kq - 1);
         if (mean_col) { wre[at] = pre; wim[at] = pim; }
-        col[ncol * (kr - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
+        col[ncol * (kq - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
+    };
+    kr = Nz - 1;
+    for (; kr - 3 >= 1; kr -= 4) {
+        double r[4], i[4], t[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            r[q] = wre[c + ncol * (kr - q - 1)];
+            i[q] = wim[c + ncol * (kr - q - 1)];
+            t[q] = wt[c + ncol * (kr - q)];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) backward(kr - q, r[q], i[q], t[q]);
     }
+    for (; kr >= 1; --kr) backward(kr, wre[c + ncol * (kr - 1)], wim[c + ncol * (kr - 1)], wt[c + ncol * kr]);
     if (mean_col) {
         double mre = 0, mim = 0;
         for (int k = 0; k < Nz; ++k) { mre += wre[c + ncol * k]; mim += wim[c + ncol * k]; }

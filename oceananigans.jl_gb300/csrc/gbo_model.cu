@@ -261,6 +261,9 @@ struct gbo_model {
     virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
     virtual int timing_counts(int64_t* n, int nmax) const = 0;
     virtual void* stream_ptr() = 0;
+    virtual int64_t capture_step(double dt) = 0;
+    virtual void add_launches(int64_t n) = 0;
+    virtual int finish_steps(double dt, int nsteps) = 0;
     virtual int64_t launch_count() const = 0;
     int64_t count(int field) const {
         int64_t plane = (int64_t)Nx * Ny;
@@ -509,7 +512,14 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         kchunk = flat ? 1 : std::min(16, Nz);
-        GBO_CUDA(fft_set_smem<FT>(smem_z, smem_x, smem_y));
+        // The pass kernels are shared by every model in the process: allow them the device's
+        // opt-in maximum rather than this model's sizes, so a model created later never
+        // lowers the limit an earlier, larger model needs.
+        int optin = 0;
+        GBO_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        if ((size_t)optin < std::max({smem_z, smem_x, smem_y}))
+            throw InvalidArg{"grid too large for the shared-memory tiles of the spectral Poisson solver"};
+        GBO_CUDA(fft_set_smem<FT>(optin, optin, optin));
     }
 
     // ------------------------------------------------------------------
@@ -909,6 +919,22 @@ struct ModelImpl : gbo_model {
             }
             cg_status = worst;
         }
+        return finish_steps(dt, nsteps);
+    }
+
+    // Record one time step on this model's stream while it is joined to another
+    // stream's capture (ensemble graphs); returns the kernels recorded.
+    int64_t capture_step(double dt) override {
+        const int64_t before = launches;
+        full_step(dt);
+        const int64_t n = launches - before;
+        launches = before;
+        return n;
+    }
+    void add_launches(int64_t n) override { launches += n; }
+
+    // After nsteps steps were issued: clock, NaN check, synchronisation, CG bookkeeping.
+    int finish_steps(double dt, int nsteps) override {
         for (int s = 0; s < nsteps; ++s) {
             // clock: tⁿ⁺¹ = tⁿ + Δt computed a priori (runge_kutta_3.jl:122,160-161)
             time = time + dt;
@@ -1219,6 +1245,145 @@ int gbo_time_step(gbo_model* m, double dt, int32_t nsteps) {
     if (!m) return GBO_ERR_INVALID;
     if (!(dt > 0) || !std::isfinite(dt)) { m->err = "dt must be positive and finite"; return GBO_ERR_INVALID; }
     return guarded(m, [&]() { return m->step(dt, nsteps); });
+}
+
+// ---------------------------------------------------------------------------
+// Ensemble: independent models advanced together.  One time step of every member
+// is captured into one CUDA graph as parallel branches (each member's stream is
+// forked from the ensemble's stream with an event and joined back), so a single
+// graph launch advances all members and the members of different sizes fill the
+// GPU together.  No reference counterpart (the reference steps models one by one).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct gbo_ensemble {
+    std::vector<gbo_model*> members;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = -1;
+    std::vector<int64_t> per_step;  // kernels each member records per step
+    std::string err;
+
+    ~gbo_ensemble() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (cudaEvent_t e : joins) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (done) cudaEventDestroy(done);
+        if (stream) cudaStreamDestroy(stream);
+        for (gbo_model* mm : members) delete mm;
+    }
+
+    void build(double dt) {
+        if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
+        cudaGraph_t g;
+        GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        GBO_CUDA(cudaEventRecord(fork, stream));
+        for (size_t i = 0; i < members.size(); ++i) {
+            cudaStream_t ms = static_cast<cudaStream_t>(members[i]->stream_ptr());
+            GBO_CUDA(cudaStreamWaitEvent(ms, fork, 0));
+            per_step[i] = members[i]->capture_step(dt);
+            GBO_CUDA(cudaEventRecord(joins[i], ms));
+            GBO_CUDA(cudaStreamWaitEvent(stream, joins[i], 0));
+        }
+        GBO_CUDA(cudaStreamEndCapture(stream, &g));
+        GBO_CUDA(cudaGraphInstantiate(&graph, g, 0));
+        GBO_CUDA(cudaGraphDestroy(g));
+        graph_dt = dt;
+    }
+
+    int step(double dt, int nsteps) {
+        if (nsteps <= 0) return GBO_OK;
+        if (!graph || graph_dt != dt) build(dt);
+        for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
+        GBO_CUDA(cudaEventRecord(done, stream));
+        int rc = GBO_OK;
+        for (size_t i = 0; i < members.size(); ++i) {
+            GBO_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(members[i]->stream_ptr()), done, 0));
+            members[i]->add_launches(per_step[i] * nsteps);
+            int r = members[i]->finish_steps(dt, nsteps);
+            if (r != GBO_OK && rc == GBO_OK) {
+                rc = r;
+                err = "member " + std::to_string(i) + ": " + members[i]->err;
+            }
+        }
+        return rc;
+    }
+};
+
+namespace {
+template <class F>
+int eguarded(gbo_ensemble* e, F&& f) {
+    try {
+        return f();
+    } catch (const CudaError& x) {
+        std::string msg = std::string("CUDA error in ") + x.what + ": " + cudaGetErrorString(x.e);
+        if (e) e->err = msg;
+        g_last_error = msg;
+        return GBO_ERR_CUDA;
+    } catch (const std::exception& x) {
+        if (e) e->err = x.what();
+        g_last_error = x.what();
+        return GBO_ERR_INVALID;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int gbo_ensemble_create(int32_t n, const gbo_grid_desc* grids, const gbo_model_desc* descs, gbo_ensemble** out) {
+    if (!out || !grids || !descs || n < 1) { g_last_error = "invalid ensemble arguments"; return GBO_ERR_INVALID; }
+    *out = nullptr;
+    auto* e = new gbo_ensemble();
+    for (int32_t i = 0; i < n; ++i) {
+        gbo_model* mm = nullptr;
+        int rc = gbo_model_create(&grids[i], &descs[i], &mm);
+        if (rc != GBO_OK) {
+            g_last_error = "member " + std::to_string(i) + ": " + g_last_error;
+            delete e;
+            return rc;
+        }
+        e->members.push_back(mm);
+    }
+    int rc = eguarded(e, [&]() {
+        GBO_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        GBO_CUDA(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming));
+        GBO_CUDA(cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming));
+        e->joins.resize(n);
+        for (auto& ev : e->joins) GBO_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        e->per_step.assign(n, 0);
+        return GBO_OK;
+    });
+    if (rc != GBO_OK) {
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return GBO_OK;
+}
+
+void gbo_ensemble_destroy(gbo_ensemble* e) { delete e; }
+
+int32_t gbo_ensemble_size(const gbo_ensemble* e) { return e ? (int32_t)e->members.size() : 0; }
+
+gbo_model* gbo_ensemble_member(gbo_ensemble* e, int32_t i) {
+    if (!e || i < 0 || i >= (int32_t)e->members.size()) return nullptr;
+    return e->members[i];
+}
+
+int gbo_ensemble_stream(gbo_ensemble* e, void** stream) {
+    if (!e || !stream) return GBO_ERR_INVALID;
+    *stream = (void*)e->stream;
+    return GBO_OK;
+}
+
+int gbo_ensemble_time_step(gbo_ensemble* e, double dt, int32_t nsteps) {
+    if (!e) return GBO_ERR_INVALID;
+    if (!(dt > 0) || !std::isfinite(dt)) { e->err = "dt must be positive and finite"; g_last_error = e->err; return GBO_ERR_INVALID; }
+    int rc = eguarded(e, [&]() { return e->step(dt, nsteps); });
+    if (rc != GBO_OK) g_last_error = e->err;
+    return rc;
 }
 
 int gbo_clock(const gbo_model* m, double* time, int64_t* iteration) {

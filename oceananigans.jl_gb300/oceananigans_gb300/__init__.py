@@ -9,6 +9,6 @@ from .api import (  # noqa: F401
     WENO, SmagorinskyLilly, AnisotropicMinimumDissipation, BuoyancyTracer, FPlane,
     FluxBoundaryCondition, FieldBoundaryConditions,
     FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver,
-    NonhydrostaticModel, Simulation, set_, time_step_, run_,
+    NonhydrostaticModel, Ensemble, Simulation, set_, time_step_, run_,
 )
 from ._lib import GboError, NaNError, NotConvergedError, load  # noqa: F401

@@ -82,6 +82,13 @@ SIGNATURES = {
     "gbo_last_error": (ctypes.c_char_p, [_vp]),
     "gbo_version": (ctypes.c_char_p, []),
     "gbo_poisson_solve_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "gbo_ensemble_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc),
+                                           ctypes.POINTER(_vp)]),
+    "gbo_ensemble_destroy": (None, [_vp]),
+    "gbo_ensemble_size": (ctypes.c_int32, [_vp]),
+    "gbo_ensemble_member": (_vp, [_vp, ctypes.c_int32]),
+    "gbo_ensemble_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "gbo_ensemble_time_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32]),
     "gbo_poisson_solve_fft_static": (ctypes.c_int, [ctypes.POINTER(GridDesc), _vp, _vp, _vp]),
     "gbo_model_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "gbo_kernel_launches": (ctypes.c_int64, [_vp]),

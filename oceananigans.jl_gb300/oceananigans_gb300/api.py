@@ -283,9 +283,20 @@ class NonhydrostaticModel:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h:
+        if h and getattr(self, "_owner", None) is None:
             L.load().gbo_model_destroy(h)
-            self._h = None
+        self._h = None
+
+    @classmethod
+    def _member(cls, owner, grid, desc, tracers, handle):
+        """A member handle of an Ensemble (owned and stepped by the ensemble)."""
+        self = cls.__new__(cls)
+        self.grid, self.desc, self.tracers = grid, desc, tracers
+        self._gdesc = grid.descriptor()
+        self._h = ctypes.c_void_p(handle)
+        self._owner = owner
+        self.dtype = grid.float_type
+        return self
 
     # -- field access --------------------------------------------------------
     def _fid(self, name):
@@ -352,6 +363,51 @@ class NonhydrostaticModel:
     @property
     def solver_iterations(self):
         return L.load().gbo_last_solver_iterations(self._h)
+
+
+class Ensemble:
+    """Independent NonhydrostaticModels advanced together: one CUDA graph launch per
+    step runs every member's RK3 step as a parallel branch.  `specs` is a list of
+    (grid, keyword arguments of NonhydrostaticModel).  No reference counterpart."""
+
+    def __init__(self, specs):
+        n = len(specs)
+        grids = (L.GridDesc * n)()
+        descs = (L.ModelDesc * n)()
+        self._keep, info = [], []
+        for i, (grid, kw) in enumerate(specs):
+            d, tracers = model_descriptor(grid, **kw)
+            g = grid.descriptor()
+            self._keep.append(g)
+            ctypes.memmove(ctypes.byref(grids, i * ctypes.sizeof(L.GridDesc)), ctypes.byref(g), ctypes.sizeof(L.GridDesc))
+            ctypes.memmove(ctypes.byref(descs, i * ctypes.sizeof(L.ModelDesc)), ctypes.byref(d), ctypes.sizeof(L.ModelDesc))
+            info.append((grid, d, tracers))
+        lib = L.load()
+        h = ctypes.c_void_p()
+        rc = lib.gbo_ensemble_create(n, grids, descs, ctypes.byref(h))
+        if rc == L.GBO_ERR_INVALID:
+            raise ValueError(lib.gbo_last_error(None).decode())
+        L.check(rc)
+        self._h = h
+        self.members = [NonhydrostaticModel._member(self, g, d, t, lib.gbo_ensemble_member(h, i))
+                        for i, (g, d, t) in enumerate(info)]
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, i):
+        return self.members[i]
+
+    def time_step(self, dt, nsteps=1):
+        L.check(L.load().gbo_ensemble_time_step(self._h, float(dt), int(nsteps)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            for mm in getattr(self, "members", []):
+                mm._h = None
+            L.load().gbo_ensemble_destroy(h)
+            self._h = None
 
 
 def set_(model, enforce_incompressibility=True, **fields):

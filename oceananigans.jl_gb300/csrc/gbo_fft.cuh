@@ -429,20 +429,25 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
     };
     auto off = [&](int q) { return T.rdzf[q + 1 + T.zoff]; };
     const double tiny = 10 * 2.220446049250313e-16;
+    // One FP64 division per level (1/β), the rest multiplies: FP64 division is the
+    // costly operation of the sweep on this GPU.  Differs from dividing by β in the
+    // last bit only.
     double beta = D(1);
+    double rbeta = 1.0 / beta;
     Cx<FT> f1 = col[0];
-    double pre = (double)f1.re / beta, pim = (double)f1.im / beta;
+    double pre = (double)f1.re * rbeta, pim = (double)f1.im * rbeta;
     wre[c] = pre;
     wim[c] = pim;
     // forward elimination of level kr (1-based) with right-hand side fk
     auto forward = [&](int kr, Cx<FT> fk) {
         const double a = off(kr - 1);
-        const double t = a / beta;
+        const double t = a * rbeta;
         const size_t at = c + ncol * (kr - 1);
         wt[at] = t;
         beta = D(kr) - a * t;
-        const double sre = ((double)fk.re - a * pre) / beta;
-        const double sim = ((double)fk.im - a * pim) / beta;
+        rbeta = 1.0 / beta;
+        const double sre = ((double)fk.re - a * pre) * rbeta;
+        const double sim = ((double)fk.im - a * pim) * rbeta;
         const bool dd = fabs(beta) > tiny;
         pre = dd ? sre : 0.0;
         pim = dd ? sim : 0.0;

@@ -19,6 +19,8 @@ module OceananigansGB300Ext
 
 using Oceananigans
 using Oceananigans.Grids: topology, Periodic, Bounded, Flat
+using Oceananigans.ImmersedBoundaries: ImmersedBoundaryGrid
+using Oceananigans.Fields: interior
 using Oceananigans.Models.NonhydrostaticModels: NonhydrostaticModel
 import Oceananigans.TimeSteppers: time_step!
 import Oceananigans.Fields: set!
@@ -70,17 +72,21 @@ function handle(model::NonhydrostaticModel)
         grid = model.grid
         TX, TY, TZ = topology(grid)
         FT = eltype(grid)
-        zf = grid.z.cᵃᵃᶠ isa Number ? Float64[] : Float64.(collect(grid.z.cᵃᵃᶠ[1:grid.Nz+1]))
+        ug = grid isa ImmersedBoundaryGrid ? grid.underlying_grid : grid
+        zf = ug.z.cᵃᵃᶠ isa Number ? Float64[] : Float64.(collect(ug.z.cᵃᵃᶠ[1:grid.Nz+1]))
+        # GridFittedBottom heights at cell centres, x fastest (Nx*Ny values)
+        bh = grid isa ImmersedBoundaryGrid ?
+             Float64.(vec(Array(interior(grid.immersed_boundary.bottom_height))[:, :, 1])) : Float64[]
         gd = GridDesc((grid.Nx, grid.Ny, grid.Nz), (topo_code(TX), topo_code(TY), topo_code(TZ)),
                       (grid.xᶠᵃᵃ[1], grid.xᶠᵃᵃ[1] + grid.Lx), (grid.yᵃᶠᵃ[1], grid.yᵃᶠᵃ[1] + grid.Ly),
-                      (-grid.Lz, 0.0), isempty(zf) ? C_NULL : pointer(zf), C_NULL,
+                      (-grid.Lz, 0.0), isempty(zf) ? C_NULL : pointer(zf), isempty(bh) ? C_NULL : pointer(bh),
                       FT == Float32 ? Int32(4) : Int32(8))
         md = Ref{ModelDesc}()
         ccall((:gbo_model_desc_default, libgbo), Cvoid, (Ref{ModelDesc},), md)
         # closure / buoyancy / coriolis / boundary conditions are translated here
         # exactly as oceananigans_gb300.api.model_descriptor does for Python.
         h = Ref{Ptr{Cvoid}}(C_NULL)
-        GC.@preserve zf check(ccall((:gbo_model_create, libgbo), Cint,
+        GC.@preserve zf bh check(ccall((:gbo_model_create, libgbo), Cint,
                                     (Ref{GridDesc}, Ref{ModelDesc}, Ref{Ptr{Cvoid}}), Ref(gd), md, h))
         finalizer(m -> ccall((:gbo_model_destroy, libgbo), Cvoid, (Ptr{Cvoid},), handles[m]), model)
         h[]

@@ -98,3 +98,18 @@ def test_poisson_solvers_against_oracle():
         got = phi.cpu().numpy().reshape(b.shape, order="F")
         want = r.poisson_solve(b)
         assert cases.rel_l2(got, want) < 1e-12
+
+
+def test_turbulence_2d_128_400_steps():
+    # the 2-D benchmark configuration at full size: u, v, p against the oracle at
+    # steps 1, 100 and 400 (a 1e-15 perturbation of the initial state grows only to
+    # ~6e-15 over these 400 oracle steps, so 1e-10 leaves room for GPU rounding)
+    c = cases.turbulence_2d(128)
+    m, r = c.start_gpu(), c.start_oracle()
+    done = 0
+    for n, tol in ((1, 1e-12), (100, 1e-10), (400, 1e-10)):
+        og.time_step_(m, 0.01, n - done)
+        r.time_step(0.01, n - done)
+        done = n
+        compare(m, r, ("u", "v", "p"), tol)
+    assert m.clock[1] == 400

@@ -4,11 +4,13 @@
 //
 // The iteration runs without the host: every scalar (ρ, p·q, the active-cell sums
 // of the gauge, ‖V⁻¹r‖, the iteration count and the stop flag) lives in a small
-// FP64 array on the device.  k_cg_begin and k_cg_check evaluate the stopping rule
-// of `iterating` (conjugate_gradient_solver.jl:278-283) on the device and, inside a
-// CUDA graph, drive a conditional WHILE node with cudaGraphSetConditional, so a
-// whole time step with three CG solves is one graph launch.  Dot products and
-// norms accumulate in FP64 (warp shuffles, one atomic per block).
+// FP64 array on the device.  k_cg_begin and the last block of k_cg_gauge evaluate
+// the stopping rule of `iterating` (conjugate_gradient_solver.jl:278-283) on the
+// device and, inside a CUDA graph, drive a conditional WHILE node with
+// cudaGraphSetConditional, so a whole time step with three CG solves is one graph
+// launch.  Dot products and norms accumulate in FP64 (warp shuffles, one atomic
+// per block); the last block of each reduction forms the derived scalar (β, α,
+// the gauge means) once instead of every thread dividing.
 #pragma once
 #include "gbo_tendency.cuh"
 
@@ -25,7 +27,15 @@ enum {
     CG_FAIL,               // set when a solve stops at maxiter above tolerance (sticky)
     CG_NORM,               // ‖V⁻¹r‖ at the last check
     CG_SOLVES, CG_ITERS,   // running totals (instrumentation)
+    CG_BETA,               // ρ/ρ_prev of this iteration (0 on the first)
+    CG_ALPHA,              // ρ/(p·q)
+    CG_MX, CG_MR,          // active-cell means of x and r
     CG_NSLOTS
+};
+// block-completion counters of the loop kernels (last block finalises the scalars)
+enum {
+    CC_DOT = 0, CC_LAP, CC_XR, CC_GAUGE,
+    CC_N
 };
 
 // z-slices per launch of the 3-D CG kernels: blocks march over k so that each
@@ -136,83 +146,203 @@ __global__ void k_cg_begin(double* s, double reltol, double abstol, double maxit
     if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
-// ρ = z·r into the ρ slot of this iteration
-template <typename FT>
-__global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, size_t n, double* s) {
-    double acc = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-        acc += (double)a[t] * (double)b[t];
-    block_add(acc, s + CG_RHO0 + cg_parity(s));
+// True in exactly one block: the one whose completion ticket is the last.  The
+// block's reduction atomics (issued by thread 0 in block_add) are made visible
+// before its ticket; the last block then reads the totals with L2 loads.
+GBO_D bool last_block(unsigned int* counter) {
+    __shared__ bool last;
+    const unsigned int total = gridDim.x * gridDim.y * gridDim.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        last = atomicAdd(counter, 1u) == total - 1;
+        if (last) *counter = 0u;  // ready for the next launch
+    }
+    __syncthreads();
+    return last;
 }
-// p = z (first iteration) or z + (ρ/ρ_prev) p (conjugate_gradient_solver.jl:246-263)
+GBO_D double ldcg(const double* p) { return __ldcg(p); }
+
+// ρ = z·r into the ρ slot of this iteration; the last block sets β = ρ/ρ_prev
+// (conjugate_gradient_solver.jl:246-263; 0 on the first iteration)
+//
+// Fail-safe for the loop: the first thread clears the stop flag and the loop
+// condition at the start of every iteration; only the last block of k_cg_gauge
+// sets them again, so an iteration whose stopping test did not run ends the loop
+// instead of repeating it.
 template <typename FT>
-__global__ void k_cg_update_p(const FT* __restrict__ z, FT* __restrict__ p, const double* s, size_t n) {
+__global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, size_t n, double* s, unsigned int* cnt,
+                         cudaGraphConditionalHandle h, int use_handle) {
+    const int par = cg_parity(s);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s[CG_CONT] = 0.0;
+        if (use_handle) cudaGraphSetConditional(h, 0u);
+    }
+    FT acc = FT(0);  // per-thread partial sums in FT (a few terms), FP64 across threads
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        acc += a[t] * b[t];
+    block_add((double)acc, s + CG_RHO0 + par);
+    if (last_block(cnt + CC_DOT) && threadIdx.x == 0) {
+        const bool first = s[CG_IT] == 0.0;
+        s[CG_BETA] = first ? 0.0 : ldcg(s + CG_RHO0 + par) / ldcg(s + CG_RHO0 + (par ^ 1));
+    }
+}
+
+// Per-thread column context of the 3-D CG kernels: the wrapped neighbour columns and
+// their numbers of immersed cells, constant along k (a cell (c, k) is immersed iff
+// k < kb[c]).
+struct CgCol {
+    size_t C, W, E, S, N;  // column offsets of (i, j) and its x / y neighbours
+    int kC, kW, kE, kS, kN;
+};
+template <typename FT>
+GBO_D CgCol cg_col(const GridP<FT>& g, int i, int j) {
+    CgCol c;
+    const int iw = i == 0 ? g.Nx - 1 : i - 1, ie = i == g.Nx - 1 ? 0 : i + 1;
+    const int js = j == 0 ? g.Ny - 1 : j - 1, jn = j == g.Ny - 1 ? 0 : j + 1;
+    c.C = i + (size_t)g.Nx * j;
+    c.W = iw + (size_t)g.Nx * j;
+    c.E = ie + (size_t)g.Nx * j;
+    c.S = i + (size_t)g.Nx * js;
+    c.N = i + (size_t)g.Nx * jn;
+    c.kC = c.kW = c.kE = c.kS = c.kN = 0;
+    if (g.kbot) {
+        c.kC = __ldg(g.kbot + c.C); c.kW = __ldg(g.kbot + c.W); c.kE = __ldg(g.kbot + c.E);
+        c.kS = __ldg(g.kbot + c.S); c.kN = __ldg(g.kbot + c.N);
+    }
+    return c;
+}
+
+// p = z + β p_prev (p = z on the first iteration) fused with q = V∇²p: the new
+// search direction is formed at every point of the 7-point stencil from z and
+// the previous direction, so no separate pass writes p before the Laplacian reads
+// it.  Differences across a face touching an immersed cell are zero
+// (conditional_differences.jl:15-43); at the walls the mirrored halo makes them
+// zero.  The two directions alternate between p0 and p1 by iteration parity.
+// Accumulates p·q; the last block sets α = ρ/(p·q).
+template <typename FT>
+__global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __restrict__ p0, FT* __restrict__ p1,
+                               FT* __restrict__ q, double* s, unsigned int* cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool in = i < g.Nx && j < g.Ny;
     const int par = cg_parity(s);
     const bool first = s[CG_IT] == 0.0;
-    const FT beta = first ? FT(0) : FT(s[CG_RHO0 + par] / s[CG_RHO0 + (par ^ 1)]);
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-        p[t] = first ? z[t] : z[t] + beta * p[t];
+    const FT beta = FT(s[CG_BETA]);
+    const FT* __restrict__ pold = par ? p0 : p1;
+    FT* __restrict__ pnew = par ? p1 : p0;
+    const size_t plane = (size_t)g.Nx * g.Ny;
+    Met<FT> M(g);
+    FT acc = FT(0);
+    if (in) {
+        const CgCol c = cg_col(g, i, j);
+        auto pn = [&](size_t col, int kk) {
+            const size_t at = col + plane * kk;
+            return first ? z[at] : z[at] + beta * pold[at];
+        };
+        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
+            const FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
+            const FT pc = pn(c.C, k);
+            const FT pw = pn(c.W, k), pe = pn(c.E, k), ps = pn(c.S, k), pnn = pn(c.N, k);
+            const bool im = k < c.kC;
+            const FT fw = (im || k < c.kW) ? FT(0) : Ax * ((pc - pw) * g.rdx);
+            const FT fe = (im || k < c.kE) ? FT(0) : Ax * ((pe - pc) * g.rdx);
+            const FT fs = (im || k < c.kS) ? FT(0) : Ay * ((pc - ps) * g.rdy);
+            const FT fn = (im || k < c.kN) ? FT(0) : Ay * ((pnn - pc) * g.rdy);
+            FT dz = FT(0);
+            if (!g.flatz) {
+                const FT pb = k > 0 ? pn(c.C, k - 1) : pc;
+                const FT pt = k < g.Nz - 1 ? pn(c.C, k + 1) : pc;
+                const FT fb = (im || k - 1 < c.kC) ? FT(0) : Az * ((pc - pb) * M.rdzf(k));
+                const FT ft = (im || k + 1 < c.kC) ? FT(0) : Az * ((pt - pc) * M.rdzf(k + 1));
+                dz = ft - fb;
+            }
+            const FT val = (fe - fw) + (fn - fs) + dz;
+            const size_t idx = c.C + plane * k;
+            pnew[idx] = pc;
+            q[idx] = val;
+            acc += pc * val;
+        }
+    }
+    block_add((double)acc, s + CG_PQ);
+    if (last_block(cnt + CC_LAP) && threadIdx.x == 0 && threadIdx.y == 0)
+        s[CG_ALPHA] = ldcg(s + CG_RHO0 + par) / ldcg(s + CG_PQ);
 }
-// x += α p, r -= α q with α = ρ / (p·q); accumulates the active-cell sums of x and r
+
+// x += α p, r -= α q; accumulates the active-cell sums of x and r, the last block
+// sets their means
 template <typename FT>
-__global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, const FT* __restrict__ p,
-                               const FT* __restrict__ q, double* s) {
+__global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, const FT* __restrict__ p0,
+                               const FT* __restrict__ p1, const FT* __restrict__ q, double* s, unsigned int* cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i < g.Nx && j < g.Ny;
-    const FT alpha = FT(s[CG_RHO0 + cg_parity(s)] / s[CG_PQ]);
-    double ax = 0.0, ar = 0.0;
-    for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
-        if (!in) continue;
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        const FT xv = x[idx] + alpha * p[idx];
-        const FT rv = r[idx] - alpha * q[idx];
-        x[idx] = xv;
-        r[idx] = rv;
-        if (!inactive_cell(g, i, j, k)) { ax += xv; ar += rv; }
+    const FT alpha = FT(s[CG_ALPHA]);
+    const FT* p = cg_parity(s) ? p1 : p0;
+    FT ax = FT(0), ar = FT(0);
+    if (in) {
+        const int kb = g.kbot ? __ldg(g.kbot + i + (size_t)g.Nx * j) : 0;
+        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
+            const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+            const FT xv = x[idx] + alpha * p[idx];
+            const FT rv = r[idx] - alpha * q[idx];
+            x[idx] = xv;
+            r[idx] = rv;
+            if (k >= kb) { ax += xv; ar += rv; }
+        }
     }
-    block_add(ax, s + CG_SX, ar, s + CG_SR);
+    block_add((double)ax, s + CG_SX, (double)ar, s + CG_SR);
+    if (last_block(cnt + CC_XR) && threadIdx.x == 0 && threadIdx.y == 0) {
+        const double n = s[CG_NACT];
+        s[CG_MX] = ldcg(s + CG_SX) / n;
+        s[CG_MR] = ldcg(s + CG_SR) / n;
+    }
 }
-// zero-mean gauge over active cells with immersed cells zeroed (enforce_zero_mean_gauge!,
-// conjugate_gradient_poisson_solver.jl:81-96); accumulates ‖V⁻¹r‖² and, if out, writes
-// the next iteration's preconditioner right-hand side
+
+// Zero-mean gauge over active cells with immersed cells zeroed (enforce_zero_mean_gauge!,
+// conjugate_gradient_poisson_solver.jl:81-96); accumulates ‖V⁻¹r‖², writes the next
+// preconditioner input (if out) and, in the last block, applies the stopping rule
+// (conjugate_gradient_solver.jl:278-283), clears the next iteration's accumulators
+// and sets the loop condition.
 template <typename FT>
 __global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, FT* __restrict__ out, double* s,
-                           int dz_scale) {
+                           int dz_scale, unsigned int* cnt, double maxiter, cudaGraphConditionalHandle h,
+                           int use_handle) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i < g.Nx && j < g.Ny;
-    const FT mx = FT(s[CG_SX] / s[CG_NACT]), mr = FT(s[CG_SR] / s[CG_NACT]);
+    const FT mx = FT(s[CG_MX]), mr = FT(s[CG_MR]);
     Met<FT> M(g);
-    double acc = 0.0;
-    for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
-        if (!in) continue;
-        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-        const FT act = inactive_cell(g, i, j, k) ? FT(0) : FT(1);
-        x[idx] = (x[idx] - mx) * act;
-        const FT rv = (r[idx] - mr) * act;
-        r[idx] = rv;
-        const FT vr = rv * M.rVc(k);
-        if (out) out[idx] = precond_source(M, vr, k, dz_scale);
-        acc += (double)vr * (double)vr;
+    FT acc = FT(0);
+    if (in) {
+        const int kb = g.kbot ? __ldg(g.kbot + i + (size_t)g.Nx * j) : 0;
+        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
+            const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+            const FT act = k < kb ? FT(0) : FT(1);
+            x[idx] = (x[idx] - mx) * act;
+            const FT rv = (r[idx] - mr) * act;
+            r[idx] = rv;
+            const FT vr = rv * M.rVc(k);
+            if (out) out[idx] = precond_source(M, vr, k, dz_scale);
+            acc += vr * vr;
+        }
     }
-    block_add(acc, s + CG_NORM2);
+    block_add((double)acc, s + CG_NORM2);
+    if (last_block(cnt + CC_GAUGE) && threadIdx.x == 0 && threadIdx.y == 0) {
+        const double it = s[CG_IT] + 1.0;
+        const double norm = sqrt(ldcg(s + CG_NORM2));
+        const bool cont = it < maxiter && norm > s[CG_TOL];
+        if (!cont && norm > s[CG_TOL]) s[CG_FAIL] = 1.0;
+        s[CG_IT] = it;
+        s[CG_NORM] = norm;
+        s[CG_ITERS] += 1.0;
+        s[CG_CONT] = cont ? 1.0 : 0.0;
+        s[CG_PQ] = s[CG_SX] = s[CG_SR] = s[CG_NORM2] = 0.0;
+        s[CG_RHO0 + (((int)it) & 1)] = 0.0;  // ρ slot of the next iteration (its ρ_prev is kept)
+        __threadfence();
+        if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
+    }
 }
-// Stopping rule after an iteration (conjugate_gradient_solver.jl:278-283); clears the
-// accumulators of the next iteration.
-__global__ void k_cg_check(double* s, double maxiter, cudaGraphConditionalHandle h, int use_handle) {
-    const double it = s[CG_IT] + 1.0;
-    const double norm = sqrt(s[CG_NORM2]);
-    const bool cont = it < maxiter && norm > s[CG_TOL];
-    if (!cont && norm > s[CG_TOL]) s[CG_FAIL] = 1.0;
-    s[CG_IT] = it;
-    s[CG_NORM] = norm;
-    s[CG_ITERS] += 1.0;
-    s[CG_CONT] = cont ? 1.0 : 0.0;
-    s[CG_PQ] = s[CG_SX] = s[CG_SR] = s[CG_NORM2] = 0.0;
-    s[CG_RHO0 + (((int)it) & 1)] = 0.0;  // ρ slot of the next iteration (its ρ_prev is kept)
-    if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
-}
+
 // number of active cells (for the gauge means)
 template <typename FT>
 __global__ void k_cg_count(GridP<FT> g, double* s) {

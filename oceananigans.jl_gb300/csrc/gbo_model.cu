@@ -273,10 +273,11 @@ struct gbo_model {
 };
 
 enum { G_MOMENTUM = 0, G_TRACER, G_CLOSURE, G_HYDROSTATIC, G_SOURCE, G_DCT_Z, G_FFT_X, G_FFT_Y, G_THOMAS,
-       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, GROUPS };
+       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, G_CG_DOT, G_CG_DIR, G_CG_XR, G_CG_GAUGE, GROUPS };
 const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", "k_hydrostatic", "k_source",
                                          "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
-                                         "k_nan_check", "k_mask", "k_cg"};
+                                         "k_nan_check", "k_mask", "k_cg", "k_cg_dot", "k_cg_direction",
+                                         "k_cg_update_xr", "k_cg_gauge"};
 
 // The fused momentum kernel is compiled per closure kind; these pick the instance.
 template <typename FT, bool TR>
@@ -343,8 +344,9 @@ struct ModelImpl : gbo_model {
     // immersed boundary and conjugate-gradient solver
     bool ibg = false, cg = false;
     int precond_solver = GBO_SOLVER_FFT;  // spectral solver of the underlying grid
-    DBuf<FT> cg_b, cg_r, cg_q, cg_d, cg_x;
+    DBuf<FT> cg_b, cg_r, cg_q, cg_d, cg_p1, cg_x;  // cg_d / cg_p1: search directions by parity
     DBuf<double> cg_s;
+    DBuf<unsigned int> cg_cnt;
     double* h_cgs = nullptr;
     int cg_status = GBO_OK;
     cudaStream_t body_stream = nullptr;  // captures the CG loop body into a conditional node
@@ -366,9 +368,10 @@ struct ModelImpl : gbo_model {
     ~ModelImpl() override {
         if (graph) cudaGraphExecDestroy(graph);
         for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz,
-                            &cg_b, &cg_r, &cg_q, &cg_d, &cg_x})
+                            &cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x})
             b->free_();
         cg_s.free_();
+        cg_cnt.free_();
         if (h_cgs) cudaFreeHost(h_cgs);
         if (body_stream) cudaStreamDestroy(body_stream);
         for (auto* vec : {&c, &cs, &Gc, &kap})
@@ -451,8 +454,9 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned int)));
         init_poisson(Lx, Ly);
         if (cg) {
-            for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_x}) b->alloc(N);
+            for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x}) b->alloc(N);
             cg_s.alloc(CG_NSLOTS);
+            cg_cnt.alloc(CC_N);
             GBO_CUDA(cudaMallocHost(&h_cgs, CG_NSLOTS * sizeof(double)));
             GBO_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
             k_cg_count<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_s.p);
@@ -666,23 +670,18 @@ struct ModelImpl : gbo_model {
             poisson_solve(precond_solver);
             z = rb.p;
         }
-        pre(G_CG);
-        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s);
+        pre(G_CG_DOT);
+        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s, cg_cnt.p, h, use_handle);
         check_launch();
-        pre(G_CG);
-        k_cg_update_p<FT><<<lin, 256, 0, stream>>>(z, cg_d.p, s, N);
+        pre(G_CG_DIR);
+        k_cg_direction<FT><<<cg_grid(), blk(), 0, stream>>>(gp, z, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p);
         check_launch();
-        pre(G_CG);
-        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_d.p, cg_q.p, s);
+        pre(G_CG_XR);
+        k_cg_update_xr<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p);
         check_launch();
-        pre(G_CG);
-        k_cg_update_xr<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_q.p, s);
-        check_launch();
-        pre(G_CG);
-        k_cg_gauge<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, pc ? rb.p : nullptr, s, dzs);
-        check_launch();
-        pre(G_CG);
-        k_cg_check<<<1, 1, 0, stream>>>(s, maxiter, h, use_handle);
+        pre(G_CG_GAUGE);
+        k_cg_gauge<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, pc ? rb.p : nullptr, s, dzs, cg_cnt.p,
+                                                         maxiter, h, use_handle);
         check_launch();
     }
 
@@ -754,7 +753,8 @@ struct ModelImpl : gbo_model {
             launches = before;  // counted per executed iteration after the step
             cudaGraph_t captured = nullptr;
             GBO_CUDA(cudaStreamEndCapture(body_stream, &captured));
-            // the body must end with k_cg_check, the only node that can end the loop
+            // the body must hold the dot kernel (clears the loop condition) and the gauge
+            // kernel (sets it): every kernel of cg_body is a node of the body graph
             size_t nodes = 0;
             GBO_CUDA(cudaGraphGetNodes(body, nullptr, &nodes));
             if ((int64_t)nodes != body_launches || body_launches < 2)
@@ -765,7 +765,7 @@ struct ModelImpl : gbo_model {
         k_cg_begin<<<1, 1, 0, stream>>>(s, rel, abs_, maxiter, 0, 0);
         check_launch();
         read_cg_scalars();
-        while (h_cgs[CG_CONT] != 0.0) {
+        for (double n = 0; h_cgs[CG_CONT] != 0.0 && n <= maxiter; n += 1.0) {
             cg_body(maxiter, 0, 0);
             read_cg_scalars();
         }

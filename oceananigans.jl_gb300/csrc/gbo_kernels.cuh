@@ -57,8 +57,9 @@ __global__ void k_smagorinsky(StepP<FT> P, FT* __restrict__ nu_out) {
     FT N2 = FT(0);
     if (P.buoyancy && !g.flatz) {
         CFld<FT> b = cfld(P.b, g);
-        FT b1 = (b(i, j, k) - b(i, j, k - 1)) * M.rdzf(k);
-        FT b2 = (b(i, j, k + 1) - b(i, j, k)) * M.rdzf(k + 1);
+        // N² = ℑz(∂z b), conditional ∂ on an immersed grid
+        FT b1 = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (b(i, j, k) - b(i, j, k - 1)) * M.rdzf(k);
+        FT b2 = cond_zero(g, i, j, k, i, j, k + 1) ? FT(0) : (b(i, j, k + 1) - b(i, j, k)) * M.rdzf(k + 1);
         N2 = FT(0.5) * (b1 + b2);
     }
     FT N2p = fmax(FT(0), N2);
@@ -147,9 +148,16 @@ GBO_D void amd_point(const StepP<FT>& P, const GridP<FT>& g, const ST& S, const 
     }
     nu_out[idx] = fmax(FT(0), nsgs);
     if (kap_out && has_c) {
-        auto n_dxc = [&](int a, int b, int cc) { return A.Dfx() * ((c(a, b, cc) - c(a - 1, b, cc)) * g.rdx); };
-        auto n_dyc = [&](int a, int b, int cc) { return A.Dfy() * ((c(a, b, cc) - c(a, b - 1, cc)) * g.rdy); };
-        auto n_dzc = [&](int a, int b, int cc) { return A.Dfz(cc) * ((c(a, b, cc) - c(a, b, cc - 1)) * M.rdzf(cc)); };
+        // tracer gradients at faces, conditional ∂ on an immersed grid
+        auto n_dxc = [&](int a, int b, int cc) {
+            return A.Dfx() * (cond_zero(g, a - 1, b, cc, a, b, cc) ? FT(0) : (c(a, b, cc) - c(a - 1, b, cc)) * g.rdx);
+        };
+        auto n_dyc = [&](int a, int b, int cc) {
+            return A.Dfy() * (cond_zero(g, a, b - 1, cc, a, b, cc) ? FT(0) : (c(a, b, cc) - c(a, b - 1, cc)) * g.rdy);
+        };
+        auto n_dzc = [&](int a, int b, int cc) {
+            return A.Dfz(cc) * (cond_zero(g, a, b, cc - 1, a, b, cc) ? FT(0) : (c(a, b, cc) - c(a, b, cc - 1)) * M.rdzf(cc));
+        };
         auto dxc2 = [&](int a, int b, int cc) { return sq(n_dxc(a, b, cc)); };
         auto dyc2 = [&](int a, int b, int cc) { return sq(n_dyc(a, b, cc)); };
         auto dzc2 = [&](int a, int b, int cc) { return sq(n_dzc(a, b, cc)); };

@@ -792,7 +792,12 @@ struct ModelImpl : gbo_model {
         StepP<FT> P = params();
         const dim3 sgrid((Nx + smag::TX - 1) / smag::TX, (Ny + smag::TY - 1) / smag::TY, (Nz + smag::KT - 1) / smag::KT);
         const dim3 sblock(smag::TX, smag::TY);
-        if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
+        if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY && ibg) {
+            // conditional strain rates near the immersed boundary: the per-point kernel
+            pre(G_CLOSURE);
+            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(P, nu.p);
+            check_launch();
+        } else if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
             pre(G_CLOSURE);
             k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(P, nu.p);
             check_launch();
@@ -1158,7 +1163,6 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
     }
     if (g->bottom_height) {
         if (g->topology[2] != GBO_BOUNDED) return "GridFittedBottom requires Bounded z";
-        if (d->closure != GBO_CLOSURE_NONE) return "turbulence closures on an ImmersedBoundaryGrid are not implemented";
         for (int q = 0; q < g->size[0] * g->size[1]; ++q)
             if (std::isnan(g->bottom_height[q])) return "bottom_height must not be NaN";
     }

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         if (P.has_phy) G = G - (cond_zero(g, i, j - 1, k, i, j, k) ? FT(0) : (F.phy(i, j, k) - F.phy(i, j - 1, k))) * g.rdy;
         if (closure) {
             FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
-            FT cdx = Ax * (FT(-2) * (S.nu_ffc(i + 1, j, k) * S.S12(i + 1, j, k))) - Ax * (FT(-2) * (S.nu_ffc(i, j, k) * S.S12(i, j, k)));
+            FT cdx = Ax * S.tau_vx(i + 1, j, k) - Ax * S.tau_vx(i, j, k);
             FT cdy = Ay * S.tau_vy(i, j, k) - Ay * S.tau_vy(i, j - 1, k);
             FT cdz = g.flatz ? FT(0) : (Az * S.tau_vz(i, j, k + 1) - Az * S.tau_vz(i, j, k));
             G = G - M.rVc(k) * (cdx + cdy + cdz);
@@ -94,8 +94,8 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         FT G = -(M.rVf(k) * (dx_ + dy_ + dz_));
         if (closure) {
             FT Axf = M.Axf(k), Ayf = M.Ayf(k), Az = M.Az();
-            FT cdx = Axf * (FT(-2) * (S.nu_fcf(i + 1, j, k) * S.S13(i + 1, j, k))) - Axf * (FT(-2) * (S.nu_fcf(i, j, k) * S.S13(i, j, k)));
-            FT cdy = Ayf * (FT(-2) * (S.nu_cff(i, j + 1, k) * S.S23(i, j + 1, k))) - Ayf * (FT(-2) * (S.nu_cff(i, j, k) * S.S23(i, j, k)));
+            FT cdx = Axf * S.tau_wx(i + 1, j, k) - Axf * S.tau_wx(i, j, k);
+            FT cdy = Ayf * S.tau_wy(i, j + 1, k) - Ayf * S.tau_wy(i, j, k);
             FT cdz = Az * S.tau_wz(i, j, k) - Az * S.tau_wz(i, j, k - 1);
             G = G - M.rVf(k) * (cdx + cdy + cdz);
         }
@@ -148,9 +148,19 @@ __global__ void __launch_bounds__(256) k_tracer(StepP<FT> P) {
         auto kx = [&](int ii) { return P.closure == CL_AMD ? FT(0.5) * (K(ii - 1, j, k) + K(ii, j, k)) : FT(0.5) * (K(ii - 1, j, k) + K(ii, j, k)) / rPr; };
         auto ky = [&](int jj) { return P.closure == CL_AMD ? FT(0.5) * (K(i, jj - 1, k) + K(i, jj, k)) : FT(0.5) * (K(i, jj - 1, k) + K(i, jj, k)) / rPr; };
         auto kz = [&](int kk) { return P.closure == CL_AMD ? FT(0.5) * (K(i, j, kk - 1) + K(i, j, kk)) : FT(0.5) * (K(i, j, kk - 1) + K(i, j, kk)) / rPr; };
-        auto qx = [&](int ii) { return -kx(ii) * ((c(ii, j, k) - c(ii - 1, j, k)) * g.rdx); };
-        auto qy = [&](int jj) { return -ky(jj) * ((c(i, jj, k) - c(i, jj - 1, k)) * g.rdy); };
-        auto qz = [&](int kk) { return -kz(kk) * ((c(i, j, kk) - c(i, j, kk - 1)) * M.rdzf(kk)); };
+        // on an immersed grid: conditional ∂ (conditional_differences.jl:15-43) and zero flux
+        // on the immersed periphery of the flux location (immersed_diffusive_fluxes.jl:42-44)
+        auto dc = [&](int i0, int j0, int k0, int i1, int j1, int k1, FT d) { return cond_zero(g, i0, j0, k0, i1, j1, k1) ? FT(0) : d; };
+        auto zq = [&](int ii, int jj, int kk, bool fx, bool fy, bool fz) { return g.kbot && imm_periph(g, ii, jj, kk, fx, fy, fz); };
+        auto qx = [&](int ii) {
+            return zq(ii, j, k, true, false, false) ? FT(0) : -kx(ii) * dc(ii - 1, j, k, ii, j, k, (c(ii, j, k) - c(ii - 1, j, k)) * g.rdx);
+        };
+        auto qy = [&](int jj) {
+            return zq(i, jj, k, false, true, false) ? FT(0) : -ky(jj) * dc(i, jj - 1, k, i, jj, k, (c(i, jj, k) - c(i, jj - 1, k)) * g.rdy);
+        };
+        auto qz = [&](int kk) {
+            return zq(i, j, kk, false, false, true) ? FT(0) : -kz(kk) * dc(i, j, kk - 1, i, j, kk, (c(i, j, kk) - c(i, j, kk - 1)) * M.rdzf(kk));
+        };
         FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
         FT cdx = Ax * qx(i + 1) - Ax * qx(i);
         FT cdy = Ay * qy(j + 1) - Ay * qy(j);

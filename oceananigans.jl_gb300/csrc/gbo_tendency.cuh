@@ -84,6 +84,23 @@ GBO_D int ibg_level(const GridP<FT>& g, int d, int i, int j, int k, bool loc_fac
     }
     return 1;
 }
+// immersed_inactive_node at (i, j, k) of a location with Face flags (fx, fy, fz):
+// inactive on the immersed grid (every adjacent cell inactive, inactive_node.jl:127-137)
+// but active on the underlying grid (immersed_boundary_interface.jl:59-60)
+template <typename FT>
+GBO_D bool imm_inactive_node(const GridP<FT>& g, int i, int j, int k, bool fx, bool fy, bool fz) {
+    if (!g.kbot) return false;
+    bool all = true, all_out = true;
+    for (int a = 0; a <= (fx ? 1 : 0); ++a)
+        for (int b = 0; b <= (fy ? 1 : 0); ++b)
+            for (int c = 0; c <= (fz ? 1 : 0); ++c) {
+                const int kk = k - c;
+                const bool out = !g.flatz && (kk < 0 || kk >= g.Nz);
+                all_out = all_out && out;
+                all = all && (out || imm_cell(g, i - a, j - b, kk));
+            }
+    return all && !all_out;
+}
 // immersed-aware ∂ mask: a difference across a face is zero when either cell is immersed
 template <typename FT>
 GBO_D bool cond_zero(const GridP<FT>& g, int i0, int j0, int k0, int i1, int j1, int k1) {
@@ -207,15 +224,37 @@ struct StrainT {
     const FL& F;
     Met<FT> M;
     GBO_D StrainT(const GridP<FT>& gg, const FL& ff) : g(gg), F(ff), M(gg) {}
-    GBO_D FT S11(int i, int j, int k) const { return (F.u(i + 1, j, k) - F.u(i, j, k)) * g.rdx; }
-    GBO_D FT S22(int i, int j, int k) const { return (F.v(i, j + 1, k) - F.v(i, j, k)) * g.rdy; }
-    GBO_D FT S33(int i, int j, int k) const { return g.flatz ? FT(0) : (F.w(i, j, k + 1) - F.w(i, j, k)) * M.rdzc(k); }
-    GBO_D FT dyu(int i, int j, int k) const { return (F.u(i, j, k) - F.u(i, j - 1, k)) * g.rdy; }
-    GBO_D FT dxv(int i, int j, int k) const { return (F.v(i, j, k) - F.v(i - 1, j, k)) * g.rdx; }
-    GBO_D FT dzu(int i, int j, int k) const { return g.flatz ? FT(0) : (F.u(i, j, k) - F.u(i, j, k - 1)) * M.rdzf(k); }
-    GBO_D FT dxw(int i, int j, int k) const { return g.flatz ? FT(0) : (F.w(i, j, k) - F.w(i - 1, j, k)) * g.rdx; }
-    GBO_D FT dzv(int i, int j, int k) const { return g.flatz ? FT(0) : (F.v(i, j, k) - F.v(i, j, k - 1)) * M.rdzf(k); }
-    GBO_D FT dyw(int i, int j, int k) const { return g.flatz ? FT(0) : (F.w(i, j, k) - F.w(i, j - 1, k)) * g.rdy; }
+    // On an immersed grid every location-specific ∂ is conditional: zero when either
+    // differenced node is an immersed-inactive node of the field's location
+    // (conditional_differences.jl:15-43).  u at (f,c,c), v at (c,f,c), w at (c,c,f).
+    GBO_D bool cu(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return g.kbot && (imm_inactive_node(g, i0, j0, k0, true, false, false) || imm_inactive_node(g, i1, j1, k1, true, false, false));
+    }
+    GBO_D bool cv(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return g.kbot && (imm_inactive_node(g, i0, j0, k0, false, true, false) || imm_inactive_node(g, i1, j1, k1, false, true, false));
+    }
+    GBO_D bool cw(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return g.kbot && (imm_inactive_node(g, i0, j0, k0, false, false, true) || imm_inactive_node(g, i1, j1, k1, false, false, true));
+    }
+    GBO_D FT S11(int i, int j, int k) const { return cu(i, j, k, i + 1, j, k) ? FT(0) : (F.u(i + 1, j, k) - F.u(i, j, k)) * g.rdx; }
+    GBO_D FT S22(int i, int j, int k) const { return cv(i, j, k, i, j + 1, k) ? FT(0) : (F.v(i, j + 1, k) - F.v(i, j, k)) * g.rdy; }
+    GBO_D FT S33(int i, int j, int k) const {
+        return (g.flatz || cw(i, j, k, i, j, k + 1)) ? FT(0) : (F.w(i, j, k + 1) - F.w(i, j, k)) * M.rdzc(k);
+    }
+    GBO_D FT dyu(int i, int j, int k) const { return cu(i, j - 1, k, i, j, k) ? FT(0) : (F.u(i, j, k) - F.u(i, j - 1, k)) * g.rdy; }
+    GBO_D FT dxv(int i, int j, int k) const { return cv(i - 1, j, k, i, j, k) ? FT(0) : (F.v(i, j, k) - F.v(i - 1, j, k)) * g.rdx; }
+    GBO_D FT dzu(int i, int j, int k) const {
+        return (g.flatz || cu(i, j, k - 1, i, j, k)) ? FT(0) : (F.u(i, j, k) - F.u(i, j, k - 1)) * M.rdzf(k);
+    }
+    GBO_D FT dxw(int i, int j, int k) const {
+        return (g.flatz || cw(i - 1, j, k, i, j, k)) ? FT(0) : (F.w(i, j, k) - F.w(i - 1, j, k)) * g.rdx;
+    }
+    GBO_D FT dzv(int i, int j, int k) const {
+        return (g.flatz || cv(i, j, k - 1, i, j, k)) ? FT(0) : (F.v(i, j, k) - F.v(i, j, k - 1)) * M.rdzf(k);
+    }
+    GBO_D FT dyw(int i, int j, int k) const {
+        return (g.flatz || cw(i, j - 1, k, i, j, k)) ? FT(0) : (F.w(i, j, k) - F.w(i, j - 1, k)) * g.rdy;
+    }
     GBO_D FT S12(int i, int j, int k) const { return FT(0.5) * (dyu(i, j, k) + dxv(i, j, k)); }
     GBO_D FT S13(int i, int j, int k) const { return FT(0.5) * (dzu(i, j, k) + dxw(i, j, k)); }
     GBO_D FT S23(int i, int j, int k) const { return FT(0.5) * (dzv(i, j, k) + dyw(i, j, k)); }
@@ -231,12 +270,19 @@ struct StrainT {
         return FT(0.5) * (FT(0.5) * (F.nu(i, j - 1, k - 1) + F.nu(i, j, k - 1)) + FT(0.5) * (F.nu(i, j - 1, k) + F.nu(i, j, k)));
     }
     // viscous fluxes -2 ν Σ (isotropic ScalarDiffusivity form)
-    GBO_D FT tau_ux(int i, int j, int k) const { return FT(-2) * (F.nu(i, j, k) * S11(i, j, k)); }
-    GBO_D FT tau_uy(int i, int j, int k) const { return FT(-2) * (nu_ffc(i, j, k) * S12(i, j, k)); }
-    GBO_D FT tau_uz(int i, int j, int k) const { return FT(-2) * (nu_fcf(i, j, k) * S13(i, j, k)); }
-    GBO_D FT tau_vy(int i, int j, int k) const { return FT(-2) * (F.nu(i, j, k) * S22(i, j, k)); }
-    GBO_D FT tau_vz(int i, int j, int k) const { return FT(-2) * (nu_cff(i, j, k) * S23(i, j, k)); }
-    GBO_D FT tau_wz(int i, int j, int k) const { return FT(-2) * (F.nu(i, j, k) * S33(i, j, k)); }
+    // On an immersed grid each viscous flux is zero on the immersed periphery of its
+    // location (conditional_flux, immersed_diffusive_fluxes.jl:25-40); the default
+    // immersed boundary condition adds no flux.
+    GBO_D bool zp(int i, int j, int k, bool fx, bool fy, bool fz) const { return g.kbot && imm_periph(g, i, j, k, fx, fy, fz); }
+    GBO_D FT tau_ux(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? FT(0) : FT(-2) * (F.nu(i, j, k) * S11(i, j, k)); }
+    GBO_D FT tau_uy(int i, int j, int k) const { return zp(i, j, k, true, true, false) ? FT(0) : FT(-2) * (nu_ffc(i, j, k) * S12(i, j, k)); }
+    GBO_D FT tau_uz(int i, int j, int k) const { return zp(i, j, k, true, false, true) ? FT(0) : FT(-2) * (nu_fcf(i, j, k) * S13(i, j, k)); }
+    GBO_D FT tau_vx(int i, int j, int k) const { return zp(i, j, k, true, true, false) ? FT(0) : FT(-2) * (nu_ffc(i, j, k) * S12(i, j, k)); }
+    GBO_D FT tau_vy(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? FT(0) : FT(-2) * (F.nu(i, j, k) * S22(i, j, k)); }
+    GBO_D FT tau_vz(int i, int j, int k) const { return zp(i, j, k, false, true, true) ? FT(0) : FT(-2) * (nu_cff(i, j, k) * S23(i, j, k)); }
+    GBO_D FT tau_wx(int i, int j, int k) const { return zp(i, j, k, true, false, true) ? FT(0) : FT(-2) * (nu_fcf(i, j, k) * S13(i, j, k)); }
+    GBO_D FT tau_wy(int i, int j, int k) const { return zp(i, j, k, false, true, true) ? FT(0) : FT(-2) * (nu_cff(i, j, k) * S23(i, j, k)); }
+    GBO_D FT tau_wz(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? FT(0) : FT(-2) * (F.nu(i, j, k) * S33(i, j, k)); }
 };
 template <typename FT>
 using Strain = StrainT<FT>;

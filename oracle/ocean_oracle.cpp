@@ -420,6 +420,22 @@ inline bool imm_periph(const Grid& g, int i, int j, int k, bool fx, bool fy, boo
             }
     return any_imm && !any_out;
 }
+// immersed_inactive_node of a location with Face flags: every adjacent cell inactive on the
+// immersed grid but not every one outside the domain (inactive_node.jl:127-137;
+// immersed_boundary_interface.jl:59-60)
+inline bool imm_inactive_node(const Grid& g, int i, int j, int k, bool fx, bool fy, bool fz) {
+    if (!g.immersed) return false;
+    bool all = true, all_out = true;
+    for (int a = 0; a <= (fx ? 1 : 0); ++a)
+        for (int b = 0; b <= (fy ? 1 : 0); ++b)
+            for (int c = 0; c <= (fz ? 1 : 0); ++c) {
+                int kk = k - c;
+                bool out = !g.flatz && (kk < 1 || kk > g.Nz);
+                all_out = all_out && out;
+                all = all && (out || immersed_cell(g, i - a, j - b, kk));
+            }
+    return all && !all_out;
+}
 // inactive_node of the stencil nodes used by the immersed-aware reconstruction
 // (immersed_advective_fluxes.jl:114-152): Center nodes are inactive cells; Face nodes
 // are inactive when both adjacent cells are.
@@ -601,26 +617,49 @@ struct Ctx {
         const Field& n = NU();
         return 0.5 * (0.5 * (n(i, j - 1, k - 1) + n(i, j, k - 1)) + 0.5 * (n(i, j - 1, k) + n(i, j, k)));
     }
-    double S11(int i, int j, int k) const { return (m.u(i + 1, j, k) - m.u(i, j, k)) * (1 / g.dx); }
-    double S22(int i, int j, int k) const { return (m.v(i, j + 1, k) - m.v(i, j, k)) * (1 / g.dy); }
-    double S33(int i, int j, int k) const { return flatz ? 0.0 : (m.w(i, j, k + 1) - m.w(i, j, k)) * (1 / M.dzc(k)); }
-    double dyu(int i, int j, int k) const { return (m.u(i, j, k) - m.u(i, j - 1, k)) * (1 / g.dy); }
-    double dxv(int i, int j, int k) const { return (m.v(i, j, k) - m.v(i - 1, j, k)) * (1 / g.dx); }
-    double dzu(int i, int j, int k) const { return flatz ? 0.0 : (m.u(i, j, k) - m.u(i, j, k - 1)) * (1 / M.dzf(k)); }
-    double dxw(int i, int j, int k) const { return (m.w(i, j, k) - m.w(i - 1, j, k)) * (1 / g.dx); }
-    double dzv(int i, int j, int k) const { return flatz ? 0.0 : (m.v(i, j, k) - m.v(i, j, k - 1)) * (1 / M.dzf(k)); }
-    double dyw(int i, int j, int k) const { return (m.w(i, j, k) - m.w(i, j - 1, k)) * (1 / g.dy); }
+    // Conditional ∂ on an immersed grid (conditional_differences.jl:15-43): zero when either
+    // differenced node is an immersed-inactive node of the field's location.
+    bool cu(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return imm_inactive_node(g, i0, j0, k0, true, false, false) || imm_inactive_node(g, i1, j1, k1, true, false, false);
+    }
+    bool cv(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return imm_inactive_node(g, i0, j0, k0, false, true, false) || imm_inactive_node(g, i1, j1, k1, false, true, false);
+    }
+    bool cw(int i0, int j0, int k0, int i1, int j1, int k1) const {
+        return imm_inactive_node(g, i0, j0, k0, false, false, true) || imm_inactive_node(g, i1, j1, k1, false, false, true);
+    }
+    double S11(int i, int j, int k) const { return cu(i, j, k, i + 1, j, k) ? 0.0 : (m.u(i + 1, j, k) - m.u(i, j, k)) * (1 / g.dx); }
+    double S22(int i, int j, int k) const { return cv(i, j, k, i, j + 1, k) ? 0.0 : (m.v(i, j + 1, k) - m.v(i, j, k)) * (1 / g.dy); }
+    double S33(int i, int j, int k) const {
+        return (flatz || cw(i, j, k, i, j, k + 1)) ? 0.0 : (m.w(i, j, k + 1) - m.w(i, j, k)) * (1 / M.dzc(k));
+    }
+    double dyu(int i, int j, int k) const { return cu(i, j - 1, k, i, j, k) ? 0.0 : (m.u(i, j, k) - m.u(i, j - 1, k)) * (1 / g.dy); }
+    double dxv(int i, int j, int k) const { return cv(i - 1, j, k, i, j, k) ? 0.0 : (m.v(i, j, k) - m.v(i - 1, j, k)) * (1 / g.dx); }
+    double dzu(int i, int j, int k) const {
+        return (flatz || cu(i, j, k - 1, i, j, k)) ? 0.0 : (m.u(i, j, k) - m.u(i, j, k - 1)) * (1 / M.dzf(k));
+    }
+    double dxw(int i, int j, int k) const { return cw(i - 1, j, k, i, j, k) ? 0.0 : (m.w(i, j, k) - m.w(i - 1, j, k)) * (1 / g.dx); }
+    double dzv(int i, int j, int k) const {
+        return (flatz || cv(i, j, k - 1, i, j, k)) ? 0.0 : (m.v(i, j, k) - m.v(i, j, k - 1)) * (1 / M.dzf(k));
+    }
+    double dyw(int i, int j, int k) const { return cw(i, j - 1, k, i, j, k) ? 0.0 : (m.w(i, j, k) - m.w(i, j - 1, k)) * (1 / g.dy); }
     double S12(int i, int j, int k) const { return 0.5 * (dyu(i, j, k) + dxv(i, j, k)); }
     double S13(int i, int j, int k) const { return 0.5 * (dzu(i, j, k) + dxw(i, j, k)); }
     double S23(int i, int j, int k) const { return 0.5 * (dzv(i, j, k) + dyw(i, j, k)); }
 
     // viscous fluxes τ (-2 ν Σ)
-    double tau_ux(int i, int j, int k) const { return -2 * (NU()(i, j, k) * S11(i, j, k)); }
-    double tau_uy(int i, int j, int k) const { return -2 * (nu_ffc(i, j, k) * S12(i, j, k)); }
-    double tau_uz(int i, int j, int k) const { return -2 * (nu_fcf(i, j, k) * S13(i, j, k)); }
-    double tau_vy(int i, int j, int k) const { return -2 * (NU()(i, j, k) * S22(i, j, k)); }
-    double tau_vz(int i, int j, int k) const { return -2 * (nu_cff(i, j, k) * S23(i, j, k)); }
-    double tau_wz(int i, int j, int k) const { return -2 * (NU()(i, j, k) * S33(i, j, k)); }
+    // each viscous flux is zero on the immersed periphery of its location (conditional_flux,
+    // immersed_diffusive_fluxes.jl:25-40); the default immersed boundary condition adds none
+    bool zp(int i, int j, int k, bool fx, bool fy, bool fz) const { return imm_periph(g, i, j, k, fx, fy, fz); }
+    double tau_ux(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? 0.0 : -2 * (NU()(i, j, k) * S11(i, j, k)); }
+    double tau_uy(int i, int j, int k) const { return zp(i, j, k, true, true, false) ? 0.0 : -2 * (nu_ffc(i, j, k) * S12(i, j, k)); }
+    double tau_uz(int i, int j, int k) const { return zp(i, j, k, true, false, true) ? 0.0 : -2 * (nu_fcf(i, j, k) * S13(i, j, k)); }
+    double tau_vx(int i, int j, int k) const { return zp(i, j, k, true, true, false) ? 0.0 : -2 * (nu_ffc(i, j, k) * S12(i, j, k)); }
+    double tau_vy(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? 0.0 : -2 * (NU()(i, j, k) * S22(i, j, k)); }
+    double tau_vz(int i, int j, int k) const { return zp(i, j, k, false, true, true) ? 0.0 : -2 * (nu_cff(i, j, k) * S23(i, j, k)); }
+    double tau_wx(int i, int j, int k) const { return zp(i, j, k, true, false, true) ? 0.0 : -2 * (nu_fcf(i, j, k) * S13(i, j, k)); }
+    double tau_wy(int i, int j, int k) const { return zp(i, j, k, false, true, true) ? 0.0 : -2 * (nu_cff(i, j, k) * S23(i, j, k)); }
+    double tau_wz(int i, int j, int k) const { return zp(i, j, k, false, false, false) ? 0.0 : -2 * (NU()(i, j, k) * S33(i, j, k)); }
 
     // diffusive tracer fluxes; κ at faces = ℑ(κ_ccc) (/Pr for Smagorinsky)
     double kap_x(int n, int i, int j, int k) const {
@@ -635,9 +674,20 @@ struct Ctx {
         if (m.desc.closure == GBO_CLOSURE_AMD) { const Field& K = m.kappa[n]; return 0.5 * (K(i, j, k - 1) + K(i, j, k)); }
         return 0.5 * (m.nu(i, j, k - 1) + m.nu(i, j, k)) / m.desc.closure_Pr;
     }
-    double q_x(int n, const Field& cc, int i, int j, int k) const { return -kap_x(n, i, j, k) * ((cc(i, j, k) - cc(i - 1, j, k)) * (1 / g.dx)); }
-    double q_y(int n, const Field& cc, int i, int j, int k) const { return -kap_y(n, i, j, k) * ((cc(i, j, k) - cc(i, j - 1, k)) * (1 / g.dy)); }
-    double q_z(int n, const Field& cc, int i, int j, int k) const { return -kap_z(n, i, j, k) * ((cc(i, j, k) - cc(i, j, k - 1)) * (1 / M.dzf(k))); }
+    // conditional tracer gradients and zero flux on the immersed periphery of the flux
+    // location (immersed_diffusive_fluxes.jl:42-44)
+    double dcx(const Field& cc, int i, int j, int k) const {
+        return (imm_in(g, i - 1, j, k) || imm_in(g, i, j, k)) ? 0.0 : (cc(i, j, k) - cc(i - 1, j, k)) * (1 / g.dx);
+    }
+    double dcy(const Field& cc, int i, int j, int k) const {
+        return (imm_in(g, i, j - 1, k) || imm_in(g, i, j, k)) ? 0.0 : (cc(i, j, k) - cc(i, j - 1, k)) * (1 / g.dy);
+    }
+    double dcz(const Field& cc, int i, int j, int k) const {
+        return (imm_in(g, i, j, k - 1) || imm_in(g, i, j, k)) ? 0.0 : (cc(i, j, k) - cc(i, j, k - 1)) * (1 / M.dzf(k));
+    }
+    double q_x(int n, const Field& cc, int i, int j, int k) const { return zp(i, j, k, true, false, false) ? 0.0 : -kap_x(n, i, j, k) * dcx(cc, i, j, k); }
+    double q_y(int n, const Field& cc, int i, int j, int k) const { return zp(i, j, k, false, true, false) ? 0.0 : -kap_y(n, i, j, k) * dcy(cc, i, j, k); }
+    double q_z(int n, const Field& cc, int i, int j, int k) const { return zp(i, j, k, false, false, true) ? 0.0 : -kap_z(n, i, j, k) * dcz(cc, i, j, k); }
 
     bool closure_on() const { return m.desc.closure != GBO_CLOSURE_NONE; }
 
@@ -694,7 +744,7 @@ struct Ctx {
         }
         if (m.has_phy) G = G - ((imm_in(g, i, j - 1, k) || imm_in(g, i, j, k)) ? 0.0 : (m.phy(i, j, k) - m.phy(i, j - 1, k))) * (1 / g.dy);
         if (closure_on()) {
-            double dx_ = M.Ax_c(k) * (-2 * (nu_ffc(i + 1, j, k) * S12(i + 1, j, k))) - M.Ax_c(k) * (-2 * (nu_ffc(i, j, k) * S12(i, j, k)));
+            double dx_ = M.Ax_c(k) * tau_vx(i + 1, j, k) - M.Ax_c(k) * tau_vx(i, j, k);
             double dy_ = M.Ay_c(k) * tau_vy(i, j, k) - M.Ay_c(k) * tau_vy(i, j - 1, k);
             double dz_ = flatz ? 0.0 : (M.Az() * tau_vz(i, j, k + 1) - M.Az() * tau_vz(i, j, k));
             G = G - (1 / M.Vc(k)) * (dx_ + dy_ + dz_);
@@ -712,8 +762,8 @@ struct Ctx {
         double G = -adv;
         // buoyancy: with a hydrostatic pressure anomaly w gets no buoyancy term (:171-173)
         if (closure_on()) {
-            auto twx = [&](int ii) { return -2 * (nu_fcf(ii, j, k) * S13(ii, j, k)); };
-            auto twy = [&](int jj) { return -2 * (nu_cff(i, jj, k) * S23(i, jj, k)); };
+            auto twx = [&](int ii) { return tau_wx(ii, j, k); };
+            auto twy = [&](int jj) { return tau_wy(i, jj, k); };
             double dx_ = M.Ax_f(k) * twx(i + 1) - M.Ax_f(k) * twx(i);
             double dy_ = M.Ay_f(k) * twy(j + 1) - M.Ay_f(k) * twy(j);
             double dz_ = M.Az() * tau_wz(i, j, k) - M.Az() * tau_wz(i, j, k - 1);
@@ -769,8 +819,9 @@ double smagorinsky_nu(const Ctx& C, int i, int j, int k) {
     double N2 = 0;
     if (m.desc.buoyancy_tracer && !C.flatz) {
         const Field& b = m.c[0];
-        double b1 = (b(i, j, k) - b(i, j, k - 1)) * (1 / C.M.dzf(k));
-        double b2 = (b(i, j, k + 1) - b(i, j, k)) * (1 / C.M.dzf(k + 1));
+        // N² = ℑz(∂z b), conditional ∂ on an immersed grid
+        double b1 = (imm_in(C.g, i, j, k - 1) || imm_in(C.g, i, j, k)) ? 0.0 : (b(i, j, k) - b(i, j, k - 1)) * (1 / C.M.dzf(k));
+        double b2 = (imm_in(C.g, i, j, k) || imm_in(C.g, i, j, k + 1)) ? 0.0 : (b(i, j, k + 1) - b(i, j, k)) * (1 / C.M.dzf(k + 1));
         N2 = 0.5 * (b1 + b2);
     }
     double c0 = m.desc.closure_C, cb = m.desc.closure_Cb;
@@ -860,9 +911,10 @@ struct AMDops {
     }
     double kappa(const Field& c, int i, int j, int k) const {
         auto sq = [](double x) { return x * x; };
-        auto n_dxc = [&](int a, int b, int cc) { return Dfx() * ((c(a, b, cc) - c(a - 1, b, cc)) * (1 / C.g.dx)); };
-        auto n_dyc = [&](int a, int b, int cc) { return Dfy() * ((c(a, b, cc) - c(a, b - 1, cc)) * (1 / C.g.dy)); };
-        auto n_dzc = [&](int a, int b, int cc) { return Dfz(cc) * ((c(a, b, cc) - c(a, b, cc - 1)) * (1 / C.M.dzf(cc))); };
+        // conditional ∂ of the tracer on an immersed grid
+        auto n_dxc = [&](int a, int b, int cc) { return Dfx() * C.dcx(c, a, b, cc); };
+        auto n_dyc = [&](int a, int b, int cc) { return Dfy() * C.dcy(c, a, b, cc); };
+        auto n_dzc = [&](int a, int b, int cc) { return Dfz(cc) * C.dcz(c, a, b, cc); };
         auto dxc2 = [&](int a, int b, int cc) { return sq(n_dxc(a, b, cc)); };
         auto dyc2 = [&](int a, int b, int cc) { return sq(n_dyc(a, b, cc)); };
         auto dzc2 = [&](int a, int b, int cc) { return sq(n_dzc(a, b, cc)); };

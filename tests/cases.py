@@ -86,7 +86,7 @@ def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0
 
 
 def seamount(N=(32, 32, 16), float_type=np.float64, seed=0, solver="cg", reltol=0.0, abstol=0.0,
-             height=1200.0, width=800.0, N2=1e-6, U=0.1, noise=1e-3, stretched=False):
+             height=1200.0, width=800.0, N2=1e-6, U=0.1, noise=1e-3, stretched=False, closure=None):
     """Seamount on an ImmersedBoundaryGrid(GridFittedBottom): x, y in [-5, 5] km, z in [-2, 0] km,
     h = -2000 + height exp(-(x² + y²) / (2 width²)), b = N² z, u = U + noise, v, w = noise."""
     Nx, Ny, Nz = N
@@ -113,8 +113,9 @@ def seamount(N=(32, 32, 16), float_type=np.float64, seed=0, solver="cg", reltol=
             "v": noise * rng.uniform(-1, 1, (Nx, Ny, Nz)),
             "w": noise * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
             "b": N2 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz))}
+    cl = {None: None, "smagorinsky": og.SmagorinskyLilly, "amd": og.AnisotropicMinimumDissipation}[closure]
     return Case(grid, init, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
-                pressure_solver=ps)
+                pressure_solver=ps, closure=cl() if cl else None)
 
 
 def immersed_mask(grid):

@@ -99,3 +99,19 @@ def test_fft_preconditioned_cg_one_iteration_without_immersed_cells():
     phi = torch.zeros_like(rhs)
     m.poisson_solve_device(phi.data_ptr(), rhs.data_ptr())
     assert m.solver_iterations == 1
+
+
+@pytest.mark.parametrize("closure", ["smagorinsky", "amd"])
+def test_seamount_closure_fp64(closure):
+    # turbulence closures on the immersed grid: conditional strain rates and diffusive
+    # fluxes zeroed on the immersed periphery (immersed_diffusive_fluxes.jl:25-44)
+    c = cases.seamount((32, 32, 16), solver="cg", reltol=1e-13, abstol=1e-300, closure=closure, U=0.02, noise=2e-2)
+    m, r = c.start_gpu(), c.start_oracle()
+    names = FIELDS + ("nu",) + (("kappa",) if closure == "amd" else ())
+    compare(m, r, names, 1e-10)
+    og.time_step_(m, 20.0)
+    r.time_step(20.0)
+    compare(m, r, names, 1e-10)
+    og.time_step_(m, 20.0, 4)
+    r.time_step(20.0, 4)
+    compare(m, r, names, 1e-8)

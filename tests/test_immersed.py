@@ -95,3 +95,35 @@ def test_seamount_step_masks_and_incompressibility():
     div = (np.roll(u, -1, 0) - u) / dx + (np.roll(v, -1, 1) - v) / dy + (w[:, :, 1:] - w[:, :, :-1]) / dzc
     assert np.abs(div[~imm]).max() < 1e-9 * 0.1 / dx
     assert 0 < ref.last_cg_iterations() < 100
+
+
+@pytest.mark.parametrize("closure", ["smagorinsky", "amd"])
+def test_immersed_closure_without_immersed_cells_matches_rectilinear(closure):
+    # conditional strain rates and diffusive-flux masks reduce to the RectilinearGrid
+    # closure when no cell is immersed
+    flat = cases.seamount((16, 16, 12), solver="fft", height=-500.0, closure=closure, U=0.02, noise=2e-2)
+    ref_ibg = flat.start_oracle()
+    plain = cases.Case(flat.grid.underlying_grid, flat.init, **dict(flat.physics, pressure_solver=og.FFTBasedPoissonSolver()))
+    ref_plain = plain.start_oracle()
+    for r in (ref_ibg, ref_plain):
+        r.time_step(20.0, 2)
+    for name in ("u", "v", "w", "b", "p", "nu"):
+        a, b = ref_ibg.get(name), ref_plain.get(name)
+        assert np.abs(a - b).max() <= 1e-13 * max(np.abs(b).max(), 1e-30), name
+
+
+@pytest.mark.parametrize("closure", ["smagorinsky", "amd"])
+def test_immersed_closure_masks_fluxes(closure):
+    # with a closure the masks still hold and the active cells stay divergence-free
+    c = cases.seamount((16, 16, 12), solver="cg", reltol=1e-12, abstol=1e-300, closure=closure, U=0.02, noise=2e-2)
+    ref = c.start_oracle()
+    ref.time_step(20.0, 2)
+    imm = cases.immersed_mask(c.grid)
+    u, v, w, b = ref.get("u"), ref.get("v"), ref.get("w"), ref.get("b")
+    assert np.all(b[imm] == 0.0)
+    assert np.all(u[imm | np.roll(imm, 1, 0)] == 0.0)
+    dzc, _ = cases.interior_spacings(ref, 12)
+    dx, dy = c.grid.Lx / 16, c.grid.Ly / 16
+    div = (np.roll(u, -1, 0) - u) / dx + (np.roll(v, -1, 1) - v) / dy + (w[:, :, 1:] - w[:, :, :-1]) / dzc
+    assert np.abs(div[~imm]).max() < 1e-9 * 0.1 / dx
+    assert np.isfinite(ref.get("nu")).all()

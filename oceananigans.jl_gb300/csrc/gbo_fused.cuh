@@ -27,6 +27,9 @@ constexpr int TX = 32, TY = 8, H = 3;
 constexpr int PX = TX + 2 * H, PY = TY + 2 * H, PS = PX * PY;
 constexpr int NT = TX * TY;
 constexpr int EPT = (PS + NT - 1) / NT;  // plane elements loaded per thread
+// immersed-boundary column table: halo 4 (a centred reconstruction checks cells up to 4 away)
+constexpr int KBH = 4, KBX = TX + 2 * KBH, KBY = TY + 2 * KBH, KBS = KBX * KBY;
+GBO_D int kbidx(int x, int y) { return (y + KBH) * KBX + (x + KBH); }
 
 GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + H); }
 
@@ -45,13 +48,16 @@ struct Smem {
     FT CC[2][PS];                      // tracer: k (+k+1)
     FT WX[NWX][TY][TX + 1];
     FT SY[NSY][TY + 1][TX];
-    FT KP[3][PS];                      // AMD κₑ: k, k+1 (+k+2); last, so that other closures
-                                       // launch without it (smem_bytes)
+    // last, so that launches without AMD or an immersed boundary omit it (smem_bytes):
+    union {
+        FT KP[3][PS];                  // AMD κₑ: k, k+1 (+k+2)
+        int KB[KBS];                   // immersed cells per column, tile with halo 4
+    };
 };
-// Dynamic shared memory of a launch: the κₑ ring only with AMD.
+// Dynamic shared memory of a launch: the last member only with AMD or an immersed grid.
 template <typename FT>
-constexpr size_t smem_bytes(bool amd) {
-    return amd ? sizeof(Smem<FT>) : sizeof(Smem<FT>) - sizeof(FT) * 3 * PS;
+constexpr size_t smem_bytes(bool amd_or_ibg) {
+    return amd_or_ibg ? sizeof(Smem<FT>) : sizeof(Smem<FT>) - sizeof(FT) * 3 * PS;
 }
 
 // Asynchronous 4/8-byte global -> shared copy; src_bytes = 0 writes zero.
@@ -125,7 +131,7 @@ struct Col {
 
 // Column-marching fused kernel (see the file header).  TR: also advance one tracer
 // (P.c -> P.co, P.Gc) in the same march.
-template <typename FT, bool TR, int CLK>
+template <typename FT, bool TR, int CLK, bool IBG = false>
 __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 1) k_momentum_fused(StepP<FT> P, int kchunk) {
     using namespace fused;
     extern __shared__ unsigned char smem_raw[];
@@ -153,6 +159,55 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     auto m3 = [](int k) { return ((k % 3) + 3) % 3; };
     auto m4 = [](int k) { return k & 3; };
     auto m2 = [](int k) { return k & 1; };
+
+    // ---- immersed boundary (IBG): the rules of gbo_tendency.cuh (ibg_level, imm_periph,
+    // cond_zero) evaluated from a shared tile of the column table; (x, y) are tile-local ----
+    static_assert(!IBG || CLK == CL_NONE, "the fused immersed-boundary kernel carries no closure");
+    if constexpr (IBG) {
+        for (int e = tid; e < KBS; e += NT) {
+            const int x = e % KBX - KBH, y = e / KBX - KBH;
+            s.KB[e] = __ldg(g.kbot + wrapi(i0 + x, g.Nx) + (size_t)g.Nx * wrapi(j0 + y, g.Ny));
+        }
+    }
+    // cell (x, y, k) immersed / inactive (immersed or outside the Bounded z)
+    auto imm_t = [&](int x, int y, int kk) { return kk >= 0 && kk < Nz && kk < s.KB[kbidx(x, y)]; };
+    auto inact_t = [&](int x, int y, int kk) { return kk < 0 || kk >= Nz || kk < s.KB[kbidx(x, y)]; };
+    // immersed_peripheral_node with Face flags
+    auto periph_t = [&](int x, int y, int kk, bool fx, bool fy, bool fzz) {
+        bool any_imm = false, any_out = false;
+        for (int a = 0; a <= (fx ? 1 : 0); ++a)
+            for (int b = 0; b <= (fy ? 1 : 0); ++b)
+                for (int c2 = 0; c2 <= (fzz ? 1 : 0); ++c2) {
+                    const int k2 = kk - c2;
+                    const bool out = k2 < 0 || k2 >= Nz;
+                    any_out |= out;
+                    any_imm |= (!out) && k2 < s.KB[kbidx(x - a, y - b)];
+                }
+        return any_imm && !any_out;
+    };
+    // reconstruction level (3 WENO5 / C4, 2 WENO3, 1 second order) in direction d at (x, y, k)
+    auto level_t = [&](int d, int x, int y, int kk, bool loc_face) {
+        for (int B = 3; B >= 2; --B) {
+            const int lo = loc_face ? -B : -B + 1, hi = loc_face ? B - 1 : B;
+            bool near = false;
+            for (int o = lo; o <= hi; ++o) {
+                const int xx = x + (d == 0 ? o : 0), yy = y + (d == 1 ? o : 0), k2 = kk + (d == 2 ? o : 0);
+                bool ia = inact_t(xx, yy, k2);
+                if (!loc_face) ia = ia && inact_t(xx - (d == 0), yy - (d == 1), k2 - (d == 2));
+                near |= ia;
+            }
+            if (!near) return B;
+        }
+        return 1;
+    };
+    auto sym_t = [&](int d, int x, int y, int kk, bool loc_face) { return level_t(d, x, y, kk, loc_face) == 3 ? 3 : 1; };
+    // advective momentum flux ũ ψ on the immersed grid: zero on the periphery, symmetric
+    // (level sl) and biased (level bl) reconstructions of reduced order near inactive cells
+    auto mflux_t = [&](bool zero, auto qs, int sl, auto qb, int bl) -> FT {
+        if (zero) return FT(0);
+        const FT ut = symm<FT>(qs, sl);
+        return ut * biased<FT>(qb, bias_left(ut), bl);
+    };
 
     // ---- prologue: planes for level kb ----
     issue_plane(s.U[m3(kb - 1)], P.u, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
@@ -192,6 +247,16 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     // bottom fluxes at level kb (faces kb / centre kb-1)
     {
         const FT* Wk = s.W[m3(kb)];
+        if constexpr (IBG) {
+            c.fWu = mflux_t(periph_t(tx, ty, kb, true, false, true), [&](int o) { return Az * Wk[pidx(tx + o, ty)]; },
+                            sym_t(0, tx, ty, kb, true), [&](int o) { return c.uc[3 + o]; }, level_t(2, tx, ty, kb, true));
+            c.fWv = mflux_t(periph_t(tx, ty, kb, false, true, true), [&](int o) { return Az * Wk[pidx(tx, ty + o)]; },
+                            sym_t(1, tx, ty, kb, true), [&](int o) { return c.vc[3 + o]; }, level_t(2, tx, ty, kb, true));
+            const int kc = kb - 1;
+            c.fWw = mflux_t(periph_t(tx, ty, kc, false, false, false), [&](int o) { return Az * (o == -3 ? wm3 : c.wc[2 + o]); },
+                            sym_t(2, tx, ty, kc, false), [&](int o) { return o == -3 ? wm3 : c.wc[2 + o]; },
+                            level_t(2, tx, ty, kc, false));
+        } else {
         {
             FT wt = cen4<FT>(Az * Wk[pidx(tx - 2, ty)], Az * Wk[pidx(tx - 1, ty)], Az * Wk[pidx(tx, ty)], Az * Wk[pidx(tx + 1, ty)]);
             auto q = [&](int o) { return c.uc[3 + o]; };
@@ -208,6 +273,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             FT wt = symm<FT>(qs, zlev_symm_center(kc + 1, Nz));
             auto qb = [&](int o) { return o == -3 ? wm3 : c.wc[2 + o]; };
             c.fWw = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(kc + 1, Nz));
+        }
         }
         c.t13 = c.t23 = c.t33 = FT(0);
         if (closure) {
@@ -226,7 +292,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         if (TR) {
             FT wk = c.wc[2];
             auto q = [&](int o) { return c.cc[3 + o]; };
-            c.fWc = Az * wk * biased<FT>(q, bias_left(wk), zlev_biased_face(kb + 1, Nz));
+            c.fWc = Az * wk * biased<FT>(q, bias_left(wk), IBG ? level_t(2, tx, ty, kb, true) : zlev_biased_face(kb + 1, Nz));
             c.qzc = FT(0);
             if (closure) {
                 FT km = amd ? km_amd : s.NU[m4(kb - 1)][pidx(tx, ty)];
@@ -285,10 +351,18 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             FT S[6];
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x - 3 + o, y)];
-            s.WX[A_UU][y][x] = flux_c4_w5<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4], S);
+            if constexpr (IBG)
+                s.WX[A_UU][y][x] = mflux_t(periph_t(x - 1, y, k, false, false, false), [&](int o) { return Ax * S[o + 3]; },
+                                           sym_t(0, x - 1, y, k, false), [&](int o) { return S[o + 3]; }, level_t(0, x - 1, y, k, false));
+            else
+                s.WX[A_UU][y][x] = flux_c4_w5<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4], S);
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x - 3 + o, y)];
-            s.WX[A_UV][y][x] = flux_c4_w5<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)], S);
+            if constexpr (IBG)
+                s.WX[A_UV][y][x] = mflux_t(periph_t(x, y, k, true, true, false), [&](int o) { return Ax * Uk[pidx(x, y + o)]; },
+                                           sym_t(1, x, y, k, true), [&](int o) { return S[o + 3]; }, level_t(0, x, y, k, true));
+            else
+                s.WX[A_UV][y][x] = flux_c4_w5<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)], S);
             if (!fz) {
                 FT uz[4];
                 if (own) {
@@ -299,10 +373,15 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     for (int o = 0; o < 4; ++o) uz[o] = Ug(i0 + x, j0 + y, k - 2 + o);
                 }
                 auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
-                FT ut = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
 #pragma unroll
                 for (int o = 0; o < 6; ++o) S[o] = Wk[pidx(x - 3 + o, y)];
-                s.WX[A_UW][y][x] = ut * weno5<FT>(S, bias_left(ut));
+                if constexpr (IBG) {
+                    s.WX[A_UW][y][x] = mflux_t(periph_t(x, y, k, true, false, true), qs, sym_t(2, x, y, k, true),
+                                               [&](int o) { return S[o + 3]; }, level_t(0, x, y, k, true));
+                } else {
+                    FT ut = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+                    s.WX[A_UW][y][x] = ut * weno5<FT>(S, bias_left(ut));
+                }
             }
             if (closure) {
                 FT s11 = (Uk[pidx(x, y)] - Uk[pidx(x - 1, y)]) * g.rdx;
@@ -324,7 +403,10 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT ut = Uk[pidx(x, y)];
 #pragma unroll
                 for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x - 3 + o, y)];
-                s.WX[A_CX][y][x] = Ax * ut * weno5<FT>(S, bias_left(ut));
+                if constexpr (IBG)
+                    s.WX[A_CX][y][x] = Ax * ut * biased<FT>([&](int o) { return S[o + 3]; }, bias_left(ut), level_t(0, x, y, k, true));
+                else
+                    s.WX[A_CX][y][x] = Ax * ut * weno5<FT>(S, bias_left(ut));
                 if (closure) {
                     const FT* K = amd ? Kk : Nk;
                     FT kx = amd ? FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) / P.Pr;
@@ -336,10 +418,18 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             FT S[6];
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x, y - 3 + o)];
-            s.SY[A_VU][y][x] = flux_c4_w5<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)], S);
+            if constexpr (IBG)
+                s.SY[A_VU][y][x] = mflux_t(periph_t(x, y, k, true, true, false), [&](int o) { return Ay * Vk[pidx(x + o, y)]; },
+                                           sym_t(0, x, y, k, true), [&](int o) { return S[o + 3]; }, level_t(1, x, y, k, true));
+            else
+                s.SY[A_VU][y][x] = flux_c4_w5<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)], S);
 #pragma unroll
             for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x, y - 3 + o)];
-            s.SY[A_VV][y][x] = flux_c4_w5<FT>(Ay * S[1], Ay * S[2], Ay * S[3], Ay * S[4], S);
+            if constexpr (IBG)
+                s.SY[A_VV][y][x] = mflux_t(periph_t(x, y - 1, k, false, false, false), [&](int o) { return Ay * S[o + 3]; },
+                                           sym_t(1, x, y - 1, k, false), [&](int o) { return S[o + 3]; }, level_t(1, x, y - 1, k, false));
+            else
+                s.SY[A_VV][y][x] = flux_c4_w5<FT>(Ay * S[1], Ay * S[2], Ay * S[3], Ay * S[4], S);
             if (!fz) {
                 FT vz[4];
                 if (own) {
@@ -350,10 +440,15 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     for (int o = 0; o < 4; ++o) vz[o] = Vg(i0 + x, j0 + y, k - 2 + o);
                 }
                 auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
-                FT vt = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
 #pragma unroll
                 for (int o = 0; o < 6; ++o) S[o] = Wk[pidx(x, y - 3 + o)];
-                s.SY[A_VW][y][x] = vt * weno5<FT>(S, bias_left(vt));
+                if constexpr (IBG) {
+                    s.SY[A_VW][y][x] = mflux_t(periph_t(x, y, k, false, true, true), qs, sym_t(2, x, y, k, true),
+                                               [&](int o) { return S[o + 3]; }, level_t(1, x, y, k, true));
+                } else {
+                    FT vt = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+                    s.SY[A_VW][y][x] = vt * weno5<FT>(S, bias_left(vt));
+                }
             }
             if (closure) {
                 FT s22 = (Vk[pidx(x, y)] - Vk[pidx(x, y - 1)]) * g.rdy;
@@ -375,7 +470,10 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT vt = Vk[pidx(x, y)];
 #pragma unroll
                 for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x, y - 3 + o)];
-                s.SY[A_CY][y][x] = Ay * vt * weno5<FT>(S, bias_left(vt));
+                if constexpr (IBG)
+                    s.SY[A_CY][y][x] = Ay * vt * biased<FT>([&](int o) { return S[o + 3]; }, bias_left(vt), level_t(1, x, y, k, true));
+                else
+                    s.SY[A_CY][y][x] = Ay * vt * weno5<FT>(S, bias_left(vt));
                 if (closure) {
                     const FT* K = amd ? Kk : Nk;
                     FT ky = amd ? FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) / P.Pr;
@@ -396,6 +494,14 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         FT fWu_t = FT(0), fWv_t = FT(0), fWw_t = FT(0), t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);
         FT fWc_t = FT(0), qzc_t = FT(0);
         if (!fz) {
+            if constexpr (IBG) {
+                fWu_t = mflux_t(periph_t(tx, ty, k + 1, true, false, true), [&](int o) { return Az * Wp[pidx(tx + o, ty)]; },
+                                sym_t(0, tx, ty, k + 1, true), [&](int o) { return c.uc[4 + o]; }, level_t(2, tx, ty, k + 1, true));
+                fWv_t = mflux_t(periph_t(tx, ty, k + 1, false, true, true), [&](int o) { return Az * Wp[pidx(tx, ty + o)]; },
+                                sym_t(1, tx, ty, k + 1, true), [&](int o) { return c.vc[4 + o]; }, level_t(2, tx, ty, k + 1, true));
+                fWw_t = mflux_t(periph_t(tx, ty, k, false, false, false), [&](int o) { return Az * c.wc[3 + o]; },
+                                sym_t(2, tx, ty, k, false), [&](int o) { return c.wc[3 + o]; }, level_t(2, tx, ty, k, false));
+            } else {
             {
                 FT wt = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
                 auto q = [&](int o) { return c.uc[4 + o]; };
@@ -412,6 +518,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 auto qb = [&](int o) { return c.wc[3 + o]; };
                 fWw_t = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, Nz));
             }
+            }
             if (closure) {
                 FT nfcf = FT(0.5) * (FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx - 1, ty)] + Np[pidx(tx, ty)]));
                 FT dzu = (c.uc[4] - c.uc[3]) * M.rdzf(k + 1);
@@ -426,7 +533,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             if (TR) {
                 FT wt = c.wc[3];
                 auto q = [&](int o) { return c.cc[4 + o]; };
-                fWc_t = Az * wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
+                fWc_t = Az * wt * biased<FT>(q, bias_left(wt), IBG ? level_t(2, tx, ty, k + 1, true) : zlev_biased_face(k + 2, Nz));
                 if (closure) {
                     const FT* K0 = amd ? Kk : Nk;
                     const FT* K1 = amd ? Kp : Np;
@@ -448,12 +555,14 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dz_ = fz ? FT(0) : (fWu_t - c.fWu);
                 FT G = -(rVc * (dx_ + dy_ + dz_));
                 if (P.has_cor) {
-                    FT ixy = FT(0.5) * (FT(0.5) * (Ay * Vk[pidx(tx - 1, ty)] + Ay * Vk[pidx(tx, ty)]) +
-                                        FT(0.5) * (Ay * Vk[pidx(tx - 1, ty + 1)] + Ay * Vk[pidx(tx, ty + 1)]));
+                    // masked_Ay_qᶜᶠᶜ on an immersed grid (coriolis_schemes.jl:55-58)
+                    auto AyV = [&](int x, int y) { return (IBG && periph_t(x, y, k, false, true, false)) ? FT(0) : Ay * Vk[pidx(x, y)]; };
+                    FT ixy = FT(0.5) * (FT(0.5) * (AyV(tx - 1, ty) + AyV(tx, ty)) + FT(0.5) * (AyV(tx - 1, ty + 1) + AyV(tx, ty + 1)));
                     FT xfu = -P.f * ixy * (FT(1) / Ay);
                     G = G - xfu;
                 }
-                if (P.has_phy) G = G - (PHk[pidx(tx, ty)] - PHk[pidx(tx - 1, ty)]) * g.rdx;
+                if (P.has_phy)
+                    G = G - ((IBG && (imm_t(tx - 1, ty, k) || imm_t(tx, ty, k))) ? FT(0) : (PHk[pidx(tx, ty)] - PHk[pidx(tx - 1, ty)])) * g.rdx;
                 if (closure) {
                     FT cdx = Ax * s.WX[C_11][ty][tx + 1] - Ax * s.WX[C_11][ty][tx];
                     FT cdy = Ay * s.SY[C_12N][ty + 1][tx] - Ay * s.SY[C_12N][ty][tx];
@@ -469,12 +578,13 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dz_ = fz ? FT(0) : (fWv_t - c.fWv);
                 FT G = -(rVc * (dx_ + dy_ + dz_));
                 if (P.has_cor) {
-                    FT ixy = FT(0.5) * (FT(0.5) * (Ax * Uk[pidx(tx, ty - 1)] + Ax * Uk[pidx(tx + 1, ty - 1)]) +
-                                        FT(0.5) * (Ax * Uk[pidx(tx, ty)] + Ax * Uk[pidx(tx + 1, ty)]));
+                    auto AxU = [&](int x, int y) { return (IBG && periph_t(x, y, k, true, false, false)) ? FT(0) : Ax * Uk[pidx(x, y)]; };
+                    FT ixy = FT(0.5) * (FT(0.5) * (AxU(tx, ty - 1) + AxU(tx + 1, ty - 1)) + FT(0.5) * (AxU(tx, ty) + AxU(tx + 1, ty)));
                     FT yfu = P.f * ixy * (FT(1) / Ax);
                     G = G - yfu;
                 }
-                if (P.has_phy) G = G - (PHk[pidx(tx, ty)] - PHk[pidx(tx, ty - 1)]) * g.rdy;
+                if (P.has_phy)
+                    G = G - ((IBG && (imm_t(tx, ty - 1, k) || imm_t(tx, ty, k))) ? FT(0) : (PHk[pidx(tx, ty)] - PHk[pidx(tx, ty - 1)])) * g.rdy;
                 if (closure) {
                     FT cdx = Ax * s.WX[C_12][ty][tx + 1] - Ax * s.WX[C_12][ty][tx];
                     FT cdy = Ay * s.SY[C_22][ty + 1][tx] - Ay * s.SY[C_22][ty][tx];

@@ -281,9 +281,10 @@ const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", 
 
 // The fused momentum kernel is compiled per closure kind; these pick the instance.
 template <typename FT, bool TR>
-void launch_fused(int closure, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk) {
-    const size_t smem = fused::smem_bytes<FT>(closure == CL_AMD);
-    if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk);
+void launch_fused(int closure, bool ibg, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk) {
+    const size_t smem = fused::smem_bytes<FT>(closure == CL_AMD || ibg);
+    if (ibg) k_momentum_fused<FT, TR, CL_NONE, true><<<grid, block, smem, st>>>(P, kchunk);
+    else if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk);
     else if (closure == CL_AMD) k_momentum_fused<FT, TR, CL_AMD><<<grid, block, smem, st>>>(P, kchunk);
     else k_momentum_fused<FT, TR, CL_NONE><<<grid, block, smem, st>>>(P, kchunk);
 }
@@ -293,7 +294,8 @@ cudaError_t fused_set_smem() {
     cudaError_t e = cudaSuccess;
     for (const void* f : {(const void*)k_momentum_fused<FT, true, CL_NONE>, (const void*)k_momentum_fused<FT, true, CL_SMAG>,
                           (const void*)k_momentum_fused<FT, true, CL_AMD>, (const void*)k_momentum_fused<FT, false, CL_NONE>,
-                          (const void*)k_momentum_fused<FT, false, CL_SMAG>, (const void*)k_momentum_fused<FT, false, CL_AMD>}) {
+                          (const void*)k_momentum_fused<FT, false, CL_SMAG>, (const void*)k_momentum_fused<FT, false, CL_AMD>,
+                          (const void*)k_momentum_fused<FT, true, CL_NONE, true>, (const void*)k_momentum_fused<FT, false, CL_NONE, true>}) {
         cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
         if (r != cudaSuccess) e = r;
     }
@@ -834,8 +836,8 @@ struct ModelImpl : gbo_model {
         const dim3 fgrid((Nx + fused::TX - 1) / fused::TX, (Ny + fused::TY - 1) / fused::TY, (Nz + kchunk - 1) / kchunk);
         const dim3 fblock(fused::TX, fused::TY);
         int tracer0 = 1;
-        if (ibg) {
-            // the column-marching kernel has no immersed-boundary logic: per-point kernels
+        if (ibg && desc.closure != GBO_CLOSURE_NONE) {
+            // closures on an immersed grid: the per-point kernels carry the conditional strain rates
             pre(G_MOMENTUM);
             k_momentum<FT><<<grd(), blk(), 0, stream>>>(P);
             check_launch();
@@ -848,11 +850,11 @@ struct ModelImpl : gbo_model {
             M0.flux_top = FT(desc.tracer_flux_top[0]);
             M0.flux_bot = FT(desc.tracer_flux_bottom[0]);
             pre(G_MOMENTUM);
-            launch_fused<FT, true>(desc.closure, fgrid, fblock, stream, M0, kchunk);
+            launch_fused<FT, true>(desc.closure, ibg, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         } else {
             pre(G_MOMENTUM);
-            launch_fused<FT, false>(desc.closure, fgrid, fblock, stream, M0, kchunk);
+            launch_fused<FT, false>(desc.closure, ibg, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         }
         for (int n = tracer0; n < ntr; ++n) {

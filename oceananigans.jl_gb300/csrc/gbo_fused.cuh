@@ -666,9 +666,19 @@ namespace smag {
 constexpr int TX = 32, TY = 8, KT = 4;
 constexpr int BX = TX + 2, BY = TY + 2, BZ = KT + 2, BS = BX * BY * BZ;
 GBO_D int bidx(int x, int y, int z) { return ((z + 1) * BY + (y + 1)) * BX + (x + 1); }
+// squared edge strains of the tile: Σ₁₂² at (x ∈ 0..TX, y ∈ 0..TY, z < KT),
+// Σ₁₃² at (x ∈ 0..TX, y < TY, z ∈ 0..KT), Σ₂₃² at (x < TX, y ∈ 0..TY, z ∈ 0..KT)
+constexpr int E12 = (TX + 1) * (TY + 1) * KT, E13 = (TX + 1) * TY * (KT + 1), E23 = TX * (TY + 1) * (KT + 1);
+GBO_D int i12(int x, int y, int z) { return (z * (TY + 1) + y) * (TX + 1) + x; }
+GBO_D int i13(int x, int y, int z) { return (z * TY + y) * (TX + 1) + x; }
+GBO_D int i23(int x, int y, int z) { return (z * (TY + 1) + y) * TX + x; }
 template <typename FT>
 struct Smem {
     FT u[BS], v[BS], w[BS], b[BS];
+};
+template <typename FT>
+struct SmemS : Smem<FT> {
+    FT s12[E12], s13[E13], s23[E23];
 };
 }  // namespace smag
 
@@ -676,62 +686,85 @@ template <typename FT>
 __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __restrict__ nu_out) {
     using namespace smag;
     extern __shared__ unsigned char smem_raw[];
-    Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
+    SmemS<FT>& s = *reinterpret_cast<SmemS<FT>*>(smem_raw);
     const GridP<FT>& g = P.g;
     Met<FT> M(g);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Bg = cfld(P.b, g);
-    WFld<FT> Wg = wfld(P.w, g);
     const bool buoy = P.buoyancy && !g.flatz;
+    const int Nz = g.Nz, fz = g.flatz;
+    const size_t plane = (size_t)g.Nx * g.Ny;
+    // tile fill with asynchronous copies: halos synthesised as in CFld / WFld (periodic
+    // wrap in x, y; one mirrored layer in z and zero beyond for centres; zero at and
+    // beyond the walls for w), a zero-filled copy where the value is zero
     for (int e = tid; e < BS; e += TX * TY) {
-        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
-        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
-        s.u[e] = Ug(gi, gj, gk);
-        s.v[e] = Vg(gi, gj, gk);
-        s.w[e] = Wg(gi, gj, gk);
-        s.b[e] = buoy ? Bg(gi, gj, gk) : FT(0);
+        const int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
+        const size_t col = wrapi(i0 + x, g.Nx) + (size_t)g.Nx * wrapi(j0 + y, g.Ny);
+        const int zc = fused::zsrc_c(k0 + z, Nz, fz), zw = fz ? -1 : fused::zsrc_w(k0 + z, Nz);
+        const size_t oc = col + (zc < 0 ? 0 : (size_t)zc * plane), ow = col + (zw < 0 ? 0 : (size_t)zw * plane);
+        fused::cp_async(&s.u[e], P.u + oc, zc < 0);
+        fused::cp_async(&s.v[e], P.v + oc, zc < 0);
+        if (fz) s.w[e] = FT(0);
+        else fused::cp_async(&s.w[e], P.w + ow, zw < 0);
+        if (buoy) fused::cp_async(&s.b[e], P.b + oc, zc < 0);
+        else s.b[e] = FT(0);
+    }
+    fused::cp_async_commit();
+    fused::cp_async_wait_all();
+    __syncthreads();
+    auto U = [&](int x, int y, int zz) { return s.u[bidx(x, y, zz)]; };
+    auto V = [&](int x, int y, int zz) { return s.v[bidx(x, y, zz)]; };
+    auto W = [&](int x, int y, int zz) { return s.w[bidx(x, y, zz)]; };
+    // strain components at the staggered points around the cells (velocity_tracer_gradients.jl),
+    // each evaluated once for the tile
+    for (int e = tid; e < E12; e += TX * TY) {
+        const int x = e % (TX + 1), y = (e / (TX + 1)) % (TY + 1), z = e / ((TX + 1) * (TY + 1));
+        FT dyu = (U(x, y, z) - U(x, y - 1, z)) * g.rdy;
+        FT dxv = (V(x, y, z) - V(x - 1, y, z)) * g.rdx;
+        FT v12 = FT(0.5) * (dyu + dxv);
+        s.s12[e] = v12 * v12;
+    }
+    for (int e = tid; e < E13; e += TX * TY) {
+        const int x = e % (TX + 1), y = (e / (TX + 1)) % TY, z = e / ((TX + 1) * TY);
+        FT v13 = FT(0);
+        if (!fz) {
+            FT dzu = (U(x, y, z) - U(x, y, z - 1)) * M.rdzf(k0 + z);
+            FT dxw = (W(x, y, z) - W(x - 1, y, z)) * g.rdx;
+            v13 = FT(0.5) * (dzu + dxw);
+        }
+        s.s13[e] = v13 * v13;
+    }
+    for (int e = tid; e < E23; e += TX * TY) {
+        const int x = e % TX, y = (e / TX) % (TY + 1), z = e / (TX * (TY + 1));
+        FT v23 = FT(0);
+        if (!fz) {
+            FT dzv = (V(x, y, z) - V(x, y, z - 1)) * M.rdzf(k0 + z);
+            FT dyw = (W(x, y, z) - W(x, y - 1, z)) * g.rdy;
+            v23 = FT(0.5) * (dzv + dyw);
+        }
+        s.s23[e] = v23 * v23;
     }
     __syncthreads();
     const int i = i0 + tx, j = j0 + ty;
     if (i >= g.Nx || j >= g.Ny) return;
     for (int z = 0; z < KT; ++z) {
         const int k = k0 + z;
-        if (k >= g.Nz) break;
-        auto U = [&](int x, int y, int zz) { return s.u[bidx(x, y, zz)]; };
-        auto V = [&](int x, int y, int zz) { return s.v[bidx(x, y, zz)]; };
-        auto W = [&](int x, int y, int zz) { return s.w[bidx(x, y, zz)]; };
-        // strain components at the staggered points around the cell (velocity_tracer_gradients.jl)
-        auto S12 = [&](int x, int y) {
-            FT dyu = (U(x, y, z) - U(x, y - 1, z)) * g.rdy;
-            FT dxv = (V(x, y, z) - V(x - 1, y, z)) * g.rdx;
-            return FT(0.5) * (dyu + dxv);
-        };
-        auto S13 = [&](int x, int zz) {
-            if (g.flatz) return FT(0);
-            FT dzu = (U(x, ty, zz) - U(x, ty, zz - 1)) * M.rdzf(k0 + zz);
-            FT dxw = (W(x, ty, zz) - W(x - 1, ty, zz)) * g.rdx;
-            return FT(0.5) * (dzu + dxw);
-        };
-        auto S23 = [&](int y, int zz) {
-            if (g.flatz) return FT(0);
-            FT dzv = (V(tx, y, zz) - V(tx, y, zz - 1)) * M.rdzf(k0 + zz);
-            FT dyw = (W(tx, y, zz) - W(tx, y - 1, zz)) * g.rdy;
-            return FT(0.5) * (dzv + dyw);
-        };
-        auto sq = [](FT x) { return x * x; };
+        if (k >= Nz) break;
         FT s11 = (U(tx + 1, ty, z) - U(tx, ty, z)) * g.rdx;
         FT s22 = (V(tx, ty + 1, z) - V(tx, ty, z)) * g.rdy;
-        FT s33 = g.flatz ? FT(0) : (W(tx, ty, z + 1) - W(tx, ty, z)) * M.rdzc(k);
+        FT s33 = fz ? FT(0) : (W(tx, ty, z + 1) - W(tx, ty, z)) * M.rdzc(k);
         FT tr = s11 * s11 + s22 * s22 + s33 * s33;
-        FT ixy = FT(0.5) * (FT(0.5) * (sq(S12(tx, ty)) + sq(S12(tx + 1, ty))) + FT(0.5) * (sq(S12(tx, ty + 1)) + sq(S12(tx + 1, ty + 1))));
+        FT ixy = FT(0.5) * (FT(0.5) * (s.s12[i12(tx, ty, z)] + s.s12[i12(tx + 1, ty, z)]) +
+                            FT(0.5) * (s.s12[i12(tx, ty + 1, z)] + s.s12[i12(tx + 1, ty + 1, z)]));
         FT ixz, iyz;
-        if (g.flatz) {
+        if (fz) {
             ixz = FT(0);
             iyz = FT(0);
         } else {
-            ixz = FT(0.5) * (FT(0.5) * (sq(S13(tx, z)) + sq(S13(tx + 1, z))) + FT(0.5) * (sq(S13(tx, z + 1)) + sq(S13(tx + 1, z + 1))));
-            iyz = FT(0.5) * (FT(0.5) * (sq(S23(ty, z)) + sq(S23(ty + 1, z))) + FT(0.5) * (sq(S23(ty, z + 1)) + sq(S23(ty + 1, z + 1))));
+            ixz = FT(0.5) * (FT(0.5) * (s.s13[i13(tx, ty, z)] + s.s13[i13(tx + 1, ty, z)]) +
+                             FT(0.5) * (s.s13[i13(tx, ty, z + 1)] + s.s13[i13(tx + 1, ty, z + 1)]));
+            iyz = FT(0.5) * (FT(0.5) * (s.s23[i23(tx, ty, z)] + s.s23[i23(tx, ty + 1, z)]) +
+                             FT(0.5) * (s.s23[i23(tx, ty, z + 1)] + s.s23[i23(tx, ty + 1, z + 1)]));
         }
         FT Sig2 = tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
         FT D3 = g.dx * g.dy * M.dzc(k);

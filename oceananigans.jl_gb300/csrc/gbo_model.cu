@@ -515,7 +515,7 @@ struct ModelImpl : gbo_model {
         while (YT > 1 && (size_t)2 * YT * Ny * cs_ > lim) YT /= 2;
         smem_y = (size_t)2 * YT * Ny * cs_;
         GBO_CUDA(fused_set_smem<FT>());
-        GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::SmemS<FT>)));
         GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         kchunk = flat ? 1 : std::min(16, Nz);
         // The pass kernels are shared by every model in the process: allow them the device's
@@ -801,7 +801,7 @@ struct ModelImpl : gbo_model {
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
             pre(G_CLOSURE);
-            k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(P, nu.p);
+            k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemS<FT>), stream>>>(P, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;

@@ -113,3 +113,34 @@ def test_turbulence_2d_128_400_steps():
         done = n
         compare(m, r, ("u", "v", "p"), tol)
     assert m.clock[1] == 400
+
+
+def test_convection_full_size_fp32_against_fp64():
+    # the convection benchmark grid (256²×128): FP32 against FP64 on the GPU after 100
+    # steps, and incompressibility of both (test_time_stepping.jl:138-171 at full size)
+    c32 = cases.convection_3d((256, 256, 128), float_type=np.float32, seed=5)
+    c64 = cases.convection_3d((256, 256, 128), seed=5)
+    m32, m64 = c32.start_gpu(), c64.start_gpu()
+    og.time_step_(m32, 2.0, 100)
+    og.time_step_(m64, 2.0, 100)
+    errs = {n: cases.rel_l2(m32.get(n), m64.get(n)) for n in ("u", "v", "w", "b")}
+    print("fp32 vs fp64 after 100 steps at 256x256x128:", errs)
+    assert max(errs.values()) < 1e-3
+    g = c64.grid
+    for m, tol in ((m64, 1e-12), (m32, 1e-5)):
+        u, v, w = m.get("u").astype(np.float64), m.get("v").astype(np.float64), m.get("w").astype(np.float64)
+        dx, dy, dz = g.Lx / g.Nx, g.Ly / g.Ny, g.Lz / g.Nz
+        div = (np.roll(u, -1, 0) - u) / dx + (np.roll(v, -1, 1) - v) / dy + (w[:, :, 1:] - w[:, :, :-1]) / dz
+        scale = np.abs(u).max() / dx
+        assert np.abs(div).max() < tol * scale
+
+
+def test_stretched_amd_128_fp32_against_fp64_oracle():
+    # the stretched AMD configuration checked against the FP64 oracle at 128²×64
+    c32 = cases.convection_3d((128, 128, 64), closure="amd", stretched=True, float_type=np.float32, N2=1e-7, U0=2e-2)
+    c64 = cases.convection_3d((128, 128, 64), closure="amd", stretched=True, N2=1e-7, U0=2e-2)
+    m, r = c32.start_gpu(), c64.start_oracle()
+    og.time_step_(m, 1.0, 3)
+    r.time_step(1.0, 3)
+    errs = compare(m, r, ("u", "v", "w", "b"), 1e-4)
+    print("stretched AMD fp32 vs fp64 oracle at 128x128x64 after 3 steps:", errs)

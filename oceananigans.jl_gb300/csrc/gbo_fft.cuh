@@ -198,6 +198,20 @@ __device__ __forceinline__ Cx<FT>* fft_any(Cx<FT>* A, Cx<FT>* B, int L, const FF
 // (index_permutations.jl:18-20 restated: even samples first, odd samples reversed).
 GBO_D int makhoul_dest(int k, int N) { return (k & 1) ? N - 1 - (k >> 1) : (k >> 1); }
 
+// Asynchronous global -> shared copy of 4, 8 or 16 bytes (zero-filled when zero is
+// set; src must still be a valid address).  The pass kernels issue their whole tile
+// this way and wait once, instead of one dependent load per element.
+template <int BYTES>
+GBO_D void cp_async_n(void* dst, const void* src, bool zero) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(BYTES), "r"(zero ? 0 : BYTES));
+}
+GBO_D void cp_async_wait() {
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
 struct PoissonTables;  // host side
 
 template <typename FT>
@@ -236,10 +250,11 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
     if (!inverse) {
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
             int c = t % ZT, k = t / ZT;
-            FT x = (i0 + c < P.Nx) ? col0[c + plane * k] : FT(0);
+            const bool in = i0 + c < P.Nx;
             Cx<FT>& d = A[makhoul_dest(k, N) * L + (c >> 1)];
-            if (c & 1) d.im = x; else d.re = x;
+            cp_async_n<sizeof(FT)>((c & 1) ? &d.im : &d.re, in ? col0 + c + plane * k : col0, !in);
         }
+        cp_async_wait();
         __syncthreads();
         Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, -1, P.tw_z);
         Cx<FT>* O = (R == A) ? B : A;
@@ -262,8 +277,10 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
         FT* in = reinterpret_cast<FT*>(B);
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
             int c = t % ZT, k = t / ZT;
-            in[c + ZT * k] = (i0 + c < P.Nx) ? col0[c + plane * k] : FT(0);
+            const bool ok = i0 + c < P.Nx;
+            cp_async_n<sizeof(FT)>(&in[c + ZT * k], ok ? col0 + c + plane * k : col0, !ok);
         }
+        cp_async_wait();
         __syncthreads();
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
             int l = t % L, k = t / L;
@@ -303,7 +320,8 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
     if (!inverse) {
         const FT* src = P.rb + (size_t)line0 * P.Nx;
         FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
-        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) As[t] = src[t];
+        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) cp_async_n<sizeof(FT)>(&As[t], src + t, false);
+        cp_async_wait();
         __syncthreads();
         Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, -1, P.tw_xh);
         Cx<FT>* dst = P.cb + (size_t)line0 * Nh;
@@ -320,9 +338,13 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
         }
     } else {
         const Cx<FT>* src = P.cb + (size_t)line0 * Nh;
+        Cx<FT>* S = B;  // the block's L lines of Nh coefficients, staged asynchronously
+        for (int t = threadIdx.x; t < L * Nh; t += blockDim.x) cp_async_n<sizeof(Cx<FT>)>(&S[t], src + t, false);
+        cp_async_wait();
+        __syncthreads();
         for (int t = threadIdx.x; t < L * M; t += blockDim.x) {
             int l = t / M, k = t - l * M;
-            Cx<FT> Xk = src[l * Nh + k], Xn = src[l * Nh + (M - k)];
+            Cx<FT> Xk = S[l * Nh + k], Xn = S[l * Nh + (M - k)];
             Cx<FT> e = Xk + conj(Xn);
             Cx<FT> w = conj(P.tw_x[k]);
             Cx<FT> o = w * (Xk - conj(Xn));
@@ -352,8 +374,10 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     Cx<FT>* base = P.cb + kx0 + (size_t)Nh * N * kz;
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
         int c = t % YT, ky = t / YT;
-        A[ky * YT + c] = (kx0 + c < Nh) ? base[c + (size_t)Nh * ky] : cx(FT(0), FT(0));
+        const bool ok = kx0 + c < Nh;
+        cp_async_n<sizeof(Cx<FT>)>(&A[ky * YT + c], ok ? base + c + (size_t)Nh * ky : base, !ok);
     }
+    cp_async_wait();
     __syncthreads();
     Cx<FT>* R = A;
     if (mode != 2) R = fft_any<FT, NC, true>(A, B, YT, P.py, -1, P.tw_y);

@@ -509,8 +509,9 @@ struct ModelImpl : gbo_model {
         while (ZT > 2 && (size_t)ZT * Nz * cs_ > lim) ZT /= 2;
         smem_z = (size_t)ZT * Nz * cs_;
         XL = 8;
-        while (XL > 1 && (size_t)2 * XL * (Nx / 2) * cs_ > lim) XL /= 2;
-        smem_x = (size_t)2 * XL * (Nx / 2) * cs_;
+        // two buffers of XL lines of Nx/2 coefficients, plus XL for staging Nx/2+1 per line
+        while (XL > 1 && (size_t)XL * (Nx + 1) * cs_ > lim) XL /= 2;
+        smem_x = (size_t)XL * (Nx + 1) * cs_;
         YT = 16;
         while (YT > 1 && (size_t)2 * YT * Ny * cs_ > lim) YT /= 2;
         smem_y = (size_t)2 * YT * Ny * cs_;

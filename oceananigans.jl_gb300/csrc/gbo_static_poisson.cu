@@ -184,9 +184,9 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
     const size_t cs = sizeof(Cx<FT>), lim = 100 * 1024;
     int ZT = 32, XL = 8, YT = 16;
     while (ZT > 2 && (size_t)ZT * Nz * cs > lim) ZT /= 2;
-    while (XL > 1 && (size_t)2 * XL * (Nx / 2) * cs > lim) XL /= 2;
+    while (XL > 1 && (size_t)XL * (Nx + 1) * cs > lim) XL /= 2;
     while (YT > 1 && (size_t)2 * YT * Ny * cs > lim) YT /= 2;
-    const size_t smem_z = (size_t)ZT * Nz * cs, smem_x = (size_t)2 * XL * (Nx / 2) * cs, smem_y = (size_t)2 * YT * Ny * cs;
+    const size_t smem_z = (size_t)ZT * Nz * cs, smem_x = (size_t)XL * (Nx + 1) * cs, smem_y = (size_t)2 * YT * Ny * cs;
     if (std::max({smem_z, smem_x, smem_y}) > (size_t)optin)
         return fail(GBO_ERR_INVALID, "grid needs %lld bytes of shared memory per block; the device allows %lld",
                     (long long)std::max({smem_z, smem_x, smem_y}), optin);

@@ -214,6 +214,15 @@ GBO_D void cp_async_wait() {
 
 struct PoissonTables;  // host side
 
+// Tile shapes of the pass kernels: columns per DCT block and the shared-memory budget
+// per block within which the tiles are chosen (both solvers choose them the same way).
+#ifndef GBO_DCT_TILE
+#define GBO_DCT_TILE 32
+#endif
+#ifndef GBO_PASS_SMEM_LIMIT
+#define GBO_PASS_SMEM_LIMIT (100 * 1024)
+#endif
+
 template <typename FT>
 struct PassP {
     int Nx, Ny, Nz, Nh;        // Nh = Nx/2 + 1

@@ -356,7 +356,7 @@ struct ModelImpl : gbo_model {
     double iters_seen = 0;               // CG_ITERS already accounted in `launches`
     PassP<FT> pp{};
     ThomasP tp{};
-    int ZT = 32, XL = 8, YT = 16;
+    int ZT = GBO_DCT_TILE, XL = 8, YT = 16;
     int kchunk = 16;  // levels marched per block by the fused momentum kernel
     size_t smem_z = 0, smem_x = 0, smem_y = 0;
     // flags
@@ -504,8 +504,8 @@ struct ModelImpl : gbo_model {
             tp.ws = t_ws.p;
         }
         // shared-memory tiles: keep each block at or below ~100 KB
-        const size_t cs_ = sizeof(C), lim = 100 * 1024;
-        ZT = 32;
+        const size_t cs_ = sizeof(C), lim = GBO_PASS_SMEM_LIMIT;
+        ZT = GBO_DCT_TILE;
         while (ZT > 2 && (size_t)ZT * Nz * cs_ > lim) ZT /= 2;
         smem_z = (size_t)ZT * Nz * cs_;
         XL = 8;

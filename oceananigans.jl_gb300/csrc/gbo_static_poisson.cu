@@ -181,8 +181,8 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
     P.scale = flat ? FT(1.0 / ((double)Nx * Ny)) : FT(1.0 / ((double)Nx * Ny * Nz));
 
     // shared-memory tiles chosen exactly as the model's solver chooses them
-    const size_t cs = sizeof(Cx<FT>), lim = 100 * 1024;
-    int ZT = 32, XL = 8, YT = 16;
+    const size_t cs = sizeof(Cx<FT>), lim = GBO_PASS_SMEM_LIMIT;
+    int ZT = GBO_DCT_TILE, XL = 8, YT = 16;
     while (ZT > 2 && (size_t)ZT * Nz * cs > lim) ZT /= 2;
     while (XL > 1 && (size_t)XL * (Nx + 1) * cs > lim) XL /= 2;
     while (YT > 1 && (size_t)2 * YT * Ny * cs > lim) YT /= 2;

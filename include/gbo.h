@@ -155,6 +155,20 @@ const char* gbo_last_error(const gbo_model* m);
 /* Library version string. */
 const char* gbo_version(void);
 
+/* ---- checkpoint / restart ------------------------------------------------------
+ * Replaces prognostic_state(model) / restore_prognostic_state!(model, state)
+ * (src/Models/NonhydrostaticModels/nonhydrostatic_model.jl:354-377), which the
+ * Checkpointer and run!(sim; pickup=true) use.  The state is one host buffer of
+ * gbo_state_bytes(m) bytes: a header (clock, sizes, float type) and the interior
+ * values of u, v, w, the tracers and pNHS (the conjugate-gradient initial guess).
+ * RK3 needs no tendency history across steps (ζ₁ = 0); the closure fields and the
+ * hydrostatic pressure anomaly are recomputed on restore, so a restored model
+ * continues exactly as the original.  gbo_set_state rejects a buffer written by a
+ * model of another size, float type or tracer count. */
+int64_t gbo_state_bytes(const gbo_model* m);
+int gbo_get_state(gbo_model* m, void* buf, int64_t bytes);
+int gbo_set_state(gbo_model* m, const void* buf, int64_t bytes);
+
 /* ---- standalone Poisson solve ---------------------------------------------
  * Solve ∇²ϕ = rhs with the model's pressure solver on device buffers holding
  * Nx*Ny*Nz interior values of the model's float type.

@@ -258,6 +258,9 @@ struct gbo_model {
     virtual int sync() = 0;
     virtual int device_pointer(int field, void** p, int64_t* n) = 0;
     virtual int poisson_device(void* phi, const void* rhs) = 0;
+    virtual int64_t state_bytes() const = 0;
+    virtual int get_state(void* buf, int64_t bytes) = 0;
+    virtual int set_state(const void* buf, int64_t bytes) = 0;
     virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
     virtual int timing_counts(int64_t* n, int nmax) const = 0;
     virtual void* stream_ptr() = 0;
@@ -1086,6 +1089,60 @@ struct ModelImpl : gbo_model {
         return GBO_OK;
     }
 
+    // ---- prognostic state (prognostic_state / restore_prognostic_state!,
+    // nonhydrostatic_model.jl:354-377): clock, velocities, tracers and pNHS (the CG
+    // initial guess).  RK3 keeps no tendency history across steps (ζ₁ = 0), and the
+    // closure fields and pHY′ are recomputed from the restored state.
+    struct StateHeader {
+        uint64_t magic;
+        int32_t version, dtype, Nx, Ny, Nz, ntr;
+        double time;
+        int64_t iteration;
+    };
+    static constexpr uint64_t kStateMagic = 0x31657461747362ULL;  // "bstate1"
+    std::vector<const FT*> state_fields() const {
+        std::vector<const FT*> f{u.p, v.p};
+        if (!flat) f.push_back(w.p);
+        for (int n = 0; n < ntr; ++n) f.push_back(c[n].p);
+        f.push_back(p.p);
+        return f;
+    }
+    int64_t state_bytes() const override {
+        return (int64_t)sizeof(StateHeader) + (int64_t)state_fields().size() * (int64_t)N * (int64_t)sizeof(FT);
+    }
+    int get_state(void* buf, int64_t bytes) override {
+        if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
+        StateHeader h{kStateMagic, 1, dtype, Nx, Ny, Nz, ntr, time, iteration};
+        std::memcpy(buf, &h, sizeof(h));
+        char* at = static_cast<char*>(buf) + sizeof(h);
+        for (const FT* f : state_fields()) {
+            GBO_CUDA(cudaMemcpyAsync(at, f, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+            at += N * sizeof(FT);
+        }
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        return GBO_OK;
+    }
+    int set_state(const void* buf, int64_t bytes) override {
+        if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
+        StateHeader h;
+        std::memcpy(&h, buf, sizeof(h));
+        if (h.magic != kStateMagic || h.version != 1) { err = "not a state written by gbo_get_state"; return GBO_ERR_INVALID; }
+        if (h.dtype != dtype || h.Nx != Nx || h.Ny != Ny || h.Nz != Nz || h.ntr != ntr) {
+            err = "state was written by a model of another size, float type or tracer count";
+            return GBO_ERR_INVALID;
+        }
+        const char* at = static_cast<const char*>(buf) + sizeof(h);
+        for (const FT* f : state_fields()) {
+            GBO_CUDA(cudaMemcpyAsync(const_cast<FT*>(f), at, N * sizeof(FT), cudaMemcpyHostToDevice, stream));
+            at += N * sizeof(FT);
+        }
+        time = h.time;
+        iteration = h.iteration;
+        mask_tracers();
+        auxiliaries();
+        return sync();
+    }
+
     int poisson_device(void* phi, const void* rhs) override {
         if (cg) {
             // V∇²ϕ = rhs by preconditioned CG from the initial guess in ϕ
@@ -1242,6 +1299,18 @@ int gbo_get_field(gbo_model* m, int32_t field, void* host, int32_t dtype, int64_
 }
 
 int64_t gbo_field_count(const gbo_model* m, int32_t field) { return m ? m->count(field) : -1; }
+
+int64_t gbo_state_bytes(const gbo_model* m) { return m ? m->state_bytes() : 0; }
+
+int gbo_get_state(gbo_model* m, void* buf, int64_t bytes) {
+    if (!m || !buf) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->get_state(buf, bytes); });
+}
+
+int gbo_set_state(gbo_model* m, const void* buf, int64_t bytes) {
+    if (!m || !buf) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->set_state(buf, bytes); });
+}
 
 int gbo_field_device_pointer(gbo_model* m, int32_t field, void** dptr, int64_t* count) {
     if (!m || !dptr || !count) return GBO_ERR_INVALID;

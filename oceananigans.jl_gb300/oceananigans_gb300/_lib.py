@@ -82,6 +82,9 @@ SIGNATURES = {
     "gbo_last_error": (ctypes.c_char_p, [_vp]),
     "gbo_version": (ctypes.c_char_p, []),
     "gbo_poisson_solve_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "gbo_state_bytes": (ctypes.c_int64, [_vp]),
+    "gbo_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
+    "gbo_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "gbo_ensemble_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc),
                                            ctypes.POINTER(_vp)]),
     "gbo_ensemble_destroy": (None, [_vp]),

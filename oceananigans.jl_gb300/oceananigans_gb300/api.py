@@ -360,6 +360,18 @@ class NonhydrostaticModel:
     def poisson_solve_device(self, phi_ptr, rhs_ptr):
         L.check(L.load().gbo_poisson_solve_device(self._h, ctypes.c_void_p(phi_ptr), ctypes.c_void_p(rhs_ptr)), self._h)
 
+    def prognostic_state(self):
+        """prognostic_state(model): the restart state as a numpy byte array."""
+        lib = L.load()
+        buf = np.empty(int(lib.gbo_state_bytes(self._h)), dtype=np.uint8)
+        L.check(lib.gbo_get_state(self._h, buf.ctypes.data, buf.size), self._h)
+        return buf
+
+    def restore_prognostic_state_(self, state):
+        """restore_prognostic_state!(model, state)."""
+        buf = np.ascontiguousarray(state, dtype=np.uint8)
+        L.check(L.load().gbo_set_state(self._h, buf.ctypes.data, buf.size), self._h)
+
     @property
     def solver_iterations(self):
         return L.load().gbo_last_solver_iterations(self._h)

@@ -169,6 +169,52 @@ int64_t gbo_state_bytes(const gbo_model* m);
 int gbo_get_state(gbo_model* m, void* buf, int64_t bytes);
 int gbo_set_state(gbo_model* m, const void* buf, int64_t bytes);
 
+/* ---- simulation loop ------------------------------------------------------
+ * run!(Simulation(model; Δt, stop_time, stop_iteration, wall_time_limit,
+ * align_time_step)) with the default NaNChecker and an optional TimeStepWizard
+ * callback (src/Simulations/run.jl:165-262, simulation.jl:68-119,
+ * time_step_wizard.jl:66-115).  The loop runs on the device: Δt alignment with
+ * stop_time, the step, the clock, the stop criteria, the NaN check and the
+ * wizard's CFL reductions are nodes of one CUDA graph whose conditional WHILE
+ * node repeats them, so the host waits only once per iterations_per_launch
+ * iterations (where wall_time_limit is checked).  As in the reference at least
+ * one step is taken per call, and a model at iteration 0 first evaluates every
+ * callback once (initialize!(sim), run.jl:319-347). */
+enum gbo_stop_reason { GBO_STOP_NONE = 0, GBO_STOP_TIME = 1, GBO_STOP_ITERATION = 2, GBO_STOP_NAN = 3,
+                       GBO_STOP_WALL_TIME = 4 };
+typedef struct gbo_run_desc {
+    double  dt;                    /* Simulation(model; Δt): the first time step */
+    double  stop_time;             /* INFINITY: none */
+    double  stop_iteration;        /* INFINITY: none (a Float64, as in the reference) */
+    double  wall_time_limit;       /* seconds; INFINITY: none */
+    int32_t align_time_step;       /* 1: align Δt with stop_time (default) */
+    double  minimum_relative_step; /* must be 0 (the default): skipped steps are not supported */
+    int32_t nan_check_interval;    /* NaNChecker on u every N iterations (default 100; 0: none) */
+    int32_t nan_erroring;          /* 1: a NaN makes gbo_run return GBO_ERR_NAN */
+    int32_t wizard_interval;       /* TimeStepWizard callback on IterationInterval(N); 0: none */
+    double  cfl, diffusive_cfl;    /* TimeStepWizard(cfl = 0.2, diffusive_cfl = Inf, */
+    double  max_change, min_change;/*   max_change = 1.1, min_change = 0.5, */
+    double  max_dt, min_dt;        /*   max_Δt = Inf, min_Δt = 0) */
+    int32_t iterations_per_launch; /* iterations per graph launch (default 100) */
+} gbo_run_desc;
+typedef struct gbo_run_result {
+    double  dt;                    /* simulation.Δt at the end (the wizard's last value) */
+    double  time;                  /* model.clock.time */
+    int64_t iteration;             /* model.clock.iteration */
+    int64_t steps;                 /* steps taken by this call */
+    int32_t stop_reason;           /* gbo_stop_reason of the first criterion met */
+    int32_t nan_detected;
+} gbo_run_result;
+void gbo_run_desc_default(gbo_run_desc* d);
+int gbo_run(gbo_model* m, const gbo_run_desc* d, gbo_run_result* out);
+
+/* cell_advection_timescale(model) (src/Advection/cell_advection_timescale.jl:15-36)
+ * and cell_diffusion_timescale(model) of the closure
+ * (src/TurbulenceClosures/turbulence_closure_diagnostics.jl:48-63; Inf without a
+ * closure), reduced on the device from the current state. */
+int gbo_cell_advection_timescale(gbo_model* m, double* out);
+int gbo_cell_diffusion_timescale(gbo_model* m, double* out);
+
 /* ---- standalone Poisson solve ---------------------------------------------
  * Solve ∇²ϕ = rhs with the model's pressure solver on device buffers holding
  * Nx*Ny*Nz interior values of the model's float type.

@@ -104,7 +104,9 @@ __global__ void k_cg_init(const FT* __restrict__ b, const FT* __restrict__ q, FT
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) r[t] = b[t] - q[t];
 }
 template <typename FT>
-__global__ void k_cg_scale(const FT* __restrict__ a, FT* __restrict__ out, FT sc, size_t n) {
+__global__ void k_cg_scale(const FT* __restrict__ a, FT* __restrict__ out, FT sc, size_t n,
+                           const FT* scp = nullptr) {
+    if (scp) sc = __ldg(scp);
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) out[t] = a[t] * sc;
 }
 // V⁻¹r of one cell; times Δzᶜ for the Fourier-tridiagonal preconditioner, whose solve!

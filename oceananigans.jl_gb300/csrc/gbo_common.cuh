@@ -56,6 +56,27 @@ GBO_D int wrapi(int i, int N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
 template <typename FT>
 GBO_D FT ldg(const FT* p) { return __ldg(p); }
 
+// eps(FT) in double: the floor of Δτ in the pressure correction (pressure_correction.jl:102-104)
+template <typename FT>
+GBO_HD double machine_eps() { return sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16; }
+// Δt and the projection factors of the three RK3 stages, in FT, as the stage kernels
+// read them from device memory: Δτ = FT(Δt c) with c = γ₁ on the first stage and γ + ζ
+// (summed in FT) on the others (nonhydrostatic_rk3_substep.jl:34-36); the correction
+// uses 1 / max(eps, Δτ) and the CG initial guess pNHS max(eps, Δτ) (pressure_correction.jl:102-104).
+enum { DTF_DT = 0, DTF_RDTAU = 1, DTF_SCALE = 4, DTF_N = 8 };
+template <typename FT>
+GBO_HD void stage_factors(double dt, double c0, double c1, double c2, FT* out) {
+    const double c[3] = {c0, c1, c2};
+    out[DTF_DT] = FT(dt);
+    for (int s = 0; s < 3; ++s) {
+        const double tau = (double)FT(dt * c[s]);
+        const double e = machine_eps<FT>();
+        const FT m = FT(tau > e ? tau : e);
+        out[DTF_RDTAU + s] = FT(1) / m;
+        out[DTF_SCALE + s] = m;
+    }
+}
+
 // Accessor for a Center-in-z field.
 template <typename FT>
 struct CFld {

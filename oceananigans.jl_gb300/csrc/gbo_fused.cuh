@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         }
     }
 
+    const FT dt = stage_dt(P);
     int r3 = m3(kb);
     for (int k = kb; k < ke; ++k) {
         // ring slots of levels k-1, k, k+1 (and k+2, which shares the slot of k-1)
@@ -570,7 +571,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     G = G - rVc * (cdx + cdy + cdz);
                 }
                 P.Gu[idx] = G;
-                P.uo[idx] = rk3_update(Uk[pidx(tx, ty)], G, Gum, P);
+                P.uo[idx] = rk3_update(Uk[pidx(tx, ty)], G, Gum, P, dt);
             }
             {
                 FT dx_ = s.WX[A_UV][ty][tx + 1] - s.WX[A_UV][ty][tx];
@@ -592,7 +593,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     G = G - rVc * (cdx + cdy + cdz);
                 }
                 P.Gv[idx] = G;
-                P.vo[idx] = rk3_update(Vk[pidx(tx, ty)], G, Gvm, P);
+                P.vo[idx] = rk3_update(Vk[pidx(tx, ty)], G, Gvm, P, dt);
             }
             if (!fz) {
                 if (k == 0) {
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                         G = G - rVf * (cdx + cdy + cdz);
                     }
                     P.Gw[idx] = G;
-                    P.wo[idx] = rk3_update(Wk[pidx(tx, ty)], G, Gwm, P);
+                    P.wo[idx] = rk3_update(Wk[pidx(tx, ty)], G, Gwm, P, dt);
                 }
             }
             if (TR) {
@@ -630,7 +631,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     if (k == 0 && P.flux_bot != FT(0)) G += P.flux_bot * Az / (Az * M.dzc(k));
                 }
                 P.Gc[idx] = G;
-                P.co[idx] = rk3_update(CCk[pidx(tx, ty)], G, Gcm, P);
+                P.co[idx] = rk3_update(CCk[pidx(tx, ty)], G, Gcm, P, dt);
             }
         }
 

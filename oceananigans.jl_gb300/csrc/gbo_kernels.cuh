@@ -19,6 +19,7 @@ struct StepP {
     FT flux_top, flux_bot;
     FT C, Cb;
     FT dt, gamma, zeta;
+    const FT* dtf;                          // stage factors in device memory (Δt overrides dt)
     int first;
 };
 

@@ -1,5 +1,6 @@
 // gbo_model.cu -- model lifecycle, RK3 orchestration and the C ABI of libgb300ocean.so.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -9,6 +10,7 @@
 #include "../../include/gbo.h"
 #include "gbo_fft.cuh"
 #include "gbo_cg.cuh"
+#include "gbo_sim.cuh"
 #include "gbo_fused.cuh"
 
 // ===========================================================================
@@ -44,7 +46,8 @@ __global__ void k_source(GridP<FT> g, const FT* __restrict__ u, const FT* __rest
 // (every point reads only its own u*).
 template <typename FT>
 __global__ void k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws, const FT* __restrict__ phi,
-                          FT* u, FT* v, FT* w, FT* __restrict__ p, FT rdtau, FT phi_shift) {
+                          FT* u, FT* v, FT* w, FT* __restrict__ p, FT rdtau, FT phi_shift,
+                          const FT* rdp = nullptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = blockIdx.z;
@@ -52,6 +55,7 @@ __global__ void k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws,
     CFld<FT> P = cfld(phi, g);
     Met<FT> M(g);
     const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+    if (rdp) rdtau = __ldg(rdp);
     FT pc = P(i, j, k) - phi_shift;
     // ∂ operators are conditional on an immersed grid (conditional_differences.jl:15-43)
     FT dx_ = cond_zero(g, i - 1, j, k, i, j, k) ? FT(0) : (pc - (P(i - 1, j, k) - phi_shift));
@@ -261,10 +265,12 @@ struct gbo_model {
     virtual int64_t state_bytes() const = 0;
     virtual int get_state(void* buf, int64_t bytes) = 0;
     virtual int set_state(const void* buf, int64_t bytes) = 0;
+    virtual int run(const gbo_run_desc* d, gbo_run_result* out) = 0;
+    virtual int timescales(double* adv, double* dif) = 0;
     virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
     virtual int timing_counts(int64_t* n, int nmax) const = 0;
     virtual void* stream_ptr() = 0;
-    virtual int64_t capture_step(double dt) = 0;
+    virtual int64_t capture_step(const float* dtf32, const double* dtf64) = 0;
     virtual void add_launches(int64_t n) = 0;
     virtual int finish_steps(double dt, int nsteps) = 0;
     virtual int64_t launch_count() const = 0;
@@ -276,11 +282,11 @@ struct gbo_model {
 };
 
 enum { G_MOMENTUM = 0, G_TRACER, G_CLOSURE, G_HYDROSTATIC, G_SOURCE, G_DCT_Z, G_FFT_X, G_FFT_Y, G_THOMAS,
-       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, G_CG_DOT, G_CG_DIR, G_CG_XR, G_CG_GAUGE, GROUPS };
+       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, G_CG_DOT, G_CG_DIR, G_CG_XR, G_CG_GAUGE, G_SIM, GROUPS };
 const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", "k_hydrostatic", "k_source",
                                          "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
                                          "k_nan_check", "k_mask", "k_cg", "k_cg_dot", "k_cg_direction",
-                                         "k_cg_update_xr", "k_cg_gauge"};
+                                         "k_cg_update_xr", "k_cg_gauge", "k_simulation"};
 
 // The fused momentum kernel is compiled per closure kind; these pick the instance.
 template <typename FT, bool TR>
@@ -365,13 +371,27 @@ struct ModelImpl : gbo_model {
     // flags
     unsigned int* d_flags = nullptr;
     unsigned int* h_flags = nullptr;
-    // graph of one time step (per dt)
+    // graph of one time step (Δt is read from the stage factors dtf, so one graph serves every Δt)
     cudaGraphExec_t graph = nullptr;
-    double graph_dt = -1;
     bool use_graph = true;
+    // simulation loop (gbo_run): state slots, block partials, graph of the loop
+    DBuf<FT> dtf;                        // stage factors of the current Δt (DTF_*)
+    DBuf<double> run_s, run_part;
+    DBuf<unsigned int> run_cnt;
+    double* h_run = nullptr;
+    cudaStream_t run_stream = nullptr;   // captures the loop body into a conditional node
+    cudaGraphExec_t run_graph = nullptr;
+    int64_t run_iter_launches = 0;       // kernels per loop iteration (CG iterations apart)
 
     ~ModelImpl() override {
         if (graph) cudaGraphExecDestroy(graph);
+        if (run_graph) cudaGraphExecDestroy(run_graph);
+        dtf.free_();
+        run_s.free_();
+        run_part.free_();
+        run_cnt.free_();
+        if (h_run) cudaFreeHost(h_run);
+        if (run_stream) cudaStreamDestroy(run_stream);
         for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz,
                             &cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x})
             b->free_();
@@ -457,6 +477,11 @@ struct ModelImpl : gbo_model {
         GBO_CUDA(cudaMalloc(&d_flags, sizeof(unsigned int)));
         GBO_CUDA(cudaMemset(d_flags, 0, sizeof(unsigned int)));
         GBO_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned int)));
+        dtf.alloc(DTF_N);
+        run_s.alloc(RUN_NSLOTS);
+        run_part.alloc((size_t)SIM_BLOCKS * SIM_PARTS);
+        run_cnt.alloc(1);
+        GBO_CUDA(cudaMallocHost(&h_run, RUN_NSLOTS * sizeof(double)));
         init_poisson(Lx, Ly);
         if (cg) {
             for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x}) b->alloc(N);
@@ -626,8 +651,9 @@ struct ModelImpl : gbo_model {
 
     // compute_pressure_correction! + make_pressure_correction! on the predictor (us, vs, ws)
     // writing the state (u, v, w) and p; in == out is allowed.
-    void project(FT* ui, FT* vi, FT* wi, double dtau) {
-        const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+    // With rdp / scp set, 1/max(eps, Δτ) and max(eps, Δτ) are read on the device.
+    void project(FT* ui, FT* vi, FT* wi, double dtau, const FT* rdp = nullptr, const FT* scp = nullptr) {
+        const double eps = machine_eps<FT>();
         if (ibg) {  // mask_immersed_field! on the velocities (pressure_correction.jl:9)
             pre(G_MASK);
             k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, nullptr, flat ? 3 : 7);
@@ -635,7 +661,7 @@ struct ModelImpl : gbo_model {
         }
         const FT* phi = rb.p;
         if (cg) {
-            cg_status = cg_solve(ui, vi, wi, std::max(eps, dtau) * (std::isfinite(dtau) ? 1.0 : 0.0));
+            cg_status = cg_solve(ui, vi, wi, std::max(eps, dtau) * (std::isfinite(dtau) ? 1.0 : 0.0), scp);
             phi = cg_x.p;
         } else {
             int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
@@ -646,17 +672,18 @@ struct ModelImpl : gbo_model {
         }
         FT rdtau = FT(1) / FT(std::max(eps, dtau));
         pre(G_CORRECT);
-        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, phi, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0));
+        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, phi, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0),
+                                                   rdp);
         check_launch();
     }
 
     // Preconditioned conjugate gradient for V∇²x = V·div u* with x₀ = p·Δτ
     // (solve_for_pressure.jl:52-72; conjugate_gradient_solver.jl:177-284).  Each
     // iteration reads ‖V⁻¹r‖ back to the host for the stopping test.
-    int cg_solve(const FT* ui, const FT* vi, const FT* wi, double dtp) {
+    int cg_solve(const FT* ui, const FT* vi, const FT* wi, double dtp, const FT* scp = nullptr) {
         const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
         pre(G_CG);
-        k_cg_scale<FT><<<lin, 256, 0, stream>>>(p.p, cg_x.p, FT(dtp), N);
+        k_cg_scale<FT><<<lin, 256, 0, stream>>>(p.p, cg_x.p, FT(dtp), N, scp);
         check_launch();
         pre(G_SOURCE);
         k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, cg_b.p, SRC_CG);
@@ -828,10 +855,12 @@ struct ModelImpl : gbo_model {
         }
     }
 
-    // One RK3 stage: Gⁿ from the current state, predictor, projection.
-    void stage(double dt, double gamma, double zeta, bool first) {
+    // One RK3 stage: Gⁿ from the current state, predictor, projection.  Δt is read
+    // on the device from the stage factors at dtf, so a captured step serves every Δt.
+    void stage(const FT* dtf, int s, double gamma, double zeta, bool first) {
         StepP<FT> P = params();
-        P.dt = FT(dt);
+        P.dt = FT(0);
+        P.dtf = dtf;
         P.gamma = FT(gamma);
         P.zeta = FT(zeta);
         P.first = first;
@@ -875,8 +904,7 @@ struct ModelImpl : gbo_model {
         }
         // Δτ = Δt γ (first stage) or Δt (γ + ζ) with γ, ζ in the working precision
         // (nonhydrostatic_rk3_substep.jl:34-36; runge_kutta_3.jl:186-187)
-        double dtau = first ? (double)FT(dt * (double)FT(gamma)) : (double)FT(dt * (double)(FT(gamma) + FT(zeta)));
-        project(us.p, vs.p, flat ? nullptr : ws.p, dtau);
+        project(us.p, vs.p, flat ? nullptr : ws.p, 0.0, dtf + DTF_RDTAU + s, dtf + DTF_SCALE + s);
         for (int n = 0; n < ntr; ++n) {
             pre(G_COPY);
             k_copy<FT><<<std::min<size_t>((N + 255) / 256, 4096), 256, 0, stream>>>(cs[n].p, c[n].p, N);
@@ -896,36 +924,48 @@ struct ModelImpl : gbo_model {
         }
     }
 
-    void full_step(double dt) {
+    void full_step(const FT* dtf) {
         using K = GboCoeffs<double>;
-        stage(dt, K::rk3_gamma1, 0.0, true);
-        stage(dt, K::rk3_gamma2, K::rk3_zeta2, false);
-        stage(dt, K::rk3_gamma3, K::rk3_zeta3, false);
+        stage(dtf, 0, K::rk3_gamma1, 0.0, true);
+        stage(dtf, 1, K::rk3_gamma2, K::rk3_zeta2, false);
+        stage(dtf, 2, K::rk3_gamma3, K::rk3_zeta3, false);
+    }
+    // c of Δτ = FT(Δt c) per stage: γ₁, and γ + ζ summed in FT (runge_kutta_3.jl:186-187)
+    static StageC stage_c() {
+        using K = GboCoeffs<double>;
+        return StageC{(double)FT(K::rk3_gamma1), (double)(FT(K::rk3_gamma2) + FT(K::rk3_zeta2)),
+                      (double)(FT(K::rk3_gamma3) + FT(K::rk3_zeta3))};
+    }
+
+    // Δt of the next steps into the stage factors the stage kernels read
+    void set_dt(double dt, cudaStream_t st) {
+        pre(G_SIM);
+        k_set_dt<FT><<<1, 1, 0, st>>>(dtf.p, dt, stage_c());
+        check_launch();
     }
 
     int step(double dt, int nsteps) override {
         if (nsteps <= 0) return GBO_OK;
         cg_status = GBO_OK;
+        set_dt(dt, stream);
         if (use_graph) {
-            if (!graph || graph_dt != dt) {
-                if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
+            if (!graph) {
                 cudaGraph_t gph;
                 GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
                 int64_t before = launches;
-                full_step(dt);
+                full_step(dtf.p);
                 graph_launches_per_step = launches - before;
                 launches = before;
                 GBO_CUDA(cudaStreamEndCapture(stream, &gph));
                 GBO_CUDA(cudaGraphInstantiate(&graph, gph, 0));
                 GBO_CUDA(cudaGraphDestroy(gph));
-                graph_dt = dt;
             }
             for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
             launches += graph_launches_per_step * nsteps;
         } else {
             int worst = GBO_OK;
             for (int s = 0; s < nsteps; ++s) {
-                full_step(dt);
+                full_step(dtf.p);
                 if (cg_status != GBO_OK) worst = cg_status;
             }
             cg_status = worst;
@@ -934,10 +974,11 @@ struct ModelImpl : gbo_model {
     }
 
     // Record one time step on this model's stream while it is joined to another
-    // stream's capture (ensemble graphs); returns the kernels recorded.
-    int64_t capture_step(double dt) override {
+    // stream's capture (ensemble graphs), reading Δt from dtp; returns the kernels recorded.
+    int64_t capture_step(const float* dtf32, const double* dtf64) override {
         const int64_t before = launches;
-        full_step(dt);
+        if constexpr (sizeof(FT) == 4) full_step(dtf32);
+        else full_step(dtf64);
         const int64_t n = launches - before;
         launches = before;
         return n;
@@ -977,8 +1018,9 @@ struct ModelImpl : gbo_model {
         std::fill(group_n.begin(), group_n.end(), 0);
         timing = true;
         try {
+            set_dt(dt, stream);
             for (int s = 0; s < nsteps; ++s) {
-                full_step(dt);
+                full_step(dtf.p);
                 time += dt;
                 iteration += 1;
             }
@@ -1141,6 +1183,195 @@ struct ModelImpl : gbo_model {
         mask_tracers();
         auxiliaries();
         return sync();
+    }
+
+    // ---- simulation loop (run!(sim), src/Simulations/run.jl:165-262) ----
+    SimP<FT> sim_params() {
+        SimP<FT> S{};
+        S.g = gp;
+        S.u = u.p; S.v = v.p; S.w = flat ? nullptr : w.p;
+        S.nu = nu.p;
+        for (int n = 0; n < ntr; ++n) S.kap[n] = kap.empty() ? nullptr : kap[n].p;
+        S.ntr = ntr;
+        S.closure = desc.closure;
+        S.run = run_s.p;
+        S.part = run_part.p;
+        S.cnt = run_cnt.p;
+        return S;
+    }
+    // Δ² = min(Δx, Δy, min Δz)² and max(1, 1/Pr) of the diffusion timescale, in FT
+    // (turbulence_closure_diagnostics.jl:8-13,48-53; min_Pr = 1 without tracers)
+    void diffusion_constants(double* d2, double* prf) const {
+        FT D = std::min(gp.dx, gp.dy);
+        if (!flat)
+            for (int kr = 1; kr <= Nz; ++kr) D = std::min(D, Z.at(Z.dzc, kr));
+        *d2 = (double)(D * D);
+        const FT pr = ntr > 0 ? FT(desc.closure_Pr) : FT(1);
+        *prf = (double)std::max(FT(1), FT(1) / pr);
+    }
+    void read_run() {
+        GBO_CUDA(cudaMemcpyAsync(h_run, run_s.p, RUN_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    int timescales(double* adv, double* dif) override {
+        diffusion_constants(&h_run[RUN_DELTA2], &h_run[RUN_PR_FACTOR]);
+        GBO_CUDA(cudaMemcpyAsync(run_s.p + RUN_DELTA2, h_run + RUN_DELTA2, 2 * sizeof(double), cudaMemcpyHostToDevice, stream));
+        pre(G_SIM);
+        k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(sim_params(), SIM_TIMESCALES, 0, 0);
+        check_launch();
+        read_run();
+        if (adv) *adv = h_run[RUN_TAU_ADV];
+        if (dif) *dif = h_run[RUN_TAU_DIF];
+        return GBO_OK;
+    }
+
+    // The loop graph: k_sim_start, then WHILE { k_sim_begin, one time step reading Δt
+    // from RUN_DT, k_sim_callbacks }.  The condition starts at 1 on every launch (a
+    // time_step!(sim) always steps once); k_sim_begin clears it and only the last block of
+    // k_sim_callbacks sets it again, to 1 while running and below RUN_MAX_TAKEN iterations.
+    void build_run_graph() {
+        if (!run_stream) GBO_CUDA(cudaStreamCreateWithFlags(&run_stream, cudaStreamNonBlocking));
+        const SimP<FT> S = sim_params();
+        cudaGraph_t gph;
+        GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        k_sim_start<<<1, 1, 0, stream>>>(run_s.p);
+        GBO_CUDA(cudaGetLastError());
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        GBO_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+        cudaGraphConditionalHandle h;
+        GBO_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        GBO_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GBO_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        GBO_CUDA(cudaStreamBeginCaptureToGraph(run_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        const int64_t before = launches;
+        {
+            std::swap(stream, run_stream);  // the step's launches go to `stream`
+            try {
+                pre(G_SIM);
+                k_sim_begin<FT><<<1, 1, 0, stream>>>(run_s.p, dtf.p, stage_c(), h, 1);
+                check_launch();
+                full_step(dtf.p);
+                pre(G_SIM);
+                k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(S, SIM_AFTER_STEP, h, 1);
+                check_launch();
+            } catch (...) {
+                std::swap(stream, run_stream);
+                throw;
+            }
+            std::swap(stream, run_stream);
+        }
+        run_iter_launches = launches - before;
+        launches = before;
+        cudaGraph_t captured = nullptr;
+        GBO_CUDA(cudaStreamEndCapture(run_stream, &captured));
+        GBO_CUDA(cudaStreamEndCapture(stream, &gph));
+        GBO_CUDA(cudaGraphInstantiate(&run_graph, gph, 0));
+        GBO_CUDA(cudaGraphDestroy(gph));
+    }
+
+    int run(const gbo_run_desc* d, gbo_run_result* out) override {
+        if (!(d->dt > 0) || !std::isfinite(d->dt)) { err = "dt must be positive and finite"; return GBO_ERR_INVALID; }
+        if (d->minimum_relative_step != 0.0) { err = "minimum_relative_step > 0 (skipped time steps) is not supported"; return GBO_ERR_INVALID; }
+        if (d->iterations_per_launch < 1) { err = "iterations_per_launch must be at least 1"; return GBO_ERR_INVALID; }
+        if (d->nan_check_interval < 0 || d->wizard_interval < 0) { err = "callback intervals must be >= 0"; return GBO_ERR_INVALID; }
+        if (std::isnan(d->stop_time) || std::isnan(d->stop_iteration) || std::isnan(d->wall_time_limit)) {
+            err = "stop criteria must not be NaN";
+            return GBO_ERR_INVALID;
+        }
+        if (d->wizard_interval > 0) {
+            // TimeStepWizard's own checks (time_step_wizard.jl:75-77)
+            if (!(d->min_change < 1)) { err = "min_change must be < 1"; return GBO_ERR_INVALID; }
+            if (!(d->max_change > 1)) { err = "max_change must be > 1"; return GBO_ERR_INVALID; }
+        }
+        double* H = h_run;
+        std::fill(H, H + RUN_NSLOTS, 0.0);
+        // Simulation converts Δt and stop_time to the model's float type (simulation.jl:97-104)
+        H[RUN_SIM_DT] = (double)FT(d->dt);
+        H[RUN_DT] = H[RUN_SIM_DT];
+        H[RUN_TIME] = time;
+        H[RUN_ITER] = (double)iteration;
+        H[RUN_STOP_TIME] = (double)FT(d->stop_time);
+        H[RUN_STOP_ITER] = d->stop_iteration;
+        H[RUN_ALIGN] = d->align_time_step ? 1.0 : 0.0;
+        H[RUN_RUNNING] = 1.0;
+        H[RUN_MAX_TAKEN] = (double)d->iterations_per_launch;
+        H[RUN_WIZ_EVERY] = (double)d->wizard_interval;
+        H[RUN_CFL] = d->cfl;
+        H[RUN_DCFL] = d->diffusive_cfl;
+        H[RUN_MAX_CHANGE] = d->max_change;
+        H[RUN_MIN_CHANGE] = d->min_change;
+        H[RUN_MAX_DT] = d->max_dt;
+        H[RUN_MIN_DT] = d->min_dt;
+        H[RUN_NAN_EVERY] = (double)d->nan_check_interval;
+        diffusion_constants(&H[RUN_DELTA2], &H[RUN_PR_FACTOR]);
+        H[RUN_TAU_ADV] = H[RUN_TAU_DIF] = INFINITY;
+        GBO_CUDA(cudaMemcpyAsync(run_s.p, H, RUN_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));  // H is reused for the read-back
+        cg_status = GBO_OK;
+        if (iteration == 0) {  // initialize!(sim) of a fresh simulation: every callback once
+            pre(G_SIM);
+            k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(sim_params(), SIM_INIT, 0, 0);
+            check_launch();
+        }
+        if (!run_graph) build_run_graph();
+        const auto t0 = std::chrono::steady_clock::now();
+        int64_t steps = 0;
+        int reason = GBO_STOP_NONE;
+        for (;;) {
+            GBO_CUDA(cudaGraphLaunch(run_graph, stream));
+            read_run();
+            const int64_t taken = (int64_t)H[RUN_TAKEN];
+            steps += taken;
+            launches += 1 + run_iter_launches * taken;
+            time = H[RUN_TIME];
+            iteration = (int64_t)H[RUN_ITER];
+            if (cg) {  // CG iterations ran inside the graph: account for them now
+                read_cg_scalars();
+                launches += body_launches * (int64_t)(h_cgs[CG_ITERS] - iters_seen);
+                iters_seen = h_cgs[CG_ITERS];
+                last_iters = (int)h_cgs[CG_IT];
+                int st = cg_outcome();
+                if (st != GBO_OK) cg_status = st;
+            }
+            if (taken < 1) { err = "the simulation loop took no step"; return GBO_ERR_STATE; }
+            if (H[RUN_RUNNING] == 0.0) {
+                reason = (int)H[RUN_REASON];
+                break;
+            }
+            // wall_time_limit_exceeded (simulation.jl:257-269), checked once per launch
+            const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (wall >= d->wall_time_limit) {
+                reason = GBO_STOP_WALL_TIME;
+                break;
+            }
+        }
+        if (out) {
+            out->dt = H[RUN_SIM_DT];
+            out->time = time;
+            out->iteration = iteration;
+            out->steps = steps;
+            out->stop_reason = reason;
+            out->nan_detected = H[RUN_NAN] != 0.0;
+        }
+        if (H[RUN_NAN] != 0.0 && d->nan_erroring) {
+            char msg[160];
+            std::snprintf(msg, sizeof msg, "time = %.17g, iteration = %lld: NaN found in field u. Aborting simulation.", time,
+                          (long long)iteration);
+            err = msg;
+            return GBO_ERR_NAN;
+        }
+        return cg_status;
     }
 
     int poisson_device(void* phi, const void* rhs) override {
@@ -1312,6 +1543,42 @@ int gbo_set_state(gbo_model* m, const void* buf, int64_t bytes) {
     return guarded(m, [&]() { return m->set_state(buf, bytes); });
 }
 
+void gbo_run_desc_default(gbo_run_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    d->dt = 1.0;
+    d->stop_time = INFINITY;
+    d->stop_iteration = INFINITY;
+    d->wall_time_limit = INFINITY;
+    d->align_time_step = 1;
+    d->minimum_relative_step = 0.0;
+    d->nan_check_interval = 100;
+    d->nan_erroring = 0;
+    d->wizard_interval = 0;
+    d->cfl = 0.2;
+    d->diffusive_cfl = INFINITY;
+    d->max_change = 1.1;
+    d->min_change = 0.5;
+    d->max_dt = INFINITY;
+    d->min_dt = 0.0;
+    d->iterations_per_launch = 100;
+}
+
+int gbo_run(gbo_model* m, const gbo_run_desc* d, gbo_run_result* out) {
+    if (!m || !d) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->run(d, out); });
+}
+
+int gbo_cell_advection_timescale(gbo_model* m, double* out) {
+    if (!m || !out) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->timescales(out, nullptr); });
+}
+
+int gbo_cell_diffusion_timescale(gbo_model* m, double* out) {
+    if (!m || !out) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->timescales(nullptr, out); });
+}
+
 int gbo_field_device_pointer(gbo_model* m, int32_t field, void** dptr, int64_t* count) {
     if (!m || !dptr || !count) return GBO_ERR_INVALID;
     return guarded(m, [&]() { return m->device_pointer(field, dptr, count); });
@@ -1338,12 +1605,15 @@ struct gbo_ensemble {
     cudaEvent_t fork = nullptr, done = nullptr;
     std::vector<cudaEvent_t> joins;
     cudaGraphExec_t graph = nullptr;
-    double graph_dt = -1;
+    float* d_f32 = nullptr;         // stage factors of Δt for the FP32 and the FP64 members
+    double* d_f64 = nullptr;
     std::vector<int64_t> per_step;  // kernels each member records per step
     std::string err;
 
     ~gbo_ensemble() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (d_f32) cudaFree(d_f32);
+        if (d_f64) cudaFree(d_f64);
         for (cudaEvent_t e : joins) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (done) cudaEventDestroy(done);
@@ -1351,28 +1621,31 @@ struct gbo_ensemble {
         for (gbo_model* mm : members) delete mm;
     }
 
-    void build(double dt) {
-        if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
+    void build() {
+        if (!d_f32) GBO_CUDA(cudaMalloc(&d_f32, DTF_N * sizeof(float)));
+        if (!d_f64) GBO_CUDA(cudaMalloc(&d_f64, DTF_N * sizeof(double)));
         cudaGraph_t g;
         GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         GBO_CUDA(cudaEventRecord(fork, stream));
         for (size_t i = 0; i < members.size(); ++i) {
             cudaStream_t ms = static_cast<cudaStream_t>(members[i]->stream_ptr());
             GBO_CUDA(cudaStreamWaitEvent(ms, fork, 0));
-            per_step[i] = members[i]->capture_step(dt);
+            per_step[i] = members[i]->capture_step(d_f32, d_f64);
             GBO_CUDA(cudaEventRecord(joins[i], ms));
             GBO_CUDA(cudaStreamWaitEvent(stream, joins[i], 0));
         }
         GBO_CUDA(cudaStreamEndCapture(stream, &g));
         GBO_CUDA(cudaGraphInstantiate(&graph, g, 0));
         GBO_CUDA(cudaGraphDestroy(g));
-        graph_dt = dt;
     }
 
     int step(double dt, int nsteps) {
         if (nsteps <= 0) return GBO_OK;
-        if (!graph || graph_dt != dt) build(dt);
+        if (!graph) build();
+        k_set_dt_pair<<<1, 1, 0, stream>>>(d_f32, ModelImpl<float>::stage_c(), d_f64, ModelImpl<double>::stage_c(), dt);
+        GBO_CUDA(cudaGetLastError());
         for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
+        members[0]->add_launches(1);  // k_set_dt_pair
         GBO_CUDA(cudaEventRecord(done, stream));
         int rc = GBO_OK;
         for (size_t i = 0; i < members.size(); ++i) {

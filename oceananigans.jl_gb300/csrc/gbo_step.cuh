@@ -10,10 +10,16 @@
 #pragma once
 #include "gbo_kernels.cuh"
 
+// Δt of this stage: read from device memory when the step graph is Δt-independent
 template <typename FT>
-GBO_D FT rk3_update(FT U, FT G, FT Gm, const StepP<FT>& P) {
-    if (P.first) return U + (P.dt * P.gamma) * G;
-    return U + P.dt * (P.gamma * G + P.zeta * Gm);
+GBO_D FT stage_dt(const StepP<FT>& P) {
+    return P.dtf ? __ldg(P.dtf + DTF_DT) : P.dt;
+}
+
+template <typename FT>
+GBO_D FT rk3_update(FT U, FT G, FT Gm, const StepP<FT>& P, FT dt) {
+    if (P.first) return U + (dt * P.gamma) * G;
+    return U + dt * (P.gamma * G + P.zeta * Gm);
 }
 
 // Momentum: Gu, Gv, Gw at one (i, j, k) with the predictor update.
@@ -55,7 +61,7 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         }
         FT Gm = P.first ? FT(0) : P.Gu[idx];
         P.Gu[idx] = G;
-        P.uo[idx] = rk3_update(P.u[idx], G, Gm, P);
+        P.uo[idx] = rk3_update(P.u[idx], G, Gm, P, stage_dt(P));
     }
     // ---------------- v ----------------
     {
@@ -80,7 +86,7 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         }
         FT Gm = P.first ? FT(0) : P.Gv[idx];
         P.Gv[idx] = G;
-        P.vo[idx] = rk3_update(P.v[idx], G, Gm, P);
+        P.vo[idx] = rk3_update(P.v[idx], G, Gm, P, stage_dt(P));
     }
     // ---------------- w (interior faces only; k = 0 is the wall) ----------------
     if (!g.flatz) {
@@ -101,7 +107,7 @@ __global__ void __launch_bounds__(256) k_momentum(StepP<FT> P) {
         }
         FT Gm = P.first ? FT(0) : P.Gw[idx];
         P.Gw[idx] = G;
-        P.wo[idx] = rk3_update(P.w[idx], G, Gm, P);
+        P.wo[idx] = rk3_update(P.w[idx], G, Gm, P, stage_dt(P));
     }
 }
 
@@ -173,5 +179,5 @@ __global__ void __launch_bounds__(256) k_tracer(StepP<FT> P) {
     }
     FT Gm = P.first ? FT(0) : P.Gc[idx];
     P.Gc[idx] = G;
-    P.co[idx] = rk3_update(P.c[idx], G, Gm, P);
+    P.co[idx] = rk3_update(P.c[idx], G, Gm, P, stage_dt(P));
 }

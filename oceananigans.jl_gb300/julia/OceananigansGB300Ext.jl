@@ -22,8 +22,20 @@ using Oceananigans.Grids: topology, Periodic, Bounded, Flat
 using Oceananigans.ImmersedBoundaries: ImmersedBoundaryGrid
 using Oceananigans.Fields: interior
 using Oceananigans.Models.NonhydrostaticModels: NonhydrostaticModel
+using Oceananigans.Simulations: TimeStepWizard
+using Oceananigans.Utils: IterationInterval
 import Oceananigans.TimeSteppers: time_step!
 import Oceananigans.Fields: set!
+import Oceananigans: prognostic_state, restore_prognostic_state!
+import Oceananigans.Simulations: run!
+import Oceananigans.Advection: cell_advection_timescale
+
+# run!(sim) on a GB300 model: the whole loop on the device when its callbacks allow,
+# else the reference loop, which calls the time_step! method below once per step
+function run!(sim::Simulation{<:NonhydrostaticModel{<:Any, <:Any, <:Any, <:GB300}}; pickup=false, kw...)
+    pickup == false && isempty(kw) && device_run!(sim) && return nothing
+    return invoke(run!, Tuple{Any}, sim; pickup, kw...)
+end
 
 const libgbo = get(ENV, "GB300OCEAN_LIB", "libgb300ocean.so")
 
@@ -116,6 +128,85 @@ function time_step!(model::NonhydrostaticModel{<:Any, <:Any, <:Any, <:GB300}, Δ
     model.clock.time = t[]
     model.clock.iteration = it[]
     return nothing
+end
+
+# --- checkpointing: the state blob of gbo_get_state / gbo_set_state -------------------
+function prognostic_state(model::NonhydrostaticModel{<:Any, <:Any, <:Any, <:GB300})
+    h = handle(model)
+    buf = Vector{UInt8}(undef, ccall((:gbo_state_bytes, libgbo), Int64, (Ptr{Cvoid},), h))
+    check(ccall((:gbo_get_state, libgbo), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64), h, buf, length(buf)), h)
+    return (; gb300_state = buf)
+end
+
+function restore_prognostic_state!(model::NonhydrostaticModel{<:Any, <:Any, <:Any, <:GB300}, from)
+    h = handle(model)
+    buf = from.gb300_state
+    check(ccall((:gbo_set_state, libgbo), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64), h, buf, length(buf)), h)
+    t = Ref{Float64}(); it = Ref{Int64}()
+    ccall((:gbo_clock, libgbo), Cint, (Ptr{Cvoid}, Ref{Float64}, Ref{Int64}), h, t, it)
+    model.clock.time, model.clock.iteration = t[], it[]
+    return model
+end
+
+# --- run!(sim) as one device loop when its callbacks are the ones gbo_run implements ----
+struct RunDesc
+    dt::Float64
+    stop_time::Float64
+    stop_iteration::Float64
+    wall_time_limit::Float64
+    align_time_step::Int32
+    minimum_relative_step::Float64
+    nan_check_interval::Int32
+    nan_erroring::Int32
+    wizard_interval::Int32
+    cfl::Float64
+    diffusive_cfl::Float64
+    max_change::Float64
+    min_change::Float64
+    max_dt::Float64
+    min_dt::Float64
+    iterations_per_launch::Int32
+end
+
+struct RunResult
+    dt::Float64
+    time::Float64
+    iteration::Int64
+    steps::Int64
+    stop_reason::Int32
+    nan_detected::Int32
+end
+
+const default_callbacks = (:stop_time_exceeded, :stop_iteration_exceeded, :wall_time_limit_exceeded, :nan_checker)
+
+function device_run!(sim)
+    model = sim.model
+    extra = [k for k in keys(sim.callbacks) if k ∉ default_callbacks]
+    wizard = length(extra) == 1 ? sim.callbacks[extra[1]] : nothing
+    device_loop = isempty(sim.output_writers) && isempty(sim.diagnostics) &&
+                  (isempty(extra) || (wizard !== nothing && wizard.func isa TimeStepWizard &&
+                                      wizard.schedule isa IterationInterval && wizard.schedule.offset == 0))
+    device_loop || return false
+    nan = get(sim.callbacks, :nan_checker, nothing)
+    w = wizard === nothing ? TimeStepWizard() : wizard.func
+    d = RunDesc(sim.Δt, sim.stop_time, sim.stop_iteration, sim.wall_time_limit, sim.align_time_step,
+                sim.minimum_relative_step, nan === nothing ? 0 : nan.schedule.interval,
+                nan === nothing ? 0 : nan.func.erroring, wizard === nothing ? 0 : wizard.schedule.interval,
+                w.cfl, w.diffusive_cfl, w.max_change, w.min_change, w.max_Δt, w.min_Δt, 100)
+    r = Ref{RunResult}()
+    h = handle(model)
+    check(ccall((:gbo_run, libgbo), Cint, (Ptr{Cvoid}, Ref{RunDesc}, Ref{RunResult}), h, Ref(d), r), h)
+    sim.Δt = r[].dt
+    model.clock.time, model.clock.iteration = r[].time, r[].iteration
+    r[].nan_detected != 0 && (nan.func.nan_detected = true)
+    sim.running = false
+    return true
+end
+
+function cell_advection_timescale(model::NonhydrostaticModel{<:Any, <:Any, <:Any, <:GB300})
+    τ = Ref{Float64}()
+    check(ccall((:gbo_cell_advection_timescale, libgbo), Cint, (Ptr{Cvoid}, Ref{Float64}), handle(model), τ))
+    return τ[]
 end
 
 "Copy the device state into the host `Field`s (for output writers and diagnostics)."

@@ -10,5 +10,6 @@ from .api import (  # noqa: F401
     FluxBoundaryCondition, FieldBoundaryConditions,
     FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver,
     NonhydrostaticModel, Ensemble, Simulation, set_, time_step_, run_,
+    TimeStepWizard, conjure_time_step_wizard_, cell_advection_timescale, cell_diffusion_timescale,
 )
 from ._lib import GboError, NaNError, NotConvergedError, load  # noqa: F401

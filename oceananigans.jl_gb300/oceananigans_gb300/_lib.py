@@ -63,6 +63,25 @@ class NaNError(GboError):
     pass
 
 
+GBO_STOP_NONE, GBO_STOP_TIME, GBO_STOP_ITERATION, GBO_STOP_NAN, GBO_STOP_WALL_TIME = 0, 1, 2, 3, 4
+
+
+class RunDesc(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("stop_time", ctypes.c_double), ("stop_iteration", ctypes.c_double),
+                ("wall_time_limit", ctypes.c_double), ("align_time_step", ctypes.c_int32),
+                ("minimum_relative_step", ctypes.c_double), ("nan_check_interval", ctypes.c_int32),
+                ("nan_erroring", ctypes.c_int32), ("wizard_interval", ctypes.c_int32),
+                ("cfl", ctypes.c_double), ("diffusive_cfl", ctypes.c_double),
+                ("max_change", ctypes.c_double), ("min_change", ctypes.c_double),
+                ("max_dt", ctypes.c_double), ("min_dt", ctypes.c_double),
+                ("iterations_per_launch", ctypes.c_int32)]
+
+
+class RunResult(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("time", ctypes.c_double), ("iteration", ctypes.c_int64),
+                ("steps", ctypes.c_int64), ("stop_reason", ctypes.c_int32), ("nan_detected", ctypes.c_int32)]
+
+
 # Every exported entry point with its ctypes signature.  The test suite checks
 # that this table, include/gbo.h and the built library agree.
 _vp = ctypes.c_void_p
@@ -85,6 +104,10 @@ SIGNATURES = {
     "gbo_state_bytes": (ctypes.c_int64, [_vp]),
     "gbo_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "gbo_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
+    "gbo_run_desc_default": (None, [ctypes.POINTER(RunDesc)]),
+    "gbo_run": (ctypes.c_int, [_vp, ctypes.POINTER(RunDesc), ctypes.POINTER(RunResult)]),
+    "gbo_cell_advection_timescale": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "gbo_cell_diffusion_timescale": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "gbo_ensemble_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc),
                                            ctypes.POINTER(_vp)]),
     "gbo_ensemble_destroy": (None, [_vp]),

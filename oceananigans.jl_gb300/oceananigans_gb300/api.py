@@ -9,6 +9,7 @@ Names and argument meanings follow Oceananigans.jl:
   set!(model; u=..., b=...)                       set_nonhydrostatic_model.jl:39   -> set_
   time_step!(model, Δt)                           src/TimeSteppers/runge_kutta_3.jl:103 -> time_step_
   Simulation(model; Δt, stop_time), run!(sim)     src/Simulations/simulation.jl:12, run.jl:151 -> run_
+  TimeStepWizard, cell_advection_timescale       src/Simulations/time_step_wizard.jl:66, Advection/cell_advection_timescale.jl:15
 A trailing underscore stands for Julia's `!`.  Errors mirror the reference:
 invalid configurations raise ValueError (ArgumentError there).
 """
@@ -434,29 +435,101 @@ def time_step_(model, dt, nsteps=1):
     L.check(L.load().gbo_time_step(model._h, float(dt), int(nsteps)), model._h)
 
 
-class Simulation:
-    """Simulation(model; Δt, stop_time, stop_iteration) (src/Simulations/simulation.jl:12)."""
+class TimeStepWizard:
+    """TimeStepWizard(; cfl=0.2, diffusive_cfl=Inf, max_change=1.1, min_change=0.5,
+    max_Δt=Inf, min_Δt=0) (src/Simulations/time_step_wizard.jl:66-89).  Attached to a
+    Simulation as a callback on IterationInterval(interval); evaluated on the device."""
 
-    def __init__(self, model, dt, stop_time=math.inf, stop_iteration=math.inf, callbacks=()):
+    def __init__(self, cfl=0.2, diffusive_cfl=math.inf, max_change=1.1, min_change=0.5, max_dt=math.inf, min_dt=0.0):
+        if min_change >= 1:
+            raise ValueError("min_change must be < 1. You provided min_change = %r." % min_change)
+        if max_change <= 1:
+            raise ValueError("max_change must be > 1. You provided max_change = %r." % max_change)
+        self.cfl, self.diffusive_cfl = float(cfl), float(diffusive_cfl)
+        self.max_change, self.min_change = float(max_change), float(min_change)
+        self.max_dt, self.min_dt = float(max_dt), float(min_dt)
+
+
+class Simulation:
+    """Simulation(model; Δt, stop_time, stop_iteration, wall_time_limit, align_time_step,
+    minimum_relative_step) with the default NaNChecker (u every 100 iterations)
+    (src/Simulations/simulation.jl:68-119).  `dt` is converted to the model's float
+    type as in the reference; `wizard` / `wizard_interval` add a TimeStepWizard callback."""
+
+    def __init__(self, model, dt, stop_time=math.inf, stop_iteration=math.inf, wall_time_limit=math.inf,
+                 align_time_step=True, minimum_relative_step=0.0, nan_check_interval=100, nan_erroring=False,
+                 wizard=None, wizard_interval=10):
         self.model = model
-        self.dt = float(dt)
+        ft = np.float32 if model.dtype == np.float32 else np.float64
+        self.dt = float(ft(dt))
         self.stop_time = stop_time
         self.stop_iteration = stop_iteration
-        self.callbacks = list(callbacks)
+        self.wall_time_limit = wall_time_limit
+        self.align_time_step = bool(align_time_step)
+        self.minimum_relative_step = float(minimum_relative_step)
+        self.nan_check_interval = int(nan_check_interval)
+        self.nan_erroring = bool(nan_erroring)
+        self.wizard = wizard
+        self.wizard_interval = int(wizard_interval)
+        self.running = False
+        self.stop_reason = None
+        self.nan_detected = False
 
 
-def run_(sim, chunk=None):
-    """run!(sim): step until stop_time / stop_iteration; callbacks run between chunks."""
-    m = sim.model
-    while True:
-        t, it = m.clock
-        if it >= sim.stop_iteration or t >= sim.stop_time - 1e-12 * max(1.0, abs(sim.stop_time)):
-            break
-        n_time = math.ceil((sim.stop_time - t) / sim.dt - 1e-9) if math.isfinite(sim.stop_time) else 1 << 30
-        n_iter = sim.stop_iteration - it if math.isfinite(sim.stop_iteration) else 1 << 30
-        n = int(min(n_time, n_iter, chunk or (1 << 30)))
-        if n <= 0:
-            break
-        time_step_(m, sim.dt, n)
-        for cb in sim.callbacks:
-            cb(sim)
+def conjure_time_step_wizard_(sim, interval=10, **wizard_kw):
+    """conjure_time_step_wizard!(simulation, IterationInterval(interval); wizard_kw...)
+    (src/Simulations/time_step_wizard.jl:117-126)."""
+    sim.wizard = TimeStepWizard(**wizard_kw)
+    sim.wizard_interval = int(interval)
+
+
+STOP_REASONS = {L.GBO_STOP_NONE: None, L.GBO_STOP_TIME: "stop_time", L.GBO_STOP_ITERATION: "stop_iteration",
+                L.GBO_STOP_NAN: "nan", L.GBO_STOP_WALL_TIME: "wall_time_limit"}
+
+
+def run_(sim, iterations_per_launch=100):
+    """run!(sim) (src/Simulations/run.jl:151-187): the whole loop -- Δt alignment with
+    stop_time, time steps, stop criteria, NaN check, TimeStepWizard -- runs on the device
+    as one CUDA-graph launch per `iterations_per_launch` iterations."""
+    lib = L.load()
+    d = L.RunDesc()
+    lib.gbo_run_desc_default(ctypes.byref(d))
+    d.dt = sim.dt
+    d.stop_time = float(sim.stop_time)
+    d.stop_iteration = float(sim.stop_iteration)
+    d.wall_time_limit = float(sim.wall_time_limit)
+    d.align_time_step = int(sim.align_time_step)
+    d.minimum_relative_step = sim.minimum_relative_step
+    d.nan_check_interval = sim.nan_check_interval
+    d.nan_erroring = int(sim.nan_erroring)
+    if sim.wizard is not None:
+        w = sim.wizard
+        d.wizard_interval = sim.wizard_interval
+        d.cfl, d.diffusive_cfl = w.cfl, w.diffusive_cfl
+        d.max_change, d.min_change = w.max_change, w.min_change
+        d.max_dt, d.min_dt = w.max_dt, w.min_dt
+    d.iterations_per_launch = int(iterations_per_launch)
+    r = L.RunResult()
+    sim.running = True
+    try:
+        L.check(lib.gbo_run(sim.model._h, ctypes.byref(d), ctypes.byref(r)), sim.model._h)
+    finally:
+        sim.running = False
+    sim.dt = r.dt
+    sim.stop_reason = STOP_REASONS.get(r.stop_reason)
+    sim.nan_detected = bool(r.nan_detected)
+    return r
+
+
+def cell_advection_timescale(model):
+    """cell_advection_timescale(model) (src/Advection/cell_advection_timescale.jl:15-21)."""
+    out = ctypes.c_double()
+    L.check(L.load().gbo_cell_advection_timescale(model._h, ctypes.byref(out)), model._h)
+    return out.value
+
+
+def cell_diffusion_timescale(model):
+    """cell_diffusion_timescale(model) (src/TurbulenceClosures/turbulence_closure_diagnostics.jl:21-63)."""
+    out = ctypes.c_double()
+    L.check(L.load().gbo_cell_diffusion_timescale(model._h, ctypes.byref(out)), model._h)
+    return out.value

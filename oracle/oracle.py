@@ -6,6 +6,7 @@ C++ restatement of Oceananigans.jl's NonhydrostaticModel RK3 step; see the
 header of ocean_oracle.cpp for what it follows and how it is pinned.
 """
 import ctypes
+import math
 import os
 import subprocess
 import sys
@@ -188,3 +189,103 @@ def max_threads():
 def weno5(stencil, left=True):
     s = np.ascontiguousarray(np.asarray(stencil, dtype=np.float64))
     return lib().orc_weno5(_dptr(s), int(bool(left)))
+
+
+# ---------------------------------------------------------------------------
+# run!(simulation) restated over the oracle model (FP64): the checker of the
+# device-side simulation loop of the library.
+# ---------------------------------------------------------------------------
+STOP_TIME, STOP_ITERATION, STOP_NAN = 1, 2, 3
+
+
+def cell_advection_timescale(ref):
+    """min over cells of 1 / (|u|/Δxᶠᶜᶜ + |v|/Δyᶜᶠᶜ + |w|/Δzᶜᶜᶠ)
+    (src/Advection/cell_advection_timescale.jl:15-36); w at the bottom face of each cell."""
+    g = ref.grid
+    Nx, Ny, Nz = ref.shape
+    rdx, rdy = 1 / ((g.x[1] - g.x[0]) / Nx), 1 / ((g.y[1] - g.y[0]) / Ny)
+    inv = np.abs(ref.get("u")) * rdx + np.abs(ref.get("v")) * rdy
+    if not ref.flat:
+        H = 4 if g.bottom_height else 3
+        _, dzf = ref.z_spacings()
+        inv = inv + np.abs(ref.get("w")[:, :, :Nz]) * (1 / dzf[H:H + Nz])[None, None, :]
+    with np.errstate(divide="ignore"):
+        return float(np.min(1 / inv))
+
+
+def cell_diffusion_timescale(ref):
+    """Diffusion timescale of the closure (TurbulenceClosures/turbulence_closure_diagnostics.jl:8-13,
+    48-63): Δ² / (max νₑ max(1, 1/Pr)) for Smagorinsky-Lilly, min(Δ²/max νₑ, Δ²/max κₑ) for AMD
+    (max κₑ = Inf without tracers), Inf without a closure; Δ = min(Δx, Δy, min Δzᶜ)."""
+    g, d = ref.grid, ref.desc
+    if d.closure == 0:
+        return math.inf
+    Nx, Ny, Nz = ref.shape
+    D = min((g.x[1] - g.x[0]) / Nx, (g.y[1] - g.y[0]) / Ny)
+    if not ref.flat:
+        H = 4 if g.bottom_height else 3
+        dzc, _ = ref.z_spacings()
+        D = min(D, float(np.min(dzc[H:H + Nz])))
+    d2 = np.float64(D * D)
+    numax = np.max(ref.get("nu"))
+    with np.errstate(divide="ignore"):  # Δ²/0 = Inf as in Julia
+        if d.closure == 1:
+            pr = d.closure_Pr if d.ntracers > 0 else 1.0
+            return float(d2 / (numax * max(1.0, 1 / pr)))
+        kmax = np.max(ref.get("kappa")) if d.ntracers > 0 else np.inf
+        return float(min(d2 / numax, d2 / kmax))
+
+
+def new_time_step(old_dt, tau_adv, tau_dif, cfl=0.2, diffusive_cfl=math.inf, max_change=1.1, min_change=0.5,
+                  max_dt=math.inf, min_dt=0.0):
+    """new_time_step(old_Δt, wizard, model) (src/Simulations/time_step_wizard.jl:97-112)."""
+    adv = cfl * tau_adv
+    dif = math.inf if math.isinf(diffusive_cfl) else diffusive_cfl * tau_dif
+    dt = min(adv, dif)
+    dt = min(max_change * old_dt, dt)
+    dt = max(min_change * old_dt, dt)
+    return min(max(dt, min_dt), max_dt)
+
+
+def run(ref, dt, stop_time=math.inf, stop_iteration=math.inf, align_time_step=True, nan_check_interval=100,
+        wizard=None, wizard_interval=10, float_type=np.float64):
+    """run!(Simulation(model; Δt, stop_time, stop_iteration, align_time_step)) with the default
+    NaNChecker and an optional TimeStepWizard (keyword dict) on IterationInterval(wizard_interval)
+    (src/Simulations/run.jl:151-262, simulation.jl:68-119,243-269, run.jl:319-347).  Δt and
+    stop_time are rounded to the model's float type as Simulation does.  Returns the final
+    simulation Δt, the steps taken, the first stop reason and whether a NaN was found."""
+    ft = float_type
+    sim_dt = float(ft(dt))
+    stop_time = float(ft(stop_time))
+    st = {"running": True, "reason": 0, "nan": False, "dt": sim_dt}
+
+    def callbacks(every):
+        t, it = ref.clock()
+        if t >= stop_time:
+            st["running"] = False
+            st["reason"] = st["reason"] or STOP_TIME
+        if it >= stop_iteration:
+            st["running"] = False
+            st["reason"] = st["reason"] or STOP_ITERATION
+        if nan_check_interval > 0 and (every or it % nan_check_interval == 0) and np.isnan(ref.get("u")).any():
+            st["running"] = False
+            st["nan"] = True
+            st["reason"] = st["reason"] or STOP_NAN
+        if wizard is not None and wizard_interval > 0 and (every or it % wizard_interval == 0):
+            new = new_time_step(st["dt"], cell_advection_timescale(ref), cell_diffusion_timescale(ref), **wizard)
+            st["dt"] = float(ft(new))
+
+    if ref.clock()[1] == 0:  # initialize!(sim) of a fresh simulation
+        callbacks(True)
+    steps = 0
+    while True:
+        step_dt = st["dt"]
+        if align_time_step:
+            a = min(step_dt, stop_time - ref.clock()[0])
+            step_dt = step_dt if a <= 0 else a
+        ref.time_step(step_dt, 1)
+        steps += 1
+        callbacks(False)
+        if not st["running"]:
+            break
+    return {"dt": st["dt"], "steps": steps, "reason": st["reason"], "nan": st["nan"]}

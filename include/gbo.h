@@ -46,7 +46,8 @@ enum gbo_topology   { GBO_FLAT = 0, GBO_PERIODIC = 1, GBO_BOUNDED = 2 };
 enum gbo_float_type { GBO_FLOAT32 = 4, GBO_FLOAT64 = 8 };
 enum gbo_advection  { GBO_ADVECTION_NONE = 0, GBO_ADVECTION_CENTERED2 = 2, GBO_ADVECTION_WENO5 = 5 };
 enum gbo_closure    { GBO_CLOSURE_NONE = 0, GBO_CLOSURE_SMAGORINSKY_LILLY = 1,
-                      GBO_CLOSURE_AMD = 2 };
+                      GBO_CLOSURE_AMD = 2, GBO_CLOSURE_SCALAR_DIFFUSIVITY = 3 };
+enum gbo_timestepper { GBO_TIMESTEPPER_RK3 = 0, GBO_TIMESTEPPER_QAB2 = 1 };
 enum gbo_solver     { GBO_SOLVER_FFT = 0, GBO_SOLVER_FOURIER_TRIDIAGONAL = 1,
                       GBO_SOLVER_CONJUGATE_GRADIENT = 2 };
 enum gbo_precond    { GBO_PRECOND_FFT = 0, GBO_PRECOND_NONE = 1, GBO_PRECOND_LEARNED = 2 };
@@ -99,6 +100,14 @@ typedef struct gbo_model_desc {
     double  cg_reltol;               /* 0 -> sqrt(eps(FT)) as the reference defaults */
     double  cg_abstol;               /* 0 -> sqrt(eps(FT)) */
     int32_t cg_maxiter;              /* 0 -> Nx*Ny*Nz */
+    /* ScalarDiffusivity(ν, κ) with constant coefficients, isotropic and explicit
+     * (turbulence_closure_implementations/scalar_diffusivity.jl:8-80) */
+    double  closure_nu;
+    double  closure_kappa[GBO_MAX_TRACERS];
+    /* timestepper = :RungeKutta3 (default) or :QuasiAdamsBashforth2 with χ
+     * (src/TimeSteppers/quasi_adams_bashforth_2.jl:39-48; default χ = 0.1) */
+    int32_t timestepper;             /* gbo_timestepper */
+    double  ab2_chi;
 } gbo_model_desc;
 
 typedef struct gbo_model gbo_model;

@@ -51,7 +51,21 @@ struct GridP {
     const int* kbot;  // Nx*Ny entries or nullptr
 };
 
+// Periodic index within one period of the domain (the per-point stencils: |offset| <= 4
+// and N >= 8)
 GBO_D int wrapi(int i, int N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
+// Periodic index for any offset: tile fills and tile-edge loads reach up to a tile width
+// beyond the domain, which is more than one period when N is below the tile width plus
+// its halo
+GBO_D int wrapm(int i, int N) {
+    const int r = i % N;
+    return r < 0 ? r + N : r;
+}
+// The same with the one-period case first (tile fills: the modulo only on small grids)
+GBO_D int wrapt(int i, int N) {
+    i = i < 0 ? i + N : (i >= N ? i - N : i);
+    return (unsigned)i < (unsigned)N ? i : wrapm(i, N);
+}
 
 template <typename FT>
 GBO_D FT ldg(const FT* p) { return __ldg(p); }
@@ -82,6 +96,15 @@ template <typename FT>
 struct CFld {
     const FT* __restrict__ a;
     int Nx, Ny, Nz, flatz;
+    // (i, j) any distance outside the domain (tile fills)
+    GBO_D FT far(int i, int j, int k) const { return (*this)(wrapt(i, Nx), wrapt(j, Ny), k); }
+    // the column at offset c = i + Nx j of the domain, at level k
+    GBO_D FT col(size_t c, int k) const {
+        if (flatz) return ldg(a + c);
+        if (k < -1 || k > Nz) return FT(0);
+        k = k < 0 ? 0 : (k >= Nz ? Nz - 1 : k);
+        return ldg(a + c + (size_t)Nx * Ny * k);
+    }
     GBO_D FT operator()(int i, int j, int k) const {
         i = wrapi(i, Nx);
         j = wrapi(j, Ny);
@@ -97,6 +120,7 @@ template <typename FT>
 struct WFld {
     const FT* __restrict__ a;
     int Nx, Ny, Nz;
+    GBO_D FT far(int i, int j, int k) const { return (*this)(wrapt(i, Nx), wrapt(j, Ny), k); }
     GBO_D FT operator()(int i, int j, int k) const {
         if (k <= 0 || k >= Nz) return FT(0);
         i = wrapi(i, Nx);

@@ -88,7 +88,7 @@ GBO_D PlanePlan make_plan(const GridP<FT>& g, int i0, int j0, int tid) {
         p.off[m] = 0;
         if (e < PS) {
             int px = e % PX, py = e / PX;
-            int gi = wrapi(i0 + px - H, g.Nx), gj = wrapi(j0 + py - H, g.Ny);
+            int gi = wrapm(i0 + px - H, g.Nx), gj = wrapm(j0 + py - H, g.Ny);
             p.off[m] = gi + g.Nx * gj;
             p.n = m + 1;
         }
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     if constexpr (IBG) {
         for (int e = tid; e < KBS; e += NT) {
             const int x = e % KBX - KBH, y = e / KBX - KBH;
-            s.KB[e] = __ldg(g.kbot + wrapi(i0 + x, g.Nx) + (size_t)g.Nx * wrapi(j0 + y, g.Ny));
+            s.KB[e] = __ldg(g.kbot + wrapt(i0 + x, g.Nx) + (size_t)g.Nx * wrapt(j0 + y, g.Ny));
         }
     }
     // cell (x, y, k) immersed / inactive (immersed or outside the Bounded z)
@@ -305,6 +305,10 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     }
 
     const FT dt = stage_dt(P);
+    // the tile-edge column that pass 1 below loads (the east column for warp 0, the north
+    // row for warp 1), wrapped once: on grids narrower than a tile it lies more than one
+    // period outside the domain
+    const size_t fcol = (size_t)wrapm(i0 + (ty == 0 ? TX : tx), g.Nx) + (size_t)g.Nx * wrapm(j0 + (ty == 0 ? tx : TY), g.Ny);
     int r3 = m3(kb);
     for (int k = kb; k < ke; ++k) {
         // ring slots of levels k-1, k, k+1 (and k+2, which shares the slot of k-1)
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
                 } else {
 #pragma unroll
-                    for (int o = 0; o < 4; ++o) uz[o] = Ug(i0 + x, j0 + y, k - 2 + o);
+                    for (int o = 0; o < 4; ++o) uz[o] = Ug.col(fcol, k - 2 + o);
                 }
                 auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
 #pragma unroll
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
                 } else {
 #pragma unroll
-                    for (int o = 0; o < 4; ++o) vz[o] = Vg(i0 + x, j0 + y, k - 2 + o);
+                    for (int o = 0; o < 4; ++o) vz[o] = Vg.col(fcol, k - 2 + o);
                 }
                 auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
 #pragma unroll
@@ -698,18 +702,23 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
     // tile fill with asynchronous copies: halos synthesised as in CFld / WFld (periodic
     // wrap in x, y; one mirrored layer in z and zero beyond for centres; zero at and
     // beyond the walls for w), a zero-filled copy where the value is zero
-    for (int e = tid; e < BS; e += TX * TY) {
-        const int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
-        const size_t col = wrapi(i0 + x, g.Nx) + (size_t)g.Nx * wrapi(j0 + y, g.Ny);
-        const int zc = fused::zsrc_c(k0 + z, Nz, fz), zw = fz ? -1 : fused::zsrc_w(k0 + z, Nz);
-        const size_t oc = col + (zc < 0 ? 0 : (size_t)zc * plane), ow = col + (zw < 0 ? 0 : (size_t)zw * plane);
-        fused::cp_async(&s.u[e], P.u + oc, zc < 0);
-        fused::cp_async(&s.v[e], P.v + oc, zc < 0);
-        if (fz) s.w[e] = FT(0);
-        else fused::cp_async(&s.w[e], P.w + ow, zw < 0);
-        if (buoy) fused::cp_async(&s.b[e], P.b + oc, zc < 0);
-        else s.b[e] = FT(0);
-    }
+    auto fill = [&](auto wrap) {
+        for (int e = tid; e < BS; e += TX * TY) {
+            const int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
+            const size_t col = wrap(i0 + x, g.Nx) + (size_t)g.Nx * wrap(j0 + y, g.Ny);
+            const int zc = fused::zsrc_c(k0 + z, Nz, fz), zw = fz ? -1 : fused::zsrc_w(k0 + z, Nz);
+            const size_t oc = col + (zc < 0 ? 0 : (size_t)zc * plane), ow = col + (zw < 0 ? 0 : (size_t)zw * plane);
+            fused::cp_async(&s.u[e], P.u + oc, zc < 0);
+            fused::cp_async(&s.v[e], P.v + oc, zc < 0);
+            if (fz) s.w[e] = FT(0);
+            else fused::cp_async(&s.w[e], P.w + ow, zw < 0);
+            if (buoy) fused::cp_async(&s.b[e], P.b + oc, zc < 0);
+            else s.b[e] = FT(0);
+        }
+    };
+    // a tile reaches at most one period outside a domain of at least two tiles
+    if (g.Nx >= 2 * BX && g.Ny >= 2 * BY) fill([](int i, int n) { return wrapi(i, n); });
+    else fill([](int i, int n) { return wrapm(i, n); });
     fused::cp_async_commit();
     fused::cp_async_wait_all();
     __syncthreads();
@@ -819,10 +828,10 @@ __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__
     for (int e = tid; e < BS; e += TX * TY) {
         int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
         int gi = i0 + x, gj = j0 + y, gk = k0 + z;
-        s.u[e] = Ug(gi, gj, gk);
-        s.v[e] = Vg(gi, gj, gk);
-        s.w[e] = Wg(gi, gj, gk);
-        s.b[e] = has_c ? Cg(gi, gj, gk) : FT(0);
+        s.u[e] = Ug.far(gi, gj, gk);
+        s.v[e] = Vg.far(gi, gj, gk);
+        s.w[e] = Wg.far(gi, gj, gk);
+        s.b[e] = has_c ? Cg.far(gi, gj, gk) : FT(0);
     }
     __syncthreads();
     const int i = i0 + tx, j = j0 + ty;

@@ -373,18 +373,23 @@ struct ModelImpl : gbo_model {
     unsigned int* h_flags = nullptr;
     // graph of one time step (Δt is read from the stage factors dtf, so one graph serves every Δt)
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph_euler = nullptr;  // QAB2: the Euler step
     bool use_graph = true;
+    bool qab2 = false;
+    double last_dt = INFINITY;           // clock.last_Δt
     // simulation loop (gbo_run): state slots, block partials, graph of the loop
     DBuf<FT> dtf;                        // stage factors of the current Δt (DTF_*)
     DBuf<double> run_s, run_part;
     DBuf<unsigned int> run_cnt;
     double* h_run = nullptr;
     cudaStream_t run_stream = nullptr;   // captures the loop body into a conditional node
+    cudaStream_t if_stream = nullptr;    // captures the Euler / AB2 branches (QAB2)
     cudaGraphExec_t run_graph = nullptr;
     int64_t run_iter_launches = 0;       // kernels per loop iteration (CG iterations apart)
 
     ~ModelImpl() override {
         if (graph) cudaGraphExecDestroy(graph);
+        if (graph_euler) cudaGraphExecDestroy(graph_euler);
         if (run_graph) cudaGraphExecDestroy(run_graph);
         dtf.free_();
         run_s.free_();
@@ -392,6 +397,7 @@ struct ModelImpl : gbo_model {
         run_cnt.free_();
         if (h_run) cudaFreeHost(h_run);
         if (run_stream) cudaStreamDestroy(run_stream);
+        if (if_stream) cudaStreamDestroy(if_stream);
         for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz,
                             &cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x})
             b->free_();
@@ -466,7 +472,8 @@ struct ModelImpl : gbo_model {
         // fields
         for (DBuf<FT>* b : {&u, &v, &us, &vs, &Gu, &Gv, &p, &rb}) b->alloc(N);
         if (!flat) { w.alloc(N); ws.alloc(N); Gw.alloc(N); }
-        if (md->closure != GBO_CLOSURE_NONE) nu.alloc(N);
+        const bool scalar = md->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY;
+        if (md->closure != GBO_CLOSURE_NONE && !scalar) nu.alloc(N);
         if (has_phy) phy.alloc(N);
         c.resize(ntr); cs.resize(ntr); Gc.resize(ntr);
         for (int n = 0; n < ntr; ++n) { c[n].alloc(N); cs[n].alloc(N); Gc[n].alloc(N); }
@@ -474,6 +481,14 @@ struct ModelImpl : gbo_model {
             kap.resize(ntr);
             for (int n = 0; n < ntr; ++n) kap[n].alloc(N);
         }
+        if (scalar) {
+            kap.resize(ntr);
+            // constant ν and κ held as fields: the AMD flux code reads them, and ν at
+            // edges, ½(a + a) and ¼(4a), is a exactly as the reference's constant
+            nu.upload(std::vector<FT>(N, FT(md->closure_nu)));
+            for (int n = 0; n < ntr; ++n) kap[n].upload(std::vector<FT>(N, FT(md->closure_kappa[n])));
+        }
+        qab2 = md->timestepper == GBO_TIMESTEPPER_QAB2;
         GBO_CUDA(cudaMalloc(&d_flags, sizeof(unsigned int)));
         GBO_CUDA(cudaMemset(d_flags, 0, sizeof(unsigned int)));
         GBO_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned int)));
@@ -588,6 +603,13 @@ struct ModelImpl : gbo_model {
         }
     }
 
+    // Flux code of the closure: ScalarDiffusivity runs the AMD fluxes on its constant
+    // ν and κ fields (viscous fluxes 2νΣᵢⱼ and diffusive fluxes κ∂c of
+    // abstract_scalar_diffusivity_closure.jl:214-262 for every AbstractScalarDiffusivity)
+    int kernel_closure() const {
+        return desc.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY ? (int)CL_AMD : desc.closure;
+    }
+
     StepP<FT> params() {
         StepP<FT> P{};
         P.g = gp;
@@ -599,7 +621,7 @@ struct ModelImpl : gbo_model {
         P.f = FT(desc.coriolis_f);
         P.has_cor = desc.has_coriolis;
         P.has_phy = has_phy;
-        P.closure = desc.closure;
+        P.closure = kernel_closure();
         P.buoyancy = desc.buoyancy_tracer && ntr > 0;
         P.Pr = FT(desc.closure_Pr);
         P.C = FT(desc.closure_C);
@@ -883,11 +905,11 @@ struct ModelImpl : gbo_model {
             M0.flux_top = FT(desc.tracer_flux_top[0]);
             M0.flux_bot = FT(desc.tracer_flux_bottom[0]);
             pre(G_MOMENTUM);
-            launch_fused<FT, true>(desc.closure, ibg, fgrid, fblock, stream, M0, kchunk);
+            launch_fused<FT, true>(kernel_closure(), ibg, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         } else {
             pre(G_MOMENTUM);
-            launch_fused<FT, false>(desc.closure, ibg, fgrid, fblock, stream, M0, kchunk);
+            launch_fused<FT, false>(kernel_closure(), ibg, fgrid, fblock, stream, M0, kchunk);
             check_launch();
         }
         for (int n = tracer0; n < ntr; ++n) {
@@ -924,18 +946,48 @@ struct ModelImpl : gbo_model {
         }
     }
 
-    void full_step(const FT* dtf) {
+    // One time step.  RK3: three stages.  QAB2 (quasi_adams_bashforth_2.jl:100-121,
+    // nonhydrostatic_ab2_step.jl:29-58): one stage U* = U + Δt (α Gⁿ - β G⁻) with
+    // α = 3/2 + χ, β = 1/2 + χ in FT, projected with Δτ = Δt; `euler` (χ = -1/2) takes
+    // U + Δt Gⁿ and reads no G⁻.
+    void full_step(const FT* dtf, bool euler = false) {
         using K = GboCoeffs<double>;
+        if (qab2) {
+            const FT chi = FT(desc.ab2_chi);
+            const FT alpha = FT(1.5) + chi, beta = FT(0.5) + chi;
+            if (euler) stage(dtf, 0, 1.0, 0.0, true);
+            else stage(dtf, 0, (double)alpha, -(double)beta, false);
+            return;
+        }
         stage(dtf, 0, K::rk3_gamma1, 0.0, true);
         stage(dtf, 1, K::rk3_gamma2, K::rk3_zeta2, false);
         stage(dtf, 2, K::rk3_gamma3, K::rk3_zeta3, false);
     }
     // c of Δτ = FT(Δt c) per stage: γ₁, and γ + ζ summed in FT (runge_kutta_3.jl:186-187)
-    static StageC stage_c() {
+    static StageC rk3_stage_c() {
         using K = GboCoeffs<double>;
         return StageC{(double)FT(K::rk3_gamma1), (double)(FT(K::rk3_gamma2) + FT(K::rk3_zeta2)),
                       (double)(FT(K::rk3_gamma3) + FT(K::rk3_zeta3))};
     }
+    // QAB2 projects with Δτ = FT(Δt) (kernel_Δt, nonhydrostatic_ab2_step.jl:30,56-57)
+    StageC stage_c() const { return qab2 ? StageC{1.0, 1.0, 1.0} : rk3_stage_c(); }
+
+    cudaGraphExec_t capture_graph(bool euler) {
+        cudaGraph_t gph;
+        cudaGraphExec_t exec = nullptr;
+        GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int64_t before = launches;
+        full_step(dtf.p, euler);
+        graph_launches_per_step = launches - before;
+        launches = before;
+        GBO_CUDA(cudaStreamEndCapture(stream, &gph));
+        GBO_CUDA(cudaGraphInstantiate(&exec, gph, 0));
+        GBO_CUDA(cudaGraphDestroy(gph));
+        return exec;
+    }
+    // QAB2 takes an Euler step whenever Δt differs from the last one, the first
+    // step included (last_Δt = Inf; quasi_adams_bashforth_2.jl:101)
+    bool euler_step(double dt) const { return qab2 && dt != last_dt; }
 
     // Δt of the next steps into the stage factors the stage kernels read
     void set_dt(double dt, cudaStream_t st) {
@@ -949,23 +1001,18 @@ struct ModelImpl : gbo_model {
         cg_status = GBO_OK;
         set_dt(dt, stream);
         if (use_graph) {
-            if (!graph) {
-                cudaGraph_t gph;
-                GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-                int64_t before = launches;
-                full_step(dtf.p);
-                graph_launches_per_step = launches - before;
-                launches = before;
-                GBO_CUDA(cudaStreamEndCapture(stream, &gph));
-                GBO_CUDA(cudaGraphInstantiate(&graph, gph, 0));
-                GBO_CUDA(cudaGraphDestroy(gph));
+            if (!graph) graph = capture_graph(false);
+            if (qab2 && !graph_euler) graph_euler = capture_graph(true);
+            for (int s = 0; s < nsteps; ++s) {
+                GBO_CUDA(cudaGraphLaunch(euler_step(dt) ? graph_euler : graph, stream));
+                last_dt = dt;
             }
-            for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
             launches += graph_launches_per_step * nsteps;
         } else {
             int worst = GBO_OK;
             for (int s = 0; s < nsteps; ++s) {
-                full_step(dtf.p);
+                full_step(dtf.p, euler_step(dt));
+                last_dt = dt;
                 if (cg_status != GBO_OK) worst = cg_status;
             }
             cg_status = worst;
@@ -1020,7 +1067,8 @@ struct ModelImpl : gbo_model {
         try {
             set_dt(dt, stream);
             for (int s = 0; s < nsteps; ++s) {
-                full_step(dtf.p);
+                full_step(dtf.p, euler_step(dt));
+                last_dt = dt;
                 time += dt;
                 iteration += 1;
             }
@@ -1137,16 +1185,25 @@ struct ModelImpl : gbo_model {
     // closure fields and pHY′ are recomputed from the restored state.
     struct StateHeader {
         uint64_t magic;
-        int32_t version, dtype, Nx, Ny, Nz, ntr;
+        int32_t version, dtype, Nx, Ny, Nz, ntr, timestepper;
         double time;
         int64_t iteration;
+        double last_dt;
     };
     static constexpr uint64_t kStateMagic = 0x31657461747362ULL;  // "bstate1"
+    static constexpr int32_t kStateVersion = 2;
+    // QAB2 also keeps G⁻ (prognostic_state of its timestepper): the next step reads it
     std::vector<const FT*> state_fields() const {
         std::vector<const FT*> f{u.p, v.p};
         if (!flat) f.push_back(w.p);
         for (int n = 0; n < ntr; ++n) f.push_back(c[n].p);
         f.push_back(p.p);
+        if (qab2) {
+            f.push_back(Gu.p);
+            f.push_back(Gv.p);
+            if (!flat) f.push_back(Gw.p);
+            for (int n = 0; n < ntr; ++n) f.push_back(Gc[n].p);
+        }
         return f;
     }
     int64_t state_bytes() const override {
@@ -1154,7 +1211,7 @@ struct ModelImpl : gbo_model {
     }
     int get_state(void* buf, int64_t bytes) override {
         if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
-        StateHeader h{kStateMagic, 1, dtype, Nx, Ny, Nz, ntr, time, iteration};
+        StateHeader h{kStateMagic, kStateVersion, dtype, Nx, Ny, Nz, ntr, desc.timestepper, time, iteration, last_dt};
         std::memcpy(buf, &h, sizeof(h));
         char* at = static_cast<char*>(buf) + sizeof(h);
         for (const FT* f : state_fields()) {
@@ -1168,9 +1225,9 @@ struct ModelImpl : gbo_model {
         if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
         StateHeader h;
         std::memcpy(&h, buf, sizeof(h));
-        if (h.magic != kStateMagic || h.version != 1) { err = "not a state written by gbo_get_state"; return GBO_ERR_INVALID; }
-        if (h.dtype != dtype || h.Nx != Nx || h.Ny != Ny || h.Nz != Nz || h.ntr != ntr) {
-            err = "state was written by a model of another size, float type or tracer count";
+        if (h.magic != kStateMagic || h.version != kStateVersion) { err = "not a state written by gbo_get_state"; return GBO_ERR_INVALID; }
+        if (h.dtype != dtype || h.Nx != Nx || h.Ny != Ny || h.Nz != Nz || h.ntr != ntr || h.timestepper != desc.timestepper) {
+            err = "state was written by a model of another size, float type, tracer count or timestepper";
             return GBO_ERR_INVALID;
         }
         const char* at = static_cast<const char*>(buf) + sizeof(h);
@@ -1180,6 +1237,7 @@ struct ModelImpl : gbo_model {
         }
         time = h.time;
         iteration = h.iteration;
+        last_dt = h.last_dt;
         mask_tracers();
         auxiliaries();
         return sync();
@@ -1226,55 +1284,86 @@ struct ModelImpl : gbo_model {
         return GBO_OK;
     }
 
-    // The loop graph: k_sim_start, then WHILE { k_sim_begin, one time step reading Δt
-    // from RUN_DT, k_sim_callbacks }.  The condition starts at 1 on every launch (a
-    // time_step!(sim) always steps once); k_sim_begin clears it and only the last block of
-    // k_sim_callbacks sets it again, to 1 while running and below RUN_MAX_TAKEN iterations.
-    void build_run_graph() {
-        if (!run_stream) GBO_CUDA(cudaStreamCreateWithFlags(&run_stream, cudaStreamNonBlocking));
-        const SimP<FT> S = sim_params();
-        cudaGraph_t gph;
-        GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        k_sim_start<<<1, 1, 0, stream>>>(run_s.p);
-        GBO_CUDA(cudaGetLastError());
+    // Add a conditional node (WHILE, or IF with an ELSE body) after the work captured so
+    // far on `stream` and record each body with body(i) while `stream` points at a
+    // stream capturing into that body.
+    template <class F>
+    void capture_conditional(cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned nbodies,
+                             cudaStream_t& aux, F&& body) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaGraph_t g = nullptr;
         const cudaGraphNode_t* deps = nullptr;
         size_t nd = 0;
         GBO_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &nd));
-        cudaGraphConditionalHandle h;
-        GBO_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = h;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
+        cp.conditional.type = type;
+        cp.conditional.size = nbodies;
         cudaGraphNode_t node;
         GBO_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
         GBO_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-        GBO_CUDA(cudaStreamBeginCaptureToGraph(run_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        const int64_t before = launches;
-        {
-            std::swap(stream, run_stream);  // the step's launches go to `stream`
+        for (unsigned b = 0; b < nbodies; ++b) {
+            GBO_CUDA(cudaStreamBeginCaptureToGraph(aux, cp.conditional.phGraph_out[b], nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal));
+            std::swap(stream, aux);
             try {
-                pre(G_SIM);
-                k_sim_begin<FT><<<1, 1, 0, stream>>>(run_s.p, dtf.p, stage_c(), h, 1);
-                check_launch();
-                full_step(dtf.p);
-                pre(G_SIM);
-                k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(S, SIM_AFTER_STEP, h, 1);
-                check_launch();
+                body(b);
             } catch (...) {
-                std::swap(stream, run_stream);
+                std::swap(stream, aux);
                 throw;
             }
-            std::swap(stream, run_stream);
+            std::swap(stream, aux);
+            cudaGraph_t captured = nullptr;
+            GBO_CUDA(cudaStreamEndCapture(aux, &captured));
         }
-        run_iter_launches = launches - before;
+    }
+    cudaGraphConditionalHandle new_handle(unsigned dflt, unsigned flags) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaGraph_t g = nullptr;
+        GBO_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+        cudaGraphConditionalHandle h;
+        GBO_CUDA(cudaGraphConditionalHandleCreate(&h, g, dflt, flags));
+        return h;
+    }
+
+    // The loop graph: k_sim_start, then WHILE { k_sim_begin, one time step reading Δt
+    // from the stage factors, k_sim_callbacks }.  The condition starts at 1 on every
+    // launch (a time_step!(sim) always steps once); k_sim_begin clears it and only the
+    // last block of k_sim_callbacks sets it again, to 1 while running and below
+    // RUN_MAX_TAKEN iterations.  With QAB2 the step is an IF node whose bodies are the
+    // Euler step and the AB2 step, chosen by k_sim_begin.
+    void build_run_graph() {
+        if (!run_stream) GBO_CUDA(cudaStreamCreateWithFlags(&run_stream, cudaStreamNonBlocking));
+        if (qab2 && !if_stream) GBO_CUDA(cudaStreamCreateWithFlags(&if_stream, cudaStreamNonBlocking));
+        const SimP<FT> S = sim_params();
+        cudaGraph_t gph;
+        GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        k_sim_start<<<1, 1, 0, stream>>>(run_s.p);
+        GBO_CUDA(cudaGetLastError());
+        const cudaGraphConditionalHandle h = new_handle(1, cudaGraphCondAssignDefault);
+        const int64_t before = launches;
+        int64_t branch = 0;  // kernels of the branch not taken (QAB2)
+        capture_conditional(h, cudaGraphCondTypeWhile, 1, run_stream, [&](unsigned) {
+            const cudaGraphConditionalHandle he = qab2 ? new_handle(0, 0) : 0;
+            pre(G_SIM);
+            k_sim_begin<FT><<<1, 1, 0, stream>>>(run_s.p, dtf.p, stage_c(), h, he, 1, qab2 ? 1 : 0);
+            check_launch();
+            if (qab2) {
+                capture_conditional(he, cudaGraphCondTypeIf, 2, if_stream, [&](unsigned b) {
+                    const int64_t at = launches;
+                    full_step(dtf.p, b == 0);
+                    if (b == 1) branch = launches - at;
+                });
+            } else {
+                full_step(dtf.p);
+            }
+            pre(G_SIM);
+            k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(S, SIM_AFTER_STEP, h, 1);
+            check_launch();
+        });
+        run_iter_launches = launches - before - branch;
         launches = before;
-        cudaGraph_t captured = nullptr;
-        GBO_CUDA(cudaStreamEndCapture(run_stream, &captured));
         GBO_CUDA(cudaStreamEndCapture(stream, &gph));
         GBO_CUDA(cudaGraphInstantiate(&run_graph, gph, 0));
         GBO_CUDA(cudaGraphDestroy(gph));
@@ -1316,6 +1405,7 @@ struct ModelImpl : gbo_model {
         H[RUN_NAN_EVERY] = (double)d->nan_check_interval;
         diffusion_constants(&H[RUN_DELTA2], &H[RUN_PR_FACTOR]);
         H[RUN_TAU_ADV] = H[RUN_TAU_DIF] = INFINITY;
+        H[RUN_LAST_DT] = last_dt;
         GBO_CUDA(cudaMemcpyAsync(run_s.p, H, RUN_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, stream));
         GBO_CUDA(cudaStreamSynchronize(stream));  // H is reused for the read-back
         cg_status = GBO_OK;
@@ -1336,6 +1426,7 @@ struct ModelImpl : gbo_model {
             launches += 1 + run_iter_launches * taken;
             time = H[RUN_TIME];
             iteration = (int64_t)H[RUN_ITER];
+            last_dt = H[RUN_LAST_DT];
             if (cg) {  // CG iterations ran inside the graph: account for them now
                 read_cg_scalars();
                 launches += body_launches * (int64_t)(h_cgs[CG_ITERS] - iters_seen);
@@ -1440,7 +1531,15 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
         for (int k = 0; k < nz; ++k)
             if (!(g->z_faces[k + 1] > g->z_faces[k])) return "z_faces must be increasing";
     if (d->advection != GBO_ADVECTION_WENO5) return "only WENO(order=5) advection is implemented";
-    if (d->closure < 0 || d->closure > 2) return "unknown closure";
+    if (d->closure < 0 || d->closure > 3) return "unknown closure";
+    if (d->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
+        if (!(d->closure_nu >= 0) || !std::isfinite(d->closure_nu)) return "ScalarDiffusivity ν must be finite and >= 0";
+        for (int n = 0; n < d->ntracers && n < GBO_MAX_TRACERS; ++n)
+            if (!(d->closure_kappa[n] >= 0) || !std::isfinite(d->closure_kappa[n]))
+                return "ScalarDiffusivity κ must be finite and >= 0";
+    }
+    if (d->timestepper != GBO_TIMESTEPPER_RK3 && d->timestepper != GBO_TIMESTEPPER_QAB2) return "unknown timestepper";
+    if (d->timestepper == GBO_TIMESTEPPER_QAB2 && !std::isfinite(d->ab2_chi)) return "QuasiAdamsBashforth2 χ must be finite";
     if (d->ntracers < 0 || d->ntracers > GBO_MAX_TRACERS) return "ntracers out of range";
     if (d->buoyancy_tracer && d->ntracers < 1) return "BuoyancyTracer requires tracer b (tracer 0)";
     if (d->pressure_solver == GBO_SOLVER_FFT && g->z_faces) return "FFTBasedPoissonSolver requires a regular grid";
@@ -1476,6 +1575,8 @@ void gbo_model_desc_default(gbo_model_desc* d) {
     d->closure_Pr = 1.0;
     d->pressure_solver = GBO_SOLVER_FFT;
     d->preconditioner = GBO_PRECOND_FFT;
+    d->timestepper = GBO_TIMESTEPPER_RK3;
+    d->ab2_chi = 0.1;
 }
 
 int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out) {
@@ -1642,7 +1743,7 @@ struct gbo_ensemble {
     int step(double dt, int nsteps) {
         if (nsteps <= 0) return GBO_OK;
         if (!graph) build();
-        k_set_dt_pair<<<1, 1, 0, stream>>>(d_f32, ModelImpl<float>::stage_c(), d_f64, ModelImpl<double>::stage_c(), dt);
+        k_set_dt_pair<<<1, 1, 0, stream>>>(d_f32, ModelImpl<float>::rk3_stage_c(), d_f64, ModelImpl<double>::rk3_stage_c(), dt);
         GBO_CUDA(cudaGetLastError());
         for (int s = 0; s < nsteps; ++s) GBO_CUDA(cudaGraphLaunch(graph, stream));
         members[0]->add_launches(1);  // k_set_dt_pair
@@ -1684,6 +1785,11 @@ extern "C" {
 int gbo_ensemble_create(int32_t n, const gbo_grid_desc* grids, const gbo_model_desc* descs, gbo_ensemble** out) {
     if (!out || !grids || !descs || n < 1) { g_last_error = "invalid ensemble arguments"; return GBO_ERR_INVALID; }
     *out = nullptr;
+    for (int32_t i = 0; i < n; ++i)
+        if (descs[i].timestepper != GBO_TIMESTEPPER_RK3) {
+            g_last_error = "member " + std::to_string(i) + ": ensembles step RungeKutta3 models only";
+            return GBO_ERR_INVALID;
+        }
     auto* e = new gbo_ensemble();
     for (int32_t i = 0; i < n; ++i) {
         gbo_model* mm = nullptr;

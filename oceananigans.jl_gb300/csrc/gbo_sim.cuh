@@ -41,6 +41,7 @@ enum {
     RUN_DELTA2,        // Δ² of the diffusion timescale (minimum spacing squared, in FT)
     RUN_PR_FACTOR,     // max(1, 1 / Pr) of Smagorinsky-Lilly, in FT
     RUN_TAU_ADV, RUN_TAU_DIF,  // timescales of the last reduction
+    RUN_LAST_DT,       // clock.last_Δt (QAB2 takes an Euler step when Δt differs from it)
     RUN_NSLOTS
 };
 
@@ -85,9 +86,12 @@ __global__ void k_sim_start(double* run) { run[RUN_TAKEN] = 0.0; }
 // aligned_time_step (run.jl:37-53): Δt = min(simulation.Δt, stop_time - time), and
 // simulation.Δt again when that is not positive; its stage factors go to dtf.  Clears
 // the loop condition first: only the last block of k_sim_callbacks sets it, so an
-// iteration whose callbacks did not run ends the loop instead of repeating it.
+// iteration whose callbacks did not run ends the loop instead of repeating it.  With
+// QAB2 it selects the Euler branch when Δt differs from clock.last_Δt
+// (quasi_adams_bashforth_2.jl:101).
 template <typename FT>
-__global__ void k_sim_begin(double* run, FT* dtf, StageC c, cudaGraphConditionalHandle h, int use_handle) {
+__global__ void k_sim_begin(double* run, FT* dtf, StageC c, cudaGraphConditionalHandle h,
+                            cudaGraphConditionalHandle h_euler, int use_handle, int qab2) {
     if (use_handle) cudaGraphSetConditional(h, 0u);
     const double dt = run[RUN_SIM_DT];
     double a = dt;
@@ -97,6 +101,7 @@ __global__ void k_sim_begin(double* run, FT* dtf, StageC c, cudaGraphConditional
     }
     run[RUN_DT] = a;
     stage_factors<FT>(a, c.c0, c.c1, c.c2, dtf);
+    if (use_handle && qab2) cudaGraphSetConditional(h_euler, a != run[RUN_LAST_DT] ? 1u : 0u);
 }
 
 GBO_D double warp_max(double v) {
@@ -157,7 +162,7 @@ __global__ void __launch_bounds__(256) k_sim_callbacks(SimP<FT> S, int mode, cud
                 if (!g.flatz) a = a + fabs(S.w[t]) * M.rdzf(k);
                 inv = jmax(inv, (double)a);
                 if (S.closure != GBO_CLOSURE_NONE) numax = jmax(numax, (double)S.nu[t]);
-                if (S.closure == GBO_CLOSURE_AMD)
+                if (S.closure == GBO_CLOSURE_AMD || S.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY)
                     for (int q = 0; q < S.ntr; ++q) kapmax = jmax(kapmax, (double)S.kap[q][t]);
             }
             if (nan) bad |= isnan(uu);
@@ -201,12 +206,18 @@ __global__ void __launch_bounds__(256) k_sim_callbacks(SimP<FT> S, int mode, cud
             // with no tracers the reference takes max κₑ = Inf, so Δ²/max κₑ = 0
             const FT kmax = S.ntr > 0 ? FT(a2) : FT(CUDART_INF);
             dif = jmin((double)(d2 / FT(a1)), (double)(d2 / kmax));
+        } else if (S.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
+            // min(Δ²/ν, Δ²/max κ) with max κ = 0 without tracers
+            // (turbulence_closure_diagnostics.jl:41-46)
+            const FT kmax = S.ntr > 0 ? FT(a2) : FT(0);
+            dif = jmin((double)(d2 / FT(a1)), (double)(d2 / kmax));
         }
         W[RUN_TAU_DIF] = dif;
     }
     if (mode == SIM_TIMESCALES) return;
     if (mode == SIM_AFTER_STEP) {
         W[RUN_TIME] = W[RUN_TIME] + W[RUN_DT];  // tick! (the clock is Float64)
+        W[RUN_LAST_DT] = W[RUN_DT];
         W[RUN_ITER] = it_now;
         W[RUN_TAKEN] = W[RUN_TAKEN] + 1.0;
     }

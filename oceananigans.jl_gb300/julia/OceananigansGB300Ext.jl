@@ -68,6 +68,10 @@ struct ModelDesc
     cg_reltol::Float64
     cg_abstol::Float64
     cg_maxiter::Int32
+    closure_nu::Float64
+    closure_kappa::NTuple{4, Float64}
+    timestepper::Int32
+    ab2_chi::Float64
 end
 
 const handles = IdDict{Any, Ptr{Cvoid}}()

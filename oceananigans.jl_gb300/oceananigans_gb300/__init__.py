@@ -6,7 +6,8 @@ is the host-side mirror of the reference's model API.
 from .api import (  # noqa: F401
     Periodic, Bounded, Flat,
     RectilinearGrid, ImmersedBoundaryGrid, GridFittedBottom,
-    WENO, SmagorinskyLilly, AnisotropicMinimumDissipation, BuoyancyTracer, FPlane,
+    WENO, SmagorinskyLilly, AnisotropicMinimumDissipation, ScalarDiffusivity, BuoyancyTracer, FPlane,
+    QuasiAdamsBashforth2TimeStepper,
     FluxBoundaryCondition, FieldBoundaryConditions,
     FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver,
     NonhydrostaticModel, Ensemble, Simulation, set_, time_step_, run_,

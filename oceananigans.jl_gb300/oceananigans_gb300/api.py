@@ -151,6 +151,30 @@ class AnisotropicMinimumDissipation:
         self.C = float(C)
 
 
+class ScalarDiffusivity:
+    """ScalarDiffusivity(; ν=0, κ=0) with constant coefficients, isotropic
+    (ThreeDimensionalFormulation) and explicit (turbulence_closure_implementations/
+    scalar_diffusivity.jl:8-80).  κ is one number for every tracer or a dict by tracer."""
+
+    def __init__(self, nu=0.0, kappa=0.0):
+        self.nu = float(nu)
+        self.kappa = dict(kappa) if isinstance(kappa, dict) else float(kappa)
+
+    def kappa_of(self, tracer):
+        if isinstance(self.kappa, dict):
+            if tracer not in self.kappa:
+                raise ValueError("ScalarDiffusivity κ has no entry for tracer %s" % tracer)
+            return float(self.kappa[tracer])
+        return self.kappa
+
+
+class QuasiAdamsBashforth2TimeStepper:
+    """QuasiAdamsBashforth2TimeStepper(; χ = 0.1) (src/TimeSteppers/quasi_adams_bashforth_2.jl:60-65)."""
+
+    def __init__(self, chi=0.1):
+        self.chi = float(chi)
+
+
 class BuoyancyTracer:
     pass
 
@@ -201,8 +225,12 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
     src/Models/NonhydrostaticModels/NonhydrostaticModels.jl:30-76), and
     ArgumentError-style failures raised as ValueError.
     """
-    if timestepper != "RungeKutta3":
-        raise ValueError("timestepper = :%s is not supported; use :RungeKutta3" % timestepper)
+    if isinstance(timestepper, QuasiAdamsBashforth2TimeStepper):
+        ab2_chi, timestepper = timestepper.chi, "QuasiAdamsBashforth2"
+    else:
+        ab2_chi = 0.1
+    if timestepper not in ("RungeKutta3", "QuasiAdamsBashforth2"):
+        raise ValueError("timestepper = :%s is not supported; use :RungeKutta3 or :QuasiAdamsBashforth2" % timestepper)
     advection = advection if advection is not None else WENO()
     if not isinstance(advection, WENO):
         raise ValueError("advection must be WENO(order=5)")
@@ -222,6 +250,11 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
     elif isinstance(closure, AnisotropicMinimumDissipation):
         d.closure = L.GBO_CLOSURE_AMD
         d.closure_C = closure.C
+    elif isinstance(closure, ScalarDiffusivity):
+        d.closure = L.GBO_CLOSURE_SCALAR_DIFFUSIVITY
+        d.closure_nu = closure.nu
+        for n, name in enumerate(tracers):
+            d.closure_kappa[n] = closure.kappa_of(name)
     elif closure is not None:
         raise ValueError("unsupported closure %r" % (closure,))
     d.ntracers = len(tracers)
@@ -249,6 +282,8 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
             pressure_solver = FFTBasedPoissonSolver()
         else:
             pressure_solver = FourierTridiagonalPoissonSolver()
+    d.timestepper = L.GBO_TIMESTEPPER_QAB2 if timestepper == "QuasiAdamsBashforth2" else L.GBO_TIMESTEPPER_RK3
+    d.ab2_chi = ab2_chi
     d.pressure_solver = pressure_solver.kind
     if isinstance(pressure_solver, ConjugateGradientPoissonSolver):
         d.preconditioner = pressure_solver.preconditioner

@@ -184,6 +184,7 @@ struct Model {
     std::vector<Field> Gn, Gm;                      // tendencies (u,v,w,tracers...)
     double time = 0;
     int64_t iteration = 0;
+    double last_dt = INFINITY;                      // clock.last_Δt (QAB2 Euler steps)
     bool has_phy = false;
     std::string err;
     // FT solver persistent storage (the reference keeps solver.storage between solves)
@@ -663,15 +664,15 @@ struct Ctx {
 
     // diffusive tracer fluxes; κ at faces = ℑ(κ_ccc) (/Pr for Smagorinsky)
     double kap_x(int n, int i, int j, int k) const {
-        if (m.desc.closure == GBO_CLOSURE_AMD) { const Field& K = m.kappa[n]; return 0.5 * (K(i - 1, j, k) + K(i, j, k)); }
+        if (kappa_field()) { const Field& K = m.kappa[n]; return 0.5 * (K(i - 1, j, k) + K(i, j, k)); }
         return 0.5 * (m.nu(i - 1, j, k) + m.nu(i, j, k)) / m.desc.closure_Pr;
     }
     double kap_y(int n, int i, int j, int k) const {
-        if (m.desc.closure == GBO_CLOSURE_AMD) { const Field& K = m.kappa[n]; return 0.5 * (K(i, j - 1, k) + K(i, j, k)); }
+        if (kappa_field()) { const Field& K = m.kappa[n]; return 0.5 * (K(i, j - 1, k) + K(i, j, k)); }
         return 0.5 * (m.nu(i, j - 1, k) + m.nu(i, j, k)) / m.desc.closure_Pr;
     }
     double kap_z(int n, int i, int j, int k) const {
-        if (m.desc.closure == GBO_CLOSURE_AMD) { const Field& K = m.kappa[n]; return 0.5 * (K(i, j, k - 1) + K(i, j, k)); }
+        if (kappa_field()) { const Field& K = m.kappa[n]; return 0.5 * (K(i, j, k - 1) + K(i, j, k)); }
         return 0.5 * (m.nu(i, j, k - 1) + m.nu(i, j, k)) / m.desc.closure_Pr;
     }
     // conditional tracer gradients and zero flux on the immersed periphery of the flux
@@ -690,6 +691,8 @@ struct Ctx {
     double q_z(int n, const Field& cc, int i, int j, int k) const { return zp(i, j, k, false, false, true) ? 0.0 : -kap_z(n, i, j, k) * dcz(cc, i, j, k); }
 
     bool closure_on() const { return m.desc.closure != GBO_CLOSURE_NONE; }
+    // AMD and ScalarDiffusivity carry per-tracer diffusivity fields
+    bool kappa_field() const { return m.desc.closure == GBO_CLOSURE_AMD || m.desc.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY; }
 
     // --- immersed flux masking (immersed_advective_fluxes.jl:19-70; immersed_diffusive_fluxes.jl)
     // fluxes through faces on the immersed periphery are zero.
@@ -1114,6 +1117,13 @@ void ft_poisson(Model& m, std::vector<double>& phi, const std::vector<double>& b
 // ---------------------------------------------------------------------------
 void compute_closure(Model& m) {
     if (m.desc.closure == GBO_CLOSURE_NONE) return;
+    if (m.desc.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
+        // ScalarDiffusivity(ν, κ): numbers, the same at every point and halo point
+        // (scalar_diffusivity.jl:8-12; νᶜᶜᶜ(i, j, k, grid, closure::ScalarDiffusivity, ...) = ν)
+        std::fill(m.nu.d.begin(), m.nu.d.end(), m.desc.closure_nu);
+        for (int n = 0; n < m.ntr; ++n) std::fill(m.kappa[n].d.begin(), m.kappa[n].d.end(), m.desc.closure_kappa[n]);
+        return;
+    }
     Ctx C(m);
     const Grid& g = m.g;
 #pragma omp parallel for collapse(2)
@@ -1287,7 +1297,46 @@ int rk3_substep(Model& m, double dt, double gamma, double zeta, bool first) {
     return pressure_correction(m, dtau);
 }
 
+// One QuasiAdamsBashforth2 step (quasi_adams_bashforth_2.jl:100-121, :134-147;
+// nonhydrostatic_ab2_step.jl:29-58): U += Δt (α Gⁿ - β G⁻ not_euler) with α = 3/2 + χ,
+// β = 1/2 + χ and χ = -1/2 for an Euler step, taken whenever Δt differs from
+// clock.last_Δt; the projection uses Δτ = Δt; then G⁻ = Gⁿ, tick!, update_state!.
+int time_step_ab2(Model& m, double dt) {
+    const bool euler = dt != m.last_dt;
+    if (m.iteration == 0) {  // maybe_prepare_first_time_step! (TimeSteppers.jl:41-48)
+        m.last_dt = dt;
+        update_state(m);
+    }
+    const double chi = euler ? -0.5 : m.desc.ab2_chi;
+    const double alpha = 1.5 + chi, beta = 0.5 + chi;
+    const Grid& g = m.g;
+    flux_bc_tendencies(m);
+    for (int n = 0; n < m.nfields(); ++n) {
+        Field& U = m.fld(n);
+        Field& G = m.Gn[n];
+        Field& Gm = m.Gm[n];
+        int k0 = 1;
+        if (n == 2 && !g.flatz) k0 = 2;  // w excludes the Bounded periphery
+        if (n == 2 && g.flatz) continue;
+#pragma omp parallel for collapse(2)
+        for (int k = k0; k <= g.Nz; ++k)
+            for (int j = 1; j <= g.Ny; ++j)
+                for (int i = 1; i <= g.Nx; ++i) {
+                    double Gu = alpha * G(i, j, k) - (euler ? 0.0 : beta * Gm(i, j, k));
+                    U.at(i, j, k) += dt * Gu;
+                }
+    }
+    int rc = pressure_correction(m, dt);
+    for (int n = 0; n < m.nfields(); ++n) m.Gm[n].d = m.Gn[n].d;
+    m.time += dt;
+    m.iteration += 1;
+    m.last_dt = dt;
+    update_state(m);
+    return rc;
+}
+
 int time_step(Model& m, double dt) {
+    if (m.desc.timestepper == GBO_TIMESTEPPER_QAB2) return time_step_ab2(m, dt);
     const double g1 = 8.0 / 15, g2 = 5.0 / 12, g3 = 3.0 / 4, z2 = -17.0 / 60, z3 = -5.0 / 12;
     if (m.iteration == 0) update_state(m);
     double tnext = m.time + dt;
@@ -1529,7 +1578,7 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
     m->nu.init(g.Nx, g.Ny, g.Nz, H, Hz);
     m->c.resize(m->ntr);
     for (auto& f : m->c) f.init(g.Nx, g.Ny, g.Nz, H, Hz);
-    if (md->closure == GBO_CLOSURE_AMD) {
+    if (md->closure == GBO_CLOSURE_AMD || md->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
         m->kappa.resize(m->ntr);
         for (auto& f : m->kappa) f.init(g.Nx, g.Ny, g.Nz, H, Hz);
     }

@@ -39,7 +39,9 @@ class ModelDesc(ctypes.Structure):
                 ("tracer_flux_top", ctypes.c_double * MAX_TRACERS),
                 ("tracer_flux_bottom", ctypes.c_double * MAX_TRACERS),
                 ("pressure_solver", ctypes.c_int32), ("preconditioner", ctypes.c_int32),
-                ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32)]
+                ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32),
+                ("closure_nu", ctypes.c_double), ("closure_kappa", ctypes.c_double * MAX_TRACERS),
+                ("timestepper", ctypes.c_int32), ("ab2_chi", ctypes.c_double)]
 
 
 def build(force=False):

@@ -60,8 +60,14 @@ def turbulence_2d(N=64, float_type=np.float64, seed=0):
     return Case(grid, init, advection=og.WENO())
 
 
+def _closure(name):
+    return {None: None, "smagorinsky": og.SmagorinskyLilly, "amd": og.AnisotropicMinimumDissipation,
+            "scalar": lambda: og.ScalarDiffusivity(nu=0.5, kappa=0.2)}[name]
+
+
 def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0, 256.0),
-                  closure="smagorinsky", stretched=False, N2=1e-5, flux=1e-8, f=1e-4, U0=1e-3):
+                  closure="smagorinsky", stretched=False, N2=1e-5, flux=1e-8, f=1e-4, U0=1e-3,
+                  timestepper="RungeKutta3"):
     """3-D free convection: BuoyancyTracer b = N² z + 1e-8 noise, velocities 1e-3 U[-1,1]."""
     Nx, Ny, Nz = N
     if stretched:
@@ -72,7 +78,8 @@ def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0
         z = (-L[2], 0.0)
     grid = og.RectilinearGrid(size=N, x=(0, L[0]), y=(0, L[1]), z=z, topology=("Periodic", "Periodic", "Bounded"),
                               float_type=float_type)
-    cl = og.SmagorinskyLilly() if closure == "smagorinsky" else (og.AnisotropicMinimumDissipation() if closure == "amd" else None)
+    cl = _closure(closure)
+    cl = cl() if cl else None
     bcs = {"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(flux))}
     rng = np.random.default_rng(seed)
     _, _, zc = grid.nodes()
@@ -82,11 +89,25 @@ def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0
             "w": U0 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
             "b": b}
     return Case(grid, init, advection=og.WENO(), closure=cl, buoyancy=og.BuoyancyTracer(),
-                coriolis=og.FPlane(f) if f else None, tracers=("b",), boundary_conditions=bcs)
+                coriolis=og.FPlane(f) if f else None, tracers=("b",), boundary_conditions=bcs,
+                timestepper=timestepper)
+
+
+def diffusion_cosine(fieldname, timestepper="RungeKutta3", N=128, m=2):
+    """test_dynamics.jl:63-85 on a Periodic x, y grid: one of u, v, c = cos(m z) on
+    z in (0, π/2), ScalarDiffusivity(ν=1, κ=1), no buoyancy, everything else zero."""
+    grid = og.RectilinearGrid(size=(8, 8, N), x=(0, 1), y=(0, 1), z=(0, np.pi / 2),
+                              topology=("Periodic", "Periodic", "Bounded"))
+    _, _, zc = grid.nodes()
+    init = {name: np.zeros((8, 8, N)) for name in ("u", "v", "c")}
+    init[fieldname] = np.broadcast_to(np.cos(m * zc)[None, None, :], (8, 8, N)).copy()
+    return Case(grid, init, advection=og.WENO(), closure=og.ScalarDiffusivity(nu=1.0, kappa=1.0), tracers=("c",),
+                timestepper=timestepper)
 
 
 def seamount(N=(32, 32, 16), float_type=np.float64, seed=0, solver="cg", reltol=0.0, abstol=0.0,
-             height=1200.0, width=800.0, N2=1e-6, U=0.1, noise=1e-3, stretched=False, closure=None):
+             height=1200.0, width=800.0, N2=1e-6, U=0.1, noise=1e-3, stretched=False, closure=None,
+             timestepper="RungeKutta3"):
     """Seamount on an ImmersedBoundaryGrid(GridFittedBottom): x, y in [-5, 5] km, z in [-2, 0] km,
     h = -2000 + height exp(-(x² + y²) / (2 width²)), b = N² z, u = U + noise, v, w = noise."""
     Nx, Ny, Nz = N
@@ -113,9 +134,9 @@ def seamount(N=(32, 32, 16), float_type=np.float64, seed=0, solver="cg", reltol=
             "v": noise * rng.uniform(-1, 1, (Nx, Ny, Nz)),
             "w": noise * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
             "b": N2 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz))}
-    cl = {None: None, "smagorinsky": og.SmagorinskyLilly, "amd": og.AnisotropicMinimumDissipation}[closure]
+    cl = _closure(closure)
     return Case(grid, init, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
-                pressure_solver=ps, closure=cl() if cl else None)
+                pressure_solver=ps, closure=cl() if cl else None, timestepper=timestepper)
 
 
 def immersed_mask(grid):

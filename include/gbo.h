@@ -234,6 +234,26 @@ int gbo_cell_diffusion_timescale(gbo_model* m, double* out);
  * (src/Solvers/conjugate_gradient_poisson_solver.jl; the rhs there is V·div). */
 int gbo_poisson_solve_device(gbo_model* m, void* phi_device, const void* rhs_device);
 
+/* ---- learned preconditioner correction ---------------------------------------
+ * No counterpart in the reference (its CG preconditioners are FFT-based, diagonal or
+ * none).  For a model with the ConjugateGradientPoissonSolver and its FFT
+ * preconditioner, gbo_learned_preconditioner loads a 3-D U-Net (four levels, 16, 32,
+ * 48, 64 channels, 3³ kernels; BF16 on the tensor cores, FP32 accumulation) whose
+ * output corrects the FFT preconditioner: z = z_fft + s_z net(r/s_r, z_fft/s_z,
+ * active), s_r = RMS(r), s_z = RMS(z_fft).  The CG becomes the flexible (Polak-Ribière)
+ * variant.  `weights` holds
+ * gbo_learned_weight_count() FP32 values, per layer [cout][cin][3][3][3] then bias, in
+ * the order enc0 (3→16), enc1 (16→32), enc2 (32→48), enc3 (48→64), dec3 (64→48),
+ * dec2 (48→32), dec1 (32→16), out (16→1); NULL restores the plain FFT preconditioner.
+ * Nx, Ny and Nz must be divisible by 8. */
+int64_t gbo_learned_weight_count(void);
+int gbo_learned_preconditioner(gbo_model* m, const float* weights, int64_t count);
+/* out = V∇²x, the CG operator with the conditional differences of the immersed grid
+ * (conjugate_gradient_poisson_solver.jl:111-137); device buffers of the model's float type. */
+int gbo_poisson_operator_device(gbo_model* m, const void* x_device, void* out_device);
+/* z = M r with the model's CG preconditioner (including a loaded learned correction). */
+int gbo_precondition_device(gbo_model* m, const void* r_device, void* z_device);
+
 /* ---- ensembles ---------------------------------------------------------------
  * No counterpart in the reference, which advances models one at a time.  An
  * ensemble owns n independent models (each created as by gbo_model_create from

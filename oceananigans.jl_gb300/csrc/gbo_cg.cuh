@@ -30,6 +30,7 @@ enum {
     CG_BETA,               // ρ/ρ_prev of this iteration (0 on the first)
     CG_ALPHA,              // ρ/(p·q)
     CG_MX, CG_MR,          // active-cell means of x and r
+    CG_ZRP,                // z·r_prev (flexible CG)
     CG_NSLOTS
 };
 // block-completion counters of the loop kernels (last block finalises the scalars)
@@ -173,19 +174,26 @@ GBO_D double ldcg(const double* p) { return __ldcg(p); }
 // instead of repeating it.
 template <typename FT>
 __global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, size_t n, double* s, unsigned int* cnt,
-                         cudaGraphConditionalHandle h, int use_handle) {
+                         cudaGraphConditionalHandle h, int use_handle, const FT* __restrict__ rprev = nullptr) {
     const int par = cg_parity(s);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         s[CG_CONT] = 0.0;
         if (use_handle) cudaGraphSetConditional(h, 0u);
     }
-    FT acc = FT(0);  // per-thread partial sums in FT (a few terms), FP64 across threads
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    FT acc = FT(0), acc2 = FT(0);  // per-thread partial sums in FT (a few terms), FP64 across threads
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         acc += a[t] * b[t];
-    block_add((double)acc, s + CG_RHO0 + par);
+        if (rprev) acc2 += a[t] * rprev[t];
+    }
+    if (rprev) block_add((double)acc, s + CG_RHO0 + par, (double)acc2, s + CG_ZRP);
+    else block_add((double)acc, s + CG_RHO0 + par);
     if (last_block(cnt + CC_DOT) && threadIdx.x == 0) {
         const bool first = s[CG_IT] == 0.0;
-        s[CG_BETA] = first ? 0.0 : ldcg(s + CG_RHO0 + par) / ldcg(s + CG_RHO0 + (par ^ 1));
+        const double rho = ldcg(s + CG_RHO0 + par), prev = ldcg(s + CG_RHO0 + (par ^ 1));
+        // flexible (Polak-Ribière) CG for a preconditioner that varies: β = z·(r - r_prev) / ρ_prev
+        const double num = rprev ? rho - ldcg(s + CG_ZRP) : rho;
+        s[CG_BETA] = first ? 0.0 : num / prev;
+        s[CG_ZRP] = 0.0;
     }
 }
 
@@ -274,7 +282,8 @@ __global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __rest
 // sets their means
 template <typename FT>
 __global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, const FT* __restrict__ p0,
-                               const FT* __restrict__ p1, const FT* __restrict__ q, double* s, unsigned int* cnt) {
+                               const FT* __restrict__ p1, const FT* __restrict__ q, double* s, unsigned int* cnt,
+                               FT* __restrict__ rprev = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i < g.Nx && j < g.Ny;
@@ -286,7 +295,9 @@ __global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__
         for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
             const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
             const FT xv = x[idx] + alpha * p[idx];
-            const FT rv = r[idx] - alpha * q[idx];
+            const FT rold = r[idx];
+            const FT rv = rold - alpha * q[idx];
+            if (rprev) rprev[idx] = rold;
             x[idx] = xv;
             r[idx] = rv;
             if (k >= kb) { ax += xv; ar += rv; }
@@ -333,7 +344,8 @@ __global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, 
         const double it = s[CG_IT] + 1.0;
         const double norm = sqrt(ldcg(s + CG_NORM2));
         const bool cont = it < maxiter && norm > s[CG_TOL];
-        if (!cont && norm > s[CG_TOL]) s[CG_FAIL] = 1.0;
+        // stopped above tolerance, or on a NaN residual (which no comparison passes)
+        if (!cont && !(norm <= s[CG_TOL])) s[CG_FAIL] = 1.0;
         s[CG_IT] = it;
         s[CG_NORM] = norm;
         s[CG_ITERS] += 1.0;

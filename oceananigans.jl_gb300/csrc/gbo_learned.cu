@@ -1,0 +1,364 @@
+// gbo_learned.cu -- kernels and host side of the learned preconditioner correction
+// (see gbo_learned.cuh for the network, the layouts and the boundary rules).
+#include <cmath>
+#include <vector>
+
+#include "gbo_learned.cuh"
+
+namespace learned {
+
+using bf16 = __nv_bfloat16;
+
+struct ConvP {
+    const bf16* in;      // [n][cin]
+    const bf16* w;       // [cout][kpad(cin)]
+    const float* bias;   // [cout]
+    bf16* out;           // mode 0: [n][cout]
+    void* z;             // mode 1: FT field, z += s (acc + bias) for output channel 0
+    const float* scale;  // mode 1: s (the RMS of the incoming z)
+    Dims d;
+};
+
+GBO_D void cp16(void* smem, const void* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0));
+}
+GBO_D void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+GBO_D void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+GBO_D uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// D = A B + D for one 16 × 8 × 16 tile: A row-major 16 × 16, B column-major 16 × 8
+// (BF16), D FP32.  Fragments (g = lane / 4, t = lane % 4): a0 = A[g][2t..], a1 =
+// A[g+8][2t..], a2 = A[g][2t+8..], a3 = A[g+8][2t+8..]; b0 = B[2t..][g], b1 = B[2t+8..][g];
+// d0, d1 = D[g][2t, 2t+1], d2, d3 = D[g+8][2t, 2t+1].
+GBO_D void mma16816(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+GBO_D uint32_t pack2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (lower address)
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// 3³ convolution as an implicit GEMM (see the file header of gbo_learned.cuh).
+// MODE 0: out = bf16(relu(acc + bias)); MODE 1: z += s (acc₀ + bias₀) in FT.
+template <int CIN, int COUT, int MODE, typename FT>
+__global__ void __launch_bounds__(128) k_conv(ConvP p) {
+    static_assert(CIN % 8 == 0 && COUT % 8 == 0 && COUT <= 64, "channel counts");
+    constexpr int K = 27 * CIN, KP = kpad(CIN), KC = KP / 16, NT = COUT / 8;
+    __shared__ __align__(16) bf16 As[2][MT * AS];
+    __shared__ __align__(16) bf16 Bs[2][COUT * AS];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+    const int64_t n = p.d.n();
+    const int64_t m0 = (int64_t)blockIdx.x * MT;
+    // the im2col row (cell) this thread stages and its 8-wide half of each k chunk
+    const int row = tid >> 1, half = tid & 1;
+    const int64_t cell = m0 + row;
+    const bool cell_ok = cell < n;
+    const int ci = cell_ok ? (int)(cell % nx) : 0;
+    const int cj = cell_ok ? (int)((cell / nx) % ny) : 0;
+    const int ck = cell_ok ? (int)(cell / ((int64_t)nx * ny)) : 0;
+    auto load_chunk = [&](int kc, int buf) {
+        const int kk = kc * 16 + half * 8;  // one tap, channels c0 .. c0 + 7
+        bool ok = cell_ok && kk < K;
+        int64_t src = 0;
+        if (ok) {
+            const int tap = kk / CIN, c0 = kk % CIN;
+            const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+            const int kz = ck + dz;
+            int ii = ci + dx, jj = cj + dy;
+            ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
+            jj = jj < 0 ? jj + ny : (jj >= ny ? jj - ny : jj);
+            ok = kz >= 0 && kz < nz;
+            src = (ii + (int64_t)nx * (jj + (int64_t)ny * kz)) * CIN + c0;
+        }
+        cp16(&As[buf][row * AS + half * 8], p.in + (ok ? src : 0), ok);
+        if (tid < 2 * COUT) {
+            const int r = tid >> 1, h = tid & 1;
+            cp16(&Bs[buf][r * AS + h * 8], p.w + (int64_t)r * KP + kc * 16 + h * 8, true);
+        }
+    };
+    float acc[NT][4];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    load_chunk(0, 0);
+    cp_commit();
+    for (int kc = 0; kc < KC; ++kc) {
+        if (kc + 1 < KC) load_chunk(kc + 1, (kc + 1) & 1);
+        cp_commit();
+        cp_wait1();
+        __syncthreads();
+        const bf16* A = As[kc & 1] + warp * 16 * AS;
+        const uint32_t a0 = ld32(A + g * AS + 2 * t), a1 = ld32(A + (g + 8) * AS + 2 * t);
+        const uint32_t a2 = ld32(A + g * AS + 2 * t + 8), a3 = ld32(A + (g + 8) * AS + 2 * t + 8);
+        const bf16* B = Bs[kc & 1];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            const uint32_t b0 = ld32(B + (q * 8 + g) * AS + 2 * t), b1 = ld32(B + (q * 8 + g) * AS + 2 * t + 8);
+            mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+        }
+        __syncthreads();
+    }
+    const int64_t r0 = m0 + warp * 16 + g, r1 = r0 + 8;
+    if constexpr (MODE == 0) {
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            const int col = q * 8 + 2 * t;
+            const float b0 = p.bias[col], b1 = p.bias[col + 1];
+            if (r0 < n)
+                *reinterpret_cast<uint32_t*>(p.out + r0 * COUT + col) =
+                    pack2(fmaxf(acc[q][0] + b0, 0.f), fmaxf(acc[q][1] + b1, 0.f));
+            if (r1 < n)
+                *reinterpret_cast<uint32_t*>(p.out + r1 * COUT + col) =
+                    pack2(fmaxf(acc[q][2] + b0, 0.f), fmaxf(acc[q][3] + b1, 0.f));
+        }
+    } else {
+        if (t == 0) {
+            FT* z = static_cast<FT*>(p.z);
+            const float s = *p.scale, b0 = p.bias[0];
+            if (r0 < n) z[r0] += FT(s * (acc[0][0] + b0));
+            if (r1 < n) z[r1] += FT(s * (acc[0][2] + b0));
+        }
+    }
+}
+
+// s = sqrt(mean(r²)) (1 when r = 0): FP64 block sums, the last block finishes
+template <typename FT>
+__global__ void __launch_bounds__(256) k_rms(const FT* __restrict__ r, int64_t n, double* acc, unsigned* cnt, float* scale) {
+    __shared__ double sh[8];
+    __shared__ bool last;
+    double v = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = (double)r[i];
+        v += x * x;
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += sh[w];
+        atomicAdd(acc, b);
+        __threadfence();
+        last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        const double total = __ldcg(acc);
+        const float s = (float)sqrt(total / (double)n);
+        *scale = s > 0.f ? s : 1.f;
+        *acc = 0.0;
+        *cnt = 0u;
+    }
+}
+
+// The first layer's input: (r / s_r, z / s_z, active, 0 …) in BF16, 8 channels per cell
+template <typename FT>
+__global__ void k_features(const FT* __restrict__ r, const FT* __restrict__ z, const int* __restrict__ kbot, Dims d,
+                           const float* scale_r, const float* scale_z, bf16* __restrict__ out) {
+    const int64_t n = d.n(), plane = (int64_t)d.nx * d.ny;
+    const float inv = 1.f / *scale_r, invz = 1.f / *scale_z;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(c / plane);
+        const float active = (kbot && k < kbot[c % plane]) ? 0.f : 1.f;
+        uint4 v;
+        v.x = pack2((float)r[c] * inv, (float)z[c] * invz);
+        v.y = pack2(active, 0.f);
+        v.z = 0u;
+        v.w = 0u;
+        *reinterpret_cast<uint4*>(out + c * FEAT) = v;
+    }
+}
+
+// Average pooling 2 × 2 × 2: one thread per coarse cell and 8 channels
+template <int C>
+__global__ void k_pool(const bf16* __restrict__ in, Dims fine, bf16* __restrict__ out) {
+    const Dims cd{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+    const int64_t total = cd.n() * (C / 8);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e / (C / 8);
+        const int ch = (int)(e % (C / 8)) * 8;
+        const int i = (int)(c % cd.nx), j = (int)((c / cd.nx) % cd.ny), k = (int)(c / ((int64_t)cd.nx * cd.ny));
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int o = 0; o < 8; ++o) {
+            const int64_t f = (2 * i + (o & 1)) + (int64_t)fine.nx * ((2 * j + ((o >> 1) & 1)) + (int64_t)fine.ny * (2 * k + (o >> 2)));
+            const uint4 v = *reinterpret_cast<const uint4*>(in + f * C + ch);
+            const bf16* h = reinterpret_cast<const bf16*>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s[q] += __bfloat162float(h[q]);
+        }
+        uint4 o4;
+        o4.x = pack2(s[0] * 0.125f, s[1] * 0.125f);
+        o4.y = pack2(s[2] * 0.125f, s[3] * 0.125f);
+        o4.z = pack2(s[4] * 0.125f, s[5] * 0.125f);
+        o4.w = pack2(s[6] * 0.125f, s[7] * 0.125f);
+        *reinterpret_cast<uint4*>(out + c * C + ch) = o4;
+    }
+}
+
+// Nearest upsampling of the coarse features plus the fine skip: one thread per fine
+// cell and 8 channels
+template <int C>
+__global__ void k_upadd(const bf16* __restrict__ coarse, const bf16* __restrict__ skip, Dims fine, bf16* __restrict__ out) {
+    const Dims cd{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+    const int64_t total = fine.n() * (C / 8);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = e / (C / 8);
+        const int ch = (int)(e % (C / 8)) * 8;
+        const int i = (int)(f % fine.nx), j = (int)((f / fine.nx) % fine.ny), k = (int)(f / ((int64_t)fine.nx * fine.ny));
+        const int64_t c = (i / 2) + (int64_t)cd.nx * ((j / 2) + (int64_t)cd.ny * (k / 2));
+        const uint4 a = *reinterpret_cast<const uint4*>(coarse + c * C + ch);
+        const uint4 b = *reinterpret_cast<const uint4*>(skip + f * C + ch);
+        const bf16* ha = reinterpret_cast<const bf16*>(&a);
+        const bf16* hb = reinterpret_cast<const bf16*>(&b);
+        float s[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[q] = __bfloat162float(ha[q]) + __bfloat162float(hb[q]);
+        uint4 o4;
+        o4.x = pack2(s[0], s[1]);
+        o4.y = pack2(s[2], s[3]);
+        o4.z = pack2(s[4], s[5]);
+        o4.w = pack2(s[6], s[7]);
+        *reinterpret_cast<uint4*>(out + f * C + ch) = o4;
+    }
+}
+
+}  // namespace learned
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+using learned::bf16;
+using learned::Dims;
+
+struct LearnedNet {
+    Dims d[learned::LEVELS];
+    bf16* w[learned::NLAYERS] = {};
+    float* b[learned::NLAYERS] = {};
+    // activations: features, encoder outputs, pooled inputs, decoder inputs / outputs
+    bf16 *f0 = nullptr, *e0 = nullptr, *d0in = nullptr;
+    bf16 *p1 = nullptr, *e1 = nullptr, *d1in = nullptr, *d1 = nullptr;
+    bf16 *p2 = nullptr, *e2 = nullptr, *d2in = nullptr, *d2 = nullptr;
+    bf16 *p3 = nullptr, *e3 = nullptr, *d3 = nullptr;
+    double* acc = nullptr;
+    unsigned* cnt = nullptr;
+    float* scale = nullptr;  // s_r, s_z
+    std::vector<void*> owned;
+
+    template <typename T>
+    T* dev(size_t count) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, std::max<size_t>(1, count) * sizeof(T));
+        owned.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~LearnedNet() {
+        for (void* p : owned) cudaFree(p);
+    }
+};
+
+LearnedNet* learned_create(int nx, int ny, int nz, const float* weights, int64_t count, std::string* err) {
+    using namespace learned;
+    if (nx % 8 || ny % 8 || nz % 8 || nx < 8 || ny < 8 || nz < 8) {
+        *err = "the learned preconditioner needs Nx, Ny and Nz divisible by 8";
+        return nullptr;
+    }
+    if (!weights || count != file_count()) {
+        *err = "learned preconditioner weights: expected " + std::to_string(file_count()) + " FP32 values";
+        return nullptr;
+    }
+    auto* net = new LearnedNet();
+    for (int l = 0; l < LEVELS; ++l) net->d[l] = Dims{nx >> l, ny >> l, nz >> l};
+    const int64_t n0 = net->d[0].n(), n1 = net->d[1].n(), n2 = net->d[2].n(), n3 = net->d[3].n();
+    bool ok = true;
+    auto need = [&](auto* p) { ok = ok && p != nullptr; return p; };
+    // weights: the file's [cout][cin][kz][ky][kx] then bias, re-laid to [cout][tap·cin + ci]
+    const float* at = weights;
+    for (int l = 0; l < NLAYERS && ok; ++l) {
+        const int cin = LAYER_CIN[l], cout = LAYER_COUT[l], kp = kpad(cin);
+        std::vector<bf16> hw((size_t)cout * kp, __float2bfloat16(0.f));
+        std::vector<float> hb(cout, 0.f);
+        for (int co = 0; co < FILE_COUT[l]; ++co)
+            for (int c = 0; c < FILE_CIN[l]; ++c)
+                for (int tap = 0; tap < 27; ++tap) hw[(size_t)co * kp + tap * cin + c] = __float2bfloat16(*at++);
+        for (int co = 0; co < FILE_COUT[l]; ++co) hb[co] = *at++;
+        net->w[l] = need(net->dev<bf16>(hw.size()));
+        net->b[l] = need(net->dev<float>(hb.size()));
+        if (ok) {
+            cudaMemcpy(net->w[l], hw.data(), hw.size() * sizeof(bf16), cudaMemcpyHostToDevice);
+            cudaMemcpy(net->b[l], hb.data(), hb.size() * sizeof(float), cudaMemcpyHostToDevice);
+        }
+    }
+    net->f0 = need(net->dev<bf16>(n0 * FEAT));
+    net->e0 = need(net->dev<bf16>(n0 * C0));
+    net->d0in = need(net->dev<bf16>(n0 * C0));
+    net->p1 = need(net->dev<bf16>(n1 * C0));
+    net->e1 = need(net->dev<bf16>(n1 * C1));
+    net->d1in = need(net->dev<bf16>(n1 * C1));
+    net->d1 = need(net->dev<bf16>(n1 * C0));
+    net->p2 = need(net->dev<bf16>(n2 * C1));
+    net->e2 = need(net->dev<bf16>(n2 * C2));
+    net->d2in = need(net->dev<bf16>(n2 * C2));
+    net->d2 = need(net->dev<bf16>(n2 * C1));
+    net->p3 = need(net->dev<bf16>(n3 * C2));
+    net->e3 = need(net->dev<bf16>(n3 * C3));
+    net->d3 = need(net->dev<bf16>(n3 * C2));
+    net->acc = need(net->dev<double>(1));
+    net->cnt = need(net->dev<unsigned>(1));
+    net->scale = need(net->dev<float>(2));
+    if (!ok || cudaGetLastError() != cudaSuccess) {
+        *err = "learned preconditioner: device allocation failed";
+        delete net;
+        return nullptr;
+    }
+    return net;
+}
+
+void learned_destroy(LearnedNet* net) { delete net; }
+
+namespace {
+
+template <int CIN, int COUT, int MODE, typename FT>
+void conv(const LearnedNet* net, int layer, int level, const bf16* in, bf16* out, void* z, cudaStream_t st) {
+    learned::ConvP p{in, net->w[layer], net->b[layer], out, z, net->scale + 1, net->d[level]};
+    const int64_t blocks = (net->d[level].n() + learned::MT - 1) / learned::MT;
+    learned::k_conv<CIN, COUT, MODE, FT><<<(unsigned)blocks, 128, 0, st>>>(p);
+}
+
+unsigned grid_for(int64_t work) { return (unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16); }
+
+template <typename FT>
+int apply(LearnedNet* net, const FT* r, FT* z, const int* kbot, cudaStream_t st) {
+    using namespace learned;
+    const Dims* d = net->d;
+    k_rms<FT><<<grid_for(d[0].n()), 256, 0, st>>>(r, d[0].n(), net->acc, net->cnt, net->scale);
+    k_rms<FT><<<grid_for(d[0].n()), 256, 0, st>>>(z, d[0].n(), net->acc, net->cnt, net->scale + 1);
+    k_features<FT><<<grid_for(d[0].n()), 256, 0, st>>>(r, z, kbot, d[0], net->scale, net->scale + 1, net->f0);
+    conv<FEAT, C0, 0, FT>(net, L_ENC0, 0, net->f0, net->e0, nullptr, st);
+    k_pool<C0><<<grid_for(d[1].n() * C0 / 8), 256, 0, st>>>(net->e0, d[0], net->p1);
+    conv<C0, C1, 0, FT>(net, L_ENC1, 1, net->p1, net->e1, nullptr, st);
+    k_pool<C1><<<grid_for(d[2].n() * C1 / 8), 256, 0, st>>>(net->e1, d[1], net->p2);
+    conv<C1, C2, 0, FT>(net, L_ENC2, 2, net->p2, net->e2, nullptr, st);
+    k_pool<C2><<<grid_for(d[3].n() * C2 / 8), 256, 0, st>>>(net->e2, d[2], net->p3);
+    conv<C2, C3, 0, FT>(net, L_ENC3, 3, net->p3, net->e3, nullptr, st);
+    conv<C3, C2, 0, FT>(net, L_DEC3, 3, net->e3, net->d3, nullptr, st);
+    k_upadd<C2><<<grid_for(d[2].n() * C2 / 8), 256, 0, st>>>(net->d3, net->e2, d[2], net->d2in);
+    conv<C2, C1, 0, FT>(net, L_DEC2, 2, net->d2in, net->d2, nullptr, st);
+    k_upadd<C1><<<grid_for(d[1].n() * C1 / 8), 256, 0, st>>>(net->d2, net->e1, d[1], net->d1in);
+    conv<C1, C0, 0, FT>(net, L_DEC1, 1, net->d1in, net->d1, nullptr, st);
+    k_upadd<C0><<<grid_for(d[0].n() * C0 / 8), 256, 0, st>>>(net->d1, net->e0, d[0], net->d0in);
+    conv<C0, 8, 1, FT>(net, L_OUT, 0, net->d0in, nullptr, z, st);
+    return 17;
+}
+
+}  // namespace
+
+int learned_apply(LearnedNet* net, const void* r, void* z, const int* kbot, int fp64, cudaStream_t stream) {
+    if (fp64) return apply<double>(net, static_cast<const double*>(r), static_cast<double*>(z), kbot, stream);
+    return apply<float>(net, static_cast<const float*>(r), static_cast<float*>(z), kbot, stream);
+}

@@ -11,6 +11,7 @@
 #include "gbo_fft.cuh"
 #include "gbo_cg.cuh"
 #include "gbo_sim.cuh"
+#include "gbo_learned.cuh"
 #include "gbo_fused.cuh"
 
 // ===========================================================================
@@ -266,6 +267,11 @@ struct gbo_model {
     virtual int get_state(void* buf, int64_t bytes) = 0;
     virtual int set_state(const void* buf, int64_t bytes) = 0;
     virtual int run(const gbo_run_desc* d, gbo_run_result* out) = 0;
+    virtual int set_learned(const float* weights, int64_t count) = 0;
+    virtual int operator_device(const void* x, void* out) = 0;
+    virtual int precondition_device(const void* r, void* z) = 0;
+    virtual void abort_capture() = 0;
+    bool ensemble_member = false;
     virtual int timescales(double* adv, double* dif) = 0;
     virtual int timed_steps(double dt, int nsteps, double* ms, int nmax) = 0;
     virtual int timing_counts(int64_t* n, int nmax) const = 0;
@@ -282,11 +288,11 @@ struct gbo_model {
 };
 
 enum { G_MOMENTUM = 0, G_TRACER, G_CLOSURE, G_HYDROSTATIC, G_SOURCE, G_DCT_Z, G_FFT_X, G_FFT_Y, G_THOMAS,
-       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, G_CG_DOT, G_CG_DIR, G_CG_XR, G_CG_GAUGE, G_SIM, GROUPS };
+       G_CORRECT, G_COPY, G_NAN, G_MASK, G_CG, G_CG_DOT, G_CG_DIR, G_CG_XR, G_CG_GAUGE, G_SIM, G_LEARNED, GROUPS };
 const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", "k_hydrostatic", "k_source",
                                          "k_dct_z", "k_rfft_x", "k_fft_y", "k_thomas_z", "k_correct", "k_copy",
                                          "k_nan_check", "k_mask", "k_cg", "k_cg_dot", "k_cg_direction",
-                                         "k_cg_update_xr", "k_cg_gauge", "k_simulation"};
+                                         "k_cg_update_xr", "k_cg_gauge", "k_simulation", "k_cg_learned"};
 
 // The fused momentum kernel is compiled per closure kind; these pick the instance.
 template <typename FT, bool TR>
@@ -379,6 +385,8 @@ struct ModelImpl : gbo_model {
     double last_dt = INFINITY;           // clock.last_Δt
     // simulation loop (gbo_run): state slots, block partials, graph of the loop
     DBuf<FT> dtf;                        // stage factors of the current Δt (DTF_*)
+    LearnedNet* net = nullptr;           // learned correction of the CG preconditioner
+    DBuf<FT> cg_rp;                      // previous residual (flexible CG)
     DBuf<double> run_s, run_part;
     DBuf<unsigned int> run_cnt;
     double* h_run = nullptr;
@@ -391,6 +399,8 @@ struct ModelImpl : gbo_model {
         if (graph) cudaGraphExecDestroy(graph);
         if (graph_euler) cudaGraphExecDestroy(graph_euler);
         if (run_graph) cudaGraphExecDestroy(run_graph);
+        if (net) learned_destroy(net);
+        cg_rp.free_();
         dtf.free_();
         run_s.free_();
         run_part.free_();
@@ -724,20 +734,80 @@ struct ModelImpl : gbo_model {
         if (pc) {
             poisson_solve(precond_solver);
             z = rb.p;
+            learned_correction(cg_r.p, rb.p);
         }
+        FT* rprev = net ? cg_rp.p : nullptr;
         pre(G_CG_DOT);
-        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s, cg_cnt.p, h, use_handle);
+        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s, cg_cnt.p, h, use_handle, rprev);
         check_launch();
         pre(G_CG_DIR);
         k_cg_direction<FT><<<cg_grid(), blk(), 0, stream>>>(gp, z, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p);
         check_launch();
         pre(G_CG_XR);
-        k_cg_update_xr<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p);
+        k_cg_update_xr<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p, rprev);
         check_launch();
         pre(G_CG_GAUGE);
         k_cg_gauge<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_r.p, pc ? rb.p : nullptr, s, dzs, cg_cnt.p,
                                                          maxiter, h, use_handle);
         check_launch();
+    }
+
+    // z += s · net(r / s, z / s, active) when a learned correction is loaded
+    void learned_correction(const FT* r, FT* z) {
+        if (!net) return;
+        pre(G_LEARNED);
+        const int nk = learned_apply(net, r, z, gp.kbot, sizeof(FT) == 8, stream);
+        check_launch();
+        launches += nk - 1;
+    }
+
+    void drop_graphs() {
+        if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
+        if (graph_euler) { GBO_CUDA(cudaGraphExecDestroy(graph_euler)); graph_euler = nullptr; }
+        if (run_graph) { GBO_CUDA(cudaGraphExecDestroy(run_graph)); run_graph = nullptr; }
+    }
+
+    int set_learned(const float* weights, int64_t count) override {
+        if (!cg || desc.preconditioner != GBO_PRECOND_FFT) {
+            err = "the learned correction needs the ConjugateGradientPoissonSolver with its FFT preconditioner";
+            return GBO_ERR_INVALID;
+        }
+        if (ensemble_member) { err = "the preconditioner of an ensemble member cannot change"; return GBO_ERR_INVALID; }
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        drop_graphs();  // the captured CG loops change
+        if (net) { learned_destroy(net); net = nullptr; }
+        if (!weights) return GBO_OK;
+        std::string why;
+        net = learned_create(Nx, Ny, Nz, weights, count, &why);
+        if (!net) { err = why; return GBO_ERR_INVALID; }
+        if (!cg_rp.p) cg_rp.alloc(N);
+        return GBO_OK;
+    }
+
+    // V∇²x with the conditional differences of the CG operator (out must not alias x)
+    int operator_device(const void* x, void* out) override {
+        if (!ibg && !cg) { err = "the CG operator needs an immersed grid or the CG solver"; return GBO_ERR_INVALID; }
+        pre(G_CG);
+        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, static_cast<const FT*>(x), static_cast<FT*>(out), nullptr);
+        check_launch();
+        return sync();
+    }
+
+    // z = M r with the CG preconditioner (FFT solve of V⁻¹r on the underlying grid plus the
+    // learned correction when loaded)
+    int precondition_device(const void* r, void* z) override {
+        if (!cg || desc.preconditioner != GBO_PRECOND_FFT) { err = "the model has no CG preconditioner"; return GBO_ERR_INVALID; }
+        const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
+        GBO_CUDA(cudaMemcpyAsync(cg_r.p, r, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+        pre(G_CG);
+        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, cg_s.p, dzs);
+        check_launch();
+        poisson_solve(precond_solver);
+        learned_correction(cg_r.p, rb.p);
+        GBO_CUDA(cudaMemcpyAsync(z, rb.p, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
+        // k_cg_vinv accumulated ‖V⁻¹r‖² into the solver's scalars: clear it for the next solve
+        GBO_CUDA(cudaMemsetAsync(cg_s.p + CG_NORM2, 0, sizeof(double), stream));
+        return sync();
     }
 
     void read_cg_scalars() {
@@ -972,12 +1042,33 @@ struct ModelImpl : gbo_model {
     // QAB2 projects with Δτ = FT(Δt) (kernel_Δt, nonhydrostatic_ab2_step.jl:30,56-57)
     StageC stage_c() const { return qab2 ? StageC{1.0, 1.0, 1.0} : rk3_stage_c(); }
 
+    // After a failure inside a capture: end every capture this model's streams are in,
+    // so that the thread's later CUDA calls (allocations included) are not refused
+    void abort_capture() override {
+        for (cudaStream_t s : {stream, body_stream, run_stream, if_stream}) {
+            if (!s) continue;
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(s, &g);
+                if (g) cudaGraphDestroy(g);
+            }
+        }
+        cudaGetLastError();
+    }
+
     cudaGraphExec_t capture_graph(bool euler) {
         cudaGraph_t gph;
         cudaGraphExec_t exec = nullptr;
         GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         int64_t before = launches;
-        full_step(dtf.p, euler);
+        try {
+            full_step(dtf.p, euler);
+        } catch (...) {
+            launches = before;
+            abort_capture();
+            throw;
+        }
         graph_launches_per_step = launches - before;
         launches = before;
         GBO_CUDA(cudaStreamEndCapture(stream, &gph));
@@ -1344,6 +1435,7 @@ struct ModelImpl : gbo_model {
         const cudaGraphConditionalHandle h = new_handle(1, cudaGraphCondAssignDefault);
         const int64_t before = launches;
         int64_t branch = 0;  // kernels of the branch not taken (QAB2)
+        try {
         capture_conditional(h, cudaGraphCondTypeWhile, 1, run_stream, [&](unsigned) {
             const cudaGraphConditionalHandle he = qab2 ? new_handle(0, 0) : 0;
             pre(G_SIM);
@@ -1362,6 +1454,11 @@ struct ModelImpl : gbo_model {
             k_sim_callbacks<FT><<<SIM_BLOCKS, 256, 0, stream>>>(S, SIM_AFTER_STEP, h, 1);
             check_launch();
         });
+        } catch (...) {
+            launches = before;
+            abort_capture();
+            throw;
+        }
         run_iter_launches = launches - before - branch;
         launches = before;
         GBO_CUDA(cudaStreamEndCapture(stream, &gph));
@@ -1728,12 +1825,20 @@ struct gbo_ensemble {
         cudaGraph_t g;
         GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         GBO_CUDA(cudaEventRecord(fork, stream));
-        for (size_t i = 0; i < members.size(); ++i) {
-            cudaStream_t ms = static_cast<cudaStream_t>(members[i]->stream_ptr());
-            GBO_CUDA(cudaStreamWaitEvent(ms, fork, 0));
-            per_step[i] = members[i]->capture_step(d_f32, d_f64);
-            GBO_CUDA(cudaEventRecord(joins[i], ms));
-            GBO_CUDA(cudaStreamWaitEvent(stream, joins[i], 0));
+        try {
+            for (size_t i = 0; i < members.size(); ++i) {
+                cudaStream_t ms = static_cast<cudaStream_t>(members[i]->stream_ptr());
+                GBO_CUDA(cudaStreamWaitEvent(ms, fork, 0));
+                per_step[i] = members[i]->capture_step(d_f32, d_f64);
+                GBO_CUDA(cudaEventRecord(joins[i], ms));
+                GBO_CUDA(cudaStreamWaitEvent(stream, joins[i], 0));
+            }
+        } catch (...) {
+            cudaGraph_t partial = nullptr;
+            cudaStreamEndCapture(stream, &partial);
+            if (partial) cudaGraphDestroy(partial);
+            for (gbo_model* mm : members) mm->abort_capture();
+            throw;
         }
         GBO_CUDA(cudaStreamEndCapture(stream, &g));
         GBO_CUDA(cudaGraphInstantiate(&graph, g, 0));
@@ -1799,6 +1904,7 @@ int gbo_ensemble_create(int32_t n, const gbo_grid_desc* grids, const gbo_model_d
             delete e;
             return rc;
         }
+        mm->ensemble_member = true;
         e->members.push_back(mm);
     }
     int rc = eguarded(e, [&]() {
@@ -1888,6 +1994,23 @@ const char* gbo_kernel_group_name(int32_t g) { return (g >= 0 && g < GROUPS) ? G
 int gbo_poisson_solve_device(gbo_model* m, void* phi, const void* rhs) {
     if (!m || !phi || !rhs) return GBO_ERR_INVALID;
     return guarded(m, [&]() { return m->poisson_device(phi, rhs); });
+}
+
+int64_t gbo_learned_weight_count(void) { return learned::file_count(); }
+
+int gbo_learned_preconditioner(gbo_model* m, const float* weights, int64_t count) {
+    if (!m) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->set_learned(weights, count); });
+}
+
+int gbo_poisson_operator_device(gbo_model* m, const void* x, void* out) {
+    if (!m || !x || !out || x == out) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->operator_device(x, out); });
+}
+
+int gbo_precondition_device(gbo_model* m, const void* r, void* z) {
+    if (!m || !r || !z) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->precondition_device(r, z); });
 }
 
 }  // extern "C"

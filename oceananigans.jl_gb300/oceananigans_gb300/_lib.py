@@ -104,6 +104,10 @@ SIGNATURES = {
     "gbo_last_error": (ctypes.c_char_p, [_vp]),
     "gbo_version": (ctypes.c_char_p, []),
     "gbo_poisson_solve_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "gbo_learned_weight_count": (ctypes.c_int64, []),
+    "gbo_learned_preconditioner": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int64]),
+    "gbo_poisson_operator_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "gbo_precondition_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "gbo_state_bytes": (ctypes.c_int64, [_vp]),
     "gbo_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "gbo_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),

@@ -396,6 +396,28 @@ class NonhydrostaticModel:
     def poisson_solve_device(self, phi_ptr, rhs_ptr):
         L.check(L.load().gbo_poisson_solve_device(self._h, ctypes.c_void_p(phi_ptr), ctypes.c_void_p(rhs_ptr)), self._h)
 
+    def set_learned_preconditioner(self, weights):
+        """Load the learned correction of the CG's FFT preconditioner (an FP32 array of
+        gbo_learned_weight_count() values, or a path to one saved with numpy.save);
+        None restores the plain FFT preconditioner.  No reference counterpart."""
+        lib = L.load()
+        if weights is None:
+            L.check(lib.gbo_learned_preconditioner(self._h, None, 0), self._h)
+            return
+        if isinstance(weights, str):
+            weights = np.load(weights)
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        L.check(lib.gbo_learned_preconditioner(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), w.size),
+                self._h)
+
+    def poisson_operator_device(self, x_ptr, out_ptr):
+        """out = V∇²x (the CG operator) on device buffers of the model's float type."""
+        L.check(L.load().gbo_poisson_operator_device(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(out_ptr)), self._h)
+
+    def precondition_device(self, r_ptr, z_ptr):
+        """z = M r with the model's CG preconditioner, on device buffers."""
+        L.check(L.load().gbo_precondition_device(self._h, ctypes.c_void_p(r_ptr), ctypes.c_void_p(z_ptr)), self._h)
+
     def prognostic_state(self):
         """prognostic_state(model): the restart state as a numpy byte array."""
         lib = L.load()

@@ -1,0 +1,101 @@
+"""Train and evaluate the learned correction of the CG preconditioner on the seamount
+workload (256×256×128 ImmersedBoundaryGrid(GridFittedBottom), WENO5, BuoyancyTracer,
+ConjugateGradientPoissonSolver(reltol=1e-8) in FP32):
+
+    python -m oceananigans_gb300.train_preconditioner --out weights.npy
+
+1. spin-up with the FFT-preconditioned CG, recording a pair (b = V∇²x, x = pNHS) per
+   step (exact pairs of the model's own operator) and the residuals of a few
+   FFT-preconditioned CG iterations on each b with their errors (learned.collect_pairs);
+2. fit the U-Net (learned.train, PyTorch) and save the weight file (numpy .npy, FP32);
+3. held-out comparison: the right-hand sides of later steps solved from a zero initial
+   guess with FFT-PCG and with the learned flexible PCG, timed with CUDA events on the
+   model's stream.  Prints one JSON line.
+"""
+import argparse
+import ctypes
+import json
+import time
+
+import numpy as np
+
+
+def seamount(size, float_type=np.float32, seed=2024):
+    import oceananigans_gb300 as og
+    Nx, Ny, Nz = size
+    under = og.RectilinearGrid(size=size, x=(-5000.0, 5000.0), y=(-5000.0, 5000.0), z=(-2000.0, 0.0),
+                               topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    grid = og.ImmersedBoundaryGrid(under, og.GridFittedBottom(
+        lambda x, y: -2000.0 + 1200.0 * np.exp(-(x * x + y * y) / (2 * 800.0 ** 2))))
+    model = og.NonhydrostaticModel(grid, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
+                                   pressure_solver=og.ConjugateGradientPoissonSolver(reltol=1e-8, abstol=1e-30))
+    rng = np.random.default_rng(seed)
+    _, _, zc = under.nodes()
+    og.set_(model, u=0.1 + 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)), v=1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            w=1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
+            b=1e-6 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz)))
+    return model
+
+
+def timed_solves(model, rhs, torch):
+    """Solve every right-hand side from zero: mean ms, mean iterations, failures."""
+    from . import _lib as L
+    lib = L.load()
+    st = ctypes.c_void_p()
+    L.check(lib.gbo_model_stream(model._h, ctypes.byref(st)), model._h)
+    stream = torch.cuda.ExternalStream(st.value)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phi = torch.zeros_like(rhs[0])
+    ms, its, failed = [], [], 0
+    for r in rhs:
+        phi.zero_()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        try:
+            model.poisson_solve_device(phi.data_ptr(), r.data_ptr())
+        except L.NotConvergedError:
+            failed += 1
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        its.append(model.solver_iterations)
+    return {"ms_mean": float(np.mean(ms)), "iterations_mean": float(np.mean(its)), "not_converged": failed}
+
+
+def main(argv=None):
+    import torch
+    from . import learned
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--size", type=int, nargs=3, default=(256, 256, 128))
+    ap.add_argument("--dt", type=float, default=20.0)
+    ap.add_argument("--pairs", type=int, default=60)
+    ap.add_argument("--heldout", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--cg-iterations", type=int, default=4)
+    args = ap.parse_args(argv)
+    log = lambda s: print(s, flush=True)  # noqa: E731
+    model = seamount(tuple(args.size))
+    t0 = time.time()
+    b, z, x, active = learned.collect_pairs(model, args.dt, args.pairs, cg_iterations=args.cg_iterations)
+    log("collected %d triples in %.1f s" % (b.shape[0], time.time() - t0))
+    t0 = time.time()
+    net = learned.train(b, z, x, active, epochs=args.epochs, lr=args.lr, log=log)
+    log("trained in %.1f s" % (time.time() - t0))
+    w = learned.export_weights(net)
+    np.save(args.out, w)
+    del b, z, x
+    hb, _, _, _ = learned.collect_pairs(model, args.dt, args.heldout)
+    rhs = [hb[i].contiguous() for i in range(hb.shape[0])]
+    fft = timed_solves(model, rhs, torch)
+    model.set_learned_preconditioner(w)
+    lrn = timed_solves(model, rhs, torch)
+    print(json.dumps({"heldout_solves": len(rhs), "reltol": 1e-8, "size": list(args.size),
+                      "training_triples": int(args.pairs * (args.cg_iterations + 1)), "epochs": args.epochs,
+                      "fft_pcg": fft, "learned_pcg": lrn,
+                      "time_ratio_learned_over_fft": lrn["ms_mean"] / fft["ms_mean"]}), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -624,6 +624,18 @@ def main():
     poisson = None
     if isinstance(physics.get("pressure_solver"), og.ConjugateGradientPoissonSolver):
         poisson = held_out_solves(model, grid, torch, stream, ft, n=50)
+        # the learned correction of the preconditioner, trained for this grid, on the same
+        # right-hand sides (flexible CG)
+        wpath = os.path.join(os.path.dirname(og.__file__), "weights", "seamount_%dx%dx%d.npy" % tuple(size))
+        if os.path.exists(wpath):
+            model.set_learned_preconditioner(wpath)
+            try:
+                learned = held_out_solves(model, grid, torch, stream, ft, n=50)
+            except L.NotConvergedError as e:
+                learned = {"not_converged": str(e)}
+            model.set_learned_preconditioner(None)
+            learned["preconditioner"] = "fft + learned correction (flexible CG), %s" % os.path.basename(wpath)
+            poisson = {"fft_pcg": poisson, "learned_pcg": learned}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -48,58 +48,71 @@ GBO_D uint32_t pack2(float lo, float hi) {
 template <int CIN, int COUT, int MODE, typename FT>
 __global__ void __launch_bounds__(128) k_conv(ConvP p) {
     static_assert(CIN % 8 == 0 && COUT % 8 == 0 && COUT <= 64, "channel counts");
-    constexpr int K = 27 * CIN, KP = kpad(CIN), KC = KP / 16, NT = COUT / 8;
+    constexpr int K = 27 * CIN, KP = kpad(CIN), NS = KP / KS, NT = COUT / 8, BP = COUT * (KS / 8);
     __shared__ __align__(16) bf16 As[2][MT * AS];
     __shared__ __align__(16) bf16 Bs[2][COUT * AS];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
     const int64_t n = p.d.n();
     const int64_t m0 = (int64_t)blockIdx.x * MT;
-    // the im2col row (cell) this thread stages and its 8-wide half of each k chunk
-    const int row = tid >> 1, half = tid & 1;
-    const int64_t cell = m0 + row;
-    const bool cell_ok = cell < n;
-    const int ci = cell_ok ? (int)(cell % nx) : 0;
-    const int cj = cell_ok ? (int)((cell / nx) % ny) : 0;
-    const int ck = cell_ok ? (int)(cell / ((int64_t)nx * ny)) : 0;
-    auto load_chunk = [&](int kc, int buf) {
-        const int kk = kc * 16 + half * 8;  // one tap, channels c0 .. c0 + 7
-        bool ok = cell_ok && kk < K;
-        int64_t src = 0;
-        if (ok) {
-            const int tap = kk / CIN, c0 = kk % CIN;
-            const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-            const int kz = ck + dz;
-            int ii = ci + dx, jj = cj + dy;
-            ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
-            jj = jj < 0 ? jj + ny : (jj >= ny ? jj - ny : jj);
-            ok = kz >= 0 && kz < nz;
-            src = (ii + (int64_t)nx * (jj + (int64_t)ny * kz)) * CIN + c0;
+    // this thread stages the 8-wide piece `part` of rows row0 + 16 q (q = 0..3) of each stage
+    const int part = tid & 7, row0 = tid >> 3;
+    int ci[4], cj[4], ck[4];
+    bool cok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int64_t cell = m0 + row0 + 16 * q;
+        cok[q] = cell < n;
+        ci[q] = cok[q] ? (int)(cell % nx) : 0;
+        cj[q] = cok[q] ? (int)((cell / nx) % ny) : 0;
+        ck[q] = cok[q] ? (int)(cell / ((int64_t)nx * ny)) : 0;
+    }
+    auto load_stage = [&](int st, int buf) {
+        const int kk = st * KS + part * 8;  // one tap, channels c0 .. c0 + 7
+        const bool kin = kk < K;
+        const int tap = kin ? kk / CIN : 0, c0 = kk % CIN;
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            bool ok = cok[q] && kin;
+            int64_t src = 0;
+            if (ok) {
+                const int kz = ck[q] + dz;
+                int ii = ci[q] + dx, jj = cj[q] + dy;
+                ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
+                jj = jj < 0 ? jj + ny : (jj >= ny ? jj - ny : jj);
+                ok = kz >= 0 && kz < nz;
+                src = (ii + (int64_t)nx * (jj + (int64_t)ny * kz)) * CIN + c0;
+            }
+            cp16(&As[buf][(row0 + 16 * q) * AS + part * 8], p.in + (ok ? src : 0), ok);
         }
-        cp16(&As[buf][row * AS + half * 8], p.in + (ok ? src : 0), ok);
-        if (tid < 2 * COUT) {
-            const int r = tid >> 1, h = tid & 1;
-            cp16(&Bs[buf][r * AS + h * 8], p.w + (int64_t)r * KP + kc * 16 + h * 8, true);
+        for (int e = tid; e < BP; e += 128) {
+            const int r = e / (KS / 8), h = e % (KS / 8);
+            cp16(&Bs[buf][r * AS + h * 8], p.w + (int64_t)r * KP + st * KS + h * 8, true);
         }
     };
     float acc[NT][4];
 #pragma unroll
     for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-    load_chunk(0, 0);
+    load_stage(0, 0);
     cp_commit();
-    for (int kc = 0; kc < KC; ++kc) {
-        if (kc + 1 < KC) load_chunk(kc + 1, (kc + 1) & 1);
+    for (int st = 0; st < NS; ++st) {
+        if (st + 1 < NS) load_stage(st + 1, (st + 1) & 1);
         cp_commit();
         cp_wait1();
         __syncthreads();
-        const bf16* A = As[kc & 1] + warp * 16 * AS;
-        const uint32_t a0 = ld32(A + g * AS + 2 * t), a1 = ld32(A + (g + 8) * AS + 2 * t);
-        const uint32_t a2 = ld32(A + g * AS + 2 * t + 8), a3 = ld32(A + (g + 8) * AS + 2 * t + 8);
-        const bf16* B = Bs[kc & 1];
+        const bf16* A = As[st & 1] + warp * 16 * AS;
+        const bf16* B = Bs[st & 1];
 #pragma unroll
-        for (int q = 0; q < NT; ++q) {
-            const uint32_t b0 = ld32(B + (q * 8 + g) * AS + 2 * t), b1 = ld32(B + (q * 8 + g) * AS + 2 * t + 8);
-            mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+        for (int ks = 0; ks < KS / 16; ++ks) {
+            const int ko = ks * 16 + 2 * t;
+            const uint32_t a0 = ld32(A + g * AS + ko), a1 = ld32(A + (g + 8) * AS + ko);
+            const uint32_t a2 = ld32(A + g * AS + ko + 8), a3 = ld32(A + (g + 8) * AS + ko + 8);
+#pragma unroll
+            for (int q = 0; q < NT; ++q) {
+                const uint32_t b0 = ld32(B + (q * 8 + g) * AS + ko), b1 = ld32(B + (q * 8 + g) * AS + ko + 8);
+                mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+            }
         }
         __syncthreads();
     }

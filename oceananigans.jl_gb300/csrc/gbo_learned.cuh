@@ -12,14 +12,14 @@
 // Data layout: activations are BF16, channels last ([cell][channel], cell = i + nx (j +
 // ny k) on the level's grid), so the 8 or 16 channels of one neighbour are one or two
 // 16-byte copies.  Weights are BF16 [cout][27 · cin] (k = tap · cin + ci, tap = 9 (dz+1)
-// + 3 (dy+1) + (dx+1)), zero padded to whole 16-wide k chunks; biases FP32.  Boundaries:
+// + 3 (dy+1) + (dx+1)), zero padded to whole 64-wide k stages; biases FP32.  Boundaries:
 // periodic in x and y, zero padding in z.
 //
 // Convolutions are implicit GEMMs on the warp-level tensor-core instruction
 // mma.sync.m16n8k16 (BF16 in, FP32 accumulate): a block computes 64 cells × cout; per
-// 16-wide k chunk it stages the 64 × 16 im2col rows and the cout × 16 weights in shared
+// 64-wide k stage it stages the 64 × 64 im2col rows and the cout × 64 weights in shared
 // memory with asynchronous copies (double buffered) and each of its four warps issues
-// cout / 8 MMAs for its 16 cells.
+// 4 · cout / 8 MMAs for its 16 cells between two barriers.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -34,7 +34,8 @@ constexpr int LEVELS = 4;
 constexpr int C0 = 16, C1 = 32, C2 = 48, C3 = 64;
 constexpr int FEAT = 8;  // input channels of the first convolution (3 used)
 constexpr int MT = 64;   // cells per block
-constexpr int AS = 24;   // shared row stride in BF16 (16 data + 8 pad: conflict-free fragment loads)
+constexpr int KS = 64;   // k per pipeline stage (four MMA k-steps between barriers)
+constexpr int AS = KS + 8;  // shared row stride in BF16 (pad: conflict-free fragment loads)
 
 // The layers in order; cin / cout as above, out = final layer (one channel into z)
 enum { L_ENC0 = 0, L_ENC1, L_ENC2, L_ENC3, L_DEC3, L_DEC2, L_DEC1, L_OUT, NLAYERS };
@@ -45,7 +46,7 @@ constexpr int LAYER_COUT[NLAYERS] = {C0, C1, C2, C3, C2, C1, C0, 8};  // out: ch
 constexpr int FILE_CIN[NLAYERS] = {3, C0, C1, C2, C3, C2, C1, C0};
 constexpr int FILE_COUT[NLAYERS] = {C0, C1, C2, C3, C2, C1, C0, 1};
 
-GBO_HD constexpr int kpad(int cin) { return ((27 * cin + 15) / 16) * 16; }
+GBO_HD constexpr int kpad(int cin) { return ((27 * cin + KS - 1) / KS) * KS; }
 
 // Number of FP32 values in a weight file (all layers, weights then biases per layer).
 inline int64_t file_count() {

@@ -24,8 +24,6 @@ GBO_D void cp16(void* smem, const void* src, bool valid) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0));
 }
 GBO_D void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-GBO_D void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
-GBO_D uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
 // D = A B + D for one 16 × 8 × 16 tile: A row-major 16 × 16, B column-major 16 × 8
 // (BF16), D FP32.  Fragments (g = lane / 4, t = lane % 4): a0 = A[g][2t..], a1 =
@@ -43,98 +41,141 @@ GBO_D uint32_t pack2(float lo, float hi) {
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// 3³ convolution as an implicit GEMM (see the file header of gbo_learned.cuh).
-// MODE 0: out = bf16(relu(acc + bias)); MODE 1: z += s (acc₀ + bias₀) in FT.
+GBO_D void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const bf16* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
+}
+GBO_D void ldsm_x2(uint32_t& r0, uint32_t& r1, const bf16* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
+}
+
+// Halo-tile convolution: a block computes a TX × TY patch of one z level (128 cells) ×
+// cout.  Per 16-channel chunk of the input it stages the (TX+2) × (TY+2) × 3 halo tile
+// once in shared memory (each input value then serves all 27 taps) and the chunk's
+// weights [cout][27 taps × 16]; each warp then issues, per tap, one ldmatrix for its
+// 16 rows of A (rows of the tile shifted by the tap) and cout / 8 MMAs.
+namespace halo {
+constexpr int TX = 32, TY = 4, HX = TX + 2, HY = TY + 2, HC = HX * HY * 3;  // tile cells
+constexpr int CS = 24;             // shared stride of one tile cell (16 channels + pad; conflict-free)
+constexpr int BS = 27 * 16 + 8;    // shared stride of one weight row
+template <int COUT>
+constexpr size_t smem_bytes() { return (size_t)(HC * CS + COUT * BS) * sizeof(bf16); }
+}  // namespace halo
+
 template <int CIN, int COUT, int MODE, typename FT>
-__global__ void __launch_bounds__(128) k_conv(ConvP p) {
-    static_assert(CIN % 8 == 0 && COUT % 8 == 0 && COUT <= 64, "channel counts");
-    constexpr int K = 27 * CIN, KP = kpad(CIN), NS = KP / KS, NT = COUT / 8, BP = COUT * (KS / 8);
-    __shared__ __align__(16) bf16 As[2][MT * AS];
-    __shared__ __align__(16) bf16 Bs[2][COUT * AS];
+__global__ void __launch_bounds__(256) k_conv_halo(ConvP p) {
+    using namespace halo;
+    static_assert((CIN == 8 || CIN % 16 == 0) && COUT % 8 == 0 && COUT <= 64, "channel counts");
+    static_assert(CIN != 8 || COUT % 16 == 0, "the 8-channel path pairs n tiles");
+    constexpr int NCH = CIN == 8 ? 1 : CIN / 16, CW = CIN == 8 ? 8 : 16;  // chunks, channels per chunk
+    constexpr int NT = COUT / 8, KP = kpad(CIN);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* tile = reinterpret_cast<bf16*>(smem_raw);  // [HC][CS]
+    bf16* wsm = tile + HC * CS;                       // [COUT][BS]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-    const int64_t n = p.d.n();
-    const int64_t m0 = (int64_t)blockIdx.x * MT;
-    // this thread stages the 8-wide piece `part` of rows row0 + 16 q (q = 0..3) of each stage
-    const int part = tid & 7, row0 = tid >> 3;
-    int ci[4], cj[4], ck[4];
-    bool cok[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int64_t cell = m0 + row0 + 16 * q;
-        cok[q] = cell < n;
-        ci[q] = cok[q] ? (int)(cell % nx) : 0;
-        cj[q] = cok[q] ? (int)((cell / nx) % ny) : 0;
-        ck[q] = cok[q] ? (int)(cell / ((int64_t)nx * ny)) : 0;
-    }
-    auto load_stage = [&](int st, int buf) {
-        const int kk = st * KS + part * 8;  // one tap, channels c0 .. c0 + 7
-        const bool kin = kk < K;
-        const int tap = kin ? kk / CIN : 0, c0 = kk % CIN;
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            bool ok = cok[q] && kin;
-            int64_t src = 0;
-            if (ok) {
-                const int kz = ck[q] + dz;
-                int ii = ci[q] + dx, jj = cj[q] + dy;
-                ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
-                jj = jj < 0 ? jj + ny : (jj >= ny ? jj - ny : jj);
-                ok = kz >= 0 && kz < nz;
-                src = (ii + (int64_t)nx * (jj + (int64_t)ny * kz)) * CIN + c0;
-            }
-            cp16(&As[buf][(row0 + 16 * q) * AS + part * 8], p.in + (ok ? src : 0), ok);
-        }
-        for (int e = tid; e < BP; e += 128) {
-            const int r = e / (KS / 8), h = e % (KS / 8);
-            cp16(&Bs[buf][r * AS + h * 8], p.w + (int64_t)r * KP + st * KS + h * 8, true);
-        }
-    };
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
+    // this warp's 16 output rows: y = y0 + my, x = x0 + mx0 .. mx0 + 15
+    const int my = warp >> 1, mx0 = (warp & 1) * 16;
     float acc[NT][4];
 #pragma unroll
     for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-    load_stage(0, 0);
-    cp_commit();
-    for (int st = 0; st < NS; ++st) {
-        if (st + 1 < NS) load_stage(st + 1, (st + 1) & 1);
+    for (int cc = 0; cc < NCH; ++cc) {
+        // halo tile: 16-byte pieces (HC cells × 2 halves)
+        for (int e = tid; e < HC * 2; e += 256) {
+            const int c = e >> 1, h = e & 1;
+            const int tx = c % HX, ty = (c / HX) % HY, tz = c / (HX * HY);
+            const int gx = wrapm(x0 + tx - 1, nx), gy = wrapm(y0 + ty - 1, ny), gz = z + tz - 1;
+            const bool ok = gz >= 0 && gz < nz && h * 8 < CW;
+            const int64_t src = (gx + (int64_t)nx * (gy + (int64_t)ny * gz)) * CIN + cc * 16 + h * 8;
+            cp16(tile + c * CS + h * 8, p.in + (ok ? src : 0), ok);
+        }
+        if constexpr (CIN == 8) {
+            // 8 channels: k = tap · 8 + c as stored, two taps per 16-wide MMA step
+            for (int e = tid; e < COUT * 28; e += 256) {
+                const int n = e / 28, piece = e % 28;
+                cp16(wsm + n * BS + piece * 8, p.w + (int64_t)n * KP + piece * 8, true);
+            }
+        } else {
+            // weights of this chunk: row n, tap, 16 channels (two pieces)
+            for (int e = tid; e < COUT * 27 * 2; e += 256) {
+                const int n = e / 54, rem = e % 54, tap = rem >> 1, h = rem & 1;
+                const int64_t src = (int64_t)n * KP + tap * CIN + cc * 16 + h * 8;
+                cp16(wsm + n * BS + tap * 16 + h * 8, p.w + src, true);
+            }
+        }
         cp_commit();
-        cp_wait1();
+        asm volatile("cp.async.wait_group 0;\n" ::);
         __syncthreads();
-        const bf16* A = As[st & 1] + warp * 16 * AS;
-        const bf16* B = Bs[st & 1];
+        // A rows: lane → row (lane & 15), k half (lane >> 4)
+        const int ar = lane & 15, ah = (lane >> 4) * 8;
+        if constexpr (CIN == 8) {
+            // step s covers taps 2s (k 0-7, lanes 0-15) and 2s + 1 (k 8-15, lanes 16-31); the
+            // 28th tap of the last step has zero weights
+#pragma unroll 2
+            for (int st = 0; st < 14; ++st) {
+                const int tap = min(2 * st + (lane >> 4), 26);
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                const int tc = (dz * HY + my + dy) * HX + mx0 + ar + dx;
+                uint32_t a0, a1, a2, a3;
+                ldsm_x4(a0, a1, a2, a3, tile + tc * CS);
 #pragma unroll
-        for (int ks = 0; ks < KS / 16; ++ks) {
-            const int ko = ks * 16 + 2 * t;
-            const uint32_t a0 = ld32(A + g * AS + ko), a1 = ld32(A + (g + 8) * AS + ko);
-            const uint32_t a2 = ld32(A + g * AS + ko + 8), a3 = ld32(A + (g + 8) * AS + ko + 8);
+                for (int q = 0; q < NT; q += 2) {
+                    uint32_t b0, b1, b2, b3;
+                    const int mi = lane >> 3;
+                    ldsm_x4(b0, b1, b2, b3, wsm + ((q + (mi >> 1)) * 8 + (lane & 7)) * BS + st * 16 + (mi & 1) * 8);
+                    mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+                    mma16816(acc[q + 1], a0, a1, a2, a3, b2, b3);
+                }
+            }
+        } else {
+#pragma unroll 3
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // tile offsets (0..2)
+                const int tc = (dz * HY + my + dy) * HX + mx0 + ar + dx;
+                uint32_t a0, a1, a2, a3;
+                ldsm_x4(a0, a1, a2, a3, tile + tc * CS + ah);
+                if constexpr (NT == 1) {
+                    uint32_t b0, b1;
+                    ldsm_x2(b0, b1, wsm + (lane & 7) * BS + tap * 16 + ((lane >> 3) & 1) * 8);
+                    mma16816(acc[0], a0, a1, a2, a3, b0, b1);
+                } else {
 #pragma unroll
-            for (int q = 0; q < NT; ++q) {
-                const uint32_t b0 = ld32(B + (q * 8 + g) * AS + ko), b1 = ld32(B + (q * 8 + g) * AS + ko + 8);
-                mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+                    for (int q = 0; q < NT; q += 2) {
+                        uint32_t b0, b1, b2, b3;
+                        const int mi = lane >> 3;
+                        ldsm_x4(b0, b1, b2, b3, wsm + ((q + (mi >> 1)) * 8 + (lane & 7)) * BS + tap * 16 + (mi & 1) * 8);
+                        mma16816(acc[q], a0, a1, a2, a3, b0, b1);
+                        mma16816(acc[q + 1], a0, a1, a2, a3, b2, b3);
+                    }
+                }
             }
         }
         __syncthreads();
     }
-    const int64_t r0 = m0 + warp * 16 + g, r1 = r0 + 8;
+    const int y = y0 + my, xa = x0 + mx0 + g, xb = xa + 8;
+    const bool oka = y < ny && xa < nx, okb = y < ny && xb < nx;
+    const int64_t ra = xa + (int64_t)nx * (y + (int64_t)ny * z), rb = ra + 8;
     if constexpr (MODE == 0) {
 #pragma unroll
         for (int q = 0; q < NT; ++q) {
             const int col = q * 8 + 2 * t;
             const float b0 = p.bias[col], b1 = p.bias[col + 1];
-            if (r0 < n)
-                *reinterpret_cast<uint32_t*>(p.out + r0 * COUT + col) =
+            if (oka)
+                *reinterpret_cast<uint32_t*>(p.out + ra * COUT + col) =
                     pack2(fmaxf(acc[q][0] + b0, 0.f), fmaxf(acc[q][1] + b1, 0.f));
-            if (r1 < n)
-                *reinterpret_cast<uint32_t*>(p.out + r1 * COUT + col) =
+            if (okb)
+                *reinterpret_cast<uint32_t*>(p.out + rb * COUT + col) =
                     pack2(fmaxf(acc[q][2] + b0, 0.f), fmaxf(acc[q][3] + b1, 0.f));
         }
     } else {
         if (t == 0) {
-            FT* z = static_cast<FT*>(p.z);
+            FT* zz = static_cast<FT*>(p.z);
             const float s = *p.scale, b0 = p.bias[0];
-            if (r0 < n) z[r0] += FT(s * (acc[0][0] + b0));
-            if (r1 < n) z[r1] += FT(s * (acc[0][2] + b0));
+            if (oka) zz[ra] += FT(s * (acc[0][0] + b0));
+            if (okb) zz[rb] += FT(s * (acc[0][2] + b0));
         }
     }
 }
@@ -275,6 +316,10 @@ struct LearnedNet {
     }
 };
 
+namespace {
+cudaError_t conv_smem_all();
+}
+
 LearnedNet* learned_create(int nx, int ny, int nz, const float* weights, int64_t count, std::string* err) {
     using namespace learned;
     if (nx % 8 || ny % 8 || nz % 8 || nx < 8 || ny < 8 || nz < 8) {
@@ -324,8 +369,9 @@ LearnedNet* learned_create(int nx, int ny, int nz, const float* weights, int64_t
     net->acc = need(net->dev<double>(1));
     net->cnt = need(net->dev<unsigned>(1));
     net->scale = need(net->dev<float>(2));
+    if (ok && conv_smem_all() != cudaSuccess) ok = false;
     if (!ok || cudaGetLastError() != cudaSuccess) {
-        *err = "learned preconditioner: device allocation failed";
+        *err = "learned preconditioner: device allocation or kernel set-up failed";
         delete net;
         return nullptr;
     }
@@ -338,9 +384,30 @@ namespace {
 
 template <int CIN, int COUT, int MODE, typename FT>
 void conv(const LearnedNet* net, int layer, int level, const bf16* in, bf16* out, void* z, cudaStream_t st) {
+    using namespace learned::halo;
     learned::ConvP p{in, net->w[layer], net->b[layer], out, z, net->scale + 1, net->d[level]};
-    const int64_t blocks = (net->d[level].n() + learned::MT - 1) / learned::MT;
-    learned::k_conv<CIN, COUT, MODE, FT><<<(unsigned)blocks, 128, 0, st>>>(p);
+    const learned::Dims& d = net->d[level];
+    const dim3 grid((d.nx + TX - 1) / TX, (d.ny + TY - 1) / TY, d.nz);
+    learned::k_conv_halo<CIN, COUT, MODE, FT><<<grid, 256, smem_bytes<COUT>(), st>>>(p);
+}
+
+// dynamic shared memory above the default 48 KB for every instance
+template <int CIN, int COUT, int MODE, typename FT>
+cudaError_t conv_smem() {
+    return cudaFuncSetAttribute(learned::k_conv_halo<CIN, COUT, MODE, FT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)learned::halo::smem_bytes<COUT>());
+}
+cudaError_t conv_smem_all() {
+    using namespace learned;
+    cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {conv_smem<FEAT, C0, 0, float>(), conv_smem<C0, C1, 0, float>(), conv_smem<C1, C2, 0, float>(),
+                          conv_smem<C2, C3, 0, float>(), conv_smem<C3, C2, 0, float>(), conv_smem<C2, C1, 0, float>(),
+                          conv_smem<C1, C0, 0, float>(), conv_smem<C0, 8, 1, float>(), conv_smem<FEAT, C0, 0, double>(),
+                          conv_smem<C0, C1, 0, double>(), conv_smem<C1, C2, 0, double>(), conv_smem<C2, C3, 0, double>(),
+                          conv_smem<C3, C2, 0, double>(), conv_smem<C2, C1, 0, double>(), conv_smem<C1, C0, 0, double>(),
+                          conv_smem<C0, 8, 1, double>()})
+        if (r != cudaSuccess) e = r;
+    return e;
 }
 
 unsigned grid_for(int64_t work) { return (unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16); }

@@ -16,10 +16,11 @@
 // periodic in x and y, zero padding in z.
 //
 // Convolutions are implicit GEMMs on the warp-level tensor-core instruction
-// mma.sync.m16n8k16 (BF16 in, FP32 accumulate): a block computes 64 cells × cout; per
-// 64-wide k stage it stages the 64 × 64 im2col rows and the cout × 64 weights in shared
-// memory with asynchronous copies (double buffered) and each of its four warps issues
-// 4 · cout / 8 MMAs for its 16 cells between two barriers.
+// mma.sync.m16n8k16 (BF16 in, FP32 accumulate): a block computes a 32 × 4 patch of one
+// level (128 cells) × cout.  Per 16-channel chunk of the input it stages the patch's
+// halo tile (34 × 6 × 3 cells) and the chunk's weights in shared memory with
+// asynchronous copies; every input value then serves all 27 taps, and each of the
+// eight warps loads its A fragments per tap with one ldmatrix from the shifted tile.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -33,9 +34,7 @@ namespace learned {
 constexpr int LEVELS = 4;
 constexpr int C0 = 16, C1 = 32, C2 = 48, C3 = 64;
 constexpr int FEAT = 8;  // input channels of the first convolution (3 used)
-constexpr int MT = 64;   // cells per block
-constexpr int KS = 64;   // k per pipeline stage (four MMA k-steps between barriers)
-constexpr int AS = KS + 8;  // shared row stride in BF16 (pad: conflict-free fragment loads)
+constexpr int KS = 64;   // weight rows are padded to a multiple of KS
 
 // The layers in order; cin / cout as above, out = final layer (one channel into z)
 enum { L_ENC0 = 0, L_ENC1, L_ENC2, L_ENC3, L_DEC3, L_DEC2, L_DEC1, L_OUT, NLAYERS };

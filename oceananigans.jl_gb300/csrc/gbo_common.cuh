@@ -47,6 +47,7 @@ struct GridP {
     const FT* dzf;    // Δzᵃᵃᶠ(kr)
     const FT* rdzc;   // 1/Δzᵃᵃᶜ(kr)
     const FT* rdzf;   // 1/Δzᵃᵃᶠ(kr)
+    const FT* rvc;    // 1/Vᶜᶜᶜ(kr) = 1/(Δx Δy Δzᵃᵃᶜ), formed in FT as the operators do
     // immersed boundary: per-column index of the first active cell (0 = none immersed)
     const int* kbot;  // Nx*Ny entries or nullptr
 };

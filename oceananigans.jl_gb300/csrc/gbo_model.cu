@@ -19,55 +19,95 @@
 // ===========================================================================
 enum { SRC_FFT = 0, SRC_FT = 1, SRC_CG = 2 };
 
+// Levels marched by one thread of the column kernels (k_source, k_correct): the z
+// neighbour of one level is the value of the previous one, and the index arithmetic
+// and the immersed-column lookups are done once per column
+constexpr int COL_LEVELS = 8;
+
 // rhs = divᶜᶜᶜ(u*) (solve_for_pressure.jl:12-50): × Δzᶜ for the Fourier-tridiagonal
 // solver, × Vᶜᶜᶜ for CG.
 template <typename FT>
-__global__ void k_source(GridP<FT> g, const FT* __restrict__ u, const FT* __restrict__ v, const FT* __restrict__ w,
-                         FT* __restrict__ rhs, int mode) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
+__global__ void __launch_bounds__(256) k_source(GridP<FT> g, const FT* __restrict__ u, const FT* __restrict__ v,
+                                                const FT* __restrict__ w, FT* __restrict__ rhs, int mode) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
-    CFld<FT> U = cfld(u, g), V = cfld(v, g);
-    WFld<FT> W = wfld(w, g);
+    const int k0 = blockIdx.z * COL_LEVELS, k1 = min(g.Nz, k0 + COL_LEVELS);
+    const size_t plane = (size_t)g.Nx * g.Ny, c = i + (size_t)g.Nx * j;
+    const size_t cx = wrapi(i + 1, g.Nx) + (size_t)g.Nx * j, cy = i + (size_t)g.Nx * wrapi(j + 1, g.Ny);
     Met<FT> M(g);
-    FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
-    FT div = M.rVc(k) * ((Ax * U(i + 1, j, k) - Ax * U(i, j, k)) + (Ay * V(i, j + 1, k) - Ay * V(i, j, k)) +
-                         (g.flatz ? FT(0) : (Az * W(i, j, k + 1) - Az * W(i, j, k))));
-    bool active = true;
-    if (g.kbot) active = k >= g.kbot[i + (size_t)g.Nx * j];
-    FT r = active ? div : FT(0);
-    if (mode == SRC_FT) r = (active ? M.dzc(k) : FT(0)) * div;
-    if (mode == SRC_CG) r = r * (Az * M.dzc(k));
-    rhs[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = r;
+    const FT Az = M.Az();
+    const int kb = g.kbot ? __ldg(g.kbot + c) : 0;
+    // w at the bottom face of the first level (zero at the wall, face 0)
+    FT wlo = (g.flatz || k0 <= 0) ? FT(0) : w[c + plane * k0];
+    for (int k = k0; k < k1; ++k) {
+        const size_t o = plane * k;
+        const FT whi = (g.flatz || k + 1 >= g.Nz) ? FT(0) : w[c + o + plane];
+        const FT Ax = M.Ax(k), Ay = M.Ay(k);
+        const FT div = M.rVc(k) * ((Ax * u[cx + o] - Ax * u[c + o]) + (Ay * v[cy + o] - Ay * v[c + o]) +
+                                   (g.flatz ? FT(0) : (Az * whi - Az * wlo)));
+        const bool active = k >= kb;
+        FT r = active ? div : FT(0);
+        if (mode == SRC_FT) r = (active ? M.dzc(k) : FT(0)) * div;
+        if (mode == SRC_CG) r = r * (Az * M.dzc(k));
+        rhs[c + o] = r;
+        wlo = whi;
+    }
 }
 
 // u = u* - ∂x(pΔτ), ... (pressure_correction.jl:67-73), p = pΔτ / max(eps, Δτ)
 // (:102-104), and the tracer predictor copied to the state.  In place is allowed
-// (every point reads only its own u*).
+// (every point reads only its own u*).  ∂ operators are conditional on an immersed
+// grid (conditional_differences.jl:15-43): zero across a face touching an immersed cell.
 template <typename FT>
-__global__ void k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws, const FT* __restrict__ phi,
-                          FT* u, FT* v, FT* w, FT* __restrict__ p, FT rdtau, FT phi_shift,
-                          const FT* rdp = nullptr) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
+__global__ void __launch_bounds__(256) k_correct(GridP<FT> g, const FT* us, const FT* vs, const FT* ws,
+                                                 const FT* __restrict__ phi, FT* u, FT* v, FT* w, FT* __restrict__ p,
+                                                 FT rdtau, FT phi_shift, const FT* rdp = nullptr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
-    CFld<FT> P = cfld(phi, g);
+    const int k0 = blockIdx.z * COL_LEVELS, k1 = min(g.Nz, k0 + COL_LEVELS);
+    const size_t plane = (size_t)g.Nx * g.Ny, c = i + (size_t)g.Nx * j;
+    const size_t cw = wrapi(i - 1, g.Nx) + (size_t)g.Nx * j, cs = i + (size_t)g.Nx * wrapi(j - 1, g.Ny);
     Met<FT> M(g);
-    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
     if (rdp) rdtau = __ldg(rdp);
-    FT pc = P(i, j, k) - phi_shift;
-    // ∂ operators are conditional on an immersed grid (conditional_differences.jl:15-43)
-    FT dx_ = cond_zero(g, i - 1, j, k, i, j, k) ? FT(0) : (pc - (P(i - 1, j, k) - phi_shift));
-    FT dy_ = cond_zero(g, i, j - 1, k, i, j, k) ? FT(0) : (pc - (P(i, j - 1, k) - phi_shift));
-    u[idx] = us[idx] - dx_ * g.rdx;
-    v[idx] = vs[idx] - dy_ * g.rdy;
-    if (!g.flatz) {
-        FT dz_ = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (pc - (P(i, j, k - 1) - phi_shift));
-        w[idx] = ws[idx] - dz_ * M.rdzf(k);
+    const bool ibg = g.kbot != nullptr;
+    const int kbC = ibg ? __ldg(g.kbot + c) : 0, kbW = ibg ? __ldg(g.kbot + cw) : 0, kbS = ibg ? __ldg(g.kbot + cs) : 0;
+    auto imm = [&](int kb, int k) { return ibg && k >= 0 && k < g.Nz && k < kb; };
+    // all loads of the column first: u* may alias u (in place), so loads issued after a
+    // store could not move ahead of it
+    FT rp[COL_LEVELS + 1], rw[COL_LEVELS], rs[COL_LEVELS], ru[COL_LEVELS], rv[COL_LEVELS], rz[COL_LEVELS];
+    rp[0] = phi[c + plane * (k0 > 0 ? k0 - 1 : 0)];  // ϕ below the first level (mirrored at the bottom)
+#pragma unroll
+    for (int l = 0; l < COL_LEVELS; ++l) {
+        const int k = k0 + l;
+        if (k < k1) {
+            const size_t o = plane * k;
+            rp[l + 1] = phi[c + o];
+            rw[l] = phi[cw + o];
+            rs[l] = phi[cs + o];
+            ru[l] = us[c + o];
+            rv[l] = vs[c + o];
+            rz[l] = g.flatz ? FT(0) : ws[c + o];
+        }
     }
-    p[idx] = pc * rdtau;
+#pragma unroll
+    for (int l = 0; l < COL_LEVELS; ++l) {
+        const int k = k0 + l;
+        if (k < k1) {
+            const size_t o = plane * k;
+            const FT pc = rp[l + 1] - phi_shift;
+            const FT dx_ = (imm(kbW, k) || imm(kbC, k)) ? FT(0) : (pc - (rw[l] - phi_shift));
+            const FT dy_ = (imm(kbS, k) || imm(kbC, k)) ? FT(0) : (pc - (rs[l] - phi_shift));
+            u[c + o] = ru[l] - dx_ * g.rdx;
+            v[c + o] = rv[l] - dy_ * g.rdy;
+            if (!g.flatz) {
+                const FT dz_ = (imm(kbC, k - 1) || imm(kbC, k)) ? FT(0) : (pc - (rp[l] - phi_shift));
+                w[c + o] = rz[l] - dz_ * M.rdzf(k);
+            }
+            p[c + o] = pc * rdtau;
+        }
+    }
 }
 
 // mask_immersed_field! (mask_immersed_field.jl:65-77): zero on the immersed periphery
@@ -350,7 +390,7 @@ struct ModelImpl : gbo_model {
     DBuf<FT> u, v, w, us, vs, ws, Gu, Gv, Gw, nu, phy, p;
     std::vector<DBuf<FT>> c, cs, Gc, kap;
     // grid tables
-    DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf;
+    DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf, t_rvc;
     DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64, t_ws;
     DBuf<int> t_kbot;
     ZGrid<FT> Z;
@@ -408,7 +448,7 @@ struct ModelImpl : gbo_model {
         if (h_run) cudaFreeHost(h_run);
         if (run_stream) cudaStreamDestroy(run_stream);
         if (if_stream) cudaStreamDestroy(if_stream);
-        for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &rb, &lx, &ly, &lz,
+        for (DBuf<FT>* b : {&u, &v, &w, &us, &vs, &ws, &Gu, &Gv, &Gw, &nu, &phy, &p, &t_dzc, &t_dzf, &t_rdzc, &t_rdzf, &t_rvc, &rb, &lx, &ly, &lz,
                             &cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x})
             b->free_();
         cg_s.free_();
@@ -459,6 +499,14 @@ struct ModelImpl : gbo_model {
         gp.dx = FT(Lx / Nx); gp.dy = FT(Ly / Ny);
         gp.rdx = FT(1) / gp.dx; gp.rdy = FT(1) / gp.dy;
         gp.dzc = t_dzc.p; gp.dzf = t_dzf.p; gp.rdzc = t_rdzc.p; gp.rdzf = t_rdzf.p;
+        {
+            // 1/Vᶜᶜᶜ = FT(1) / ((Δx Δy) Δzᶜ), the operation order of Met::rVc
+            std::vector<FT> rvc(Z.dzc.size());
+            const FT az = gp.dx * gp.dy;
+            for (size_t q = 0; q < rvc.size(); ++q) rvc[q] = FT(1) / (az * Z.dzc[q]);
+            t_rvc.upload(rvc);
+            gp.rvc = t_rvc.p;
+        }
         gp.kbot = nullptr;
         if (gd->bottom_height) {
             // GridFittedBottom: a cell is immersed iff its centre lies at or below the bottom
@@ -586,6 +634,7 @@ struct ModelImpl : gbo_model {
     dim3 blk() const { return dim3(32, 8, 1); }
     dim3 grd() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, Nz); }
     dim3 cg_grid() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, std::min(Nz, CG_ZSLICES)); }
+    dim3 col_grid() const { return dim3((Nx + 31) / 32, (Ny + 7) / 8, (Nz + COL_LEVELS - 1) / COL_LEVELS); }
 
     // kernel accounting: group of the next launch, launches per captured step,
     // optional per-group CUDA events (timing mode)
@@ -698,13 +747,13 @@ struct ModelImpl : gbo_model {
         } else {
             int mode = desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ? SRC_FT : SRC_FFT;
             pre(G_SOURCE);
-            k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
+            k_source<FT><<<col_grid(), blk(), 0, stream>>>(gp, ui, vi, wi, rb.p, mode);
             check_launch();
             poisson_solve(desc.pressure_solver);
         }
         FT rdtau = FT(1) / FT(std::max(eps, dtau));
         pre(G_CORRECT);
-        k_correct<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, phi, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0),
+        k_correct<FT><<<col_grid(), blk(), 0, stream>>>(gp, ui, vi, wi, phi, u.p, v.p, flat ? nullptr : w.p, p.p, rdtau, FT(0),
                                                    rdp);
         check_launch();
     }
@@ -718,7 +767,7 @@ struct ModelImpl : gbo_model {
         k_cg_scale<FT><<<lin, 256, 0, stream>>>(p.p, cg_x.p, FT(dtp), N, scp);
         check_launch();
         pre(G_SOURCE);
-        k_source<FT><<<grd(), blk(), 0, stream>>>(gp, ui, vi, wi, cg_b.p, SRC_CG);
+        k_source<FT><<<col_grid(), blk(), 0, stream>>>(gp, ui, vi, wi, cg_b.p, SRC_CG);
         check_launch();
         return cg_iterate();
     }

@@ -31,7 +31,7 @@ struct Met {
     GBO_D FT Ay(int k) const { return g.dx * dzc(k); }   // Ayᶜᶠᶜ
     GBO_D FT Ayf(int k) const { return g.dx * dzf(k); }  // Ayᶜᶠᶠ
     GBO_D FT Az() const { return g.dx * g.dy; }          // Azᶜᶜᵃ
-    GBO_D FT rVc(int k) const { return FT(1) / (Az() * dzc(k)); }
+    GBO_D FT rVc(int k) const { return g.flatz ? FT(1) / Az() : g.rvc[k + 1 + g.zoff]; }
     GBO_D FT rVf(int k) const { return FT(1) / (Az() * dzf(k)); }
 };
 

@@ -39,9 +39,11 @@ enum {
     CC_N
 };
 
-// z-slices per launch of the 3-D CG kernels: blocks march over k so that each
-// kernel issues a few thousand block reductions, not one per (tile, level)
+// z-slices per launch of the 3-D CG kernels: blocks march over a contiguous slice of
+// levels so that each kernel issues a few thousand block reductions, not one per
+// (tile, level); the streaming kernels load CG_UNROLL levels before storing them
 constexpr int CG_ZSLICES = 8;
+constexpr int CG_UNROLL = 4;
 
 GBO_D double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -181,6 +183,7 @@ __global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, siz
         if (use_handle) cudaGraphSetConditional(h, 0u);
     }
     FT acc = FT(0), acc2 = FT(0);  // per-thread partial sums in FT (a few terms), FP64 across threads
+#pragma unroll 4
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         acc += a[t] * b[t];
         if (rprev) acc2 += a[t] * rprev[t];
@@ -249,9 +252,15 @@ __global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __rest
             const size_t at = col + plane * kk;
             return first ? z[at] : z[at] + beta * pold[at];
         };
-        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
+        // this block's contiguous slice of levels; p below, at and above the level roll
+        // through registers
+        const int per = (g.Nz + (int)gridDim.z - 1) / (int)gridDim.z;
+        const int k0 = blockIdx.z * per, k1 = min(g.Nz, k0 + per);
+        FT pc = k0 < k1 ? pn(c.C, k0) : FT(0);
+        FT pb = k0 > 0 && k0 < k1 ? pn(c.C, k0 - 1) : pc;
+        for (int k = k0; k < k1; ++k) {
             const FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
-            const FT pc = pn(c.C, k);
+            const FT pt = k < g.Nz - 1 ? pn(c.C, k + 1) : pc;
             const FT pw = pn(c.W, k), pe = pn(c.E, k), ps = pn(c.S, k), pnn = pn(c.N, k);
             const bool im = k < c.kC;
             const FT fw = (im || k < c.kW) ? FT(0) : Ax * ((pc - pw) * g.rdx);
@@ -260,8 +269,6 @@ __global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __rest
             const FT fn = (im || k < c.kN) ? FT(0) : Ay * ((pnn - pc) * g.rdy);
             FT dz = FT(0);
             if (!g.flatz) {
-                const FT pb = k > 0 ? pn(c.C, k - 1) : pc;
-                const FT pt = k < g.Nz - 1 ? pn(c.C, k + 1) : pc;
                 const FT fb = (im || k - 1 < c.kC) ? FT(0) : Az * ((pc - pb) * M.rdzf(k));
                 const FT ft = (im || k + 1 < c.kC) ? FT(0) : Az * ((pt - pc) * M.rdzf(k + 1));
                 dz = ft - fb;
@@ -271,6 +278,8 @@ __global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __rest
             pnew[idx] = pc;
             q[idx] = val;
             acc += pc * val;
+            pb = pc;
+            pc = pt;
         }
     }
     block_add((double)acc, s + CG_PQ);
@@ -292,15 +301,29 @@ __global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__
     FT ax = FT(0), ar = FT(0);
     if (in) {
         const int kb = g.kbot ? __ldg(g.kbot + i + (size_t)g.Nx * j) : 0;
-        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
-            const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-            const FT xv = x[idx] + alpha * p[idx];
-            const FT rold = r[idx];
-            const FT rv = rold - alpha * q[idx];
-            if (rprev) rprev[idx] = rold;
-            x[idx] = xv;
-            r[idx] = rv;
-            if (k >= kb) { ax += xv; ar += rv; }
+        const size_t plane = (size_t)g.Nx * g.Ny, c = i + (size_t)g.Nx * j;
+        const int per = (g.Nz + (int)gridDim.z - 1) / (int)gridDim.z;
+        const int k0 = blockIdx.z * per, k1 = min(g.Nz, k0 + per);
+        // groups of CG_UNROLL levels: every load of the group before its stores
+        for (int ka = k0; ka < k1; ka += CG_UNROLL) {
+            FT xs[CG_UNROLL], rs[CG_UNROLL], ps[CG_UNROLL], qs[CG_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CG_UNROLL; ++u) {
+                const size_t idx = c + plane * (ka + u);
+                if (ka + u < k1) { xs[u] = x[idx]; rs[u] = r[idx]; ps[u] = p[idx]; qs[u] = q[idx]; }
+            }
+#pragma unroll
+            for (int u = 0; u < CG_UNROLL; ++u) {
+                const int k = ka + u;
+                if (k >= k1) break;
+                const size_t idx = c + plane * k;
+                const FT xv = xs[u] + alpha * ps[u];
+                const FT rv = rs[u] - alpha * qs[u];
+                if (rprev) rprev[idx] = rs[u];
+                x[idx] = xv;
+                r[idx] = rv;
+                if (k >= kb) { ax += xv; ar += rv; }
+            }
         }
     }
     block_add((double)ax, s + CG_SX, (double)ar, s + CG_SR);
@@ -328,15 +351,29 @@ __global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, 
     FT acc = FT(0);
     if (in) {
         const int kb = g.kbot ? __ldg(g.kbot + i + (size_t)g.Nx * j) : 0;
-        for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
-            const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-            const FT act = k < kb ? FT(0) : FT(1);
-            x[idx] = (x[idx] - mx) * act;
-            const FT rv = (r[idx] - mr) * act;
-            r[idx] = rv;
-            const FT vr = rv * M.rVc(k);
-            if (out) out[idx] = precond_source(M, vr, k, dz_scale);
-            acc += vr * vr;
+        const size_t plane = (size_t)g.Nx * g.Ny, c = i + (size_t)g.Nx * j;
+        const int per = (g.Nz + (int)gridDim.z - 1) / (int)gridDim.z;
+        const int k0 = blockIdx.z * per, k1 = min(g.Nz, k0 + per);
+        for (int ka = k0; ka < k1; ka += CG_UNROLL) {
+            FT xs[CG_UNROLL], rs[CG_UNROLL];
+#pragma unroll
+            for (int u = 0; u < CG_UNROLL; ++u) {
+                const size_t idx = c + plane * (ka + u);
+                if (ka + u < k1) { xs[u] = x[idx]; rs[u] = r[idx]; }
+            }
+#pragma unroll
+            for (int u = 0; u < CG_UNROLL; ++u) {
+                const int k = ka + u;
+                if (k >= k1) break;
+                const size_t idx = c + plane * k;
+                const FT act = k < kb ? FT(0) : FT(1);
+                x[idx] = (xs[u] - mx) * act;
+                const FT rv = (rs[u] - mr) * act;
+                r[idx] = rv;
+                const FT vr = rv * M.rVc(k);
+                if (out) out[idx] = precond_source(M, vr, k, dz_scale);
+                acc += vr * vr;
+            }
         }
     }
     block_add((double)acc, s + CG_NORM2);

@@ -12,6 +12,8 @@
 // per block); the last block of each reduction forms the derived scalar (β, α,
 // the gauge means) once instead of every thread dividing.
 #pragma once
+#include <type_traits>
+
 #include "gbo_tendency.cuh"
 
 // scalar slots
@@ -182,14 +184,38 @@ __global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, siz
         s[CG_CONT] = 0.0;
         if (use_handle) cudaGraphSetConditional(h, 0u);
     }
-    FT acc = FT(0), acc2 = FT(0);  // per-thread partial sums in FT (a few terms), FP64 across threads
-#pragma unroll 4
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-        acc += a[t] * b[t];
-        if (rprev) acc2 += a[t] * rprev[t];
+    // 16-byte vectors (4 floats or 2 doubles): each vector's products summed in FT, the
+    // running sums in FP64
+    double acc = 0.0, acc2 = 0.0;
+    const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    constexpr int W = 16 / sizeof(FT);
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                           reinterpret_cast<uintptr_t>(rprev)) & 15) == 0;
+    size_t head = 0;
+    if (aligned) {
+        using V = typename std::conditional<sizeof(FT) == 4, float4, double2>::type;
+        const V* av = reinterpret_cast<const V*>(a);
+        const V* bv = reinterpret_cast<const V*>(b);
+        const V* pv = reinterpret_cast<const V*>(rprev);
+        const size_t nv = n / W;
+        auto dot = [](const V& x, const V& y) {
+            if constexpr (sizeof(FT) == 4) return (double)(x.x * y.x + x.y * y.y + x.z * y.z + x.w * y.w);
+            else return x.x * y.x + x.y * y.y;
+        };
+#pragma unroll 2
+        for (size_t t = gid; t < nv; t += stride) {
+            const V x = av[t];
+            acc += dot(x, bv[t]);
+            if (rprev) acc2 += dot(x, pv[t]);
+        }
+        head = nv * W;
     }
-    if (rprev) block_add((double)acc, s + CG_RHO0 + par, (double)acc2, s + CG_ZRP);
-    else block_add((double)acc, s + CG_RHO0 + par);
+    for (size_t t = head + gid; t < n; t += stride) {
+        acc += (double)(a[t] * b[t]);
+        if (rprev) acc2 += (double)(a[t] * rprev[t]);
+    }
+    if (rprev) block_add(acc, s + CG_RHO0 + par, acc2, s + CG_ZRP);
+    else block_add(acc, s + CG_RHO0 + par);
     if (last_block(cnt + CC_DOT) && threadIdx.x == 0) {
         const bool first = s[CG_IT] == 0.0;
         const double rho = ldcg(s + CG_RHO0 + par), prev = ldcg(s + CG_RHO0 + (par ^ 1));

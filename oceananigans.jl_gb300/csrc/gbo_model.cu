@@ -136,9 +136,17 @@ __global__ void k_scale_dzc(GridP<FT> g, FT* __restrict__ a) {
 
 template <typename FT>
 __global__ void k_copy(const FT* __restrict__ a, FT* __restrict__ b, size_t n) {
-    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (; t < n; t += stride) b[t] = a[t];
+    const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    // 16-byte vectors where both arrays allow it, then the remainder
+    size_t head = 0;
+    if (((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0) {
+        const size_t nv = n * sizeof(FT) / 16;
+        const uint4* av = reinterpret_cast<const uint4*>(a);
+        uint4* bv = reinterpret_cast<uint4*>(b);
+        for (size_t t = gid; t < nv; t += stride) bv[t] = av[t];
+        head = nv * 16 / sizeof(FT);
+    }
+    for (size_t t = head + gid; t < n; t += stride) b[t] = a[t];
 }
 
 template <typename FT>
@@ -1048,7 +1056,7 @@ struct ModelImpl : gbo_model {
         project(us.p, vs.p, flat ? nullptr : ws.p, 0.0, dtf + DTF_RDTAU + s, dtf + DTF_SCALE + s);
         for (int n = 0; n < ntr; ++n) {
             pre(G_COPY);
-            k_copy<FT><<<std::min<size_t>((N + 255) / 256, 4096), 256, 0, stream>>>(cs[n].p, c[n].p, N);
+            k_copy<FT><<<(unsigned)std::min<size_t>((N * sizeof(FT) / 16 + 255) / 256 + 1, 4 * 152 * 8), 256, 0, stream>>>(cs[n].p, c[n].p, N);
             check_launch();
         }
         mask_tracers();

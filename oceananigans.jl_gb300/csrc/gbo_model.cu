@@ -795,7 +795,10 @@ struct ModelImpl : gbo_model {
         }
         FT* rprev = net ? cg_rp.p : nullptr;
         pre(G_CG_DOT);
-        k_cg_dot<FT><<<lin, 256, 0, stream>>>(z, cg_r.p, N, s, cg_cnt.p, h, use_handle, rprev);
+        // one block per SM × 8: each thread sums several 16-byte vectors before the block
+        // reduction, so few blocks reach the FP64 atomics and the completion ticket
+        const unsigned dot_blocks = (unsigned)std::min<size_t>((N / 4 + 255) / 256 + 1, 152 * 8);
+        k_cg_dot<FT><<<dot_blocks, 256, 0, stream>>>(z, cg_r.p, N, s, cg_cnt.p, h, use_handle, rprev);
         check_launch();
         pre(G_CG_DIR);
         k_cg_direction<FT><<<cg_grid(), blk(), 0, stream>>>(gp, z, cg_d.p, cg_p1.p, cg_q.p, s, cg_cnt.p);

@@ -215,10 +215,21 @@ __global__ void k_hydrostatic(StepP<FT> P, FT* __restrict__ phy) {
     // ℑz(b) at the top face uses the mirrored halo b[Nz+1] = b[Nz]
     FT pk = -(FT(0.5) * (bk + bk)) * M.dzf(Nz);
     phy[col + plane * (Nz - 1)] = pk;
-    for (int k = Nz - 2; k >= 0; --k) {
-        FT bb = b[col + plane * k];
-        pk -= (FT(0.5) * (bb + bk)) * M.dzf(k + 1);
-        phy[col + plane * k] = pk;
-        bk = bb;
+    // one thread per column (few warps per SM): the levels are loaded eight at a time
+    // ahead of the scan so that the loads overlap
+    constexpr int U = 8;
+    for (int ka = Nz - 2; ka >= 0; ka -= U) {
+        FT bs[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (ka - u >= 0) bs[u] = b[col + plane * (ka - u)];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = ka - u;
+            if (k < 0) break;
+            pk -= (FT(0.5) * (bs[u] + bk)) * M.dzf(k + 1);
+            phy[col + plane * k] = pk;
+            bk = bs[u];
+        }
     }
 }

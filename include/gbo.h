@@ -46,7 +46,8 @@ enum gbo_topology   { GBO_FLAT = 0, GBO_PERIODIC = 1, GBO_BOUNDED = 2 };
 enum gbo_float_type { GBO_FLOAT32 = 4, GBO_FLOAT64 = 8 };
 enum gbo_advection  { GBO_ADVECTION_NONE = 0, GBO_ADVECTION_CENTERED2 = 2, GBO_ADVECTION_WENO5 = 5 };
 enum gbo_closure    { GBO_CLOSURE_NONE = 0, GBO_CLOSURE_SMAGORINSKY_LILLY = 1,
-                      GBO_CLOSURE_AMD = 2, GBO_CLOSURE_SCALAR_DIFFUSIVITY = 3 };
+                      GBO_CLOSURE_AMD = 2, GBO_CLOSURE_SCALAR_DIFFUSIVITY = 3,
+                      GBO_CLOSURE_DYNAMIC_SMAGORINSKY = 4 };
 enum gbo_timestepper { GBO_TIMESTEPPER_RK3 = 0, GBO_TIMESTEPPER_QAB2 = 1 };
 enum gbo_solver     { GBO_SOLVER_FFT = 0, GBO_SOLVER_FOURIER_TRIDIAGONAL = 1,
                       GBO_SOLVER_CONJUGATE_GRADIENT = 2 };
@@ -108,6 +109,12 @@ typedef struct gbo_model_desc {
      * (src/TimeSteppers/quasi_adams_bashforth_2.jl:39-48; default χ = 0.1) */
     int32_t timestepper;             /* gbo_timestepper */
     double  ab2_chi;
+    /* DynamicSmagorinsky(averaging = (1, 2), schedule = IterationInterval(1)): the
+     * coefficient is averaged over x and y per level and recomputed at every state
+     * update; minimum_numerator bounds its numerator from below (1e-32)
+     * (turbulence_closure_implementations/Smagorinskys/dynamic_coefficient.jl:1-20,
+     * 215-275; scale_invariant_operators.jl).  Uses closure_Pr; ignores C and Cb. */
+    double  closure_min_numerator;
 } gbo_model_desc;
 
 typedef struct gbo_model gbo_model;

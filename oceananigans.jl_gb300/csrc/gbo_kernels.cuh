@@ -21,6 +21,7 @@ struct StepP {
     FT dt, gamma, zeta;
     const FT* dtf;                          // stage factors in device memory (Δt overrides dt)
     int first;
+    const FT* cs2;                          // DynamicSmagorinsky: c² per level (else null)
 };
 
 // ---------------------------------------------------------------------------
@@ -55,20 +56,26 @@ __global__ void k_smagorinsky(StepP<FT> P, FT* __restrict__ nu_out) {
     FT Sig2 = tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
     FT D3 = g.dx * g.dy * M.dzc(k);
     FT Df = cbrt(D3);
-    FT N2 = FT(0);
-    if (P.buoyancy && !g.flatz) {
-        CFld<FT> b = cfld(P.b, g);
-        // N² = ℑz(∂z b), conditional ∂ on an immersed grid
-        FT b1 = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (b(i, j, k) - b(i, j, k - 1)) * M.rdzf(k);
-        FT b2 = cond_zero(g, i, j, k, i, j, k + 1) ? FT(0) : (b(i, j, k + 1) - b(i, j, k)) * M.rdzf(k + 1);
-        N2 = FT(0.5) * (b1 + b2);
+    FT cs2;
+    if (P.cs2) {
+        // DynamicSmagorinsky: the level's averaged coefficient (k_dyn_coef)
+        cs2 = P.cs2[k];
+    } else {
+        FT N2 = FT(0);
+        if (P.buoyancy && !g.flatz) {
+            CFld<FT> b = cfld(P.b, g);
+            // N² = ℑz(∂z b), conditional ∂ on an immersed grid
+            FT b1 = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (b(i, j, k) - b(i, j, k - 1)) * M.rdzf(k);
+            FT b2 = cond_zero(g, i, j, k, i, j, k + 1) ? FT(0) : (b(i, j, k + 1) - b(i, j, k)) * M.rdzf(k + 1);
+            N2 = FT(0.5) * (b1 + b2);
+        }
+        FT N2p = fmax(FT(0), N2);
+        FT r = P.Cb * N2p / Sig2;
+        FT mn = isnan(r) ? r : fmin(FT(1), r);
+        FT vs2 = FT(1) - mn;
+        FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
+        cs2 = vs * (P.C * P.C);
     }
-    FT N2p = fmax(FT(0), N2);
-    FT r = P.Cb * N2p / Sig2;
-    FT mn = isnan(r) ? r : fmin(FT(1), r);
-    FT vs2 = FT(1) - mn;
-    FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
-    FT cs2 = vs * (P.C * P.C);
     nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * (Df * Df) * sqrt(FT(2) * Sig2);
 }
 

@@ -13,6 +13,7 @@
 #include "gbo_sim.cuh"
 #include "gbo_learned.cuh"
 #include "gbo_fused.cuh"
+#include "gbo_dynamic.cuh"
 
 // ===========================================================================
 // Pressure source and projection kernels
@@ -397,6 +398,9 @@ struct ModelImpl : gbo_model {
     // state and work arrays
     DBuf<FT> u, v, w, us, vs, ws, Gu, Gv, Gw, nu, phy, p;
     std::vector<DBuf<FT>> c, cs, Gc, kap;
+    // DynamicSmagorinsky: Σ, Σ̄, per-tile LM/MM sums, and per level c², 𝒥ᴸᴹ, 𝒥ᴹᴹ
+    DBuf<FT> dyn_sig, dyn_sigb, dyn_cs2, dyn_jlm, dyn_jmm;
+    DBuf<double> dyn_part;
     // grid tables
     DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf, t_rvc;
     DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64, t_ws;
@@ -547,6 +551,12 @@ struct ModelImpl : gbo_model {
             kap.resize(ntr);
             for (int n = 0; n < ntr; ++n) kap[n].alloc(N);
         }
+        if (md->closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
+            dyn_sig.alloc(N);
+            dyn_sigb.alloc(N);
+            dyn_part.alloc((size_t)2 * Nz * ((Nx + dyn::TX - 1) / dyn::TX) * ((Ny + dyn::TY - 1) / dyn::TY));
+            for (DBuf<FT>* b : {&dyn_cs2, &dyn_jlm, &dyn_jmm}) b->alloc(Nz);
+        }
         if (scalar) {
             kap.resize(ntr);
             // constant ν and κ held as fields: the AMD flux code reads them, and ν at
@@ -674,6 +684,7 @@ struct ModelImpl : gbo_model {
     // ν and κ fields (viscous fluxes 2νΣᵢⱼ and diffusive fluxes κ∂c of
     // abstract_scalar_diffusivity_closure.jl:214-262 for every AbstractScalarDiffusivity)
     int kernel_closure() const {
+        if (desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) return CL_SMAG;  // the νₑ fluxes of every Smagorinsky
         return desc.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY ? (int)CL_AMD : desc.closure;
     }
 
@@ -985,6 +996,26 @@ struct ModelImpl : gbo_model {
         } else if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
             pre(G_CLOSURE);
             k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemS<FT>), stream>>>(P, nu.p);
+            check_launch();
+        } else if (desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
+            // Σ and Σ̄, the tile sums of LM and MM, the per-level coefficient, then νₑ
+            // (compute_coefficient_fields!, dynamic_coefficient.jl:225-250; smagorinsky.jl:90-104)
+            const dim3 dg((Nx + dyn::TX - 1) / dyn::TX, (Ny + dyn::TY - 1) / dyn::TY, Nz), db(dyn::TX, dyn::TY);
+            pre(G_CLOSURE);
+            k_dyn_sigma<FT><<<dg, db, 0, stream>>>(P, dyn_sig.p, dyn_sigb.p);
+            check_launch();
+            pre(G_CLOSURE);
+            k_dyn_lm<FT><<<dg, db, 0, stream>>>(P, dyn_sig.p, dyn_sigb.p, dyn_part.p);
+            check_launch();
+            pre(G_CLOSURE);
+            k_dyn_coef<FT><<<Nz, dyn::COEF_THREADS, 0, stream>>>(dyn_part.p, (int)(dg.x * dg.y), (double)Nx * (double)Ny,
+                                                                 FT(desc.closure_min_numerator), dyn_cs2.p, dyn_jlm.p,
+                                                                 dyn_jmm.p);
+            check_launch();
+            StepP<FT> Q = P;
+            Q.cs2 = dyn_cs2.p;
+            pre(G_CLOSURE);
+            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;
@@ -1688,7 +1719,12 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
         for (int k = 0; k < nz; ++k)
             if (!(g->z_faces[k + 1] > g->z_faces[k])) return "z_faces must be increasing";
     if (d->advection != GBO_ADVECTION_WENO5) return "only WENO(order=5) advection is implemented";
-    if (d->closure < 0 || d->closure > 3) return "unknown closure";
+    if (d->closure < 0 || d->closure > 4) return "unknown closure";
+    if (d->closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
+        if (g->topology[2] != GBO_BOUNDED) return "DynamicSmagorinsky requires a three-dimensional grid with Bounded z";
+        if (g->bottom_height) return "DynamicSmagorinsky is not available on an ImmersedBoundaryGrid";
+        if (!std::isfinite(d->closure_min_numerator)) return "DynamicSmagorinsky minimum_numerator must be finite";
+    }
     if (d->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
         if (!(d->closure_nu >= 0) || !std::isfinite(d->closure_nu)) return "ScalarDiffusivity ν must be finite and >= 0";
         for (int n = 0; n < d->ntracers && n < GBO_MAX_TRACERS; ++n)
@@ -1734,6 +1770,7 @@ void gbo_model_desc_default(gbo_model_desc* d) {
     d->preconditioner = GBO_PRECOND_FFT;
     d->timestepper = GBO_TIMESTEPPER_RK3;
     d->ab2_chi = 0.1;
+    d->closure_min_numerator = 1e-32;
 }
 
 int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out) {

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) k_sim_callbacks(SimP<FT> S, int mode, cud
         W[RUN_TAU_ADV] = (double)(FT(1) / FT(a0));
         const FT d2 = FT(W[RUN_DELTA2]);
         double dif = CUDART_INF;
-        if (S.closure == GBO_CLOSURE_SMAGORINSKY_LILLY) {
+        if (S.closure == GBO_CLOSURE_SMAGORINSKY_LILLY || S.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
             dif = (double)(d2 / (FT(a1) * FT(W[RUN_PR_FACTOR])));
         } else if (S.closure == GBO_CLOSURE_AMD) {
             // with no tracers the reference takes max κₑ = Inf, so Δ²/max κₑ = 0

@@ -151,6 +151,24 @@ class AnisotropicMinimumDissipation:
         self.C = float(C)
 
 
+class DynamicSmagorinsky:
+    """DynamicSmagorinsky(; averaging=(1, 2), Pr=1, schedule=IterationInterval(1),
+    minimum_numerator=1e-32) (turbulence_closure_implementations/Smagorinskys/
+    dynamic_coefficient.jl:104-117,215-300).  The coefficient is averaged over x and y per
+    level and recomputed at every state update; other averagings and schedules are not
+    available and raise ValueError."""
+
+    def __init__(self, averaging=(1, 2), Pr=1.0, minimum_numerator=1e-32, schedule=1):
+        avg = tuple(averaging) if isinstance(averaging, (tuple, list)) else (averaging,)
+        if tuple(sorted(avg)) != (1, 2):
+            raise ValueError("DynamicSmagorinsky: only averaging=(1, 2) is available on GB300")
+        if schedule != 1:
+            raise ValueError("DynamicSmagorinsky: only schedule=IterationInterval(1) is available on GB300")
+        self.averaging = (1, 2)
+        self.Pr = float(Pr)
+        self.minimum_numerator = float(minimum_numerator)
+
+
 class ScalarDiffusivity:
     """ScalarDiffusivity(; ν=0, κ=0) with constant coefficients, isotropic
     (ThreeDimensionalFormulation) and explicit (turbulence_closure_implementations/
@@ -250,6 +268,10 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
     elif isinstance(closure, AnisotropicMinimumDissipation):
         d.closure = L.GBO_CLOSURE_AMD
         d.closure_C = closure.C
+    elif isinstance(closure, DynamicSmagorinsky):
+        d.closure = L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY
+        d.closure_Pr = closure.Pr
+        d.closure_min_numerator = closure.minimum_numerator
     elif isinstance(closure, ScalarDiffusivity):
         d.closure = L.GBO_CLOSURE_SCALAR_DIFFUSIVITY
         d.closure_nu = closure.nu

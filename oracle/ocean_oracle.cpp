@@ -181,6 +181,8 @@ struct Model {
     int ntr = 0;
     Field u, v, w, p, phy, nu;
     std::vector<Field> c, kappa;                    // tracers and AMD diffusivities
+    Field sig, sigb;                                // DynamicSmagorinsky: Σ and Σ̄
+    std::vector<double> dyn_cs2;                    // DynamicSmagorinsky: c² per level (1-based)
     std::vector<Field> Gn, Gm;                      // tendencies (u,v,w,tracers...)
     double time = 0;
     int64_t iteration = 0;
@@ -837,6 +839,151 @@ double smagorinsky_nu(const Ctx& C, int i, int j, int k) {
     return cs2 * (Df * Df) * std::sqrt(2 * Sig2);
 }
 
+// DynamicSmagorinsky with averaging = (1, 2) (Smagorinskys/dynamic_coefficient.jl:215-300;
+// scale_invariant_operators.jl:8-13,94-188): Σ = √(ΣᵢⱼΣᵢⱼ) and Σ̄ of the test-filtered
+// velocities, Lᵢⱼ and Mᵢⱼ per cell, their x-y means per level, c² = max(𝒥ᴸᴹ, min) / 𝒥ᴹᴹ
+// (0 where 𝒥ᴹᴹ ≤ 0), νₑ = c² Δᶠ² √(2Σ²).  Halo reads follow the stored fields: one
+// mirrored layer beyond the z walls, zeros further out.
+template <class ST>
+double strain_sq(const ST& S, int i, int j, int k) {
+    auto sq = [](double x) { return x * x; };
+    double s11 = S.S11(i, j, k), s22 = S.S22(i, j, k), s33 = S.S33(i, j, k);
+    double tr = s11 * s11 + s22 * s22 + s33 * s33;
+    double ixy = 0.5 * (0.5 * (sq(S.S12(i, j, k)) + sq(S.S12(i + 1, j, k))) + 0.5 * (sq(S.S12(i, j + 1, k)) + sq(S.S12(i + 1, j + 1, k))));
+    double ixz = 0.5 * (0.5 * (sq(S.S13(i, j, k)) + sq(S.S13(i + 1, j, k))) + 0.5 * (sq(S.S13(i, j, k + 1)) + sq(S.S13(i + 1, j, k + 1))));
+    double iyz = 0.5 * (0.5 * (sq(S.S23(i, j, k)) + sq(S.S23(i, j + 1, k))) + 0.5 * (sq(S.S23(i, j, k + 1)) + sq(S.S23(i, j + 1, k + 1))));
+    return tr + 2 * ixy + 2 * ixz + 2 * iyz;
+}
+
+// filter(i, j, k, grid, f) = (6 f + the six face neighbours) / 12 (scale_invariant_operators.jl:94-104)
+template <class F>
+double test_filter(const F& f, int i, int j, int k) {
+    return (6 * f(i, j, k) + f(i + 1, j, k) + f(i - 1, j, k) + f(i, j + 1, k) + f(i, j - 1, k) + f(i, j, k + 1) + f(i, j, k - 1)) / 12;
+}
+
+// Σ̄ᵢⱼ: the strain of the filtered velocities at the reference's locations (:110-150)
+struct FiltStrain {
+    const Ctx& C;
+    double fu(int i, int j, int k) const { return test_filter([&](int a, int b, int c) { return C.m.u(a, b, c); }, i, j, k); }
+    double fv(int i, int j, int k) const { return test_filter([&](int a, int b, int c) { return C.m.v(a, b, c); }, i, j, k); }
+    double fw(int i, int j, int k) const { return test_filter([&](int a, int b, int c) { return C.m.w(a, b, c); }, i, j, k); }
+    double S11(int i, int j, int k) const { return (fu(i + 1, j, k) - fu(i, j, k)) * (1 / C.g.dx); }
+    double S22(int i, int j, int k) const { return (fv(i, j + 1, k) - fv(i, j, k)) * (1 / C.g.dy); }
+    double S33(int i, int j, int k) const { return (fw(i, j, k + 1) - fw(i, j, k)) * (1 / C.M.dzc(k)); }
+    double S12(int i, int j, int k) const {
+        return 0.5 * ((fu(i, j, k) - fu(i, j - 1, k)) * (1 / C.g.dy) + (fv(i, j, k) - fv(i - 1, j, k)) * (1 / C.g.dx));
+    }
+    double S13(int i, int j, int k) const {
+        return 0.5 * ((fu(i, j, k) - fu(i, j, k - 1)) * (1 / C.M.dzf(k)) + (fw(i, j, k) - fw(i - 1, j, k)) * (1 / C.g.dx));
+    }
+    double S23(int i, int j, int k) const {
+        return 0.5 * ((fv(i, j, k) - fv(i, j, k - 1)) * (1 / C.M.dzf(k)) + (fw(i, j, k) - fw(i, j - 1, k)) * (1 / C.g.dy));
+    }
+};
+
+// LM_and_MM (dynamic_coefficient.jl:254-276): Lᵢⱼ = ⟨uᵢuⱼ⟩ − ⟨uᵢ⟩⟨uⱼ⟩ from cell-centre
+// products, Mᵢⱼ = 2Δᶠ² (⟨Σ Σᵢⱼ⟩ − ᾱ²β Σ̄ Σ̄ᵢⱼ) with ᾱ² = 4, β = 1 (scale_invariant_operators.jl:152-188)
+void lm_mm(const Ctx& C, const FiltStrain& B, int i, int j, int k, double& LM, double& MM) {
+    const Model& m = C.m;
+    const Field &u = m.u, &v = m.v, &w = m.w, &sg = m.sig, &sb = m.sigb;
+    auto sq = [](double x) { return x * x; };
+    auto ixu = [&](int a, int b, int c) { return 0.5 * (u(a, b, c) + u(a + 1, b, c)); };
+    auto iyv = [&](int a, int b, int c) { return 0.5 * (v(a, b, c) + v(a, b + 1, c)); };
+    auto izw = [&](int a, int b, int c) { return 0.5 * (w(a, b, c) + w(a, b, c + 1)); };
+    auto u1u1 = [&](int a, int b, int c) { return 0.5 * (sq(u(a, b, c)) + sq(u(a + 1, b, c))); };
+    auto u2u2 = [&](int a, int b, int c) { return 0.5 * (sq(v(a, b, c)) + sq(v(a, b + 1, c))); };
+    auto u3u3 = [&](int a, int b, int c) { return 0.5 * (sq(w(a, b, c)) + sq(w(a, b, c + 1))); };
+    auto u1u2 = [&](int a, int b, int c) { return ixu(a, b, c) * iyv(a, b, c); };
+    auto u1u3 = [&](int a, int b, int c) { return ixu(a, b, c) * izw(a, b, c); };
+    auto u2u3 = [&](int a, int b, int c) { return iyv(a, b, c) * izw(a, b, c); };
+    double fu0 = B.fu(i, j, k), fu1 = B.fu(i + 1, j, k);
+    double fv0 = B.fv(i, j, k), fv1 = B.fv(i, j + 1, k);
+    double fw0 = B.fw(i, j, k), fw1 = B.fw(i, j, k + 1);
+    double ixfu = 0.5 * (fu0 + fu1), iyfv = 0.5 * (fv0 + fv1), izfw = 0.5 * (fw0 + fw1);
+    double L11 = test_filter(u1u1, i, j, k) - 0.5 * (sq(fu0) + sq(fu1));
+    double L22 = test_filter(u2u2, i, j, k) - 0.5 * (sq(fv0) + sq(fv1));
+    double L33 = test_filter(u3u3, i, j, k) - 0.5 * (sq(fw0) + sq(fw1));
+    double L12 = test_filter(u1u2, i, j, k) - ixfu * iyfv;
+    double L13 = test_filter(u1u3, i, j, k) - ixfu * izfw;
+    double L23 = test_filter(u2u3, i, j, k) - iyfv * izfw;
+    // ℑxyᶜᶜᵃ = ℑyᵃᶜᵃ ∘ ℑxᶜᵃᵃ etc. (interpolation_operators.jl:45-53)
+    auto ixy = [](auto f, int a, int b, int c) { return 0.5 * (0.5 * (f(a, b, c) + f(a + 1, b, c)) + 0.5 * (f(a, b + 1, c) + f(a + 1, b + 1, c))); };
+    auto ixz = [](auto f, int a, int b, int c) { return 0.5 * (0.5 * (f(a, b, c) + f(a + 1, b, c)) + 0.5 * (f(a, b, c + 1) + f(a + 1, b, c + 1))); };
+    auto iyz = [](auto f, int a, int b, int c) { return 0.5 * (0.5 * (f(a, b, c) + f(a, b + 1, c)) + 0.5 * (f(a, b, c + 1) + f(a, b + 1, c + 1))); };
+    auto s12 = [&](int a, int b, int c) { return C.S12(a, b, c); };
+    auto s13 = [&](int a, int b, int c) { return C.S13(a, b, c); };
+    auto s23 = [&](int a, int b, int c) { return C.S23(a, b, c); };
+    auto b12 = [&](int a, int b, int c) { return B.S12(a, b, c); };
+    auto b13 = [&](int a, int b, int c) { return B.S13(a, b, c); };
+    auto b23 = [&](int a, int b, int c) { return B.S23(a, b, c); };
+    auto ss11 = [&](int a, int b, int c) { return sg(a, b, c) * C.S11(a, b, c); };
+    auto ss22 = [&](int a, int b, int c) { return sg(a, b, c) * C.S22(a, b, c); };
+    auto ss33 = [&](int a, int b, int c) { return sg(a, b, c) * C.S33(a, b, c); };
+    auto ss12 = [&](int a, int b, int c) { return sg(a, b, c) * ixy(s12, a, b, c); };
+    auto ss13 = [&](int a, int b, int c) { return sg(a, b, c) * ixz(s13, a, b, c); };
+    auto ss23 = [&](int a, int b, int c) { return sg(a, b, c) * iyz(s23, a, b, c); };
+    double sbar = sb(i, j, k);
+    double bb11 = sbar * B.S11(i, j, k), bb22 = sbar * B.S22(i, j, k), bb33 = sbar * B.S33(i, j, k);
+    double bb12 = sbar * ixy(b12, i, j, k), bb13 = sbar * ixz(b13, i, j, k), bb23 = sbar * iyz(b23, i, j, k);
+    double Df = std::cbrt(C.g.dx * C.g.dy * C.M.dzc(k));  // ∛volume
+    double f2 = 2 * (Df * Df);
+    double M11 = f2 * (test_filter(ss11, i, j, k) - 4 * bb11);
+    double M22 = f2 * (test_filter(ss22, i, j, k) - 4 * bb22);
+    double M33 = f2 * (test_filter(ss33, i, j, k) - 4 * bb33);
+    double M12 = f2 * (test_filter(ss12, i, j, k) - 4 * bb12);
+    double M13 = f2 * (test_filter(ss13, i, j, k) - 4 * bb13);
+    double M23 = f2 * (test_filter(ss23, i, j, k) - 4 * bb23);
+    LM = L11 * M11 + L22 * M22 + L33 * M33 + 2 * L12 * M12 + 2 * L13 * M13 + 2 * L23 * M23;
+    MM = M11 * M11 + M22 * M22 + M33 * M33 + 2 * M12 * M12 + 2 * M13 * M13 + 2 * M23 * M23;
+}
+
+void dynamic_smagorinsky(Model& m) {
+    Ctx C(m);
+    const Grid& g = m.g;
+    FiltStrain B{C};
+    // _compute_Σ!, _compute_Σ̄! over the interior, then their halos
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                m.sig.at(i, j, k) = std::sqrt(strain_sq(C, i, j, k));
+                m.sigb.at(i, j, k) = std::sqrt(strain_sq(B, i, j, k));
+            }
+    fill_halos(m, m.sig, 0);
+    fill_halos(m, m.sigb, 0);
+    const size_t plane = (size_t)g.Nx * g.Ny;
+    std::vector<double> LM(plane * g.Nz), MM(plane * g.Nz);
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                size_t q = (size_t)(i - 1) + (size_t)g.Nx * (j - 1) + plane * (k - 1);
+                lm_mm(C, B, i, j, k, LM[q], MM[q]);
+            }
+    // 𝒥ᴸᴹ, 𝒥ᴹᴹ = Average over x and y; square_smagorinsky_coefficient (dynamic_coefficient.jl:236-248)
+    const double lmin = m.desc.closure_min_numerator;
+    m.dyn_cs2.assign(g.Nz + 1, 0.0);
+    for (int k = 1; k <= g.Nz; ++k) {
+        double a = 0, b = 0;
+        for (size_t q = 0; q < plane; ++q) {
+            a += LM[plane * (k - 1) + q];
+            b += MM[plane * (k - 1) + q];
+        }
+        double jlm = a / (double)plane, jmm = b / (double)plane;
+        double num = std::isnan(jlm) ? jlm : std::max(jlm, lmin);  // Julia's max propagates NaN
+        m.dyn_cs2[k] = jmm > 0 ? num / jmm : 0.0;                 // × (𝒥ᴹᴹ > 0), a strong zero
+    }
+    // _compute_smagorinsky_viscosity! (smagorinsky.jl:90-104)
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                double Df = std::cbrt(g.dx * g.dy * C.M.dzc(k));
+                m.nu.at(i, j, k) = m.dyn_cs2[k] * (Df * Df) * std::sqrt(2 * strain_sq(C, i, j, k));
+            }
+    fill_halos(m, m.nu, 0);
+}
+
 // AMD (anisotropic_minimum_dissipation.jl:161-204,243-358; velocity_tracer_gradients.jl:120-250)
 struct AMDops {
     const Ctx& C;
@@ -1122,6 +1269,10 @@ void compute_closure(Model& m) {
         // (scalar_diffusivity.jl:8-12; νᶜᶜᶜ(i, j, k, grid, closure::ScalarDiffusivity, ...) = ν)
         std::fill(m.nu.d.begin(), m.nu.d.end(), m.desc.closure_nu);
         for (int n = 0; n < m.ntr; ++n) std::fill(m.kappa[n].d.begin(), m.kappa[n].d.end(), m.desc.closure_kappa[n]);
+        return;
+    }
+    if (m.desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
+        dynamic_smagorinsky(m);
         return;
     }
     Ctx C(m);
@@ -1576,6 +1727,10 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
     m->p.init(g.Nx, g.Ny, g.Nz, H, Hz);
     m->phy.init(g.Nx, g.Ny, g.Nz, H, Hz);
     m->nu.init(g.Nx, g.Ny, g.Nz, H, Hz);
+    if (md->closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
+        m->sig.init(g.Nx, g.Ny, g.Nz, H, Hz);
+        m->sigb.init(g.Nx, g.Ny, g.Nz, H, Hz);
+    }
     m->c.resize(m->ntr);
     for (auto& f : m->c) f.init(g.Nx, g.Ny, g.Nz, H, Hz);
     if (md->closure == GBO_CLOSURE_AMD || md->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {

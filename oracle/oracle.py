@@ -41,7 +41,8 @@ class ModelDesc(ctypes.Structure):
                 ("pressure_solver", ctypes.c_int32), ("preconditioner", ctypes.c_int32),
                 ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32),
                 ("closure_nu", ctypes.c_double), ("closure_kappa", ctypes.c_double * MAX_TRACERS),
-                ("timestepper", ctypes.c_int32), ("ab2_chi", ctypes.c_double)]
+                ("timestepper", ctypes.c_int32), ("ab2_chi", ctypes.c_double),
+                ("closure_min_numerator", ctypes.c_double)]
 
 
 def build(force=False):
@@ -217,7 +218,7 @@ def cell_advection_timescale(ref):
 
 def cell_diffusion_timescale(ref):
     """Diffusion timescale of the closure (TurbulenceClosures/turbulence_closure_diagnostics.jl:8-13,
-    48-63): Δ² / (max νₑ max(1, 1/Pr)) for Smagorinsky-Lilly, min(Δ²/max νₑ, Δ²/max κₑ) for AMD
+    48-63): Δ² / (max νₑ max(1, 1/Pr)) for Smagorinsky (Lilly or dynamic), min(Δ²/max νₑ, Δ²/max κₑ) for AMD
     (max κₑ = Inf without tracers), Inf without a closure; Δ = min(Δx, Δy, min Δzᶜ)."""
     g, d = ref.grid, ref.desc
     if d.closure == 0:
@@ -231,7 +232,7 @@ def cell_diffusion_timescale(ref):
     d2 = np.float64(D * D)
     numax = np.max(ref.get("nu"))
     with np.errstate(divide="ignore"):  # Δ²/0 = Inf as in Julia
-        if d.closure == 1:
+        if d.closure in (1, 4):  # every Smagorinsky, the dynamic one included
             pr = d.closure_Pr if d.ntracers > 0 else 1.0
             return float(d2 / (numax * max(1.0, 1 / pr)))
         kmax = np.max(ref.get("kappa")) if d.ntracers > 0 else np.inf

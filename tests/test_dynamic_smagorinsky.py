@@ -1,0 +1,169 @@
+"""DynamicSmagorinsky(averaging=(1, 2)) in the oracle, pinned against an independent
+numpy restatement of the reference's operators (Smagorinskys/dynamic_coefficient.jl:
+215-300, scale_invariant_operators.jl:8-13,94-188, smagorinsky.jl:90-104), plus the
+properties the reference's own tests check (test_turbulence_closures.jl:421-465: the
+closure builds and yields a non-zero eddy viscosity from random velocities) and the
+host-side validation of the C ABI.  The reference has no golden values for this closure.
+
+The numpy version stores every field with 3 halo levels in z (one mirrored layer beyond
+each wall for Center fields, zeros beyond it, w zero on and beyond the walls) and wraps
+x and y periodically, as the reference's fields are filled."""
+import numpy as np
+import pytest
+
+import cases
+import oceananigans_gb300 as og
+
+H = 3  # z halo levels of the padded arrays
+
+
+def _X(a, d):
+    return np.roll(a, -d, axis=0)
+
+
+def _Y(a, d):
+    return np.roll(a, -d, axis=1)
+
+
+def _Z(a, d):
+    out = np.zeros_like(a)
+    if d > 0:
+        out[:, :, :-d] = a[:, :, d:]
+    else:
+        out[:, :, -d:] = a[:, :, :d]
+    return out
+
+
+def _pad_center(c):
+    Nx, Ny, Nz = c.shape
+    p = np.zeros((Nx, Ny, Nz + 2 * H + 1))
+    p[:, :, H:H + Nz] = c
+    p[:, :, H - 1] = c[:, :, 0]
+    p[:, :, H + Nz] = c[:, :, -1]
+    return p
+
+
+def _pad_face(w):
+    Nx, Ny, Nf = w.shape
+    p = np.zeros((Nx, Ny, Nf + 2 * H))
+    p[:, :, H + 1:H + Nf - 1] = w[:, :, 1:-1]  # walls (faces 0 and Nz) stay zero
+    return p
+
+
+def _filt(a):
+    return (6 * a + _X(a, 1) + _X(a, -1) + _Y(a, 1) + _Y(a, -1) + _Z(a, 1) + _Z(a, -1)) / 12
+
+
+def _strain(U, V, W, dx, dy, dz):
+    s11 = (_X(U, 1) - U) / dx
+    s22 = (_Y(V, 1) - V) / dy
+    s33 = (_Z(W, 1) - W) / dz
+    s12 = 0.5 * ((U - _Y(U, -1)) / dy + (V - _X(V, -1)) / dx)
+    s13 = 0.5 * ((U - _Z(U, -1)) / dz + (W - _X(W, -1)) / dx)
+    s23 = 0.5 * ((V - _Z(V, -1)) / dz + (W - _Y(W, -1)) / dy)
+    return s11, s22, s33, s12, s13, s23
+
+
+def _ixy(q):
+    return 0.5 * (0.5 * (q + _X(q, 1)) + 0.5 * (_Y(q, 1) + _X(_Y(q, 1), 1)))
+
+
+def _ixz(q):
+    return 0.5 * (0.5 * (q + _X(q, 1)) + 0.5 * (_Z(q, 1) + _X(_Z(q, 1), 1)))
+
+
+def _iyz(q):
+    return 0.5 * (0.5 * (q + _Y(q, 1)) + 0.5 * (_Z(q, 1) + _Y(_Z(q, 1), 1)))
+
+
+def _sig2(s):
+    s11, s22, s33, s12, s13, s23 = s
+    return s11 ** 2 + s22 ** 2 + s33 ** 2 + 2 * _ixy(s12 ** 2) + 2 * _ixz(s13 ** 2) + 2 * _iyz(s23 ** 2)
+
+
+def numpy_dynamic_nu(u, v, w, L, min_numerator=1e-32):
+    """νₑ of DynamicSmagorinsky(averaging=(1, 2)) on a regular Periodic-Periodic-Bounded grid."""
+    Nx, Ny, Nz = u.shape
+    dx, dy, dz = L[0] / Nx, L[1] / Ny, L[2] / Nz
+    U, V, W = _pad_center(u), _pad_center(v), _pad_face(w)
+    interior = slice(H, H + Nz)
+    S = _strain(U, V, W, dx, dy, dz)
+    FU, FV, FW = _filt(U), _filt(V), _filt(W)
+    SB = _strain(FU, FV, FW, dx, dy, dz)
+    sig2 = _sig2(S)
+    SG = _pad_center(np.sqrt(sig2[:, :, interior]))
+    SBB = _pad_center(np.sqrt(_sig2(SB)[:, :, interior]))
+    # Leonard stresses from cell-centre products
+    ixu, iyv, izw = 0.5 * (U + _X(U, 1)), 0.5 * (V + _Y(V, 1)), 0.5 * (W + _Z(W, 1))
+    ixfu, iyfv, izfw = 0.5 * (FU + _X(FU, 1)), 0.5 * (FV + _Y(FV, 1)), 0.5 * (FW + _Z(FW, 1))
+    Ls = [_filt(0.5 * (U ** 2 + _X(U, 1) ** 2)) - 0.5 * (FU ** 2 + _X(FU, 1) ** 2),
+          _filt(0.5 * (V ** 2 + _Y(V, 1) ** 2)) - 0.5 * (FV ** 2 + _Y(FV, 1) ** 2),
+          _filt(0.5 * (W ** 2 + _Z(W, 1) ** 2)) - 0.5 * (FW ** 2 + _Z(FW, 1) ** 2),
+          _filt(ixu * iyv) - ixfu * iyfv,
+          _filt(ixu * izw) - ixfu * izfw,
+          _filt(iyv * izw) - iyfv * izfw]
+    s11, s22, s33, s12, s13, s23 = S
+    b11, b22, b33, b12, b13, b23 = SB
+    ss = [SG * s11, SG * s22, SG * s33, SG * _ixy(s12), SG * _ixz(s13), SG * _iyz(s23)]
+    bb = [SBB * b11, SBB * b22, SBB * b33, SBB * _ixy(b12), SBB * _ixz(b13), SBB * _iyz(b23)]
+    Df = np.cbrt(dx * dy * dz)
+    Ms = [2 * Df ** 2 * (_filt(a) - 4 * b) for a, b in zip(ss, bb)]
+    wts = [1, 1, 1, 2, 2, 2]
+    LM = sum(c * l * m for c, l, m in zip(wts, Ls, Ms))[:, :, interior]
+    MM = sum(c * m * m for c, m in zip(wts, Ms))[:, :, interior]
+    jlm, jmm = LM.mean(axis=(0, 1)), MM.mean(axis=(0, 1))
+    num = np.maximum(jlm, min_numerator)
+    cs2 = np.where(jmm > 0, num / np.where(jmm > 0, jmm, 1.0), 0.0)
+    return cs2[None, None, :] * Df ** 2 * np.sqrt(2 * sig2[:, :, interior])
+
+
+def _random_case(N=(12, 10, 8), seed=3, U0=0.3):
+    c = cases.convection_3d(N, closure="dynamic", f=0.0, flux=0.0, U0=U0, seed=seed)
+    w = c.init["w"].copy()
+    w[:, :, 0] = 0.0
+    w[:, :, -1] = 0.0
+    c.init["w"] = w
+    return c
+
+
+def test_oracle_matches_numpy_restatement():
+    c = _random_case()
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(False)
+    nu = numpy_dynamic_nu(c.init["u"], c.init["v"], c.init["w"], (512.0, 512.0, 256.0))
+    got = ref.get("nu")
+    assert np.any(nu > 0)
+    assert cases.rel_l2(got, nu) <= 1e-13
+
+
+def test_dynamic_viscosity_nonnegative_and_nonzero_from_random_velocities():
+    # test_turbulence_closures.jl:457-465 checks a non-zero νₑ after random velocities
+    c = _random_case(N=(16, 16, 8), seed=11)
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(True)
+    nu = ref.get("nu")
+    assert np.all(nu >= 0) and np.any(nu > 0)
+
+
+def test_zero_flow_has_zero_viscosity():
+    c = _random_case(U0=0.0)
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(False)
+    assert np.all(ref.get("nu") == 0.0)
+
+
+def test_unsupported_averaging_and_grids_rejected():
+    with pytest.raises(ValueError, match="averaging"):
+        og.DynamicSmagorinsky(averaging=(2, 3))
+    with pytest.raises(ValueError, match="schedule"):
+        og.DynamicSmagorinsky(schedule=5)
+    flat = og.RectilinearGrid(size=(16, 16), x=(0, 1), y=(0, 1), topology=("Periodic", "Periodic", "Flat"))
+    # invalid configurations are rejected on the host, before any device work
+    with pytest.raises(ValueError, match="Bounded z"):
+        og.NonhydrostaticModel(flat, closure=og.DynamicSmagorinsky())
+    c = cases.seamount((16, 16, 8), solver="cg")
+    with pytest.raises(ValueError, match="ImmersedBoundaryGrid"):
+        og.NonhydrostaticModel(c.grid, closure=og.DynamicSmagorinsky(), pressure_solver=og.ConjugateGradientPoissonSolver())

@@ -72,6 +72,7 @@ struct ModelDesc
     closure_kappa::NTuple{4, Float64}
     timestepper::Int32
     ab2_chi::Float64
+    closure_min_numerator::Float64   # DynamicSmagorinsky(averaging=(1, 2)).coefficient.minimum_numerator
 end
 
 const handles = IdDict{Any, Ptr{Cvoid}}()

@@ -48,3 +48,65 @@ def test_bf16_rounding_is_round_to_nearest_even():
     y = R.bf16(x)
     assert y[0] == 1.0 and y[1] == 1.0 and y[2] == 1.0 + 2**-6 and y[3] == -2.5
     assert abs(y[4] - 3.0e-3) <= 3.0e-3 * 2**-8
+
+
+def test_numpy_gradients_match_torch_autograd():
+    # the gradient checker for training kernels: the numpy backward pass of the oracle
+    # network against autograd of the training module's network, on the training loss
+    torch = pytest.importorskip("torch")
+    from oceananigans_gb300 import learned
+    net = learned.make_net(seed=5)
+    with torch.no_grad():  # a last layer of ordinary size, so every gradient is O(1)
+        net.convs[-1].weight.mul_(100.0)
+        net.convs[-1].bias.fill_(0.1)
+    flat = learned.export_weights(net)
+    layers = R.unpack(flat)
+    net = net.double()
+    learned.load_weights(net, flat)
+    rng = np.random.default_rng(2)
+    nz, ny, nx = 8, 16, 16
+    feat = rng.standard_normal((nz, ny, nx, 3))
+    active = (rng.uniform(size=(nz, ny, nx)) > 0.2).astype(np.float64)
+    target = rng.standard_normal((nz, ny, nx))
+    loss, grads = R.loss_and_grads(layers, feat, target, active)
+    y = net(torch.from_numpy(feat).permute(3, 0, 1, 2)[None])[0, 0]
+    a, t = torch.from_numpy(active), torch.from_numpy(target)
+    na = a.sum()
+    d = (y - t) * a
+    d = d - (d.sum() / na) * a
+    tc = (t - (t * a).sum() / na) * a
+    lt = (d * d).sum() / (tc * tc).sum()
+    lt.backward()
+    assert abs(float(lt.detach()) - loss) <= 1e-12 * loss
+    for n, ((gw, gb), conv) in enumerate(zip(grads, net.convs)):
+        tw, tb = conv.weight.grad.numpy(), conv.bias.grad.numpy()
+        assert np.linalg.norm(tw - gw) <= 1e-10 * np.linalg.norm(tw), n
+        # the output bias shifts every cell equally, which the mean-free loss ignores: its
+        # gradient is zero up to roundoff, so it is measured against the weight gradient
+        assert np.linalg.norm(tb - gb) <= 1e-10 * max(np.linalg.norm(tb), np.linalg.norm(tw)), n
+
+
+def test_numpy_gradient_matches_finite_difference():
+    # an independent check of the backward pass that needs no torch: central differences
+    # of the loss along random weight directions of three layers
+    rng = np.random.default_rng(4)
+    layers = []
+    for _, ci, co in R.LAYERS:
+        layers.append((rng.standard_normal((co, ci, 3, 3, 3)) * np.sqrt(2.0 / (27 * ci)), 0.05 * rng.standard_normal(co)))
+    nz, ny, nx = 8, 8, 8
+    feat = rng.standard_normal((nz, ny, nx, 3))
+    active = np.ones((nz, ny, nx))
+    target = rng.standard_normal((nz, ny, nx))
+    _, grads = R.loss_and_grads(layers, feat, target, active)
+    for li in (0, 3, 7):
+        dw = rng.standard_normal(layers[li][0].shape)
+        h = 1e-6
+
+        def loss_at(s):
+            L = list(layers)
+            L[li] = (layers[li][0] + s * dw, layers[li][1])
+            return R.loss_and_grads(L, feat, target, active)[0]
+
+        fd = (loss_at(h) - loss_at(-h)) / (2 * h)
+        an = float((grads[li][0] * dw).sum())
+        assert abs(fd - an) <= 1e-5 * max(abs(an), 1e-12), (li, fd, an)

@@ -327,6 +327,23 @@ def algorithmic_bytes(group, size, s, ntr=1, closure="smagorinsky", has_phy=True
     return per.get(group, 0) * N * s
 
 
+def max_over_ranks(x, dist, device):
+    """x of the slowest rank: the job's time is the largest over all ranks (x itself
+    on one rank, dist None)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells, steps, world, elapsed):
+    """Whole-job cell-updates/s: every rank advances its own replica of `cells` cells
+    `steps` times, and the job takes the slowest rank's `elapsed` seconds."""
+    return cells * steps * world / elapsed
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -334,8 +351,7 @@ def run_reference(args):
     size = tuple(args.size)
     samples = []
     cpu = None
-    for _ in range(max(1, args.warmup)):
-        pass
+    # each sample takes one untimed warm-up step of its own (cpu_sample)
     t_all = time.perf_counter()
     for _ in range(args.steps):
         cpu = cpu_sample(args.workload, steps_budget_s=max(2.0, 60.0 / max(1, args.steps)))
@@ -549,14 +565,10 @@ def main():
         og.time_step_(model, DT, args.steps)
         e1.record(stream)
         barrier()
-    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed = max_over_ranks(e0.elapsed_time(e1) / 1e3, dist, "cuda")
     launches = lib.gbo_kernel_launches(model._h) - launches0
-    if dist is not None:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
     cells = float(np.prod(size))
-    value = cells * args.steps * world / elapsed
+    value = replica_value(cells, args.steps, world, elapsed)
 
     # per-kernel durations from an instrumented pass on the same stream: every launch
     # bracketed by CUDA events, launched one by one
@@ -611,13 +623,9 @@ def main():
         for n in fields:
             L.check(lib.gbo_get_field(model._h, model._fid(n), host[n].data_ptr(), code, host[n].numel()), model._h)
     barrier()
-    e2e_el = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_el], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_el = float(t.item())
+    e2e_el = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     if fields:
-        e2e = {"value": cells * args.e2e_steps * world / e2e_el, "unit": UNIT,
+        e2e = {"value": replica_value(cells, args.e2e_steps, world, e2e_el), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                "path": "gbo_set_field x%d (pinned host) + gbo_time_step(1) + gbo_get_field x%d" % (len(fields), len(fields))}
 

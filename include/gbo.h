@@ -48,6 +48,9 @@ enum gbo_advection  { GBO_ADVECTION_NONE = 0, GBO_ADVECTION_CENTERED2 = 2, GBO_A
 enum gbo_closure    { GBO_CLOSURE_NONE = 0, GBO_CLOSURE_SMAGORINSKY_LILLY = 1,
                       GBO_CLOSURE_AMD = 2, GBO_CLOSURE_SCALAR_DIFFUSIVITY = 3,
                       GBO_CLOSURE_DYNAMIC_SMAGORINSKY = 4 };
+/* DynamicSmagorinsky averaging (dynamic_coefficient.jl:104-117): over x and y, or
+ * along Lagrangian trajectories (the reference's default, not available on GB300) */
+enum gbo_averaging  { GBO_AVERAGING_XY = 0, GBO_AVERAGING_LAGRANGIAN = 1 };
 enum gbo_timestepper { GBO_TIMESTEPPER_RK3 = 0, GBO_TIMESTEPPER_QAB2 = 1 };
 enum gbo_solver     { GBO_SOLVER_FFT = 0, GBO_SOLVER_FOURIER_TRIDIAGONAL = 1,
                       GBO_SOLVER_CONJUGATE_GRADIENT = 2 };
@@ -115,6 +118,7 @@ typedef struct gbo_model_desc {
      * (turbulence_closure_implementations/Smagorinskys/dynamic_coefficient.jl:1-20,
      * 215-275; scale_invariant_operators.jl).  Uses closure_Pr; ignores C and Cb. */
     double  closure_min_numerator;
+    int32_t closure_averaging;       /* a gbo_averaging; LAGRANGIAN by default, as for DynamicSmagorinsky() */
 } gbo_model_desc;
 
 typedef struct gbo_model gbo_model;

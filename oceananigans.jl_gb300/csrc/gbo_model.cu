@@ -1724,6 +1724,9 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
         if (g->topology[2] != GBO_BOUNDED) return "DynamicSmagorinsky requires a three-dimensional grid with Bounded z";
         if (g->bottom_height) return "DynamicSmagorinsky is not available on an ImmersedBoundaryGrid";
         if (!std::isfinite(d->closure_min_numerator)) return "DynamicSmagorinsky minimum_numerator must be finite";
+        if (d->closure_averaging == GBO_AVERAGING_LAGRANGIAN)
+            return "DynamicSmagorinsky with LagrangianAveraging is not available on GB300; use averaging=(1, 2)";
+        if (d->closure_averaging != GBO_AVERAGING_XY) return "unknown DynamicSmagorinsky averaging";
     }
     if (d->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
         if (!(d->closure_nu >= 0) || !std::isfinite(d->closure_nu)) return "ScalarDiffusivity ν must be finite and >= 0";
@@ -1771,6 +1774,7 @@ void gbo_model_desc_default(gbo_model_desc* d) {
     d->timestepper = GBO_TIMESTEPPER_RK3;
     d->ab2_chi = 0.1;
     d->closure_min_numerator = 1e-32;
+    d->closure_averaging = GBO_AVERAGING_LAGRANGIAN;
 }
 
 int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out) {

@@ -72,7 +72,8 @@ struct ModelDesc
     closure_kappa::NTuple{4, Float64}
     timestepper::Int32
     ab2_chi::Float64
-    closure_min_numerator::Float64   # DynamicSmagorinsky(averaging=(1, 2)).coefficient.minimum_numerator
+    closure_min_numerator::Float64   # DynamicSmagorinsky(...).coefficient.minimum_numerator
+    closure_averaging::Int32         # 0: averaging=(1, 2); 1: LagrangianAveraging()
 end
 
 const handles = IdDict{Any, Ptr{Cvoid}}()

@@ -24,6 +24,7 @@ GBO_FLOAT32, GBO_FLOAT64 = 4, 8
 GBO_ADVECTION_NONE, GBO_ADVECTION_CENTERED2, GBO_ADVECTION_WENO5 = 0, 2, 5
 GBO_CLOSURE_NONE, GBO_CLOSURE_SMAGORINSKY_LILLY, GBO_CLOSURE_AMD, GBO_CLOSURE_SCALAR_DIFFUSIVITY = 0, 1, 2, 3
 GBO_CLOSURE_DYNAMIC_SMAGORINSKY = 4
+GBO_AVERAGING_XY, GBO_AVERAGING_LAGRANGIAN = 0, 1
 GBO_TIMESTEPPER_RK3, GBO_TIMESTEPPER_QAB2 = 0, 1
 GBO_SOLVER_FFT, GBO_SOLVER_FOURIER_TRIDIAGONAL, GBO_SOLVER_CONJUGATE_GRADIENT = 0, 1, 2
 GBO_PRECOND_FFT, GBO_PRECOND_NONE, GBO_PRECOND_LEARNED = 0, 1, 2
@@ -51,7 +52,7 @@ class ModelDesc(ctypes.Structure):
                 ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32),
                 ("closure_nu", ctypes.c_double), ("closure_kappa", ctypes.c_double * GBO_MAX_TRACERS),
                 ("timestepper", ctypes.c_int32), ("ab2_chi", ctypes.c_double),
-                ("closure_min_numerator", ctypes.c_double)]
+                ("closure_min_numerator", ctypes.c_double), ("closure_averaging", ctypes.c_int32)]
 
 
 class GboError(RuntimeError):

@@ -151,20 +151,29 @@ class AnisotropicMinimumDissipation:
         self.C = float(C)
 
 
-class DynamicSmagorinsky:
-    """DynamicSmagorinsky(; averaging=(1, 2), Pr=1, schedule=IterationInterval(1),
-    minimum_numerator=1e-32) (turbulence_closure_implementations/Smagorinskys/
-    dynamic_coefficient.jl:104-117,215-300).  The coefficient is averaged over x and y per
-    level and recomputed at every state update; other averagings and schedules are not
-    available and raise ValueError."""
+class LagrangianAveraging:
+    """LagrangianAveraging() (Smagorinskys/dynamic_coefficient.jl:133-135): the dynamic
+    coefficient averaged along fluid trajectories."""
 
-    def __init__(self, averaging=(1, 2), Pr=1.0, minimum_numerator=1e-32, schedule=1):
-        avg = tuple(averaging) if isinstance(averaging, (tuple, list)) else (averaging,)
-        if tuple(sorted(avg)) != (1, 2):
-            raise ValueError("DynamicSmagorinsky: only averaging=(1, 2) is available on GB300")
+
+class DynamicSmagorinsky:
+    """DynamicSmagorinsky(; averaging=LagrangianAveraging(), Pr=1, schedule=IterationInterval(1),
+    minimum_numerator=1e-32) (turbulence_closure_implementations/Smagorinskys/
+    dynamic_coefficient.jl:104-117,215-300).  On GB300 the coefficient is averaged over x and
+    y (averaging=(1, 2)) and recomputed at every state update; the reference's default
+    LagrangianAveraging is described but rejected when the model is built, other
+    averagings and schedules raise ValueError here."""
+
+    def __init__(self, averaging=None, Pr=1.0, minimum_numerator=1e-32, schedule=1):
+        if averaging is None or isinstance(averaging, LagrangianAveraging):
+            self.averaging = LagrangianAveraging()
+        else:
+            avg = tuple(averaging) if isinstance(averaging, (tuple, list)) else (averaging,)
+            if tuple(sorted(avg)) != (1, 2):
+                raise ValueError("DynamicSmagorinsky: only averaging=(1, 2) is available on GB300")
+            self.averaging = (1, 2)
         if schedule != 1:
             raise ValueError("DynamicSmagorinsky: only schedule=IterationInterval(1) is available on GB300")
-        self.averaging = (1, 2)
         self.Pr = float(Pr)
         self.minimum_numerator = float(minimum_numerator)
 
@@ -272,6 +281,8 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
         d.closure = L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY
         d.closure_Pr = closure.Pr
         d.closure_min_numerator = closure.minimum_numerator
+        d.closure_averaging = (L.GBO_AVERAGING_LAGRANGIAN if isinstance(closure.averaging, LagrangianAveraging)
+                               else L.GBO_AVERAGING_XY)
     elif isinstance(closure, ScalarDiffusivity):
         d.closure = L.GBO_CLOSURE_SCALAR_DIFFUSIVITY
         d.closure_nu = closure.nu

@@ -73,6 +73,7 @@ struct Grid {
     int Nx = 0, Ny = 0, Nz = 0, H = 3, Hz = 3;
     bool flatz = false;
     double Lx = 0, Ly = 0, Lz = 0, dx = 0, dy = 0;
+    double x0 = 0, y0 = 0;  // west and south domain edges
     // vertical spacings indexed k in [1-Hz, Nz+Hz+1] (Δzᵃᵃᶜ and Δzᵃᵃᶠ)
     std::vector<double> dzc_, dzf_, zf_, zc_;
     int zoff = 0;  // vector index = k + zoff
@@ -183,6 +184,12 @@ struct Model {
     std::vector<Field> c, kappa;                    // tracers and AMD diffusivities
     Field sig, sigb;                                // DynamicSmagorinsky: Σ and Σ̄
     std::vector<double> dyn_cs2;                    // DynamicSmagorinsky: c² per level (1-based)
+    Field jlm, jmm, jlm_prev, jmm_prev;             // Lagrangian averaging: 𝒥ᴸᴹ, 𝒥ᴹᴹ and their previous values
+    double prev_compute_time = 0;                   // time of the last Lagrangian update
+    bool velocities_set = false;                    // set! received u, v or w since the last finalize
+    bool lagrangian() const {
+        return desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY && desc.closure_averaging == GBO_AVERAGING_LAGRANGIAN;
+    }
     std::vector<Field> Gn, Gm;                      // tendencies (u,v,w,tracers...)
     double time = 0;
     int64_t iteration = 0;
@@ -937,11 +944,10 @@ void lm_mm(const Ctx& C, const FiltStrain& B, int i, int j, int k, double& LM, d
     MM = M11 * M11 + M22 * M22 + M33 * M33 + 2 * M12 * M12 + 2 * M13 * M13 + 2 * M23 * M23;
 }
 
-void dynamic_smagorinsky(Model& m) {
-    Ctx C(m);
+// _compute_Σ!, _compute_Σ̄! over the interior from the velocities as they are (their
+// halos included), then the halos of Σ and Σ̄
+void compute_sigmas(Model& m, const Ctx& C, const FiltStrain& B) {
     const Grid& g = m.g;
-    FiltStrain B{C};
-    // _compute_Σ!, _compute_Σ̄! over the interior, then their halos
 #pragma omp parallel for collapse(2)
     for (int k = 1; k <= g.Nz; ++k)
         for (int j = 1; j <= g.Ny; ++j)
@@ -951,6 +957,13 @@ void dynamic_smagorinsky(Model& m) {
             }
     fill_halos(m, m.sig, 0);
     fill_halos(m, m.sigb, 0);
+}
+
+void dynamic_smagorinsky(Model& m) {
+    Ctx C(m);
+    const Grid& g = m.g;
+    FiltStrain B{C};
+    compute_sigmas(m, C, B);
     const size_t plane = (size_t)g.Nx * g.Ny;
     std::vector<double> LM(plane * g.Nz), MM(plane * g.Nz);
 #pragma omp parallel for collapse(2)
@@ -982,6 +995,132 @@ void dynamic_smagorinsky(Model& m) {
                 m.nu.at(i, j, k) = m.dyn_cs2[k] * (Df * Df) * std::sqrt(2 * strain_sq(C, i, j, k));
             }
     fill_halos(m, m.nu, 0);
+}
+
+// ---------------------------------------------------------------------------
+// DynamicSmagorinsky with LagrangianAveraging (Smagorinskys/dynamic_coefficient.jl:322-487):
+// 𝒥ᴸᴹ, 𝒥ᴹᴹ are relaxed towards LM, MM along trajectories once per time step
+// (step_closure_prognostics!, after the step's last projection and before update_state!,
+// so the velocities' halos still hold the values filled before that projection).
+// ---------------------------------------------------------------------------
+inline double jl_max(double a, double b) { return (std::isnan(a) || std::isnan(b)) ? NAN : std::max(a, b); }
+inline double jl_clamp(double x, double lo, double hi) { return x > hi ? hi : (x < lo ? lo : x); }
+
+// interpolator (Utils/interpolation.jl:34-42): i⁻ = unsafe_trunc(fi), ξ = mod(fi, 1)
+inline void interpolator(double fi, int& lo, double& xi) {
+    lo = (int)fi;
+    double r = std::fmod(fi, 1.0);
+    xi = (r == 0) ? 0.0 : (r < 0 ? r + 1.0 : r);
+}
+
+// fractional indices of a point (Fields/interpolate.jl:44-58,72-79,166-201): regular
+// spacings by division, a z given by its faces by a binary search over the cell centres
+double frac_x(const Grid& g, double x) { return (x - (g.x0 + 0.5 * g.dx)) / g.dx + 1; }
+double frac_y(const Grid& g, double y) { return (y - (g.y0 + 0.5 * g.dy)) / g.dy + 1; }
+double frac_z(const Grid& g, double z) {
+    if (!g.stretched) return (z - g.zC(1)) / g.dzC(1) + 1;
+    int low = 0, high = g.Nz - 1;
+    while (low + 1 < high) {
+        int mid = (low + high) / 2;
+        double v = g.zC(mid + 1);
+        if (v == z) return mid + 1;
+        if (v < z) low = mid;
+        else high = mid;
+    }
+    const int i1 = low + 1, i2 = high + 1;
+    const double x1 = g.zC(i1), x2 = g.zC(i2);
+    return (double)(i2 - i1) / (x2 - x1) * (z - x1) + i1;
+}
+
+// _interpolate (Utils/interpolation.jl:58-72): trilinear, the eight terms in this order
+double trilinear(const Field& f, double fi, double fj, double fk) {
+    int i0, j0, k0;
+    double x, y, z;
+    interpolator(fi, i0, x);
+    interpolator(fj, j0, y);
+    interpolator(fk, k0, z);
+    const int i1 = i0 + 1, j1 = j0 + 1, k1 = k0 + 1;
+    return (1 - x) * (1 - y) * (1 - z) * f(i0, j0, k0) + (1 - x) * (1 - y) * z * f(i0, j0, k1) +
+           (1 - x) * y * (1 - z) * f(i0, j1, k0) + (1 - x) * y * z * f(i0, j1, k1) +
+           x * (1 - y) * (1 - z) * f(i1, j0, k0) + x * (1 - y) * z * f(i1, j0, k1) +
+           x * y * (1 - z) * f(i1, j1, k0) + x * y * z * f(i1, j1, k1);
+}
+
+// initialize_closure_fields! (:407-437): 𝒥ᴸᴹ = max(mean LM, min), 𝒥ᴹᴹ = mean MM everywhere
+void lagrangian_initialize(Model& m) {
+    Ctx C(m);
+    const Grid& g = m.g;
+    FiltStrain B{C};
+    compute_sigmas(m, C, B);
+    const size_t N = (size_t)g.Nx * g.Ny * g.Nz;
+    std::vector<double> LM(N), MM(N);
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                size_t q = (size_t)(i - 1) + (size_t)g.Nx * ((j - 1) + (size_t)g.Ny * (k - 1));
+                lm_mm(C, B, i, j, k, LM[q], MM[q]);
+            }
+    double a = 0, b = 0;
+    for (size_t q = 0; q < N; ++q) {
+        a += LM[q];
+        b += MM[q];
+    }
+    std::fill(m.jlm.d.begin(), m.jlm.d.end(), jl_max(a / (double)N, m.desc.closure_min_numerator));
+    std::fill(m.jmm.d.begin(), m.jmm.d.end(), b / (double)N);
+    m.prev_compute_time = m.time;
+}
+
+// step_closure_prognostics! and _lagrangian_average_LM_MM! (:342-405,439-484)
+void lagrangian_step(Model& m) {
+    Ctx C(m);
+    const Grid& g = m.g;
+    FiltStrain B{C};
+    compute_sigmas(m, C, B);
+    m.jlm_prev.d = m.jlm.d;
+    m.jmm_prev.d = m.jmm.d;
+    const double dt = m.time - m.prev_compute_time;
+    m.prev_compute_time = m.time;
+    const double lmin = m.desc.closure_min_numerator;
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                double LM, MM;
+                lm_mm(C, B, i, j, k, LM, MM);
+                const double lmp = jl_max(m.jlm_prev(i, j, k), lmin), mmp = m.jmm_prev(i, j, k);
+                const double Df = std::cbrt(g.dx * g.dy * C.M.dzc(k));
+                const double Tm = 1.5 * Df / std::sqrt(std::sqrt(std::sqrt(lmp * mmp)));  // √∜
+                const double tau = dt / Tm, eps = tau / (1 + tau);
+                const double x = g.x0 + (i - 0.5) * g.dx, y = g.y0 + (j - 0.5) * g.dy, z = g.zC(k);
+                const double dzk = C.M.dzc(k);
+                const double ddx = jl_clamp(m.u(i, j, k) * dt, -g.dx, g.dx);
+                const double ddy = jl_clamp(m.v(i, j, k) * dt, -g.dy, g.dy);
+                const double ddz = jl_clamp(m.w(i, j, k) * dt, -dzk, dzk);
+                const double fi = frac_x(g, x - ddx), fj = frac_y(g, y - ddy), fk = frac_z(g, z - ddz);
+                const double imm = trilinear(m.jmm_prev, fi, fj, fk), ilm = trilinear(m.jlm_prev, fi, fj, fk);
+                m.jmm.at(i, j, k) = eps * MM + (1 - eps) * imm;
+                const double lms = eps * LM + (1 - eps) * jl_max(ilm, lmin);
+                m.jlm.at(i, j, k) = jl_max(lms, lmin);
+            }
+}
+
+// νₑ from the pointwise coefficient (square_smagorinsky_coefficient, :236-248), then the
+// halos of every closure field (update_nonhydrostatic_model_state.jl:50)
+void lagrangian_nu(Model& m) {
+    Ctx C(m);
+    const Grid& g = m.g;
+    const double lmin = m.desc.closure_min_numerator;
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= g.Nz; ++k)
+        for (int j = 1; j <= g.Ny; ++j)
+            for (int i = 1; i <= g.Nx; ++i) {
+                const double lm = jl_max(m.jlm(i, j, k), lmin), mm = m.jmm(i, j, k);
+                const double cs2 = mm > 0 ? lm / mm : 0.0;
+                const double Df = std::cbrt(g.dx * g.dy * C.M.dzc(k));
+                m.nu.at(i, j, k) = cs2 * (Df * Df) * std::sqrt(2 * strain_sq(C, i, j, k));
+            }
+    for (Field* f : {&m.nu, &m.jlm, &m.jmm, &m.jlm_prev, &m.jmm_prev, &m.sig, &m.sigb}) fill_halos(m, *f, 0);
 }
 
 // AMD (anisotropic_minimum_dissipation.jl:161-204,243-358; velocity_tracer_gradients.jl:120-250)
@@ -1272,7 +1411,8 @@ void compute_closure(Model& m) {
         return;
     }
     if (m.desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
-        dynamic_smagorinsky(m);
+        if (m.lagrangian()) lagrangian_nu(m);
+        else dynamic_smagorinsky(m);
         return;
     }
     Ctx C(m);
@@ -1482,6 +1622,7 @@ int time_step_ab2(Model& m, double dt) {
     m.time += dt;
     m.iteration += 1;
     m.last_dt = dt;
+    if (m.lagrangian()) lagrangian_step(m);  // quasi_adams_bashforth_2.jl:117
     update_state(m);
     return rc;
 }
@@ -1505,6 +1646,7 @@ int time_step(Model& m, double dt) {
     cache();
     m.time = tnext;
     m.iteration += 1;
+    if (m.lagrangian()) lagrangian_step(m);  // only when clock.stage == 1 again (runge_kutta_3.jl:163)
     update_state(m);
     return rc;
 }
@@ -1693,6 +1835,8 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
     g.Ly = gd->y[1] - gd->y[0];
     g.dx = g.Lx / g.Nx;
     g.dy = g.Ly / g.Ny;
+    g.x0 = gd->x[0];
+    g.y0 = gd->y[0];
     if (g.flatz) {
         g.Lz = 1;
         g.dzc_.assign(9, 1.0); g.dzf_.assign(9, 1.0); g.zc_.assign(9, 0.0); g.zf_.assign(9, 0.0);
@@ -1731,6 +1875,8 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
         m->sig.init(g.Nx, g.Ny, g.Nz, H, Hz);
         m->sigb.init(g.Nx, g.Ny, g.Nz, H, Hz);
     }
+    if (m->lagrangian())
+        for (Field* f : {&m->jlm, &m->jmm, &m->jlm_prev, &m->jmm_prev}) f->init(g.Nx, g.Ny, g.Nz, H, Hz);
     m->c.resize(m->ntr);
     for (auto& f : m->c) f.init(g.Nx, g.Ny, g.Nz, H, Hz);
     if (md->closure == GBO_CLOSURE_AMD || md->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
@@ -1745,6 +1891,9 @@ void* orc_create(const gbo_grid_desc* gd, const gbo_model_desc* md) {
         m->Gm[n].init(g.Nx, g.Ny, nzl, H, Hz);
     }
     for (Field* f : {&m->cg_r, &m->cg_p, &m->cg_q, &m->cg_z, &m->cg_rhs}) f->init(g.Nx, g.Ny, g.Nz, H, Hz);
+    // the constructor initializes the closure fields from the zero velocities
+    // (nonhydrostatic_model.jl:310): 𝒥ᴸᴹ = minimum_numerator, 𝒥ᴹᴹ = 0
+    if (m->lagrangian()) lagrangian_initialize(*m);
     return m;
 }
 
@@ -1761,6 +1910,8 @@ static Field* field_ptr(Model* m, int id, int* nzl) {
     if (id == GBO_FIELD_PHY) return &m->phy;
     if (id == GBO_FIELD_NU) return &m->nu;
     if (id == GBO_FIELD_KAPPA && !m->kappa.empty()) return &m->kappa[0];
+    if (id == 104 && m->lagrangian()) return &m->jlm;  // oracle only: 𝒥ᴸᴹ, 𝒥ᴹᴹ
+    if (id == 105 && m->lagrangian()) return &m->jmm;
     return nullptr;
 }
 
@@ -1775,6 +1926,7 @@ int orc_set_field(void* h, int id, const double* data, int64_t n) {
             for (int i = 1; i <= g.Nx; ++i) f->at(i, j, k) = data[(i - 1) + (size_t)g.Nx * ((j - 1) + (size_t)g.Ny * (k - 1))];
     // set! then fill_halo_regions!(ϕ) with normal-flow fills (set_nonhydrostatic_model.jl:57)
     fill_halos(*m, *f, id == GBO_FIELD_W ? 1 : 0, true);
+    if (id == GBO_FIELD_U || id == GBO_FIELD_V || id == GBO_FIELD_W) m->velocities_set = true;
     return GBO_OK;
 }
 
@@ -1797,10 +1949,14 @@ int orc_set_finalize(void* h, int enforce) {
     mask_immersed(*m, m->u, 1);
     mask_immersed(*m, m->v, 2);
     mask_immersed(*m, m->w, 3);
+    const bool init = m->lagrangian() && m->velocities_set;  // initialize_closure_fields! (:62,69)
+    m->velocities_set = false;
+    if (init) lagrangian_initialize(*m);
     update_state(*m);
     int rc = 0;
     if (enforce) {
         rc = pressure_correction(*m, 1.0);
+        if (init) lagrangian_initialize(*m);
         update_state(*m);
     }
     return rc;

@@ -42,7 +42,7 @@ class ModelDesc(ctypes.Structure):
                 ("cg_reltol", ctypes.c_double), ("cg_abstol", ctypes.c_double), ("cg_maxiter", ctypes.c_int32),
                 ("closure_nu", ctypes.c_double), ("closure_kappa", ctypes.c_double * MAX_TRACERS),
                 ("timestepper", ctypes.c_int32), ("ab2_chi", ctypes.c_double),
-                ("closure_min_numerator", ctypes.c_double)]
+                ("closure_min_numerator", ctypes.c_double), ("closure_averaging", ctypes.c_int32)]
 
 
 def build(force=False):
@@ -88,7 +88,8 @@ def _dptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-FIELD_IDS = {"u": 0, "v": 1, "w": 2, "p": 100, "pHY": 101, "nu": 102, "kappa": 103}
+FIELD_IDS = {"u": 0, "v": 1, "w": 2, "p": 100, "pHY": 101, "nu": 102, "kappa": 103,
+             "jlm": 104, "jmm": 105}  # 𝒥ᴸᴹ, 𝒥ᴹᴹ of a Lagrangian-averaged DynamicSmagorinsky
 
 
 class OracleModel:

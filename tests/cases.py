@@ -62,7 +62,8 @@ def turbulence_2d(N=64, float_type=np.float64, seed=0):
 
 def _closure(name):
     return {None: None, "smagorinsky": og.SmagorinskyLilly, "amd": og.AnisotropicMinimumDissipation,
-            "scalar": lambda: og.ScalarDiffusivity(nu=0.5, kappa=0.2), "dynamic": og.DynamicSmagorinsky}[name]
+            "scalar": lambda: og.ScalarDiffusivity(nu=0.5, kappa=0.2), "dynamic": lambda: og.DynamicSmagorinsky(averaging=(1, 2)),
+            "lagrangian": og.DynamicSmagorinsky}[name]
 
 
 def convection_3d(N=(32, 32, 16), float_type=np.float64, seed=0, L=(512.0, 512.0, 256.0),

@@ -34,9 +34,10 @@ def test_struct_layout_matches_header(tmp_path):
 #include <stddef.h>
 #include "gbo.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gbo_grid_desc), offsetof(gbo_grid_desc, z_faces),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gbo_grid_desc), offsetof(gbo_grid_desc, z_faces),
          offsetof(gbo_grid_desc, float_type), sizeof(gbo_model_desc), offsetof(gbo_model_desc, pressure_solver),
-         offsetof(gbo_model_desc, cg_maxiter), offsetof(gbo_model_desc, closure_min_numerator));
+         offsetof(gbo_model_desc, cg_maxiter), offsetof(gbo_model_desc, closure_min_numerator),
+         offsetof(gbo_model_desc, closure_averaging));
   return 0; }
 ''')
     exe = tmp_path / "probe"
@@ -45,7 +46,7 @@ int main(void) {
     got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
     want = [ctypes.sizeof(L.GridDesc), L.GridDesc.z_faces.offset, L.GridDesc.float_type.offset,
             ctypes.sizeof(L.ModelDesc), L.ModelDesc.pressure_solver.offset, L.ModelDesc.cg_maxiter.offset,
-            L.ModelDesc.closure_min_numerator.offset]
+            L.ModelDesc.closure_min_numerator.offset, L.ModelDesc.closure_averaging.offset]
     assert got == want
 
 

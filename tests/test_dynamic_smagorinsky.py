@@ -81,8 +81,8 @@ def _sig2(s):
     return s11 ** 2 + s22 ** 2 + s33 ** 2 + 2 * _ixy(s12 ** 2) + 2 * _ixz(s13 ** 2) + 2 * _iyz(s23 ** 2)
 
 
-def numpy_dynamic_nu(u, v, w, L, min_numerator=1e-32):
-    """νₑ of DynamicSmagorinsky(averaging=(1, 2)) on a regular Periodic-Periodic-Bounded grid."""
+def numpy_lm_mm(u, v, w, L):
+    """Per-cell LᵢⱼMᵢⱼ, MᵢⱼMᵢⱼ, Σ² and Δᶠ on a regular Periodic-Periodic-Bounded grid."""
     Nx, Ny, Nz = u.shape
     dx, dy, dz = L[0] / Nx, L[1] / Ny, L[2] / Nz
     U, V, W = _pad_center(u), _pad_center(v), _pad_face(w)
@@ -111,14 +111,20 @@ def numpy_dynamic_nu(u, v, w, L, min_numerator=1e-32):
     wts = [1, 1, 1, 2, 2, 2]
     LM = sum(c * l * m for c, l, m in zip(wts, Ls, Ms))[:, :, interior]
     MM = sum(c * m * m for c, m in zip(wts, Ms))[:, :, interior]
+    return LM, MM, sig2[:, :, interior], Df
+
+
+def numpy_dynamic_nu(u, v, w, L, min_numerator=1e-32):
+    """νₑ of DynamicSmagorinsky(averaging=(1, 2)) on a regular Periodic-Periodic-Bounded grid."""
+    LM, MM, sig2, Df = numpy_lm_mm(u, v, w, L)
     jlm, jmm = LM.mean(axis=(0, 1)), MM.mean(axis=(0, 1))
     num = np.maximum(jlm, min_numerator)
     cs2 = np.where(jmm > 0, num / np.where(jmm > 0, jmm, 1.0), 0.0)
-    return cs2[None, None, :] * Df ** 2 * np.sqrt(2 * sig2[:, :, interior])
+    return cs2[None, None, :] * Df ** 2 * np.sqrt(2 * sig2)
 
 
-def _random_case(N=(12, 10, 8), seed=3, U0=0.3):
-    c = cases.convection_3d(N, closure="dynamic", f=0.0, flux=0.0, U0=U0, seed=seed)
+def _random_case(N=(12, 10, 8), seed=3, U0=0.3, closure="dynamic", **kw):
+    c = cases.convection_3d(N, closure=closure, f=0.0, flux=0.0, U0=U0, seed=seed, **kw)
     w = c.init["w"].copy()
     w[:, :, 0] = 0.0
     w[:, :, -1] = 0.0
@@ -167,3 +173,54 @@ def test_unsupported_averaging_and_grids_rejected():
     c = cases.seamount((16, 16, 8), solver="cg")
     with pytest.raises(ValueError, match="ImmersedBoundaryGrid"):
         og.NonhydrostaticModel(c.grid, closure=og.DynamicSmagorinsky(), pressure_solver=og.ConjugateGradientPoissonSolver())
+
+
+# ---- LagrangianAveraging (dynamic_coefficient.jl:322-487): the oracle only; GB300 rejects it ----
+
+def test_lagrangian_initialization_matches_numpy():
+    # initialize_closure_fields!: 𝒥ᴸᴹ = max(mean LM, min), 𝒥ᴹᴹ = mean MM over the whole
+    # domain, so νₑ = c² Δᶠ² √(2Σ²) with one c² everywhere
+    c = _random_case(closure="lagrangian")
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(False)
+    LM, MM, sig2, Df = numpy_lm_mm(c.init["u"], c.init["v"], c.init["w"], (512.0, 512.0, 256.0))
+    jlm, jmm = max(LM.mean(), 1e-32), MM.mean()
+    assert cases.rel_l2(ref.get("jlm"), np.full(LM.shape, jlm)) <= 1e-12
+    assert cases.rel_l2(ref.get("jmm"), np.full(LM.shape, jmm)) <= 1e-13
+    assert cases.rel_l2(ref.get("nu"), jlm / jmm * Df ** 2 * np.sqrt(2 * sig2)) <= 1e-12
+
+
+@pytest.mark.parametrize("timestepper", ["RungeKutta3", "QuasiAdamsBashforth2"])
+def test_lagrangian_step_bounds(timestepper):
+    c = _random_case(N=(16, 16, 8), seed=5, U0=0.05, closure="lagrangian", timestepper=timestepper)
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(True)
+    jlm0 = ref.get("jlm")
+    ref.time_step(2.0, 3)
+    jlm, jmm, nu = ref.get("jlm"), ref.get("jmm"), ref.get("nu")
+    assert np.all(np.isfinite(jlm)) and np.all(np.isfinite(jmm))
+    assert np.all(jlm >= 1e-32) and np.all(jmm >= 0) and np.all(nu >= 0)
+    assert np.ptp(jlm) > 0 and np.ptp(jlm0) == 0  # constant after set!, pointwise after the steps
+
+
+def test_lagrangian_relaxation_vanishes_with_the_step():
+    # ϵ = τ / (1 + τ) with τ = Δt / T: a short step barely moves 𝒥 away from its
+    # initial constant, a longer one moves it further
+    moves = []
+    for dt in (1e-4, 1e-1):
+        c = _random_case(N=(16, 16, 8), seed=5, U0=0.05, closure="lagrangian")
+        ref = c.oracle_model()
+        ref.set(**c.init)
+        ref.finalize_set(True)
+        j0 = ref.get("jmm").mean()
+        ref.time_step(dt)
+        moves.append(np.abs(ref.get("jmm") - j0).max() / j0)
+    assert moves[0] < 1e-2 and moves[1] > 10 * moves[0]
+
+
+def test_lagrangian_rejected_on_gb300():
+    c = _random_case(closure="lagrangian")
+    with pytest.raises(ValueError, match="LagrangianAveraging is not available"):
+        og.NonhydrostaticModel(c.grid, **c.physics)

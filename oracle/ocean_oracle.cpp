@@ -1969,6 +1969,30 @@ int orc_time_step(void* h, double dt, int nsteps) {
     return rc;
 }
 
+// Checker access for the Lagrangian-averaging tests: a field's parent array (halos
+// included, x fastest; dims = nx, ny, nz of the parent) and one Lagrangian update of
+// 𝒥ᴸᴹ, 𝒥ᴹᴹ from the current state with the clock advanced by dt.
+int orc_parent(void* h, int id, double* out, int64_t n, int* dims) {
+    Model* m = static_cast<Model*>(h);
+    int nzl;
+    Field* f = field_ptr(m, id, &nzl);
+    if (!f) return GBO_ERR_INVALID;
+    dims[0] = f->nx; dims[1] = f->ny; dims[2] = f->nz;
+    if (out) {
+        if (n != (int64_t)f->d.size()) return GBO_ERR_INVALID;
+        std::copy(f->d.begin(), f->d.end(), out);
+    }
+    return GBO_OK;
+}
+
+int orc_lagrangian_update(void* h, double dt) {
+    Model* m = static_cast<Model*>(h);
+    if (!m->lagrangian()) return GBO_ERR_INVALID;
+    m->time += dt;
+    lagrangian_step(*m);
+    return GBO_OK;
+}
+
 int orc_clock(void* h, double* t, int64_t* it) {
     Model* m = static_cast<Model*>(h);
     *t = m->time;

@@ -77,6 +77,8 @@ def lib():
         L.orc_weno5.restype = ctypes.c_double
         L.orc_weno5.argtypes = [dp, ctypes.c_int]
         L.orc_clock.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_int64)]
+        L.orc_parent.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+        L.orc_lagrangian_update.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_last_cg_iterations.argtypes = [ctypes.c_void_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
@@ -140,6 +142,20 @@ class OracleModel:
         if rc:
             raise ValueError("oracle get failed for %s" % name)
         return out.reshape(shp, order="F")
+
+    def parent(self, name):
+        """The field's parent array, halos included, indexed [i, j, k] (1-based interior
+        index i at parent index i + H - 1)."""
+        dims = (ctypes.c_int * 3)()
+        if lib().orc_parent(self.h, self._fid(name), None, 0, dims):
+            raise ValueError("oracle has no parent array for %s" % name)
+        out = np.zeros(dims[0] * dims[1] * dims[2], dtype=np.float64)
+        _checked(lib().orc_parent(self.h, self._fid(name), _dptr(out), out.size, dims))
+        return out.reshape((dims[0], dims[1], dims[2]), order="F")
+
+    def lagrangian_update(self, dt):
+        """One Lagrangian update of 𝒥ᴸᴹ, 𝒥ᴹᴹ from the current state, the clock advanced by dt."""
+        return _checked(lib().orc_lagrangian_update(self.h, float(dt)))
 
     def time_step(self, dt, nsteps=1):
         return _checked(lib().orc_time_step(self.h, float(dt), int(nsteps)))

@@ -224,3 +224,114 @@ def test_lagrangian_rejected_on_gb300():
     c = _random_case(closure="lagrangian")
     with pytest.raises(ValueError, match="LagrangianAveraging is not available"):
         og.NonhydrostaticModel(c.grid, **c.physics)
+
+
+# ---- the Lagrangian update restated on the oracle's own arrays (halos as they are) ----
+
+def _shift(a, d, axis):
+    """out[i] = a[i + d] along axis, zero beyond the array."""
+    out = np.zeros_like(a)
+    n = a.shape[axis]
+    dst, src = [slice(None)] * 3, [slice(None)] * 3
+    if d > 0:
+        dst[axis], src[axis] = slice(0, n - d), slice(d, n)
+    else:
+        dst[axis], src[axis] = slice(-d, n), slice(0, n + d)
+    out[tuple(dst)] = a[tuple(src)]
+    return out
+
+
+def _lm_mm_parents(U, V, W, dx, dy, dz):
+    """LM, MM, Σ², Δᶠ at the interior from parent arrays with 3 halo points on every side
+    (all shifts by slicing, so the arrays' own halo values are used)."""
+    global _X, _Y, _Z
+    saved = (_X, _Y, _Z)
+    _X, _Y, _Z = (lambda a, d: _shift(a, d, 0)), (lambda a, d: _shift(a, d, 1)), (lambda a, d: _shift(a, d, 2))
+    try:
+        Nx, Ny = U.shape[0] - 2 * H, U.shape[1] - 2 * H
+        Nz = W.shape[2] - 2 * H - 1
+        Uc = np.zeros_like(W)
+        Uc[:, :, :-1] = U
+        Vc = np.zeros_like(W)
+        Vc[:, :, :-1] = V
+        I = (slice(H, H + Nx), slice(H, H + Ny), slice(H, H + Nz))
+
+        def fill(c):  # Σ, Σ̄ halos: one mirrored z layer, zeros beyond, periodic x and y
+            p = _pad_center(c)
+            return np.pad(p, ((H, H), (H, H), (0, 0)), mode="wrap")
+
+        S = _strain(Uc, Vc, W, dx, dy, dz)
+        FU, FV, FW = _filt(Uc), _filt(Vc), _filt(W)
+        SB = _strain(FU, FV, FW, dx, dy, dz)
+        sig2 = _sig2(S)
+        SG, SBB = fill(np.sqrt(sig2[I])), fill(np.sqrt(_sig2(SB)[I]))
+        ixu, iyv, izw = 0.5 * (Uc + _X(Uc, 1)), 0.5 * (Vc + _Y(Vc, 1)), 0.5 * (W + _Z(W, 1))
+        ixfu, iyfv, izfw = 0.5 * (FU + _X(FU, 1)), 0.5 * (FV + _Y(FV, 1)), 0.5 * (FW + _Z(FW, 1))
+        Ls = [_filt(0.5 * (Uc ** 2 + _X(Uc, 1) ** 2)) - 0.5 * (FU ** 2 + _X(FU, 1) ** 2),
+              _filt(0.5 * (Vc ** 2 + _Y(Vc, 1) ** 2)) - 0.5 * (FV ** 2 + _Y(FV, 1) ** 2),
+              _filt(0.5 * (W ** 2 + _Z(W, 1) ** 2)) - 0.5 * (FW ** 2 + _Z(FW, 1) ** 2),
+              _filt(ixu * iyv) - ixfu * iyfv, _filt(ixu * izw) - ixfu * izfw, _filt(iyv * izw) - iyfv * izfw]
+        s11, s22, s33, s12, s13, s23 = S
+        b11, b22, b33, b12, b13, b23 = SB
+        ss = [SG * s11, SG * s22, SG * s33, SG * _ixy(s12), SG * _ixz(s13), SG * _iyz(s23)]
+        bb = [SBB * b11, SBB * b22, SBB * b33, SBB * _ixy(b12), SBB * _ixz(b13), SBB * _iyz(b23)]
+        Df = np.cbrt(dx * dy * dz)
+        Ms = [2 * Df ** 2 * (_filt(a) - 4 * b) for a, b in zip(ss, bb)]
+        wts = [1, 1, 1, 2, 2, 2]
+        LM = sum(c * l * m for c, l, m in zip(wts, Ls, Ms))[I]
+        MM = sum(c * m * m for c, m in zip(wts, Ms))[I]
+        return LM, MM, I, Df
+    finally:
+        _X, _Y, _Z = saved
+
+
+def numpy_lagrangian_update(ref, dt, L, z0, lmin=1e-32):
+    """𝒥ᴸᴹ, 𝒥ᴹᴹ after one update from the oracle's current parent arrays
+    (_lagrangian_average_LM_MM!, dynamic_coefficient.jl:342-405)."""
+    U, V, W = ref.parent("u"), ref.parent("v"), ref.parent("w")
+    JL, JM = ref.parent("jlm"), ref.parent("jmm")
+    Nx, Ny, Nz = ref.shape
+    dx, dy, dz = L[0] / Nx, L[1] / Ny, L[2] / Nz
+    LM, MM, I, Df = _lm_mm_parents(U, V, W, dx, dy, dz)
+    lmp, mmp = np.maximum(JL[I], lmin), JM[I]
+    with np.errstate(divide="ignore"):
+        T = 1.5 * Df / np.sqrt(np.sqrt(np.sqrt(lmp * mmp)))
+    tau = dt / T
+    eps = tau / (1 + tau)
+    i, j, k = np.meshgrid(np.arange(1, Nx + 1), np.arange(1, Ny + 1), np.arange(1, Nz + 1), indexing="ij")
+    x, y, z = (i - 0.5) * dx, (j - 0.5) * dy, z0 + (k - 0.5) * dz
+    ddx = np.clip(U[I] * dt, -dx, dx)
+    ddy = np.clip(V[I] * dt, -dy, dy)
+    ddz = np.clip(W[I] * dt, -dz, dz)
+    fi, fj, fk = (x - ddx - 0.5 * dx) / dx + 1, (y - ddy - 0.5 * dy) / dy + 1, (z - ddz - (z0 + 0.5 * dz)) / dz + 1
+
+    def itp(F):
+        i0, j0, k0 = (np.trunc(f).astype(int) for f in (fi, fj, fk))
+        a, b, c = np.mod(fi, 1.0), np.mod(fj, 1.0), np.mod(fk, 1.0)
+        g = lambda p, q, r: F[p + H - 1, q + H - 1, r + H - 1]  # noqa: E731  (1-based index -> parent)
+        return ((1 - a) * (1 - b) * (1 - c) * g(i0, j0, k0) + (1 - a) * (1 - b) * c * g(i0, j0, k0 + 1) +
+                (1 - a) * b * (1 - c) * g(i0, j0 + 1, k0) + (1 - a) * b * c * g(i0, j0 + 1, k0 + 1) +
+                a * (1 - b) * (1 - c) * g(i0 + 1, j0, k0) + a * (1 - b) * c * g(i0 + 1, j0, k0 + 1) +
+                a * b * (1 - c) * g(i0 + 1, j0 + 1, k0) + a * b * c * g(i0 + 1, j0 + 1, k0 + 1))
+
+    jmm = eps * MM + (1 - eps) * itp(JM)
+    jlm = np.maximum(eps * LM + (1 - eps) * np.maximum(itp(JL), lmin), lmin)
+    return jlm, jmm
+
+
+@pytest.mark.parametrize("dt", [2.0, 2000.0])
+def test_lagrangian_update_matches_numpy(dt):
+    # after a step 𝒥 varies in space; one more update from those arrays, in the oracle and
+    # in numpy (dt = 2000 s clamps most displacements at one cell)
+    c = _random_case(N=(16, 12, 8), seed=9, U0=0.05, closure="lagrangian")
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(True)
+    ref.time_step(2.0)
+    t = ref.clock()[0]
+    if dt > 100:
+        assert np.mean(np.abs(ref.get("u")) * dt > 512.0 / 16) > 0.5
+    want_lm, want_mm = numpy_lagrangian_update(ref, (t + dt) - t, (512.0, 512.0, 256.0), -256.0)
+    ref.lagrangian_update(dt)
+    assert cases.rel_l2(ref.get("jmm"), want_mm) <= 1e-12
+    assert cases.rel_l2(ref.get("jlm"), want_lm) <= 1e-12

@@ -335,3 +335,19 @@ def test_lagrangian_update_matches_numpy(dt):
     ref.lagrangian_update(dt)
     assert cases.rel_l2(ref.get("jmm"), want_mm) <= 1e-12
     assert cases.rel_l2(ref.get("jlm"), want_lm) <= 1e-12
+
+
+def test_closure_defaults_and_descriptor():
+    # DynamicSmagorinsky() defaults to LagrangianAveraging, Pr = 1, minimum_numerator = 1e-32
+    # (dynamic_coefficient.jl:104-117); the descriptor carries each choice
+    from oceananigans_gb300 import _lib as L
+    from oceananigans_gb300.api import model_descriptor
+    c = _random_case()
+    d0 = og.DynamicSmagorinsky()
+    assert isinstance(d0.averaging, og.LagrangianAveraging) and d0.Pr == 1.0 and d0.minimum_numerator == 1e-32
+    assert og.DynamicSmagorinsky(averaging=[2, 1]).averaging == (1, 2)
+    for closure, avg in ((d0, L.GBO_AVERAGING_LAGRANGIAN),
+                         (og.DynamicSmagorinsky(averaging=(1, 2), Pr=0.5, minimum_numerator=1e-20), L.GBO_AVERAGING_XY)):
+        d, _ = model_descriptor(c.grid, closure=closure, tracers=("b",), buoyancy=og.BuoyancyTracer())
+        assert d.closure == L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY and d.closure_averaging == avg
+        assert d.closure_Pr == closure.Pr and d.closure_min_numerator == closure.minimum_numerator

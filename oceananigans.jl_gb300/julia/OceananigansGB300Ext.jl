@@ -78,6 +78,79 @@ end
 
 const handles = IdDict{Any, Ptr{Cvoid}}()
 
+# --- model → descriptor (oceananigans_gb300.api.model_descriptor does the same) --------
+using Oceananigans.TurbulenceClosures: ScalarDiffusivity, AnisotropicMinimumDissipation
+using Oceananigans.TurbulenceClosures.Smagorinskys: Smagorinsky, LillyCoefficient, DynamicCoefficient,
+                                                    LagrangianAveraging
+using Oceananigans.BuoyancyFormulations: BuoyancyTracer
+using Oceananigans.Coriolis: FPlane
+using Oceananigans.BoundaryConditions: BoundaryCondition, Flux
+using Oceananigans.Solvers: FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver
+using Oceananigans.TimeSteppers: QuasiAdamsBashforth2TimeStepper
+
+# a copy of d with the named fields replaced
+function with(d::ModelDesc; kw...)
+    vals = ntuple(fieldcount(ModelDesc)) do n
+        f = fieldname(ModelDesc, n)
+        haskey(kw, f) ? convert(fieldtype(ModelDesc, f), kw[f]) : getfield(d, n)
+    end
+    return ModelDesc(vals...)
+end
+
+one_value(x::Number) = Float64(x)
+one_value(x::NamedTuple) = Float64(first(values(x)))   # one Pr / κ for every tracer
+padded4(x::Number) = ntuple(_ -> Float64(x), 4)
+padded4(x::NamedTuple) = ntuple(n -> n ≤ length(x) ? Float64(values(x)[n]) : 0.0, 4)
+
+closure_desc(::Nothing) = (; closure = Int32(0))
+# a constant coefficient is the Lilly form with Cb = 0 (smagorinsky.jl:47,106)
+closure_desc(c::Smagorinsky{<:Any, <:Number}) =
+    (; closure = Int32(1), closure_C = Float64(c.coefficient), closure_Cb = 0.0, closure_Pr = one_value(c.Pr))
+closure_desc(c::Smagorinsky{<:Any, <:LillyCoefficient}) =
+    (; closure = Int32(1), closure_C = Float64(c.coefficient.smagorinsky),
+       closure_Cb = Float64(c.coefficient.reduction_factor), closure_Pr = one_value(c.Pr))
+function closure_desc(c::Smagorinsky{<:Any, <:DynamicCoefficient})
+    a = c.coefficient.averaging
+    avg = a isa LagrangianAveraging ? Int32(1) : (a isa Tuple && sort(collect(a)) == [1, 2]) ? Int32(0) : Int32(-1)
+    return (; closure = Int32(4), closure_Pr = one_value(c.Pr), closure_averaging = avg,
+              closure_min_numerator = Float64(c.coefficient.minimum_numerator))
+end
+function closure_desc(c::AnisotropicMinimumDissipation)
+    isnothing(c.Cb) || throw(ArgumentError("AnisotropicMinimumDissipation with Cb is not available on GB300"))
+    return (; closure = Int32(2), closure_C = one_value(c.Cν))
+end
+closure_desc(c::ScalarDiffusivity) = (; closure = Int32(3), closure_nu = Float64(c.ν), closure_kappa = padded4(c.κ))
+closure_desc(c) = throw(ArgumentError("closure $(summary(c)) is not available on GB300"))
+
+flux_value(bc::BoundaryCondition{<:Flux}) = bc.condition isa Number ? Float64(bc.condition) :
+    throw(ArgumentError("only constant FluxBoundaryConditions are available on GB300"))
+flux_value(bc) = 0.0   # nothing / no-flux
+
+solver_desc(::FFTBasedPoissonSolver) = (; pressure_solver = Int32(0))
+solver_desc(::FourierTridiagonalPoissonSolver) = (; pressure_solver = Int32(1))
+function solver_desc(s::ConjugateGradientPoissonSolver)
+    cg = s.conjugate_gradient_solver
+    return (; pressure_solver = Int32(2), preconditioner = Int32(0), cg_reltol = Float64(cg.reltol),
+              cg_abstol = Float64(cg.abstol), cg_maxiter = Int32(cg.maxiter))
+end
+
+function describe(model, md::ModelDesc)
+    tracers = model.tracers
+    tops = ntuple(n -> n ≤ length(tracers) ? flux_value(tracers[n].boundary_conditions.top) : 0.0, 4)
+    bots = ntuple(n -> n ≤ length(tracers) ? flux_value(tracers[n].boundary_conditions.bottom) : 0.0, 4)
+    b = model.buoyancy isa Nothing ? 0 :
+        (model.buoyancy.formulation isa BuoyancyTracer && first(keys(tracers)) == :b) ? 1 :
+        throw(ArgumentError("only BuoyancyTracer with b as the first tracer is available on GB300"))
+    f = model.coriolis isa FPlane ? (; has_coriolis = Int32(1), coriolis_f = Float64(model.coriolis.f)) :
+        model.coriolis isa Nothing ? (; has_coriolis = Int32(0)) :
+        throw(ArgumentError("only FPlane Coriolis is available on GB300"))
+    ts = model.timestepper isa QuasiAdamsBashforth2TimeStepper ?
+         (; timestepper = Int32(1), ab2_chi = Float64(model.timestepper.χ)) : (; timestepper = Int32(0))
+    return with(md; ntracers = Int32(length(tracers)), buoyancy_tracer = Int32(b),
+                tracer_flux_top = tops, tracer_flux_bottom = bots,
+                closure_desc(model.closure)..., solver_desc(model.pressure_solver)..., f..., ts...)
+end
+
 check(rc, h=C_NULL) = rc == 0 ||
     throw(ErrorException(unsafe_string(ccall((:gbo_last_error, libgbo), Cstring, (Ptr{Cvoid},), h))))
 
@@ -99,10 +172,9 @@ function handle(model::NonhydrostaticModel)
                       (grid.xᶠᵃᵃ[1], grid.xᶠᵃᵃ[1] + grid.Lx), (grid.yᵃᶠᵃ[1], grid.yᵃᶠᵃ[1] + grid.Ly),
                       (-grid.Lz, 0.0), isempty(zf) ? C_NULL : pointer(zf), isempty(bh) ? C_NULL : pointer(bh),
                       FT == Float32 ? Int32(4) : Int32(8))
-        md = Ref{ModelDesc}()
-        ccall((:gbo_model_desc_default, libgbo), Cvoid, (Ref{ModelDesc},), md)
-        # closure / buoyancy / coriolis / boundary conditions are translated here
-        # exactly as oceananigans_gb300.api.model_descriptor does for Python.
+        md0 = Ref{ModelDesc}()
+        ccall((:gbo_model_desc_default, libgbo), Cvoid, (Ref{ModelDesc},), md0)
+        md = Ref(describe(model, md0[]))
         h = Ref{Ptr{Cvoid}}(C_NULL)
         GC.@preserve zf bh check(ccall((:gbo_model_create, libgbo), Cint,
                                     (Ref{GridDesc}, Ref{ModelDesc}, Ref{Ptr{Cvoid}}), Ref(gd), md, h))

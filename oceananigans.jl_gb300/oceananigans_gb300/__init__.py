@@ -6,7 +6,7 @@ is the host-side mirror of the reference's model API.
 from .api import (  # noqa: F401
     Periodic, Bounded, Flat,
     RectilinearGrid, ImmersedBoundaryGrid, GridFittedBottom,
-    WENO, SmagorinskyLilly, AnisotropicMinimumDissipation, DynamicSmagorinsky, LagrangianAveraging, ScalarDiffusivity, BuoyancyTracer, FPlane,
+    WENO, Smagorinsky, SmagorinskyLilly, AnisotropicMinimumDissipation, DynamicSmagorinsky, LagrangianAveraging, ScalarDiffusivity, BuoyancyTracer, FPlane,
     QuasiAdamsBashforth2TimeStepper,
     FluxBoundaryCondition, FieldBoundaryConditions,
     FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver,

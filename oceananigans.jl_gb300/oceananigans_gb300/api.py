@@ -141,6 +141,19 @@ class WENO:
         self.order = order
 
 
+class Smagorinsky:
+    """Smagorinsky(; coefficient=0.16, Pr=1) with a constant coefficient
+    (turbulence_closure_implementations/Smagorinskys/smagorinsky.jl:47,77-83,90-106):
+    νₑ = C² Δᶠ² √(2Σ²).  That is the Lilly form with Cb = 0 (ς = 1 wherever Σ² > 0,
+    and νₑ = 0 where Σ² = 0 in both), so it runs as SmagorinskyLilly(C, Cb=0)."""
+
+    def __init__(self, coefficient=0.16, Pr=1.0):
+        if isinstance(coefficient, bool) or not isinstance(coefficient, (int, float)):
+            raise ValueError("Smagorinsky: the coefficient must be a number (use SmagorinskyLilly or "
+                             "DynamicSmagorinsky for the other coefficients)")
+        self.C, self.Pr = float(coefficient), float(Pr)
+
+
 class SmagorinskyLilly:
     def __init__(self, C=0.16, Cb=1.0, Pr=1.0):
         self.C, self.Cb, self.Pr = float(C), float(Cb), float(Pr)
@@ -271,7 +284,10 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
     d = L.ModelDesc()
     L.load().gbo_model_desc_default(ctypes.byref(d))
     d.advection = L.GBO_ADVECTION_WENO5
-    if isinstance(closure, SmagorinskyLilly):
+    if isinstance(closure, Smagorinsky):
+        d.closure = L.GBO_CLOSURE_SMAGORINSKY_LILLY
+        d.closure_C, d.closure_Cb, d.closure_Pr = closure.C, 0.0, closure.Pr
+    elif isinstance(closure, SmagorinskyLilly):
         d.closure = L.GBO_CLOSURE_SMAGORINSKY_LILLY
         d.closure_C, d.closure_Cb, d.closure_Pr = closure.C, closure.Cb, closure.Pr
     elif isinstance(closure, AnisotropicMinimumDissipation):

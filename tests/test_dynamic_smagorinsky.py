@@ -351,3 +351,17 @@ def test_closure_defaults_and_descriptor():
         d, _ = model_descriptor(c.grid, closure=closure, tracers=("b",), buoyancy=og.BuoyancyTracer())
         assert d.closure == L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY and d.closure_averaging == avg
         assert d.closure_Pr == closure.Pr and d.closure_min_numerator == closure.minimum_numerator
+
+
+def test_constant_smagorinsky_is_lilly_without_buoyancy_reduction():
+    # Smagorinsky(coefficient=C): νₑ = C² Δᶠ² √(2Σ²) (smagorinsky.jl:90-106), here from the
+    # oracle through the Lilly path with Cb = 0, against the numpy strain
+    c = _random_case(closure=None)
+    c.physics["closure"] = og.Smagorinsky(coefficient=0.2)
+    ref = c.oracle_model()
+    ref.set(**c.init)
+    ref.finalize_set(False)
+    _, _, sig2, Df = numpy_lm_mm(c.init["u"], c.init["v"], c.init["w"], (512.0, 512.0, 256.0))
+    assert cases.rel_l2(ref.get("nu"), 0.2 ** 2 * Df ** 2 * np.sqrt(2 * sig2)) <= 1e-13
+    with pytest.raises(ValueError, match="number"):
+        og.Smagorinsky(coefficient="dynamic")

@@ -97,3 +97,17 @@ def test_no_device_is_reported_cleanly():
         pytest.skip("a device is present")
     grid = og.RectilinearGrid(size=(16, 16, 8), z=(-1, 0))
     assert _create(grid) == L.GBO_ERR_NO_DEVICE
+
+
+def test_ensemble_arguments_rejected_before_device():
+    # gbo_ensemble_create validates every member before any device work
+    import cases
+    c = cases.convection_3d((16, 16, 8))
+    qab2 = dict(c.physics, timestepper="QuasiAdamsBashforth2")
+    with pytest.raises(ValueError, match="member 1: ensembles step RungeKutta3 models only"):
+        og.Ensemble([(c.grid, c.physics), (c.grid, qab2)])
+    flat = og.RectilinearGrid(size=(16, 16), x=(0, 1), y=(0, 1), topology=("Periodic", "Periodic", "Flat"))
+    with pytest.raises(ValueError, match="member 0: DynamicSmagorinsky requires"):
+        og.Ensemble([(flat, dict(closure=og.DynamicSmagorinsky(averaging=(1, 2))))])
+    with pytest.raises(ValueError, match="invalid ensemble arguments"):
+        og.Ensemble([])

@@ -117,6 +117,8 @@ function closure_desc(c::Smagorinsky{<:Any, <:DynamicCoefficient})
 end
 function closure_desc(c::AnisotropicMinimumDissipation)
     isnothing(c.Cb) || throw(ArgumentError("AnisotropicMinimumDissipation with Cb is not available on GB300"))
+    Cκ = c.Cκ isa NamedTuple ? collect(values(c.Cκ)) : [c.Cκ]
+    all(==(c.Cν), Cκ) || throw(ArgumentError("AnisotropicMinimumDissipation with Cκ ≠ Cν is not available on GB300"))
     return (; closure = Int32(2), closure_C = one_value(c.Cν))
 end
 closure_desc(c::ScalarDiffusivity) = (; closure = Int32(3), closure_nu = Float64(c.ν), closure_kappa = padded4(c.κ))

@@ -160,8 +160,19 @@ class SmagorinskyLilly:
 
 
 class AnisotropicMinimumDissipation:
-    def __init__(self, C=1.0 / 3.0):
-        self.C = float(C)
+    """AnisotropicMinimumDissipation(; C=1/3, Cν=C, Cκ=C, Cb=nothing)
+    (anisotropic_minimum_dissipation.jl:138-147), with Cν as `Cnu` and Cκ as `Ckappa`.
+    The library carries one coefficient for the viscosity and the diffusivities and no
+    buoyancy modification: Ckappa ≠ Cnu or a Cb raise ValueError."""
+
+    def __init__(self, C=1.0 / 3.0, Cnu=None, Ckappa=None, Cb=None):
+        cnu = float(C if Cnu is None else Cnu)
+        ckappa = float(C if Ckappa is None else Ckappa)
+        if ckappa != cnu:
+            raise ValueError("AnisotropicMinimumDissipation with Cκ ≠ Cν is not available on GB300")
+        if Cb is not None:
+            raise ValueError("AnisotropicMinimumDissipation with Cb is not available on GB300")
+        self.C = cnu
 
 
 class LagrangianAveraging:

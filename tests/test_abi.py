@@ -111,3 +111,14 @@ def test_ensemble_arguments_rejected_before_device():
         og.Ensemble([(flat, dict(closure=og.DynamicSmagorinsky(averaging=(1, 2))))])
     with pytest.raises(ValueError, match="invalid ensemble arguments"):
         og.Ensemble([])
+
+
+def test_amd_coefficients_mirror_the_reference_keywords():
+    # AnisotropicMinimumDissipation(; C, Cν = C, Cκ = C, Cb) (anisotropic_minimum_dissipation.jl:138-147)
+    assert og.AnisotropicMinimumDissipation().C == 1.0 / 3.0
+    assert og.AnisotropicMinimumDissipation(C=0.2).C == 0.2
+    assert og.AnisotropicMinimumDissipation(Cnu=0.25, Ckappa=0.25).C == 0.25
+    with pytest.raises(ValueError, match="Cκ ≠ Cν"):
+        og.AnisotropicMinimumDissipation(Cnu=0.3, Ckappa=0.2)
+    with pytest.raises(ValueError, match="Cb"):
+        og.AnisotropicMinimumDissipation(Cb=1.0)

@@ -29,14 +29,29 @@ _TOPO = {Periodic: L.GBO_PERIODIC, Bounded: L.GBO_BOUNDED, Flat: L.GBO_FLAT}
 # Grids
 # ---------------------------------------------------------------------------
 class RectilinearGrid:
-    """RectilinearGrid(size, x, y, z, topology, float_type).
+    """RectilinearGrid(size, x, y, z, extent, topology, float_type).
 
     `z` is an extent tuple (regular spacing) or a callable / array of Nz+1
-    increasing face positions (stretched), as in the reference.
+    increasing face positions (stretched), as in the reference.  `extent = (Lx, Ly, Lz)`
+    ((Lx, Ly) with a Flat z) places the domain at 0 ≤ x ≤ Lx, 0 ≤ y ≤ Ly, -Lz ≤ z ≤ 0
+    and excludes x, y and z (src/Grids/rectilinear_grid.jl:121-124,
+    input_validation.jl:107-117).
     """
 
-    def __init__(self, size, x=(0.0, 1.0), y=(0.0, 1.0), z=(-1.0, 0.0),
-                 topology=(Periodic, Periodic, Bounded), float_type=np.float64, halo=None):
+    def __init__(self, size, x=None, y=None, z=None, topology=(Periodic, Periodic, Bounded),
+                 float_type=np.float64, halo=None, extent=None):
+        if extent is not None:
+            if x is not None or y is not None or z is not None:
+                raise ValueError("Cannot specify both 'extent' and 'x, y, z' keyword arguments.")
+            flat = tuple(topology)[2] == Flat
+            extent = tuple(float(e) for e in extent)
+            if len(extent) != (2 if flat else 3):
+                raise ValueError("extent must have %d entries for this topology" % (2 if flat else 3))
+            x, y = (0.0, extent[0]), (0.0, extent[1])
+            z = None if flat else (-extent[2], 0.0)
+        x = (0.0, 1.0) if x is None else x
+        y = (0.0, 1.0) if y is None else y
+        z = (-1.0, 0.0) if z is None else z
         topology = tuple(topology)
         if topology[0] != Periodic or topology[1] != Periodic:
             raise ValueError("only Periodic x and y topologies are supported")

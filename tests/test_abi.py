@@ -122,3 +122,13 @@ def test_amd_coefficients_mirror_the_reference_keywords():
         og.AnisotropicMinimumDissipation(Cnu=0.3, Ckappa=0.2)
     with pytest.raises(ValueError, match="Cb"):
         og.AnisotropicMinimumDissipation(Cb=1.0)
+
+
+def test_grid_extent_keyword():
+    # extent = (Lx, Ly, Lz): 0 ≤ x ≤ Lx, 0 ≤ y ≤ Ly, -Lz ≤ z ≤ 0 (rectilinear_grid.jl:121-124)
+    g = og.RectilinearGrid(size=(8, 8, 4), extent=(1, 2, 3))
+    assert g.x == (0.0, 1.0) and g.y == (0.0, 2.0) and g.z == (-3.0, 0.0)
+    f = og.RectilinearGrid(size=(8, 8), extent=(2 * np.pi, 4 * np.pi), topology=("Periodic", "Periodic", "Flat"))
+    assert f.x == (0.0, 2 * np.pi) and f.y == (0.0, 4 * np.pi)
+    with pytest.raises(ValueError, match="Cannot specify both"):
+        og.RectilinearGrid(size=(8, 8, 4), extent=(1, 1, 1), x=(0, 1))

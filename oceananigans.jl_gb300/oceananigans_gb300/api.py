@@ -446,7 +446,17 @@ class NonhydrostaticModel:
         else:
             zs = zc
         X, Y, Zz = np.meshgrid(xs, ys, zs, indexing="ij")
-        return np.vectorize(fn)(X, Y, Zz)
+        # one call on the coordinate arrays when fn maps them elementwise to an array of
+        # the field's shape; otherwise (scalar-only code, or a result that is not per point,
+        # such as one random draw) fn is called at every point, as the reference does
+        try:
+            with np.errstate(all="ignore"):
+                out = np.asarray(fn(X, Y, Zz), dtype=np.float64)
+            if out.shape == X.shape:
+                return out
+        except Exception:  # noqa: BLE001  (any failure means fn is not array-safe)
+            pass
+        return np.vectorize(fn, otypes=[np.float64])(X, Y, Zz)
 
     def get(self, name, dtype=np.float64):
         shp = self.field_shape(name)

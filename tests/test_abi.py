@@ -132,3 +132,22 @@ def test_grid_extent_keyword():
     assert f.x == (0.0, 2 * np.pi) and f.y == (0.0, 4 * np.pi)
     with pytest.raises(ValueError, match="Cannot specify both"):
         og.RectilinearGrid(size=(8, 8, 4), extent=(1, 1, 1), x=(0, 1))
+
+
+def test_callable_initial_conditions_evaluate_per_point():
+    # set!(model, u = f) evaluates f(x, y, z) at every node of the field's location
+    import math
+    from types import SimpleNamespace
+    g = og.RectilinearGrid(size=(8, 6, 4), extent=(1, 2, 3))
+    fake = SimpleNamespace(grid=g)
+    ev = lambda name, fn: og.NonhydrostaticModel._evaluate(fake, name, fn)  # noqa: E731
+    xc, yc, zc = g.nodes()
+    a = ev("b", lambda x, y, z: np.sin(x) * y + z)            # array-safe: one call
+    b = ev("b", lambda x, y, z: math.sin(x) * y + z)          # scalar-only: per point
+    assert a.shape == (8, 6, 4) and np.allclose(a, b, rtol=0, atol=1e-15)
+    assert np.allclose(a, np.sin(xc)[:, None, None] * yc[None, :, None] + zc[None, None, :])
+    rng = np.random.default_rng(0)
+    r = ev("u", lambda x, y, z: rng.standard_normal())        # one draw per point, not one in all
+    assert np.unique(r).size == r.size
+    w = ev("w", lambda x, y, z: z)                            # w at the Nz + 1 faces
+    assert w.shape == (8, 6, 5) and w[0, 0, 0] == -3.0 and w[0, 0, -1] == 0.0

@@ -91,7 +91,8 @@ typedef struct gbo_model_desc {
     int32_t advection;               /* gbo_advection */
     int32_t closure;                 /* gbo_closure */
     double  closure_C;               /* Smagorinsky C (0.16) or AMD C (1/3) */
-    double  closure_Cb;              /* Lilly reduction factor Cb (1.0); unused by AMD */
+    double  closure_Cb;              /* Lilly reduction factor Cb (1.0); 0 gives the constant-coefficient
+                                        Smagorinsky(coefficient = C); unused by AMD */
     double  closure_Pr;              /* turbulent Prandtl number for all tracers (1.0) */
     int32_t ntracers;                /* 0..GBO_MAX_TRACERS */
     int32_t buoyancy_tracer;         /* 1: tracer 0 is the BuoyancyTracer `b`; 0: no buoyancy */

@@ -9,6 +9,7 @@ RK3 time step (three substeps with their pressure projections) of the whole grid
 
 Other workloads (--workload), each with seeded synthetic inputs of the stated
 shapes and distributions:
+  convection_dynamic  the headline workload with DynamicSmagorinsky(averaging=(1, 2))
   turbulence2d    128×128 (Periodic, Periodic, Flat), u, v ~ U[-1, 1] projected,
                   WENO5, FP64, Δt = 0.01
   stretched_amd   512×512×256 with faces z_k = -256(1 - tanh(2(1 - k/256))/tanh 2),
@@ -74,6 +75,14 @@ def _convection(size, float_type):
             "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
             "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
             "b": 1e-5 * zc[None, None, :] + 1e-8 * rng.standard_normal((Nx, Ny, Nz))}
+    return grid, physics, init
+
+
+def _convection_dynamic(size, float_type):
+    """The convection workload with DynamicSmagorinsky(averaging=(1, 2)) as the closure."""
+    import oceananigans_gb300 as og
+    grid, physics, init = _convection(size, float_type)
+    physics["closure"] = og.DynamicSmagorinsky(averaging=(1, 2))
     return grid, physics, init
 
 
@@ -152,6 +161,8 @@ def ensemble_specs(n=64, float_type=np.float32, seed=2025):
 WORKLOADS = {
     "convection": dict(build=_convection, size=(256, 256, 128), dtype="f32", dt=2.0, cpu_size=(128, 128, 128),
                        name="free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft"),
+    "convection_dynamic": dict(build=_convection_dynamic, size=(256, 256, 128), dtype="f32", dt=2.0,
+                               cpu_size=(64, 64, 128), name="free_convection_%dx%dx%d_weno5_dynamic_smagorinsky_xy_fft"),
     "turbulence2d": dict(build=_turbulence2d, size=(128, 128, 1), dtype="f64", dt=0.01, cpu_size=(128, 128, 1),
                          name="turbulence2d_%dx%dx%d_weno5_fft"),
     "stretched_amd": dict(build=_stretched_amd, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),
@@ -313,7 +324,9 @@ def algorithmic_bytes(group, size, s, ntr=1, closure="smagorinsky", has_phy=True
     per = {
         "k_momentum": mom,
         "k_tracer": (3 + 1 + nu) + 2 + 2.0 / 3,
-        "k_closure": 4 + 1 + kap,
+        # DynamicSmagorinsky: Σ and Σ̄ (5), LM and MM (5), the coefficient (0) and νₑ (4),
+        # averaged over its four launches
+        "k_closure": 3.5 if closure == "dynamic" else 4 + 1 + kap,
         "k_hydrostatic": 2,
         "k_source": 4,
         "k_dct_z": 2,
@@ -544,7 +557,8 @@ def main():
     stream = torch.cuda.ExternalStream(sp.value)
     closure = {type(None): None}.get(type(physics.get("closure")), None)
     cl = physics.get("closure")
-    closure = None if cl is None else ("amd" if isinstance(cl, og.AnisotropicMinimumDissipation) else "smagorinsky")
+    closure = None if cl is None else ("amd" if isinstance(cl, og.AnisotropicMinimumDissipation) else
+                                       "dynamic" if isinstance(cl, og.DynamicSmagorinsky) else "smagorinsky")
     ntr = len(physics.get("tracers", ()))
     has_phy = ntr > 0 and grid.topology[2] == "Bounded" and physics.get("buoyancy") is not None
     fused = grid.bottom_height is None

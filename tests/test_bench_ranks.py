@@ -67,3 +67,20 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     with contextlib.redirect_stdout(out):
         bench.run_reference(argparse.Namespace(size=(8, 8, 8), workload="convection", steps=1, warmup=1, gpus=2))
     assert out.getvalue() == ""
+
+
+@pytest.mark.parametrize("name", ["convection", "convection_dynamic", "turbulence2d", "stretched_amd", "seamount"])
+def test_workloads_build_descriptors(name):
+    # every bench workload builds its grid, physics and inputs and translates into a
+    # descriptor (no device work)
+    import numpy as np
+    import bench
+    from oceananigans_gb300 import _lib as L
+    from oceananigans_gb300.api import model_descriptor
+    size = (32, 32, 1) if name == "turbulence2d" else (32, 32, 16)
+    grid, physics, init = bench.workload(name, size, np.float32)
+    d, tracers = model_descriptor(grid, **physics)
+    assert set(init) <= {"u", "v", "w"} | set(tracers)
+    if name == "convection_dynamic":
+        assert d.closure == L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY and d.closure_averaging == L.GBO_AVERAGING_XY
+        assert bench.algorithmic_bytes("k_closure", size, 4, closure="dynamic") == 3.5 * 32 * 32 * 16 * 4

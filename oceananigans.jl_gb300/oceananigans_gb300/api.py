@@ -246,8 +246,16 @@ class BuoyancyTracer:
 
 
 class FPlane:
-    def __init__(self, f):
-        self.f = float(f)
+    """FPlane(; f, rotation_rate=7.292115e-5, latitude) (Coriolis/f_plane.jl:30-50, the
+    rotation rate default of src/Oceananigans.jl:171): either f, or a rotation rate and a
+    latitude in degrees with f = 2 Ω sin(latitude).  (Julia's `sind` converts degrees in
+    extended precision, so f can differ from it in the last bit.)"""
+
+    def __init__(self, f=None, rotation_rate=7.292115e-5, latitude=None):
+        if (f is None) == (latitude is None):
+            raise ValueError("Either both keywords rotation_rate and latitude must be specified, "
+                             "*or* only f must be specified.")
+        self.f = float(f) if f is not None else 2 * float(rotation_rate) * math.sin(math.radians(float(latitude)))
 
 
 class FluxBoundaryCondition:

@@ -151,3 +151,13 @@ def test_callable_initial_conditions_evaluate_per_point():
     assert np.unique(r).size == r.size
     w = ev("w", lambda x, y, z: z)                            # w at the Nz + 1 faces
     assert w.shape == (8, 6, 5) and w[0, 0, 0] == -3.0 and w[0, 0, -1] == 0.0
+
+
+def test_fplane_keywords():
+    # FPlane(; f) or FPlane(; rotation_rate, latitude) with f = 2Ω sind(latitude) (f_plane.jl:30-50)
+    assert og.FPlane(1e-4).f == 1e-4 and og.FPlane(f=2e-4).f == 2e-4
+    assert abs(og.FPlane(latitude=45).f - 2 * 7.292115e-5 * np.sqrt(0.5)) <= 1e-20
+    assert abs(og.FPlane(rotation_rate=1e-4, latitude=90).f - 2e-4) <= 1e-20
+    for bad in (dict(), dict(f=1e-4, latitude=10.0)):
+        with pytest.raises(ValueError, match="Either both keywords"):
+            og.FPlane(**bad)

@@ -606,9 +606,12 @@ class Simulation:
     (src/Simulations/simulation.jl:68-119).  `dt` is converted to the model's float
     type as in the reference; `wizard` / `wizard_interval` add a TimeStepWizard callback."""
 
-    def __init__(self, model, dt, stop_time=math.inf, stop_iteration=math.inf, wall_time_limit=math.inf,
+    def __init__(self, model, dt=None, stop_time=math.inf, stop_iteration=math.inf, wall_time_limit=math.inf,
                  align_time_step=True, minimum_relative_step=0.0, nan_check_interval=100, nan_erroring=False,
-                 wizard=None, wizard_interval=10):
+                 wizard=None, wizard_interval=10, Δt=None):
+        if (dt is None) == (Δt is None):
+            raise ValueError("Simulation needs the time step as dt or Δt (one of them)")
+        dt = Δt if dt is None else dt
         self.model = model
         ft = np.float32 if model.dtype == np.float32 else np.float64
         self.dt = float(ft(dt))

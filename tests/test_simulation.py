@@ -69,3 +69,17 @@ def test_wizard_argument_checks():
         og.TimeStepWizard(min_change=1.0)
     with pytest.raises(ValueError, match="max_change"):
         og.TimeStepWizard(max_change=1.0)
+
+
+def test_simulation_time_step_keyword():
+    # Simulation(model; Δt, ...) (simulation.jl:68-119); dt is the ASCII spelling, and Δt is
+    # converted to the model's float type
+    from types import SimpleNamespace
+    import oceananigans_gb300 as og
+    m = SimpleNamespace(dtype=np.float32)
+    assert og.Simulation(m, Δt=0.1).dt == float(np.float32(0.1))
+    assert og.Simulation(m, dt=2.0, stop_iteration=3).dt == 2.0
+    with pytest.raises(ValueError, match="dt or Δt"):
+        og.Simulation(m)
+    with pytest.raises(ValueError, match="dt or Δt"):
+        og.Simulation(m, dt=1.0, Δt=1.0)

@@ -61,21 +61,75 @@ def parse():
     return a
 
 
+PPB = ("Periodic", "Periodic", "Bounded")
+
+
+def _noise_init(size, zc, N2, bnoise, U=0.0, seed=2024):
+    """u = U + 1e-3 U[-1, 1], v, w = 1e-3 U[-1, 1], b = N² z + bnoise N(0, 1) (seeded)."""
+    Nx, Ny, Nz = size
+    rng = np.random.default_rng(seed)
+    return {"u": U + 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
+            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
+            "b": N2 * zc[None, None, :] + bnoise * rng.standard_normal((Nx, Ny, Nz))}
+
+
+# Each workload is described once in plain numbers: grid keywords, the oracle's model
+# description (oracle.model_desc keywords) and the seeded initial fields.  The library's
+# model objects are built from the same numbers by the functions after these.
+def _convection_spec(size, float_type):
+    Nx, Ny, Nz = size
+    gkw = dict(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=(-256.0, 0.0), topology=PPB,
+               float_type=float_type)
+    ophys = dict(closure="SmagorinskyLilly", buoyancy=True, coriolis=1e-4, tracers=("b",), flux_top={"b": 1e-8})
+    zc = -256.0 + (np.arange(Nz) + 0.5) * 256.0 / Nz
+    return gkw, ophys, _noise_init(size, zc, 1e-5, 1e-8)
+
+
+def _convection_dynamic_spec(size, float_type):
+    gkw, ophys, init = _convection_spec(size, float_type)
+    return gkw, dict(ophys, closure=("DynamicSmagorinsky", {"averaging": (1, 2)})), init
+
+
+def _turbulence2d_spec(size, float_type):
+    Nx, Ny = size[0], size[1]
+    gkw = dict(size=(Nx, Ny), x=(0, 2 * np.pi), y=(0, 2 * np.pi), topology=("Periodic", "Periodic", "Flat"),
+               float_type=float_type)
+    rng = np.random.default_rng(2024)
+    return gkw, {}, {"u": rng.uniform(-1, 1, (Nx, Ny, 1)), "v": rng.uniform(-1, 1, (Nx, Ny, 1))}
+
+
+def _stretched_amd_spec(size, float_type):
+    Nx, Ny, Nz = size
+    # faces -256 (1 - tanh(2 (1 - k/Nz)) / tanh 2), k = 0..Nz, in increasing order (finest at the surface)
+    zf = np.sort([-256.0 * (1 - np.tanh(2 * (1 - k / Nz)) / np.tanh(2)) for k in range(Nz + 1)])
+    gkw = dict(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=zf, topology=PPB, float_type=float_type)
+    ophys = dict(closure="AnisotropicMinimumDissipation", buoyancy=True, coriolis=1e-4, tracers=("b",),
+                 flux_top={"b": 1e-8}, pressure_solver="FourierTridiagonalPoissonSolver")
+    return gkw, ophys, _noise_init(size, 0.5 * (zf[1:] + zf[:-1]), 1e-5, 1e-8)
+
+
+def _seamount_bottom(x, y):
+    return -2000.0 + 1200.0 * np.exp(-(x * x + y * y) / (2 * 800.0 ** 2))
+
+
+def _seamount_spec(size, float_type):
+    Nz = size[2]
+    gkw = dict(size=size, x=(-5000.0, 5000.0), y=(-5000.0, 5000.0), z=(-2000.0, 0.0), topology=PPB,
+               float_type=float_type)
+    ophys = dict(buoyancy=True, tracers=("b",),
+                 pressure_solver=("ConjugateGradientPoissonSolver", {"reltol": 1e-8, "abstol": 1e-30}))
+    zc = -2000.0 + (np.arange(Nz) + 0.5) * 2000.0 / Nz
+    return dict(gkw, bottom_height=_seamount_bottom), ophys, _noise_init(size, zc, 1e-6, 1e-9, U=0.1)
+
+
 def _convection(size, float_type):
     import oceananigans_gb300 as og
-    Nx, Ny, Nz = size
-    grid = og.RectilinearGrid(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=(-256.0, 0.0),
-                              topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    gkw, _, init = _convection_spec(size, float_type)
     physics = dict(advection=og.WENO(), closure=og.SmagorinskyLilly(), buoyancy=og.BuoyancyTracer(),
                    coriolis=og.FPlane(1e-4), tracers=("b",),
                    boundary_conditions={"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(1e-8))})
-    rng = np.random.default_rng(2024)
-    _, _, zc = grid.nodes()
-    init = {"u": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
-            "b": 1e-5 * zc[None, None, :] + 1e-8 * rng.standard_normal((Nx, Ny, Nz))}
-    return grid, physics, init
+    return og.RectilinearGrid(**gkw), physics, init
 
 
 def _convection_dynamic(size, float_type):
@@ -88,49 +142,28 @@ def _convection_dynamic(size, float_type):
 
 def _turbulence2d(size, float_type):
     import oceananigans_gb300 as og
-    Nx, Ny = size[0], size[1]
-    grid = og.RectilinearGrid(size=(Nx, Ny), x=(0, 2 * np.pi), y=(0, 2 * np.pi),
-                              topology=("Periodic", "Periodic", "Flat"), float_type=float_type)
-    rng = np.random.default_rng(2024)
-    init = {"u": rng.uniform(-1, 1, (Nx, Ny, 1)), "v": rng.uniform(-1, 1, (Nx, Ny, 1))}
-    return grid, dict(advection=og.WENO()), init
+    gkw, _, init = _turbulence2d_spec(size, float_type)
+    return og.RectilinearGrid(**gkw), dict(advection=og.WENO()), init
 
 
 def _stretched_amd(size, float_type):
     import oceananigans_gb300 as og
-    Nx, Ny, Nz = size
-    # faces -256 (1 - tanh(2 (1 - k/Nz)) / tanh 2), k = 0..Nz, in increasing order (finest at the surface)
-    zf = np.sort([-256.0 * (1 - np.tanh(2 * (1 - k / Nz)) / np.tanh(2)) for k in range(Nz + 1)])
-    grid = og.RectilinearGrid(size=size, x=(0, 512.0 * Nx / 256), y=(0, 512.0 * Ny / 256), z=zf,
-                              topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
+    gkw, _, init = _stretched_amd_spec(size, float_type)
     physics = dict(advection=og.WENO(), closure=og.AnisotropicMinimumDissipation(), buoyancy=og.BuoyancyTracer(),
                    coriolis=og.FPlane(1e-4), tracers=("b",),
                    boundary_conditions={"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(1e-8))},
                    pressure_solver=og.FourierTridiagonalPoissonSolver())
-    rng = np.random.default_rng(2024)
-    _, _, zc = grid.nodes()
-    init = {"u": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
-            "b": 1e-5 * zc[None, None, :] + 1e-8 * rng.standard_normal((Nx, Ny, Nz))}
-    return grid, physics, init
+    return og.RectilinearGrid(**gkw), physics, init
 
 
 def _seamount(size, float_type):
     import oceananigans_gb300 as og
-    Nx, Ny, Nz = size
-    under = og.RectilinearGrid(size=size, x=(-5000.0, 5000.0), y=(-5000.0, 5000.0), z=(-2000.0, 0.0),
-                               topology=("Periodic", "Periodic", "Bounded"), float_type=float_type)
-    grid = og.ImmersedBoundaryGrid(under, og.GridFittedBottom(
-        lambda x, y: -2000.0 + 1200.0 * np.exp(-(x * x + y * y) / (2 * 800.0 ** 2))))
+    gkw, _, init = _seamount_spec(size, float_type)
+    gkw = dict(gkw)
+    bottom = gkw.pop("bottom_height")
+    grid = og.ImmersedBoundaryGrid(og.RectilinearGrid(**gkw), og.GridFittedBottom(bottom))
     physics = dict(advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
                    pressure_solver=og.ConjugateGradientPoissonSolver(reltol=1e-8, abstol=1e-30))
-    rng = np.random.default_rng(2024)
-    _, _, zc = under.nodes()
-    init = {"u": 0.1 + 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "v": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz)),
-            "w": 1e-3 * rng.uniform(-1, 1, (Nx, Ny, Nz + 1)),
-            "b": 1e-6 * zc[None, None, :] + 1e-9 * rng.standard_normal((Nx, Ny, Nz))}
     return grid, physics, init
 
 
@@ -159,17 +192,17 @@ def ensemble_specs(n=64, float_type=np.float32, seed=2025):
 
 
 WORKLOADS = {
-    "convection": dict(build=_convection, size=(256, 256, 128), dtype="f32", dt=2.0, cpu_size=(128, 128, 128),
+    "convection": dict(build=_convection, spec=_convection_spec, size=(256, 256, 128), dtype="f32", dt=2.0, cpu_size=(128, 128, 128),
                        name="free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft"),
-    "convection_dynamic": dict(build=_convection_dynamic, size=(256, 256, 128), dtype="f32", dt=2.0,
+    "convection_dynamic": dict(build=_convection_dynamic, spec=_convection_dynamic_spec, size=(256, 256, 128), dtype="f32", dt=2.0,
                                cpu_size=(64, 64, 128), name="free_convection_%dx%dx%d_weno5_dynamic_smagorinsky_xy_fft"),
-    "turbulence2d": dict(build=_turbulence2d, size=(128, 128, 1), dtype="f64", dt=0.01, cpu_size=(128, 128, 1),
+    "turbulence2d": dict(build=_turbulence2d, spec=_turbulence2d_spec, size=(128, 128, 1), dtype="f64", dt=0.01, cpu_size=(128, 128, 1),
                          name="turbulence2d_%dx%dx%d_weno5_fft"),
-    "stretched_amd": dict(build=_stretched_amd, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),
+    "stretched_amd": dict(build=_stretched_amd, spec=_stretched_amd_spec, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),
                           name="stretched_convection_%dx%dx%d_weno5_amd_fourier_tridiagonal"),
-    "ensemble": dict(build=None, size=(0, 0, 0), dtype="f32", dt=1.0, cpu_size=(128, 128, 128),
+    "ensemble": dict(build=None, spec=None, size=(0, 0, 0), dtype="f32", dt=1.0, cpu_size=(128, 128, 128),
                      name="ensemble_64_members_convection_smagorinsky_fft"),
-    "seamount": dict(build=_seamount, size=(256, 256, 128), dtype="f32", dt=20.0, cpu_size=(64, 64, 128),
+    "seamount": dict(build=_seamount, spec=_seamount_spec, size=(256, 256, 128), dtype="f32", dt=20.0, cpu_size=(64, 64, 128),
                      name="seamount_ibg_%dx%dx%d_weno5_fft_pcg"),
 }
 
@@ -204,7 +237,6 @@ def config_dict(args, n):
 def cpu_sample(name, steps_budget_s=20.0):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from oceananigans_gb300.api import model_descriptor
     oracle.build()
     nthreads = os.cpu_count() or 1
     oracle.set_threads(nthreads)
@@ -212,17 +244,11 @@ def cpu_sample(name, steps_budget_s=20.0):
     w = WORKLOADS[name]
     size = w["cpu_size"]
     dt = w["dt"]
-    # the ensemble's members carry the convection physics
-    grid, physics, init = workload("convection" if name == "ensemble" else name, size, np.float64)
-    d = grid.descriptor()
-    g = oracle.GridDesc()
-    for f, _ in oracle.GridDesc._fields_:
-        setattr(g, f, getattr(d, f))
-    md, tracers = model_descriptor(grid, **physics)
-    m = oracle.ModelDesc()
-    for f, _ in oracle.ModelDesc._fields_:
-        setattr(m, f, getattr(md, f))
-    ref = oracle.OracleModel(g, m, tracers=tracers)
+    # the ensemble's members carry the convection physics; the oracle is configured from
+    # its own description of the workload (reference defaults), not through the library
+    spec = WORKLOADS["convection" if name == "ensemble" else name]["spec"]
+    gkw, ophys, init = spec(size, np.float64)
+    ref = oracle.model(gkw, **ophys)
     ref.set(**init)
     ref.finalize_set(True)
     ref.time_step(dt, 1)  # warm-up

@@ -127,6 +127,15 @@ typedef struct gbo_model gbo_model;
 /* Fill *d with the reference's defaults: WENO5, no closure, no tracers, FFT solver. */
 void gbo_model_desc_default(gbo_model_desc* d);
 
+/* The conjugate-gradient stopping parameters a model of this grid and descriptor uses,
+ * with zeros replaced by the reference's defaults: reltol = abstol = sqrt(eps(FT)) and
+ * maxiter = Nx*Ny*Nz (ConjugateGradientPoissonSolver(grid; reltol, abstol, maxiter),
+ * src/Solvers/conjugate_gradient_poisson_solver.jl:134-137, conjugate_gradient_solver.jl:91;
+ * the reference's summary shows them, conjugate_gradient_poisson_solver.jl:55-57).
+ * Host only; no device is needed. */
+int gbo_cg_parameters(const gbo_grid_desc* grid, const gbo_model_desc* desc, double* reltol, double* abstol,
+                      double* maxiter);
+
 /* Construct a model on the current CUDA device.
  * Replaces NonhydrostaticModel(grid; ...) (nonhydrostatic_model.jl:124). */
 int gbo_model_create(const gbo_grid_desc* grid, const gbo_model_desc* desc, gbo_model** out);

@@ -167,6 +167,17 @@ namespace {
 
 thread_local std::string g_last_error = "";
 
+// Conjugate-gradient stopping parameters with the reference's defaults filled in:
+// reltol = abstol = sqrt(eps(FT)) (conjugate_gradient_poisson_solver.jl:134-137) and
+// maxiter = the number of cells (conjugate_gradient_solver.jl:91).
+void cg_parameters(int32_t float_type, const gbo_model_desc& d, int64_t cells, double* rel, double* abs_,
+                   double* maxiter) {
+    const double eps = float_type == GBO_FLOAT32 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+    *rel = d.cg_reltol > 0 ? d.cg_reltol : std::sqrt(eps);
+    *abs_ = d.cg_abstol > 0 ? d.cg_abstol : std::sqrt(eps);
+    *maxiter = d.cg_maxiter > 0 ? (double)d.cg_maxiter : (double)cells;
+}
+
 struct CudaError {
     cudaError_t e;
     const char* what;
@@ -892,13 +903,10 @@ struct ModelImpl : gbo_model {
     // reads the stop flag after each iteration.  Non-convergence is reported through
     // CG_FAIL when the step (or solve) is synchronised.
     int cg_iterate() {
-        const double eps = sizeof(FT) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
-        const double rel = desc.cg_reltol > 0 ? desc.cg_reltol : std::sqrt(eps);
-        const double abs_ = desc.cg_abstol > 0 ? desc.cg_abstol : std::sqrt(eps);
-        // maxiter defaults to the number of cells as in the reference; the device loop is
-        // additionally capped so that a stagnating solve ends in bounded time
-        const double maxiter = std::min((double)GBO_CG_MAX_ITERATIONS,
-                                        desc.cg_maxiter > 0 ? (double)desc.cg_maxiter : (double)N);
+        double rel, abs_, maxiter;
+        cg_parameters(sizeof(FT) == 4 ? GBO_FLOAT32 : GBO_FLOAT64, desc, (int64_t)N, &rel, &abs_, &maxiter);
+        // the device loop is additionally capped so that a stagnating solve ends in bounded time
+        maxiter = std::min((double)GBO_CG_MAX_ITERATIONS, maxiter);
         const unsigned lin = (unsigned)std::min<size_t>((N + 255) / 256, 4 * 152 * 8);
         const bool pc = desc.preconditioner == GBO_PRECOND_FFT;
         const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
@@ -1761,6 +1769,14 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
 void gbo_record_error(const char* msg) { g_last_error = msg; }
 
 extern "C" {
+
+int gbo_cg_parameters(const gbo_grid_desc* grid, const gbo_model_desc* desc, double* reltol, double* abstol,
+                      double* maxiter) {
+    if (!grid || !desc || !reltol || !abstol || !maxiter) return GBO_ERR_INVALID;
+    const int64_t cells = (int64_t)grid->size[0] * grid->size[1] * (grid->topology[2] == GBO_FLAT ? 1 : grid->size[2]);
+    cg_parameters(grid->float_type, *desc, cells, reltol, abstol, maxiter);
+    return GBO_OK;
+}
 
 void gbo_model_desc_default(gbo_model_desc* d) {
     std::memset(d, 0, sizeof(*d));

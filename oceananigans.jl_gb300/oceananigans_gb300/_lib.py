@@ -93,6 +93,9 @@ class RunResult(ctypes.Structure):
 _vp = ctypes.c_void_p
 SIGNATURES = {
     "gbo_model_desc_default": (None, [ctypes.POINTER(ModelDesc)]),
+    "gbo_cg_parameters": (ctypes.c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc),
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
     "gbo_model_create": (ctypes.c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(ModelDesc), ctypes.POINTER(_vp)]),
     "gbo_model_destroy": (None, [_vp]),
     "gbo_set_field": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int64]),

@@ -190,6 +190,168 @@ class OracleNotConverged(RuntimeError):
     pass
 
 
+# ---------------------------------------------------------------------------
+# Configuration.  The oracle's grid and model descriptors are built here from a
+# plain description of the physics, and every parameter the description leaves
+# out takes the reference's default, restated below from the Oceananigans.jl
+# v0.110.19 sources.  Nothing is read from the library under test (its defaults
+# are checked against this table by tests/test_oracle_config.py).
+# ---------------------------------------------------------------------------
+REFERENCE_DEFAULTS = {
+    # SmagorinskyLilly(...; C=0.16, Cb=1, Pr=1)  (Smagorinskys/lilly_coefficient.jl:109)
+    "SmagorinskyLilly": {"C": 0.16, "Cb": 1.0, "Pr": 1.0},
+    # Smagorinsky(; coefficient=0.16, Pr=1.0)  (Smagorinskys/smagorinsky.jl:51-52, 78)
+    "Smagorinsky": {"coefficient": 0.16, "Pr": 1.0},
+    # AnisotropicMinimumDissipation(; C=1/3, Cν=C, Cκ=C, Cb=nothing)
+    # (anisotropic_minimum_dissipation.jl:139-142)
+    "AnisotropicMinimumDissipation": {"C": 1.0 / 3.0},
+    # DynamicSmagorinsky(; averaging=LagrangianAveraging(), Pr=1, minimum_numerator=1e-32)
+    # (Smagorinskys/dynamic_coefficient.jl:107-112)
+    "DynamicSmagorinsky": {"averaging": "lagrangian", "Pr": 1.0, "minimum_numerator": 1e-32},
+    # ScalarDiffusivity(; ν=0, κ=0)  (scalar_diffusivity.jl:113-116)
+    "ScalarDiffusivity": {"nu": 0.0, "kappa": 0.0},
+    # QuasiAdamsBashforth2TimeStepper(; χ=0.1)  (TimeSteppers/quasi_adams_bashforth_2.jl:63)
+    "QuasiAdamsBashforth2": {"chi": 0.1},
+    # ConjugateGradientPoissonSolver(grid; reltol=sqrt(eps(grid)), abstol=sqrt(eps(grid)))
+    # (Solvers/conjugate_gradient_poisson_solver.jl:134-137), maxiter=prod(size(template_field))
+    # (Solvers/conjugate_gradient_solver.jl:91), the FFT solver of the underlying grid as the
+    # preconditioner of an immersed grid (conjugate_gradient_poisson_solver.jl:141-147)
+    "ConjugateGradientPoissonSolver": {"reltol": "sqrt(eps(FT))", "abstol": "sqrt(eps(FT))",
+                                       "maxiter": "Nx*Ny*Nz", "preconditioner": "fft"},
+    # FPlane(; rotation_rate=Oceananigans.defaults.planet_rotation_rate)
+    # (Coriolis/f_plane.jl:17; src/Oceananigans.jl:171)
+    "FPlane": {"rotation_rate": 7.292115e-5},
+}
+
+# descriptor codes (the C layout both libraries accept)
+_CLOSURE_CODES = {None: 0, "SmagorinskyLilly": 1, "Smagorinsky": 1, "AnisotropicMinimumDissipation": 2,
+                  "ScalarDiffusivity": 3, "DynamicSmagorinsky": 4}
+_SOLVER_CODES = {"FFTBasedPoissonSolver": 0, "FourierTridiagonalPoissonSolver": 1,
+                 "ConjugateGradientPoissonSolver": 2}
+_PRECOND_CODES = {"fft": 0, None: 1, "learned": 2}
+
+
+def grid_desc(size, x, y, z=(-1.0, 0.0), topology=("Periodic", "Periodic", "Bounded"), float_type=np.float64,
+              bottom_height=None):
+    """GridDesc of RectilinearGrid(size, x, y, z, topology), optionally wrapped in
+    ImmersedBoundaryGrid(GridFittedBottom(h)): `z` is an extent or the Nz+1 increasing
+    face positions; `bottom_height` a callable h(x, y) evaluated here at the cell centres
+    (rectilinear_grid.jl:266-305), or an (Nx, Ny) array."""
+    flat = topology[2] == "Flat"
+    size = tuple(int(s) for s in size)
+    if flat and len(size) == 2:
+        size = size + (1,)
+    Nx, Ny, Nz = size
+    g = GridDesc()
+    g.size[:] = (Nx, Ny, 1 if flat else Nz)
+    codes = {"Flat": GBO_FLAT, "Periodic": GBO_PERIODIC, "Bounded": GBO_BOUNDED}
+    g.topology[:] = tuple(codes[t] for t in topology)
+    g.x[:] = tuple(float(a) for a in x)
+    g.y[:] = tuple(float(a) for a in y)
+    keep = []
+    if flat:
+        g.z[:] = (0.0, 1.0)
+    elif np.ndim(z) == 1 and len(z) == Nz + 1:
+        zf = np.ascontiguousarray(z, dtype=np.float64)
+        keep.append(zf)
+        g.z_faces = zf.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        g.z[:] = (float(zf[0]), float(zf[-1]))
+    else:
+        g.z[:] = tuple(float(a) for a in z)
+    if bottom_height is not None:
+        if callable(bottom_height):
+            xc = g.x[0] + (np.arange(Nx) + 0.5) * (g.x[1] - g.x[0]) / Nx
+            yc = g.y[0] + (np.arange(Ny) + 0.5) * (g.y[1] - g.y[0]) / Ny
+            X, Y = np.meshgrid(xc, yc, indexing="ij")
+            h = np.vectorize(bottom_height, otypes=[np.float64])(X, Y)
+        else:
+            h = np.asarray(bottom_height, dtype=np.float64).reshape(Nx, Ny)
+        h = np.ascontiguousarray(h.ravel(order="F"))
+        keep.append(h)
+        g.bottom_height = h.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    g.float_type = GBO_FLOAT32 if np.dtype(float_type) == np.float32 else GBO_FLOAT64
+    g._keep = keep
+    return g
+
+
+def model_desc(grid, closure=None, buoyancy=False, coriolis=None, tracers=(), flux_top=None, flux_bottom=None,
+               pressure_solver=None, timestepper="RungeKutta3"):
+    """ModelDesc of NonhydrostaticModel(grid; advection=WENO(), closure, buoyancy, coriolis,
+    tracers, boundary_conditions, pressure_solver, timestepper).
+
+    closure, pressure_solver, timestepper: None, a name, or (name, {parameters}); a parameter
+    left out takes REFERENCE_DEFAULTS.  coriolis: f, or {"latitude": φ[, "rotation_rate": Ω]}.
+    buoyancy: True for BuoyancyTracer (tracer b first).  flux_top / flux_bottom: {tracer: flux}.
+    The pressure solver defaults as in nonhydrostatic_pressure_solver
+    (NonhydrostaticModels.jl:30-76): FFT on a regular grid, Fourier-tridiagonal on a stretched one.
+    """
+    def named(spec):
+        if spec is None:
+            return None, {}
+        if isinstance(spec, str):
+            return spec, {}
+        return spec[0], dict(spec[1])
+
+    tracers = tuple(tracers)
+    if buoyancy:
+        tracers = ("b",) + tuple(t for t in tracers if t != "b")
+    Nx, Ny, Nz = grid.size
+    ft = np.float32 if grid.float_type == GBO_FLOAT32 else np.float64
+    d = ModelDesc()
+    d.advection = 5
+    name, p = named(closure)
+    d.closure = _CLOSURE_CODES[name]
+    if name is not None:
+        q = dict(REFERENCE_DEFAULTS[name], **p)
+        if name == "SmagorinskyLilly":
+            d.closure_C, d.closure_Cb, d.closure_Pr = q["C"], q["Cb"], q["Pr"]
+        elif name == "Smagorinsky":  # constant coefficient: the Lilly form without the N² reduction
+            d.closure_C, d.closure_Cb, d.closure_Pr = q["coefficient"], 0.0, q["Pr"]
+        elif name == "AnisotropicMinimumDissipation":
+            d.closure_C = q["C"]
+        elif name == "DynamicSmagorinsky":
+            d.closure_Pr, d.closure_min_numerator = q["Pr"], q["minimum_numerator"]
+            d.closure_averaging = 1 if q["averaging"] == "lagrangian" else 0
+        elif name == "ScalarDiffusivity":
+            d.closure_nu = q["nu"]
+            for n, t in enumerate(tracers):
+                d.closure_kappa[n] = q["kappa"][t] if isinstance(q["kappa"], dict) else q["kappa"]
+    d.ntracers = len(tracers)
+    d.buoyancy_tracer = int(bool(buoyancy))
+    if coriolis is not None:
+        d.has_coriolis = 1
+        if isinstance(coriolis, dict):
+            omega = coriolis.get("rotation_rate", REFERENCE_DEFAULTS["FPlane"]["rotation_rate"])
+            d.coriolis_f = 2 * omega * math.sin(math.radians(coriolis["latitude"]))
+        else:
+            d.coriolis_f = float(coriolis)
+    for src, dst in ((flux_top or {}, d.tracer_flux_top), (flux_bottom or {}, d.tracer_flux_bottom)):
+        for t, q in src.items():
+            dst[tracers.index(t)] = q
+    name, p = named(pressure_solver)
+    if name is None:
+        name = "FFTBasedPoissonSolver" if not grid.z_faces else "FourierTridiagonalPoissonSolver"
+    d.pressure_solver = _SOLVER_CODES[name]
+    if name == "ConjugateGradientPoissonSolver":
+        q = dict(REFERENCE_DEFAULTS[name], **p)
+        tol = math.sqrt(float(np.finfo(ft).eps))
+        d.cg_reltol = tol if q["reltol"] == "sqrt(eps(FT))" else q["reltol"]
+        d.cg_abstol = tol if q["abstol"] == "sqrt(eps(FT))" else q["abstol"]
+        d.cg_maxiter = Nx * Ny * Nz if q["maxiter"] == "Nx*Ny*Nz" else q["maxiter"]
+        d.preconditioner = _PRECOND_CODES[q["preconditioner"]]
+    name, p = named(timestepper)
+    d.timestepper = 1 if name == "QuasiAdamsBashforth2" else 0
+    d.ab2_chi = dict(REFERENCE_DEFAULTS["QuasiAdamsBashforth2"], **p)["chi"]
+    return d, tracers
+
+
+def model(grid_kw, **physics):
+    """An OracleModel from grid_desc keywords and model_desc keywords."""
+    g = grid_desc(**grid_kw)
+    d, tracers = model_desc(g, **physics)
+    return OracleModel(g, d, tracers=tracers)
+
+
 def _checked(rc):
     if rc == -4:
         raise OracleNotConverged("oracle conjugate-gradient solve hit maxiter")

@@ -357,7 +357,8 @@ def test_constant_smagorinsky_is_lilly_without_buoyancy_reduction():
     # Smagorinsky(coefficient=C): νₑ = C² Δᶠ² √(2Σ²) (smagorinsky.jl:90-106), here from the
     # oracle through the Lilly path with Cb = 0, against the numpy strain
     c = _random_case(closure=None)
-    c.physics["closure"] = og.Smagorinsky(coefficient=0.2)
+    c = c.with_physics(dict(c.ophysics, closure=("Smagorinsky", {"coefficient": 0.2})),
+                       **dict(c.physics, closure=og.Smagorinsky(coefficient=0.2)))
     ref = c.oracle_model()
     ref.set(**c.init)
     ref.finalize_set(False)

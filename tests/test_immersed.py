@@ -66,7 +66,10 @@ def test_immersed_grid_without_immersed_cells_matches_rectilinear():
     flat = cases.seamount((16, 16, 12), solver="fft", height=-500.0)
     ref_ibg = flat.start_oracle()
     plain_grid = flat.grid.underlying_grid
-    plain = cases.Case(plain_grid, flat.init, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
+    plain_ogrid = {k: v for k, v in flat.ogrid.items() if k != "bottom_height"}
+    plain = cases.Case(plain_grid, flat.init, plain_ogrid,
+                       dict(buoyancy=True, tracers=("b",), pressure_solver="FFTBasedPoissonSolver"),
+                       advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("b",),
                        pressure_solver=og.FFTBasedPoissonSolver())
     ref_plain = plain.start_oracle()
     for r in (ref_ibg, ref_plain):
@@ -103,7 +106,10 @@ def test_immersed_closure_without_immersed_cells_matches_rectilinear(closure):
     # closure when no cell is immersed
     flat = cases.seamount((16, 16, 12), solver="fft", height=-500.0, closure=closure, U=0.02, noise=2e-2)
     ref_ibg = flat.start_oracle()
-    plain = cases.Case(flat.grid.underlying_grid, flat.init, **dict(flat.physics, pressure_solver=og.FFTBasedPoissonSolver()))
+    plain_ogrid = {k: v for k, v in flat.ogrid.items() if k != "bottom_height"}
+    plain = cases.Case(flat.grid.underlying_grid, flat.init, plain_ogrid,
+                       dict(flat.ophysics, pressure_solver="FFTBasedPoissonSolver"),
+                       **dict(flat.physics, pressure_solver=og.FFTBasedPoissonSolver()))
     ref_plain = plain.start_oracle()
     for r in (ref_ibg, ref_plain):
         r.time_step(20.0, 2)

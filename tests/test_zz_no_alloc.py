@@ -29,9 +29,9 @@ CASES = [
 
 def _case(kind, shape, float_type):
     if kind == "flat":
-        grid = og.RectilinearGrid(size=shape[:2], x=(0, 2 * np.pi), y=(0, 3.0),
-                                  topology=("Periodic", "Periodic", "Flat"), float_type=float_type)
-        return cases.Case(grid, {}, advection=og.WENO())
+        gkw = dict(size=shape[:2], x=(0, 2 * np.pi), y=(0, 3.0), topology=("Periodic", "Periodic", "Flat"),
+                   float_type=float_type)
+        return cases.Case(og.RectilinearGrid(**gkw), {}, gkw, {}, advection=og.WENO())
     return cases.convection_3d(shape, float_type=float_type)
 
 

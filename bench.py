@@ -314,10 +314,10 @@ class ClockSampler:
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch from an ncu
-# capture of this workload; the capture, its command and the algorithmic bytes of the
-# same launch are in the named profile.
+# capture of this workload, keyed by (workload, kernel group, grid, float type); the
+# capture, its command and the algorithmic bytes of the same launch are in the named profile.
 PROFILED_TRAFFIC = {
-    ("k_momentum", (256, 256, 128), "f32"): {
+    ("convection", "k_momentum", (256, 256, 128), "f32"): {
         "traffic": 426.7e6,
         "traffic_launch": "one RK3 stage-1 launch (algorithmic bytes of that launch 469.8e6; stages 2-3 also read G-)",
         "traffic_profile": "profiles/k_momentum_fused_free_convection_256x256x128_f32.md",
@@ -446,6 +446,107 @@ def held_out_solves(model, grid, torch, stream, ft, n=50):
             "iterations_mean": float(np.mean(iters)), "ms_per_iteration": float(np.sum(times) / max(1, np.sum(iters))),
             "preconditioner": "fft", "reltol": 1e-8,
             "path": "gbo_poisson_solve_device from a zero initial guess (host reads the stop flag each iteration)"}
+
+
+def torch_fft_poisson(torch, rhs, Lx, Ly, Lz):
+    """∇²ϕ = rhs on a regular (Periodic, Periodic, Bounded) grid with torch.fft (cuFFT):
+    DCT-II in z by Makhoul's reordering and one complex FFT, real FFT in x and FFT in y,
+    division by the eigenvalues (zero mean), and the inverse transforms -- the transform
+    chain of the reference's GPU solver, which calls cuFFT (fft_based_poisson_solver.jl:94-136,
+    ext/OceananigansCUDAExt.jl:118-129).  rhs: (Nz, Ny, Nx) tensor, x fastest.  Used only
+    as a timing yardstick beside the library's hand-written passes."""
+    Nz, Ny, Nx = rhs.shape
+    dev, rdt = rhs.device, rhs.dtype
+    k = torch.arange(Nz, device=dev, dtype=rdt)
+    w = torch.polar(torch.ones_like(k), -torch.pi * k / (2 * Nz)).reshape(Nz, 1, 1)
+    v = torch.cat([rhs[0::2], rhs[1::2].flip(0)], 0)
+    X = (w * torch.fft.fft(v, dim=0)).real                       # DCT-II along z
+    F = torch.fft.rfft2(X, dim=(1, 2))                           # FFT in y, real FFT in x
+    lx = (2 * torch.sin(torch.pi * torch.arange(Nx // 2 + 1, device=dev, dtype=rdt) / Nx) / (Lx / Nx)) ** 2
+    ly = (2 * torch.sin(torch.pi * torch.arange(Ny, device=dev, dtype=rdt) / Ny) / (Ly / Ny)) ** 2
+    lz = (2 * torch.sin(torch.pi * k / (2 * Nz)) / (Lz / Nz)) ** 2
+    lam = -(lz.reshape(Nz, 1, 1) + ly.reshape(1, Ny, 1) + lx.reshape(1, 1, -1))
+    lam[0, 0, 0] = 1
+    F = F / lam
+    F[0, 0, 0] = 0
+    X = torch.fft.irfft2(F, s=(Ny, Nx), dim=(1, 2))
+    # inverse DCT-II: V_k = e^{iπk/2N} (X_k - i X_{N-k}), X_N = 0, v = ifft(V), then un-reorder
+    Xr = torch.cat([torch.zeros_like(X[:1]), X[1:].flip(0)], 0)
+    V = torch.conj(w) * torch.complex(X, -Xr)
+    vv = torch.fft.ifft(V, dim=0).real
+    out = torch.empty_like(rhs)
+    h = (Nz + 1) // 2
+    out[0::2] = vv[:h]
+    out[1::2] = vv[h:].flip(0)
+    return out
+
+
+def cufft_yardstick(model, grid, torch, stream, ft, reps=20):
+    """The library's FFT Poisson solve (gbo_poisson_solve_device) and the torch.fft (cuFFT)
+    solve of the same right-hand side: time per solve (CUDA events, each on its own stream)
+    and their relative difference (the yardstick must solve the same problem)."""
+    Nx, Ny, Nz = grid.Nx, grid.Ny, grid.Nz
+    tdt = torch.float32 if ft == np.float32 else torch.float64
+    rng = np.random.default_rng(9)
+    b = rng.standard_normal((Nx, Ny, Nz))
+    b -= b.mean()
+    rhs = torch.tensor(b.ravel(order="F"), dtype=tdt, device="cuda")
+    phi = torch.empty_like(rhs)
+    rhs3 = rhs.reshape(Nz, Ny, Nx)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = {}
+    for name in ("gbo", "cufft"):
+        for _ in range(3):
+            if name == "gbo":
+                model.poisson_solve_device(phi.data_ptr(), rhs.data_ptr())
+            else:
+                ref = torch_fft_poisson(torch, rhs3, grid.Lx, grid.Ly, grid.Lz)
+        torch.cuda.synchronize()
+        st = stream if name == "gbo" else torch.cuda.current_stream()
+        e0.record(st)
+        for _ in range(reps):
+            if name == "gbo":
+                model.poisson_solve_device(phi.data_ptr(), rhs.data_ptr())
+            else:
+                ref = torch_fft_poisson(torch, rhs3, grid.Lx, grid.Ly, grid.Lz)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times[name] = e0.elapsed_time(e1) / reps
+    ref = ref.reshape(-1)
+    diff = float(torch.linalg.vector_norm((phi - ref).double()) / torch.linalg.vector_norm(ref.double()))
+    return {"gbo_ms": times["gbo"], "cufft_reference_ms": times["cufft"], "speedup": times["cufft"] / times["gbo"],
+            "rel_l2_difference": diff, "grid": [Nx, Ny, Nz], "solves": reps,
+            "cufft_path": "torch.fft (cuFFT): Makhoul DCT-II in z + rfft2 in x, y, eigenvalue divide, inverse",
+            "gbo_path": "gbo_poisson_solve_device (k_dct_z, k_rfft_x, k_fft_y hand-written passes)"}
+
+
+def seamount_poisson_record(torch, og, L, n=20):
+    """Poisson-solve ms to a 1e-8 relative residual on the seamount benchmark grid
+    (256x256x128 ImmersedBoundaryGrid, FP32 state, FP64 dot products): FFT-preconditioned
+    CG and the learned flexible PCG on the same held-out right-hand sides, after two
+    spin-up steps."""
+    lib = og.load()
+    size = WORKLOADS["seamount"]["size"]
+    grid, physics, init = workload("seamount", size, np.float32)
+    model = og.NonhydrostaticModel(grid, **physics)
+    og.set_(model, **init)
+    og.time_step_(model, WORKLOADS["seamount"]["dt"], 2)
+    sp = ctypes.c_void_p()
+    lib.gbo_model_stream(model._h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    rec = {"grid": list(size), "fft_pcg": held_out_solves(model, grid, torch, stream, np.float32, n=n)}
+    wpath = os.path.join(os.path.dirname(og.__file__), "weights", "seamount_%dx%dx%d.npy" % tuple(size))
+    if os.path.exists(wpath):
+        model.set_learned_preconditioner(wpath)
+        try:
+            rec["learned_pcg"] = held_out_solves(model, grid, torch, stream, np.float32, n=n)
+            rec["learned_pcg"]["preconditioner"] = "fft + learned correction (flexible CG), %s" % os.path.basename(wpath)
+        except L.NotConvergedError as e:
+            rec["learned_pcg"] = {"not_converged": str(e)}
+        model.set_learned_preconditioner(None)
+        if "ms_mean" in rec["learned_pcg"]:
+            rec["learned_over_fft_time"] = rec["learned_pcg"]["ms_mean"] / rec["fft_pcg"]["ms_mean"]
+    return rec
 
 
 def run_ensemble(args, torch, og, L, lib, local):
@@ -634,7 +735,7 @@ def main():
     roofline = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": ab}
-    prof = PROFILED_TRAFFIC.get((top, tuple(size), args.dtype))
+    prof = PROFILED_TRAFFIC.get((args.workload, top, tuple(size), args.dtype))
     if prof:
         roofline.update(prof)
     for n, k in kernels.items():
@@ -685,6 +786,15 @@ def main():
             learned["preconditioner"] = "fft + learned correction (flexible CG), %s" % os.path.basename(wpath)
             poisson = {"fft_pcg": poisson, "learned_pcg": learned}
 
+    # the rest of the metric on the headline run: the cuFFT yardstick of the FFT solve on this
+    # grid, and the seamount grid's Poisson-solve times (FFT-PCG and learned PCG to 1e-8)
+    yard = None
+    if (rank == 0 and physics.get("pressure_solver") is None and grid.bottom_height is None and grid.z_faces is None
+            and grid.topology[2] == "Bounded"):
+        yard = cufft_yardstick(model, grid, torch, stream, ft)
+    if rank == 0 and args.workload == "convection" and tuple(size) == WORKLOADS["convection"]["size"]:
+        poisson = seamount_poisson_record(torch, og, L)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(args.workload)
@@ -696,6 +806,8 @@ def main():
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "kernels": kernels}
         if poisson:
             line["poisson_solve"] = poisson
+        if yard:
+            line["fft_poisson_vs_cufft"] = yard
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -160,8 +160,18 @@ int gbo_get_field(gbo_model* m, int32_t field, void* host, int32_t dtype, int64_
 int64_t gbo_field_count(const gbo_model* m, int32_t field);
 
 /* Device pointer and element count of a field (zero-copy access for a host binding's
- * unsafe_wrap / torch view).  The element type is the model's float type. */
+ * unsafe_wrap / torch view).  The element type is the model's float type.
+ * Tracers of GBO_FLOAT32 models on a Bounded z are stored as departures from a
+ * per-level reference profile (the horizontal mean of the values the tracer was last
+ * set to): the device array holds c - profile[k], and gbo_get_field returns the sum.
+ * A stratification b = N² z + b′ held directly in FP32 would round b′ at the ulp of
+ * N² z on every stage; as departures it is rounded at the ulp of b′. */
 int gbo_field_device_pointer(gbo_model* m, int32_t field, void** dptr, int64_t* count);
+
+/* The reference profile (Nz values, FP64) of a tracer field: zeros where the tracer
+ * is stored as it is (GBO_FLOAT64 models, Flat z).  No counterpart in the reference,
+ * which stores every tracer directly. */
+int gbo_field_reference_profile(gbo_model* m, int32_t field, double* out, int64_t count);
 
 /* Advance nsteps RK3 time steps of size dt.
  * Replaces time_step!(model::AbstractModel{<:RungeKutta3TimeStepper}, Δt)
@@ -315,10 +325,12 @@ int gbo_ensemble_time_step(gbo_ensemble* e, double dt, int32_t nsteps);
  *     default stream.  The call returns once the work is enqueued.
  *   - Grids whose work space exceeds GBO_STATIC_SCRATCH_BYTES are rejected with
  *     GBO_ERR_INVALID and a message giving the bytes needed (FP32: about
- *     Nx/2*Ny*Nz*8 bytes, e.g. up to 256x256x64; FP64: twice that, e.g. 128^3).
- *   - The first call on each device does the set-up (it looks up the static
- *     array's device address with that device current); make that first call
- *     before any stream capture.
+ *     (Nx/2+1)*Ny*Nz*8 bytes, e.g. up to 256x256x64, or 2048x2048 on a Flat z;
+ *     FP64: twice that, e.g. 128^3, or 2048x1024 on a Flat z).
+ *   - Every call looks up the static array's address in the current CUDA context
+ *     (a host-side lookup, so a context reset or another current context is safe);
+ *     the first call in each context also raises the pass kernels' shared-memory
+ *     limits.  Make that first call before any stream capture.
  *   - The scratch is one array per device shared by all callers: calls that
  *     overlap in time (other streams, other threads) race on it and must be
  *     serialized by the caller.  Nothing in it has to start at zero; every

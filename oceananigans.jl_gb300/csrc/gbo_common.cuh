@@ -93,18 +93,30 @@ GBO_HD void stage_factors(double dt, double c0, double c1, double c2, FT* out) {
 }
 
 // Accessor for a Center-in-z field.
+//
+// Tracers of single-precision models on a Bounded z are stored as departures from a
+// per-level reference profile `ref` (Nz values, fixed when the tracer is set): a
+// stratification b = N² z + b′ held in FP32 would round b′ at the ulp of N² z at
+// every stage.  The accessor returns ref[k] + a[i, j, k], the field's value; the
+// mirrored halo layer mirrors both, and the deeper layers (zero in the reference)
+// stay zero.
 template <typename FT>
 struct CFld {
     const FT* __restrict__ a;
     int Nx, Ny, Nz, flatz;
+    const FT* ref = nullptr;  // reference profile of a departure field (Bounded z only), or null
     // (i, j) any distance outside the domain (tile fills)
     GBO_D FT far(int i, int j, int k) const { return (*this)(wrapt(i, Nx), wrapt(j, Ny), k); }
+    GBO_D FT at(size_t off, int k) const {
+        const FT x = ldg(a + off);
+        return ref ? ldg(ref + k) + x : x;
+    }
     // the column at offset c = i + Nx j of the domain, at level k
     GBO_D FT col(size_t c, int k) const {
         if (flatz) return ldg(a + c);
         if (k < -1 || k > Nz) return FT(0);
         k = k < 0 ? 0 : (k >= Nz ? Nz - 1 : k);
-        return ldg(a + c + (size_t)Nx * Ny * k);
+        return at(c + (size_t)Nx * Ny * k, k);
     }
     GBO_D FT operator()(int i, int j, int k) const {
         i = wrapi(i, Nx);
@@ -112,7 +124,7 @@ struct CFld {
         if (flatz) return ldg(a + i + (size_t)Nx * j);
         if (k < -1 || k > Nz) return FT(0);
         k = k < 0 ? 0 : (k >= Nz ? Nz - 1 : k);
-        return ldg(a + i + (size_t)Nx * (j + (size_t)Ny * k));
+        return at(i + (size_t)Nx * (j + (size_t)Ny * k), k);
     }
 };
 
@@ -131,7 +143,9 @@ struct WFld {
 };
 
 template <typename FT>
-GBO_D CFld<FT> cfld(const FT* a, const GridP<FT>& g) { return CFld<FT>{a, g.Nx, g.Ny, g.Nz, g.flatz}; }
+GBO_D CFld<FT> cfld(const FT* a, const GridP<FT>& g, const FT* ref = nullptr) {
+    return CFld<FT>{a, g.Nx, g.Ny, g.Nz, g.flatz, g.flatz ? nullptr : ref};
+}
 template <typename FT>
 GBO_D WFld<FT> wfld(const FT* a, const GridP<FT>& g) { return WFld<FT>{a, g.Nx, g.Ny, g.Nz}; }
 

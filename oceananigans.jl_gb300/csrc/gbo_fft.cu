@@ -43,6 +43,11 @@ void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, cudaStream_t st) {
     k_thomas_z<FT><<<(unsigned)((ncol + 127) / 128), 128, 0, st>>>(P, T);
 }
 
+void launch_thomas_tables(const ThomasP& T, cudaStream_t st) {
+    const size_t ncol = (size_t)T.Nh * T.Ny;
+    k_thomas_tables<<<(unsigned)((ncol + 127) / 128), 128, 0, st>>>(T);
+}
+
 template <typename FT>
 cudaError_t fft_set_smem(size_t sz, size_t sx, size_t sy) {
     cudaError_t e = cudaSuccess;

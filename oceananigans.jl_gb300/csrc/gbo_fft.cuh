@@ -426,11 +426,11 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
 //
 // One thread per (kx, ky) column; a plane of the half spectrum is Nh·Ny
 // consecutive columns, so thread c of a level reads and writes column c of that
-// plane and every access is coalesced.  The forward sweep keeps its FP64
-// intermediates (the eliminated right-hand side and the ratios t_k) in a global
-// scratch laid out [level][column] (3·Nz·Nh·Ny doubles), which the backward sweep
-// reads in reverse: the sweep streams at HBM speed with full occupancy instead of
-// holding whole columns in shared memory.
+// plane and every access is coalesced.  The pivots 1/β_k and ratios t_k are
+// tabulated once per model (k_thomas_tables, laid out [level][column]); the forward
+// sweep keeps the eliminated right-hand side in a global FP64 scratch of the same
+// layout, which the backward sweep reads in reverse: the sweep streams at HBM speed
+// with full occupancy instead of holding whole columns in shared memory.
 // ---------------------------------------------------------------------------
 struct ThomasP {
     int Nh, Ny, Nz;
@@ -440,9 +440,53 @@ struct ThomasP {
     const double* lx;     // λx, λy in FP64
     const double* ly;
     double scale;         // 1/(Nx Ny)
-    double* ws;           // scratch: 3 arrays of Nz * Nh * Ny doubles (re, im, t)
+    double* ws;           // scratch: 2 arrays of Nz * Nh * Ny doubles (re, im of the forward sweep)
+    double* tab_s;        // pivots: 1/β of level kr, or 0 where the elimination is elided (Nz * Nh * Ny)
+    double* tab_t;        // elimination factors t of level kr (Nz * Nh * Ny; kr = 1 unused)
 };
 
+// The tridiagonal system of column (kx, ky) (fourier_tridiagonal_poisson_solver.jl:199-212,
+// 225-260): diagonal D(kr) = -(1/Δzᶠ(kr+1) + 1/Δzᶠ(kr)) - Δzᶜ(kr) λ with the Neumann rows at the
+// ends, off-diagonals 1/Δzᶠ, λ = λx + λy.
+struct ThomasColumn {
+    const ThomasP& T;
+    double lam;
+    GBO_D double D(int kr) const {
+        if (kr == 1) return -T.rdzf[2 + T.zoff] - T.dzc[1 + T.zoff] * lam;
+        if (kr == T.Nz) return -T.rdzf[T.Nz + T.zoff] - T.dzc[T.Nz + T.zoff] * lam;
+        return -(T.rdzf[kr + 1 + T.zoff] + T.rdzf[kr + T.zoff]) - T.dzc[kr + T.zoff] * lam;
+    }
+    GBO_D double off(int q) const { return T.rdzf[q + 1 + T.zoff]; }
+};
+
+// Pivots of the Thomas sweep (batched_tridiagonal_solver.jl:217-243): β, t = c/β and the
+// elision of the forward update where |β| <= 10 eps depend on the grid and the column's
+// wavenumbers only, never on the right-hand side, so they are computed once per model and
+// the sweep itself has no FP64 division (the costly operation of the sweep on this GPU).
+__global__ void __launch_bounds__(128) k_thomas_tables(ThomasP T) {
+    const size_t ncol = (size_t)T.Nh * T.Ny;
+    const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const ThomasColumn C{T, T.lx[c % T.Nh] + T.ly[c / T.Nh]};
+    const double tiny = 10 * 2.220446049250313e-16;
+    double beta = C.D(1);
+    double rbeta = 1.0 / beta;
+    T.tab_s[c] = rbeta;
+    T.tab_t[c] = 0.0;
+    for (int kr = 2; kr <= T.Nz; ++kr) {
+        const double a = C.off(kr - 1);
+        const double t = a * rbeta;
+        const size_t at = c + ncol * (kr - 1);
+        T.tab_t[at] = t;
+        beta = C.D(kr) - a * t;
+        rbeta = 1.0 / beta;
+        T.tab_s[at] = fabs(beta) > tiny ? rbeta : 0.0;
+    }
+}
+
+// The sweep with tabulated pivots: forward elimination (ϕ = (f - a ϕ⁻) / β, elided where
+// the table holds 0) into the FP64 scratch, backward substitution into the spectrum.
+// Multiplying by 1/β differs from dividing by β in the last bit only.
 template <typename FT>
 __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
     const size_t ncol = (size_t)T.Nh * T.Ny;
@@ -452,38 +496,23 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
     const int Nz = T.Nz;
     double* wre = T.ws;
     double* wim = T.ws + ncol * Nz;
-    double* wt = T.ws + 2 * ncol * Nz;
+    const double* ts = T.tab_s;
+    const double* tt = T.tab_t;
+    const ThomasColumn C{T, 0.0};
     Cx<FT>* col = P.cb + c;
-    const double lam = T.lx[kx] + T.ly[ky];
-    auto D = [&](int kr) {
-        if (kr == 1) return -T.rdzf[2 + T.zoff] - T.dzc[1 + T.zoff] * lam;
-        if (kr == Nz) return -T.rdzf[Nz + T.zoff] - T.dzc[Nz + T.zoff] * lam;
-        return -(T.rdzf[kr + 1 + T.zoff] + T.rdzf[kr + T.zoff]) - T.dzc[kr + T.zoff] * lam;
-    };
-    auto off = [&](int q) { return T.rdzf[q + 1 + T.zoff]; };
-    const double tiny = 10 * 2.220446049250313e-16;
-    // One FP64 division per level (1/β), the rest multiplies: FP64 division is the
-    // costly operation of the sweep on this GPU.  Differs from dividing by β in the
-    // last bit only.
-    double beta = D(1);
-    double rbeta = 1.0 / beta;
+    const double s1 = __ldg(ts + c);
     Cx<FT> f1 = col[0];
-    double pre = (double)f1.re * rbeta, pim = (double)f1.im * rbeta;
+    double pre = (double)f1.re * s1, pim = (double)f1.im * s1;
     wre[c] = pre;
     wim[c] = pim;
-    // forward elimination of level kr (1-based) with right-hand side fk
-    auto forward = [&](int kr, Cx<FT> fk) {
-        const double a = off(kr - 1);
-        const double t = a * rbeta;
+    // forward elimination of level kr (1-based) with right-hand side fk and pivot s
+    auto forward = [&](int kr, Cx<FT> fk, double s) {
+        const double a = C.off(kr - 1);
         const size_t at = c + ncol * (kr - 1);
-        wt[at] = t;
-        beta = D(kr) - a * t;
-        rbeta = 1.0 / beta;
-        const double sre = ((double)fk.re - a * pre) * rbeta;
-        const double sim = ((double)fk.im - a * pim) * rbeta;
-        const bool dd = fabs(beta) > tiny;
-        pre = dd ? sre : 0.0;
-        pim = dd ? sim : 0.0;
+        const double sre = ((double)fk.re - a * pre) * s;
+        const double sim = ((double)fk.im - a * pim) * s;
+        pre = s != 0.0 ? sre : 0.0;
+        pim = s != 0.0 ? sim : 0.0;
         wre[at] = pre;
         wim[at] = pim;
     };
@@ -491,12 +520,16 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
     int kr = 2;
     for (; kr + 3 <= Nz; kr += 4) {
         Cx<FT> f[4];
+        double sv[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) f[q] = col[ncol * (kr - 1 + q)];
+        for (int q = 0; q < 4; ++q) {
+            f[q] = col[ncol * (kr - 1 + q)];
+            sv[q] = __ldg(ts + c + ncol * (kr - 1 + q));
+        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) forward(kr + q, f[q]);
+        for (int q = 0; q < 4; ++q) forward(kr + q, f[q], sv[q]);
     }
-    for (; kr <= Nz; ++kr) forward(kr, col[ncol * (kr - 1)]);
+    for (; kr <= Nz; ++kr) forward(kr, col[ncol * (kr - 1)], __ldg(ts + c + ncol * (kr - 1)));
     // backward substitution; the (0,0) column keeps its solution for the mean
     const bool mean_col = kx == 0 && ky == 0;
     col[ncol * (Nz - 1)] = cx((FT)(pre * T.scale), (FT)(pim * T.scale));
@@ -514,12 +547,12 @@ __global__ void __launch_bounds__(128) k_thomas_z(PassP<FT> P, ThomasP T) {
         for (int q = 0; q < 4; ++q) {
             r[q] = wre[c + ncol * (kr - q - 1)];
             i[q] = wim[c + ncol * (kr - q - 1)];
-            t[q] = wt[c + ncol * (kr - q)];
+            t[q] = __ldg(tt + c + ncol * (kr - q));
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) backward(kr - q, r[q], i[q], t[q]);
     }
-    for (; kr >= 1; --kr) backward(kr, wre[c + ncol * (kr - 1)], wim[c + ncol * (kr - 1)], wt[c + ncol * kr]);
+    for (; kr >= 1; --kr) backward(kr, wre[c + ncol * (kr - 1)], wim[c + ncol * (kr - 1)], __ldg(tt + c + ncol * kr));
     if (mean_col) {
         double mre = 0, mim = 0;
         for (int k = 0; k < Nz; ++k) { mre += wre[c + ncol * k]; mim += wim[c + ncol * k]; }
@@ -538,4 +571,5 @@ template <typename FT> void launch_dct_z(const PassP<FT>& P, int inverse, int ZT
 template <typename FT> void launch_rfft_x(const PassP<FT>& P, int inverse, int XL, size_t smem, cudaStream_t st);
 template <typename FT> void launch_fft_y(const PassP<FT>& P, int mode, int YT, size_t smem, cudaStream_t st);
 template <typename FT> void launch_thomas_z(const PassP<FT>& P, const ThomasP& T, cudaStream_t st);
+void launch_thomas_tables(const ThomasP& T, cudaStream_t st);
 template <typename FT> cudaError_t fft_set_smem(size_t smem_z, size_t smem_x, size_t smem_y);

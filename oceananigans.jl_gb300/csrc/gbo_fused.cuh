@@ -145,7 +145,9 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     constexpr bool closure = CLK != CL_NONE;
     constexpr bool amd = CLK == CL_AMD;
     const bool inside = (i < g.Nx) && (j < g.Ny);
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g);
+    // the tracer's register window holds field values (reference profile added); its
+    // shared-memory planes hold the stored values (departures where a profile exists)
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g, P.cref);
     WFld<FT> Wg = wfld(P.w, g);
     const int Nz = g.Nz, fz = g.flatz;
     const FT Az = M.Az();
@@ -350,25 +352,72 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         const FT* Kk = s.KP[s3k];
         const FT* Kp = s.KP[s3p];
         const FT Ax = M.Ax(k), Ay = M.Ay(k);
+        // horizontal reconstructions of a departure field: the level's profile value is
+        // constant along x and y, and every stencil reproduces constants, so the field's
+        // reconstruction is the profile value plus that of the departures (the smoothness
+        // indicators see only differences)
+        const FT cref_k = (TR && sizeof(FT) == 4 && P.cref && !fz) ? __ldg(P.cref + k) : FT(0);
+        auto with_ref = [&](FT x) -> FT {
+            if constexpr (sizeof(FT) == 4) return cref_k + x;
+            else return x;
+        };
 
         // ---- west / south face quantities of this thread (and the tile edges) ----
         auto west = [&](int x, int y, bool own) {
             FT S[6];
+            if constexpr (IBG) {
 #pragma unroll
-            for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x - 3 + o, y)];
-            if constexpr (IBG)
+                for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x - 3 + o, y)];
                 s.WX[A_UU][y][x] = mflux_t(periph_t(x - 1, y, k, false, false, false), [&](int o) { return Ax * S[o + 3]; },
                                            sym_t(0, x - 1, y, k, false), [&](int o) { return S[o + 3]; }, level_t(0, x - 1, y, k, false));
-            else
-                s.WX[A_UU][y][x] = flux_c4_w5<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4], S);
 #pragma unroll
-            for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x - 3 + o, y)];
-            if constexpr (IBG)
+                for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x - 3 + o, y)];
                 s.WX[A_UV][y][x] = mflux_t(periph_t(x, y, k, true, true, false), [&](int o) { return Ax * Uk[pidx(x, y + o)]; },
                                            sym_t(1, x, y, k, true), [&](int o) { return S[o + 3]; }, level_t(0, x, y, k, true));
-            else
-                s.WX[A_UV][y][x] = flux_c4_w5<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)], S);
-            if (!fz) {
+            } else {
+                // u and v through this x face: both WENO5 reconstructions at once
+                FT T[6];
+#pragma unroll
+                for (int o = 0; o < 6; ++o) {
+                    S[o] = Uk[pidx(x - 3 + o, y)];
+                    T[o] = Vk[pidx(x - 3 + o, y)];
+                }
+                const FT uu = cen4<FT>(Ax * S[1], Ax * S[2], Ax * S[3], Ax * S[4]);
+                const FT uv = cen4<FT>(Ax * Uk[pidx(x, y - 2)], Ax * Uk[pidx(x, y - 1)], Ax * Uk[pidx(x, y)], Ax * Uk[pidx(x, y + 1)]);
+                FT ru, rv;
+                weno5_2<FT>(S, bias_left(uu), T, bias_left(uv), ru, rv);
+                s.WX[A_UU][y][x] = uu * ru;
+                s.WX[A_UV][y][x] = uv * rv;
+            }
+            // w and the tracer through this x face, paired where both exist
+            bool paired = false;
+            if constexpr (!IBG && TR) {
+                if (!fz) {
+                    paired = true;
+                    FT uz[4];
+                    if (own) {
+#pragma unroll
+                        for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < 4; ++o) uz[o] = Ug.col(fcol, k - 2 + o);
+                    }
+                    auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
+                    const FT uw = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+                    const FT uc = Uk[pidx(x, y)];
+                    FT T[6];
+#pragma unroll
+                    for (int o = 0; o < 6; ++o) {
+                        S[o] = Wk[pidx(x - 3 + o, y)];
+                        T[o] = CCk[pidx(x - 3 + o, y)];
+                    }
+                    FT rw, rc;
+                    weno5_2<FT>(S, bias_left(uw), T, bias_left(uc), rw, rc);
+                    s.WX[A_UW][y][x] = uw * rw;
+                    s.WX[A_CX][y][x] = Ax * uc * with_ref(rc);
+                }
+            }
+            if (!fz && !paired) {
                 FT uz[4];
                 if (own) {
 #pragma unroll
@@ -405,13 +454,15 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 }
             }
             if (TR) {
-                FT ut = Uk[pidx(x, y)];
+                if (!paired) {
+                    FT ut = Uk[pidx(x, y)];
 #pragma unroll
-                for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x - 3 + o, y)];
-                if constexpr (IBG)
-                    s.WX[A_CX][y][x] = Ax * ut * biased<FT>([&](int o) { return S[o + 3]; }, bias_left(ut), level_t(0, x, y, k, true));
-                else
-                    s.WX[A_CX][y][x] = Ax * ut * weno5<FT>(S, bias_left(ut));
+                    for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x - 3 + o, y)];
+                    if constexpr (IBG)
+                        s.WX[A_CX][y][x] = Ax * ut * with_ref(biased<FT>([&](int o) { return S[o + 3]; }, bias_left(ut), level_t(0, x, y, k, true)));
+                    else
+                        s.WX[A_CX][y][x] = Ax * ut * with_ref(weno5<FT>(S, bias_left(ut)));
+                }
                 if (closure) {
                     const FT* K = amd ? Kk : Nk;
                     FT kx = amd ? FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x - 1, y)] + K[pidx(x, y)]) / P.Pr;
@@ -421,21 +472,59 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         };
         auto south = [&](int x, int y, bool own) {
             FT S[6];
+            if constexpr (IBG) {
 #pragma unroll
-            for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x, y - 3 + o)];
-            if constexpr (IBG)
+                for (int o = 0; o < 6; ++o) S[o] = Uk[pidx(x, y - 3 + o)];
                 s.SY[A_VU][y][x] = mflux_t(periph_t(x, y, k, true, true, false), [&](int o) { return Ay * Vk[pidx(x + o, y)]; },
                                            sym_t(0, x, y, k, true), [&](int o) { return S[o + 3]; }, level_t(1, x, y, k, true));
-            else
-                s.SY[A_VU][y][x] = flux_c4_w5<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)], S);
 #pragma unroll
-            for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x, y - 3 + o)];
-            if constexpr (IBG)
+                for (int o = 0; o < 6; ++o) S[o] = Vk[pidx(x, y - 3 + o)];
                 s.SY[A_VV][y][x] = mflux_t(periph_t(x, y - 1, k, false, false, false), [&](int o) { return Ay * S[o + 3]; },
                                            sym_t(1, x, y - 1, k, false), [&](int o) { return S[o + 3]; }, level_t(1, x, y - 1, k, false));
-            else
-                s.SY[A_VV][y][x] = flux_c4_w5<FT>(Ay * S[1], Ay * S[2], Ay * S[3], Ay * S[4], S);
-            if (!fz) {
+            } else {
+                // u and v through this y face: both WENO5 reconstructions at once
+                FT T[6];
+#pragma unroll
+                for (int o = 0; o < 6; ++o) {
+                    S[o] = Uk[pidx(x, y - 3 + o)];
+                    T[o] = Vk[pidx(x, y - 3 + o)];
+                }
+                const FT vu = cen4<FT>(Ay * Vk[pidx(x - 2, y)], Ay * Vk[pidx(x - 1, y)], Ay * Vk[pidx(x, y)], Ay * Vk[pidx(x + 1, y)]);
+                const FT vv = cen4<FT>(Ay * T[1], Ay * T[2], Ay * T[3], Ay * T[4]);
+                FT ru, rv;
+                weno5_2<FT>(S, bias_left(vu), T, bias_left(vv), ru, rv);
+                s.SY[A_VU][y][x] = vu * ru;
+                s.SY[A_VV][y][x] = vv * rv;
+            }
+            // w and the tracer through this y face, paired where both exist
+            bool paired = false;
+            if constexpr (!IBG && TR) {
+                if (!fz) {
+                    paired = true;
+                    FT vz[4];
+                    if (own) {
+#pragma unroll
+                        for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < 4; ++o) vz[o] = Vg.col(fcol, k - 2 + o);
+                    }
+                    auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
+                    const FT vw = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
+                    const FT vc = Vk[pidx(x, y)];
+                    FT T[6];
+#pragma unroll
+                    for (int o = 0; o < 6; ++o) {
+                        S[o] = Wk[pidx(x, y - 3 + o)];
+                        T[o] = CCk[pidx(x, y - 3 + o)];
+                    }
+                    FT rw, rc;
+                    weno5_2<FT>(S, bias_left(vw), T, bias_left(vc), rw, rc);
+                    s.SY[A_VW][y][x] = vw * rw;
+                    s.SY[A_CY][y][x] = Ay * vc * with_ref(rc);
+                }
+            }
+            if (!fz && !paired) {
                 FT vz[4];
                 if (own) {
 #pragma unroll
@@ -472,13 +561,15 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 }
             }
             if (TR) {
-                FT vt = Vk[pidx(x, y)];
+                if (!paired) {
+                    FT vt = Vk[pidx(x, y)];
 #pragma unroll
-                for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x, y - 3 + o)];
-                if constexpr (IBG)
-                    s.SY[A_CY][y][x] = Ay * vt * biased<FT>([&](int o) { return S[o + 3]; }, bias_left(vt), level_t(1, x, y, k, true));
-                else
-                    s.SY[A_CY][y][x] = Ay * vt * weno5<FT>(S, bias_left(vt));
+                    for (int o = 0; o < 6; ++o) S[o] = CCk[pidx(x, y - 3 + o)];
+                    if constexpr (IBG)
+                        s.SY[A_CY][y][x] = Ay * vt * with_ref(biased<FT>([&](int o) { return S[o + 3]; }, bias_left(vt), level_t(1, x, y, k, true)));
+                    else
+                        s.SY[A_CY][y][x] = Ay * vt * with_ref(weno5<FT>(S, bias_left(vt)));
+                }
                 if (closure) {
                     const FT* K = amd ? Kk : Nk;
                     FT ky = amd ? FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) : FT(0.5) * (K[pidx(x, y - 1)] + K[pidx(x, y)]) / P.Pr;
@@ -507,22 +598,36 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 fWw_t = mflux_t(periph_t(tx, ty, k, false, false, false), [&](int o) { return Az * c.wc[3 + o]; },
                                 sym_t(2, tx, ty, k, false), [&](int o) { return c.wc[3 + o]; }, level_t(2, tx, ty, k, false));
             } else {
-            {
-                FT wt = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
-                auto q = [&](int o) { return c.uc[4 + o]; };
-                fWu_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
-            }
-            {
-                FT wt = cen4<FT>(Az * Wp[pidx(tx, ty - 2)], Az * Wp[pidx(tx, ty - 1)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx, ty + 1)]);
-                auto q = [&](int o) { return c.vc[4 + o]; };
-                fWv_t = wt * biased<FT>(q, bias_left(wt), zlev_biased_face(k + 2, Nz));
-            }
-            {
-                auto qs = [&](int o) { return Az * c.wc[3 + o]; };
-                FT wt = symm<FT>(qs, zlev_symm_center(k + 1, Nz));
-                auto qb = [&](int o) { return c.wc[3 + o]; };
-                fWw_t = wt * biased<FT>(qb, bias_left(wt), zlev_biased_center(k + 1, Nz));
-            }
+                // u and v through the top face (the same reconstruction level): paired
+                // WENO5 away from the walls
+                const int lf = zlev_biased_face(k + 2, Nz);
+                const FT wu = cen4<FT>(Az * Wp[pidx(tx - 2, ty)], Az * Wp[pidx(tx - 1, ty)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx + 1, ty)]);
+                const FT wv = cen4<FT>(Az * Wp[pidx(tx, ty - 2)], Az * Wp[pidx(tx, ty - 1)], Az * Wp[pidx(tx, ty)], Az * Wp[pidx(tx, ty + 1)]);
+                if (lf == 3) {
+                    FT ru, rv;
+                    weno5_2<FT>(&c.uc[1], bias_left(wu), &c.vc[1], bias_left(wv), ru, rv);
+                    fWu_t = wu * ru;
+                    fWv_t = wv * rv;
+                } else {
+                    fWu_t = wu * biased<FT>([&](int o) { return c.uc[4 + o]; }, bias_left(wu), lf);
+                    fWv_t = wv * biased<FT>([&](int o) { return c.vc[4 + o]; }, bias_left(wv), lf);
+                }
+                // w (and the tracer, paired when both take WENO5) through the centre above
+                const int lc = zlev_biased_center(k + 1, Nz);
+                const FT ww = symm<FT>([&](int o) { return Az * c.wc[3 + o]; }, zlev_symm_center(k + 1, Nz));
+                if (TR && lc == 3 && lf == 3) {
+                    const FT wc = c.wc[3];
+                    FT rw, rc;
+                    weno5_2<FT>(&c.wc[0], bias_left(ww), &c.cc[1], bias_left(wc), rw, rc);
+                    fWw_t = ww * rw;
+                    fWc_t = Az * wc * rc;
+                } else {
+                    fWw_t = ww * biased<FT>([&](int o) { return c.wc[3 + o]; }, bias_left(ww), lc);
+                    if (TR) {
+                        const FT wc = c.wc[3];
+                        fWc_t = Az * wc * biased<FT>([&](int o) { return c.cc[4 + o]; }, bias_left(wc), lf);
+                    }
+                }
             }
             if (closure) {
                 FT nfcf = FT(0.5) * (FT(0.5) * (Nk[pidx(tx - 1, ty)] + Nk[pidx(tx, ty)]) + FT(0.5) * (Np[pidx(tx - 1, ty)] + Np[pidx(tx, ty)]));
@@ -536,9 +641,10 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 t33_t = FT(-2) * (Nk[pidx(tx, ty)] * ((c.wc[3] - c.wc[2]) * M.rdzc(k)));
             }
             if (TR) {
-                FT wt = c.wc[3];
-                auto q = [&](int o) { return c.cc[4 + o]; };
-                fWc_t = Az * wt * biased<FT>(q, bias_left(wt), IBG ? level_t(2, tx, ty, k + 1, true) : zlev_biased_face(k + 2, Nz));
+                if constexpr (IBG) {
+                    const FT wt = c.wc[3];
+                    fWc_t = Az * wt * biased<FT>([&](int o) { return c.cc[4 + o]; }, bias_left(wt), level_t(2, tx, ty, k + 1, true));
+                }
                 if (closure) {
                     const FT* K0 = amd ? Kk : Nk;
                     const FT* K1 = amd ? Kp : Np;
@@ -635,7 +741,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                     if (k == 0 && P.flux_bot != FT(0)) G += P.flux_bot * Az / (Az * M.dzc(k));
                 }
                 P.Gc[idx] = G;
-                P.co[idx] = rk3_update(CCk[pidx(tx, ty)], G, Gcm, P, dt);
+                P.co[idx] = rk3_update(CCk[pidx(tx, ty)], G, Gcm, P, dt);  // the stored value (departure)
             }
         }
 
@@ -721,6 +827,14 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
     else fill([](int i, int n) { return wrapm(i, n); });
     fused::cp_async_commit();
     fused::cp_async_wait_all();
+    if (buoy && P.bref) {
+        // b stored as departures: each thread adds the reference profile to the elements it
+        // copied (its own copies are complete after the wait); zero-filled layers stay zero
+        for (int e = tid; e < BS; e += TX * TY) {
+            const int zc = fused::zsrc_c(k0 + e / (BX * BY) - 1, Nz, fz);
+            if (zc >= 0) s.b[e] += __ldg(P.bref + zc);
+        }
+    }
     __syncthreads();
     auto U = [&](int x, int y, int zz) { return s.u[bidx(x, y, zz)]; };
     auto V = [&](int x, int y, int zz) { return s.v[bidx(x, y, zz)]; };
@@ -822,7 +936,7 @@ __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__
     const GridP<FT>& g = P.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g);
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g, P.cref);
     WFld<FT> Wg = wfld(P.w, g);
     const bool has_c = P.c != nullptr;
     for (int e = tid; e < BS; e += TX * TY) {

@@ -11,6 +11,8 @@ struct StepP {
     const FT* c;                            // tracer (tracer kernel)
     const FT* nu; const FT* kap; const FT* phy;
     const FT* b;                            // buoyancy tracer (closures)
+    const FT* cref;                         // reference profile of c (departure storage), or null
+    const FT* bref;                         // reference profile of b, or null
     FT* uo; FT* vo; FT* wo; FT* co;         // predictor outputs U*
     FT* Gu; FT* Gv; FT* Gw; FT* Gc;         // tendency buffers (G⁻ in, Gⁿ out)
     FT f;
@@ -63,7 +65,7 @@ __global__ void k_smagorinsky(StepP<FT> P, FT* __restrict__ nu_out) {
     } else {
         FT N2 = FT(0);
         if (P.buoyancy && !g.flatz) {
-            CFld<FT> b = cfld(P.b, g);
+            CFld<FT> b = cfld(P.b, g, P.bref);
             // N² = ℑz(∂z b), conditional ∂ on an immersed grid
             FT b1 = cond_zero(g, i, j, k - 1, i, j, k) ? FT(0) : (b(i, j, k) - b(i, j, k - 1)) * M.rdzf(k);
             FT b2 = cond_zero(g, i, j, k, i, j, k + 1) ? FT(0) : (b(i, j, k + 1) - b(i, j, k)) * M.rdzf(k + 1);
@@ -200,13 +202,19 @@ __global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap
     if (i >= g.Nx || j >= g.Ny) return;
     Fields<FT> F{cfld(P.u, g), cfld(P.v, g), cfld(P.nu, g), cfld(P.phy, g), wfld(P.w, g)};
     Strain<FT> S(g, F);
-    CFld<FT> c = cfld(P.c, g);
+    CFld<FT> c = cfld(P.c, g, P.cref);
     amd_point<FT>(P, g, S, c, P.c != nullptr, i, j, k, i + (size_t)g.Nx * (j + (size_t)g.Ny * k), nu_out, kap_out);
 }
 
 // ---------------------------------------------------------------------------
 // Hydrostatic pressure anomaly: downward integral of ℑz(b)·Δzᶠ
 // (update_hydrostatic_pressure.jl:11-21).  One thread per (i, j) column.
+// When b is stored as departures from a reference profile, the integral runs over
+// the departures only: the profile's part is the same in every column, and pHY′
+// enters the momentum equations only through its horizontal differences
+// (∂x pHY′, ∂y pHY′; w has no buoyancy term when pHY′ is present), so dropping it
+// changes no tendency and keeps those differences free of the cancellation of two
+// O(N² H²) column integrals.  Reading the field back adds the profile's part.
 // ---------------------------------------------------------------------------
 template <typename FT>
 __global__ void k_hydrostatic(StepP<FT> P, FT* __restrict__ phy) {

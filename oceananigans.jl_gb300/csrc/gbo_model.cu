@@ -112,9 +112,10 @@ __global__ void __launch_bounds__(256) k_correct(GridP<FT> g, const FT* us, cons
 }
 
 // mask_immersed_field! (mask_immersed_field.jl:65-77): zero on the immersed periphery
-// of each field's location.  which: bit 0 u, bit 1 v, bit 2 w, bit 3 tracer c.
+// of each field's location.  which: bit 0 u, bit 1 v, bit 2 w, bit 3 tracer c (stored
+// as departures from cref when cref is given: the masked value is then -cref[k]).
 template <typename FT>
-__global__ void k_mask(GridP<FT> g, FT* u, FT* v, FT* w, FT* c, int which) {
+__global__ void k_mask(GridP<FT> g, FT* u, FT* v, FT* w, FT* c, int which, const FT* cref = nullptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = blockIdx.z;
@@ -123,7 +124,45 @@ __global__ void k_mask(GridP<FT> g, FT* u, FT* v, FT* w, FT* c, int which) {
     if ((which & 1) && imm_periph(g, i, j, k, true, false, false)) u[idx] = FT(0);
     if ((which & 2) && imm_periph(g, i, j, k, false, true, false)) v[idx] = FT(0);
     if ((which & 4) && !g.flatz && imm_periph(g, i, j, k, false, false, true)) w[idx] = FT(0);
-    if ((which & 8) && imm_periph(g, i, j, k, false, false, false)) c[idx] = FT(0);
+    if ((which & 8) && imm_periph(g, i, j, k, false, false, false)) c[idx] = cref ? -cref[k] : FT(0);
+}
+
+// Tracers of single-precision Bounded-z models are stored as departures from a per-level
+// reference profile, the horizontal mean of the values they were last set to.
+// k_level_mean: that mean in FP64 (one block per level); k_to_departure: the profile in
+// FT and the departures from it; k_from_departure: profile + departure in the output type.
+constexpr int LM_THREADS = 256;
+template <typename T>
+__global__ void __launch_bounds__(LM_THREADS) k_level_mean(const T* __restrict__ a, size_t plane, double* __restrict__ mean) {
+    __shared__ double red[LM_THREADS];
+    const size_t base = plane * blockIdx.x;
+    double sum = 0;
+    for (size_t q = threadIdx.x; q < plane; q += LM_THREADS) sum += (double)a[base + q];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int h = LM_THREADS / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) mean[blockIdx.x] = red[0] / (double)plane;
+}
+template <typename FT, typename T>
+__global__ void k_to_departure(const T* __restrict__ a, const double* __restrict__ mean, FT* __restrict__ ref,
+                               FT* __restrict__ c, size_t plane, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += stride) {
+        const size_t k = q / plane;
+        const FT r = FT(mean[k]);
+        c[q] = FT((double)a[q] - (double)r);
+        if (q == k * plane) ref[k] = r;
+    }
+}
+template <typename FT, typename T>
+__global__ void k_from_departure(const FT* __restrict__ c, const FT* __restrict__ ref, T* __restrict__ out, size_t plane,
+                                 size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += stride)
+        out[q] = T((double)ref[q / plane] + (double)c[q]);
 }
 
 template <typename FT>
@@ -322,6 +361,7 @@ struct gbo_model {
     virtual int step(double dt, int nsteps) = 0;
     virtual int sync() = 0;
     virtual int device_pointer(int field, void** p, int64_t* n) = 0;
+    virtual int reference_profile(int field, double* out, int64_t n) = 0;
     virtual int poisson_device(void* phi, const void* rhs) = 0;
     virtual int64_t state_bytes() const = 0;
     virtual int get_state(void* buf, int64_t bytes) = 0;
@@ -354,27 +394,16 @@ const char* const GROUP_NAMES[GROUPS] = {"k_momentum", "k_tracer", "k_closure", 
                                          "k_nan_check", "k_mask", "k_cg", "k_cg_dot", "k_cg_direction",
                                          "k_cg_update_xr", "k_cg_gauge", "k_simulation", "k_cg_learned"};
 
-// The fused momentum kernel is compiled per closure kind; these pick the instance.
+// The fused momentum kernel is compiled per closure kind in its own translation units
+// (gbo_fused_*.cu, compiled in parallel); these pick the instance.
 template <typename FT, bool TR>
-void launch_fused(int closure, bool ibg, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk) {
-    const size_t smem = fused::smem_bytes<FT>(closure == CL_AMD || ibg);
-    if (ibg) k_momentum_fused<FT, TR, CL_NONE, true><<<grid, block, smem, st>>>(P, kchunk);
-    else if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk);
-    else if (closure == CL_AMD) k_momentum_fused<FT, TR, CL_AMD><<<grid, block, smem, st>>>(P, kchunk);
-    else k_momentum_fused<FT, TR, CL_NONE><<<grid, block, smem, st>>>(P, kchunk);
-}
+void launch_fused(int closure, bool ibg, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk);
+template <typename FT, bool TR>
+cudaError_t fused_set_smem_tr();
 template <typename FT>
 cudaError_t fused_set_smem() {
-    const int b = (int)sizeof(fused::Smem<FT>);
-    cudaError_t e = cudaSuccess;
-    for (const void* f : {(const void*)k_momentum_fused<FT, true, CL_NONE>, (const void*)k_momentum_fused<FT, true, CL_SMAG>,
-                          (const void*)k_momentum_fused<FT, true, CL_AMD>, (const void*)k_momentum_fused<FT, false, CL_NONE>,
-                          (const void*)k_momentum_fused<FT, false, CL_SMAG>, (const void*)k_momentum_fused<FT, false, CL_AMD>,
-                          (const void*)k_momentum_fused<FT, true, CL_NONE, true>, (const void*)k_momentum_fused<FT, false, CL_NONE, true>}) {
-        cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-        if (r != cudaSuccess) e = r;
-    }
-    return e;
+    cudaError_t a = fused_set_smem_tr<FT, true>(), b = fused_set_smem_tr<FT, false>();
+    return a != cudaSuccess ? a : b;
 }
 
 namespace {
@@ -409,6 +438,12 @@ struct ModelImpl : gbo_model {
     // state and work arrays
     DBuf<FT> u, v, w, us, vs, ws, Gu, Gv, Gw, nu, phy, p;
     std::vector<DBuf<FT>> c, cs, Gc, kap;
+    // tracer departures (single precision on a Bounded z): per-level reference profiles on
+    // the device and on the host, and a staging buffer for set / get conversions
+    bool departures = false;
+    std::vector<DBuf<FT>> cref;
+    std::vector<std::vector<double>> cref_h;
+    DBuf<double> tstage, tmean;
     // DynamicSmagorinsky: Σ, Σ̄, per-tile LM/MM sums, and per level c², 𝒥ᴸᴹ, 𝒥ᴹᴹ
     DBuf<FT> dyn_sig, dyn_sigb, dyn_cs2, dyn_jlm, dyn_jmm;
     DBuf<double> dyn_part;
@@ -478,8 +513,10 @@ struct ModelImpl : gbo_model {
         cg_cnt.free_();
         if (h_cgs) cudaFreeHost(h_cgs);
         if (body_stream) cudaStreamDestroy(body_stream);
-        for (auto* vec : {&c, &cs, &Gc, &kap})
+        for (auto* vec : {&c, &cs, &Gc, &kap, &cref})
             for (auto& b : *vec) b.free_();
+        tstage.free_();
+        tmean.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_ws.free_(); t_kbot.free_();
         for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
         if (ev0) cudaEventDestroy(ev0);
@@ -558,6 +595,14 @@ struct ModelImpl : gbo_model {
         if (has_phy) phy.alloc(N);
         c.resize(ntr); cs.resize(ntr); Gc.resize(ntr);
         for (int n = 0; n < ntr; ++n) { c[n].alloc(N); cs[n].alloc(N); Gc[n].alloc(N); }
+        departures = sizeof(FT) == 4 && !flat && ntr > 0;
+        if (departures) {
+            cref.resize(ntr);
+            cref_h.assign(ntr, std::vector<double>(Nz, 0.0));
+            for (int n = 0; n < ntr; ++n) cref[n].upload(std::vector<FT>(Nz, FT(0)));
+            tstage.alloc(N);
+            tmean.alloc(Nz);
+        }
         if (md->closure == GBO_CLOSURE_AMD) {
             kap.resize(ntr);
             for (int n = 0; n < ntr; ++n) kap[n].alloc(N);
@@ -630,8 +675,13 @@ struct ModelImpl : gbo_model {
         // (as the pressure solver or as the CG preconditioner on a stretched grid)
         if (desc.pressure_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL ||
             (desc.pressure_solver == GBO_SOLVER_CONJUGATE_GRADIENT && precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL)) {
-            t_ws.alloc((size_t)3 * Nz * Nh * Ny);
+            const size_t cl = (size_t)Nz * Nh * Ny;
+            t_ws.alloc(4 * cl);  // forward-sweep re, im; then the pivot tables
             tp.ws = t_ws.p;
+            tp.tab_s = t_ws.p + 2 * cl;
+            tp.tab_t = t_ws.p + 3 * cl;
+            launch_thomas_tables(tp, stream);
+            GBO_CUDA(cudaGetLastError());
         }
         // shared-memory tiles: keep each block at or below ~100 KB
         const size_t cs_ = sizeof(C), lim = GBO_PASS_SMEM_LIMIT;
@@ -699,12 +749,16 @@ struct ModelImpl : gbo_model {
         return desc.closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY ? (int)CL_AMD : desc.closure;
     }
 
+    const FT* tracer_ref(int n) const { return departures && n < ntr ? cref[n].p : nullptr; }
+
     StepP<FT> params() {
         StepP<FT> P{};
         P.g = gp;
         P.u = u.p; P.v = v.p; P.w = flat ? nullptr : w.p;
         P.nu = nu.p; P.phy = phy.p;
         P.b = (desc.buoyancy_tracer && ntr > 0) ? c[0].p : nullptr;
+        P.bref = (desc.buoyancy_tracer && departures) ? cref[0].p : nullptr;
+        P.cref = nullptr;
         P.uo = us.p; P.vo = vs.p; P.wo = flat ? nullptr : ws.p;
         P.Gu = Gu.p; P.Gv = Gv.p; P.Gw = flat ? nullptr : Gw.p;
         P.f = FT(desc.coriolis_f);
@@ -1028,11 +1082,13 @@ struct ModelImpl : gbo_model {
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;
             Q.c = ntr > 0 ? c[0].p : nullptr;
+            Q.cref = tracer_ref(0);
             pre(G_CLOSURE);
             k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
             check_launch();
             for (int n = 1; n < ntr; ++n) {
                 Q.c = c[n].p;
+                Q.cref = tracer_ref(n);
                 // viscosity recomputed identically; only κₑ of tracer n is new
                 pre(G_CLOSURE);
                 k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, kap[n].p);
@@ -1068,6 +1124,7 @@ struct ModelImpl : gbo_model {
             tracer0 = 0;
         } else if (ntr > 0) {
             M0.c = c[0].p;
+            M0.cref = tracer_ref(0);
             M0.co = cs[0].p;
             M0.Gc = Gc[0].p;
             M0.kap = kap.empty() ? nullptr : kap[0].p;
@@ -1084,6 +1141,7 @@ struct ModelImpl : gbo_model {
         for (int n = tracer0; n < ntr; ++n) {
             StepP<FT> Q = P;
             Q.c = c[n].p;
+            Q.cref = tracer_ref(n);
             Q.co = cs[n].p;
             Q.Gc = Gc[n].p;
             Q.kap = kap.empty() ? nullptr : kap[n].p;
@@ -1110,7 +1168,7 @@ struct ModelImpl : gbo_model {
         if (!ibg) return;
         for (int n = 0; n < ntr; ++n) {
             pre(G_MASK);
-            k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, nullptr, nullptr, nullptr, c[n].p, 8);
+            k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, nullptr, nullptr, nullptr, c[n].p, 8, tracer_ref(n));
             check_launch();
         }
     }
@@ -1297,12 +1355,56 @@ struct ModelImpl : gbo_model {
         return nullptr;
     }
 
+    // index of a tracer stored as departures from its reference profile, or -1
+    int departure_tracer(int field) const {
+        const int n = field - GBO_FIELD_TRACER;
+        return (departures && field >= GBO_FIELD_TRACER && n < ntr) ? n : -1;
+    }
+    unsigned conv_blocks() const { return (unsigned)std::min<size_t>((N + 255) / 256, (size_t)4 * 152 * 8); }
+    // The hydrostatic pressure anomaly of the buoyancy profile alone (the part the kernels
+    // leave out, see k_hydrostatic): the same downward integral in FP64.
+    std::vector<double> phy_reference() const {
+        const std::vector<double>& r = cref_h[0];
+        std::vector<double> ph(Nz);
+        double pk = -(0.5 * (r[Nz - 1] + r[Nz - 1])) * (double)Z.at(Z.dzf, Nz + 1);
+        ph[Nz - 1] = pk;
+        for (int k = Nz - 2; k >= 0; --k) {
+            pk -= (0.5 * (r[k] + r[k + 1])) * (double)Z.at(Z.dzf, k + 2);
+            ph[k] = pk;
+        }
+        return ph;
+    }
+    void download_profile(int n) {
+        std::vector<FT> r(Nz);
+        GBO_CUDA(cudaMemcpyAsync(r.data(), cref[n].p, Nz * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        for (int k = 0; k < Nz; ++k) cref_h[n][k] = (double)r[k];
+    }
+
     // Interior transfer with type conversion; w carries Nz+1 faces at the boundary.
     int set_field(int field, const void* host, int dt_, int64_t count) override {
         FT* d = field_ptr(field);
         if (field == GBO_FIELD_W && flat) { err = "w does not exist on a Flat-z grid"; return GBO_ERR_INVALID; }
         if (!d) { err = "unknown field id"; return GBO_ERR_INVALID; }
         if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
+        const int dn = departure_tracer(field);
+        if (dn >= 0) {
+            // the profile is the horizontal mean of the new values; the field stores departures
+            const size_t plane = (size_t)Nx * Ny;
+            if (dt_ == GBO_FLOAT32) {
+                float* st = reinterpret_cast<float*>(tstage.p);
+                GBO_CUDA(cudaMemcpyAsync(st, host, N * sizeof(float), cudaMemcpyHostToDevice, stream));
+                k_level_mean<float><<<Nz, LM_THREADS, 0, stream>>>(st, plane, tmean.p);
+                k_to_departure<FT, float><<<conv_blocks(), 256, 0, stream>>>(st, tmean.p, cref[dn].p, d, plane, N);
+            } else {
+                GBO_CUDA(cudaMemcpyAsync(tstage.p, host, N * sizeof(double), cudaMemcpyHostToDevice, stream));
+                k_level_mean<double><<<Nz, LM_THREADS, 0, stream>>>(tstage.p, plane, tmean.p);
+                k_to_departure<FT, double><<<conv_blocks(), 256, 0, stream>>>(tstage.p, tmean.p, cref[dn].p, d, plane, N);
+            }
+            GBO_CUDA(cudaGetLastError());
+            download_profile(dn);
+            return GBO_OK;
+        }
         const bool same = (dt_ == GBO_FLOAT32) == (sizeof(FT) == 4);
         if (same) {
             GBO_CUDA(cudaMemcpyAsync(d, host, N * sizeof(FT), cudaMemcpyHostToDevice, stream));
@@ -1322,6 +1424,36 @@ struct ModelImpl : gbo_model {
     int get_field(int field, void* host, int dt_, int64_t count) override {
         FT* d = field_ptr(field);
         if (count != this->count(field)) { err = "element count does not match the field size"; return GBO_ERR_INVALID; }
+        const int dn = departure_tracer(field);
+        if (dn >= 0) {  // reference profile + departure
+            const size_t plane = (size_t)Nx * Ny;
+            if (dt_ == GBO_FLOAT32) {
+                float* st = reinterpret_cast<float*>(tstage.p);
+                k_from_departure<FT, float><<<conv_blocks(), 256, 0, stream>>>(d, cref[dn].p, st, plane, N);
+                GBO_CUDA(cudaGetLastError());
+                GBO_CUDA(cudaMemcpyAsync(host, st, N * sizeof(float), cudaMemcpyDeviceToHost, stream));
+            } else {
+                k_from_departure<FT, double><<<conv_blocks(), 256, 0, stream>>>(d, cref[dn].p, tstage.p, plane, N);
+                GBO_CUDA(cudaGetLastError());
+                GBO_CUDA(cudaMemcpyAsync(host, tstage.p, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            }
+            GBO_CUDA(cudaStreamSynchronize(stream));
+            return GBO_OK;
+        }
+        if (field == GBO_FIELD_PHY && d && departures && desc.buoyancy_tracer) {
+            // the kernels hold pHY′ of the departures; add that of the buoyancy profile
+            std::vector<FT> h(N);
+            GBO_CUDA(cudaMemcpyAsync(h.data(), d, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
+            const std::vector<double> ph = phy_reference();
+            const size_t plane = (size_t)Nx * Ny;
+            for (size_t q = 0; q < N; ++q) {
+                const double x = ph[q / plane] + (double)h[q];
+                if (dt_ == GBO_FLOAT32) static_cast<float*>(host)[q] = (float)x;
+                else static_cast<double*>(host)[q] = x;
+            }
+            return GBO_OK;
+        }
         const bool same = (dt_ == GBO_FLOAT32) == (sizeof(FT) == 4);
         if (d && same) {
             GBO_CUDA(cudaMemcpyAsync(host, d, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
@@ -1361,6 +1493,14 @@ struct ModelImpl : gbo_model {
         return rc != GBO_OK ? rc : cg_status;
     }
 
+    int reference_profile(int field, double* out, int64_t n) override {
+        if (n != Nz) { err = "the profile has Nz values"; return GBO_ERR_INVALID; }
+        const int t = field - GBO_FIELD_TRACER;
+        if (field < GBO_FIELD_TRACER || t >= ntr) { err = "reference profiles exist for tracers only"; return GBO_ERR_INVALID; }
+        for (int k = 0; k < Nz; ++k) out[k] = departures ? cref_h[t][k] : 0.0;
+        return GBO_OK;
+    }
+
     int device_pointer(int field, void** ptr, int64_t* n) override {
         FT* d = field_ptr(field);
         if (!d) { err = "field not present in this model"; return GBO_ERR_INVALID; }
@@ -1381,7 +1521,7 @@ struct ModelImpl : gbo_model {
         double last_dt;
     };
     static constexpr uint64_t kStateMagic = 0x31657461747362ULL;  // "bstate1"
-    static constexpr int32_t kStateVersion = 2;
+    static constexpr int32_t kStateVersion = 3;
     // QAB2 also keeps G⁻ (prognostic_state of its timestepper): the next step reads it
     std::vector<const FT*> state_fields() const {
         std::vector<const FT*> f{u.p, v.p};
@@ -1396,8 +1536,12 @@ struct ModelImpl : gbo_model {
         }
         return f;
     }
+    // after the fields: the tracers' reference profiles (Nz values each) when tracers are
+    // stored as departures
+    int64_t profile_bytes() const { return departures ? (int64_t)ntr * Nz * (int64_t)sizeof(FT) : 0; }
     int64_t state_bytes() const override {
-        return (int64_t)sizeof(StateHeader) + (int64_t)state_fields().size() * (int64_t)N * (int64_t)sizeof(FT);
+        return (int64_t)sizeof(StateHeader) + (int64_t)state_fields().size() * (int64_t)N * (int64_t)sizeof(FT) +
+               profile_bytes();
     }
     int get_state(void* buf, int64_t bytes) override {
         if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
@@ -1407,6 +1551,10 @@ struct ModelImpl : gbo_model {
         for (const FT* f : state_fields()) {
             GBO_CUDA(cudaMemcpyAsync(at, f, N * sizeof(FT), cudaMemcpyDeviceToHost, stream));
             at += N * sizeof(FT);
+        }
+        for (int n = 0; departures && n < ntr; ++n) {
+            GBO_CUDA(cudaMemcpyAsync(at, cref[n].p, Nz * sizeof(FT), cudaMemcpyDeviceToHost, stream));
+            at += Nz * sizeof(FT);
         }
         GBO_CUDA(cudaStreamSynchronize(stream));
         return GBO_OK;
@@ -1424,6 +1572,11 @@ struct ModelImpl : gbo_model {
         for (const FT* f : state_fields()) {
             GBO_CUDA(cudaMemcpyAsync(const_cast<FT*>(f), at, N * sizeof(FT), cudaMemcpyHostToDevice, stream));
             at += N * sizeof(FT);
+        }
+        for (int n = 0; departures && n < ntr; ++n) {
+            GBO_CUDA(cudaMemcpyAsync(cref[n].p, at, Nz * sizeof(FT), cudaMemcpyHostToDevice, stream));
+            at += Nz * sizeof(FT);
+            download_profile(n);
         }
         time = h.time;
         iteration = h.iteration;
@@ -1847,6 +2000,11 @@ int gbo_get_field(gbo_model* m, int32_t field, void* host, int32_t dtype, int64_
 int64_t gbo_field_count(const gbo_model* m, int32_t field) { return m ? m->count(field) : -1; }
 
 int64_t gbo_state_bytes(const gbo_model* m) { return m ? m->state_bytes() : 0; }
+
+int gbo_field_reference_profile(gbo_model* m, int32_t field, double* out, int64_t count) {
+    if (!m || !out) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->reference_profile(field, out, count); });
+}
 
 int gbo_get_state(gbo_model* m, void* buf, int64_t bytes) {
     if (!m || !buf) return GBO_ERR_INVALID;

@@ -28,10 +28,13 @@ namespace {
 static_assert(GBO_STATIC_SCRATCH_BYTES % 256 == 0, "scratch size must be a multiple of 256 bytes");
 static __device__ __align__(256) unsigned char g_scratch[GBO_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
-int g_smem_optin[kMaxDevices] = {};
+// per-context set-up already done: the ID of the CUDA context (unique for the life of the
+// process) and its opt-in shared-memory limit
+constexpr int kMaxContexts = 64;
+unsigned long long g_ctx_ids[kMaxContexts] = {};
+int g_ctx_optin[kMaxContexts] = {};
+int g_nctx = 0;
 
 thread_local char g_msg[256];
 
@@ -121,22 +124,60 @@ __global__ void k_static_tables(PassP<FT> P, Cx<FT>* tw_xh, Cx<FT>* tw_x, Cx<FT>
     }
 }
 
-// Once per device, with that device current: the address of g_scratch and the
-// opt-in shared-memory limit.
+// The address of g_scratch in the current context, looked up on every call (a host-side
+// lookup): the array belongs to the module loaded in a context, and a context reset
+// (cudaDeviceReset, a primary-context reset, or another context made current) loads the
+// module again, possibly elsewhere.  Once per context, with that context current: the
+// opt-in shared-memory limit and the pass kernels' dynamic shared-memory attribute
+// (function attributes are per context too).  The context is identified by its ID from
+// the driver (cuCtxGetId, fetched through the runtime's driver entry point so the library
+// needs no link to libcuda).
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
 int setup(int dev, unsigned char** base, int* optin) {
+    void* p = nullptr;
+    cudaError_t rc = cudaGetSymbolAddress(&p, g_scratch);  // also makes the context current
+    if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed (error %lld)", (long long)rc);
+    *base = static_cast<unsigned char*>(p);
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t rc = cudaGetSymbolAddress(&p, g_scratch);
-        if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed (error %lld)", (long long)rc);
-        int v = 0;
-        rc = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaDeviceGetAttribute failed (error %lld)", (long long)rc);
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-        g_smem_optin[dev] = v;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess)
+            return fail_msg(GBO_ERR_CUDA, "the driver does not provide cuCtxGetCurrent / cuCtxGetId");
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
     }
-    *base = g_scratch_ptr[dev];
-    *optin = g_smem_optin[dev];
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0)
+        return fail_msg(GBO_ERR_CUDA, "no current CUDA context after the scratch lookup");
+    for (int q = 0; q < g_nctx; ++q)
+        if (g_ctx_ids[q] == id) {
+            *optin = g_ctx_optin[q];
+            return GBO_OK;
+        }
+    int v = 0;
+    rc = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaDeviceGetAttribute failed (error %lld)", (long long)rc);
+    // Raise (never lower) the pass kernels' dynamic shared-memory limit, for both float
+    // types, to the opt-in maximum: models set the same value when they are created, so
+    // no later call lowers it.
+    rc = fft_set_smem<float>(v, v, v);
+    if (rc == cudaSuccess) rc = fft_set_smem<double>(v, v, v);
+    if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaFuncSetAttribute failed (error %lld)", (long long)rc);
+    if (g_nctx < kMaxContexts) {
+        g_ctx_ids[g_nctx] = id;
+        g_ctx_optin[g_nctx] = v;
+        ++g_nctx;
+    }
+    *optin = v;
     return GBO_OK;
 }
 
@@ -158,7 +199,6 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
     int dev = 0;
     cudaError_t rc = cudaGetDevice(&dev);
     if (rc != cudaSuccess) return fail(GBO_ERR_NO_DEVICE, "no CUDA device (error %lld)", (long long)rc);
-    if (dev < 0 || dev >= kMaxDevices) return fail(GBO_ERR_INVALID, "device ordinal %lld out of range", dev);
     unsigned char* base = nullptr;
     int optin = 0;
     int s = setup(dev, &base, &optin);
@@ -190,10 +230,6 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
     if (std::max({smem_z, smem_x, smem_y}) > (size_t)optin)
         return fail(GBO_ERR_INVALID, "grid needs %lld bytes of shared memory per block; the device allows %lld",
                     (long long)std::max({smem_z, smem_x, smem_y}), optin);
-    // Raise (never lower) the pass kernels' dynamic shared-memory limit: the kernels are
-    // shared with models, which set their own, smaller limits when they are created.
-    rc = fft_set_smem<FT>(optin, optin, optin);
-    if (rc != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaFuncSetAttribute failed (error %lld)", (long long)rc);
 
     if (phi != rhs) {
         rc = cudaMemcpyAsync(phi, rhs, N * sizeof(FT), cudaMemcpyDeviceToDevice, st);

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256) k_tracer(StepP<FT> P) {
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = blockIdx.z;
     if (i >= g.Nx || j >= g.Ny) return;
-    CFld<FT> u = cfld(P.u, g), v = cfld(P.v, g), c = cfld(P.c, g);
+    CFld<FT> u = cfld(P.u, g), v = cfld(P.v, g), c = cfld(P.c, g, P.cref);
     WFld<FT> w = wfld(P.w, g);
     Met<FT> M(g);
     const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
@@ -179,5 +179,6 @@ __global__ void __launch_bounds__(256) k_tracer(StepP<FT> P) {
     }
     FT Gm = P.first ? FT(0) : P.Gc[idx];
     P.Gc[idx] = G;
+    // the update of a departure field acts on the stored departure (the profile is fixed)
     P.co[idx] = rk3_update(P.c[idx], G, Gm, P, stage_dt(P));
 }

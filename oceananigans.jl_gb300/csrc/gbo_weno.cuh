@@ -85,6 +85,64 @@ GBO_D FT weno5(const FT S[6], bool left) {
     return weno5v<FT>(S[0], S[1], S[2], S[3], S[4], S[5], left);
 }
 
+// Two WENO5 reconstructions at once: (weno5(A, la), weno5(B, lb)).  The generic form
+// evaluates them one after the other; the FP32 form below evaluates both in packed FP32
+// (FFMA2 / FADD2 / FMUL2, sm_100 and later), component x for A and y for B, with the
+// operations of weno5v in the same order (the β of a shifted stencil drops its terms in
+// the centre value, which are exactly zero there), so each component equals the scalar
+// result up to the contraction of products into FMAs.
+template <typename FT>
+GBO_D void weno5_2(const FT A[6], bool la, const FT B[6], bool lb, FT& ra, FT& rb) {
+    ra = weno5<FT>(A, la);
+    rb = weno5<FT>(B, lb);
+}
+
+namespace wenopk {
+GBO_D float2 f2(float a, float b) { return make_float2(a, b); }
+GBO_D float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+GBO_D float2 sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+GBO_D float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+GBO_D float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+GBO_D float2 sc(float c) { return make_float2(c, c); }
+// β of a shifted 3-point stencil (weno_interpolants.jl:169-174, shift :268-281):
+// p0, p2 are the outer values minus the centre value
+GBO_D float2 beta(float2 p0, float2 p2, float c00, float c02, float c22) {
+    // p0 (c00 p0 + c02 p2) + c22 p2 p2, as weno5v's polynomial with its centre terms removed
+    return fma2(p0, fma2(sc(c02), p2, mul(sc(c00), p0)), mul(mul(p2, p2), sc(c22)));
+}
+}  // namespace wenopk
+
+template <>
+GBO_D void weno5_2<float>(const float A[6], bool la, const float B[6], bool lb, float& ra, float& rb) {
+    using namespace wenopk;
+    using K = GboCoeffs<float>;
+    // a right-biased reconstruction is the left-biased one of the reversed stencil
+    float2 t[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) t[j] = f2(la ? A[j] : A[5 - j], lb ? B[j] : B[5 - j]);
+    // stencils P0 = (t2, t3, t4), P1 = (t1, t2, t3), P2 = (t0, t1, t2)
+    const float2 be0 = beta(sub(t[2], t[3]), sub(t[4], t[3]), 10.f, 11.f, 4.f);
+    const float2 be1 = beta(sub(t[1], t[2]), sub(t[3], t[2]), 4.f, 5.f, 4.f);
+    const float2 be2 = beta(sub(t[0], t[1]), sub(t[2], t[1]), 4.f, 11.f, 10.f);
+    const float2 d = sub(be0, be2);
+    const float2 tau = f2(fabsf(d.x), fabsf(d.y));
+    const float2 e0 = add(be0, sc(K::eps)), e1 = add(be1, sc(K::eps)), e2 = add(be2, sc(K::eps));
+    const float2 q0 = f2(__fdividef(tau.x, e0.x), __fdividef(tau.y, e0.y));
+    const float2 q1 = f2(__fdividef(tau.x, e1.x), __fdividef(tau.y, e1.y));
+    const float2 q2 = f2(__fdividef(tau.x, e2.x), __fdividef(tau.y, e2.y));
+    const float2 al0 = mul(sc(K::weno3_cstar[0]), fma2(q0, q0, sc(1.f)));
+    const float2 al1 = mul(sc(K::weno3_cstar[1]), fma2(q1, q1, sc(1.f)));
+    const float2 al2 = mul(sc(K::weno3_cstar[2]), fma2(q2, q2, sc(1.f)));
+    const float2 sum = add(add(al0, al1), al2);
+    const float2 inv = f2(__fdividef(1.f, sum.x), __fdividef(1.f, sum.y));
+    const float2 p0 = fma2(sc(K::weno3_p0[2]), t[4], fma2(sc(K::weno3_p0[1]), t[3], mul(sc(K::weno3_p0[0]), t[2])));
+    const float2 p1 = fma2(sc(K::weno3_p1[2]), t[3], fma2(sc(K::weno3_p1[1]), t[2], mul(sc(K::weno3_p1[0]), t[1])));
+    const float2 p2 = fma2(sc(K::weno3_p2[2]), t[2], fma2(sc(K::weno3_p2[1]), t[1], mul(sc(K::weno3_p2[0]), t[0])));
+    const float2 r = fma2(mul(al2, inv), p2, fma2(mul(al1, inv), p1, mul(mul(al0, inv), p0)));
+    ra = r.x;
+    rb = r.y;
+}
+
 // WENO3 biased reconstruction at a face; S[0..3] = ψ at face offsets -2..+1.
 template <typename FT>
 GBO_D FT weno3(const FT S[4], bool left) {

@@ -103,6 +103,7 @@ SIGNATURES = {
     "gbo_get_field": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int64]),
     "gbo_field_count": (ctypes.c_int64, [_vp, ctypes.c_int32]),
     "gbo_field_device_pointer": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(_vp), ctypes.POINTER(ctypes.c_int64)]),
+    "gbo_field_reference_profile": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_int64]),
     "gbo_time_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32]),
     "gbo_clock": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     "gbo_synchronize": (ctypes.c_int, [_vp]),

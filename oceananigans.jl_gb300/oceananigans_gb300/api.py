@@ -486,6 +486,15 @@ class NonhydrostaticModel:
         L.check(L.load().gbo_field_device_pointer(self._h, self._fid(name), ctypes.byref(p), ctypes.byref(n)), self._h)
         return p.value, n.value
 
+    def reference_profile(self, name):
+        """The per-level reference profile a tracer's device array is a departure from
+        (zeros where the tracer is stored directly: FP64 models, Flat z)."""
+        out = np.zeros(self.grid.Nz, dtype=np.float64)
+        L.check(L.load().gbo_field_reference_profile(self._h, self._fid(name),
+                                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size),
+                self._h)
+        return out
+
     def poisson_solve_device(self, phi_ptr, rhs_ptr):
         L.check(L.load().gbo_poisson_solve_device(self._h, ctypes.c_void_p(phi_ptr), ctypes.c_void_p(rhs_ptr)), self._h)
 

@@ -13,7 +13,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py <path of the Oceananigans.jl source tree>")
+REF = sys.argv[1]
 
 
 def read(rel):

@@ -117,15 +117,20 @@ def test_turbulence_2d_128_400_steps():
 
 def test_convection_full_size_fp32_against_fp64():
     # the convection benchmark grid (256²×128): FP32 against FP64 on the GPU after 100
-    # steps, and incompressibility of both (test_time_stepping.jl:138-171 at full size)
+    # steps within the FP32 bar of 1e-5 relative L2 per prognostic field (measured
+    # u, v 5.1e-7, w 5.9e-7, b 1.5e-9 with tracers stored as departures from their level
+    # means), and incompressibility of both (test_time_stepping.jl:138-171 at full size)
     c32 = cases.convection_3d((256, 256, 128), float_type=np.float32, seed=5)
     c64 = cases.convection_3d((256, 256, 128), seed=5)
     m32, m64 = c32.start_gpu(), c64.start_gpu()
     og.time_step_(m32, 2.0, 100)
     og.time_step_(m64, 2.0, 100)
-    errs = {n: cases.rel_l2(m32.get(n), m64.get(n)) for n in ("u", "v", "w", "b")}
+    errs = {n: cases.rel_l2(m32.get(n), m64.get(n)) for n in ("u", "v", "w", "b", "pHY")}
     print("fp32 vs fp64 after 100 steps at 256x256x128:", errs)
-    assert max(errs.values()) < 1e-3
+    assert max(errs.values()) <= 1e-5, errs
+    # the non-hydrostatic pressure solves ∇²p = ∇·u*/Δt, a small difference of O(|u|) face
+    # values rounded in FP32 (measured 1.8e-5)
+    assert cases.rel_l2(m32.get("p"), m64.get("p")) <= 5e-5
     g = c64.grid
     for m, tol in ((m64, 1e-12), (m32, 1e-5)):
         u, v, w = m.get("u").astype(np.float64), m.get("v").astype(np.float64), m.get("w").astype(np.float64)

@@ -70,6 +70,11 @@ def test_static_solve_matches_model_solve(kind, shape, float_type, tol):
     inplace = rhs.clone()
     _static_solve(c.grid, inplace, inplace, torch)
     assert cases.rel_l2(inplace.cpu().numpy().astype(np.float64), want) <= tol
+    if float_type == np.float64:
+        # and against the FP64 oracle's own FFT solve, which shares no code with either
+        # GPU path (its transforms, tables and eigenvalues are its own)
+        oracle_phi = c.oracle_model().poisson_solve(b).ravel(order="F")
+        assert cases.rel_l2(got, oracle_phi) <= 1e-12
 
 
 def test_static_solve_rejects_grids_beyond_the_scratch():

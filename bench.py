@@ -53,8 +53,15 @@ def parse():
     p.add_argument("--size", type=int, nargs=3, default=None)
     p.add_argument("--dtype", default=None, choices=["f32", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-other-workloads", action="store_true",
+                   help="skip the records of the other benchmark configurations in the headline line")
+    p.add_argument("--timed-only", action="store_true",
+                   help="the timed steps and the per-kernel pass only (no e2e, CPU baseline, yardstick or "
+                        "secondary records): the run a profiler captures")
     p.add_argument("--e2e-steps", type=int, default=5)
     a = p.parse_args()
+    if a.timed_only:
+        a.no_cpu_baseline, a.no_other_workloads, a.e2e_steps = True, True, 0
     w = WORKLOADS[a.workload]
     a.size = tuple(a.size) if a.size else w["size"]
     a.dtype = a.dtype or w["dtype"]
@@ -318,11 +325,13 @@ class ClockSampler:
 # capture, its command and the algorithmic bytes of the same launch are in the named profile.
 PROFILED_TRAFFIC = {
     ("convection", "k_momentum", (256, 256, 128), "f32"): {
-        "traffic": 426.7e6,
+        "traffic": 433.6e6,
         "traffic_launch": "one RK3 stage-1 launch (algorithmic bytes of that launch 469.8e6; stages 2-3 also read G-)",
         "traffic_profile": "profiles/k_momentum_fused_free_convection_256x256x128_f32.md",
-        "issue_active_frac": 0.578,
-        "dram_throughput_frac": 0.053,
+        "issue_active_frac": 0.681,
+        "fma_pipe_inst_frac": 0.235,
+        "alu_pipe_inst_frac": 0.395,
+        "dram_throughput_frac": 0.067,
     },
 }
 
@@ -547,6 +556,103 @@ def seamount_poisson_record(torch, og, L, n=20):
         if "ms_mean" in rec["learned_pcg"]:
             rec["learned_over_fft_time"] = rec["learned_pcg"]["ms_mean"] / rec["fft_pcg"]["ms_mean"]
     return rec
+
+
+def kernel_table(lib, L, model, dt, size, s, nt=2, **ab_kw):
+    """Per-kernel-group ms per launch, launches per step and achieved GB/s from the
+    instrumented pass (CUDA events around every launch on the model's stream)."""
+    ng = lib.gbo_kernel_group_count()
+    ms = (ctypes.c_double * ng)()
+    cnt = (ctypes.c_int64 * ng)()
+    L.check(lib.gbo_kernel_timings(model._h, dt, nt, ms, ng), model._h)
+    L.check(lib.gbo_kernel_timing_counts(model._h, cnt, ng), model._h)
+    out = {}
+    for g in range(ng):
+        n = lib.gbo_kernel_group_name(g).decode()
+        if ms[g] > 0 and n != "k_nan_check":
+            b = algorithmic_bytes(n, size, s, **ab_kw)
+            out[n] = {"ms_per_launch": ms[g], "launches_per_step": cnt[g] / nt, "ms_per_step": ms[g] * cnt[g] / nt,
+                      "achieved_gbs": b / (ms[g] / 1e3) / 1e9 if b else None}
+    tot = sum(k["ms_per_step"] for k in out.values()) or 1.0
+    for k in out.values():
+        k["share"] = k["ms_per_step"] / tot
+    return out
+
+
+def workload_record(name, torch, og, L, lib, steps, warmup=2):
+    """One benchmark configuration timed on this GPU: cell-updates/s from CUDA events on
+    the model's stream around `steps` graph-replayed steps, and its top kernel groups."""
+    w = WORKLOADS[name]
+    size = w["size"]
+    ft = np.float32 if w["dtype"] == "f32" else np.float64
+    s = 4 if ft == np.float32 else 8
+    grid, physics, init = workload(name, size, ft)
+    model = og.NonhydrostaticModel(grid, **physics)
+    og.set_(model, **init)
+    sp = ctypes.c_void_p()
+    lib.gbo_model_stream(model._h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    og.time_step_(model, w["dt"], warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    og.time_step_(model, w["dt"], steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el = e0.elapsed_time(e1) / 1e3
+    cells = float(np.prod(size))
+    cl = physics.get("closure")
+    closure = None if cl is None else ("amd" if isinstance(cl, og.AnisotropicMinimumDissipation) else "smagorinsky")
+    ntr = len(physics.get("tracers", ()))
+    kern = kernel_table(lib, L, model, w["dt"], size, s, ntr=ntr, closure=closure,
+                        has_phy=ntr > 0 and grid.topology[2] == "Bounded", fused=grid.bottom_height is None)
+    top = sorted(kern, key=lambda n: -kern[n]["ms_per_step"])[:4]
+    rec = {"workload": w["name"] % tuple(size), "float": w["dtype"], "dt_s": w["dt"], "steps": steps,
+           "value": cells * steps / el, "unit": UNIT, "ms_per_step": 1e3 * el / steps,
+           "top_kernels": {n: kern[n] for n in top}}
+    if isinstance(physics.get("pressure_solver"), og.ConjugateGradientPoissonSolver):
+        rec["cg_iterations_last_solve"] = model.solver_iterations
+    del model
+    torch.cuda.synchronize()
+    return rec
+
+
+def ensemble_record(torch, og, L, lib, steps=10):
+    """The 64-member ensemble (one graph launch per step) against the same members
+    stepped one after another: cell-updates/s of each."""
+    dt = WORKLOADS["ensemble"]["dt"]
+    specs = ensemble_specs(64, np.float32)
+    ens = og.Ensemble([(g, p) for g, p, _ in specs])
+    for mm, (_, _, init) in zip(ens.members, specs):
+        og.set_(mm, **init)
+    cells = float(sum(np.prod(g.size()) for g, _, _ in specs))
+    sp = ctypes.c_void_p()
+    lib.gbo_ensemble_stream(ens._h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    ens.time_step(dt, 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ens.time_step(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched = cells * steps / (e0.elapsed_time(e1) / 1e3)
+    del ens
+    singles = []
+    for g, p, init in specs:
+        m = og.NonhydrostaticModel(g, **p)
+        og.set_(m, **init)
+        og.time_step_(m, dt, 1)
+        singles.append(m)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for m in singles:
+        og.time_step_(m, dt, steps)
+    torch.cuda.synchronize()
+    seq = cells * steps / (time.perf_counter() - t0)
+    return {"workload": WORKLOADS["ensemble"]["name"], "members": len(specs), "cells": int(cells), "float": "f32",
+            "steps": steps, "value": batched, "unit": UNIT, "ms_per_step": 1e3 * cells / batched,
+            "sequential_value": seq, "speedup_of_batched": batched / seq}
 
 
 def run_ensemble(args, torch, og, L, lib, local):
@@ -789,11 +895,19 @@ def main():
     # the rest of the metric on the headline run: the cuFFT yardstick of the FFT solve on this
     # grid, and the seamount grid's Poisson-solve times (FFT-PCG and learned PCG to 1e-8)
     yard = None
-    if (rank == 0 and physics.get("pressure_solver") is None and grid.bottom_height is None and grid.z_faces is None
-            and grid.topology[2] == "Bounded"):
+    if (rank == 0 and not args.timed_only and physics.get("pressure_solver") is None and grid.bottom_height is None
+            and grid.z_faces is None and grid.topology[2] == "Bounded"):
         yard = cufft_yardstick(model, grid, torch, stream, ft)
-    if rank == 0 and args.workload == "convection" and tuple(size) == WORKLOADS["convection"]["size"]:
+    others = None
+    if (rank == 0 and not args.timed_only and args.workload == "convection"
+            and tuple(size) == WORKLOADS["convection"]["size"]):
         poisson = seamount_poisson_record(torch, og, L)
+        # the other benchmark configurations, each timed on this GPU in the same run
+        if not args.no_other_workloads:
+            others = {"turbulence2d": workload_record("turbulence2d", torch, og, L, lib, steps=400),
+                      "stretched_amd": workload_record("stretched_amd", torch, og, L, lib, steps=10),
+                      "seamount": workload_record("seamount", torch, og, L, lib, steps=5),
+                      "ensemble": ensemble_record(torch, og, L, lib)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -808,6 +922,8 @@ def main():
             line["poisson_solve"] = poisson
         if yard:
             line["fft_poisson_vs_cufft"] = yard
+        if others:
+            line["other_workloads"] = others
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -463,7 +463,7 @@ struct ThomasColumn {
 // elision of the forward update where |β| <= 10 eps depend on the grid and the column's
 // wavenumbers only, never on the right-hand side, so they are computed once per model and
 // the sweep itself has no FP64 division (the costly operation of the sweep on this GPU).
-__global__ void __launch_bounds__(128) k_thomas_tables(ThomasP T) {
+static __global__ void __launch_bounds__(128) k_thomas_tables(ThomasP T) {
     const size_t ncol = (size_t)T.Nh * T.Ny;
     const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= ncol) return;

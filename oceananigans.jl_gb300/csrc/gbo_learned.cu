@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "gbo_learned.cuh"
+#include "gbo_umma.cuh"
 
 namespace learned {
 
@@ -180,6 +181,162 @@ __global__ void __launch_bounds__(256) k_conv_halo(ConvP p) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Convolution on the fifth-generation tensor cores (tcgen05, TMEM accumulators).
+//
+// Implicit GEMM: M = 128 cells of a level (one MMA, one TMEM lane each), N = 16 output
+// channels per block, K = 27 taps × cin.  A block owns BY consecutive rows (y) of one
+// z level and stages their halo -- rows y0-1 .. y0+BY, levels z-1 .. z+1, x with one
+// periodic halo cell each side -- once in shared memory, channel plane by channel plane
+// (8 channels of a cell = 16 bytes): plane cg holds, for every tile position, channels
+// 8 cg .. 8 cg + 7.  Tile positions are flattened (dz, row, x + 1) with row stride
+// RS = nx + 2, so output cell (row r, x) is M row m = r RS + x and its neighbour
+// (dz, dy, dx) sits at tile position m + ((dz (BY + 2) + dy) RS + dx): every tap of the
+// 3³ stencil is the same K-major canonical operand (8-row groups 128 bytes apart,
+// SBO = 128) started at another 16-byte offset, so the tile is loaded once and each
+// tap is one descriptor.  M rows that fall on halo positions or beyond the block's
+// rows compute values that are never stored.  K = 16 per MMA: with 16 or more input
+// channels one tap and two channel planes (LBO = the plane stride); with 8 input
+// channels two consecutive taps (LBO = the distance of their offsets).  Weights are
+// the B operand, [k group][16 outputs][8 k] per block.  One thread issues the MMAs,
+// tcgen05.commit arrives on an mbarrier, the four warps read their 32 TMEM lanes each
+// (tcgen05.ld) and apply bias and ReLU (or the final z update).
+// ---------------------------------------------------------------------------
+namespace umc {
+constexpr int M = 128, NB = 16;
+struct Geo {
+    int BY, RS, MT, cells;  // rows per block, row stride, M tiles, tile positions per plane
+};
+GBO_HD Geo geo(int nx) {
+    Geo g;
+    g.RS = nx + 2;
+    g.BY = nx >= M ? 1 : (M - nx) / g.RS + 1;
+    g.MT = ((g.BY - 1) * g.RS + nx + M - 1) / M;
+    const int tmax = (2 * (g.BY + 2) + 2) * g.RS + 2;  // offset of the last tap
+    const int real = 3 * (g.BY + 2) * g.RS;
+    g.cells = ((real > M * g.MT + tmax ? real : M * g.MT + tmax) + 7) / 8 * 8;
+    return g;
+}
+GBO_HD constexpr int kgroups(int cin) { return cin == 8 ? 28 : 27 * cin / 8; }
+inline size_t smem_bytes(int cin, int nx) {
+    const Geo g = geo(nx);
+    return (size_t)(cin / 8) * g.cells * 16 + (size_t)kgroups(cin) * NB * 16 + 16;
+}
+constexpr int WAIT_LIMIT = 1 << 24;  // mbarrier polls before a block reports a timeout
+}  // namespace umc
+
+struct UConvP {
+    const bf16* in;      // [n][cin]
+    const bf16* w;       // [cout / 16][k groups][16][8]
+    const float* bias;   // [cout]
+    bf16* out;           // mode 0: [n][cout]
+    void* z;             // mode 1: FT field, z += s (acc + bias) for output channel 0
+    const float* scale;  // mode 1: s
+    unsigned* flags;     // GBO_FLAG_TIMEOUT on a wait that gave up (may be null)
+    Dims d;
+    int cout;
+};
+
+template <int CIN, int MODE, typename FT>
+__global__ void __launch_bounds__(128) k_conv_umma(UConvP p) {
+    using namespace umc;
+    constexpr int PL = CIN / 8, KGN = kgroups(CIN);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const Geo G = geo(p.d.nx);
+    bf16* tile = reinterpret_cast<bf16*>(smem_raw);       // [PL][cells][8]
+    bf16* wsm = tile + (size_t)PL * G.cells * 8;           // [KGN][NB][8]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(wsm + KGN * NB * 8);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+    const int y0 = blockIdx.x * G.BY, z = blockIdx.y, nb = blockIdx.z;
+    if (warp == 0) umma::tmem_alloc(slot, 32);
+    if (tid == 0) umma::mbar_init(mbar, 1);
+    const int real = 3 * (G.BY + 2) * G.RS;
+    for (int e = tid; e < PL * G.cells; e += 128) {
+        const int cg = e / G.cells, pos = e - cg * G.cells;
+        int64_t src = 0;
+        bool ok = false;
+        if (pos < real) {
+            const int xx = pos % G.RS, r = pos / G.RS, ry = r % (G.BY + 2), dz = r / (G.BY + 2);
+            const int gz = z + dz - 1;
+            if (gz >= 0 && gz < nz) {
+                const int gx = wrapm(xx - 1, nx), gy = wrapm(y0 + ry - 1, ny);
+                src = (gx + (int64_t)nx * (gy + (int64_t)ny * gz)) * CIN + cg * 8;
+                ok = true;
+            }
+        }
+        cp16(tile + ((size_t)cg * G.cells + pos) * 8, p.in + src, ok);
+    }
+    const bf16* wsrc = p.w + (size_t)nb * KGN * NB * 8;
+    for (int e = tid; e < KGN * NB; e += 128) cp16(wsm + e * 8, wsrc + e * 8, true);
+    cp_commit();
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *slot;
+    if (tid == 0) {
+        constexpr uint32_t idesc = umma::idesc_bf16_f32(M, NB);
+        const uint32_t tb = umma::smem_addr(tile), wb = umma::smem_addr(wsm);
+        const uint32_t pstride = (uint32_t)G.cells * 16;
+        auto toff = [&](int tap) { return ((tap / 9) * (G.BY + 2) + (tap / 3) % 3) * G.RS + tap % 3; };
+        for (int q = 0; q < G.MT; ++q) {
+            const uint32_t d = tmem + (uint32_t)(q * NB);
+            if constexpr (CIN == 8) {
+                for (int st = 0; st < 14; ++st) {
+                    const int o0 = toff(2 * st), o1 = 2 * st + 1 <= 26 ? toff(2 * st + 1) : o0 + 1;
+                    const uint64_t ad = umma::sdesc(tb + (uint32_t)(M * q + o0) * 16, (uint32_t)(o1 - o0) * 16, 128);
+                    const uint64_t bd = umma::sdesc(wb + (uint32_t)(2 * st) * NB * 16, NB * 16, 128);
+                    umma::mma_bf16(d, ad, bd, idesc, st > 0);
+                }
+            } else {
+                for (int tap = 0; tap < 27; ++tap) {
+                    const uint32_t a0 = tb + (uint32_t)(M * q + toff(tap)) * 16;
+#pragma unroll
+                    for (int c = 0; c < PL / 2; ++c) {
+                        const uint64_t ad = umma::sdesc(a0 + (uint32_t)(2 * c) * pstride, pstride, 128);
+                        const uint64_t bd = umma::sdesc(wb + (uint32_t)(tap * PL + 2 * c) * NB * 16, NB * 16, 128);
+                        umma::mma_bf16(d, ad, bd, idesc, tap > 0 || c > 0);
+                    }
+                }
+            }
+        }
+        umma::commit(mbar);
+    }
+    const bool done = umma::mbar_wait(mbar, 0, WAIT_LIMIT);
+    if (!done && tid == 0 && p.flags) atomicOr(p.flags, GBO_FLAG_TIMEOUT);
+    umma::fence_after_sync();
+    if (done) {
+        for (int q = 0; q < G.MT; ++q) {
+            float v[16];
+            umma::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(q * NB), v);
+            const int m = M * q + 32 * warp + lane;
+            const int ry = m / G.RS, x = m - ry * G.RS, y = y0 + ry;
+            if (ry < G.BY && x < nx && y < ny) {
+                const int64_t cell = x + (int64_t)nx * (y + (int64_t)ny * z);
+                if constexpr (MODE == 0) {
+                    const float* b = p.bias + nb * NB;
+                    uint4 o[2];
+                    uint32_t* ow = reinterpret_cast<uint32_t*>(o);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) ow[c] = pack2(fmaxf(v[2 * c] + b[2 * c], 0.f), fmaxf(v[2 * c + 1] + b[2 * c + 1], 0.f));
+                    uint4* dst = reinterpret_cast<uint4*>(p.out + cell * p.cout + nb * NB);
+                    dst[0] = o[0];
+                    dst[1] = o[1];
+                } else {
+                    FT* zz = static_cast<FT*>(p.z);
+                    zz[cell] += FT(*p.scale * (v[0] + p.bias[0]));
+                }
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tmem, 32);
+}
+
 // s = sqrt(mean(r²)) (1 when r = 0): FP64 block sums, the last block finishes
 template <typename FT>
 __global__ void __launch_bounds__(256) k_rms(const FT* __restrict__ r, int64_t n, double* acc, unsigned* cnt, float* scale) {
@@ -292,6 +449,7 @@ using learned::Dims;
 struct LearnedNet {
     Dims d[learned::LEVELS];
     bf16* w[learned::NLAYERS] = {};
+    bf16* wu[learned::NLAYERS] = {};  // the tcgen05 B operand: [cout / 16][k groups][16][8]
     float* b[learned::NLAYERS] = {};
     // activations: features, encoder outputs, pooled inputs, decoder inputs / outputs
     bf16 *f0 = nullptr, *e0 = nullptr, *d0in = nullptr;
@@ -345,10 +503,25 @@ LearnedNet* learned_create(int nx, int ny, int nz, const float* weights, int64_t
             for (int c = 0; c < FILE_CIN[l]; ++c)
                 for (int tap = 0; tap < 27; ++tap) hw[(size_t)co * kp + tap * cin + c] = __float2bfloat16(*at++);
         for (int co = 0; co < FILE_COUT[l]; ++co) hb[co] = *at++;
+        // the same weights as tcgen05 B operands: block nb of 16 outputs, k group kg (tap kg with
+        // 8 input channels, else tap kg / (cin/8) and channels 8 (kg mod cin/8) ..), 8 k each
+        const int kgn = umc::kgroups(cin), pl = cin / 8, nbk = (cout + 15) / 16;
+        std::vector<bf16> hu((size_t)nbk * kgn * 16 * 8, __float2bfloat16(0.f));
+        for (int nb = 0; nb < nbk; ++nb)
+            for (int kg = 0; kg < kgn; ++kg)
+                for (int n = 0; n < 16; ++n)
+                    for (int e = 0; e < 8; ++e) {
+                        const int co = nb * 16 + n;
+                        const int tap = cin == 8 ? kg : kg / pl, ci = cin == 8 ? e : (kg % pl) * 8 + e;
+                        if (tap < 27 && co < cout && ci < cin)
+                            hu[(((size_t)nb * kgn + kg) * 16 + n) * 8 + e] = hw[(size_t)co * kp + tap * cin + ci];
+                    }
         net->w[l] = need(net->dev<bf16>(hw.size()));
-        net->b[l] = need(net->dev<float>(hb.size()));
+        net->wu[l] = need(net->dev<bf16>(hu.size()));
+        net->b[l] = need(net->dev<float>(std::max<size_t>(hb.size(), 16)));
         if (ok) {
             cudaMemcpy(net->w[l], hw.data(), hw.size() * sizeof(bf16), cudaMemcpyHostToDevice);
+            cudaMemcpy(net->wu[l], hu.data(), hu.size() * sizeof(bf16), cudaMemcpyHostToDevice);
             cudaMemcpy(net->b[l], hb.data(), hb.size() * sizeof(float), cudaMemcpyHostToDevice);
         }
     }
@@ -382,11 +555,23 @@ void learned_destroy(LearnedNet* net) { delete net; }
 
 namespace {
 
+#ifndef GBO_LEARNED_UMMA
+#define GBO_LEARNED_UMMA 0
+#endif
+
 template <int CIN, int COUT, int MODE, typename FT>
-void conv(const LearnedNet* net, int layer, int level, const bf16* in, bf16* out, void* z, cudaStream_t st) {
+void conv(const LearnedNet* net, int layer, int level, const bf16* in, bf16* out, void* z, cudaStream_t st,
+          unsigned* flags) {
+    const learned::Dims& d = net->d[level];
+    if (GBO_LEARNED_UMMA) {
+        const learned::umc::Geo g = learned::umc::geo(d.nx);
+        learned::UConvP p{in, net->wu[layer], net->b[layer], out, z, net->scale + 1, flags, d, COUT};
+        const dim3 grid((d.ny + g.BY - 1) / g.BY, d.nz, (COUT + 15) / 16);
+        learned::k_conv_umma<CIN, MODE, FT><<<grid, 128, learned::umc::smem_bytes(CIN, d.nx), st>>>(p);
+        return;
+    }
     using namespace learned::halo;
     learned::ConvP p{in, net->w[layer], net->b[layer], out, z, net->scale + 1, net->d[level]};
-    const learned::Dims& d = net->d[level];
     const dim3 grid((d.nx + TX - 1) / TX, (d.ny + TY - 1) / TY, d.nz);
     learned::k_conv_halo<CIN, COUT, MODE, FT><<<grid, 256, smem_bytes<COUT>(), st>>>(p);
 }
@@ -397,9 +582,18 @@ cudaError_t conv_smem() {
     return cudaFuncSetAttribute(learned::k_conv_halo<CIN, COUT, MODE, FT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)learned::halo::smem_bytes<COUT>());
 }
+template <int CIN, int MODE, typename FT>
+cudaError_t uconv_smem() {
+    return cudaFuncSetAttribute(learned::k_conv_umma<CIN, MODE, FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
 cudaError_t conv_smem_all() {
     using namespace learned;
     cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {uconv_smem<8, 0, float>(), uconv_smem<16, 0, float>(), uconv_smem<32, 0, float>(),
+                          uconv_smem<48, 0, float>(), uconv_smem<64, 0, float>(), uconv_smem<16, 1, float>(),
+                          uconv_smem<8, 0, double>(), uconv_smem<16, 0, double>(), uconv_smem<32, 0, double>(),
+                          uconv_smem<48, 0, double>(), uconv_smem<64, 0, double>(), uconv_smem<16, 1, double>()})
+        if (r != cudaSuccess) e = r;
     for (cudaError_t r : {conv_smem<FEAT, C0, 0, float>(), conv_smem<C0, C1, 0, float>(), conv_smem<C1, C2, 0, float>(),
                           conv_smem<C2, C3, 0, float>(), conv_smem<C3, C2, 0, float>(), conv_smem<C2, C1, 0, float>(),
                           conv_smem<C1, C0, 0, float>(), conv_smem<C0, 8, 1, float>(), conv_smem<FEAT, C0, 0, double>(),
@@ -413,32 +607,33 @@ cudaError_t conv_smem_all() {
 unsigned grid_for(int64_t work) { return (unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16); }
 
 template <typename FT>
-int apply(LearnedNet* net, const FT* r, FT* z, const int* kbot, cudaStream_t st) {
+int apply(LearnedNet* net, const FT* r, FT* z, const int* kbot, cudaStream_t st, unsigned* flags) {
     using namespace learned;
     const Dims* d = net->d;
     k_rms<FT><<<grid_for(d[0].n()), 256, 0, st>>>(r, d[0].n(), net->acc, net->cnt, net->scale);
     k_rms<FT><<<grid_for(d[0].n()), 256, 0, st>>>(z, d[0].n(), net->acc, net->cnt, net->scale + 1);
     k_features<FT><<<grid_for(d[0].n()), 256, 0, st>>>(r, z, kbot, d[0], net->scale, net->scale + 1, net->f0);
-    conv<FEAT, C0, 0, FT>(net, L_ENC0, 0, net->f0, net->e0, nullptr, st);
+    conv<FEAT, C0, 0, FT>(net, L_ENC0, 0, net->f0, net->e0, nullptr, st, flags);
     k_pool<C0><<<grid_for(d[1].n() * C0 / 8), 256, 0, st>>>(net->e0, d[0], net->p1);
-    conv<C0, C1, 0, FT>(net, L_ENC1, 1, net->p1, net->e1, nullptr, st);
+    conv<C0, C1, 0, FT>(net, L_ENC1, 1, net->p1, net->e1, nullptr, st, flags);
     k_pool<C1><<<grid_for(d[2].n() * C1 / 8), 256, 0, st>>>(net->e1, d[1], net->p2);
-    conv<C1, C2, 0, FT>(net, L_ENC2, 2, net->p2, net->e2, nullptr, st);
+    conv<C1, C2, 0, FT>(net, L_ENC2, 2, net->p2, net->e2, nullptr, st, flags);
     k_pool<C2><<<grid_for(d[3].n() * C2 / 8), 256, 0, st>>>(net->e2, d[2], net->p3);
-    conv<C2, C3, 0, FT>(net, L_ENC3, 3, net->p3, net->e3, nullptr, st);
-    conv<C3, C2, 0, FT>(net, L_DEC3, 3, net->e3, net->d3, nullptr, st);
+    conv<C2, C3, 0, FT>(net, L_ENC3, 3, net->p3, net->e3, nullptr, st, flags);
+    conv<C3, C2, 0, FT>(net, L_DEC3, 3, net->e3, net->d3, nullptr, st, flags);
     k_upadd<C2><<<grid_for(d[2].n() * C2 / 8), 256, 0, st>>>(net->d3, net->e2, d[2], net->d2in);
-    conv<C2, C1, 0, FT>(net, L_DEC2, 2, net->d2in, net->d2, nullptr, st);
+    conv<C2, C1, 0, FT>(net, L_DEC2, 2, net->d2in, net->d2, nullptr, st, flags);
     k_upadd<C1><<<grid_for(d[1].n() * C1 / 8), 256, 0, st>>>(net->d2, net->e1, d[1], net->d1in);
-    conv<C1, C0, 0, FT>(net, L_DEC1, 1, net->d1in, net->d1, nullptr, st);
+    conv<C1, C0, 0, FT>(net, L_DEC1, 1, net->d1in, net->d1, nullptr, st, flags);
     k_upadd<C0><<<grid_for(d[0].n() * C0 / 8), 256, 0, st>>>(net->d1, net->e0, d[0], net->d0in);
-    conv<C0, 8, 1, FT>(net, L_OUT, 0, net->d0in, nullptr, z, st);
+    conv<C0, 8, 1, FT>(net, L_OUT, 0, net->d0in, nullptr, z, st, flags);
     return 17;
 }
 
 }  // namespace
 
-int learned_apply(LearnedNet* net, const void* r, void* z, const int* kbot, int fp64, cudaStream_t stream) {
-    if (fp64) return apply<double>(net, static_cast<const double*>(r), static_cast<double*>(z), kbot, stream);
-    return apply<float>(net, static_cast<const float*>(r), static_cast<float*>(z), kbot, stream);
+int learned_apply(LearnedNet* net, const void* r, void* z, const int* kbot, int fp64, cudaStream_t stream,
+                  unsigned* flags) {
+    if (fp64) return apply<double>(net, static_cast<const double*>(r), static_cast<double*>(z), kbot, stream, flags);
+    return apply<float>(net, static_cast<const float*>(r), static_cast<float*>(z), kbot, stream, flags);
 }

@@ -72,4 +72,6 @@ void learned_destroy(LearnedNet* net);
 // synchronisation).  r, z are FT (float or double, `fp64` selects) interior fields;
 // kbot the immersed-bottom table (nullptr: every cell active).  Returns the kernels
 // launched.
-int learned_apply(LearnedNet* net, const void* r, void* z, const int* kbot, int fp64, cudaStream_t stream);
+// flags: the model's device flag word (GBO_FLAG_TIMEOUT when a tensor-core wait gave up).
+int learned_apply(LearnedNet* net, const void* r, void* z, const int* kbot, int fp64, cudaStream_t stream,
+                  unsigned* flags);

@@ -892,7 +892,7 @@ struct ModelImpl : gbo_model {
     void learned_correction(const FT* r, FT* z) {
         if (!net) return;
         pre(G_LEARNED);
-        const int nk = learned_apply(net, r, z, gp.kbot, sizeof(FT) == 8, stream);
+        const int nk = learned_apply(net, r, z, gp.kbot, sizeof(FT) == 8, stream, d_flags);
         check_launch();
         launches += nk - 1;
     }

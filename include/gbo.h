@@ -285,6 +285,34 @@ int gbo_poisson_operator_device(gbo_model* m, const void* x_device, void* out_de
 /* z = M r with the model's CG preconditioner (including a loaded learned correction). */
 int gbo_precondition_device(gbo_model* m, const void* r_device, void* z_device);
 
+/* ---- training the learned correction on the GPU ----------------------------------
+ * No counterpart in the reference.  A trainer holds the network for an Nx × Ny × Nz
+ * grid (divisible by 8) with FP32 master weights (initial values from `weights`, the
+ * layout of gbo_learned_preconditioner) and Adam moments, and trains it with the
+ * library's own kernels: the forward and data-gradient convolutions on the
+ * fifth-generation tensor cores (tcgen05, BF16 operands, FP32 accumulation in TMEM),
+ * weight gradients on BF16 tensor-core MMAs with FP32 accumulation, pooling /
+ * up-sampling / ReLU backward passes, the loss and Adam.  One sample is a residual r,
+ * its FFT-preconditioned z_fft and the error e = A⁻¹ r (the exact correction is
+ * e - z_fft), with the active-cell mask `active` (1 or 0): device arrays of Nx*Ny*Nz
+ * FP32 values, x fastest.  The loss is Σ d² / Σ t_c² with t = (e - z_fft) / s_z,
+ * d = (net - t)·active and t_c = t·active, each less its active-cell mean.
+ *   gbo_learned_trainer_gradients: the loss and d(loss)/d(weights) (host, same layout)
+ *     of one sample, without updating;
+ *   gbo_learned_trainer_step: one Adam step (β1 = 0.9, β2 = 0.999, ε = 1e-8) on one sample;
+ *   gbo_learned_trainer_weights: the current FP32 weights (host). */
+typedef struct gbo_learned_trainer gbo_learned_trainer;
+int gbo_learned_trainer_create(int32_t nx, int32_t ny, int32_t nz, const float* weights, int64_t count,
+                               gbo_learned_trainer** out);
+void gbo_learned_trainer_destroy(gbo_learned_trainer* t);
+int gbo_learned_trainer_gradients(gbo_learned_trainer* t, const float* r_device, const float* z_device,
+                                  const float* e_device, const float* active_device, double* loss, float* grad);
+int gbo_learned_trainer_step(gbo_learned_trainer* t, const float* r_device, const float* z_device,
+                             const float* e_device, const float* active_device, double lr, double* loss);
+int gbo_learned_trainer_weights(gbo_learned_trainer* t, float* weights);
+/* The cudaStream_t (as void*) the trainer's work is issued on. */
+int gbo_learned_trainer_stream(gbo_learned_trainer* t, void** stream);
+
 /* ---- ensembles ---------------------------------------------------------------
  * No counterpart in the reference, which advances models one at a time.  An
  * ensemble owns n independent models (each created as by gbo_model_create from

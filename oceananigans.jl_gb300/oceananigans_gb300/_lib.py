@@ -113,6 +113,15 @@ SIGNATURES = {
     "gbo_poisson_solve_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "gbo_learned_weight_count": (ctypes.c_int64, []),
     "gbo_learned_preconditioner": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int64]),
+    "gbo_learned_trainer_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.POINTER(ctypes.c_float), ctypes.c_int64, ctypes.POINTER(_vp)]),
+    "gbo_learned_trainer_destroy": (None, [_vp]),
+    "gbo_learned_trainer_gradients": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double),
+                                                     ctypes.POINTER(ctypes.c_float)]),
+    "gbo_learned_trainer_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_double,
+                                                ctypes.POINTER(ctypes.c_double)]),
+    "gbo_learned_trainer_weights": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "gbo_learned_trainer_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "gbo_poisson_operator_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "gbo_precondition_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "gbo_state_bytes": (ctypes.c_int64, [_vp]),

@@ -5,7 +5,7 @@ BF16 tensor-core convolutions); this module only produces its weights, offline, 
 PyTorch: it runs a model with the CG solver, records pairs (b = V∇²x, x) from the
 pressure of every step (exact pairs of the model's own operator), applies the model's
 FFT preconditioner to each b, and fits the U-Net to the part of A⁻¹b the FFT solve
-misses.  The network and the weight-file layout are those of gbo_learned.cuh:
+misses -- on the GPU, with the library's own training kernels (GpuTrainer).  The network and the weight-file layout are those of gbo_learned.cuh:
 
     z = z_fft + s_z · net(r / s_r, z_fft / s_z, active),   s_r = RMS(r), s_z = RMS(z_fft)
 
@@ -13,7 +13,8 @@ misses.  The network and the weight-file layout are those of gbo_learned.cuh:
     up + enc2, dec2 48→32, up + enc1, dec1 32→16, up + enc0, out 16→1
     (3³ kernels, ReLU after every layer but the last, x / y periodic, z zero padded)
 
-PyTorch is needed only here; importing the package does not import it.
+PyTorch (device arrays and the CG iterations that generate the samples) is needed only
+here; importing the package does not import it.
 """
 import ctypes
 
@@ -30,76 +31,79 @@ def _torch():
     return torch
 
 
-def make_net(seed=0):
-    torch = _torch()
-    F = torch.nn.functional
-
-    class UNet(torch.nn.Module):
-        def __init__(self):
-            super().__init__()
-            torch.manual_seed(seed)
-            self.convs = torch.nn.ModuleList([torch.nn.Conv3d(ci, co, 3, padding=0) for _, ci, co in LAYERS])
-            with torch.no_grad():  # start as a small correction
-                self.convs[-1].weight.mul_(0.01)
-                self.convs[-1].bias.zero_()
-
-        @staticmethod
-        def pad(x):  # (N, C, z, y, x): periodic in x and y, zeros in z
-            x = F.pad(x, (1, 1, 1, 1, 0, 0), mode="circular")
-            return F.pad(x, (0, 0, 0, 0, 1, 1))
-
-        def conv(self, i, x, relu=True):
-            y = self.convs[i](self.pad(x))
-            return F.relu(y) if relu else y
-
-        def forward(self, f):
-            up = lambda t: t.repeat_interleave(2, 2).repeat_interleave(2, 3).repeat_interleave(2, 4)  # noqa: E731
-            e0 = self.conv(0, f)
-            e1 = self.conv(1, F.avg_pool3d(e0, 2))
-            e2 = self.conv(2, F.avg_pool3d(e1, 2))
-            e3 = self.conv(3, F.avg_pool3d(e2, 2))
-            d3 = self.conv(4, e3)
-            d2 = self.conv(5, up(d3) + e2)
-            d1 = self.conv(6, up(d2) + e1)
-            return self.conv(7, up(d1) + e0, relu=False)
-
-    return UNet()
-
-
-def export_weights(net):
-    """The weight file: per layer W[cout][cin][3][3][3] then bias, FP32."""
+def initial_weights(seed=0, out_scale=0.01):
+    """A weight file of fresh weights: W, b ~ U[-1/√fan_in, 1/√fan_in] per layer (fan_in =
+    27 cin, the default of a 3-D convolution), the output layer's weights scaled by
+    `out_scale` and its bias zero so that training starts from a small correction."""
+    rng = np.random.default_rng(seed)
     parts = []
-    for c in net.convs:
-        parts.append(c.weight.detach().float().cpu().numpy().ravel())
-        parts.append(c.bias.detach().float().cpu().numpy().ravel())
-    flat = np.concatenate(parts).astype(np.float32)
-    assert flat.size == L.load().gbo_learned_weight_count()
-    return flat
+    for i, (_, ci, co) in enumerate(LAYERS):
+        bound = 1.0 / np.sqrt(27 * ci)
+        w = rng.uniform(-bound, bound, co * ci * 27)
+        b = rng.uniform(-bound, bound, co)
+        if i == len(LAYERS) - 1:
+            w, b = w * out_scale, np.zeros(co)
+        parts += [w, b]
+    return np.concatenate(parts).astype(np.float32)
 
 
-def load_weights(net, flat):
-    torch = _torch()
-    at = 0
-    with torch.no_grad():
-        for c in net.convs:
-            for t in (c.weight, c.bias):
-                n = t.numel()
-                t.copy_(torch.from_numpy(np.asarray(flat[at:at + n], dtype=np.float32)).view_as(t))
-                at += n
+class GpuTrainer:
+    """The network trained on the GPU by the library's own kernels (gbo_learned_trainer_*):
+    tcgen05 convolutions forward and for data gradients, tensor-core weight gradients,
+    Adam on FP32 master weights.  Samples are CUDA FP32 tensors (nz, ny, nx): residual r,
+    FFT-preconditioned z, error e = A⁻¹ r and the active mask."""
+
+    def __init__(self, size, weights=None, seed=0):
+        nx, ny, nz = (int(a) for a in size)
+        w = initial_weights(seed) if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+        lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(lib.gbo_learned_trainer_create(nx, ny, nz, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), w.size,
+                                               ctypes.byref(h)))
+        self._h, self.count = h, w.size
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.load().gbo_learned_trainer_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _ptrs(*ts):
+        for t in ts:
+            if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float32"):
+                raise ValueError("trainer samples are contiguous CUDA float32 tensors")
+        return [ctypes.c_void_p(t.data_ptr()) for t in ts]
+
+    def stream(self):
+        sp = ctypes.c_void_p()
+        L.check(L.load().gbo_learned_trainer_stream(self._h, ctypes.byref(sp)))
+        return sp.value
+
+    def gradients(self, r, z, e, active):
+        """(loss, gradient in the weight-file layout) of one sample; no update."""
+        g = np.zeros(self.count, dtype=np.float32)
+        loss = ctypes.c_double()
+        L.check(L.load().gbo_learned_trainer_gradients(self._h, *self._ptrs(r, z, e, active), ctypes.byref(loss),
+                                                       g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return loss.value, g
+
+    def step(self, r, z, e, active, lr):
+        """One Adam step on one sample; returns the sample's loss before the step."""
+        loss = ctypes.c_double()
+        L.check(L.load().gbo_learned_trainer_step(self._h, *self._ptrs(r, z, e, active), float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def weights(self):
+        w = np.zeros(self.count, dtype=np.float32)
+        L.check(L.load().gbo_learned_trainer_weights(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return w
 
 
 def _rms(a):
     torch = _torch()
     s = torch.sqrt(torch.mean(a.double() ** 2)).float()
     return torch.where(s > 0, s, torch.ones_like(s))
-
-
-def features(r, z, active):
-    """(1, 3, z, y, x) network input for a residual r and its FFT-preconditioned z
-    (fields (z, y, x)), and the output scale s_z."""
-    torch = _torch()
-    sr, sz = _rms(r), _rms(z)
-    return torch.stack([r / sr, z / sz, active], dim=0)[None], sz
 
 
 def _active_mean_free(a, active):
@@ -166,30 +170,21 @@ def collect_pairs(model, dt, steps, every=1, cg_iterations=0):
     return torch.stack(rs), torch.stack(zs), torch.stack(es), active
 
 
-def train(b, z, x, active, epochs=20, lr=1e-3, seed=0, log=None):
+def train(r, z, e, active, epochs=20, lr=1e-3, seed=0, log=None, weights=None):
     """Fit net(r/s_r, z/s_z, active) to (e - z)/s_z over active cells, up to a constant
-    (the Neumann problem's null space), for triples (r = b, z, e = x) as collect_pairs
-    returns them.  Returns the network."""
+    (the Neumann problem's null space), for samples (r, z_fft, e) as collect_pairs returns
+    them, on the GPU with the library's own kernels (GpuTrainer: tcgen05 convolutions,
+    tensor-core weight gradients, Adam).  Starts from `weights` (a weight file) or from
+    initial_weights(seed).  Returns the trained weight file (FP32)."""
     torch = _torch()
-    net = make_net(seed).cuda()
-    opt = torch.optim.Adam(net.parameters(), lr=lr)
-    n = b.shape[0]
-    na = active.sum()
+    n, nz, ny, nx = r.shape
+    tr = GpuTrainer((nx, ny, nz), weights, seed)
+    act = active.float().contiguous()
     gen = torch.Generator().manual_seed(seed)
     for ep in range(epochs):
         total = 0.0
         for i in torch.randperm(n, generator=gen).tolist():
-            f, s = features(b[i], z[i], active)
-            t = (x[i] - z[i]) / s
-            y = net(f)[0, 0]
-            d = (y - t) * active
-            d = d - (d.sum() / na) * active  # constant offsets are free
-            tc = (t - (t * active).sum() / na) * active
-            loss = (d * d).sum() / (tc * tc).sum().clamp_min(1e-30)
-            opt.zero_grad()
-            loss.backward()
-            opt.step()
-            total += float(loss.detach())
+            total += tr.step(r[i].contiguous(), z[i].contiguous(), e[i].contiguous(), act, lr)
         if log:
             log("epoch %d: mean relative loss %.4e" % (ep, total / n))
-    return net
+    return tr.weights()

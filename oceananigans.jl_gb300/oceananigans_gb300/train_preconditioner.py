@@ -7,7 +7,8 @@ ConjugateGradientPoissonSolver(reltol=1e-8) in FP32):
 1. spin-up with the FFT-preconditioned CG, recording a pair (b = V∇²x, x = pNHS) per
    step (exact pairs of the model's own operator) and the residuals of a few
    FFT-preconditioned CG iterations on each b with their errors (learned.collect_pairs);
-2. fit the U-Net (learned.train, PyTorch) and save the weight file (numpy .npy, FP32);
+2. fit the U-Net on the GPU with the library's own kernels (learned.train: tcgen05
+   convolutions, tensor-core weight gradients, Adam) and save the weight file (numpy .npy, FP32);
 3. held-out comparison: the right-hand sides of later steps solved from a zero initial
    guess with FFT-PCG and with the learned flexible PCG, timed with CUDA events on the
    model's stream.  Prints one JSON line.
@@ -81,9 +82,8 @@ def main(argv=None):
     b, z, x, active = learned.collect_pairs(model, args.dt, args.pairs, cg_iterations=args.cg_iterations)
     log("collected %d triples in %.1f s" % (b.shape[0], time.time() - t0))
     t0 = time.time()
-    net = learned.train(b, z, x, active, epochs=args.epochs, lr=args.lr, log=log)
-    log("trained in %.1f s" % (time.time() - t0))
-    w = learned.export_weights(net)
+    w = learned.train(b, z, x, active, epochs=args.epochs, lr=args.lr, log=log)
+    log("trained on the GPU in %.1f s" % (time.time() - t0))
     np.save(args.out, w)
     del b, z, x
     hb, _, _, _ = learned.collect_pairs(model, args.dt, args.heldout)

@@ -1,12 +1,70 @@
 """CPU tests of the learned preconditioner correction's restatements: the numpy
 network (the checker of the CUDA inference kernels) against torch.nn.functional.conv3d
-and the training module's PyTorch network, and the weight-file size against the
+and a torch.nn restatement of the same network, and the weight-file size against the
 library.  The network has no counterpart in the reference."""
 import numpy as np
 import pytest
 
 import learned_ref as R
 from oceananigans_gb300 import _lib as L
+
+
+# The network of the numpy restatement written with torch.nn (a second, independent
+# restatement used to pin the numpy one): 3³ convolutions with periodic x / y and zero z
+# padding, average pooling, nearest up-sampling with additive skips.
+def make_net(seed=0):
+    torch = pytest.importorskip("torch")
+    F = torch.nn.functional
+
+    class UNet(torch.nn.Module):
+        def __init__(self):
+            super().__init__()
+            torch.manual_seed(seed)
+            self.convs = torch.nn.ModuleList([torch.nn.Conv3d(ci, co, 3, padding=0) for _, ci, co in R.LAYERS])
+            with torch.no_grad():
+                self.convs[-1].weight.mul_(0.01)
+                self.convs[-1].bias.zero_()
+
+        @staticmethod
+        def pad(x):
+            x = F.pad(x, (1, 1, 1, 1, 0, 0), mode="circular")
+            return F.pad(x, (0, 0, 0, 0, 1, 1))
+
+        def conv(self, i, x, relu=True):
+            y = self.convs[i](self.pad(x))
+            return F.relu(y) if relu else y
+
+        def forward(self, f):
+            up = lambda t: t.repeat_interleave(2, 2).repeat_interleave(2, 3).repeat_interleave(2, 4)  # noqa: E731
+            e0 = self.conv(0, f)
+            e1 = self.conv(1, F.avg_pool3d(e0, 2))
+            e2 = self.conv(2, F.avg_pool3d(e1, 2))
+            e3 = self.conv(3, F.avg_pool3d(e2, 2))
+            d3 = self.conv(4, e3)
+            d2 = self.conv(5, up(d3) + e2)
+            d1 = self.conv(6, up(d2) + e1)
+            return self.conv(7, up(d1) + e0, relu=False)
+
+    return UNet()
+
+
+def export_weights(net):
+    parts = []
+    for c in net.convs:
+        parts.append(c.weight.detach().float().cpu().numpy().ravel())
+        parts.append(c.bias.detach().float().cpu().numpy().ravel())
+    return np.concatenate(parts).astype(np.float32)
+
+
+def load_weights(net, flat):
+    torch = pytest.importorskip("torch")
+    at = 0
+    with torch.no_grad():
+        for c in net.convs:
+            for p in (c.weight, c.bias):
+                n = p.numel()
+                p.copy_(torch.from_numpy(np.asarray(flat[at:at + n], dtype=np.float32)).view_as(p))
+                at += n
 
 
 def test_weight_count_matches_library():
@@ -29,12 +87,11 @@ def test_numpy_convolution_matches_torch_layout():
 
 def test_training_network_matches_numpy_network():
     torch = pytest.importorskip("torch")
-    from oceananigans_gb300 import learned
-    net = learned.make_net(seed=3).double()
-    flat = learned.export_weights(net.float())
+    net = make_net(seed=3).double()
+    flat = export_weights(net.float())
     layers = R.unpack(flat)
     net = net.double()
-    learned.load_weights(net, flat)
+    load_weights(net, flat)
     rng = np.random.default_rng(1)
     feat = rng.standard_normal((16, 16, 24, 3)).astype(np.float32)
     want = R.forward(layers, feat.astype(np.float64), bf16_path=False)
@@ -54,15 +111,14 @@ def test_numpy_gradients_match_torch_autograd():
     # the gradient checker for training kernels: the numpy backward pass of the oracle
     # network against autograd of the training module's network, on the training loss
     torch = pytest.importorskip("torch")
-    from oceananigans_gb300 import learned
-    net = learned.make_net(seed=5)
+    net = make_net(seed=5)
     with torch.no_grad():  # a last layer of ordinary size, so every gradient is O(1)
         net.convs[-1].weight.mul_(100.0)
         net.convs[-1].bias.fill_(0.1)
-    flat = learned.export_weights(net)
+    flat = export_weights(net)
     layers = R.unpack(flat)
     net = net.double()
-    learned.load_weights(net, flat)
+    load_weights(net, flat)
     rng = np.random.default_rng(2)
     nz, ny, nx = 8, 16, 16
     feat = rng.standard_normal((nz, ny, nx, 3))

@@ -65,6 +65,8 @@ enum gbo_precond    { GBO_PRECOND_FFT = 0, GBO_PRECOND_NONE = 1, GBO_PRECOND_LEA
 #define GBO_FIELD_PHY    101      /* hydrostatic pressure anomaly (model.pressures.pHY′) */
 #define GBO_FIELD_NU     102      /* eddy viscosity νₑ (closure_fields.νₑ) */
 #define GBO_FIELD_KAPPA  103      /* AMD tracer diffusivity κₑ of tracer 0 */
+#define GBO_FIELD_JLM    104      /* 𝒥ᴸᴹ of a Lagrangian-averaged DynamicSmagorinsky (closure_fields.𝒥ᴸᴹ) */
+#define GBO_FIELD_JMM    105      /* 𝒥ᴹᴹ of a Lagrangian-averaged DynamicSmagorinsky (closure_fields.𝒥ᴹᴹ) */
 
 #define GBO_MAX_TRACERS 4
 /* Upper bound on conjugate-gradient iterations per pressure solve (the reference's

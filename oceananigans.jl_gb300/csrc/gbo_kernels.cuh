@@ -24,6 +24,8 @@ struct StepP {
     const FT* dtf;                          // stage factors in device memory (Δt overrides dt)
     int first;
     const FT* cs2;                          // DynamicSmagorinsky: c² per level (else null)
+    const FT* jlm; const FT* jmm;           // Lagrangian-averaged DynamicSmagorinsky: 𝒥ᴸᴹ, 𝒥ᴹᴹ per cell (else null)
+    FT lm_min;                              // its minimum_numerator
 };
 
 // ---------------------------------------------------------------------------
@@ -59,7 +61,15 @@ __global__ void k_smagorinsky(StepP<FT> P, FT* __restrict__ nu_out) {
     FT D3 = g.dx * g.dy * M.dzc(k);
     FT Df = cbrt(D3);
     FT cs2;
-    if (P.cs2) {
+    if (P.jlm) {
+        // Lagrangian-averaged DynamicSmagorinsky: the cell's coefficient
+        // max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ, a strong zero where 𝒥ᴹᴹ ≤ 0 (dynamic_coefficient.jl:236-248)
+        const size_t q = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        FT lm = P.jlm[q];
+        lm = isnan(lm) ? lm : (lm > P.lm_min ? lm : P.lm_min);
+        const FT mm = P.jmm[q];
+        cs2 = mm > FT(0) ? lm / mm : FT(0);
+    } else if (P.cs2) {
         // DynamicSmagorinsky: the level's averaged coefficient (k_dyn_coef)
         cs2 = P.cs2[k];
     } else {

@@ -447,6 +447,14 @@ struct ModelImpl : gbo_model {
     // DynamicSmagorinsky: Σ, Σ̄, per-tile LM/MM sums, and per level c², 𝒥ᴸᴹ, 𝒥ᴹᴹ
     DBuf<FT> dyn_sig, dyn_sigb, dyn_cs2, dyn_jlm, dyn_jmm;
     DBuf<double> dyn_part;
+    // DynamicSmagorinsky with LagrangianAveraging: 𝒥ᴸᴹ, 𝒥ᴹᴹ and their previous values, the
+    // FP64 clock slots (LAG_*), the cell-centre z, and where the step being recorded reads
+    // its FP64 Δt (the plain step's slot, or the simulation loop's)
+    bool lagrangian = false, velocities_set = false, stretched_z = false;
+    DBuf<FT> lag_jlm, lag_jmm, lag_jlm_prev, lag_jmm_prev;
+    DBuf<double> lag_s, lag_zc;
+    const double* lag_dtp = nullptr;
+    double lag_x0 = 0, lag_y0 = 0;
     // grid tables
     DBuf<FT> t_dzc, t_dzf, t_rdzc, t_rdzf, t_rvc;
     DBuf<double> t_rdzf64, t_dzc64, t_lx64, t_ly64, t_ws;
@@ -519,6 +527,11 @@ struct ModelImpl : gbo_model {
         tmean.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_ws.free_(); t_kbot.free_();
         for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
+        for (DBuf<FT>* b : {&dyn_sig, &dyn_sigb, &dyn_cs2, &dyn_jlm, &dyn_jmm, &lag_jlm, &lag_jmm, &lag_jlm_prev, &lag_jmm_prev})
+            b->free_();
+        dyn_part.free_();
+        lag_s.free_();
+        lag_zc.free_();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (d_flags) cudaFree(d_flags);
@@ -544,6 +557,7 @@ struct ModelImpl : gbo_model {
         // grid tables
         const int H = gd->bottom_height ? 4 : 3;
         Z = make_zgrid<FT>(Nz, H, flat, gd->z_faces, gd->z[0], gd->z[1]);
+        stretched_z = gd->z_faces != nullptr;
         std::vector<FT> rdzc(Z.dzc.size()), rdzf(Z.dzf.size());
         std::vector<double> rdzf64(Z.dzf.size()), dzc64(Z.dzc.size());
         for (size_t q = 0; q < Z.dzc.size(); ++q) {
@@ -610,8 +624,27 @@ struct ModelImpl : gbo_model {
         if (md->closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
             dyn_sig.alloc(N);
             dyn_sigb.alloc(N);
-            dyn_part.alloc((size_t)2 * Nz * ((Nx + dyn::TX - 1) / dyn::TX) * ((Ny + dyn::TY - 1) / dyn::TY));
+            dyn_part.alloc(std::max<size_t>((size_t)2 * Nz * ((Nx + dyn::TX - 1) / dyn::TX) * ((Ny + dyn::TY - 1) / dyn::TY),
+                                            (size_t)2 * LAG_SUM_BLOCKS));
             for (DBuf<FT>* b : {&dyn_cs2, &dyn_jlm, &dyn_jmm}) b->alloc(Nz);
+            lagrangian = md->closure_averaging == GBO_AVERAGING_LAGRANGIAN;
+        }
+        if (lagrangian) {
+            for (DBuf<FT>* b : {&lag_jlm, &lag_jmm, &lag_jlm_prev, &lag_jmm_prev}) b->alloc(N);
+            std::vector<double> zc(Nz);
+            for (int k = 0; k < Nz; ++k) zc[k] = (double)Z.at(Z.zc, k + 1);
+            lag_zc.upload(zc);
+            lag_x0 = gd->x[0];
+            lag_y0 = gd->y[0];
+            // the constructor's initialize_closure_fields! sees zero velocities (LM = MM = 0):
+            // 𝒥ᴸᴹ = max(0, minimum_numerator), 𝒥ᴹᴹ = 0, previous_compute_time = 0
+            std::vector<double> s0(LAG_NSLOTS, 0.0);
+            const FT lmin = FT(md->closure_min_numerator);
+            s0[LAG_LM0] = (double)(lmin > FT(0) ? lmin : FT(0));
+            lag_s.upload(s0);
+            k_lag_fill<FT><<<conv_blocks(), 256, 0, stream>>>(lag_s.p, lag_jlm.p, lag_jmm.p, N);
+            GBO_CUDA(cudaGetLastError());
+            lag_dtp = lag_s.p + LAG_DT;
         }
         if (scalar) {
             kap.resize(ntr);
@@ -1043,6 +1076,90 @@ struct ModelImpl : gbo_model {
         return GBO_OK;
     }
 
+    CFld<FT> host_cfld(const FT* a) const { return CFld<FT>{a, Nx, Ny, Nz, flat ? 1 : 0, nullptr}; }
+    WFld<FT> host_wfld(const FT* a) const { return WFld<FT>{a, Nx, Ny, Nz}; }
+    // the velocities with interior u, v, w and halos from hu, hv, hw
+    LagVel<FT> lag_vel(const FT* hu, const FT* hv, const FT* hw) const {
+        return LagVel<FT>{{host_cfld(u.p), host_cfld(hu)}, {host_cfld(v.p), host_cfld(hv)}, {host_wfld(w.p), host_wfld(hw)}};
+    }
+    dim3 dyn_grid() const { return dim3((Nx + dyn::TX - 1) / dyn::TX, (Ny + dyn::TY - 1) / dyn::TY, Nz); }
+
+    // initialize_closure_fields! (dynamic_coefficient.jl:407-437): Σ, Σ̄, LM and MM of the
+    // velocities (interior u, v, w; halos from hu, hv, hw) into 𝒥ᴸᴹ, 𝒥ᴹᴹ, then both = their
+    // domain means everywhere and previous_compute_time = clock.time
+    void lag_initialize(const FT* hu, const FT* hv, const FT* hw) {
+        const LagVel<FT> V = lag_vel(hu, hv, hw);
+        const dim3 dg = dyn_grid(), db(dyn::TX, dyn::TY);
+        pre(G_CLOSURE);
+        dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
+        check_launch();
+        pre(G_CLOSURE);
+        dyn_launch_lag_lm<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
+        check_launch();
+        const int nparts = LAG_SUM_BLOCKS;
+        pre(G_CLOSURE);
+        k_lag_sum<FT><<<nparts, 256, 0, stream>>>(lag_jlm.p, lag_jmm.p, N, dyn_part.p);
+        check_launch();
+        pre(G_CLOSURE);
+        k_lag_init_mean<FT><<<1, dyn::COEF_THREADS, 0, stream>>>(dyn_part.p, nparts, (double)N,
+                                                                 desc.closure_min_numerator, time, lag_s.p);
+        check_launch();
+        pre(G_CLOSURE);
+        k_lag_fill<FT><<<conv_blocks(), 256, 0, stream>>>(lag_s.p, lag_jlm.p, lag_jmm.p, N);
+        check_launch();
+    }
+
+    // step_closure_prognostics! (dynamic_coefficient.jl:439-484) after the step's last
+    // projection: the projected interior with the predictor's halos, 𝒥⁻ = 𝒥, one
+    // Lagrangian update over Δt = clock.time - previous_compute_time, then the clock
+    void lag_step() {
+        const LagVel<FT> V = lag_vel(us.p, vs.p, ws.p);
+        const dim3 dg = dyn_grid(), db(dyn::TX, dyn::TY);
+        pre(G_CLOSURE);
+        dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
+        check_launch();
+        const unsigned cb = (unsigned)std::min<size_t>((N * sizeof(FT) / 16 + 255) / 256 + 1, 4 * 152 * 8);
+        pre(G_COPY);
+        k_copy<FT><<<cb, 256, 0, stream>>>(lag_jlm.p, lag_jlm_prev.p, N);
+        check_launch();
+        pre(G_COPY);
+        k_copy<FT><<<cb, 256, 0, stream>>>(lag_jmm.p, lag_jmm_prev.p, N);
+        check_launch();
+        pre(G_CLOSURE);
+        dyn_launch_lag_lm<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
+        check_launch();
+        LagP<FT> L{};
+        L.g = gp;
+        L.vel = V;
+        L.jlm_prev = lag_jlm_prev.p;
+        L.jmm_prev = lag_jmm_prev.p;
+        L.jlm = lag_jlm.p;
+        L.jmm = lag_jmm.p;
+        L.lm_min = FT(desc.closure_min_numerator);
+        L.x0 = lag_x0;
+        L.y0 = lag_y0;
+        L.dx = (grid.x[1] - grid.x[0]) / Nx;
+        L.dy = (grid.y[1] - grid.y[0]) / Ny;
+        L.zc = lag_zc.p;
+        L.dz1 = (double)Z.at(Z.dzc, 1);
+        L.stretched = stretched_z ? 1 : 0;
+        L.clock = lag_s.p;
+        L.dtp = lag_dtp;
+        pre(G_CLOSURE);
+        k_lag_step<FT><<<dg, db, 0, stream>>>(L);
+        check_launch();
+        pre(G_CLOSURE);
+        k_lag_tick<<<1, 1, 0, stream>>>(lag_s.p, lag_dtp);
+        check_launch();
+    }
+    // Δt (FP64) of the next plain steps, and the clock the updates start from
+    void lag_set_dt(double dt) {
+        if (!lagrangian) return;
+        pre(G_SIM);
+        k_lag_set_dt<<<1, 1, 0, stream>>>(lag_s.p, dt, time);
+        check_launch();
+    }
+
     // Closure fields and the hydrostatic pressure anomaly of the current state: the part
     // of update_state! (update_nonhydrostatic_model_state.jl:64-83) that the next stage's
     // tendencies read.  Run after every projection, as the reference does.
@@ -1059,15 +1176,25 @@ struct ModelImpl : gbo_model {
             pre(G_CLOSURE);
             k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemS<FT>), stream>>>(P, nu.p);
             check_launch();
+        } else if (lagrangian) {
+            // νₑ from the cell's own coefficient max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ
+            StepP<FT> Q = P;
+            Q.jlm = lag_jlm.p;
+            Q.jmm = lag_jmm.p;
+            Q.lm_min = FT(desc.closure_min_numerator);
+            pre(G_CLOSURE);
+            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p);
+            check_launch();
         } else if (desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
             // Σ and Σ̄, the tile sums of LM and MM, the per-level coefficient, then νₑ
             // (compute_coefficient_fields!, dynamic_coefficient.jl:225-250; smagorinsky.jl:90-104)
             const dim3 dg((Nx + dyn::TX - 1) / dyn::TX, (Ny + dyn::TY - 1) / dyn::TY, Nz), db(dyn::TX, dyn::TY);
             pre(G_CLOSURE);
-            k_dyn_sigma<FT><<<dg, db, 0, stream>>>(P, dyn_sig.p, dyn_sigb.p);
+            const PlainVel<FT> V{host_cfld(u.p), host_cfld(v.p), host_wfld(w.p)};
+            dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
             check_launch();
             pre(G_CLOSURE);
-            k_dyn_lm<FT><<<dg, db, 0, stream>>>(P, dyn_sig.p, dyn_sigb.p, dyn_part.p);
+            dyn_launch_lm_sums<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, dyn_part.p);
             check_launch();
             pre(G_CLOSURE);
             k_dyn_coef<FT><<<Nz, dyn::COEF_THREADS, 0, stream>>>(dyn_part.p, (int)(dg.x * dg.y), (double)Nx * (double)Ny,
@@ -1104,7 +1231,7 @@ struct ModelImpl : gbo_model {
 
     // One RK3 stage: Gⁿ from the current state, predictor, projection.  Δt is read
     // on the device from the stage factors at dtf, so a captured step serves every Δt.
-    void stage(const FT* dtf, int s, double gamma, double zeta, bool first) {
+    void stage(const FT* dtf, int s, double gamma, double zeta, bool first, bool last) {
         StepP<FT> P = params();
         P.dt = FT(0);
         P.dtf = dtf;
@@ -1160,6 +1287,9 @@ struct ModelImpl : gbo_model {
             check_launch();
         }
         mask_tracers();
+        // the Lagrangian average steps once per time step, after its last projection and
+        // before update_state! (runge_kutta_3.jl:163; quasi_adams_bashforth_2.jl:117)
+        if (lagrangian && last) lag_step();
         auxiliaries();
     }
 
@@ -1182,13 +1312,13 @@ struct ModelImpl : gbo_model {
         if (qab2) {
             const FT chi = FT(desc.ab2_chi);
             const FT alpha = FT(1.5) + chi, beta = FT(0.5) + chi;
-            if (euler) stage(dtf, 0, 1.0, 0.0, true);
-            else stage(dtf, 0, (double)alpha, -(double)beta, false);
+            if (euler) stage(dtf, 0, 1.0, 0.0, true, true);
+            else stage(dtf, 0, (double)alpha, -(double)beta, false, true);
             return;
         }
-        stage(dtf, 0, K::rk3_gamma1, 0.0, true);
-        stage(dtf, 1, K::rk3_gamma2, K::rk3_zeta2, false);
-        stage(dtf, 2, K::rk3_gamma3, K::rk3_zeta3, false);
+        stage(dtf, 0, K::rk3_gamma1, 0.0, true, false);
+        stage(dtf, 1, K::rk3_gamma2, K::rk3_zeta2, false, false);
+        stage(dtf, 2, K::rk3_gamma3, K::rk3_zeta3, false, true);
     }
     // c of Δτ = FT(Δt c) per stage: γ₁, and γ + ζ summed in FT (runge_kutta_3.jl:186-187)
     static StageC rk3_stage_c() {
@@ -1219,6 +1349,7 @@ struct ModelImpl : gbo_model {
         cudaGraphExec_t exec = nullptr;
         GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         int64_t before = launches;
+        if (lagrangian) lag_dtp = lag_s.p + LAG_DT;
         try {
             full_step(dtf.p, euler);
         } catch (...) {
@@ -1248,6 +1379,7 @@ struct ModelImpl : gbo_model {
         if (nsteps <= 0) return GBO_OK;
         cg_status = GBO_OK;
         set_dt(dt, stream);
+        lag_set_dt(dt);
         if (use_graph) {
             if (!graph) graph = capture_graph(false);
             if (qab2 && !graph_euler) graph_euler = capture_graph(true);
@@ -1314,6 +1446,7 @@ struct ModelImpl : gbo_model {
         timing = true;
         try {
             set_dt(dt, stream);
+            lag_set_dt(dt);
             for (int s = 0; s < nsteps; ++s) {
                 full_step(dtf.p, euler_step(dt));
                 last_dt = dt;
@@ -1352,6 +1485,8 @@ struct ModelImpl : gbo_model {
         if (field == GBO_FIELD_PHY) return has_phy ? phy.p : nullptr;
         if (field == GBO_FIELD_NU) return nu.p;
         if (field == GBO_FIELD_KAPPA) return kap.empty() ? nullptr : kap[0].p;
+        if (field == GBO_FIELD_JLM) return lagrangian ? lag_jlm.p : nullptr;
+        if (field == GBO_FIELD_JMM) return lagrangian ? lag_jmm.p : nullptr;
         return nullptr;
     }
 
@@ -1417,6 +1552,7 @@ struct ModelImpl : gbo_model {
         }
         if (field == GBO_FIELD_W)  // impenetrable walls: the bottom face is zero (set! + fill_halo_regions!)
             GBO_CUDA(cudaMemsetAsync(d, 0, (size_t)Nx * Ny * sizeof(FT), stream));
+        if (field == GBO_FIELD_U || field == GBO_FIELD_V || field == GBO_FIELD_W) velocities_set = true;
         GBO_CUDA(cudaStreamSynchronize(stream));
         return GBO_OK;
     }
@@ -1481,13 +1617,31 @@ struct ModelImpl : gbo_model {
     int set_finalize(int enforce) override {
         // set_nonhydrostatic_model.jl:59-73: mask tracers and velocities, then project
         cg_status = GBO_OK;
+        const bool init = lagrangian && velocities_set;  // velocities_are_set && initialize_closure_fields!
+        velocities_set = false;
         mask_tracers();
         if (ibg) {
             pre(G_MASK);
             k_mask<FT><<<grd(), blk(), 0, stream>>>(gp, u.p, v.p, flat ? nullptr : w.p, nullptr, flat ? 3 : 7);
             check_launch();
         }
-        if (enforce) project(u.p, v.p, flat ? nullptr : w.p, 1.0);
+        if (init) lag_initialize(u.p, v.p, w.p);
+        if (enforce && init) {
+            // the projection corrects the interior after the halos were filled from the set
+            // values; the second initialization sees both, so keep the set values
+            const unsigned cb = (unsigned)std::min<size_t>((N * sizeof(FT) / 16 + 255) / 256 + 1, 4 * 152 * 8);
+            FT* const from[3] = {u.p, v.p, w.p};
+            FT* const to[3] = {us.p, vs.p, ws.p};
+            for (int q = 0; q < 3; ++q) {
+                pre(G_COPY);
+                k_copy<FT><<<cb, 256, 0, stream>>>(from[q], to[q], N);
+                check_launch();
+            }
+            project(us.p, vs.p, ws.p, 1.0);
+            lag_initialize(us.p, vs.p, ws.p);
+        } else if (enforce) {
+            project(u.p, v.p, flat ? nullptr : w.p, 1.0);
+        }
         auxiliaries();
         int rc = sync();
         return rc != GBO_OK ? rc : cg_status;
@@ -1512,7 +1666,9 @@ struct ModelImpl : gbo_model {
     // ---- prognostic state (prognostic_state / restore_prognostic_state!,
     // nonhydrostatic_model.jl:354-377): clock, velocities, tracers and pNHS (the CG
     // initial guess).  RK3 keeps no tendency history across steps (ζ₁ = 0), and the
-    // closure fields and pHY′ are recomputed from the restored state.
+    // closure fields and pHY′ are recomputed from the restored state, except the
+    // Lagrangian-averaged 𝒥ᴸᴹ, 𝒥ᴹᴹ and previous_compute_time, which are prognostic
+    // (dynamic_coefficient.jl:524-539).
     struct StateHeader {
         uint64_t magic;
         int32_t version, dtype, Nx, Ny, Nz, ntr, timestepper;
@@ -1534,14 +1690,20 @@ struct ModelImpl : gbo_model {
             if (!flat) f.push_back(Gw.p);
             for (int n = 0; n < ntr; ++n) f.push_back(Gc[n].p);
         }
+        if (lagrangian) {
+            f.push_back(lag_jlm.p);
+            f.push_back(lag_jmm.p);
+        }
         return f;
     }
     // after the fields: the tracers' reference profiles (Nz values each) when tracers are
     // stored as departures
     int64_t profile_bytes() const { return departures ? (int64_t)ntr * Nz * (int64_t)sizeof(FT) : 0; }
+    // then previous_compute_time (FP64) of a Lagrangian average
+    int64_t lag_bytes() const { return lagrangian ? (int64_t)sizeof(double) : 0; }
     int64_t state_bytes() const override {
         return (int64_t)sizeof(StateHeader) + (int64_t)state_fields().size() * (int64_t)N * (int64_t)sizeof(FT) +
-               profile_bytes();
+               profile_bytes() + lag_bytes();
     }
     int get_state(void* buf, int64_t bytes) override {
         if (bytes != state_bytes()) { err = "state buffer size does not match gbo_state_bytes"; return GBO_ERR_INVALID; }
@@ -1556,6 +1718,7 @@ struct ModelImpl : gbo_model {
             GBO_CUDA(cudaMemcpyAsync(at, cref[n].p, Nz * sizeof(FT), cudaMemcpyDeviceToHost, stream));
             at += Nz * sizeof(FT);
         }
+        if (lagrangian) GBO_CUDA(cudaMemcpyAsync(at, lag_s.p + LAG_PREV, sizeof(double), cudaMemcpyDeviceToHost, stream));
         GBO_CUDA(cudaStreamSynchronize(stream));
         return GBO_OK;
     }
@@ -1577,6 +1740,13 @@ struct ModelImpl : gbo_model {
             GBO_CUDA(cudaMemcpyAsync(cref[n].p, at, Nz * sizeof(FT), cudaMemcpyHostToDevice, stream));
             at += Nz * sizeof(FT);
             download_profile(n);
+        }
+        if (lagrangian) {
+            double clk[2];
+            std::memcpy(&clk[1], at, sizeof(double));
+            clk[0] = h.time;  // LAG_TIME, LAG_PREV
+            GBO_CUDA(cudaMemcpyAsync(lag_s.p + LAG_TIME, clk, sizeof clk, cudaMemcpyHostToDevice, stream));
+            GBO_CUDA(cudaStreamSynchronize(stream));
         }
         time = h.time;
         iteration = h.iteration;
@@ -1681,6 +1851,7 @@ struct ModelImpl : gbo_model {
         if (qab2 && !if_stream) GBO_CUDA(cudaStreamCreateWithFlags(&if_stream, cudaStreamNonBlocking));
         const SimP<FT> S = sim_params();
         cudaGraph_t gph;
+        if (lagrangian) lag_dtp = run_s.p + RUN_DT;  // the loop's aligned Δt
         GBO_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         k_sim_start<<<1, 1, 0, stream>>>(run_s.p);
         GBO_CUDA(cudaGetLastError());
@@ -1708,11 +1879,13 @@ struct ModelImpl : gbo_model {
         });
         } catch (...) {
             launches = before;
+            if (lagrangian) lag_dtp = lag_s.p + LAG_DT;
             abort_capture();
             throw;
         }
         run_iter_launches = launches - before - branch;
         launches = before;
+        if (lagrangian) lag_dtp = lag_s.p + LAG_DT;
         GBO_CUDA(cudaStreamEndCapture(stream, &gph));
         GBO_CUDA(cudaGraphInstantiate(&run_graph, gph, 0));
         GBO_CUDA(cudaGraphDestroy(gph));
@@ -1764,6 +1937,7 @@ struct ModelImpl : gbo_model {
             check_launch();
         }
         if (!run_graph) build_run_graph();
+        lag_set_dt(0.0);  // the Lagrangian clock starts from the model's time (Δt comes from the loop)
         const auto t0 = std::chrono::steady_clock::now();
         int64_t steps = 0;
         int reason = GBO_STOP_NONE;
@@ -1885,9 +2059,8 @@ std::string validate(const gbo_grid_desc* g, const gbo_model_desc* d) {
         if (g->topology[2] != GBO_BOUNDED) return "DynamicSmagorinsky requires a three-dimensional grid with Bounded z";
         if (g->bottom_height) return "DynamicSmagorinsky is not available on an ImmersedBoundaryGrid";
         if (!std::isfinite(d->closure_min_numerator)) return "DynamicSmagorinsky minimum_numerator must be finite";
-        if (d->closure_averaging == GBO_AVERAGING_LAGRANGIAN)
-            return "DynamicSmagorinsky with LagrangianAveraging is not available on GB300; use averaging=(1, 2)";
-        if (d->closure_averaging != GBO_AVERAGING_XY) return "unknown DynamicSmagorinsky averaging";
+        if (d->closure_averaging != GBO_AVERAGING_XY && d->closure_averaging != GBO_AVERAGING_LAGRANGIAN)
+            return "unknown DynamicSmagorinsky averaging";
     }
     if (d->closure == GBO_CLOSURE_SCALAR_DIFFUSIVITY) {
         if (!(d->closure_nu >= 0) || !std::isfinite(d->closure_nu)) return "ScalarDiffusivity ν must be finite and >= 0";
@@ -2168,6 +2341,10 @@ int gbo_ensemble_create(int32_t n, const gbo_grid_desc* grids, const gbo_model_d
     for (int32_t i = 0; i < n; ++i)
         if (descs[i].timestepper != GBO_TIMESTEPPER_RK3) {
             g_last_error = "member " + std::to_string(i) + ": ensembles step RungeKutta3 models only";
+            return GBO_ERR_INVALID;
+        } else if (descs[i].closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY && descs[i].closure_averaging == GBO_AVERAGING_LAGRANGIAN) {
+            // its FP64 clock advances with the member's own time_step! calls, not the ensemble's
+            g_last_error = "member " + std::to_string(i) + ": a Lagrangian-averaged DynamicSmagorinsky cannot join an ensemble";
             return GBO_ERR_INVALID;
         }
     auto* e = new gbo_ensemble();

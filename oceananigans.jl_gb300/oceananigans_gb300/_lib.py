@@ -30,6 +30,7 @@ GBO_SOLVER_FFT, GBO_SOLVER_FOURIER_TRIDIAGONAL, GBO_SOLVER_CONJUGATE_GRADIENT = 
 GBO_PRECOND_FFT, GBO_PRECOND_NONE, GBO_PRECOND_LEARNED = 0, 1, 2
 GBO_FIELD_U, GBO_FIELD_V, GBO_FIELD_W, GBO_FIELD_TRACER = 0, 1, 2, 3
 GBO_FIELD_PNHS, GBO_FIELD_PHY, GBO_FIELD_NU, GBO_FIELD_KAPPA = 100, 101, 102, 103
+GBO_FIELD_JLM, GBO_FIELD_JMM = 104, 105
 GBO_MAX_TRACERS = 4
 
 

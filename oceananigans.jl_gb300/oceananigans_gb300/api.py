@@ -198,10 +198,10 @@ class LagrangianAveraging:
 class DynamicSmagorinsky:
     """DynamicSmagorinsky(; averaging=LagrangianAveraging(), Pr=1, schedule=IterationInterval(1),
     minimum_numerator=1e-32) (turbulence_closure_implementations/Smagorinskys/
-    dynamic_coefficient.jl:104-117,215-300).  On GB300 the coefficient is averaged over x and
-    y (averaging=(1, 2)) and recomputed at every state update; the reference's default
-    LagrangianAveraging is described but rejected when the model is built, other
-    averagings and schedules raise ValueError here."""
+    dynamic_coefficient.jl:104-117,215-487).  Either averaging: LagrangianAveraging (the
+    default; 𝒥ᴸᴹ, 𝒥ᴹᴹ relaxed along trajectories once per time step, model fields "jlm" and
+    "jmm") or averaging=(1, 2) (the coefficient averaged over x and y at every state
+    update).  Other averagings and schedules raise ValueError here."""
 
     def __init__(self, averaging=None, Pr=1.0, minimum_numerator=1e-32, schedule=1):
         if averaging is None or isinstance(averaging, LagrangianAveraging):
@@ -421,7 +421,8 @@ class NonhydrostaticModel:
     def _fid(self, name):
         ids = {"u": L.GBO_FIELD_U, "v": L.GBO_FIELD_V, "w": L.GBO_FIELD_W, "p": L.GBO_FIELD_PNHS,
                "pNHS": L.GBO_FIELD_PNHS, "pHY": L.GBO_FIELD_PHY, "pHY′": L.GBO_FIELD_PHY,
-               "nu": L.GBO_FIELD_NU, "νₑ": L.GBO_FIELD_NU, "kappa": L.GBO_FIELD_KAPPA}
+               "nu": L.GBO_FIELD_NU, "νₑ": L.GBO_FIELD_NU, "kappa": L.GBO_FIELD_KAPPA,
+               "jlm": L.GBO_FIELD_JLM, "𝒥ᴸᴹ": L.GBO_FIELD_JLM, "jmm": L.GBO_FIELD_JMM, "𝒥ᴹᴹ": L.GBO_FIELD_JMM}
         if name in ids:
             return ids[name]
         if name in self.tracers:

@@ -9,7 +9,8 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libgb300ocean.so")
 SOURCES = ["gbo_model.cu", "gbo_fused_f32_tracer.cu", "gbo_fused_f32_momentum.cu", "gbo_fused_f64_tracer.cu",
-           "gbo_fused_f64_momentum.cu", "gbo_fft.cu", "gbo_static_poisson.cu", "gbo_learned.cu"]
+           "gbo_fused_f64_momentum.cu", "gbo_fft.cu", "gbo_static_poisson.cu", "gbo_learned.cu", "gbo_dynamic_f32.cu",
+           "gbo_dynamic_f64.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra nvcc options, e.g. GBO_NVCC_EXTRA="-DGBO_FUSED_MIN_BLOCKS=4" for a tuning build
 EXTRA = os.environ.get("GBO_NVCC_EXTRA", "").split()

@@ -107,7 +107,11 @@ def _rms(a):
 
 
 def _active_mean_free(a, active):
-    return (a - (a * active).sum() / active.sum()) * active
+    """a minus its mean over the active cells, zero elsewhere (whatever a holds there)."""
+    torch = _torch()
+    on = active > 0
+    a = torch.where(on, a, torch.zeros_like(a))
+    return torch.where(on, a - a.sum() / active.sum(), a)
 
 
 def collect_pairs(model, dt, steps, every=1, cg_iterations=0):
@@ -130,12 +134,12 @@ def collect_pairs(model, dt, steps, every=1, cg_iterations=0):
     act = active.to(dt_t)
 
     def A(v):
-        out = torch.empty_like(v)
+        out = torch.zeros_like(v)
         model.poisson_operator_device(v.data_ptr(), out.data_ptr())
         return out
 
     def M(v):
-        out = torch.empty_like(v)
+        out = torch.zeros_like(v)
         model.precondition_device(v.data_ptr(), out.data_ptr())
         return out
 

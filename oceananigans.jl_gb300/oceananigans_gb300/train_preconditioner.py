@@ -75,12 +75,19 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--cg-iterations", type=int, default=4)
+    ap.add_argument("--data-float64", action="store_true",
+                    help="collect the samples from an FP64 model (the plain FP64 CG); evaluate on the FP32 model")
     args = ap.parse_args(argv)
     log = lambda s: print(s, flush=True)  # noqa: E731
     model = seamount(tuple(args.size))
+    data_model = seamount(tuple(args.size), np.float64) if args.data_float64 else model
     t0 = time.time()
-    b, z, x, active = learned.collect_pairs(model, args.dt, args.pairs, cg_iterations=args.cg_iterations)
-    log("collected %d triples in %.1f s" % (b.shape[0], time.time() - t0))
+    b, z, x, active = learned.collect_pairs(data_model, args.dt, args.pairs, cg_iterations=args.cg_iterations)
+    log("collected %d triples (%s CG) in %.1f s" % (b.shape[0], "FP64" if args.data_float64 else "FP32", time.time() - t0))
+    if args.data_float64:
+        del data_model
+        from .api import time_step_  # noqa: PLC0415
+        time_step_(model, args.dt, args.pairs)  # the FP32 model to the same time
     t0 = time.time()
     w = learned.train(b, z, x, active, epochs=args.epochs, lr=args.lr, log=log)
     log("trained on the GPU in %.1f s" % (time.time() - t0))
@@ -93,6 +100,7 @@ def main(argv=None):
     lrn = timed_solves(model, rhs, torch)
     print(json.dumps({"heldout_solves": len(rhs), "reltol": 1e-8, "size": list(args.size),
                       "training_triples": int(args.pairs * (args.cg_iterations + 1)), "epochs": args.epochs,
+                      "data": "FP64 CG" if args.data_float64 else "FP32 CG", "trained_on": "GPU (gbo_learned_trainer)",
                       "fft_pcg": fft, "learned_pcg": lrn,
                       "time_ratio_learned_over_fft": lrn["ms_mean"] / fft["ms_mean"]}), flush=True)
 

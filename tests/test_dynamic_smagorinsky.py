@@ -175,7 +175,7 @@ def test_unsupported_averaging_and_grids_rejected():
         og.NonhydrostaticModel(c.grid, closure=og.DynamicSmagorinsky(), pressure_solver=og.ConjugateGradientPoissonSolver())
 
 
-# ---- LagrangianAveraging (dynamic_coefficient.jl:322-487): the oracle only; GB300 rejects it ----
+# ---- LagrangianAveraging (dynamic_coefficient.jl:322-487): the oracle's restatement ----
 
 def test_lagrangian_initialization_matches_numpy():
     # initialize_closure_fields!: 𝒥ᴸᴹ = max(mean LM, min), 𝒥ᴹᴹ = mean MM over the whole
@@ -220,10 +220,12 @@ def test_lagrangian_relaxation_vanishes_with_the_step():
     assert moves[0] < 1e-2 and moves[1] > 10 * moves[0]
 
 
-def test_lagrangian_rejected_on_gb300():
+def test_lagrangian_rejected_in_an_ensemble():
+    # an ensemble steps its members together; the Lagrangian clock is per model.  The
+    # check runs on the host before any member is built.
     c = _random_case(closure="lagrangian")
-    with pytest.raises(ValueError, match="LagrangianAveraging is not available"):
-        og.NonhydrostaticModel(c.grid, **c.physics)
+    with pytest.raises(ValueError, match="Lagrangian-averaged DynamicSmagorinsky cannot join an ensemble"):
+        og.Ensemble([(c.grid, c.physics)])
 
 
 # ---- the Lagrangian update restated on the oracle's own arrays (halos as they are) ----

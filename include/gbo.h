@@ -257,7 +257,15 @@ int gbo_run(gbo_model* m, const gbo_run_desc* d, gbo_run_result* out);
 int gbo_cell_advection_timescale(gbo_model* m, double* out);
 int gbo_cell_diffusion_timescale(gbo_model* m, double* out);
 
-/* ---- standalone Poisson solve ---------------------------------------------
+/* ---- device-buffer entry points ------------------------------------------------
+ * gbo_poisson_solve_device, gbo_poisson_operator_device, gbo_precondition_device and the
+ * trainer's gradients / step read device buffers on the library's own stream.  Each
+ * first orders that stream after the work already issued to the legacy default stream
+ * (cudaStreamLegacy, where PyTorch's default stream and plain CUDA calls run), and each
+ * returns after its results are written.  A caller that writes the inputs on another
+ * stream synchronises that stream first.
+ *
+ * ---- standalone Poisson solve ---------------------------------------------
  * Solve ∇²ϕ = rhs with the model's pressure solver on device buffers holding
  * Nx*Ny*Nz interior values of the model's float type.
  * Replaces solve!(ϕ, solver::FFTBasedPoissonSolver / FourierTridiagonalPoissonSolver, b)
@@ -389,6 +397,24 @@ int32_t gbo_kernel_group_count(void);
 /* Launches of each kernel group in the last gbo_kernel_timings pass (all its steps). */
 int gbo_kernel_timing_counts(const gbo_model* m, int64_t* n, int32_t nmax);
 const char* gbo_kernel_group_name(int32_t g);
+
+/* Launch shapes of the spectral Poisson passes and of the fused tendency kernel.  The
+ * pass tiles set speed only (every column and line is transformed by the same arithmetic
+ * whatever the tile); the levels per block of the fused kernel change where a block
+ * starts its vertical march, which can change results by rounding.  A model starts from
+ * the tuned shape of its size
+ * class (a table measured on GB300 and compiled into the library; see
+ * oceananigans_gb300/autotune.py) or, for sizes not in the table, from the default rule. */
+typedef struct gbo_launch_shape {
+    int32_t dct_columns; /* x columns per block of the z DCT pass: a power of two, 2..64 */
+    int32_t x_lines;     /* (y, z) lines per block of the x real-FFT pass: 1..32 */
+    int32_t y_columns;   /* kx columns per block of the y FFT pass: a power of two, 1..64 */
+    int32_t levels;      /* levels each block of the fused tendency kernel marches: 1..Nz (1 on a Flat z) */
+} gbo_launch_shape;
+int gbo_get_launch_shape(const gbo_model* m, gbo_launch_shape* out);
+/* Replaces the shape (invalid: GBO_ERR_INVALID, model unchanged); the model's captured
+ * step graphs are rebuilt at the next step.  Not for ensemble members. */
+int gbo_set_launch_shape(gbo_model* m, const gbo_launch_shape* shape);
 
 #ifdef __cplusplus
 }

@@ -112,14 +112,15 @@ __host__ __device__ constexpr CPlan cplan(int n) {
 }
 
 template <typename FT, int N, int R, int NS, bool IL>
-__device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* __restrict__ B, int L, int sign,
+__device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* __restrict__ B, int L, int lg, int sign,
                                           const Cx<FT>* __restrict__ tw) {
     constexpr int NR = N / R;
     constexpr int TWS = N / (NS * R);
     const int es = IL ? L : 1;
     for (int t = threadIdx.x; t < L * NR; t += blockDim.x) {
-        const int line = IL ? t % L : t / NR;
-        const int jj = IL ? t / L : t - line * NR;
+        // interleaved: L is a power of two (lg = log2 L), so the split is a mask and a shift
+        const int line = IL ? (t & (L - 1)) : t / NR;
+        const int jj = IL ? (t >> lg) : t - line * NR;
         const int kk = jj % NS;
         const Cx<FT>* x = A + (IL ? line : line * N);
         Cx<FT>* y = B + (IL ? line : line * N);
@@ -167,27 +168,28 @@ __device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* 
 
 template <typename FT, int N, int S, int NS, bool IL>
 struct FFTStages {
-    static __device__ __forceinline__ Cx<FT>* run(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
+    static __device__ __forceinline__ Cx<FT>* run(Cx<FT>* A, Cx<FT>* B, int L, int lg, int sign, const Cx<FT>* tw) {
         constexpr CPlan p = cplan(N);
         if constexpr (S >= p.nrad) {
             return A;
         } else {
             constexpr int R = p.rad[S];
-            fft_stage<FT, N, R, NS, IL>(A, B, L, sign, tw);
-            return FFTStages<FT, N, S + 1, NS * R, IL>::run(B, A, L, sign, tw);
+            fft_stage<FT, N, R, NS, IL>(A, B, L, lg, sign, tw);
+            return FFTStages<FT, N, S + 1, NS * R, IL>::run(B, A, L, lg, sign, tw);
         }
     }
 };
 
 template <typename FT, int N, bool IL>
 __device__ __forceinline__ Cx<FT>* block_fft_n(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
-    return FFTStages<FT, N, 0, 1, IL>::run(A, B, L, sign, tw);
+    return FFTStages<FT, N, 0, 1, IL>::run(A, B, L, __ffs(L) - 1, sign, tw);
 }
 
 // Dispatch helper: a kernel template parameter NC (0 = runtime length) selects
 // the compile-time engine when the length matches.  IL: interleaved line layout
 // (element (line, m) at m*L + line), used where a block's lines are columns of a
-// strided axis so that loads, scatters and butterflies are bank-conflict free.
+// strided axis so that loads, scatters and butterflies are bank-conflict free; L is
+// then a power of two.  tw is the block's shared-memory copy of the twiddles.
 template <typename FT, int NC, bool IL>
 __device__ __forceinline__ Cx<FT>* fft_any(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* tw) {
     if constexpr (NC > 0) return block_fft_n<FT, NC, IL>(A, B, L, sign, tw);
@@ -223,6 +225,24 @@ struct PoissonTables;  // host side
 #define GBO_PASS_SMEM_LIMIT (100 * 1024)
 #endif
 
+// Shared memory of the pass kernels: the two work buffers of the block's lines, then the
+// twiddles of its transforms staged once per block (the butterflies read them from
+// shared memory instead of global memory)
+template <typename FT>
+inline size_t dct_smem(int ZT, int Nz) { return ((size_t)ZT * Nz + 2 * (size_t)Nz) * sizeof(Cx<FT>); }
+template <typename FT>
+inline size_t rfft_smem(int XL, int Nx) { return ((size_t)XL * (Nx + 1) + (size_t)Nx) * sizeof(Cx<FT>); }
+template <typename FT>
+inline size_t ffty_smem(int YT, int Ny) { return (2 * (size_t)YT * Ny + (size_t)Ny) * sizeof(Cx<FT>); }
+// the launch shapes the kernels accept: interleaved line counts are powers of two
+GBO_HD constexpr bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+// stage n complex values (twiddles) asynchronously; waited for with the tile
+template <typename FT>
+GBO_D void stage_table(Cx<FT>* dst, const Cx<FT>* __restrict__ src, int n) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) cp_async_n<sizeof(Cx<FT>)>(&dst[t], src + t, false);
+}
+
 template <typename FT>
 struct PassP {
     int Nx, Ny, Nz, Nh;        // Nh = Nx/2 + 1
@@ -249,29 +269,34 @@ template <typename FT, int NC>
 __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
     extern __shared__ unsigned char smem_raw[];
     const int N = P.Nz;
-    const int L = ZT / 2;
+    const int L = ZT / 2;  // a power of two
+    const int lz = __ffs(ZT) - 1, ll = lz - 1;
     Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
     Cx<FT>* B = A + L * N;
+    Cx<FT>* T = B + L * N;  // twiddles of the length-N FFT
+    Cx<FT>* Q = T + N;      // ω^k = exp(-iπk/(2N)) of the DCT post-processing
     const int j = blockIdx.y;
     const int i0 = blockIdx.x * ZT;
     const size_t plane = (size_t)P.Nx * P.Ny;
     FT* col0 = P.rb + i0 + (size_t)P.Nx * j;
+    stage_table(T, P.tw_z, N);
+    stage_table(Q, P.tq_z, N);
     if (!inverse) {
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t % ZT, k = t / ZT;
+            int c = t & (ZT - 1), k = t >> lz;
             const bool in = i0 + c < P.Nx;
             Cx<FT>& d = A[makhoul_dest(k, N) * L + (c >> 1)];
             cp_async_n<sizeof(FT)>((c & 1) ? &d.im : &d.re, in ? col0 + c + plane * k : col0, !in);
         }
         cp_async_wait();
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, -1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, -1, T);
         Cx<FT>* O = (R == A) ? B : A;
         FT* out = reinterpret_cast<FT*>(O);  // ZT x N reals staged for coalesced stores
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
-            int l = t % L, k = t / L;
+            int l = t & (L - 1), k = t >> ll;
             Cx<FT> Zk = R[k * L + l], Zn = R[(k == 0 ? 0 : N - k) * L + l];
-            Cx<FT> w = P.tq_z[k];
+            Cx<FT> w = Q[k];
             Cx<FT> s = Zk + conj(Zn), d = Zk - conj(Zn);
             Cx<FT> ws = w * s, wd = w * d;
             out[(2 * l) + ZT * k] = ws.re;       // X_a[k] = Re(ω^k (Z_k + Z*_{N-k}))
@@ -279,33 +304,33 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
         }
         __syncthreads();
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t % ZT, k = t / ZT;
+            int c = t & (ZT - 1), k = t >> lz;
             if (i0 + c < P.Nx) col0[c + plane * k] = out[c + ZT * k];
         }
     } else {
         FT* in = reinterpret_cast<FT*>(B);
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t % ZT, k = t / ZT;
+            int c = t & (ZT - 1), k = t >> lz;
             const bool ok = i0 + c < P.Nx;
             cp_async_n<sizeof(FT)>(&in[c + ZT * k], ok ? col0 + c + plane * k : col0, !ok);
         }
         cp_async_wait();
         __syncthreads();
         for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
-            int l = t % L, k = t / L;
+            int l = t & (L - 1), k = t >> ll;
             FT Xa = in[2 * l + ZT * k], Xb = in[2 * l + 1 + ZT * k];
             FT Xan = k == 0 ? FT(0) : in[2 * l + ZT * (N - k)];
             FT Xbn = k == 0 ? FT(0) : in[2 * l + 1 + ZT * (N - k)];
-            Cx<FT> w = conj(P.tq_z[k]);
+            Cx<FT> w = conj(Q[k]);
             // V_a = ω^{-k}(X_a[k] - i X_a[N-k]) / 2 ; V_b likewise ; Z = V_a + i V_b
             Cx<FT> Va = FT(0.5) * (w * cx(Xa, -Xan));
             Cx<FT> Vb = FT(0.5) * (w * cx(Xb, -Xbn));
             A[k * L + l] = cx(Va.re - Vb.im, Va.im + Vb.re);
         }
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, +1, P.tw_z);
+        Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, +1, T);
         for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t % ZT, k = t / ZT;
+            int c = t & (ZT - 1), k = t >> lz;
             Cx<FT> z = R[makhoul_dest(k, N) * L + (c >> 1)];
             if (i0 + c < P.Nx) col0[c + plane * k] = (c & 1) ? z.im : z.re;
         }
@@ -323,16 +348,20 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
     const int M = P.Nx / 2, Nh = P.Nh;
     Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
     Cx<FT>* B = A + XL * M;
+    Cx<FT>* T = A + XL * (P.Nx + 1);  // twiddles of the half-length FFT
+    Cx<FT>* X = T + M;                // the real-FFT split twiddles
     const int nlines = P.Ny * P.Nz;
     const int line0 = blockIdx.x * XL;
     const int L = min(XL, nlines - line0);
+    stage_table(T, P.tw_xh, M);
+    stage_table(X, P.tw_x, M);
     if (!inverse) {
         const FT* src = P.rb + (size_t)line0 * P.Nx;
         FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) cp_async_n<sizeof(FT)>(&As[t], src + t, false);
         cp_async_wait();
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, -1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, -1, T);
         Cx<FT>* dst = P.cb + (size_t)line0 * Nh;
         for (int t = threadIdx.x; t < L * Nh; t += blockDim.x) {
             int l = t / Nh, k = t - l * Nh;
@@ -341,7 +370,7 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
             Cx<FT> e = FT(0.5) * (Zk + conj(Zn));
             Cx<FT> d = FT(0.5) * (Zk - conj(Zn));
             Cx<FT> o = cx(d.im, -d.re);  // (Z_k - Z*_{M-k}) / (2i)
-            Cx<FT> w = P.tw_x[k == M ? 0 : k];
+            Cx<FT> w = X[k == M ? 0 : k];
             if (k == M) w = cx(FT(-1), FT(0));
             dst[t] = e + w * o;
         }
@@ -355,12 +384,12 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
             int l = t / M, k = t - l * M;
             Cx<FT> Xk = S[l * Nh + k], Xn = S[l * Nh + (M - k)];
             Cx<FT> e = Xk + conj(Xn);
-            Cx<FT> w = conj(P.tw_x[k]);
+            Cx<FT> w = conj(X[k]);
             Cx<FT> o = w * (Xk - conj(Xn));
             A[l * M + k] = cx(e.re - o.im, e.im + o.re);  // e + i o
         }
         __syncthreads();
-        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, +1, P.tw_xh);
+        Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, +1, T);
         FT* dst = P.rb + (size_t)line0 * P.Nx;
         const FT* Rs = reinterpret_cast<const FT*>(R);
         for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) dst[t] = Rs[t];
@@ -376,23 +405,26 @@ template <typename FT, int NC>
 __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     extern __shared__ unsigned char smem_raw[];
     const int N = P.Ny, Nh = P.Nh;
+    const int ly = __ffs(YT) - 1;  // YT is a power of two
     Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
     Cx<FT>* B = A + YT * N;
+    Cx<FT>* T = B + YT * N;  // twiddles of the length-N FFT
     const int kz = blockIdx.y;
     const int kx0 = blockIdx.x * YT;
     Cx<FT>* base = P.cb + kx0 + (size_t)Nh * N * kz;
+    stage_table(T, P.tw_y, N);
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
-        int c = t % YT, ky = t / YT;
+        int c = t & (YT - 1), ky = t >> ly;
         const bool ok = kx0 + c < Nh;
         cp_async_n<sizeof(Cx<FT>)>(&A[ky * YT + c], ok ? base + c + (size_t)Nh * ky : base, !ok);
     }
     cp_async_wait();
     __syncthreads();
     Cx<FT>* R = A;
-    if (mode != 2) R = fft_any<FT, NC, true>(A, B, YT, P.py, -1, P.tw_y);
+    if (mode != 2) R = fft_any<FT, NC, true>(A, B, YT, P.py, -1, T);
     if (mode == 0) {
         for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
-            int c = t % YT, ky = t / YT;
+            int c = t & (YT - 1), ky = t >> ly;
             int kx = kx0 + c;
             if (kx < Nh) {
                 FT lam = (P.lx[kx] + P.ly[ky]) + (P.has_z ? P.lz[kz] : FT(0));
@@ -406,10 +438,10 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     }
     if (mode != 1) {
         Cx<FT>* O = (R == A) ? B : A;
-        R = fft_any<FT, NC, true>(R, O, YT, P.py, +1, P.tw_y);
+        R = fft_any<FT, NC, true>(R, O, YT, P.py, +1, T);
     }
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
-        int c = t % YT, ky = t / YT;
+        int c = t & (YT - 1), ky = t >> ly;
         if (kx0 + c < Nh) base[c + (size_t)Nh * ky] = R[ky * YT + c];
     }
 }

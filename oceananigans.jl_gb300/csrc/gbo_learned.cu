@@ -1050,6 +1050,7 @@ cudaError_t wgrad_attr() {
 struct gbo_learned_trainer {
     LearnedNet* net = nullptr;
     cudaStream_t stream = nullptr;
+    cudaEvent_t join_ev = nullptr;  // orders the stream after the caller's legacy-stream work
     int64_t count = 0, off[learned::NLAYERS] = {};
     float *wm = nullptr, *m = nullptr, *v = nullptr, *g = nullptr, *y = nullptr;
     double* sums = nullptr;
@@ -1068,7 +1069,14 @@ struct gbo_learned_trainer {
         owned.push_back(p);
         return static_cast<T*>(p);
     }
+    // the samples were just written by the caller: wait (on the device) for the work
+    // already issued to the legacy default stream
+    void join_caller() {
+        cudaEventRecord(join_ev, cudaStreamLegacy);
+        cudaStreamWaitEvent(stream, join_ev, 0);
+    }
     ~gbo_learned_trainer() {
+        if (join_ev) cudaEventDestroy(join_ev);
         for (void* p : owned) cudaFree(p);
         if (net) learned_destroy(net);
         if (stream) cudaStreamDestroy(stream);
@@ -1158,6 +1166,12 @@ struct gbo_learned_trainer {
     }
 
     int check() {
+        // a launch refused at configuration (shared memory, grid) is reported here, not by the sync
+        const cudaError_t launch = cudaGetLastError();
+        if (launch != cudaSuccess) {
+            err = std::string("a learned-trainer kernel could not be launched: ") + cudaGetErrorString(launch);
+            return GBO_ERR_CUDA;
+        }
         unsigned h = 0;
         if (cudaMemcpyAsync(&h, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
             cudaStreamSynchronize(stream) != cudaSuccess) {
@@ -1182,7 +1196,8 @@ int gbo_learned_trainer_create(int32_t nx, int32_t ny, int32_t nz, const float* 
     auto* t = new gbo_learned_trainer();
     t->net = net;
     t->count = count;
-    bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess;
+    bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&t->join_ev, cudaEventDisableTiming) == cudaSuccess;
     int64_t at = 0;
     for (int l = 0; l < NLAYERS; ++l) {
         t->off[l] = at;
@@ -1239,6 +1254,7 @@ void gbo_learned_trainer_destroy(gbo_learned_trainer* t) { delete t; }
 int gbo_learned_trainer_gradients(gbo_learned_trainer* t, const float* r, const float* z, const float* e,
                                   const float* active, double* loss, float* grad) {
     if (!t || !r || !z || !e || !active || !loss || !grad) return GBO_ERR_INVALID;
+    t->join_caller();
     cudaMemsetAsync(t->g, 0, t->count * sizeof(float), t->stream);
     t->forward(r, z, active);
     t->loss(z, e, active);
@@ -1256,6 +1272,7 @@ int gbo_learned_trainer_step(gbo_learned_trainer* t, const float* r, const float
                              double lr, double* loss) {
     if (!t || !r || !z || !e || !active) return GBO_ERR_INVALID;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    t->join_caller();
     t->forward(r, z, active);
     t->loss(z, e, active);
     t->backward();

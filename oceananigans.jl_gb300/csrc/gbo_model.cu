@@ -14,6 +14,7 @@
 #include "gbo_learned.cuh"
 #include "gbo_fused.cuh"
 #include "gbo_dynamic.cuh"
+#include "gbo_launch_table.h"
 
 // ===========================================================================
 // Pressure source and projection kernels
@@ -380,6 +381,8 @@ struct gbo_model {
     virtual void add_launches(int64_t n) = 0;
     virtual int finish_steps(double dt, int nsteps) = 0;
     virtual int64_t launch_count() const = 0;
+    virtual int launch_shape(gbo_launch_shape* s) const = 0;
+    virtual int set_launch_shape(const gbo_launch_shape* s) = 0;
     int64_t count(int field) const {
         int64_t plane = (int64_t)Nx * Ny;
         if (field == GBO_FIELD_W) return flat ? plane : plane * (Nz + 1);
@@ -534,6 +537,7 @@ struct ModelImpl : gbo_model {
         lag_zc.free_();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (join_ev) cudaEventDestroy(join_ev);
         if (d_flags) cudaFree(d_flags);
         if (h_flags) cudaFreeHost(h_flags);
         if (stream) cudaStreamDestroy(stream);
@@ -716,22 +720,27 @@ struct ModelImpl : gbo_model {
             launch_thomas_tables(tp, stream);
             GBO_CUDA(cudaGetLastError());
         }
-        // shared-memory tiles: keep each block at or below ~100 KB
-        const size_t cs_ = sizeof(C), lim = GBO_PASS_SMEM_LIMIT;
+        // shared-memory tiles: the tuned shape of this size class, else keep each block at
+        // or below ~100 KB
+        const size_t lim = GBO_PASS_SMEM_LIMIT;
         ZT = GBO_DCT_TILE;
-        while (ZT > 2 && (size_t)ZT * Nz * cs_ > lim) ZT /= 2;
-        smem_z = (size_t)ZT * Nz * cs_;
+        while (ZT > 2 && dct_smem<FT>(ZT, Nz) > lim) ZT /= 2;
         XL = 8;
         // two buffers of XL lines of Nx/2 coefficients, plus XL for staging Nx/2+1 per line
-        while (XL > 1 && (size_t)XL * (Nx + 1) * cs_ > lim) XL /= 2;
-        smem_x = (size_t)XL * (Nx + 1) * cs_;
+        while (XL > 1 && rfft_smem<FT>(XL, Nx) > lim) XL /= 2;
         YT = 16;
-        while (YT > 1 && (size_t)2 * YT * Ny * cs_ > lim) YT /= 2;
-        smem_y = (size_t)2 * YT * Ny * cs_;
+        while (YT > 1 && ffty_smem<FT>(YT, Ny) > lim) YT /= 2;
+        kchunk = flat ? 1 : std::min(16, Nz);
+        if (const LaunchShapeEntry* t = tuned_shape(Nx, Ny, Nz, sizeof(FT) == 8, ibg)) {
+            ZT = t->dct_columns;
+            XL = t->x_lines;
+            YT = t->y_columns;
+            if (!flat) kchunk = std::min(t->levels, Nz);
+        }
+        pass_smem();
         GBO_CUDA(fused_set_smem<FT>());
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::SmemS<FT>)));
         GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
-        kchunk = flat ? 1 : std::min(16, Nz);
         // The pass kernels are shared by every model in the process: allow them the device's
         // opt-in maximum rather than this model's sizes, so a model created later never
         // lowers the limit an earlier, larger model needs.
@@ -740,6 +749,41 @@ struct ModelImpl : gbo_model {
         if ((size_t)optin < std::max({smem_z, smem_x, smem_y}))
             throw InvalidArg{"grid too large for the shared-memory tiles of the spectral Poisson solver"};
         GBO_CUDA(fft_set_smem<FT>(optin, optin, optin));
+    }
+
+    // shared memory of the pass kernels at the current tiles
+    void pass_smem() {
+        smem_z = dct_smem<FT>(ZT, Nz);
+        smem_x = rfft_smem<FT>(XL, Nx);
+        smem_y = ffty_smem<FT>(YT, Ny);
+    }
+    int launch_shape(gbo_launch_shape* s) const override {
+        *s = gbo_launch_shape{ZT, XL, YT, kchunk};
+        return GBO_OK;
+    }
+    int set_launch_shape(const gbo_launch_shape* s) override {
+        if (ensemble_member) { err = "the launch shape of an ensemble member cannot change"; return GBO_ERR_INVALID; }
+        if (s->dct_columns < 2 || s->dct_columns > 64 || !pow2(s->dct_columns) || s->x_lines < 1 || s->x_lines > 32 ||
+            s->y_columns < 1 || s->y_columns > 64 || !pow2(s->y_columns) || s->levels < 1 || s->levels > Nz ||
+            (flat && s->levels != 1)) {
+            err = "launch shape out of range (DCT and y-FFT tiles are powers of two)";
+            return GBO_ERR_INVALID;
+        }
+        int optin = 0;
+        GBO_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        if (dct_smem<FT>(s->dct_columns, Nz) > (size_t)optin || rfft_smem<FT>(s->x_lines, Nx) > (size_t)optin ||
+            ffty_smem<FT>(s->y_columns, Ny) > (size_t)optin) {
+            err = "launch shape needs more shared memory per block than the device has";
+            return GBO_ERR_INVALID;
+        }
+        GBO_CUDA(cudaStreamSynchronize(stream));
+        drop_graphs();
+        ZT = s->dct_columns;
+        XL = s->x_lines;
+        YT = s->y_columns;
+        kchunk = s->levels;
+        pass_smem();
+        return GBO_OK;
     }
 
     // ------------------------------------------------------------------
@@ -930,6 +974,16 @@ struct ModelImpl : gbo_model {
         launches += nk - 1;
     }
 
+    // The device-pointer entry points read buffers their caller has just written: order
+    // this model's (non-blocking) stream after the work already issued to the legacy
+    // default stream, where PyTorch and most callers issue theirs, without a host wait.
+    cudaEvent_t join_ev = nullptr;
+    void join_caller() {
+        if (!join_ev) GBO_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+        GBO_CUDA(cudaEventRecord(join_ev, cudaStreamLegacy));
+        GBO_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+    }
+
     void drop_graphs() {
         if (graph) { GBO_CUDA(cudaGraphExecDestroy(graph)); graph = nullptr; }
         if (graph_euler) { GBO_CUDA(cudaGraphExecDestroy(graph_euler)); graph_euler = nullptr; }
@@ -956,6 +1010,7 @@ struct ModelImpl : gbo_model {
     // V∇²x with the conditional differences of the CG operator (out must not alias x)
     int operator_device(const void* x, void* out) override {
         if (!ibg && !cg) { err = "the CG operator needs an immersed grid or the CG solver"; return GBO_ERR_INVALID; }
+        join_caller();
         pre(G_CG);
         k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, static_cast<const FT*>(x), static_cast<FT*>(out), nullptr);
         check_launch();
@@ -967,6 +1022,7 @@ struct ModelImpl : gbo_model {
     int precondition_device(const void* r, void* z) override {
         if (!cg || desc.preconditioner != GBO_PRECOND_FFT) { err = "the model has no CG preconditioner"; return GBO_ERR_INVALID; }
         const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
+        join_caller();
         GBO_CUDA(cudaMemcpyAsync(cg_r.p, r, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
         pre(G_CG);
         k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, cg_s.p, dzs);
@@ -1989,6 +2045,7 @@ struct ModelImpl : gbo_model {
     }
 
     int poisson_device(void* phi, const void* rhs) override {
+        join_caller();
         if (cg) {
             // V∇²ϕ = rhs by preconditioned CG from the initial guess in ϕ
             GBO_CUDA(cudaMemcpyAsync(cg_x.p, phi, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
@@ -2435,6 +2492,16 @@ int gbo_kernel_timings(gbo_model* m, double dt, int32_t nsteps, double* ms, int3
 }
 
 int32_t gbo_kernel_group_count(void) { return GROUPS; }
+
+int gbo_get_launch_shape(const gbo_model* m, gbo_launch_shape* out) {
+    if (!m || !out) return GBO_ERR_INVALID;
+    return m->launch_shape(out);
+}
+
+int gbo_set_launch_shape(gbo_model* m, const gbo_launch_shape* shape) {
+    if (!m || !shape) return GBO_ERR_INVALID;
+    return guarded(m, [&]() { return m->set_launch_shape(shape); });
+}
 
 int gbo_kernel_timing_counts(const gbo_model* m, int64_t* n, int32_t nmax) {
     if (!m || !n || nmax < 0) return GBO_ERR_INVALID;

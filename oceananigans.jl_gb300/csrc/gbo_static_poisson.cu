@@ -221,12 +221,12 @@ int solve(const gbo_grid_desc* gd, void* phi, const void* rhs, cudaStream_t st) 
     P.scale = flat ? FT(1.0 / ((double)Nx * Ny)) : FT(1.0 / ((double)Nx * Ny * Nz));
 
     // shared-memory tiles chosen exactly as the model's solver chooses them
-    const size_t cs = sizeof(Cx<FT>), lim = GBO_PASS_SMEM_LIMIT;
+    const size_t lim = GBO_PASS_SMEM_LIMIT;
     int ZT = GBO_DCT_TILE, XL = 8, YT = 16;
-    while (ZT > 2 && (size_t)ZT * Nz * cs > lim) ZT /= 2;
-    while (XL > 1 && (size_t)XL * (Nx + 1) * cs > lim) XL /= 2;
-    while (YT > 1 && (size_t)2 * YT * Ny * cs > lim) YT /= 2;
-    const size_t smem_z = (size_t)ZT * Nz * cs, smem_x = (size_t)XL * (Nx + 1) * cs, smem_y = (size_t)2 * YT * Ny * cs;
+    while (ZT > 2 && dct_smem<FT>(ZT, Nz) > lim) ZT /= 2;
+    while (XL > 1 && rfft_smem<FT>(XL, Nx) > lim) XL /= 2;
+    while (YT > 1 && ffty_smem<FT>(YT, Ny) > lim) YT /= 2;
+    const size_t smem_z = dct_smem<FT>(ZT, Nz), smem_x = rfft_smem<FT>(XL, Nx), smem_y = ffty_smem<FT>(YT, Ny);
     if (std::max({smem_z, smem_x, smem_y}) > (size_t)optin)
         return fail(GBO_ERR_INVALID, "grid needs %lld bytes of shared memory per block; the device allows %lld",
                     (long long)std::max({smem_z, smem_x, smem_y}), optin);

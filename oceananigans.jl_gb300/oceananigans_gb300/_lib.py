@@ -34,6 +34,11 @@ GBO_FIELD_JLM, GBO_FIELD_JMM = 104, 105
 GBO_MAX_TRACERS = 4
 
 
+class LaunchShape(ctypes.Structure):
+    _fields_ = [("dct_columns", ctypes.c_int32), ("x_lines", ctypes.c_int32), ("y_columns", ctypes.c_int32),
+                ("levels", ctypes.c_int32)]
+
+
 class GridDesc(ctypes.Structure):
     _fields_ = [("size", ctypes.c_int32 * 3), ("topology", ctypes.c_int32 * 3),
                 ("x", ctypes.c_double * 2), ("y", ctypes.c_double * 2), ("z", ctypes.c_double * 2),
@@ -146,6 +151,8 @@ SIGNATURES = {
     "gbo_kernel_group_count": (ctypes.c_int32, []),
     "gbo_kernel_timing_counts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]),
     "gbo_kernel_group_name": (ctypes.c_char_p, [ctypes.c_int32]),
+    "gbo_get_launch_shape": (ctypes.c_int, [_vp, ctypes.POINTER(LaunchShape)]),
+    "gbo_set_launch_shape": (ctypes.c_int, [_vp, ctypes.POINTER(LaunchShape)]),
 }
 
 _lib = None

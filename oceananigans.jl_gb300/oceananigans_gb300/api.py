@@ -521,6 +521,23 @@ class NonhydrostaticModel:
         """z = M r with the model's CG preconditioner, on device buffers."""
         L.check(L.load().gbo_precondition_device(self._h, ctypes.c_void_p(r_ptr), ctypes.c_void_p(z_ptr)), self._h)
 
+    @property
+    def launch_shape(self):
+        """The launch shape (dict: dct_columns, x_lines, y_columns, levels); tuning only."""
+        sh = L.LaunchShape()
+        L.check(L.load().gbo_get_launch_shape(self._h, ctypes.byref(sh)), self._h)
+        return {f: int(getattr(sh, f)) for f, _ in L.LaunchShape._fields_}
+
+    def set_launch_shape(self, **shape):
+        """Replace some of the launch shape's entries (gbo_set_launch_shape)."""
+        cur = self.launch_shape
+        cur.update({k: int(v) for k, v in shape.items()})
+        sh = L.LaunchShape(**cur)
+        rc = L.load().gbo_set_launch_shape(self._h, ctypes.byref(sh))
+        if rc == L.GBO_ERR_INVALID:
+            raise ValueError(L.load().gbo_last_error(self._h).decode())
+        L.check(rc, self._h)
+
     def prognostic_state(self):
         """prognostic_state(model): the restart state as a numpy byte array."""
         lib = L.load()

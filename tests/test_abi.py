@@ -162,3 +162,21 @@ def test_fplane_keywords():
     for bad in (dict(), dict(f=1e-4, latitude=10.0)):
         with pytest.raises(ValueError, match="Either both keywords"):
             og.FPlane(**bad)
+
+
+def test_launch_table_entries_are_valid():
+    # the tuned shapes compiled into the library (written by oceananigans_gb300/autotune.py)
+    import re
+    path = os.path.join(os.path.dirname(__file__), "..", "oceananigans.jl_gb300", "csrc", "gbo_launch_table.h")
+    with open(path) as f:
+        text = f.read()
+    body = text[text.index("// BEGIN TABLE"):text.index("// END TABLE")]
+    rows = [tuple(int(v) for v in m.group(1).split(",")) for m in re.finditer(r"\{([-\d, ]+)\}", body)]
+    assert rows and rows[-1] == (0,) * 9  # terminated
+    seen = set()
+    for nx, ny, nz, fp64, ibg, zt, xl, yt, lev in rows[:-1]:
+        assert nx > 0 and ny > 0 and nz > 0 and fp64 in (0, 1) and ibg in (0, 1)
+        assert 2 <= zt <= 64 and zt & (zt - 1) == 0 and 1 <= xl <= 32 and 1 <= yt <= 64 and yt & (yt - 1) == 0
+        assert 1 <= lev <= nz
+        assert (nx, ny, nz, fp64, ibg) not in seen
+        seen.add((nx, ny, nz, fp64, ibg))

@@ -928,8 +928,11 @@ struct TileFields {
 };
 }  // namespace smag
 
+// AMD on an immersed grid: the tile in shared memory, every cell evaluated by amd_point
+// through the strain code with the immersed grid's conditional derivatives
+// (conditional_differences.jl:15-43)
 template <typename FT>
-__global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
+__global__ void __launch_bounds__(256) k_amd_tiled_ibg(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
     using namespace smag;
     extern __shared__ unsigned char smem_raw[];
     Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
@@ -957,5 +960,155 @@ __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__
         const int k = k0 + z;
         if (k >= g.Nz) break;
         amd_point<FT>(P, g, S, tc, has_c, i, j, k, i + (size_t)g.Nx * (j + (size_t)g.Ny * k), nu_out, kap_out);
+    }
+}
+
+namespace smag {
+// AMD: the tile plus the six normalised off-diagonal velocity gradients at their edges
+// (x·y edges at every level, x·z and y·z edges at every face of the tile).  ∂y w is kept
+// one column wider: the tracer term interpolates it over x and z (ℑxzᶜᵃᶜ, as the
+// reference does, anisotropic_minimum_dissipation.jl:344)
+constexpr int E23X = (TX + 1) * (TY + 1) * (KT + 1);
+GBO_D int i23x(int x, int y, int z) { return (z * (TY + 1) + y) * (TX + 1) + x; }
+template <typename FT>
+struct SmemA : Smem<FT> {
+    FT dxv[E12], dyu[E12], dxw[E13], dzu[E13], dyw[E23X], dzv[E23];
+};
+}  // namespace smag
+
+// Anisotropic minimum dissipation νₑ (and κₑ of one tracer) on a 32×8×4 tile
+// (anisotropic_minimum_dissipation.jl:161-204,243-358; velocity_tracer_gradients.jl:
+// 120-250).  The normalised gradients Δ̃ᵢ/Δ̃ⱼ ∂ⱼuᵢ of the cross terms live on edges and
+// each cell interpolates products of them from four edges; every edge value is shared by
+// four cells, so the block evaluates each once into shared memory (the filter-width
+// ratios once per level), then every cell combines its 24 edge values with the same
+// arithmetic, in the same order, as the per-point amd_point.  Rectilinear grids only (an
+// immersed grid takes k_amd_tiled_ibg).
+template <typename FT>
+__global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
+    using namespace smag;
+    extern __shared__ unsigned char smem_raw[];
+    SmemA<FT>& s = *reinterpret_cast<SmemA<FT>*>(smem_raw);
+    const GridP<FT>& g = P.g;
+    Met<FT> M(g);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
+    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g, P.cref);
+    WFld<FT> Wg = wfld(P.w, g);
+    const bool has_c = P.c != nullptr;
+    const int fz = g.flatz;
+    for (int e = tid; e < BS; e += TX * TY) {
+        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
+        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
+        s.u[e] = Ug.far(gi, gj, gk);
+        s.v[e] = Vg.far(gi, gj, gk);
+        s.w[e] = Wg.far(gi, gj, gk);
+        s.b[e] = has_c ? Cg.far(gi, gj, gk) : FT(0);
+    }
+    __syncthreads();
+    auto U = [&](int x, int y, int z) { return s.u[bidx(x, y, z)]; };
+    auto V = [&](int x, int y, int z) { return s.v[bidx(x, y, z)]; };
+    auto W = [&](int x, int y, int z) { return s.w[bidx(x, y, z)]; };
+    auto C = [&](int x, int y, int z) { return s.b[bidx(x, y, z)]; };
+    // filter widths 2Δ (the reference's Δᶠ at the evaluation index) and their ratios
+    const FT Dx = FT(2) * g.dx, Dy = FT(2) * g.dy;
+    const FT rxy = Dx / Dy, ryx = Dy / Dx;
+    for (int e = tid; e < E12; e += TX * TY) {
+        const int x = e % (TX + 1), y = (e / (TX + 1)) % (TY + 1), z = e / ((TX + 1) * (TY + 1));
+        s.dyu[e] = ryx * ((U(x, y, z) - U(x, y - 1, z)) * g.rdy);
+        s.dxv[e] = rxy * ((V(x, y, z) - V(x - 1, y, z)) * g.rdx);
+    }
+    for (int e = tid; e < E13; e += TX * TY) {
+        const int x = e % (TX + 1), y = (e / (TX + 1)) % TY, z = e / ((TX + 1) * TY), k = k0 + z;
+        const FT Dz = FT(2) * M.dzc(k);
+        s.dxw[e] = (Dx / Dz) * (fz ? FT(0) : (W(x, y, z) - W(x - 1, y, z)) * g.rdx);
+        s.dzu[e] = (Dz / Dx) * (fz ? FT(0) : (U(x, y, z) - U(x, y, z - 1)) * M.rdzf(k));
+    }
+    for (int e = tid; e < E23; e += TX * TY) {
+        const int x = e % TX, y = (e / TX) % (TY + 1), z = e / (TX * (TY + 1)), k = k0 + z;
+        const FT Dz = FT(2) * M.dzc(k);
+        s.dzv[e] = (Dz / Dy) * (fz ? FT(0) : (V(x, y, z) - V(x, y, z - 1)) * M.rdzf(k));
+    }
+    for (int e = tid; e < E23X; e += TX * TY) {
+        const int x = e % (TX + 1), y = (e / (TX + 1)) % (TY + 1), z = e / ((TX + 1) * (TY + 1)), k = k0 + z;
+        const FT Dz = FT(2) * M.dzc(k);
+        s.dyw[e] = (Dy / Dz) * (fz ? FT(0) : (W(x, y, z) - W(x, y - 1, z)) * g.rdy);
+    }
+    __syncthreads();
+    const int i = i0 + tx, j = j0 + ty;
+    if (i >= g.Nx || j >= g.Ny) return;
+    auto sq = [](FT a) { return a * a; };
+    // ℑ over the four edges around the cell, in the reference's order (a₀₀ + a₁₀, a₀₁ + a₁₁)
+    auto I4 = [](FT a, FT b, FT c, FT d) { return FT(0.5) * (FT(0.5) * (a + b) + FT(0.5) * (c + d)); };
+    for (int z = 0; z < KT; ++z) {
+        const int k = k0 + z;
+        if (k >= g.Nz) break;
+        const FT Dz = FT(2) * M.dzc(k);
+        const FT S11 = (U(tx + 1, ty, z) - U(tx, ty, z)) * g.rdx;
+        const FT S22 = (V(tx, ty + 1, z) - V(tx, ty, z)) * g.rdy;
+        const FT S33 = fz ? FT(0) : (W(tx, ty, z + 1) - W(tx, ty, z)) * M.rdzc(k);
+        // edge values: x·y edges (i, j), (i+1, j), (i, j+1), (i+1, j+1) at level k; x·z edges
+        // (i, k), (i+1, k), (i, k+1), (i+1, k+1); y·z edges (j, k), (j+1, k), (j, k+1), (j+1, k+1)
+        const int a0 = i12(tx, ty, z), a1 = i12(tx + 1, ty, z), a2 = i12(tx, ty + 1, z), a3 = i12(tx + 1, ty + 1, z);
+        const int b0 = i13(tx, ty, z), b1 = i13(tx + 1, ty, z), b2 = i13(tx, ty, z + 1), b3 = i13(tx + 1, ty, z + 1);
+        const int c0 = i23(tx, ty, z), c1 = i23(tx, ty + 1, z), c2 = i23(tx, ty, z + 1), c3 = i23(tx, ty + 1, z + 1);
+        const FT xv[4] = {s.dxv[a0], s.dxv[a1], s.dxv[a2], s.dxv[a3]};
+        const FT yu[4] = {s.dyu[a0], s.dyu[a1], s.dyu[a2], s.dyu[a3]};
+        const FT xw[4] = {s.dxw[b0], s.dxw[b1], s.dxw[b2], s.dxw[b3]};
+        const FT zu[4] = {s.dzu[b0], s.dzu[b1], s.dzu[b2], s.dzu[b3]};
+        const FT yw[4] = {s.dyw[i23x(tx, ty, z)], s.dyw[i23x(tx, ty + 1, z)], s.dyw[i23x(tx, ty, z + 1)],
+                          s.dyw[i23x(tx, ty + 1, z + 1)]};
+        const FT zv[4] = {s.dzv[c0], s.dzv[c1], s.dzv[c2], s.dzv[c3]};
+        FT s12[4], s13[4], s23[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            s12[q] = FT(0.5) * (yu[q] + xv[q]);
+            s13[q] = FT(0.5) * (zu[q] + xw[q]);
+            s23[q] = FT(0.5) * (zv[q] + yw[q]);
+        }
+        auto IP = [&](const FT* a, const FT* b) { return I4(a[0] * b[0], a[1] * b[1], a[2] * b[2], a[3] * b[3]); };
+        auto I = [&](const FT* a) { return I4(a[0], a[1], a[2], a[3]); };
+        const FT xv2 = IP(xv, xv), yu2 = IP(yu, yu), xw2 = IP(xw, xw), zu2 = IP(zu, zu), yw2 = IP(yw, yw), zv2 = IP(zv, zv);
+        const FT q = sq(S11) + sq(S22) + sq(S33) + xv2 + yu2 + xw2 + zu2 + yw2 + zv2;
+        const FT d2 = FT(3) / (FT(1) / sq(Dx) + FT(1) / sq(Dy) + FT(1) / sq(Dz));
+        FT nsgs = FT(0);
+        if (q != FT(0)) {
+            const FT r1 = S11 * sq(S11) + S22 * xv2 + S33 * xw2 + FT(2) * S11 * IP(xv, s12) + FT(2) * S11 * IP(xw, s13) +
+                          FT(2) * I(xv) * I(xw) * I(s23);
+            const FT r2 = S11 * yu2 + S22 * sq(S22) + S33 * yw2 + FT(2) * S22 * IP(yu, s12) + FT(2) * I(yu) * I(yw) * I(s13) +
+                          FT(2) * S22 * IP(yw, s23);
+            const FT r3 = S11 * zu2 + S22 * zv2 + S33 * sq(S33) + FT(2) * I(zu) * I(zv) * I(s12) + FT(2) * S33 * IP(zu, s13) +
+                          FT(2) * S33 * IP(zv, s23);
+            const FT r = r1 + r2 + r3;
+            nsgs = -P.C * d2 * (r - FT(0)) / q;
+        }
+        const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        nu_out[idx] = fmax(FT(0), nsgs);
+        if (kap_out && has_c) {
+            // tracer gradients at the six faces, Δ̃-weighted
+            const FT Dz1 = FT(2) * M.dzc(k + 1);
+            const FT cx0 = Dx * ((C(tx, ty, z) - C(tx - 1, ty, z)) * g.rdx);
+            const FT cx1 = Dx * ((C(tx + 1, ty, z) - C(tx, ty, z)) * g.rdx);
+            const FT cy0 = Dy * ((C(tx, ty, z) - C(tx, ty - 1, z)) * g.rdy);
+            const FT cy1 = Dy * ((C(tx, ty + 1, z) - C(tx, ty, z)) * g.rdy);
+            const FT cz0 = Dz * ((C(tx, ty, z) - C(tx, ty, z - 1)) * M.rdzf(k));
+            const FT cz1 = Dz1 * ((C(tx, ty, z + 1) - C(tx, ty, z)) * M.rdzf(k + 1));
+            const FT dxc2 = FT(0.5) * (sq(cx0) + sq(cx1)), dyc2 = FT(0.5) * (sq(cy0) + sq(cy1));
+            const FT dzc2 = FT(0.5) * (sq(cz0) + sq(cz1));
+            const FT sigma = dxc2 + dyc2 + dzc2;
+            FT ksgs = FT(0);
+            if (sigma != FT(0)) {
+                const FT ix = FT(0.5) * (cx0 + cx1), iy = FT(0.5) * (cy0 + cy1), iz = FT(0.5) * (cz0 + cz1);
+                const FT cx_ux = S11 * dxc2 + I(xv) * ix * iy + I(xw) * ix * iz;
+                // ∂y w interpolated over x and z, as the reference does (see SmemA)
+                const FT ywx = I4(s.dyw[i23x(tx, ty, z)], s.dyw[i23x(tx + 1, ty, z)], s.dyw[i23x(tx, ty, z + 1)],
+                                  s.dyw[i23x(tx + 1, ty, z + 1)]);
+                const FT cy_uy = I(yu) * iy * ix + S22 * dyc2 + ywx * iy * iz;
+                const FT cz_uz = I(zu) * iz * ix + I(zv) * iz * iy + S33 * dzc2;
+                const FT theta = cx_ux + cy_uy + cz_uz;
+                ksgs = -P.C * d2 * theta / sigma;
+            }
+            kap_out[idx] = fmax(FT(0), ksgs);
+        }
     }
 }

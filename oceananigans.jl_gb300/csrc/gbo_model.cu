@@ -740,7 +740,8 @@ struct ModelImpl : gbo_model {
         pass_smem();
         GBO_CUDA(fused_set_smem<FT>());
         GBO_CUDA(cudaFuncSetAttribute(k_smagorinsky_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::SmemS<FT>)));
-        GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::SmemA<FT>)));
+        GBO_CUDA(cudaFuncSetAttribute(k_amd_tiled_ibg<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smag::Smem<FT>)));
         // The pass kernels are shared by every model in the process: allow them the device's
         // opt-in maximum rather than this model's sizes, so a model created later never
         // lowers the limit an earlier, larger model needs.
@@ -1264,18 +1265,19 @@ struct ModelImpl : gbo_model {
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;
+            auto amd = [&](FT* kap_out) {
+                pre(G_CLOSURE);
+                if (ibg) k_amd_tiled_ibg<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, kap_out);
+                else k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemA<FT>), stream>>>(Q, nu.p, kap_out);
+                check_launch();
+            };
             Q.c = ntr > 0 ? c[0].p : nullptr;
             Q.cref = tracer_ref(0);
-            pre(G_CLOSURE);
-            k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, ntr > 0 ? kap[0].p : nullptr);
-            check_launch();
+            amd(ntr > 0 ? kap[0].p : nullptr);
             for (int n = 1; n < ntr; ++n) {
                 Q.c = c[n].p;
                 Q.cref = tracer_ref(n);
-                // viscosity recomputed identically; only κₑ of tracer n is new
-                pre(G_CLOSURE);
-                k_amd_tiled<FT><<<sgrid, sblock, sizeof(smag::Smem<FT>), stream>>>(Q, nu.p, kap[n].p);
-                check_launch();
+                amd(kap[n].p);  // viscosity recomputed identically; only κₑ of tracer n is new
             }
         }
         if (has_phy) {

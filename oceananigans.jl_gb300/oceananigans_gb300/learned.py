@@ -174,12 +174,13 @@ def collect_pairs(model, dt, steps, every=1, cg_iterations=0):
     return torch.stack(rs), torch.stack(zs), torch.stack(es), active
 
 
-def train(r, z, e, active, epochs=20, lr=1e-3, seed=0, log=None, weights=None):
+def train(r, z, e, active, epochs=20, lr=1e-3, seed=0, log=None, weights=None, on_epoch=None):
     """Fit net(r/s_r, z/s_z, active) to (e - z)/s_z over active cells, up to a constant
     (the Neumann problem's null space), for samples (r, z_fft, e) as collect_pairs returns
     them, on the GPU with the library's own kernels (GpuTrainer: tcgen05 convolutions,
     tensor-core weight gradients, Adam).  Starts from `weights` (a weight file) or from
-    initial_weights(seed).  Returns the trained weight file (FP32)."""
+    initial_weights(seed).  on_epoch(epoch, mean loss, weight file) is called after each
+    epoch.  Returns the trained weight file (FP32)."""
     torch = _torch()
     n, nz, ny, nx = r.shape
     tr = GpuTrainer((nx, ny, nz), weights, seed)
@@ -191,4 +192,6 @@ def train(r, z, e, active, epochs=20, lr=1e-3, seed=0, log=None, weights=None):
             total += tr.step(r[i].contiguous(), z[i].contiguous(), e[i].contiguous(), act, lr)
         if log:
             log("epoch %d: mean relative loss %.4e" % (ep, total / n))
+        if on_epoch:
+            on_epoch(ep, total / n, tr.weights())
     return tr.weights()

@@ -101,14 +101,86 @@ struct CPlan {
     int nrad;
     int rad[GBO_MAX_RADICES];
 };
-__host__ __device__ constexpr CPlan cplan(int n) {
+// maxr: the largest radix a stage may use (each pass kernel picks it: the register
+// butterflies of radix 8 and 16 pay off on some lengths and cost on others, measured)
+__host__ __device__ constexpr CPlan cplan(int n, int maxr = 4) {
     CPlan p{0, {}};
     int m = n;
+    if (maxr >= 16)
+        while (m % 16 == 0) { p.rad[p.nrad++] = 16; m /= 16; }
+    if (maxr >= 8)
+        while (m % 8 == 0) { p.rad[p.nrad++] = 8; m /= 8; }
     while (m % 4 == 0) { p.rad[p.nrad++] = 4; m /= 4; }
     while (m % 2 == 0) { p.rad[p.nrad++] = 2; m /= 2; }
     while (m % 3 == 0) { p.rad[p.nrad++] = 3; m /= 3; }
     while (m % 5 == 0) { p.rad[p.nrad++] = 5; m /= 5; }
     return p;
+}
+
+// Small DFTs held in registers, built from radix-4 and radix-2 layers (the Cooley-Tukey
+// factorisation; internal twiddles are the constants of the eighth and sixteenth roots of
+// unity).  sign = -1 forward, +1 inverse.
+template <typename FT>
+GBO_D void dft4r(Cx<FT>& a0, Cx<FT>& a1, Cx<FT>& a2, Cx<FT>& a3, int sign) {
+    const Cx<FT> s02 = a0 + a2, d02 = a0 - a2, s13 = a1 + a3, d13 = a1 - a3;
+    const Cx<FT> jd13 = sign < 0 ? cx(d13.im, -d13.re) : cx(-d13.im, d13.re);  // ∓i (a1 - a3)
+    a0 = s02 + s13;
+    a1 = d02 + jd13;
+    a2 = s02 - s13;
+    a3 = d02 - jd13;
+}
+// x · exp(sign 2πi m / 16) for the m that occur in the 16- and 8-point transforms
+template <typename FT>
+GBO_D Cx<FT> rot16(Cx<FT> x, int m, int sign) {
+    const FT c1 = FT(0.92387953251128675613), s1 = FT(0.38268343236508977173), h = FT(0.70710678118654752440);
+    Cx<FT> w;
+    switch (m) {
+        case 0: return x;
+        case 1: w = cx(c1, s1); break;
+        case 2: w = cx(h, h); break;
+        case 3: w = cx(s1, c1); break;
+        case 4: w = cx(FT(0), FT(1)); break;
+        case 6: w = cx(-h, h); break;
+        case 9: w = cx(-c1, -s1); break;
+        default: w = cx(FT(1), FT(0));
+    }
+    if (sign < 0) w.im = -w.im;
+    return x * w;
+}
+// X[q] = Σ_r v[r] exp(sign 2πi q r / 8)
+template <typename FT>
+GBO_D void dft8r(Cx<FT> (&v)[8], int sign) {
+    Cx<FT> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4r(e0, e1, e2, e3, sign);
+    dft4r(o0, o1, o2, o3, sign);
+    o1 = rot16(o1, 2, sign);  // ω₈ = ω₁₆²
+    o2 = rot16(o2, 4, sign);
+    o3 = rot16(o3, 6, sign);
+    v[0] = e0 + o0; v[4] = e0 - o0;
+    v[1] = e1 + o1; v[5] = e1 - o1;
+    v[2] = e2 + o2; v[6] = e2 - o2;
+    v[3] = e3 + o3; v[7] = e3 - o3;
+}
+// X[q] = Σ_r v[r] exp(sign 2πi q r / 16): four 4-point transforms over r = 4 n₁ + n₂,
+// the twiddles ω₁₆^(n₂ q₁), four 4-point transforms over n₂
+template <typename FT>
+GBO_D void dft16r(Cx<FT> (&v)[16], int sign) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4r(v[n2], v[4 + n2], v[8 + n2], v[12 + n2], sign);
+    // v[4 q1 + n2] now holds A[n2][q1]
+#pragma unroll
+    for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+        for (int q1 = 1; q1 < 4; ++q1) v[4 * q1 + n2] = rot16(v[4 * q1 + n2], n2 * q1, sign);
+    Cx<FT> X[16];
+#pragma unroll
+    for (int q1 = 0; q1 < 4; ++q1) {
+        Cx<FT> a0 = v[4 * q1], a1 = v[4 * q1 + 1], a2 = v[4 * q1 + 2], a3 = v[4 * q1 + 3];
+        dft4r(a0, a1, a2, a3, sign);
+        X[q1] = a0; X[q1 + 4] = a1; X[q1 + 8] = a2; X[q1 + 12] = a3;
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = X[q];
 }
 
 template <typename FT, int N, int R, int NS, bool IL>
@@ -136,7 +208,15 @@ __device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* 
             v[r] = a;
         }
         Cx<FT> V[R];
-        if (R == 2) {
+        if constexpr (R == 16) {
+            dft16r<FT>(v, sign);
+#pragma unroll
+            for (int q = 0; q < R; ++q) V[q] = v[q];
+        } else if constexpr (R == 8) {
+            dft8r<FT>(v, sign);
+#pragma unroll
+            for (int q = 0; q < R; ++q) V[q] = v[q];
+        } else if (R == 2) {
             V[0] = v[0] + v[1];
             V[1] = v[0] - v[1];
         } else if (R == 4) {
@@ -166,23 +246,23 @@ __device__ __forceinline__ void fft_stage(const Cx<FT>* __restrict__ A, Cx<FT>* 
     __syncthreads();
 }
 
-template <typename FT, int N, int S, int NS, bool IL>
+template <typename FT, int N, int S, int NS, bool IL, int MAXR>
 struct FFTStages {
     static __device__ __forceinline__ Cx<FT>* run(Cx<FT>* A, Cx<FT>* B, int L, int lg, int sign, const Cx<FT>* tw) {
-        constexpr CPlan p = cplan(N);
+        constexpr CPlan p = cplan(N, MAXR);
         if constexpr (S >= p.nrad) {
             return A;
         } else {
             constexpr int R = p.rad[S];
             fft_stage<FT, N, R, NS, IL>(A, B, L, lg, sign, tw);
-            return FFTStages<FT, N, S + 1, NS * R, IL>::run(B, A, L, lg, sign, tw);
+            return FFTStages<FT, N, S + 1, NS * R, IL, MAXR>::run(B, A, L, lg, sign, tw);
         }
     }
 };
 
-template <typename FT, int N, bool IL>
+template <typename FT, int N, bool IL, int MAXR>
 __device__ __forceinline__ Cx<FT>* block_fft_n(Cx<FT>* A, Cx<FT>* B, int L, int sign, const Cx<FT>* tw) {
-    return FFTStages<FT, N, 0, 1, IL>::run(A, B, L, __ffs(L) - 1, sign, tw);
+    return FFTStages<FT, N, 0, 1, IL, MAXR>::run(A, B, L, __ffs(L) - 1, sign, tw);
 }
 
 // Dispatch helper: a kernel template parameter NC (0 = runtime length) selects
@@ -190,9 +270,9 @@ __device__ __forceinline__ Cx<FT>* block_fft_n(Cx<FT>* A, Cx<FT>* B, int L, int 
 // (element (line, m) at m*L + line), used where a block's lines are columns of a
 // strided axis so that loads, scatters and butterflies are bank-conflict free; L is
 // then a power of two.  tw is the block's shared-memory copy of the twiddles.
-template <typename FT, int NC, bool IL>
+template <typename FT, int NC, bool IL, int MAXR = 4>
 __device__ __forceinline__ Cx<FT>* fft_any(Cx<FT>* A, Cx<FT>* B, int L, const FFTPlan1D& pl, int sign, const Cx<FT>* tw) {
-    if constexpr (NC > 0) return block_fft_n<FT, NC, IL>(A, B, L, sign, tw);
+    if constexpr (NC > 0) return block_fft_n<FT, NC, IL, MAXR>(A, B, L, sign, tw);
     else return block_fft<FT>(A, B, L, pl, sign, tw, IL);
 }
 
@@ -421,7 +501,10 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     cp_async_wait();
     __syncthreads();
     Cx<FT>* R = A;
-    if (mode != 2) R = fft_any<FT, NC, true>(A, B, YT, P.py, -1, T);
+    // radix-16 register butterflies in single precision (fewer shared-memory stages; measured
+    // faster on this pass, slower on the x and z passes)
+    constexpr int YR = sizeof(FT) == 4 ? 16 : 4;
+    if (mode != 2) R = fft_any<FT, NC, true, YR>(A, B, YT, P.py, -1, T);
     if (mode == 0) {
         for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
             int c = t & (YT - 1), ky = t >> ly;
@@ -438,7 +521,7 @@ __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
     }
     if (mode != 1) {
         Cx<FT>* O = (R == A) ? B : A;
-        R = fft_any<FT, NC, true>(R, O, YT, P.py, +1, T);
+        R = fft_any<FT, NC, true, YR>(R, O, YT, P.py, +1, T);
     }
     for (int t = threadIdx.x; t < YT * N; t += blockDim.x) {
         int c = t & (YT - 1), ky = t >> ly;

@@ -22,7 +22,7 @@ import re
 
 import numpy as np
 
-CANDIDATES = {"dct_columns": (4, 8, 16, 32, 64), "x_lines": (1, 2, 4, 8, 16),
+CANDIDATES = {"dct_columns": (4, 8, 16, 32, 64), "x_lines": (1, 2, 4, 8, 16, 32),
               "y_columns": (2, 4, 8, 16, 32), "levels": (1, 2, 4, 8, 16, 32)}
 GROUP = {"dct_columns": "k_dct_z", "x_lines": "k_rfft_x", "y_columns": "k_fft_y", "levels": "k_momentum"}
 

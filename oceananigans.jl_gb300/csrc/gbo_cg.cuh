@@ -37,7 +37,7 @@ enum {
 };
 // block-completion counters of the loop kernels (last block finalises the scalars)
 enum {
-    CC_DOT = 0, CC_LAP, CC_XR, CC_GAUGE,
+    CC_DOT = 0, CC_LAP, CC_XR, CC_GAUGE, CC_VINV, CC_COUNT,
     CC_N
 };
 
@@ -51,41 +51,70 @@ GBO_D double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
-// block-reduce one or two doubles and add them to device scalars
-GBO_D void block_add(double a, double* da, double b = 0.0, double* db = nullptr) {
+// Block sums in a fixed order (no floating-point atomics, so a solve is bitwise
+// reproducible): every block reduces its threads' values, stores the two partial sums at
+// its own index of part (the array after the scalar slots, s + CG_NSLOTS), and takes a
+// completion ticket; the block holding the last ticket adds all partials in block order to
+// *da (and *db) and resets the ticket.  Returns true in that block, once the totals are
+// written by its thread 0.
+GBO_D bool block_sum(double a, double* da, double b, double* db, double* part, unsigned int* ticket) {
     __shared__ double sa[32], sb[32];
-    int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
-    int wid = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
-    int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    __shared__ bool last;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int lane = tid & 31, wid = tid >> 5, nt = blockDim.x * blockDim.y, nw = (nt + 31) >> 5;
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
     a = warp_sum(a);
     b = warp_sum(b);
     if (lane == 0) { sa[wid] = a; sb[wid] = b; }
     __syncthreads();
-    if (wid == 0) {
-        a = lane < nw ? sa[lane] : 0.0;
-        b = lane < nw ? sb[lane] : 0.0;
-        a = warp_sum(a);
-        b = warp_sum(b);
-        if (lane == 0) {
-            atomicAdd(da, a);
-            if (db) atomicAdd(db, b);
-        }
+    if (tid == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < nw; ++w) { ta += sa[w]; tb += sb[w]; }
+        const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        part[2 * (size_t)bid] = ta;
+        part[2 * (size_t)bid + 1] = tb;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == nb - 1;
     }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double xa = 0.0, xb = 0.0;
+    for (unsigned q = tid; q < nb; q += nt) {
+        xa += __ldcg(part + 2 * (size_t)q);
+        xb += __ldcg(part + 2 * (size_t)q + 1);
+    }
+    xa = warp_sum(xa);
+    xb = warp_sum(xb);
+    __syncthreads();  // sa / sb are reused
+    if (lane == 0) { sa[wid] = xa; sb[wid] = xb; }
+    __syncthreads();
+    if (tid == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < nw; ++w) { ta += sa[w]; tb += sb[w]; }
+        *da += ta;
+        if (db) *db += tb;
+        *ticket = 0u;  // ready for the next launch
+        __threadfence();
+    }
+    __syncthreads();
+    return true;
 }
+// partial sums of one CG reduction launch live after the scalar slots
+GBO_D double* cg_part(double* s) { return s + CG_NSLOTS; }
 
 GBO_D int cg_parity(const double* s) { return ((int)s[CG_IT]) & 1; }
 
 // q = V∇²x with differences set to zero across faces touching immersed cells
 // (_symmetric_laplacian_operator!, conjugate_gradient_poisson_solver.jl:62-79 with
-// conditional_differences.jl:15-43).  With s, accumulates x·q into s[CG_PQ].
+// conditional_differences.jl:15-43).
 template <typename FT>
-__global__ void k_cg_laplacian(GridP<FT> g, const FT* __restrict__ x, FT* __restrict__ q, double* s) {
+__global__ void k_cg_laplacian(GridP<FT> g, const FT* __restrict__ x, FT* __restrict__ q) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i < g.Nx && j < g.Ny;
     CFld<FT> X = cfld(x, g);
     Met<FT> M(g);
-    double acc = 0.0;
     for (int k = blockIdx.z; k < g.Nz; k += gridDim.z) {
         if (!in) continue;
         const FT Ax = M.Ax(k), Ay = M.Ay(k), Az = M.Az();
@@ -98,9 +127,7 @@ __global__ void k_cg_laplacian(GridP<FT> g, const FT* __restrict__ x, FT* __rest
         const FT val = (fx(i + 1) - fx(i)) + (fy(j + 1) - fy(j)) + (fz(k + 1) - fz(k));
         const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
         q[idx] = val;
-        acc += (double)x[idx] * (double)val;
     }
-    if (s) block_add(acc, s + CG_PQ);
 }
 
 // elementwise helpers over N values (1-D grid-stride)
@@ -122,7 +149,8 @@ GBO_D FT precond_source(const Met<FT>& M, FT vr, int k, int dz_scale) { return d
 // ‖V⁻¹r‖² (VolumeInverseNorm, conjugate_gradient_poisson_solver.jl:13-34) into s[CG_NORM2]
 // and, if out, the preconditioner's right-hand side
 template <typename FT>
-__global__ void k_cg_vinv(GridP<FT> g, const FT* __restrict__ r, FT* __restrict__ out, double* s, int dz_scale) {
+__global__ void k_cg_vinv(GridP<FT> g, const FT* __restrict__ r, FT* __restrict__ out, double* s, int dz_scale,
+                          unsigned int* cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i < g.Nx && j < g.Ny;
@@ -135,7 +163,7 @@ __global__ void k_cg_vinv(GridP<FT> g, const FT* __restrict__ r, FT* __restrict_
         if (out) out[idx] = precond_source(M, vr, k, dz_scale);
         acc += (double)vr * (double)vr;
     }
-    block_add(acc, s + CG_NORM2);
+    block_sum(acc, s + CG_NORM2, 0.0, nullptr, cg_part(s), cnt + CC_VINV);
 }
 
 // Stopping rule before the first iteration: tolerance, counters, stop flag.
@@ -153,9 +181,9 @@ __global__ void k_cg_begin(double* s, double reltol, double abstol, double maxit
     if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
-// True in exactly one block: the one whose completion ticket is the last.  The
-// block's reduction atomics (issued by thread 0 in block_add) are made visible
-// before its ticket; the last block then reads the totals with L2 loads.
+// True in exactly one block: the one whose completion ticket is the last.  Each block's
+// writes of its own partial results (thread 0) are made visible before its ticket; the
+// last block then reads them all with L2 loads.
 GBO_D bool last_block(unsigned int* counter) {
     __shared__ bool last;
     const unsigned int total = gridDim.x * gridDim.y * gridDim.z;
@@ -214,9 +242,8 @@ __global__ void k_cg_dot(const FT* __restrict__ a, const FT* __restrict__ b, siz
         acc += (double)(a[t] * b[t]);
         if (rprev) acc2 += (double)(a[t] * rprev[t]);
     }
-    if (rprev) block_add(acc, s + CG_RHO0 + par, acc2, s + CG_ZRP);
-    else block_add(acc, s + CG_RHO0 + par);
-    if (last_block(cnt + CC_DOT) && threadIdx.x == 0) {
+    if (block_sum(acc, s + CG_RHO0 + par, acc2, rprev ? s + CG_ZRP : nullptr, cg_part(s), cnt + CC_DOT) &&
+        threadIdx.x == 0) {
         const bool first = s[CG_IT] == 0.0;
         const double rho = ldcg(s + CG_RHO0 + par), prev = ldcg(s + CG_RHO0 + (par ^ 1));
         // flexible (Polak-Ribière) CG for a preconditioner that varies: β = z·(r - r_prev) / ρ_prev
@@ -308,8 +335,8 @@ __global__ void k_cg_direction(GridP<FT> g, const FT* __restrict__ z, FT* __rest
             pc = pt;
         }
     }
-    block_add((double)acc, s + CG_PQ);
-    if (last_block(cnt + CC_LAP) && threadIdx.x == 0 && threadIdx.y == 0)
+    if (block_sum((double)acc, s + CG_PQ, 0.0, nullptr, cg_part(s), cnt + CC_LAP) && threadIdx.x == 0 &&
+        threadIdx.y == 0)
         s[CG_ALPHA] = ldcg(s + CG_RHO0 + par) / ldcg(s + CG_PQ);
 }
 
@@ -352,8 +379,8 @@ __global__ void k_cg_update_xr(GridP<FT> g, FT* __restrict__ x, FT* __restrict__
             }
         }
     }
-    block_add((double)ax, s + CG_SX, (double)ar, s + CG_SR);
-    if (last_block(cnt + CC_XR) && threadIdx.x == 0 && threadIdx.y == 0) {
+    if (block_sum((double)ax, s + CG_SX, (double)ar, s + CG_SR, cg_part(s), cnt + CC_XR) && threadIdx.x == 0 &&
+        threadIdx.y == 0) {
         const double n = s[CG_NACT];
         s[CG_MX] = ldcg(s + CG_SX) / n;
         s[CG_MR] = ldcg(s + CG_SR) / n;
@@ -402,8 +429,8 @@ __global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, 
             }
         }
     }
-    block_add((double)acc, s + CG_NORM2);
-    if (last_block(cnt + CC_GAUGE) && threadIdx.x == 0 && threadIdx.y == 0) {
+    if (block_sum((double)acc, s + CG_NORM2, 0.0, nullptr, cg_part(s), cnt + CC_GAUGE) && threadIdx.x == 0 &&
+        threadIdx.y == 0) {
         const double it = s[CG_IT] + 1.0;
         const double norm = sqrt(ldcg(s + CG_NORM2));
         const bool cont = it < maxiter && norm > s[CG_TOL];
@@ -422,11 +449,11 @@ __global__ void k_cg_gauge(GridP<FT> g, FT* __restrict__ x, FT* __restrict__ r, 
 
 // number of active cells (for the gauge means)
 template <typename FT>
-__global__ void k_cg_count(GridP<FT> g, double* s) {
+__global__ void k_cg_count(GridP<FT> g, double* s, unsigned int* cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double a = 0.0;
     for (int k = blockIdx.z; k < g.Nz; k += gridDim.z)
         if (i < g.Nx && j < g.Ny && !inactive_cell(g, i, j, k)) a += 1.0;
-    block_add(a, s + CG_NACT);
+    block_sum(a, s + CG_NACT, 0.0, nullptr, cg_part(s), cnt + CC_COUNT);
 }

@@ -669,11 +669,13 @@ struct ModelImpl : gbo_model {
         init_poisson(Lx, Ly);
         if (cg) {
             for (DBuf<FT>* b : {&cg_b, &cg_r, &cg_q, &cg_d, &cg_p1, &cg_x}) b->alloc(N);
-            cg_s.alloc(CG_NSLOTS);
+            // the scalar slots, then two partial sums per block of the largest CG reduction launch
+            const dim3 cgg = cg_grid();
+            cg_s.alloc(CG_NSLOTS + 2 * std::max<size_t>((size_t)cgg.x * cgg.y * cgg.z, 152 * 8));
             cg_cnt.alloc(CC_N);
             GBO_CUDA(cudaMallocHost(&h_cgs, CG_NSLOTS * sizeof(double)));
             GBO_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
-            k_cg_count<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_s.p);
+            k_cg_count<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_s.p, cg_cnt.p);
             GBO_CUDA(cudaGetLastError());
             GBO_CUDA(cudaStreamSynchronize(stream));
         }
@@ -1013,7 +1015,7 @@ struct ModelImpl : gbo_model {
         if (!ibg && !cg) { err = "the CG operator needs an immersed grid or the CG solver"; return GBO_ERR_INVALID; }
         join_caller();
         pre(G_CG);
-        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, static_cast<const FT*>(x), static_cast<FT*>(out), nullptr);
+        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, static_cast<const FT*>(x), static_cast<FT*>(out));
         check_launch();
         return sync();
     }
@@ -1026,7 +1028,7 @@ struct ModelImpl : gbo_model {
         join_caller();
         GBO_CUDA(cudaMemcpyAsync(cg_r.p, r, N * sizeof(FT), cudaMemcpyDeviceToDevice, stream));
         pre(G_CG);
-        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, cg_s.p, dzs);
+        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, rb.p, cg_s.p, dzs, cg_cnt.p);
         check_launch();
         poisson_solve(precond_solver);
         learned_correction(cg_r.p, rb.p);
@@ -1056,13 +1058,13 @@ struct ModelImpl : gbo_model {
         const int dzs = precond_solver == GBO_SOLVER_FOURIER_TRIDIAGONAL;
         double* s = cg_s.p;
         pre(G_CG);
-        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_q.p, nullptr);
+        k_cg_laplacian<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_x.p, cg_q.p);
         check_launch();
         pre(G_CG);
         k_cg_init<FT><<<lin, 256, 0, stream>>>(cg_b.p, cg_q.p, cg_r.p, N);
         check_launch();
         pre(G_CG);
-        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, pc ? rb.p : nullptr, s, dzs);
+        k_cg_vinv<FT><<<cg_grid(), blk(), 0, stream>>>(gp, cg_r.p, pc ? rb.p : nullptr, s, dzs, cg_cnt.p);
         check_launch();
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         GBO_CUDA(cudaStreamIsCapturing(stream, &cs));

@@ -77,6 +77,8 @@ def main(argv=None):
     ap.add_argument("--pairs", type=int, default=60)
     ap.add_argument("--heldout", type=int, default=40)
     ap.add_argument("--validation", type=int, default=6, help="steps whose systems choose the epoch")
+    ap.add_argument("--keep-trained", action="store_true",
+                    help="choose among the trained epochs only (not the initial weights)")
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--cg-iterations", type=int, default=4)
@@ -108,7 +110,8 @@ def main(argv=None):
         if not best or key < best["key"]:
             best.update(key=key, weights=weights, label=label)
 
-    score("initial weights", learned.initial_weights(0))
+    if not args.keep_trained:
+        score("initial weights", learned.initial_weights(0))
     t0 = time.time()
     learned.train(b, z, x, active, epochs=args.epochs, lr=args.lr, log=log,
                   on_epoch=lambda ep, loss, w: score("epoch %d" % ep, w))

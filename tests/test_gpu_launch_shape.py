@@ -8,10 +8,9 @@ bottom face itself (in the loop they are carried from the level below, in FP32 t
 the paired reconstructions), which can round differently.  Those results agree to
 rounding: 1e-13 relative L2 in FP64, 1e-6 in FP32 after three steps.
 
-The conjugate-gradient solver of an immersed grid adds its dot products' block sums with
-FP64 atomics, in whatever order the blocks finish, so two runs of the same model differ
-by rounding whatever the shape; there the preconditioner (the FFT solve the tiles act
-on) is compared bitwise and the steps to rounding."""
+The conjugate-gradient solver of an immersed grid adds its dot products' block sums in a
+fixed order, so its runs are bitwise reproducible too: two runs of one seamount model, and
+runs under other pass tiles, give equal fields."""
 import numpy as np
 import pytest
 
@@ -58,9 +57,19 @@ def test_pass_tiles_on_the_cg_preconditioner():
     assert torch.equal(za, zb)
     og.time_step_(a, dt, 3)
     og.time_step_(b, dt, 3)
-    for name in ("u", "v", "w", "b"):
-        assert cases.rel_l2(b.get(name), a.get(name)) <= 1e-13, name
-    assert cases.rel_l2(b.get("p"), a.get("p")) <= 1e-11
+    for name in ("u", "v", "w", "b", "p"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+
+
+@pytest.mark.parametrize("float_type", [np.float64, np.float32])
+def test_cg_runs_are_bitwise_reproducible(float_type):
+    c = cases.seamount((32, 32, 16), float_type=float_type, solver="cg", reltol=1e-10, abstol=1e-300)
+    a, b = c.start_gpu(), c.start_gpu()
+    og.time_step_(a, 20.0, 4)
+    og.time_step_(b, 20.0, 4)
+    for name in ("u", "v", "w", "b", "p"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+    assert a.solver_iterations == b.solver_iterations
 
 
 @pytest.mark.parametrize("kind", ["convection_fp64", "convection_fp32", "seamount"])

@@ -10,6 +10,7 @@ RK3 time step (three substeps with their pressure projections) of the whole grid
 Other workloads (--workload), each with seeded synthetic inputs of the stated
 shapes and distributions:
   convection_dynamic  the headline workload with DynamicSmagorinsky(averaging=(1, 2))
+  convection_lagrangian  the headline workload with DynamicSmagorinsky() (LagrangianAveraging)
   turbulence2d    128×128 (Periodic, Periodic, Flat), u, v ~ U[-1, 1] projected,
                   WENO5, FP64, Δt = 0.01
   stretched_amd   512×512×256 with faces z_k = -256(1 - tanh(2(1 - k/256))/tanh 2),
@@ -98,6 +99,11 @@ def _convection_dynamic_spec(size, float_type):
     return gkw, dict(ophys, closure=("DynamicSmagorinsky", {"averaging": (1, 2)})), init
 
 
+def _convection_lagrangian_spec(size, float_type):
+    gkw, ophys, init = _convection_spec(size, float_type)
+    return gkw, dict(ophys, closure="DynamicSmagorinsky"), init
+
+
 def _turbulence2d_spec(size, float_type):
     Nx, Ny = size[0], size[1]
     gkw = dict(size=(Nx, Ny), x=(0, 2 * np.pi), y=(0, 2 * np.pi), topology=("Periodic", "Periodic", "Flat"),
@@ -137,6 +143,14 @@ def _convection(size, float_type):
                    coriolis=og.FPlane(1e-4), tracers=("b",),
                    boundary_conditions={"b": og.FieldBoundaryConditions(top=og.FluxBoundaryCondition(1e-8))})
     return og.RectilinearGrid(**gkw), physics, init
+
+
+def _convection_lagrangian(size, float_type):
+    """The convection workload with DynamicSmagorinsky() (LagrangianAveraging) as the closure."""
+    import oceananigans_gb300 as og
+    grid, physics, init = _convection(size, float_type)
+    physics["closure"] = og.DynamicSmagorinsky()
+    return grid, physics, init
 
 
 def _convection_dynamic(size, float_type):
@@ -203,6 +217,9 @@ WORKLOADS = {
                        name="free_convection_%dx%dx%d_weno5_smagorinsky_lilly_fft"),
     "convection_dynamic": dict(build=_convection_dynamic, spec=_convection_dynamic_spec, size=(256, 256, 128), dtype="f32", dt=2.0,
                                cpu_size=(64, 64, 128), name="free_convection_%dx%dx%d_weno5_dynamic_smagorinsky_xy_fft"),
+    "convection_lagrangian": dict(build=_convection_lagrangian, spec=_convection_lagrangian_spec, size=(256, 256, 128),
+                                  dtype="f32", dt=2.0, cpu_size=(64, 64, 128),
+                                  name="free_convection_%dx%dx%d_weno5_dynamic_smagorinsky_lagrangian_fft"),
     "turbulence2d": dict(build=_turbulence2d, spec=_turbulence2d_spec, size=(128, 128, 1), dtype="f64", dt=0.01, cpu_size=(128, 128, 1),
                          name="turbulence2d_%dx%dx%d_weno5_fft"),
     "stretched_amd": dict(build=_stretched_amd, spec=_stretched_amd_spec, size=(512, 512, 256), dtype="f32", dt=1.0, cpu_size=(64, 64, 256),

@@ -790,6 +790,7 @@ struct Smem {
 template <typename FT>
 struct SmemS : Smem<FT> {
     FT s12[E12], s13[E13], s23[E23];
+    FT df2[KT];  // Δᶠ² = (∛(Δx Δy Δz))² of the tile's levels, one cbrt per level
 };
 }  // namespace smag
 
@@ -868,6 +869,10 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
         }
         s.s23[e] = v23 * v23;
     }
+    if (tid < KT) {
+        const FT Df = cbrt(g.dx * g.dy * M.dzc(k0 + tid));
+        s.df2[tid] = Df * Df;
+    }
     __syncthreads();
     const int i = i0 + tx, j = j0 + ty;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -891,8 +896,6 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
                              FT(0.5) * (s.s23[i23(tx, ty, z + 1)] + s.s23[i23(tx, ty + 1, z + 1)]));
         }
         FT Sig2 = tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
-        FT D3 = g.dx * g.dy * M.dzc(k);
-        FT Df = cbrt(D3);
         FT N2 = FT(0);
         if (buoy) {
             FT b1 = (s.b[bidx(tx, ty, z)] - s.b[bidx(tx, ty, z - 1)]) * M.rdzf(k);
@@ -905,7 +908,7 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
         FT vs2 = FT(1) - mn;
         FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
         FT cs2 = vs * (P.C * P.C);
-        nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * (Df * Df) * sqrt(FT(2) * Sig2);
+        nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * s.df2[z] * sqrt(FT(2) * Sig2);
     }
 }
 
@@ -973,6 +976,7 @@ GBO_D int i23x(int x, int y, int z) { return (z * (TY + 1) + y) * (TX + 1) + x; 
 template <typename FT>
 struct SmemA : Smem<FT> {
     FT dxv[E12], dyu[E12], dxw[E13], dzu[E13], dyw[E23X], dzv[E23];
+    FT d2[KT];  // δ² = 3 / (Δ̃x⁻² + Δ̃y⁻² + Δ̃z⁻²) of the tile's levels
 };
 }  // namespace smag
 
@@ -1034,10 +1038,14 @@ __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__
         const FT Dz = FT(2) * M.dzc(k);
         s.dyw[e] = (Dy / Dz) * (fz ? FT(0) : (W(x, y, z) - W(x, y - 1, z)) * g.rdy);
     }
+    auto sq = [](FT a) { return a * a; };
+    if (tid < KT) {
+        const FT Dz = FT(2) * M.dzc(k0 + tid);
+        s.d2[tid] = FT(3) / (FT(1) / sq(Dx) + FT(1) / sq(Dy) + FT(1) / sq(Dz));
+    }
     __syncthreads();
     const int i = i0 + tx, j = j0 + ty;
     if (i >= g.Nx || j >= g.Ny) return;
-    auto sq = [](FT a) { return a * a; };
     // ℑ over the four edges around the cell, in the reference's order (a₀₀ + a₁₀, a₀₁ + a₁₁)
     auto I4 = [](FT a, FT b, FT c, FT d) { return FT(0.5) * (FT(0.5) * (a + b) + FT(0.5) * (c + d)); };
     for (int z = 0; z < KT; ++z) {
@@ -1070,7 +1078,7 @@ __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__
         auto I = [&](const FT* a) { return I4(a[0], a[1], a[2], a[3]); };
         const FT xv2 = IP(xv, xv), yu2 = IP(yu, yu), xw2 = IP(xw, xw), zu2 = IP(zu, zu), yw2 = IP(yw, yw), zv2 = IP(zv, zv);
         const FT q = sq(S11) + sq(S22) + sq(S33) + xv2 + yu2 + xw2 + zu2 + yw2 + zv2;
-        const FT d2 = FT(3) / (FT(1) / sq(Dx) + FT(1) / sq(Dy) + FT(1) / sq(Dz));
+        const FT d2 = s.d2[z];
         FT nsgs = FT(0);
         if (q != FT(0)) {
             const FT r1 = S11 * sq(S11) + S22 * xv2 + S33 * xw2 + FT(2) * S11 * IP(xv, s12) + FT(2) * S11 * IP(xw, s13) +

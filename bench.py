@@ -924,6 +924,7 @@ def main():
             others = {"turbulence2d": workload_record("turbulence2d", torch, og, L, lib, steps=400),
                       "stretched_amd": workload_record("stretched_amd", torch, og, L, lib, steps=10),
                       "seamount": workload_record("seamount", torch, og, L, lib, steps=5),
+                      "convection_lagrangian": workload_record("convection_lagrangian", torch, og, L, lib, steps=5),
                       "ensemble": ensemble_record(torch, og, L, lib)}
 
     cpu = None

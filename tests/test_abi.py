@@ -180,3 +180,23 @@ def test_launch_table_entries_are_valid():
         assert 1 <= lev <= nz
         assert (nx, ny, nz, fp64, ibg) not in seen
         seen.add((nx, ny, nz, fp64, ibg))
+
+
+def test_autotune_selection_and_table_writer(tmp_path):
+    # the tuner keeps the default unless a candidate is faster by more than its margin,
+    # and writes entries the library's table parser (tuned_shape) reads
+    from oceananigans_gb300 import autotune
+    entry = {"size": [64, 64, 32], "fp64": False, "ibg": False, "kind": "rect",
+             "default": {"dct_columns": 32, "x_lines": 8, "y_columns": 16, "levels": 16},
+             "us_per_launch": {"dct_columns": {"16": 9.9, "32": 10.0},         # within the margin: keep 32
+                               "x_lines": {"4": 6.0, "8": 7.0},                # faster by 14%: take 4
+                               "y_columns": {"4": 8.0, "16": 8.5},             # faster by 6%: take 4
+                               "levels": {"2": 40.0, "16": 110.0}}}
+    assert autotune.choose(entry) == {"dct_columns": 32, "x_lines": 4, "y_columns": 4, "levels": 2}
+    entry["tuned"] = autotune.choose(entry)
+    template = os.path.join(os.path.dirname(__file__), "..", "oceananigans.jl_gb300", "csrc", "gbo_launch_table.h")
+    out = tmp_path / "table.h"
+    autotune.write_table([entry], str(out), template)
+    text = out.read_text()
+    assert "{64, 64, 32, 0, 0, 32, 4, 4, 2},  // rect" in text
+    assert text.count("// BEGIN TABLE") == 1 and "tuned_shape" in text

@@ -226,17 +226,22 @@ __global__ void k_amd(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap
 // changes no tendency and keeps those differences free of the cancellation of two
 // O(N² H²) column integrals.  Reading the field back adds the profile's part.
 // ---------------------------------------------------------------------------
+// With src (a stage's buoyancy predictor b*), the column is read from src and also stored
+// into dst (the buoyancy state), which is then the stage's copy of b* into b: one pass
+// instead of a copy kernel and this scan.
 template <typename FT>
-__global__ void k_hydrostatic(StepP<FT> P, FT* __restrict__ phy) {
+__global__ void k_hydrostatic(StepP<FT> P, FT* __restrict__ phy, const FT* __restrict__ src = nullptr,
+                              FT* __restrict__ dst = nullptr) {
     const GridP<FT>& g = P.g;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     Met<FT> M(g);
-    const FT* b = P.b;
+    const FT* b = src ? src : P.b;
     const size_t col = i + (size_t)g.Nx * j, plane = (size_t)g.Nx * g.Ny;
     const int Nz = g.Nz;
     FT bk = b[col + plane * (Nz - 1)];
+    if (dst) dst[col + plane * (Nz - 1)] = bk;
     // ℑz(b) at the top face uses the mirrored halo b[Nz+1] = b[Nz]
     FT pk = -(FT(0.5) * (bk + bk)) * M.dzf(Nz);
     phy[col + plane * (Nz - 1)] = pk;
@@ -252,6 +257,7 @@ __global__ void k_hydrostatic(StepP<FT> P, FT* __restrict__ phy) {
         for (int u = 0; u < U; ++u) {
             const int k = ka - u;
             if (k < 0) break;
+            if (dst) dst[col + plane * k] = bs[u];
             pk -= (FT(0.5) * (bs[u] + bk)) * M.dzf(k + 1);
             phy[col + plane * k] = pk;
             bk = bs[u];

@@ -1222,8 +1222,15 @@ struct ModelImpl : gbo_model {
     // Closure fields and the hydrostatic pressure anomaly of the current state: the part
     // of update_state! (update_nonhydrostatic_model_state.jl:64-83) that the next stage's
     // tendencies read.  Run after every projection, as the reference does.
-    void auxiliaries() {
+    // b_pred: the buoyancy predictor still to be stored into b (the hydrostatic scan does it,
+    // first, since the closures read b)
+    void auxiliaries(const FT* b_pred = nullptr) {
         StepP<FT> P = params();
+        if (b_pred) {
+            pre(G_HYDROSTATIC);
+            k_hydrostatic<FT><<<dim3((Nx + 31) / 32, (Ny + 7) / 8), blk(), 0, stream>>>(P, phy.p, b_pred, c[0].p);
+            check_launch();
+        }
         const dim3 sgrid((Nx + smag::TX - 1) / smag::TX, (Ny + smag::TY - 1) / smag::TY, (Nz + smag::KT - 1) / smag::KT);
         const dim3 sblock(smag::TX, smag::TY);
         if (desc.closure == GBO_CLOSURE_SMAGORINSKY_LILLY && ibg) {
@@ -1282,7 +1289,7 @@ struct ModelImpl : gbo_model {
                 amd(kap[n].p);  // viscosity recomputed identically; only κₑ of tracer n is new
             }
         }
-        if (has_phy) {
+        if (has_phy && !b_pred) {
             pre(G_HYDROSTATIC);
             k_hydrostatic<FT><<<dim3((Nx + 31) / 32, (Ny + 7) / 8), blk(), 0, stream>>>(P, phy.p);
             check_launch();
@@ -1341,7 +1348,10 @@ struct ModelImpl : gbo_model {
         // Δτ = Δt γ (first stage) or Δt (γ + ζ) with γ, ζ in the working precision
         // (nonhydrostatic_rk3_substep.jl:34-36; runge_kutta_3.jl:186-187)
         project(us.p, vs.p, flat ? nullptr : ws.p, 0.0, dtf + DTF_RDTAU + s, dtf + DTF_SCALE + s);
-        for (int n = 0; n < ntr; ++n) {
+        // the buoyancy predictor is stored into the state by the hydrostatic scan, which reads
+        // it anyway (no immersed masks to apply in between on a rectilinear grid)
+        const bool b_in_scan = has_phy && !ibg;
+        for (int n = b_in_scan ? 1 : 0; n < ntr; ++n) {
             pre(G_COPY);
             k_copy<FT><<<(unsigned)std::min<size_t>((N * sizeof(FT) / 16 + 255) / 256 + 1, 4 * 152 * 8), 256, 0, stream>>>(cs[n].p, c[n].p, N);
             check_launch();
@@ -1350,7 +1360,7 @@ struct ModelImpl : gbo_model {
         // the Lagrangian average steps once per time step, after its last projection and
         // before update_state! (runge_kutta_3.jl:163; quasi_adams_bashforth_2.jl:117)
         if (lagrangian && last) lag_step();
-        auxiliaries();
+        auxiliaries(b_in_scan ? cs[0].p : nullptr);
     }
 
     // mask_immersed_field!(model.tracers) (update_nonhydrostatic_model_state.jl:25)

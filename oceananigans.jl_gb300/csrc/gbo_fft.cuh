@@ -347,11 +347,11 @@ struct PassP {
 // ---------------------------------------------------------------------------
 template <typename FT, int NC>
 __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char fft_smem[];
     const int N = P.Nz;
     const int L = ZT / 2;  // a power of two
     const int lz = __ffs(ZT) - 1, ll = lz - 1;
-    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(fft_smem);
     Cx<FT>* B = A + L * N;
     Cx<FT>* T = B + L * N;  // twiddles of the length-N FFT
     Cx<FT>* Q = T + N;      // ω^k = exp(-iπk/(2N)) of the DCT post-processing
@@ -361,12 +361,25 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
     FT* col0 = P.rb + i0 + (size_t)P.Nx * j;
     stage_table(T, P.tw_z, N);
     stage_table(Q, P.tq_z, N);
+    // 16-byte vectors of VW columns where the rows allow them: VW consecutive reals of one
+    // level are VW / 2 consecutive complex slots of the block's layout
+    constexpr int VW = 16 / sizeof(FT);
+    const bool vec = P.Nx % VW == 0 && ZT % VW == 0 && (reinterpret_cast<uintptr_t>(P.rb) & 15) == 0;
+    const int lv = lz - (VW == 4 ? 2 : 1);  // log2(ZT / VW)
     if (!inverse) {
-        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t & (ZT - 1), k = t >> lz;
-            const bool in = i0 + c < P.Nx;
-            Cx<FT>& d = A[makhoul_dest(k, N) * L + (c >> 1)];
-            cp_async_n<sizeof(FT)>((c & 1) ? &d.im : &d.re, in ? col0 + c + plane * k : col0, !in);
+        if (vec) {
+            for (int t = threadIdx.x; t < ZT * N / VW; t += blockDim.x) {
+                const int c = (t & (ZT / VW - 1)) * VW, k = t >> lv;
+                const bool in = i0 + c < P.Nx;
+                cp_async_n<16>(&A[makhoul_dest(k, N) * L + (c >> 1)], in ? col0 + c + plane * k : col0, !in);
+            }
+        } else {
+            for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+                int c = t & (ZT - 1), k = t >> lz;
+                const bool in = i0 + c < P.Nx;
+                Cx<FT>& d = A[makhoul_dest(k, N) * L + (c >> 1)];
+                cp_async_n<sizeof(FT)>((c & 1) ? &d.im : &d.re, in ? col0 + c + plane * k : col0, !in);
+            }
         }
         cp_async_wait();
         __syncthreads();
@@ -383,16 +396,32 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
             out[(2 * l + 1) + ZT * k] = wd.im;   // X_b[k] = Im(ω^k (Z_k - Z*_{N-k}))
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t & (ZT - 1), k = t >> lz;
-            if (i0 + c < P.Nx) col0[c + plane * k] = out[c + ZT * k];
+        if (vec) {
+            for (int t = threadIdx.x; t < ZT * N / VW; t += blockDim.x) {
+                const int c = (t & (ZT / VW - 1)) * VW, k = t >> lv;
+                if (i0 + c < P.Nx)
+                    *reinterpret_cast<uint4*>(col0 + c + plane * k) = *reinterpret_cast<const uint4*>(out + c + ZT * k);
+            }
+        } else {
+            for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+                int c = t & (ZT - 1), k = t >> lz;
+                if (i0 + c < P.Nx) col0[c + plane * k] = out[c + ZT * k];
+            }
         }
     } else {
         FT* in = reinterpret_cast<FT*>(B);
-        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t & (ZT - 1), k = t >> lz;
-            const bool ok = i0 + c < P.Nx;
-            cp_async_n<sizeof(FT)>(&in[c + ZT * k], ok ? col0 + c + plane * k : col0, !ok);
+        if (vec) {
+            for (int t = threadIdx.x; t < ZT * N / VW; t += blockDim.x) {
+                const int c = (t & (ZT / VW - 1)) * VW, k = t >> lv;
+                const bool ok = i0 + c < P.Nx;
+                cp_async_n<16>(&in[c + ZT * k], ok ? col0 + c + plane * k : col0, !ok);
+            }
+        } else {
+            for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+                int c = t & (ZT - 1), k = t >> lz;
+                const bool ok = i0 + c < P.Nx;
+                cp_async_n<sizeof(FT)>(&in[c + ZT * k], ok ? col0 + c + plane * k : col0, !ok);
+            }
         }
         cp_async_wait();
         __syncthreads();
@@ -409,10 +438,19 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
         }
         __syncthreads();
         Cx<FT>* R = fft_any<FT, NC, true>(A, B, L, P.pz, +1, T);
-        for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
-            int c = t & (ZT - 1), k = t >> lz;
-            Cx<FT> z = R[makhoul_dest(k, N) * L + (c >> 1)];
-            if (i0 + c < P.Nx) col0[c + plane * k] = (c & 1) ? z.im : z.re;
+        if (vec) {
+            for (int t = threadIdx.x; t < ZT * N / VW; t += blockDim.x) {
+                const int c = (t & (ZT / VW - 1)) * VW, k = t >> lv;
+                if (i0 + c < P.Nx)
+                    *reinterpret_cast<uint4*>(col0 + c + plane * k) =
+                        *reinterpret_cast<const uint4*>(&R[makhoul_dest(k, N) * L + (c >> 1)]);
+            }
+        } else {
+            for (int t = threadIdx.x; t < ZT * N; t += blockDim.x) {
+                int c = t & (ZT - 1), k = t >> lz;
+                Cx<FT> z = R[makhoul_dest(k, N) * L + (c >> 1)];
+                if (i0 + c < P.Nx) col0[c + plane * k] = (c & 1) ? z.im : z.re;
+            }
         }
     }
 }
@@ -424,11 +462,16 @@ __global__ void k_dct_z(PassP<FT> P, int inverse, int ZT) {
 // ---------------------------------------------------------------------------
 template <typename FT, int NC>
 __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
-    extern __shared__ unsigned char smem_raw[];
-    const int M = P.Nx / 2, Nh = P.Nh;
-    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    extern __shared__ __align__(16) unsigned char fft_smem[];
+    // compile-time lengths when the kernel is instantiated for this size (constant divisors)
+    const int M = NC > 0 ? NC : P.Nx / 2, Nh = NC > 0 ? NC + 1 : P.Nh;
+    const int Nx = 2 * M;
+    constexpr int VW = 16 / sizeof(FT);
+    // whole 16-byte vectors per line, 16-byte aligned lines (the real buffer may be a caller's)
+    const bool vec = Nx % (2 * VW) == 0 && (reinterpret_cast<uintptr_t>(P.rb) & 15) == 0;
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(fft_smem);
     Cx<FT>* B = A + XL * M;
-    Cx<FT>* T = A + XL * (P.Nx + 1);  // twiddles of the half-length FFT
+    Cx<FT>* T = A + XL * (Nx + 1);    // twiddles of the half-length FFT
     Cx<FT>* X = T + M;                // the real-FFT split twiddles
     const int nlines = P.Ny * P.Nz;
     const int line0 = blockIdx.x * XL;
@@ -436,9 +479,13 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
     stage_table(T, P.tw_xh, M);
     stage_table(X, P.tw_x, M);
     if (!inverse) {
-        const FT* src = P.rb + (size_t)line0 * P.Nx;
+        const FT* src = P.rb + (size_t)line0 * Nx;
         FT* As = reinterpret_cast<FT*>(A);  // interleaving x[2m], x[2m+1] is exactly re, im
-        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) cp_async_n<sizeof(FT)>(&As[t], src + t, false);
+        if (vec) {
+            for (int t = threadIdx.x; t < L * Nx / VW; t += blockDim.x) cp_async_n<16>(&As[t * VW], src + t * VW, false);
+        } else {
+            for (int t = threadIdx.x; t < L * Nx; t += blockDim.x) cp_async_n<sizeof(FT)>(&As[t], src + t, false);
+        }
         cp_async_wait();
         __syncthreads();
         Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, -1, T);
@@ -470,9 +517,14 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
         }
         __syncthreads();
         Cx<FT>* R = fft_any<FT, NC, false>(A, B, L, P.px_half, +1, T);
-        FT* dst = P.rb + (size_t)line0 * P.Nx;
+        FT* dst = P.rb + (size_t)line0 * Nx;
         const FT* Rs = reinterpret_cast<const FT*>(R);
-        for (int t = threadIdx.x; t < L * P.Nx; t += blockDim.x) dst[t] = Rs[t];
+        if (vec) {
+            for (int t = threadIdx.x; t < L * Nx / VW; t += blockDim.x)
+                reinterpret_cast<uint4*>(dst)[t] = reinterpret_cast<const uint4*>(Rs)[t];
+        } else {
+            for (int t = threadIdx.x; t < L * Nx; t += blockDim.x) dst[t] = Rs[t];
+        }
     }
 }
 
@@ -483,10 +535,10 @@ __global__ void k_rfft_x(PassP<FT> P, int inverse, int XL) {
 // ---------------------------------------------------------------------------
 template <typename FT, int NC>
 __global__ void k_fft_y(PassP<FT> P, int mode, int YT) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char fft_smem[];
     const int N = P.Ny, Nh = P.Nh;
     const int ly = __ffs(YT) - 1;  // YT is a power of two
-    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(smem_raw);
+    Cx<FT>* A = reinterpret_cast<Cx<FT>*>(fft_smem);
     Cx<FT>* B = A + YT * N;
     Cx<FT>* T = B + YT * N;  // twiddles of the length-N FFT
     const int kz = blockIdx.y;

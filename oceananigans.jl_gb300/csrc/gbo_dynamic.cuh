@@ -1,31 +1,37 @@
 // gbo_dynamic.cuh -- DynamicSmagorinsky (turbulence_closure_implementations/Smagorinskys/
 // dynamic_coefficient.jl, scale_invariant_operators.jl:94-188) with either averaging.
 //
+// The test filter ⟨f⟩ = (6 f + the six face neighbours) / 12 (scale_invariant_operators.jl:
+// 94-104) of products of interpolated strains makes LM and MM wide stencils; the tiled
+// kernels at the end of this file (k_dyn_sigma_tiled, k_lm_mm_tiled) stage a block's
+// velocities, filtered velocities and centre products in shared memory and evaluate them
+// once per point (see there).
+//
 // Averaged over x and y (averaging = (1, 2)), per state update:
-//   k_dyn_sigma   Σ = √(ΣᵢⱼΣᵢⱼ) of the resolved strain and Σ̄ = √(Σ̄ᵢⱼΣ̄ᵢⱼ) of the strain of
-//                 the test-filtered velocities, one cell per thread (_compute_Σ!, _compute_Σ̄!);
-//   k_dyn_lm      Lᵢⱼ Mᵢⱼ and Mᵢⱼ Mᵢⱼ per cell (LM_and_MM), summed per block in FP64;
-//   k_dyn_coef    per level: 𝒥ᴸᴹ, 𝒥ᴹᴹ = the x-y means of LM and MM (Field(Average(…, dims=(1, 2)))),
-//                 c² = max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ, or 0 where 𝒥ᴹᴹ ≤ 0
-//                 (square_smagorinsky_coefficient);
-//   k_smagorinsky νₑ = c² Δᶠ² √(2Σ²) with the level's c² (_compute_smagorinsky_viscosity!).
+//   k_dyn_sigma_tiled  Σ = √(ΣᵢⱼΣᵢⱼ) of the resolved strain and Σ̄ = √(Σ̄ᵢⱼΣ̄ᵢⱼ) of the strain
+//                      of the test-filtered velocities (_compute_Σ!, _compute_Σ̄!);
+//   k_lm_mm_tiled      Lᵢⱼ Mᵢⱼ and Mᵢⱼ Mᵢⱼ per cell (LM_and_MM);
+//   k_dyn_tile_sums    their FP64 sums per 32 × 8 tile of a level;
+//   k_dyn_coef         per level: 𝒥ᴸᴹ, 𝒥ᴹᴹ = the x-y means of LM and MM
+//                      (Field(Average(…, dims=(1, 2)))), c² = max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ,
+//                      or 0 where 𝒥ᴹᴹ ≤ 0 (square_smagorinsky_coefficient);
+//   k_smagorinsky      νₑ = c² Δᶠ² √(2Σ²) with the level's c² (_compute_smagorinsky_viscosity!).
 //
 // LagrangianAveraging (dynamic_coefficient.jl:364-487): 𝒥ᴸᴹ, 𝒥ᴹᴹ are fields relaxed along
 // trajectories once per time step, after the step's last projection
 // (step_closure_prognostics!):
-//   k_dyn_sigma   Σ, Σ̄ of the velocities as they are at that point (see LagC);
-//   k_lag_lm      LM, MM per cell, written over 𝒥 after 𝒥 was copied to 𝒥⁻;
-//   k_lag_step    T = 1.5 Δᶠ (𝒥ᴸᴹ⁻𝒥ᴹᴹ⁻)^(-1/8),
-//                 ε = τ / (1 + τ) with τ = Δt / T, the departure point x - clamp(u Δt, ±Δ),
-//                 𝒥 = ε (LM, MM) + (1 - ε) trilinear(𝒥⁻ at the departure point)
-//                 (_lagrangian_average_LM_MM!);
-//   k_lag_tick    previous_compute_time = clock.time (the FP64 clock of the update);
+//   k_dyn_sigma_tiled  Σ, Σ̄ of the velocities as they are at that point (see LagC);
+//   k_lm_mm_tiled      LM, MM per cell, written over 𝒥 after 𝒥 was copied to 𝒥⁻;
+//   k_lag_step         T = 1.5 Δᶠ (𝒥ᴸᴹ⁻𝒥ᴹᴹ⁻)^(-1/8), ε = τ / (1 + τ) with τ = Δt / T, the
+//                      departure point x - clamp(u Δt, ±Δ), 𝒥 = ε (LM, MM) + (1 - ε)
+//                      trilinear(𝒥⁻ at the departure point) (_lagrangian_average_LM_MM!);
+//   k_lag_tick         previous_compute_time = clock.time (the FP64 clock of the update);
 // and per state update k_smagorinsky with the cell's c² = max(𝒥ᴸᴹ, min) / 𝒥ᴹᴹ.  At set!
 // with velocities (initialize_closure_fields!, :407-437) both fields take the domain means
-// of LM and MM (k_lag_lm, k_lag_sum, k_lag_init_mean, k_lag_fill).
+// of LM and MM (k_lm_mm_tiled, k_lag_sum, k_lag_init_mean, k_lag_fill).
 //
-// The stencil kernels (k_dyn_sigma, k_dyn_lm, k_lag_lm) are instantiated in gbo_dynamic_f32.cu / _f64.cu
-// and launched through the dyn_launch_* functions declared at the end.
+// The tiled kernels are instantiated in gbo_dynamic_f32.cu / _f64.cu and launched through
+// the dyn_launch_* functions.
 //
 // The halo conventions are the stored fields' (CFld / WFld): one mirrored layer below and
 // above the domain for Center fields and Σ, Σ̄ (fill_halo_regions_flux.jl:14-15), zero
@@ -38,20 +44,7 @@ constexpr int TX = 32, TY = 8;
 constexpr int COEF_THREADS = 256;
 }  // namespace dyn
 
-// The test filter: ⟨f⟩ = (6 f + the six face neighbours) / 12 (scale_invariant_operators.jl:94-104).
-template <typename FT, class F>
-GBO_D FT test_filter(const F& f, int i, int j, int k) {
-    return (FT(6) * f(i, j, k) + f(i + 1, j, k) + f(i - 1, j, k) + f(i, j + 1, k) + f(i, j - 1, k) + f(i, j, k + 1) +
-            f(i, j, k - 1)) / FT(12);
-}
-
-template <typename FT, class A>
-struct Filtered {
-    A a;
-    GBO_D FT operator()(int i, int j, int k) const { return test_filter<FT>(a, i, j, k); }
-};
-
-// The three velocity accessors a strain (StrainT) is taken of.
+// The three velocity accessors the tiled kernels stage their tiles through.
 template <class CU, class CW>
 struct Vel {
     CU u, v;
@@ -59,15 +52,6 @@ struct Vel {
 };
 template <typename FT>
 using PlainVel = Vel<CFld<FT>, WFld<FT>>;
-
-// The velocities seen through the test filter: the strain of these (StrainT) is Σ̄ᵢⱼ,
-// ∂ of ⟨u⟩ at the reference's locations (scale_invariant_operators.jl:110-150).
-template <typename FT, class V>
-using FiltVel = Vel<Filtered<FT, decltype(V::u)>, Filtered<FT, decltype(V::w)>>;
-template <typename FT, class V>
-GBO_D FiltVel<FT, V> filtered(const V& vel) {
-    return FiltVel<FT, V>{{vel.u}, {vel.v}, {vel.w}};
-}
 
 // The velocities as step_closure_prognostics! sees them: the interior holds the projected
 // velocities, while the halos still hold what they were filled with before the
@@ -92,144 +76,6 @@ struct LagW {
 };
 template <typename FT>
 using LagVel = Vel<LagC<FT>, LagW<FT>>;
-
-// ΣᵢⱼΣᵢⱼ at a cell centre of a 3-D grid (ΣᵢⱼΣᵢⱼᶜᶜᶜ, Σ̄ᵢⱼΣ̄ᵢⱼᶜᶜᶜ)
-template <typename FT, class ST>
-GBO_D FT strain_sq(const ST& S, int i, int j, int k) {
-    auto sq = [](FT x) { return x * x; };
-    FT s11 = S.S11(i, j, k), s22 = S.S22(i, j, k), s33 = S.S33(i, j, k);
-    FT tr = s11 * s11 + s22 * s22 + s33 * s33;
-    FT ixy = FT(0.5) * (FT(0.5) * (sq(S.S12(i, j, k)) + sq(S.S12(i + 1, j, k))) +
-                        FT(0.5) * (sq(S.S12(i, j + 1, k)) + sq(S.S12(i + 1, j + 1, k))));
-    FT ixz = FT(0.5) * (FT(0.5) * (sq(S.S13(i, j, k)) + sq(S.S13(i + 1, j, k))) +
-                        FT(0.5) * (sq(S.S13(i, j, k + 1)) + sq(S.S13(i + 1, j, k + 1))));
-    FT iyz = FT(0.5) * (FT(0.5) * (sq(S.S23(i, j, k)) + sq(S.S23(i, j + 1, k))) +
-                        FT(0.5) * (sq(S.S23(i, j, k + 1)) + sq(S.S23(i, j + 1, k + 1))));
-    return tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
-}
-
-template <typename FT, class V>
-__global__ void k_dyn_sigma(GridP<FT> g, V vel, FT* __restrict__ sig, FT* __restrict__ sigb) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.Nx || j >= g.Ny) return;
-    StrainT<FT, V> S(g, vel);
-    const FiltVel<FT, V> FF = filtered<FT>(vel);
-    StrainT<FT, FiltVel<FT, V>> SB(g, FF);
-    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-    sig[idx] = sqrt(strain_sq<FT>(S, i, j, k));
-    sigb[idx] = sqrt(strain_sq<FT>(SB, i, j, k));
-}
-
-// Lᵢⱼ Mᵢⱼ and Mᵢⱼ Mᵢⱼ at a cell (LM_and_MM, dynamic_coefficient.jl:254-276) from the
-// Leonard stresses Lᵢⱼ = ⟨uᵢuⱼ⟩ − ⟨uᵢ⟩⟨uⱼ⟩ and Mᵢⱼ = 2Δᶠ²(⟨ΣΣᵢⱼ⟩ − ᾱ²β Σ̄Σ̄ᵢⱼ), ᾱ² = 4, β = 1
-// (scale_invariant_operators.jl:152-188); products of velocities are formed at cell
-// centres from ℑ of the face values, as the reference does.
-template <typename FT, class V>
-GBO_D void lm_mm_point(const GridP<FT>& g, const V& vel, const FT* __restrict__ sig, const FT* __restrict__ sigb,
-                       int i, int j, int k, FT& LM, FT& MM) {
-    const auto& u = vel.u;
-    const auto& v = vel.v;
-    const auto& w = vel.w;
-    const CFld<FT> sg = cfld(sig, g), sb = cfld(sigb, g);
-    StrainT<FT, V> S(g, vel);
-    const FiltVel<FT, V> FF = filtered<FT>(vel);
-    StrainT<FT, FiltVel<FT, V>> SB(g, FF);
-    Met<FT> M(g);
-    const FT h = FT(0.5);
-    auto sq = [](FT x) { return x * x; };
-
-    // Leonard stresses
-    auto ixu = [&](int a, int b, int c) { return h * (u(a, b, c) + u(a + 1, b, c)); };
-    auto iyv = [&](int a, int b, int c) { return h * (v(a, b, c) + v(a, b + 1, c)); };
-    auto izw = [&](int a, int b, int c) { return h * (w(a, b, c) + w(a, b, c + 1)); };
-    auto u1u1 = [&](int a, int b, int c) { return h * (sq(u(a, b, c)) + sq(u(a + 1, b, c))); };
-    auto u2u2 = [&](int a, int b, int c) { return h * (sq(v(a, b, c)) + sq(v(a, b + 1, c))); };
-    auto u3u3 = [&](int a, int b, int c) { return h * (sq(w(a, b, c)) + sq(w(a, b, c + 1))); };
-    auto u1u2 = [&](int a, int b, int c) { return ixu(a, b, c) * iyv(a, b, c); };
-    auto u1u3 = [&](int a, int b, int c) { return ixu(a, b, c) * izw(a, b, c); };
-    auto u2u3 = [&](int a, int b, int c) { return iyv(a, b, c) * izw(a, b, c); };
-    const FT fu0 = FF.u(i, j, k), fu1 = FF.u(i + 1, j, k);
-    const FT fv0 = FF.v(i, j, k), fv1 = FF.v(i, j + 1, k);
-    const FT fw0 = FF.w(i, j, k), fw1 = FF.w(i, j, k + 1);
-    const FT ixfu = h * (fu0 + fu1), iyfv = h * (fv0 + fv1), izfw = h * (fw0 + fw1);
-    const FT L11 = test_filter<FT>(u1u1, i, j, k) - h * (sq(fu0) + sq(fu1));
-    const FT L22 = test_filter<FT>(u2u2, i, j, k) - h * (sq(fv0) + sq(fv1));
-    const FT L33 = test_filter<FT>(u3u3, i, j, k) - h * (sq(fw0) + sq(fw1));
-    const FT L12 = test_filter<FT>(u1u2, i, j, k) - ixfu * iyfv;
-    const FT L13 = test_filter<FT>(u1u3, i, j, k) - ixfu * izfw;
-    const FT L23 = test_filter<FT>(u2u3, i, j, k) - iyfv * izfw;
-
-    // Σ Σᵢⱼ at cell centres (off-diagonal strains interpolated from the edges) and their filter
-    auto ss11 = [&](int a, int b, int c) { return sg(a, b, c) * S.S11(a, b, c); };
-    auto ss22 = [&](int a, int b, int c) { return sg(a, b, c) * S.S22(a, b, c); };
-    auto ss33 = [&](int a, int b, int c) { return sg(a, b, c) * S.S33(a, b, c); };
-    auto ss12 = [&](int a, int b, int c) {
-        return sg(a, b, c) * (h * (h * (S.S12(a, b, c) + S.S12(a + 1, b, c)) + h * (S.S12(a, b + 1, c) + S.S12(a + 1, b + 1, c))));
-    };
-    auto ss13 = [&](int a, int b, int c) {
-        return sg(a, b, c) * (h * (h * (S.S13(a, b, c) + S.S13(a + 1, b, c)) + h * (S.S13(a, b, c + 1) + S.S13(a + 1, b, c + 1))));
-    };
-    auto ss23 = [&](int a, int b, int c) {
-        return sg(a, b, c) * (h * (h * (S.S23(a, b, c) + S.S23(a, b + 1, c)) + h * (S.S23(a, b, c + 1) + S.S23(a, b + 1, c + 1))));
-    };
-    const FT sbar = sb(i, j, k);
-    const FT bb11 = sbar * SB.S11(i, j, k);
-    const FT bb22 = sbar * SB.S22(i, j, k);
-    const FT bb33 = sbar * SB.S33(i, j, k);
-    const FT bb12 = sbar * (h * (h * (SB.S12(i, j, k) + SB.S12(i + 1, j, k)) + h * (SB.S12(i, j + 1, k) + SB.S12(i + 1, j + 1, k))));
-    const FT bb13 = sbar * (h * (h * (SB.S13(i, j, k) + SB.S13(i + 1, j, k)) + h * (SB.S13(i, j, k + 1) + SB.S13(i + 1, j, k + 1))));
-    const FT bb23 = sbar * (h * (h * (SB.S23(i, j, k) + SB.S23(i, j + 1, k)) + h * (SB.S23(i, j, k + 1) + SB.S23(i, j + 1, k + 1))));
-    const FT Df = cbrt(g.dx * g.dy * M.dzc(k));
-    const FT f2 = FT(2) * (Df * Df);
-    const FT M11 = f2 * (test_filter<FT>(ss11, i, j, k) - FT(4) * bb11);
-    const FT M22 = f2 * (test_filter<FT>(ss22, i, j, k) - FT(4) * bb22);
-    const FT M33 = f2 * (test_filter<FT>(ss33, i, j, k) - FT(4) * bb33);
-    const FT M12 = f2 * (test_filter<FT>(ss12, i, j, k) - FT(4) * bb12);
-    const FT M13 = f2 * (test_filter<FT>(ss13, i, j, k) - FT(4) * bb13);
-    const FT M23 = f2 * (test_filter<FT>(ss23, i, j, k) - FT(4) * bb23);
-    LM = L11 * M11 + L22 * M22 + L33 * M33 + FT(2) * L12 * M12 + FT(2) * L13 * M13 + FT(2) * L23 * M23;
-    MM = M11 * M11 + M22 * M22 + M33 * M33 + FT(2) * M12 * M12 + FT(2) * M13 * M13 + FT(2) * M23 * M23;
-}
-
-// LM and MM of every cell of a 32×8 tile of one level, summed in FP64 in a fixed order;
-// part[2 (k·nb + b)] and part[2 (k·nb + b) + 1] hold the tile's two sums.
-template <typename FT, class V>
-__global__ void __launch_bounds__(dyn::TX * dyn::TY) k_dyn_lm(GridP<FT> g, V vel, const FT* __restrict__ sig,
-                                                               const FT* __restrict__ sigb, double* __restrict__ part) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    double lm = 0.0, mm = 0.0;
-    if (i < g.Nx && j < g.Ny) {
-        FT a, b;
-        lm_mm_point<FT>(g, vel, sig, sigb, i, j, k, a, b);
-        lm = (double)a;
-        mm = (double)b;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        lm += __shfl_down_sync(0xffffffffu, lm, o);
-        mm += __shfl_down_sync(0xffffffffu, mm, o);
-    }
-    __shared__ double sh[2][dyn::TY];
-    if (threadIdx.x == 0) {
-        sh[0][threadIdx.y] = lm;
-        sh[1][threadIdx.y] = mm;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        double a = 0.0, b = 0.0;
-        for (int r = 0; r < dyn::TY; ++r) {
-            a += sh[0][r];
-            b += sh[1][r];
-        }
-        const size_t nb = (size_t)gridDim.x * gridDim.y;
-        const size_t q = (size_t)k * nb + blockIdx.x + (size_t)gridDim.x * blockIdx.y;
-        part[2 * q] = a;
-        part[2 * q + 1] = b;
-    }
-}
 
 // One block per level: the x-y means 𝒥ᴸᴹ, 𝒥ᴹᴹ from the tile sums, then the squared
 // coefficient max(𝒥ᴸᴹ, 𝒥ᴸᴹ_min) / 𝒥ᴹᴹ where 𝒥ᴹᴹ > 0, else 0 (the reference multiplies by
@@ -350,22 +196,6 @@ GBO_D double lag_trilinear(const FT* __restrict__ a, const GridP<FT>& g, int i0,
            x * y * (1 - z) * (double)lag_prev(a, g, i1, j1, k0) + x * y * z * (double)lag_prev(a, g, i1, j1, k1);
 }
 
-// LM and MM of every cell (_compute_LM_MM!), stored in FT as the reference's fields are
-template <typename FT, class V>
-__global__ void __launch_bounds__(dyn::TX * dyn::TY) k_lag_lm(GridP<FT> g, V vel, const FT* __restrict__ sig,
-                                                               const FT* __restrict__ sigb, FT* __restrict__ lm,
-                                                               FT* __restrict__ mm) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.Nx || j >= g.Ny) return;
-    FT a, b;
-    lm_mm_point<FT>(g, vel, sig, sigb, i, j, k, a, b);
-    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
-    lm[idx] = a;
-    mm[idx] = b;
-}
-
 // FP64 sums of two arrays per block (grid-stride, fixed order for a fixed launch):
 // part[2 b], part[2 b + 1]
 template <typename FT>
@@ -403,8 +233,8 @@ __global__ void __launch_bounds__(256) k_lag_sum(const FT* __restrict__ a, const
 // elapsed time Δt = clock.time - previous_compute_time is FP64 (the clock's type), so the
 // relaxation weight and the departure point are formed in FP64 as the reference's
 // promotion does; the fields are stored in FT.
-// LM and MM of this step are read from jlm / jmm (k_lag_lm wrote them there after 𝒥 was
-// copied to 𝒥⁻); each thread reads and then overwrites its own cell only.
+// LM and MM of this step are read from jlm / jmm (k_lm_mm_tiled wrote them there after 𝒥
+// was copied to 𝒥⁻); each thread reads and then overwrites its own cell only.
 template <typename FT>
 __global__ void __launch_bounds__(dyn::TX * dyn::TY) k_lag_step(LagP<FT> P) {
     const GridP<FT>& g = P.g;
@@ -502,17 +332,262 @@ __global__ void k_lag_fill(const double* __restrict__ clock, FT* __restrict__ jl
     }
 }
 
-// Launchers of the stencil kernels, instantiated for float and double in gbo_dynamic_f32.cu / _f64.cu
-// (their own translation unit: the LM / MM stencil is large).
+// Launchers of the stencil kernels (the tiled forms below), instantiated for float and
+// double in gbo_dynamic_f32.cu / _f64.cu (their own translation units: the stencils are large).
 template <typename FT>
-void dyn_launch_sigma(dim3 grid, dim3 block, cudaStream_t st, const GridP<FT>& g, const PlainVel<FT>& vel, FT* sig,
-                      FT* sigb);
+void dyn_launch_sigma(cudaStream_t st, const GridP<FT>& g, const PlainVel<FT>& vel, FT* sig, FT* sigb);
 template <typename FT>
-void dyn_launch_sigma(dim3 grid, dim3 block, cudaStream_t st, const GridP<FT>& g, const LagVel<FT>& vel, FT* sig,
-                      FT* sigb);
+void dyn_launch_sigma(cudaStream_t st, const GridP<FT>& g, const LagVel<FT>& vel, FT* sig, FT* sigb);
 template <typename FT>
-void dyn_launch_lm_sums(dim3 grid, dim3 block, cudaStream_t st, const GridP<FT>& g, const PlainVel<FT>& vel,
-                        const FT* sig, const FT* sigb, double* part);
+void dyn_launch_lm(cudaStream_t st, const GridP<FT>& g, const PlainVel<FT>& vel, const FT* sig, const FT* sigb, FT* lm,
+                   FT* mm);
 template <typename FT>
-void dyn_launch_lag_lm(dim3 grid, dim3 block, cudaStream_t st, const GridP<FT>& g, const LagVel<FT>& vel,
-                       const FT* sig, const FT* sigb, FT* lm, FT* mm);
+void dyn_launch_lm(cudaStream_t st, const GridP<FT>& g, const LagVel<FT>& vel, const FT* sig, const FT* sigb, FT* lm,
+                   FT* mm);
+template <typename FT>
+cudaError_t dyn_set_smem();
+
+// ---------------------------------------------------------------------------
+// Tiled Σ, Σ̄ and LM, MM.  The per-point forms above evaluate the test filter of products
+// of interpolated strains: every cell recomputes the filtered velocities and the centre
+// products of its neighbours many times over.  A 32 × 4 × 2 block instead stages the
+// velocities of its cells and two points around them (through the same accessors, so
+// every halo rule, the predictor halos of the Lagrangian update included, is the
+// accessor's), forms the filtered velocities and the twelve centre products of the
+// Leonard and model tensors once per point of the tile and one point around it, and then
+// every cell evaluates LM_and_MM's expressions (the reference's order of operations, each
+// strain as StrainT forms it) from those values.
+// Positions beyond one point outside the domain feed only cells outside it; their
+// indices are clamped so that every read stays in bounds.
+// ---------------------------------------------------------------------------
+namespace dtile {
+constexpr int TX = 32, TY = 4, KT = 2, NT = TX * TY * KT;
+constexpr int RX = TX + 4, RY = TY + 4, RZ = KT + 4, RS = RX * RY * RZ;  // velocities: -2 .. +1 beyond the tile
+constexpr int QX = TX + 2, QY = TY + 2, QZ = KT + 2, QS = QX * QY * QZ;  // filtered velocities, products: -1 .. +1
+GBO_D int ri(int x, int y, int z) { return ((z + 2) * RY + (y + 2)) * RX + (x + 2); }
+GBO_D int qi(int x, int y, int z) { return ((z + 1) * QY + (y + 1)) * QX + (x + 1); }
+enum { Q11 = 0, Q22, Q33, Q12, Q13, Q23, M11, M22, M33, M12, M13, M23, NQ };
+template <typename FT>
+struct SmemS {
+    FT u[RS], v[RS], w[RS];
+    FT fu[QS], fv[QS], fw[QS];
+};
+template <typename FT>
+struct SmemL : SmemS<FT> {
+    FT q[NQ][QS];
+};
+// a domain index for a tile position: at most one point beyond the domain is a real halo
+// point; farther ones only feed cells outside the domain
+GBO_D int clamp_far(int i, int n) { return i > n + 1 ? n + 1 : i; }
+}  // namespace dtile
+
+// stage u, v, w of the tile and two points around it, then the filtered velocities over
+// the tile and one point around it
+template <typename FT, class V>
+GBO_D void dtile_stage(dtile::SmemS<FT>& s, const GridP<FT>& g, const V& vel, int i0, int j0, int k0, int tid) {
+    using namespace dtile;
+    for (int e = tid; e < RS; e += NT) {
+        const int x = e % RX - 2, y = (e / RX) % RY - 2, z = e / (RX * RY) - 2;
+        const int gi = clamp_far(i0 + x, g.Nx), gj = clamp_far(j0 + y, g.Ny), gk = k0 + z;
+        s.u[e] = vel.u(gi, gj, gk);
+        s.v[e] = vel.v(gi, gj, gk);
+        s.w[e] = vel.w(gi, gj, gk);
+    }
+    __syncthreads();
+    // the test filter ⟨f⟩ = (6 f + the six face neighbours) / 12, the neighbours in the order x, y, z
+    auto tf = [&](const FT* a, int x, int y, int z) {
+        return (FT(6) * a[ri(x, y, z)] + a[ri(x + 1, y, z)] + a[ri(x - 1, y, z)] + a[ri(x, y + 1, z)] + a[ri(x, y - 1, z)] +
+                a[ri(x, y, z + 1)] + a[ri(x, y, z - 1)]) / FT(12);
+    };
+    for (int e = tid; e < QS; e += NT) {
+        const int x = e % QX - 1, y = (e / QX) % QY - 1, z = e / (QX * QY) - 1;
+        s.fu[e] = tf(s.u, x, y, z);
+        s.fv[e] = tf(s.v, x, y, z);
+        s.fw[e] = tf(s.w, x, y, z);
+    }
+}
+
+// ΣᵢⱼΣᵢⱼ of the strain of velocities held at tile positions (index function ix), at cell
+// (x, y, z) of level k: Σ₁₁² + Σ₂₂² + Σ₃₃² + 2 ℑxy(Σ₁₂²) + 2 ℑxz(Σ₁₃²) + 2 ℑyz(Σ₂₃²)
+template <typename FT, class IX>
+GBO_D FT dtile_strain_sq(const FT* u, const FT* v, const FT* w, IX ix, const GridP<FT>& g, const Met<FT>& M, int x,
+                         int y, int z, int k0) {
+    auto sq = [](FT a) { return a * a; };
+    const int k = k0 + z;
+    const FT s11 = (u[ix(x + 1, y, z)] - u[ix(x, y, z)]) * g.rdx;
+    const FT s22 = (v[ix(x, y + 1, z)] - v[ix(x, y, z)]) * g.rdy;
+    const FT s33 = (w[ix(x, y, z + 1)] - w[ix(x, y, z)]) * M.rdzc(k);
+    const FT tr = s11 * s11 + s22 * s22 + s33 * s33;
+    auto S12 = [&](int a, int b) {
+        return FT(0.5) * ((u[ix(a, b, z)] - u[ix(a, b - 1, z)]) * g.rdy + (v[ix(a, b, z)] - v[ix(a - 1, b, z)]) * g.rdx);
+    };
+    auto S13 = [&](int a, int c) {
+        return FT(0.5) * ((u[ix(a, y, c)] - u[ix(a, y, c - 1)]) * M.rdzf(k0 + c) + (w[ix(a, y, c)] - w[ix(a - 1, y, c)]) * g.rdx);
+    };
+    auto S23 = [&](int b, int c) {
+        return FT(0.5) * ((v[ix(x, b, c)] - v[ix(x, b, c - 1)]) * M.rdzf(k0 + c) + (w[ix(x, b, c)] - w[ix(x, b - 1, c)]) * g.rdy);
+    };
+    const FT ixy = FT(0.5) * (FT(0.5) * (sq(S12(x, y)) + sq(S12(x + 1, y))) + FT(0.5) * (sq(S12(x, y + 1)) + sq(S12(x + 1, y + 1))));
+    const FT ixz = FT(0.5) * (FT(0.5) * (sq(S13(x, z)) + sq(S13(x + 1, z))) + FT(0.5) * (sq(S13(x, z + 1)) + sq(S13(x + 1, z + 1))));
+    const FT iyz = FT(0.5) * (FT(0.5) * (sq(S23(y, z)) + sq(S23(y + 1, z))) + FT(0.5) * (sq(S23(y, z + 1)) + sq(S23(y + 1, z + 1))));
+    return tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
+}
+
+// Σ = √(ΣᵢⱼΣᵢⱼ) and Σ̄ = √(Σ̄ᵢⱼΣ̄ᵢⱼ) of every cell (_compute_Σ!, _compute_Σ̄!)
+template <typename FT, class V>
+__global__ void __launch_bounds__(dtile::NT) k_dyn_sigma_tiled(GridP<FT> g, V vel, FT* __restrict__ sig,
+                                                                FT* __restrict__ sigb) {
+    using namespace dtile;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    SmemS<FT>& s = *reinterpret_cast<SmemS<FT>*>(dyn_smem);
+    const int tid = threadIdx.x + TX * (threadIdx.y + TY * threadIdx.z);
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
+    dtile_stage<FT>(s, g, vel, i0, j0, k0, tid);
+    __syncthreads();
+    const int x = threadIdx.x, y = threadIdx.y, z = threadIdx.z;
+    const int i = i0 + x, j = j0 + y, k = k0 + z;
+    if (i >= g.Nx || j >= g.Ny || k >= g.Nz) return;
+    Met<FT> M(g);
+    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+    sig[idx] = sqrt(dtile_strain_sq<FT>(s.u, s.v, s.w, ri, g, M, x, y, z, k0));
+    sigb[idx] = sqrt(dtile_strain_sq<FT>(s.fu, s.fv, s.fw, qi, g, M, x, y, z, k0));
+}
+
+// LM and MM of every cell (LM_and_MM, dynamic_coefficient.jl:254-276) into lm, mm
+template <typename FT, class V>
+__global__ void __launch_bounds__(dtile::NT) k_lm_mm_tiled(GridP<FT> g, V vel, const FT* __restrict__ sig,
+                                                            const FT* __restrict__ sigb, FT* __restrict__ lm,
+                                                            FT* __restrict__ mm) {
+    using namespace dtile;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    SmemL<FT>& s = *reinterpret_cast<SmemL<FT>*>(dyn_smem);
+    const int tid = threadIdx.x + TX * (threadIdx.y + TY * threadIdx.z);
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
+    dtile_stage<FT>(s, g, vel, i0, j0, k0, tid);
+    Met<FT> M(g);
+    const CFld<FT> sg = cfld(sig, g);
+    const FT h = FT(0.5);
+    auto sq = [](FT a) { return a * a; };
+    const FT* U = s.u;
+    const FT* Vv = s.v;
+    const FT* W = s.w;
+    // the centre products of the tile and one point around it, each formed once
+    for (int e = tid; e < QS; e += NT) {
+        const int a = e % QX - 1, b = (e / QX) % QY - 1, c = e / (QX * QY) - 1;
+        const int gk = k0 + c;
+        const FT ua = U[ri(a, b, c)], ua1 = U[ri(a + 1, b, c)];
+        const FT vb = Vv[ri(a, b, c)], vb1 = Vv[ri(a, b + 1, c)];
+        const FT wc = W[ri(a, b, c)], wc1 = W[ri(a, b, c + 1)];
+        s.q[Q11][e] = h * (sq(ua) + sq(ua1));
+        s.q[Q22][e] = h * (sq(vb) + sq(vb1));
+        s.q[Q33][e] = h * (sq(wc) + sq(wc1));
+        const FT ixu = h * (ua + ua1), iyv = h * (vb + vb1), izw = h * (wc + wc1);
+        s.q[Q12][e] = ixu * iyv;
+        s.q[Q13][e] = ixu * izw;
+        s.q[Q23][e] = iyv * izw;
+        const FT sgv = sg(dtile::clamp_far(i0 + a, g.Nx), dtile::clamp_far(j0 + b, g.Ny), gk);
+        s.q[M11][e] = sgv * ((ua1 - ua) * g.rdx);
+        s.q[M22][e] = sgv * ((vb1 - vb) * g.rdy);
+        s.q[M33][e] = sgv * ((wc1 - wc) * M.rdzc(gk));
+        auto S12 = [&](int p, int r) {
+            return FT(0.5) * ((U[ri(p, r, c)] - U[ri(p, r - 1, c)]) * g.rdy + (Vv[ri(p, r, c)] - Vv[ri(p - 1, r, c)]) * g.rdx);
+        };
+        auto S13 = [&](int p, int t) {
+            return FT(0.5) * ((U[ri(p, b, t)] - U[ri(p, b, t - 1)]) * M.rdzf(k0 + t) + (W[ri(p, b, t)] - W[ri(p - 1, b, t)]) * g.rdx);
+        };
+        auto S23 = [&](int r, int t) {
+            return FT(0.5) * ((Vv[ri(a, r, t)] - Vv[ri(a, r, t - 1)]) * M.rdzf(k0 + t) + (W[ri(a, r, t)] - W[ri(a, r - 1, t)]) * g.rdy);
+        };
+        s.q[M12][e] = sgv * (h * (h * (S12(a, b) + S12(a + 1, b)) + h * (S12(a, b + 1) + S12(a + 1, b + 1))));
+        s.q[M13][e] = sgv * (h * (h * (S13(a, c) + S13(a + 1, c)) + h * (S13(a, c + 1) + S13(a + 1, c + 1))));
+        s.q[M23][e] = sgv * (h * (h * (S23(b, c) + S23(b + 1, c)) + h * (S23(b, c + 1) + S23(b + 1, c + 1))));
+    }
+    __syncthreads();
+    const int x = threadIdx.x, y = threadIdx.y, z = threadIdx.z;
+    const int i = i0 + x, j = j0 + y, k = k0 + z;
+    if (i >= g.Nx || j >= g.Ny || k >= g.Nz) return;
+    auto TF = [&](int qn) {
+        const FT* a = s.q[qn];
+        return (FT(6) * a[qi(x, y, z)] + a[qi(x + 1, y, z)] + a[qi(x - 1, y, z)] + a[qi(x, y + 1, z)] + a[qi(x, y - 1, z)] +
+                a[qi(x, y, z + 1)] + a[qi(x, y, z - 1)]) / FT(12);
+    };
+    const FT* FU = s.fu;
+    const FT* FV = s.fv;
+    const FT* FW = s.fw;
+    const FT fu0 = FU[qi(x, y, z)], fu1 = FU[qi(x + 1, y, z)];
+    const FT fv0 = FV[qi(x, y, z)], fv1 = FV[qi(x, y + 1, z)];
+    const FT fw0 = FW[qi(x, y, z)], fw1 = FW[qi(x, y, z + 1)];
+    const FT ixfu = h * (fu0 + fu1), iyfv = h * (fv0 + fv1), izfw = h * (fw0 + fw1);
+    const FT L11 = TF(Q11) - h * (sq(fu0) + sq(fu1));
+    const FT L22 = TF(Q22) - h * (sq(fv0) + sq(fv1));
+    const FT L33 = TF(Q33) - h * (sq(fw0) + sq(fw1));
+    const FT L12 = TF(Q12) - ixfu * iyfv;
+    const FT L13 = TF(Q13) - ixfu * izfw;
+    const FT L23 = TF(Q23) - iyfv * izfw;
+    // the strain of the filtered velocities at the cell and its edges
+    auto SB12 = [&](int p, int r) {
+        return FT(0.5) * ((FU[qi(p, r, z)] - FU[qi(p, r - 1, z)]) * g.rdy + (FV[qi(p, r, z)] - FV[qi(p - 1, r, z)]) * g.rdx);
+    };
+    auto SB13 = [&](int p, int t) {
+        return FT(0.5) * ((FU[qi(p, y, t)] - FU[qi(p, y, t - 1)]) * M.rdzf(k0 + t) + (FW[qi(p, y, t)] - FW[qi(p - 1, y, t)]) * g.rdx);
+    };
+    auto SB23 = [&](int r, int t) {
+        return FT(0.5) * ((FV[qi(x, r, t)] - FV[qi(x, r, t - 1)]) * M.rdzf(k0 + t) + (FW[qi(x, r, t)] - FW[qi(x, r - 1, t)]) * g.rdy);
+    };
+    const size_t idx = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+    const FT sbar = __ldg(sigb + idx);
+    const FT bb11 = sbar * ((fu1 - fu0) * g.rdx);
+    const FT bb22 = sbar * ((fv1 - fv0) * g.rdy);
+    const FT bb33 = sbar * ((fw1 - fw0) * M.rdzc(k));
+    const FT bb12 = sbar * (h * (h * (SB12(x, y) + SB12(x + 1, y)) + h * (SB12(x, y + 1) + SB12(x + 1, y + 1))));
+    const FT bb13 = sbar * (h * (h * (SB13(x, z) + SB13(x + 1, z)) + h * (SB13(x, z + 1) + SB13(x + 1, z + 1))));
+    const FT bb23 = sbar * (h * (h * (SB23(y, z) + SB23(y + 1, z)) + h * (SB23(y, z + 1) + SB23(y + 1, z + 1))));
+    const FT Df = cbrt(g.dx * g.dy * M.dzc(k));
+    const FT f2 = FT(2) * (Df * Df);
+    const FT m11 = f2 * (TF(M11) - FT(4) * bb11);
+    const FT m22 = f2 * (TF(M22) - FT(4) * bb22);
+    const FT m33 = f2 * (TF(M33) - FT(4) * bb33);
+    const FT m12 = f2 * (TF(M12) - FT(4) * bb12);
+    const FT m13 = f2 * (TF(M13) - FT(4) * bb13);
+    const FT m23 = f2 * (TF(M23) - FT(4) * bb23);
+    lm[idx] = L11 * m11 + L22 * m22 + L33 * m33 + FT(2) * L12 * m12 + FT(2) * L13 * m13 + FT(2) * L23 * m23;
+    mm[idx] = m11 * m11 + m22 * m22 + m33 * m33 + FT(2) * m12 * m12 + FT(2) * m13 * m13 + FT(2) * m23 * m23;
+}
+
+// The per-level sums of the per-cell LM, MM arrays: a 32 × 8 block per tile of a level,
+// each warp's row summed by a shuffle tree in FP64, the rows in order; k_dyn_coef sums the
+// tiles of a level in order (a fixed order, so the mean is reproducible)
+template <typename FT>
+__global__ void __launch_bounds__(dyn::TX * dyn::TY) k_dyn_tile_sums(const FT* __restrict__ lmv, const FT* __restrict__ mmv,
+                                                                     int Nx, int Ny, double* __restrict__ part) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    double lm = 0.0, mm = 0.0;
+    if (i < Nx && j < Ny) {
+        const size_t idx = i + (size_t)Nx * (j + (size_t)Ny * k);
+        lm = (double)lmv[idx];
+        mm = (double)mmv[idx];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lm += __shfl_down_sync(0xffffffffu, lm, o);
+        mm += __shfl_down_sync(0xffffffffu, mm, o);
+    }
+    __shared__ double sh[2][dyn::TY];
+    if (threadIdx.x == 0) {
+        sh[0][threadIdx.y] = lm;
+        sh[1][threadIdx.y] = mm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double a = 0.0, b = 0.0;
+        for (int r = 0; r < dyn::TY; ++r) {
+            a += sh[0][r];
+            b += sh[1][r];
+        }
+        const size_t nb = (size_t)gridDim.x * gridDim.y;
+        const size_t q = (size_t)k * nb + blockIdx.x + (size_t)gridDim.x * blockIdx.y;
+        part[2 * q] = a;
+        part[2 * q + 1] = b;
+    }
+}

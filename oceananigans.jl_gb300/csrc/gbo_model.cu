@@ -448,7 +448,7 @@ struct ModelImpl : gbo_model {
     std::vector<std::vector<double>> cref_h;
     DBuf<double> tstage, tmean;
     // DynamicSmagorinsky: Σ, Σ̄, per-tile LM/MM sums, and per level c², 𝒥ᴸᴹ, 𝒥ᴹᴹ
-    DBuf<FT> dyn_sig, dyn_sigb, dyn_cs2, dyn_jlm, dyn_jmm;
+    DBuf<FT> dyn_sig, dyn_sigb, dyn_cs2, dyn_jlm, dyn_jmm, dyn_lmv, dyn_mmv;  // lmv, mmv: per-cell LM, MM (x-y average)
     DBuf<double> dyn_part;
     // DynamicSmagorinsky with LagrangianAveraging: 𝒥ᴸᴹ, 𝒥ᴹᴹ and their previous values, the
     // FP64 clock slots (LAG_*), the cell-centre z, and where the step being recorded reads
@@ -530,7 +530,8 @@ struct ModelImpl : gbo_model {
         tmean.free_();
         t_rdzf64.free_(); t_dzc64.free_(); t_lx64.free_(); t_ly64.free_(); t_ws.free_(); t_kbot.free_();
         for (DBuf<C>* b : {&cb, &tw_xh, &tw_x, &tw_y, &tw_z, &tq_z}) b->free_();
-        for (DBuf<FT>* b : {&dyn_sig, &dyn_sigb, &dyn_cs2, &dyn_jlm, &dyn_jmm, &lag_jlm, &lag_jmm, &lag_jlm_prev, &lag_jmm_prev})
+        for (DBuf<FT>* b : {&dyn_sig, &dyn_sigb, &dyn_cs2, &dyn_jlm, &dyn_jmm, &dyn_lmv, &dyn_mmv, &lag_jlm, &lag_jmm,
+                            &lag_jlm_prev, &lag_jmm_prev})
             b->free_();
         dyn_part.free_();
         lag_s.free_();
@@ -632,6 +633,11 @@ struct ModelImpl : gbo_model {
                                             (size_t)2 * LAG_SUM_BLOCKS));
             for (DBuf<FT>* b : {&dyn_cs2, &dyn_jlm, &dyn_jmm}) b->alloc(Nz);
             lagrangian = md->closure_averaging == GBO_AVERAGING_LAGRANGIAN;
+            GBO_CUDA(dyn_set_smem<FT>());
+            if (!lagrangian) {
+                dyn_lmv.alloc(N);
+                dyn_mmv.alloc(N);
+            }
         }
         if (lagrangian) {
             for (DBuf<FT>* b : {&lag_jlm, &lag_jmm, &lag_jlm_prev, &lag_jmm_prev}) b->alloc(N);
@@ -1150,10 +1156,10 @@ struct ModelImpl : gbo_model {
         const LagVel<FT> V = lag_vel(hu, hv, hw);
         const dim3 dg = dyn_grid(), db(dyn::TX, dyn::TY);
         pre(G_CLOSURE);
-        dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
+        dyn_launch_sigma<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p);
         check_launch();
         pre(G_CLOSURE);
-        dyn_launch_lag_lm<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
+        dyn_launch_lm<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
         check_launch();
         const int nparts = LAG_SUM_BLOCKS;
         pre(G_CLOSURE);
@@ -1175,7 +1181,7 @@ struct ModelImpl : gbo_model {
         const LagVel<FT> V = lag_vel(us.p, vs.p, ws.p);
         const dim3 dg = dyn_grid(), db(dyn::TX, dyn::TY);
         pre(G_CLOSURE);
-        dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
+        dyn_launch_sigma<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p);
         check_launch();
         const unsigned cb = (unsigned)std::min<size_t>((N * sizeof(FT) / 16 + 255) / 256 + 1, 4 * 152 * 8);
         pre(G_COPY);
@@ -1185,7 +1191,7 @@ struct ModelImpl : gbo_model {
         k_copy<FT><<<cb, 256, 0, stream>>>(lag_jmm.p, lag_jmm_prev.p, N);
         check_launch();
         pre(G_CLOSURE);
-        dyn_launch_lag_lm<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
+        dyn_launch_lm<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p, lag_jlm.p, lag_jmm.p);
         check_launch();
         LagP<FT> L{};
         L.g = gp;
@@ -1257,10 +1263,13 @@ struct ModelImpl : gbo_model {
             const dim3 dg((Nx + dyn::TX - 1) / dyn::TX, (Ny + dyn::TY - 1) / dyn::TY, Nz), db(dyn::TX, dyn::TY);
             pre(G_CLOSURE);
             const PlainVel<FT> V{host_cfld(u.p), host_cfld(v.p), host_wfld(w.p)};
-            dyn_launch_sigma<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p);
+            dyn_launch_sigma<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p);
             check_launch();
             pre(G_CLOSURE);
-            dyn_launch_lm_sums<FT>(dg, db, stream, gp, V, dyn_sig.p, dyn_sigb.p, dyn_part.p);
+            dyn_launch_lm<FT>(stream, gp, V, dyn_sig.p, dyn_sigb.p, dyn_lmv.p, dyn_mmv.p);
+            check_launch();
+            pre(G_CLOSURE);
+            k_dyn_tile_sums<FT><<<dg, db, 0, stream>>>(dyn_lmv.p, dyn_mmv.p, Nx, Ny, dyn_part.p);
             check_launch();
             pre(G_CLOSURE);
             k_dyn_coef<FT><<<Nz, dyn::COEF_THREADS, 0, stream>>>(dyn_part.p, (int)(dg.x * dg.y), (double)Nx * (double)Ny,

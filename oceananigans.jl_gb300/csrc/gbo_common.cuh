@@ -134,6 +134,11 @@ struct WFld {
     const FT* __restrict__ a;
     int Nx, Ny, Nz;
     GBO_D FT far(int i, int j, int k) const { return (*this)(wrapt(i, Nx), wrapt(j, Ny), k); }
+    // the column at offset c = i + Nx j of the domain, at face k
+    GBO_D FT col(size_t c, int k) const {
+        if (k <= 0 || k >= Nz) return FT(0);
+        return ldg(a + c + (size_t)Nx * Ny * k);
+    }
     GBO_D FT operator()(int i, int j, int k) const {
         if (k <= 0 || k >= Nz) return FT(0);
         i = wrapi(i, Nx);

@@ -132,6 +132,7 @@ struct LagP {
     FT* jmm;
     FT lm_min;                            // minimum_numerator in FT
     double x0, y0, dx, dy;                // cell centres x0 + (i + 1/2) Δx (FP64)
+    double xc0, yc0;                      // the first centres x0 + 0.5 Δx, y0 + 0.5 Δy
     const double* __restrict__ zc;        // z of the Nz cell centres (FP64)
     double dz1;                           // Δzᶜ of the first cell (regular z)
     int stretched;
@@ -145,10 +146,12 @@ GBO_D T jl_max(T a, T b) { return (isnan(a) || isnan(b)) ? a + b : (a > b ? a : 
 GBO_D double jl_clamp(double x, double lo, double hi) { return x > hi ? hi : (x < lo ? lo : x); }
 
 // interpolator (Utils/interpolation.jl:34-42): i⁻ = unsafe_trunc(Int, fi), ξ = mod(fi, 1)
-// on a 1-based fractional index; returns the 0-based lower index.
+// on a 1-based fractional index; returns the 0-based lower index.  The remainder of
+// fi / 1 is fi - trunc(fi): both are exact (the fractional bits of fi are representable),
+// so this is fmod(fi, 1) without its general-divisor reduction
 GBO_D int lag_interpolator(double fi, double& xi) {
     const int lo = (int)fi;
-    const double r = fmod(fi, 1.0);
+    const double r = fi - trunc(fi);
     xi = (r == 0.0) ? 0.0 : (r < 0.0 ? r + 1.0 : r);
     return lo - 1;
 }
@@ -259,8 +262,8 @@ __global__ void __launch_bounds__(dyn::TX * dyn::TY) k_lag_step(LagP<FT> P) {
     const double ddx = jl_clamp((double)P.vel.u.in(i, j, k) * dt, -(double)g.dx, (double)g.dx);
     const double ddy = jl_clamp((double)P.vel.v.in(i, j, k) * dt, -(double)g.dy, (double)g.dy);
     const double ddz = jl_clamp((double)P.vel.w.in(i, j, k) * dt, -(double)dzk, (double)dzk);
-    const double fi = (x - ddx - (P.x0 + 0.5 * P.dx)) / P.dx + 1;
-    const double fj = (y - ddy - (P.y0 + 0.5 * P.dy)) / P.dy + 1;
+    const double fi = (x - ddx - P.xc0) / P.dx + 1;
+    const double fj = (y - ddy - P.yc0) / P.dy + 1;
     const double fk = lag_frac_z(P, z - ddz);
     double xi, yi, zi;
     const int i0 = lag_interpolator(fi, xi), j0 = lag_interpolator(fj, yi), k0 = lag_interpolator(fk, zi);

@@ -4,7 +4,8 @@
 //   * a 32 x 8 block owns a tile of (i, j) columns and marches upward over a
 //     chunk of levels k;
 //   * x / y stencils (halo 3) are read from shared-memory planes that the block
-//     loads once per level (periodic wrap and the z-halo rules applied at load);
+//     loads once per level (periodic wrap and the z-halo rules applied at load), in
+//     16-byte chunks where the grid allows (x halo widened to 4 for that);
 //   * z stencils come from per-thread register windows that slide with k;
 //   * every face flux is evaluated once: a thread computes the fluxes through
 //     the west, south and top faces of its control volumes, exchanges west and
@@ -13,6 +14,7 @@
 // The extra faces on the tile's east column and north row are evaluated by
 // warps 0 and 1 after their own work.
 #pragma once
+#include <initializer_list>
 #include "gbo_step.cuh"
 
 // Resident blocks per SM the FP32 kernel is compiled for (registers are capped so
@@ -23,15 +25,22 @@
 
 namespace fused {
 
-constexpr int TX = 32, TY = 8, H = 3;
-constexpr int PX = TX + 2 * H, PY = TY + 2 * H, PS = PX * PY;
+// planes: x halo 4 (a row is 40 values: 16-byte chunks starting on a multiple of four
+// columns), y halo 3
+constexpr int TX = 32, TY = 8, H = 3, HX = 4;
+constexpr int PX = TX + 2 * HX, PY = TY + 2 * H, PS = PX * PY;
 constexpr int NT = TX * TY;
-constexpr int EPT = (PS + NT - 1) / NT;  // plane elements loaded per thread
+constexpr int EPT = (PS + NT - 1) / NT;  // plane elements loaded per thread (4/8-byte copies)
+// 16-byte chunks: values per chunk, chunks per row and plane, chunks per thread
+template <typename FT> constexpr int VW = 16 / (int)sizeof(FT);
+template <typename FT> constexpr int CPR = PX / VW<FT>;
+template <typename FT> constexpr int CPT = (CPR<FT> * PY + NT - 1) / NT;
+static_assert(PX % 4 == 0 && HX % 4 == 0, "plane rows must split into 16-byte chunks");
 // immersed-boundary column table: halo 4 (a centred reconstruction checks cells up to 4 away)
 constexpr int KBH = 4, KBX = TX + 2 * KBH, KBY = TY + 2 * KBH, KBS = KBX * KBY;
 GBO_D int kbidx(int x, int y) { return (y + KBH) * KBX + (x + KBH); }
 
-GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + H); }
+GBO_D int pidx(int x, int y) { return (y + H) * PX + (x + HX); }
 
 // exchange quantities (west-face values live in WX[q][ty][tx], tx = 0..TX;
 // south-face values in SY[q][ty][tx], ty = 0..TY)
@@ -41,7 +50,7 @@ enum { A_VU = 0, A_VV, A_VW, C_22, C_12N, C_23, A_CY, Q_CY, NSY };  // south fac
 // Plane rings: a level's plane stays in its slot while it is in use and the
 // next level's planes are prefetched asynchronously into the free slots.
 template <typename FT>
-struct Smem {
+struct __align__(16) Smem {
     FT U[3][PS], V[3][PS], W[3][PS];  // u, v: levels k-1, k (+k+1 in flight); w: faces k, k+1 (+k+2)
     FT NU[4][PS];                      // νₑ: k-1, k, k+1 (+k+2)
     FT PH[2][PS];                      // pHY′: k (+k+1)
@@ -69,26 +78,43 @@ GBO_D void cp_async(FT* dst, const FT* src, bool zero) {
     else
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(zero ? 0 : 8));
 }
+// Asynchronous 16-byte copy (both addresses 16-byte aligned); zero = write zeros.
+GBO_D void cp_async16(void* dst, const void* src, bool zero) {
+    unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(zero ? 0 : 16));
+}
 GBO_D void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 GBO_D void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
-// Per-thread plane-load plan: offsets (within one z-level) of the wrapped
-// (i, j) points this thread copies; identical for every level.
+// Per-thread plane-load plan: offsets (within one z-level) of the wrapped (i, j) points
+// this thread copies; identical for every level.  With vec, the thread copies 16-byte
+// chunks (plane chunk tid + m NT): a chunk starts on a column that is a multiple of the
+// chunk width, and with Nx a multiple of it a chunk never straddles the periodic seam,
+// so each chunk is one contiguous, aligned run of the row it wraps to.
 struct PlanePlan {
     int off[EPT];
     int n;
+    int vec;
 };
 template <typename FT>
-GBO_D PlanePlan make_plan(const GridP<FT>& g, int i0, int j0, int tid) {
+GBO_D PlanePlan make_plan(const GridP<FT>& g, int i0, int j0, int tid, int vec) {
     PlanePlan p;
     p.n = 0;
+    p.vec = vec;
 #pragma unroll
     for (int m = 0; m < EPT; ++m) {
         int e = tid + m * NT;
         p.off[m] = 0;
-        if (e < PS) {
-            int px = e % PX, py = e / PX;
-            int gi = wrapm(i0 + px - H, g.Nx), gj = wrapm(j0 + py - H, g.Ny);
+        if (vec) {
+            if (m < CPT<FT> && e < CPR<FT> * PY) {
+                const int px = (e % CPR<FT>) * VW<FT>, py = e / CPR<FT>;
+                const int gi = wrapm(i0 + px - HX, g.Nx), gj = wrapm(j0 + py - H, g.Ny);
+                p.off[m] = gi + g.Nx * gj;
+                p.n = m + 1;
+            }
+        } else if (e < PS) {
+            const int px = e % PX, py = e / PX;
+            const int gi = wrapm(i0 + px - HX, g.Nx), gj = wrapm(j0 + py - H, g.Ny);
             p.off[m] = gi + g.Nx * gj;
             p.n = m + 1;
         }
@@ -107,9 +133,25 @@ GBO_D int zsrc_w(int k, int Nz) { return (k <= 0 || k >= Nz) ? -1 : k; }
 template <typename FT>
 GBO_D void issue_plane(FT* dst, const FT* src, int zl, size_t plane, const PlanePlan& pp, int tid) {
     const FT* base = src + (zl < 0 ? 0 : (size_t)zl * plane);
+    if (pp.vec) {
 #pragma unroll
-    for (int m = 0; m < EPT; ++m)
-        if (m < pp.n) cp_async(dst + tid + m * NT, base + pp.off[m], zl < 0);
+        for (int m = 0; m < CPT<FT>; ++m)
+            if (m < pp.n) cp_async16(dst + (tid + m * NT) * VW<FT>, base + pp.off[m], zl < 0);
+    } else {
+#pragma unroll
+        for (int m = 0; m < EPT; ++m)
+            if (m < pp.n) cp_async(dst + tid + m * NT, base + pp.off[m], zl < 0);
+    }
+}
+
+// Whether a launch can copy its planes in 16-byte chunks: Nx a multiple of the chunk
+// width (so is the plane size) and every field the planes come from 16-byte aligned
+template <typename FT>
+inline int planes_vec(const GridP<FT>& g, std::initializer_list<const void*> fields) {
+    if (g.Nx % VW<FT> != 0) return 0;
+    for (const void* f : fields)
+        if (f && ((size_t)f & 15) != 0) return 0;
+    return 1;
 }
 
 template <typename FT>
@@ -132,9 +174,9 @@ struct Col {
 // Column-marching fused kernel (see the file header).  TR: also advance one tracer
 // (P.c -> P.co, P.Gc) in the same march.
 template <typename FT, bool TR, int CLK, bool IBG = false>
-__global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 1) k_momentum_fused(StepP<FT> P, int kchunk) {
+__global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 1) k_momentum_fused(StepP<FT> P, int kchunk, int vec) {
     using namespace fused;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
     const GridP<FT>& g = P.g;
     Met<FT> M(g);
@@ -152,8 +194,9 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     const int Nz = g.Nz, fz = g.flatz;
     const FT Az = M.Az();
     const size_t plane = (size_t)g.Nx * g.Ny;
-    const PlanePlan pp = make_plan(g, i0, j0, tid);
+    const PlanePlan pp = make_plan(g, i0, j0, tid, vec);
     const int ii = i % g.Nx, jj = j % g.Ny;
+    const size_t ccol = (size_t)ii + (size_t)g.Nx * jj;  // this thread's column (in the domain)
 
     // ring slots: U/V slot of level k = k mod 3, W slot of face k = k mod 3,
     // NU slot of level k = k mod 4, PH/CC slot = k mod 2, KP slot = k mod 3
@@ -235,15 +278,15 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     Col<FT> c;
 #pragma unroll
     for (int o = 0; o < 7; ++o) {
-        c.uc[o] = Ug(ii, jj, kb - 3 + o);
-        c.vc[o] = Vg(ii, jj, kb - 3 + o);
-        if (TR) c.cc[o] = Cg(ii, jj, kb - 3 + o);
+        c.uc[o] = Ug.col(ccol, kb - 3 + o);
+        c.vc[o] = Vg.col(ccol, kb - 3 + o);
+        if (TR) c.cc[o] = Cg.col(ccol, kb - 3 + o);
     }
 #pragma unroll
-    for (int o = 0; o < 6; ++o) c.wc[o] = Wg(ii, jj, kb - 2 + o);
-    const FT wm3 = Wg(ii, jj, kb - 3);
+    for (int o = 0; o < 6; ++o) c.wc[o] = Wg.col(ccol, kb - 2 + o);
+    const FT wm3 = Wg.col(ccol, kb - 3);
     FT km_amd = FT(0);
-    if (TR && amd) km_amd = cfld(P.kap, g)(ii, jj, kb - 1);
+    if (TR && amd) km_amd = cfld(P.kap, g).col(ccol, kb - 1);
     cp_async_wait_all();
     __syncthreads();
     // bottom fluxes at level kb (faces kb / centre kb-1)
@@ -328,8 +371,8 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         }
         cp_async_commit();
         // ---- early loads: window tops for the next level, G⁻ of this level ----
-        const FT un = Ug(ii, jj, k + 4), vn = Vg(ii, jj, k + 4), wn = Wg(ii, jj, k + 4);
-        const FT cnext = TR ? Cg(ii, jj, k + 4) : FT(0);
+        const FT un = Ug.col(ccol, k + 4), vn = Vg.col(ccol, k + 4), wn = Wg.col(ccol, k + 4);
+        const FT cnext = TR ? Cg.col(ccol, k + 4) : FT(0);
         const size_t idx = ii + (size_t)g.Nx * jj + plane * k;
         FT Gum = FT(0), Gvm = FT(0), Gwm = FT(0), Gcm = FT(0);
         if (!P.first && inside) {
@@ -771,7 +814,9 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
 // Smagorinsky-Lilly νₑ on a shared-memory tile: the block stages u, v, w, b on a
 // (32+2) x (8+2) x (KT+2) box once (halo synthesis at load) and every thread
 // evaluates the closure for KT levels of its column from shared memory.
-// Arithmetic identical to k_smagorinsky (gbo_kernels.cuh).
+// Arithmetic identical to k_smagorinsky (gbo_kernels.cuh), its three coefficients
+// included: Lilly's, the level's c² of DynamicSmagorinsky averaged over x-y, and the
+// cell's max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ of Lagrangian averaging (b is not staged then).
 // ---------------------------------------------------------------------------
 namespace smag {
 constexpr int TX = 32, TY = 8, KT = 4;
@@ -803,7 +848,7 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
     Met<FT> M(g);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
-    const bool buoy = P.buoyancy && !g.flatz;
+    const bool buoy = P.buoyancy && !g.flatz && !P.jlm && !P.cs2;
     const int Nz = g.Nz, fz = g.flatz;
     const size_t plane = (size_t)g.Nx * g.Ny;
     // tile fill with asynchronous copies: halos synthesised as in CFld / WFld (periodic
@@ -896,19 +941,30 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
                              FT(0.5) * (s.s23[i23(tx, ty, z + 1)] + s.s23[i23(tx, ty + 1, z + 1)]));
         }
         FT Sig2 = tr + FT(2) * ixy + FT(2) * ixz + FT(2) * iyz;
-        FT N2 = FT(0);
-        if (buoy) {
-            FT b1 = (s.b[bidx(tx, ty, z)] - s.b[bidx(tx, ty, z - 1)]) * M.rdzf(k);
-            FT b2 = (s.b[bidx(tx, ty, z + 1)] - s.b[bidx(tx, ty, z)]) * M.rdzf(k + 1);
-            N2 = FT(0.5) * (b1 + b2);
+        const size_t q = i + (size_t)g.Nx * (j + (size_t)g.Ny * k);
+        FT cs2;
+        if (P.jlm) {
+            FT lm = P.jlm[q];
+            lm = isnan(lm) ? lm : (lm > P.lm_min ? lm : P.lm_min);
+            const FT mm = P.jmm[q];
+            cs2 = mm > FT(0) ? lm / mm : FT(0);
+        } else if (P.cs2) {
+            cs2 = P.cs2[k];
+        } else {
+            FT N2 = FT(0);
+            if (buoy) {
+                FT b1 = (s.b[bidx(tx, ty, z)] - s.b[bidx(tx, ty, z - 1)]) * M.rdzf(k);
+                FT b2 = (s.b[bidx(tx, ty, z + 1)] - s.b[bidx(tx, ty, z)]) * M.rdzf(k + 1);
+                N2 = FT(0.5) * (b1 + b2);
+            }
+            FT N2p = fmax(FT(0), N2);
+            FT r = P.Cb * N2p / Sig2;
+            FT mn = isnan(r) ? r : fmin(FT(1), r);
+            FT vs2 = FT(1) - mn;
+            FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
+            cs2 = vs * (P.C * P.C);
         }
-        FT N2p = fmax(FT(0), N2);
-        FT r = P.Cb * N2p / Sig2;
-        FT mn = isnan(r) ? r : fmin(FT(1), r);
-        FT vs2 = FT(1) - mn;
-        FT vs = (Sig2 == FT(0)) ? FT(0) : sqrt(vs2);
-        FT cs2 = vs * (P.C * P.C);
-        nu_out[i + (size_t)g.Nx * (j + (size_t)g.Ny * k)] = cs2 * s.df2[z] * sqrt(FT(2) * Sig2);
+        nu_out[q] = cs2 * s.df2[z] * sqrt(FT(2) * Sig2);
     }
 }
 

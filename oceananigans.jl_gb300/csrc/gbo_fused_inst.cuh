@@ -7,10 +7,14 @@
 template <typename FT, bool TR>
 void launch_fused(int closure, bool ibg, dim3 grid, dim3 block, cudaStream_t st, const StepP<FT>& P, int kchunk) {
     const size_t smem = fused::smem_bytes<FT>(closure == CL_AMD || ibg);
-    if (ibg) k_momentum_fused<FT, TR, CL_NONE, true><<<grid, block, smem, st>>>(P, kchunk);
-    else if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk);
-    else if (closure == CL_AMD) k_momentum_fused<FT, TR, CL_AMD><<<grid, block, smem, st>>>(P, kchunk);
-    else k_momentum_fused<FT, TR, CL_NONE><<<grid, block, smem, st>>>(P, kchunk);
+    // the fields whose planes the kernel copies
+    const int vec = fused::planes_vec<FT>(P.g, {P.u, P.v, P.w, closure != CL_NONE ? P.nu : nullptr,
+                                                P.has_phy ? P.phy : nullptr, TR ? P.c : nullptr,
+                                                closure == CL_AMD ? P.kap : nullptr});
+    if (ibg) k_momentum_fused<FT, TR, CL_NONE, true><<<grid, block, smem, st>>>(P, kchunk, vec);
+    else if (closure == CL_SMAG) k_momentum_fused<FT, TR, CL_SMAG><<<grid, block, smem, st>>>(P, kchunk, vec);
+    else if (closure == CL_AMD) k_momentum_fused<FT, TR, CL_AMD><<<grid, block, smem, st>>>(P, kchunk, vec);
+    else k_momentum_fused<FT, TR, CL_NONE><<<grid, block, smem, st>>>(P, kchunk, vec);
 }
 
 template <typename FT, bool TR>

@@ -1205,6 +1205,8 @@ struct ModelImpl : gbo_model {
         L.y0 = lag_y0;
         L.dx = (grid.x[1] - grid.x[0]) / Nx;
         L.dy = (grid.y[1] - grid.y[0]) / Ny;
+        L.xc0 = L.x0 + 0.5 * L.dx;
+        L.yc0 = L.y0 + 0.5 * L.dy;
         L.zc = lag_zc.p;
         L.dz1 = (double)Z.at(Z.dzc, 1);
         L.stretched = stretched_z ? 1 : 0;
@@ -1255,7 +1257,7 @@ struct ModelImpl : gbo_model {
             Q.jmm = lag_jmm.p;
             Q.lm_min = FT(desc.closure_min_numerator);
             pre(G_CLOSURE);
-            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p);
+            k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemS<FT>), stream>>>(Q, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_DYNAMIC_SMAGORINSKY) {
             // Σ and Σ̄, the tile sums of LM and MM, the per-level coefficient, then νₑ
@@ -1279,7 +1281,7 @@ struct ModelImpl : gbo_model {
             StepP<FT> Q = P;
             Q.cs2 = dyn_cs2.p;
             pre(G_CLOSURE);
-            k_smagorinsky<FT><<<grd(), blk(), 0, stream>>>(Q, nu.p);
+            k_smagorinsky_tiled<FT><<<sgrid, sblock, sizeof(smag::SmemS<FT>), stream>>>(Q, nu.p);
             check_launch();
         } else if (desc.closure == GBO_CLOSURE_AMD) {
             StepP<FT> Q = P;

@@ -18,10 +18,19 @@ template <typename FT> struct IsF32 { static constexpr bool value = false; };
 template <> struct IsF32<float> { static constexpr bool value = true; };
 
 // Division used in the WENO weights.  FP64 keeps IEEE division (the reference's
-// CPU semantics, the parity target); FP32 uses the fast reciprocal as the
-// reference's GPU backend does (ext/OceananigansCUDAExt.jl:147-171).
+// CPU semantics, the parity target).  FP32 forms a / b as the reference's GPU backend
+// does for its default weight computation (newton_div with BackendOptimizedDivision,
+// ext/OceananigansCUDAExt.jl:147,165-171): a times the approximate reciprocal
+// rcp.approx.ftz.f32 of b; the normalisation 1 / Σα takes the same reciprocal.
+GBO_D float rcp_approx(float b) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+    return r;
+}
 GBO_D double weno_div(double a, double b) { return a / b; }
-GBO_D float weno_div(float a, float b) { return __fdividef(a, b); }
+GBO_D float weno_div(float a, float b) { return a * rcp_approx(b); }
+GBO_D double weno_inv(double b) { return 1.0 / b; }
+GBO_D float weno_inv(float b) { return rcp_approx(b); }
 
 template <typename FT>
 GBO_D FT beta3(FT p0, FT p1, FT p2, int s) {
@@ -73,7 +82,7 @@ GBO_WENO_FN FT weno5v(FT s0, FT s1, FT s2, FT s3, FT s4, FT s5, bool left) {
     FT al0 = K::weno3_cstar[0] * (FT(1) + q0 * q0);
     FT al1 = K::weno3_cstar[1] * (FT(1) + q1 * q1);
     FT al2 = K::weno3_cstar[2] * (FT(1) + q2 * q2);
-    FT inv = weno_div(FT(1), (al0 + al1) + al2);
+    FT inv = weno_inv((al0 + al1) + al2);
     FT p0 = (K::weno3_p0[0] * a0 + K::weno3_p0[1] * a1) + K::weno3_p0[2] * a2;
     FT p1 = (K::weno3_p1[0] * b0 + K::weno3_p1[1] * b1) + K::weno3_p1[2] * b2;
     FT p2 = (K::weno3_p2[0] * c0 + K::weno3_p2[1] * c1) + K::weno3_p2[2] * c2;
@@ -127,14 +136,14 @@ GBO_D void weno5_2<float>(const float A[6], bool la, const float B[6], bool lb, 
     const float2 d = sub(be0, be2);
     const float2 tau = f2(fabsf(d.x), fabsf(d.y));
     const float2 e0 = add(be0, sc(K::eps)), e1 = add(be1, sc(K::eps)), e2 = add(be2, sc(K::eps));
-    const float2 q0 = f2(__fdividef(tau.x, e0.x), __fdividef(tau.y, e0.y));
-    const float2 q1 = f2(__fdividef(tau.x, e1.x), __fdividef(tau.y, e1.y));
-    const float2 q2 = f2(__fdividef(tau.x, e2.x), __fdividef(tau.y, e2.y));
+    const float2 q0 = mul(tau, f2(rcp_approx(e0.x), rcp_approx(e0.y)));
+    const float2 q1 = mul(tau, f2(rcp_approx(e1.x), rcp_approx(e1.y)));
+    const float2 q2 = mul(tau, f2(rcp_approx(e2.x), rcp_approx(e2.y)));
     const float2 al0 = mul(sc(K::weno3_cstar[0]), fma2(q0, q0, sc(1.f)));
     const float2 al1 = mul(sc(K::weno3_cstar[1]), fma2(q1, q1, sc(1.f)));
     const float2 al2 = mul(sc(K::weno3_cstar[2]), fma2(q2, q2, sc(1.f)));
     const float2 sum = add(add(al0, al1), al2);
-    const float2 inv = f2(__fdividef(1.f, sum.x), __fdividef(1.f, sum.y));
+    const float2 inv = f2(rcp_approx(sum.x), rcp_approx(sum.y));
     const float2 p0 = fma2(sc(K::weno3_p0[2]), t[4], fma2(sc(K::weno3_p0[1]), t[3], mul(sc(K::weno3_p0[0]), t[2])));
     const float2 p1 = fma2(sc(K::weno3_p1[2]), t[3], fma2(sc(K::weno3_p1[1]), t[2], mul(sc(K::weno3_p1[0]), t[1])));
     const float2 p2 = fma2(sc(K::weno3_p2[2]), t[2], fma2(sc(K::weno3_p2[1]), t[1], mul(sc(K::weno3_p2[0]), t[0])));
@@ -158,7 +167,7 @@ GBO_D FT weno3(const FT S[4], bool left) {
     FT q0 = weno_div(tau, be0 + K::eps), q1 = weno_div(tau, be1 + K::eps);
     FT al0 = K::weno2_cstar[0] * (FT(1) + q0 * q0);
     FT al1 = K::weno2_cstar[1] * (FT(1) + q1 * q1);
-    FT inv = weno_div(FT(1), al0 + al1);
+    FT inv = weno_inv(al0 + al1);
     FT p0 = K::weno2_p0[0] * a0 + K::weno2_p0[1] * a1;
     FT p1 = K::weno2_p1[0] * b0 + K::weno2_p1[1] * b1;
     return (al0 * inv) * p0 + (al1 * inv) * p1;

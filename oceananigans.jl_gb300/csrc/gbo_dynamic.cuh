@@ -133,6 +133,7 @@ struct LagP {
     FT lm_min;                            // minimum_numerator in FT
     double x0, y0, dx, dy;                // cell centres x0 + (i + 1/2) Δx (FP64)
     double xc0, yc0;                      // the first centres x0 + 0.5 Δx, y0 + 0.5 Δy
+    double rdx, rdy, rdz1;                // 1 / Δx, 1 / Δy, 1 / Δzᶜ of the first cell (FP64)
     const double* __restrict__ zc;        // z of the Nz cell centres (FP64)
     double dz1;                           // Δzᶜ of the first cell (regular z)
     int stretched;
@@ -162,7 +163,7 @@ GBO_D int lag_interpolator(double fi, double& xi) {
 template <typename FT>
 GBO_D double lag_frac_z(const LagP<FT>& P, double z) {
     const int Nz = P.g.Nz;
-    if (!P.stretched) return (z - P.zc[0]) / P.dz1 + 1.0;
+    if (!P.stretched) return (z - P.zc[0]) * P.rdz1 + 1.0;
     int low = 0, high = Nz - 1;
     while (low + 1 < high) {
         const int mid = (low + high) / 2;
@@ -235,7 +236,10 @@ __global__ void __launch_bounds__(256) k_lag_sum(const FT* __restrict__ a, const
 // _lagrangian_average_LM_MM! (dynamic_coefficient.jl:364-405), one cell per thread.  The
 // elapsed time Δt = clock.time - previous_compute_time is FP64 (the clock's type), so the
 // relaxation weight and the departure point are formed in FP64 as the reference's
-// promotion does; the fields are stored in FT.
+// promotion does; the fields are stored in FT.  FP64 division is the costly operation
+// here, so ε = τ / (1 + τ) with τ = Δt / T is formed as Δt / (T + Δt) and the fractional
+// indices multiply by the reciprocal spacings (both equal to the reference's forms up to
+// FP64 rounding).
 // LM and MM of this step are read from jlm / jmm (k_lm_mm_tiled wrote them there after 𝒥
 // was copied to 𝒥⁻); each thread reads and then overwrites its own cell only.
 template <typename FT>
@@ -254,16 +258,17 @@ __global__ void __launch_bounds__(dyn::TX * dyn::TY) k_lag_step(LagP<FT> P) {
     const FT dzk = M.dzc(k);
     const FT Df = cbrt(g.dx * g.dy * dzk);
     const FT Tm = FT(1.5) * Df / sqrt(sqrt(sqrt(lmp * mmp)));  // 1.5 Δᶠ / √(∜(𝒥ᴸᴹ𝒥ᴹᴹ))
-    const double tau = dt / (double)Tm;
-    const double eps = tau / (1 + tau);
+    const double Td = (double)Tm;
+    // the reference's form where T is 0, infinite or NaN (τ infinite or NaN)
+    const double eps = (Td > 0.0 && Td < INFINITY) ? dt / (Td + dt) : (dt / Td) / (1 + dt / Td);
     // departure point: the node minus the displacement by the cell's own u[i, j, k],
     // v[i, j, k], w[i, j, k] over Δt, each clamped to one cell width
     const double x = P.x0 + (i + 0.5) * P.dx, y = P.y0 + (j + 0.5) * P.dy, z = P.zc[k];
     const double ddx = jl_clamp((double)P.vel.u.in(i, j, k) * dt, -(double)g.dx, (double)g.dx);
     const double ddy = jl_clamp((double)P.vel.v.in(i, j, k) * dt, -(double)g.dy, (double)g.dy);
     const double ddz = jl_clamp((double)P.vel.w.in(i, j, k) * dt, -(double)dzk, (double)dzk);
-    const double fi = (x - ddx - P.xc0) / P.dx + 1;
-    const double fj = (y - ddy - P.yc0) / P.dy + 1;
+    const double fi = (x - ddx - P.xc0) * P.rdx + 1;
+    const double fj = (y - ddy - P.yc0) * P.rdy + 1;
     const double fk = lag_frac_z(P, z - ddz);
     double xi, yi, zi;
     const int i0 = lag_interpolator(fi, xi), j0 = lag_interpolator(fj, yi), k0 = lag_interpolator(fk, zi);

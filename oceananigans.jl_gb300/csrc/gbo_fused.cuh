@@ -812,16 +812,20 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
 
 // ---------------------------------------------------------------------------
 // Smagorinsky-Lilly νₑ on a shared-memory tile: the block stages u, v, w, b on a
-// (32+2) x (8+2) x (KT+2) box once (halo synthesis at load) and every thread
+// (32+8) x (8+2) x (KT+2) box once (halo synthesis at load, 16-byte chunks where the
+// grid allows; the stencils reach one point beyond the tile) and every thread
 // evaluates the closure for KT levels of its column from shared memory.
 // Arithmetic identical to k_smagorinsky (gbo_kernels.cuh), its three coefficients
 // included: Lilly's, the level's c² of DynamicSmagorinsky averaged over x-y, and the
 // cell's max(𝒥ᴸᴹ, minimum_numerator) / 𝒥ᴹᴹ of Lagrangian averaging (b is not staged then).
 // ---------------------------------------------------------------------------
 namespace smag {
-constexpr int TX = 32, TY = 8, KT = 4;
-constexpr int BX = TX + 2, BY = TY + 2, BZ = KT + 2, BS = BX * BY * BZ;
-GBO_D int bidx(int x, int y, int z) { return ((z + 1) * BY + (y + 1)) * BX + (x + 1); }
+// box: x from -4 (rows of 16-byte chunks that start on a multiple of four columns) to
+// TX + 3, y and z from -1 to TY and KT
+constexpr int TX = 32, TY = 8, KT = 4, BHX = 4;
+constexpr int BX = TX + 2 * BHX, BY = TY + 2, BZ = KT + 2, BS = BX * BY * BZ;
+constexpr int NT = TX * TY;
+GBO_D int bidx(int x, int y, int z) { return ((z + 1) * BY + (y + 1)) * BX + (x + BHX); }
 // squared edge strains of the tile: Σ₁₂² at (x ∈ 0..TX, y ∈ 0..TY, z < KT),
 // Σ₁₃² at (x ∈ 0..TX, y < TY, z ∈ 0..KT), Σ₂₃² at (x < TX, y ∈ 0..TY, z ∈ 0..KT)
 constexpr int E12 = (TX + 1) * (TY + 1) * KT, E13 = (TX + 1) * TY * (KT + 1), E23 = TX * (TY + 1) * (KT + 1);
@@ -829,9 +833,62 @@ GBO_D int i12(int x, int y, int z) { return (z * (TY + 1) + y) * (TX + 1) + x; }
 GBO_D int i13(int x, int y, int z) { return (z * TY + y) * (TX + 1) + x; }
 GBO_D int i23(int x, int y, int z) { return (z * (TY + 1) + y) * TX + x; }
 template <typename FT>
-struct Smem {
+struct __align__(16) Smem {
     FT u[BS], v[BS], w[BS], b[BS];
 };
+
+// Stage u, v, w and c (b when c is null: zeros) over the box of the block at (i0, j0, k0):
+// periodic wrap in x and y; for centre fields one mirrored layer below and above the
+// domain and zero beyond, for w zero at and beyond the walls (the CFld / WFld rules);
+// cref (c stored as departures) is added to c.  With Nx a multiple of the chunk width
+// and the fields 16-byte aligned, a box row is copied as 16-byte chunks (a chunk starts
+// on a multiple of its width, so it never straddles the periodic seam); otherwise one
+// value per copy.  Ends with the block's copies complete and visible (__syncthreads).
+template <typename FT>
+GBO_D void fill_box(Smem<FT>& s, const GridP<FT>& g, const FT* u, const FT* v, const FT* w, const FT* c,
+                    const FT* cref, int i0, int j0, int k0, int tid) {
+    constexpr int V = fused::VW<FT>, CR = BX / V;
+    const int Nz = g.Nz, fz = g.flatz;
+    const size_t plane = (size_t)g.Nx * g.Ny;
+    const bool vec = g.Nx % V == 0 && ((((size_t)u | (size_t)v | (size_t)w | (size_t)c) & 15) == 0);
+    const int n = vec ? CR * BY * BZ : BS, step = vec ? V : 1;
+    for (int e = tid; e < n; e += NT) {
+        const int cx = vec ? e % CR : e % BX, y = (vec ? e / CR : e / BX) % BY - 1, z = (vec ? e / (CR * BY) : e / (BX * BY)) - 1;
+        const int x = vec ? cx * V - BHX : cx - BHX;
+        const size_t col = wrapt(i0 + x, g.Nx) + (size_t)g.Nx * wrapt(j0 + y, g.Ny);
+        const int zc = fused::zsrc_c(k0 + z, Nz, fz), zw = fz ? -1 : fused::zsrc_w(k0 + z, Nz);
+        const size_t oc = col + (zc < 0 ? 0 : (size_t)zc * plane), ow = col + (zw < 0 ? 0 : (size_t)zw * plane);
+        const int d = e * step;
+        if (vec) {
+            fused::cp_async16(&s.u[d], u + oc, zc < 0);
+            fused::cp_async16(&s.v[d], v + oc, zc < 0);
+            fused::cp_async16(&s.w[d], w + ow, zw < 0);
+            if (c) fused::cp_async16(&s.b[d], c + oc, zc < 0);
+            else
+                for (int q = 0; q < V; ++q) s.b[d + q] = FT(0);
+        } else {
+            fused::cp_async(&s.u[d], u + oc, zc < 0);
+            fused::cp_async(&s.v[d], v + oc, zc < 0);
+            fused::cp_async(&s.w[d], w + ow, zw < 0);
+            if (c) fused::cp_async(&s.b[d], c + oc, zc < 0);
+            else s.b[d] = FT(0);
+        }
+    }
+    fused::cp_async_commit();
+    fused::cp_async_wait_all();
+    if (c && cref) {
+        // each thread adds the reference profile to the values it copied (its own copies
+        // are complete after the wait); zero-filled layers stay zero
+        for (int e = tid; e < n; e += NT) {
+            const int z = (vec ? e / (CR * BY) : e / (BX * BY)) - 1;
+            const int zc = fused::zsrc_c(k0 + z, Nz, fz);
+            if (zc < 0) continue;
+            const FT r = __ldg(cref + zc);
+            for (int q = 0; q < step; ++q) s.b[e * step + q] += r;
+        }
+    }
+    __syncthreads();
+}
 template <typename FT>
 struct SmemS : Smem<FT> {
     FT s12[E12], s13[E13], s23[E23];
@@ -842,7 +899,7 @@ struct SmemS : Smem<FT> {
 template <typename FT>
 __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __restrict__ nu_out) {
     using namespace smag;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemS<FT>& s = *reinterpret_cast<SmemS<FT>*>(smem_raw);
     const GridP<FT>& g = P.g;
     Met<FT> M(g);
@@ -850,38 +907,8 @@ __global__ void __launch_bounds__(256) k_smagorinsky_tiled(StepP<FT> P, FT* __re
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
     const bool buoy = P.buoyancy && !g.flatz && !P.jlm && !P.cs2;
     const int Nz = g.Nz, fz = g.flatz;
-    const size_t plane = (size_t)g.Nx * g.Ny;
-    // tile fill with asynchronous copies: halos synthesised as in CFld / WFld (periodic
-    // wrap in x, y; one mirrored layer in z and zero beyond for centres; zero at and
-    // beyond the walls for w), a zero-filled copy where the value is zero
-    auto fill = [&](auto wrap) {
-        for (int e = tid; e < BS; e += TX * TY) {
-            const int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
-            const size_t col = wrap(i0 + x, g.Nx) + (size_t)g.Nx * wrap(j0 + y, g.Ny);
-            const int zc = fused::zsrc_c(k0 + z, Nz, fz), zw = fz ? -1 : fused::zsrc_w(k0 + z, Nz);
-            const size_t oc = col + (zc < 0 ? 0 : (size_t)zc * plane), ow = col + (zw < 0 ? 0 : (size_t)zw * plane);
-            fused::cp_async(&s.u[e], P.u + oc, zc < 0);
-            fused::cp_async(&s.v[e], P.v + oc, zc < 0);
-            if (fz) s.w[e] = FT(0);
-            else fused::cp_async(&s.w[e], P.w + ow, zw < 0);
-            if (buoy) fused::cp_async(&s.b[e], P.b + oc, zc < 0);
-            else s.b[e] = FT(0);
-        }
-    };
-    // a tile reaches at most one period outside a domain of at least two tiles
-    if (g.Nx >= 2 * BX && g.Ny >= 2 * BY) fill([](int i, int n) { return wrapi(i, n); });
-    else fill([](int i, int n) { return wrapm(i, n); });
-    fused::cp_async_commit();
-    fused::cp_async_wait_all();
-    if (buoy && P.bref) {
-        // b stored as departures: each thread adds the reference profile to the elements it
-        // copied (its own copies are complete after the wait); zero-filled layers stay zero
-        for (int e = tid; e < BS; e += TX * TY) {
-            const int zc = fused::zsrc_c(k0 + e / (BX * BY) - 1, Nz, fz);
-            if (zc >= 0) s.b[e] += __ldg(P.bref + zc);
-        }
-    }
-    __syncthreads();
+    // w is null on a flat grid: the zero-filled copies never read it
+    fill_box<FT>(s, g, P.u, P.v, fz ? P.u : P.w, buoy ? P.b : nullptr, P.bref, i0, j0, k0, tid);
     auto U = [&](int x, int y, int zz) { return s.u[bidx(x, y, zz)]; };
     auto V = [&](int x, int y, int zz) { return s.v[bidx(x, y, zz)]; };
     auto W = [&](int x, int y, int zz) { return s.w[bidx(x, y, zz)]; };
@@ -993,23 +1020,13 @@ struct TileFields {
 template <typename FT>
 __global__ void __launch_bounds__(256) k_amd_tiled_ibg(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
     using namespace smag;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem<FT>& s = *reinterpret_cast<Smem<FT>*>(smem_raw);
     const GridP<FT>& g = P.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g, P.cref);
-    WFld<FT> Wg = wfld(P.w, g);
     const bool has_c = P.c != nullptr;
-    for (int e = tid; e < BS; e += TX * TY) {
-        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
-        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
-        s.u[e] = Ug.far(gi, gj, gk);
-        s.v[e] = Vg.far(gi, gj, gk);
-        s.w[e] = Wg.far(gi, gj, gk);
-        s.b[e] = has_c ? Cg.far(gi, gj, gk) : FT(0);
-    }
-    __syncthreads();
+    fill_box<FT>(s, g, P.u, P.v, g.flatz ? P.u : P.w, has_c ? P.c : nullptr, P.cref, i0, j0, k0, tid);
     const int i = i0 + tx, j = j0 + ty;
     if (i >= g.Nx || j >= g.Ny) return;
     const TileFld<FT> tu{s.u, i0, j0, k0}, tv{s.v, i0, j0, k0}, tw{s.w, i0, j0, k0}, tc{s.b, i0, j0, k0};
@@ -1047,25 +1064,15 @@ struct SmemA : Smem<FT> {
 template <typename FT>
 __global__ void __launch_bounds__(256) k_amd_tiled(StepP<FT> P, FT* __restrict__ nu_out, FT* __restrict__ kap_out) {
     using namespace smag;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemA<FT>& s = *reinterpret_cast<SmemA<FT>*>(smem_raw);
     const GridP<FT>& g = P.g;
     Met<FT> M(g);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * KT;
-    CFld<FT> Ug = cfld(P.u, g), Vg = cfld(P.v, g), Cg = cfld(P.c, g, P.cref);
-    WFld<FT> Wg = wfld(P.w, g);
     const bool has_c = P.c != nullptr;
     const int fz = g.flatz;
-    for (int e = tid; e < BS; e += TX * TY) {
-        int x = e % BX - 1, y = (e / BX) % BY - 1, z = e / (BX * BY) - 1;
-        int gi = i0 + x, gj = j0 + y, gk = k0 + z;
-        s.u[e] = Ug.far(gi, gj, gk);
-        s.v[e] = Vg.far(gi, gj, gk);
-        s.w[e] = Wg.far(gi, gj, gk);
-        s.b[e] = has_c ? Cg.far(gi, gj, gk) : FT(0);
-    }
-    __syncthreads();
+    fill_box<FT>(s, g, P.u, P.v, fz ? P.u : P.w, has_c ? P.c : nullptr, P.cref, i0, j0, k0, tid);
     auto U = [&](int x, int y, int z) { return s.u[bidx(x, y, z)]; };
     auto V = [&](int x, int y, int z) { return s.v[bidx(x, y, z)]; };
     auto W = [&](int x, int y, int z) { return s.w[bidx(x, y, z)]; };

@@ -1207,8 +1207,11 @@ struct ModelImpl : gbo_model {
         L.dy = (grid.y[1] - grid.y[0]) / Ny;
         L.xc0 = L.x0 + 0.5 * L.dx;
         L.yc0 = L.y0 + 0.5 * L.dy;
+        L.rdx = 1.0 / L.dx;
+        L.rdy = 1.0 / L.dy;
         L.zc = lag_zc.p;
         L.dz1 = (double)Z.at(Z.dzc, 1);
+        L.rdz1 = 1.0 / L.dz1;
         L.stretched = stretched_z ? 1 : 0;
         L.clock = lag_s.p;
         L.dtp = lag_dtp;

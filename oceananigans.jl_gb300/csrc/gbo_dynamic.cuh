@@ -38,6 +38,7 @@
 // beyond it, zero for w on and beyond the walls.
 #pragma once
 #include "gbo_kernels.cuh"
+#include "gbo_fused.cuh"  // 16-byte copies and the halo levels of the tile fills
 
 namespace dyn {
 constexpr int TX = 32, TY = 8;
@@ -356,9 +357,10 @@ template <typename FT>
 cudaError_t dyn_set_smem();
 
 // ---------------------------------------------------------------------------
-// Tiled Σ, Σ̄ and LM, MM.  The per-point forms above evaluate the test filter of products
-// of interpolated strains: every cell recomputes the filtered velocities and the centre
-// products of its neighbours many times over.  A 32 × 4 × 2 block instead stages the
+// Tiled Σ, Σ̄ and LM, MM.  LM_and_MM evaluates the test filter of products of
+// interpolated strains: evaluated point by point, every cell would recompute the
+// filtered velocities and the centre products of its neighbours many times over.  A
+// 32 × 4 × 2 block instead stages the
 // velocities of its cells and two points around them (through the same accessors, so
 // every halo rule, the predictor halos of the Lagrangian update included, is the
 // accessor's), forms the filtered velocities and the twelve centre products of the
@@ -370,13 +372,16 @@ cudaError_t dyn_set_smem();
 // ---------------------------------------------------------------------------
 namespace dtile {
 constexpr int TX = 32, TY = 4, KT = 2, NT = TX * TY * KT;
-constexpr int RX = TX + 4, RY = TY + 4, RZ = KT + 4, RS = RX * RY * RZ;  // velocities: -2 .. +1 beyond the tile
+// velocities: -2 .. +1 beyond the tile in y and z; in x from -4 (rows of 16-byte chunks
+// that start on a multiple of four columns) to TX + 3
+constexpr int RHX = 4;
+constexpr int RX = TX + 2 * RHX, RY = TY + 4, RZ = KT + 4, RS = RX * RY * RZ;
 constexpr int QX = TX + 2, QY = TY + 2, QZ = KT + 2, QS = QX * QY * QZ;  // filtered velocities, products: -1 .. +1
-GBO_D int ri(int x, int y, int z) { return ((z + 2) * RY + (y + 2)) * RX + (x + 2); }
+GBO_D int ri(int x, int y, int z) { return ((z + 2) * RY + (y + 2)) * RX + (x + RHX); }
 GBO_D int qi(int x, int y, int z) { return ((z + 1) * QY + (y + 1)) * QX + (x + 1); }
 enum { Q11 = 0, Q22, Q33, Q12, Q13, Q23, M11, M22, M33, M12, M13, M23, NQ };
 template <typename FT>
-struct SmemS {
+struct __align__(16) SmemS {
     FT u[RS], v[RS], w[RS];
     FT fu[QS], fv[QS], fw[QS];
 };
@@ -389,17 +394,69 @@ struct SmemL : SmemS<FT> {
 GBO_D int clamp_far(int i, int n) { return i > n + 1 ? n + 1 : i; }
 }  // namespace dtile
 
-// stage u, v, w of the tile and two points around it, then the filtered velocities over
-// the tile and one point around it
+// The first of the V values of a 16-byte chunk of a row at (gi, gj, gk) (gi a multiple of
+// V, Nx a multiple of V: the chunk lies in one period), read through each accessor's
+// halo rules; zero: the accessor's value there is zero (the copy writes zeros).
+template <typename FT>
+GBO_D const FT* chunk_src(const CFld<FT>& f, int gi, int gj, int gk, bool& zero) {
+    const int zc = fused::zsrc_c(gk, f.Nz, f.flatz);
+    zero = zc < 0;
+    return f.a + wrapt(gi, f.Nx) + (size_t)f.Nx * (wrapt(gj, f.Ny) + (size_t)f.Ny * (zc < 0 ? 0 : zc));
+}
+template <typename FT>
+GBO_D const FT* chunk_src(const WFld<FT>& f, int gi, int gj, int gk, bool& zero) {
+    zero = gk <= 0 || gk >= f.Nz;
+    return f.a + wrapt(gi, f.Nx) + (size_t)f.Nx * (wrapt(gj, f.Ny) + (size_t)f.Ny * (zero ? 0 : gk));
+}
+template <typename FT>
+GBO_D const FT* chunk_src(const LagC<FT>& f, int gi, int gj, int gk, bool& zero) {
+    const bool in = (unsigned)gi < (unsigned)f.in.Nx && (unsigned)gj < (unsigned)f.in.Ny && (unsigned)gk < (unsigned)f.in.Nz;
+    return in ? chunk_src(f.in, gi, gj, gk, zero) : chunk_src(f.halo, gi, gj, gk, zero);
+}
+template <typename FT>
+GBO_D const FT* chunk_src(const LagW<FT>& f, int gi, int gj, int gk, bool& zero) {
+    const bool in = (unsigned)gi < (unsigned)f.in.Nx && (unsigned)gj < (unsigned)f.in.Ny;
+    return in ? chunk_src(f.in, gi, gj, gk, zero) : chunk_src(f.halo, gi, gj, gk, zero);
+}
+// whether an accessor's rows can be copied in 16-byte chunks: aligned storage, no
+// reference profile to add
+template <typename FT>
+GBO_D bool chunk_ok(const CFld<FT>& f) { return f.ref == nullptr && ((size_t)f.a & 15) == 0; }
+template <typename FT>
+GBO_D bool chunk_ok(const WFld<FT>& f) { return ((size_t)f.a & 15) == 0; }
+template <typename FT>
+GBO_D bool chunk_ok(const LagC<FT>& f) { return chunk_ok(f.in) && chunk_ok(f.halo); }
+template <typename FT>
+GBO_D bool chunk_ok(const LagW<FT>& f) { return chunk_ok(f.in) && chunk_ok(f.halo); }
+
+// stage u, v, w of the tile and two points around it (in x four: whole chunks), then the
+// filtered velocities over the tile and one point around it
 template <typename FT, class V>
 GBO_D void dtile_stage(dtile::SmemS<FT>& s, const GridP<FT>& g, const V& vel, int i0, int j0, int k0, int tid) {
     using namespace dtile;
-    for (int e = tid; e < RS; e += NT) {
-        const int x = e % RX - 2, y = (e / RX) % RY - 2, z = e / (RX * RY) - 2;
-        const int gi = clamp_far(i0 + x, g.Nx), gj = clamp_far(j0 + y, g.Ny), gk = k0 + z;
-        s.u[e] = vel.u(gi, gj, gk);
-        s.v[e] = vel.v(gi, gj, gk);
-        s.w[e] = vel.w(gi, gj, gk);
+    constexpr int CW = fused::VW<FT>, CR = RX / CW;
+    const bool vec = g.Nx % CW == 0 && chunk_ok(vel.u) && chunk_ok(vel.v) && chunk_ok(vel.w);
+    if (vec) {
+        for (int e = tid; e < CR * RY * RZ; e += NT) {
+            const int gi = i0 + (e % CR) * CW - RHX, gj = j0 + (e / CR) % RY - 2, gk = k0 + e / (CR * RY) - 2;
+            bool zu, zv, zw;
+            const FT* pu = chunk_src(vel.u, gi, gj, gk, zu);
+            const FT* pv = chunk_src(vel.v, gi, gj, gk, zv);
+            const FT* pw = chunk_src(vel.w, gi, gj, gk, zw);
+            fused::cp_async16(&s.u[e * CW], pu, zu);
+            fused::cp_async16(&s.v[e * CW], pv, zv);
+            fused::cp_async16(&s.w[e * CW], pw, zw);
+        }
+        fused::cp_async_commit();
+        fused::cp_async_wait_all();
+    } else {
+        for (int e = tid; e < RS; e += NT) {
+            const int x = e % RX - RHX, y = (e / RX) % RY - 2, z = e / (RX * RY) - 2;
+            const int gi = clamp_far(i0 + x, g.Nx), gj = clamp_far(j0 + y, g.Ny), gk = k0 + z;
+            s.u[e] = vel.u(gi, gj, gk);
+            s.v[e] = vel.v(gi, gj, gk);
+            s.w[e] = vel.w(gi, gj, gk);
+        }
     }
     __syncthreads();
     // the test filter ⟨f⟩ = (6 f + the six face neighbours) / 12, the neighbours in the order x, y, z

@@ -12,20 +12,20 @@ struct LaunchShapeEntry {
 
 // BEGIN TABLE
 static const LaunchShapeEntry kLaunchTable[] = {
-    {256, 256, 128, 0, 0, 32, 8, 8, 16},  // rect
-    {256, 256, 128, 1, 0, 4, 8, 2, 16},  // rect
-    {256, 256, 128, 0, 1, 32, 8, 8, 16},  // ibg
+    {256, 256, 128, 0, 0, 32, 8, 8, 24},  // rect
+    {256, 256, 128, 1, 0, 4, 8, 2, 24},  // rect
+    {256, 256, 128, 0, 1, 32, 8, 8, 24},  // ibg
     {512, 512, 256, 0, 0, 32, 8, 8, 32},  // stretched
     {128, 128, 1, 1, 0, 32, 2, 2, 1},  // flat
     {64, 64, 32, 0, 0, 32, 4, 4, 2},  // rect
-    {64, 64, 48, 0, 0, 32, 8, 4, 2},  // rect
-    {64, 64, 64, 0, 0, 16, 32, 4, 4},  // rect
+    {64, 64, 48, 0, 0, 8, 8, 4, 2},  // rect
+    {64, 64, 64, 0, 0, 16, 32, 8, 4},  // rect
     {96, 96, 32, 0, 0, 32, 8, 4, 4},  // rect
     {96, 96, 48, 0, 0, 16, 8, 8, 4},  // rect
-    {96, 96, 64, 0, 0, 32, 8, 8, 8},  // rect
+    {96, 96, 64, 0, 0, 8, 8, 8, 8},  // rect
     {128, 128, 32, 0, 0, 32, 4, 4, 8},  // rect
     {128, 128, 48, 0, 0, 32, 8, 8, 8},  // rect
-    {128, 128, 64, 0, 0, 64, 16, 8, 4},  // rect
+    {128, 128, 64, 0, 0, 64, 8, 8, 4},  // rect
     {0, 0, 0, 0, 0, 0, 0, 0, 0},  // end
 };
 // END TABLE

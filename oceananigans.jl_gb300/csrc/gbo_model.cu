@@ -40,20 +40,34 @@ __global__ void __launch_bounds__(256) k_source(GridP<FT> g, const FT* __restric
     Met<FT> M(g);
     const FT Az = M.Az();
     const int kb = g.kbot ? __ldg(g.kbot + c) : 0;
-    // w at the bottom face of the first level (zero at the wall, face 0)
-    FT wlo = (g.flatz || k0 <= 0) ? FT(0) : w[c + plane * k0];
-    for (int k = k0; k < k1; ++k) {
-        const size_t o = plane * k;
-        const FT whi = (g.flatz || k + 1 >= g.Nz) ? FT(0) : w[c + o + plane];
-        const FT Ax = M.Ax(k), Ay = M.Ay(k);
-        const FT div = M.rVc(k) * ((Ax * u[cx + o] - Ax * u[c + o]) + (Ay * v[cy + o] - Ay * v[c + o]) +
-                                   (g.flatz ? FT(0) : (Az * whi - Az * wlo)));
-        const bool active = k >= kb;
-        FT r = active ? div : FT(0);
-        if (mode == SRC_FT) r = (active ? M.dzc(k) : FT(0)) * div;
-        if (mode == SRC_CG) r = r * (Az * M.dzc(k));
-        rhs[c + o] = r;
-        wlo = whi;
+    // all loads of the column first (w at faces k0 .. k1; face 0 and Nz are walls)
+    FT ru[COL_LEVELS], rux[COL_LEVELS], rv[COL_LEVELS], rvy[COL_LEVELS], rw[COL_LEVELS + 1];
+    rw[0] = (g.flatz || k0 <= 0) ? FT(0) : w[c + plane * k0];
+#pragma unroll
+    for (int l = 0; l < COL_LEVELS; ++l) {
+        const int k = k0 + l;
+        if (k < k1) {
+            const size_t o = plane * k;
+            ru[l] = u[c + o];
+            rux[l] = u[cx + o];
+            rv[l] = v[c + o];
+            rvy[l] = v[cy + o];
+            rw[l + 1] = (g.flatz || k + 1 >= g.Nz) ? FT(0) : w[c + o + plane];
+        }
+    }
+#pragma unroll
+    for (int l = 0; l < COL_LEVELS; ++l) {
+        const int k = k0 + l;
+        if (k < k1) {
+            const FT Ax = M.Ax(k), Ay = M.Ay(k);
+            const FT div = M.rVc(k) * ((Ax * rux[l] - Ax * ru[l]) + (Ay * rvy[l] - Ay * rv[l]) +
+                                       (g.flatz ? FT(0) : (Az * rw[l + 1] - Az * rw[l])));
+            const bool active = k >= kb;
+            FT r = active ? div : FT(0);
+            if (mode == SRC_FT) r = (active ? M.dzc(k) : FT(0)) * div;
+            if (mode == SRC_CG) r = r * (Az * M.dzc(k));
+            rhs[c + plane * k] = r;
+        }
     }
 }
 

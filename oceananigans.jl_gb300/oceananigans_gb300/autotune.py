@@ -22,8 +22,10 @@ import re
 
 import numpy as np
 
+# levels need not divide Nz or be a power of two: a value whose blocks fill the resident
+# slots of the GPU evenly can beat its power-of-two neighbours
 CANDIDATES = {"dct_columns": (4, 8, 16, 32, 64), "x_lines": (1, 2, 4, 8, 16, 32),
-              "y_columns": (2, 4, 8, 16, 32), "levels": (1, 2, 4, 8, 16, 32)}
+              "y_columns": (2, 4, 8, 16, 32), "levels": (1, 2, 4, 8, 12, 16, 19, 24, 32)}
 GROUP = {"dct_columns": "k_dct_z", "x_lines": "k_rfft_x", "y_columns": "k_fft_y", "levels": "k_momentum"}
 
 # (Nx, Ny, Nz, float type, grid): "rect" Periodic-Periodic-Bounded with the FFT solver,

@@ -12,9 +12,12 @@
 //     south values with its neighbours through shared memory, and carries the
 //     top value to the next level as the bottom value.
 // The extra faces on the tile's east column and north row are evaluated by
-// warps 0 and 1 after their own work.
+// warps 0 and 1 after their own work, by a separately compiled form of the face code
+// that takes the vertical windows of those columns from a small shared-memory ring,
+// prefetched two levels ahead.
 #pragma once
 #include <initializer_list>
+#include <type_traits>
 #include "gbo_step.cuh"
 
 // Resident blocks per SM the FP32 kernel is compiled for (registers are capped so
@@ -57,6 +60,10 @@ struct __align__(16) Smem {
     FT CC[2][PS];                      // tracer: k (+k+1)
     FT WX[NWX][TY][TX + 1];
     FT SY[NSY][TY + 1][TX];
+    // vertical windows of the tile-edge columns: u of the east column (warp 0, lane = row)
+    // and v of the north row (warp 1, lane = column), level L in slot L & 7; each entry is
+    // written and read by one thread only
+    FT EU[8][TY], EV[8][TX];
     // last, so that launches without AMD or an immersed boundary omit it (smem_bytes):
     union {
         FT KP[3][PS];                  // AMD κₑ: k, k+1 (+k+2)
@@ -254,6 +261,18 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         return ut * biased<FT>(qb, bias_left(ut), bl);
     };
 
+    // the tile-edge column whose faces this thread evaluates after its own (the east column
+    // for warp 0, the north row for warp 1), wrapped: on grids narrower than a tile it lies
+    // more than one period outside the domain; its vertical window goes to EU / EV
+    const size_t fcol = (size_t)wrapm(i0 + (ty == 0 ? TX : tx), g.Nx) + (size_t)g.Nx * wrapm(j0 + (ty == 0 ? tx : TY), g.Ny);
+    const bool edgeW = ty == 0 && tx < TY, edgeS = ty == 1;
+    auto issue_edge = [&](int kk) {
+        const int zl = zsrc_c(kk, Nz, fz);
+        const size_t off = fcol + (zl < 0 ? 0 : (size_t)zl * plane);
+        if (edgeW) cp_async(&s.EU[kk & 7][tx], P.u + off, zl < 0);
+        else if (edgeS) cp_async(&s.EV[kk & 7][tx], P.v + off, zl < 0);
+    };
+
     // ---- prologue: planes for level kb ----
     issue_plane(s.U[m3(kb - 1)], P.u, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
     issue_plane(s.V[m3(kb - 1)], P.v, zsrc_c(kb - 1, Nz, fz), plane, pp, tid);
@@ -274,6 +293,8 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         issue_plane(s.KP[m3(kb)], P.kap, zsrc_c(kb, Nz, fz), plane, pp, tid);
         issue_plane(s.KP[m3(kb + 1)], P.kap, zsrc_c(kb + 1, Nz, fz), plane, pp, tid);
     }
+    if (!fz)
+        for (int o = -2; o <= 1; ++o) issue_edge(kb + o);
     cp_async_commit();
     Col<FT> c;
 #pragma unroll
@@ -350,10 +371,6 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
     }
 
     const FT dt = stage_dt(P);
-    // the tile-edge column that pass 1 below loads (the east column for warp 0, the north
-    // row for warp 1), wrapped once: on grids narrower than a tile it lies more than one
-    // period outside the domain
-    const size_t fcol = (size_t)wrapm(i0 + (ty == 0 ? TX : tx), g.Nx) + (size_t)g.Nx * wrapm(j0 + (ty == 0 ? tx : TY), g.Ny);
     int r3 = m3(kb);
     for (int k = kb; k < ke; ++k) {
         // ring slots of levels k-1, k, k+1 (and k+2, which shares the slot of k-1)
@@ -368,6 +385,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             if (P.has_phy) issue_plane(s.PH[m2(kn)], P.phy, zsrc_c(kn, Nz, fz), plane, pp, tid);
             if (TR) issue_plane(s.CC[m2(kn)], P.c, zsrc_c(kn, Nz, fz), plane, pp, tid);
             if (TR && amd) issue_plane(s.KP[s3m], P.kap, zsrc_c(kn + 1, Nz, fz), plane, pp, tid);
+            if (!fz) issue_edge(k + 2);  // read from level k + 1 on
         }
         cp_async_commit();
         // ---- early loads: window tops for the next level, G⁻ of this level ----
@@ -406,7 +424,8 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
         };
 
         // ---- west / south face quantities of this thread (and the tile edges) ----
-        auto west = [&](int x, int y, bool own) {
+        auto west = [&](int x, int y, auto own_t) {
+            constexpr bool own = decltype(own_t)::value;
             FT S[6];
             if constexpr (IBG) {
 #pragma unroll
@@ -438,12 +457,12 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 if (!fz) {
                     paired = true;
                     FT uz[4];
-                    if (own) {
+                    if constexpr (own) {
 #pragma unroll
                         for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
                     } else {
 #pragma unroll
-                        for (int o = 0; o < 4; ++o) uz[o] = Ug.col(fcol, k - 2 + o);
+                        for (int o = 0; o < 4; ++o) uz[o] = s.EU[(k - 2 + o) & 7][y];
                     }
                     auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
                     const FT uw = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
@@ -462,12 +481,12 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
             if (!fz && !paired) {
                 FT uz[4];
-                if (own) {
+                if constexpr (own) {
 #pragma unroll
                     for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
                 } else {
 #pragma unroll
-                    for (int o = 0; o < 4; ++o) uz[o] = Ug.col(fcol, k - 2 + o);
+                    for (int o = 0; o < 4; ++o) uz[o] = s.EU[(k - 2 + o) & 7][y];
                 }
                 auto qs = [&](int o) { return M.Ax(k + o) * uz[o + 2]; };
 #pragma unroll
@@ -487,7 +506,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
                 FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
                 s.WX[C_12][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
-                if (own) {
+                if constexpr (own) {
                     s.WX[C_13][y][x] = c.t13;
                 } else if (!fz) {
                     FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(x - 1, y)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
@@ -513,7 +532,8 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 }
             }
         };
-        auto south = [&](int x, int y, bool own) {
+        auto south = [&](int x, int y, auto own_t) {
+            constexpr bool own = decltype(own_t)::value;
             FT S[6];
             if constexpr (IBG) {
 #pragma unroll
@@ -545,12 +565,12 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 if (!fz) {
                     paired = true;
                     FT vz[4];
-                    if (own) {
+                    if constexpr (own) {
 #pragma unroll
                         for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
                     } else {
 #pragma unroll
-                        for (int o = 0; o < 4; ++o) vz[o] = Vg.col(fcol, k - 2 + o);
+                        for (int o = 0; o < 4; ++o) vz[o] = s.EV[(k - 2 + o) & 7][x];
                     }
                     auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
                     const FT vw = symm<FT>(qs, zlev_symm_face(k + 1, Nz));
@@ -569,12 +589,12 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
             if (!fz && !paired) {
                 FT vz[4];
-                if (own) {
+                if constexpr (own) {
 #pragma unroll
                     for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
                 } else {
 #pragma unroll
-                    for (int o = 0; o < 4; ++o) vz[o] = Vg.col(fcol, k - 2 + o);
+                    for (int o = 0; o < 4; ++o) vz[o] = s.EV[(k - 2 + o) & 7][x];
                 }
                 auto qs = [&](int o) { return M.Ay(k + o) * vz[o + 2]; };
 #pragma unroll
@@ -594,7 +614,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
                 FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
                 s.SY[C_12N][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
-                if (own) {
+                if constexpr (own) {
                     s.SY[C_23][y][x] = c.t23;
                 } else if (!fz) {
                     FT ncff = FT(0.5) * (FT(0.5) * (Nm[pidx(x, y - 1)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x, y - 1)] + Nk[pidx(x, y)]));
@@ -620,14 +640,13 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 }
             }
         };
-        // pass 0: the faces of this thread's cells; pass 1: the tile's east column
-        // (warp 0, lanes < TY) and north row (warp 1).  One code copy serves both.
-#pragma unroll 1
-        for (int pass = 0; pass < 2; ++pass) {
-            const bool own = pass == 0;
-            if (own || (ty == 0 && tx < TY)) west(own ? tx : TX, own ? ty : tx, own);
-            if (own || ty == 1) south(tx, own ? ty : TY, own);
-        }
+        // the faces of this thread's cells (windows in registers), then the tile's east
+        // column (warp 0, lanes < TY) and north row (warp 1) from the edge columns; each
+        // form compiled separately (own is a compile-time constant in each)
+        west(tx, ty, std::true_type{});
+        south(tx, ty, std::true_type{});
+        if (ty == 0 && tx < TY) west(TX, tx, std::false_type{});
+        if (ty == 1) south(tx, TY, std::false_type{});
 
         // ---- top-face quantities (carried to the next level) ----
         FT fWu_t = FT(0), fWv_t = FT(0), fWw_t = FT(0), t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);

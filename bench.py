@@ -342,13 +342,13 @@ class ClockSampler:
 # capture, its command and the algorithmic bytes of the same launch are in the named profile.
 PROFILED_TRAFFIC = {
     ("convection", "k_momentum", (256, 256, 128), "f32"): {
-        "traffic": 432.1e6,
+        "traffic": 448.0e6,
         "traffic_launch": "one RK3 stage-1 launch (algorithmic bytes of that launch 469.8e6; stages 2-3 also read G-)",
         "traffic_profile": "profiles/k_momentum_fused_free_convection_256x256x128_f32.md",
-        "issue_active_frac": 0.663,
-        "fma_pipe_inst_frac": 0.225,
-        "alu_pipe_inst_frac": 0.312,
-        "dram_throughput_frac": 0.076,
+        "issue_active_frac": 0.680,
+        "fma_pipe_inst_frac": 0.250,
+        "alu_pipe_inst_frac": 0.299,
+        "dram_throughput_frac": 0.089,
     },
 }
 

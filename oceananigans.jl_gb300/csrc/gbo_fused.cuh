@@ -167,6 +167,12 @@ GBO_D FT flux_c4_w5(FT a0, FT a1, FT a2, FT a3, const FT* S) {
     return ut * weno5<FT>(S, bias_left(ut));
 }
 
+// whether face code evaluates a cell's own face: a compile-time constant for the
+// separately compiled forms, a run-time flag for the shared one
+GBO_D constexpr bool own_value(std::true_type) { return true; }
+GBO_D constexpr bool own_value(std::false_type) { return false; }
+GBO_D bool own_value(bool b) { return b; }
+
 template <typename FT>
 struct Col {
     FT uc[7], vc[7], wc[6];
@@ -425,7 +431,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
 
         // ---- west / south face quantities of this thread (and the tile edges) ----
         auto west = [&](int x, int y, auto own_t) {
-            constexpr bool own = decltype(own_t)::value;
+            const bool own = own_value(own_t);  // a constant for std::true_type / std::false_type
             FT S[6];
             if constexpr (IBG) {
 #pragma unroll
@@ -457,7 +463,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 if (!fz) {
                     paired = true;
                     FT uz[4];
-                    if constexpr (own) {
+                    if (own) {
 #pragma unroll
                         for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
                     } else {
@@ -481,7 +487,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
             if (!fz && !paired) {
                 FT uz[4];
-                if constexpr (own) {
+                if (own) {
 #pragma unroll
                     for (int o = 0; o < 4; ++o) uz[o] = c.uc[1 + o];
                 } else {
@@ -506,7 +512,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
                 FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
                 s.WX[C_12][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
-                if constexpr (own) {
+                if (own) {
                     s.WX[C_13][y][x] = c.t13;
                 } else if (!fz) {
                     FT nfcf = FT(0.5) * (FT(0.5) * (Nm[pidx(x - 1, y)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x - 1, y)] + Nk[pidx(x, y)]));
@@ -533,7 +539,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
         };
         auto south = [&](int x, int y, auto own_t) {
-            constexpr bool own = decltype(own_t)::value;
+            const bool own = own_value(own_t);  // a constant for std::true_type / std::false_type
             FT S[6];
             if constexpr (IBG) {
 #pragma unroll
@@ -565,7 +571,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 if (!fz) {
                     paired = true;
                     FT vz[4];
-                    if constexpr (own) {
+                    if (own) {
 #pragma unroll
                         for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
                     } else {
@@ -589,7 +595,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
             if (!fz && !paired) {
                 FT vz[4];
-                if constexpr (own) {
+                if (own) {
 #pragma unroll
                     for (int o = 0; o < 4; ++o) vz[o] = c.vc[1 + o];
                 } else {
@@ -614,7 +620,7 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
                 FT dyu = (Uk[pidx(x, y)] - Uk[pidx(x, y - 1)]) * g.rdy;
                 FT dxv = (Vk[pidx(x, y)] - Vk[pidx(x - 1, y)]) * g.rdx;
                 s.SY[C_12N][y][x] = FT(-2) * (nffc * (FT(0.5) * (dyu + dxv)));
-                if constexpr (own) {
+                if (own) {
                     s.SY[C_23][y][x] = c.t23;
                 } else if (!fz) {
                     FT ncff = FT(0.5) * (FT(0.5) * (Nm[pidx(x, y - 1)] + Nm[pidx(x, y)]) + FT(0.5) * (Nk[pidx(x, y - 1)] + Nk[pidx(x, y)]));
@@ -641,12 +647,23 @@ __global__ void __launch_bounds__(256, sizeof(FT) == 4 ? GBO_FUSED_MIN_BLOCKS : 
             }
         };
         // the faces of this thread's cells (windows in registers), then the tile's east
-        // column (warp 0, lanes < TY) and north row (warp 1) from the edge columns; each
-        // form compiled separately (own is a compile-time constant in each)
-        west(tx, ty, std::true_type{});
-        south(tx, ty, std::true_type{});
-        if (ty == 0 && tx < TY) west(TX, tx, std::false_type{});
-        if (ty == 1) south(tx, TY, std::false_type{});
+        // column (warp 0, lanes < TY) and north row (warp 1) from the edge columns.  Each
+        // form is compiled separately (own a compile-time constant in each), except on an
+        // immersed grid, whose much larger face code keeps one copy for both (a second
+        // copy measured slower there)
+        if constexpr (IBG) {
+#pragma unroll 1
+            for (int pass = 0; pass < 2; ++pass) {
+                const bool own = pass == 0;
+                if (own || (ty == 0 && tx < TY)) west(own ? tx : TX, own ? ty : tx, own);
+                if (own || ty == 1) south(tx, own ? ty : TY, own);
+            }
+        } else {
+            west(tx, ty, std::true_type{});
+            south(tx, ty, std::true_type{});
+            if (ty == 0 && tx < TY) west(TX, tx, std::false_type{});
+            if (ty == 1) south(tx, TY, std::false_type{});
+        }
 
         // ---- top-face quantities (carried to the next level) ----
         FT fWu_t = FT(0), fWv_t = FT(0), fWw_t = FT(0), t13_t = FT(0), t23_t = FT(0), t33_t = FT(0);

@@ -133,10 +133,10 @@ struct LagP {
     FT* jmm;
     FT lm_min;                            // minimum_numerator in FT
     double x0, y0, dx, dy;                // cell centres x0 + (i + 1/2) Δx (FP64)
-    double xc0, yc0;                      // the first centres x0 + 0.5 Δx, y0 + 0.5 Δy
-    double rdx, rdy, rdz1;                // 1 / Δx, 1 / Δy, 1 / Δzᶜ of the first cell (FP64)
-    const double* __restrict__ zc;        // z of the Nz cell centres (FP64)
-    double dz1;                           // Δzᶜ of the first cell (regular z)
+    double xc0, yc0;                      // the first centres x0 + 0.5 Δx, y0 + 0.5 Δy (FT values)
+    double rdx, rdy, rdz1;                // 1 / Δx, 1 / Δy, 1 / Δzᶜ of the first cell (of the FT spacings)
+    const double* __restrict__ zc;        // z of the Nz cell centres (FT values, stored as FP64)
+    double dz1;                           // Δzᶜ of the first cell (regular z; FT value)
     int stretched;
     const double* clock;                  // LAG_* slots
     const double* dtp;                    // Δt of this step (FP64)
@@ -155,6 +155,12 @@ GBO_D int lag_interpolator(double fi, double& xi) {
     const int lo = (int)fi;
     const double r = fi - trunc(fi);
     xi = (r == 0.0) ? 0.0 : (r < 0.0 ? r + 1.0 : r);
+    return lo - 1;
+}
+GBO_D int lag_interpolator(float fi, float& xi) {
+    const int lo = (int)fi;
+    const float r = fi - truncf(fi);
+    xi = (r == 0.f) ? 0.f : (r < 0.f ? r + 1.f : r);
     return lo - 1;
 }
 
@@ -187,18 +193,19 @@ GBO_D FT lag_prev(const FT* __restrict__ a, const GridP<FT>& g, int i, int j, in
     return __ldg(a + i + (size_t)g.Nx * (j + (size_t)g.Ny * k));
 }
 
-// _interpolate (Utils/interpolation.jl:58-72): the eight weights in the reference's order
-template <typename FT>
-GBO_D double lag_trilinear(const FT* __restrict__ a, const GridP<FT>& g, int i0, int j0, int k0, double x, double y,
-                           double z) {
+// _interpolate (Utils/interpolation.jl:58-72): the eight weights in the reference's order,
+// ϕ = (1 - ξ or ξ) (1 - η or η) (1 - ζ or ζ) left to right.  ξ, η have the type of the
+// fractional x and y indices (FT) and ζ that of the z index (ZT); the product of the x and
+// y factors is taken in FT, then promoted with ζ, as the reference's promotion does.
+template <typename FT, typename ZT>
+GBO_D ZT lag_trilinear(const FT* __restrict__ a, const GridP<FT>& g, int i0, int j0, int k0, FT x, FT y, ZT z) {
     const int i1 = i0 + 1, j1 = j0 + 1, k1 = k0 + 1;
-    return (1 - x) * (1 - y) * (1 - z) * (double)lag_prev(a, g, i0, j0, k0) +
-           (1 - x) * (1 - y) * z * (double)lag_prev(a, g, i0, j0, k1) +
-           (1 - x) * y * (1 - z) * (double)lag_prev(a, g, i0, j1, k0) +
-           (1 - x) * y * z * (double)lag_prev(a, g, i0, j1, k1) +
-           x * (1 - y) * (1 - z) * (double)lag_prev(a, g, i1, j0, k0) +
-           x * (1 - y) * z * (double)lag_prev(a, g, i1, j0, k1) +
-           x * y * (1 - z) * (double)lag_prev(a, g, i1, j1, k0) + x * y * z * (double)lag_prev(a, g, i1, j1, k1);
+    const FT ax = FT(1) - x, ay = FT(1) - y;
+    const ZT az = ZT(1) - z;
+    return ZT(ax * ay) * az * ZT(lag_prev(a, g, i0, j0, k0)) + ZT(ax * ay) * z * ZT(lag_prev(a, g, i0, j0, k1)) +
+           ZT(ax * y) * az * ZT(lag_prev(a, g, i0, j1, k0)) + ZT(ax * y) * z * ZT(lag_prev(a, g, i0, j1, k1)) +
+           ZT(x * ay) * az * ZT(lag_prev(a, g, i1, j0, k0)) + ZT(x * ay) * z * ZT(lag_prev(a, g, i1, j0, k1)) +
+           ZT(x * y) * az * ZT(lag_prev(a, g, i1, j1, k0)) + ZT(x * y) * z * ZT(lag_prev(a, g, i1, j1, k1));
 }
 
 // FP64 sums of two arrays per block (grid-stride, fixed order for a fixed launch):
@@ -263,18 +270,31 @@ __global__ void __launch_bounds__(dyn::TX * dyn::TY) k_lag_step(LagP<FT> P) {
     // the reference's form where T is 0, infinite or NaN (τ infinite or NaN)
     const double eps = (Td > 0.0 && Td < INFINITY) ? dt / (Td + dt) : (dt / Td) / (1 + dt / Td);
     // departure point: the node minus the displacement by the cell's own u[i, j, k],
-    // v[i, j, k], w[i, j, k] over Δt, each clamped to one cell width
-    const double x = P.x0 + (i + 0.5) * P.dx, y = P.y0 + (j + 0.5) * P.dy, z = P.zc[k];
+    // v[i, j, k], w[i, j, k] over Δt, each clamped to one cell width.  The nodes and
+    // spacings are the grid's (FT; zc and the first centres rounded to FT on the host), the
+    // displaced point FP64; the fractional x and y indices are converted to FT
+    // (fractional_x_index, Fields/interpolate.jl:60-66), the z index keeps FP64 on a
+    // regular grid (the type of z, :190-194) and is converted to FT on a stretched one (:196-201)
+    const double x = (double)FT(P.x0 + (i + 0.5) * P.dx), y = (double)FT(P.y0 + (j + 0.5) * P.dy), z = P.zc[k];
     const double ddx = jl_clamp((double)P.vel.u.in(i, j, k) * dt, -(double)g.dx, (double)g.dx);
     const double ddy = jl_clamp((double)P.vel.v.in(i, j, k) * dt, -(double)g.dy, (double)g.dy);
     const double ddz = jl_clamp((double)P.vel.w.in(i, j, k) * dt, -(double)dzk, (double)dzk);
-    const double fi = (x - ddx - P.xc0) * P.rdx + 1;
-    const double fj = (y - ddy - P.yc0) * P.rdy + 1;
-    const double fk = lag_frac_z(P, z - ddz);
-    double xi, yi, zi;
-    const int i0 = lag_interpolator(fi, xi), j0 = lag_interpolator(fj, yi), k0 = lag_interpolator(fk, zi);
-    const double imm = lag_trilinear(P.jmm_prev, g, i0, j0, k0, xi, yi, zi);
-    const double ilm = lag_trilinear(P.jlm_prev, g, i0, j0, k0, xi, yi, zi);
+    const FT fi = FT((x - ddx - P.xc0) * P.rdx) + FT(1);
+    const FT fj = FT((y - ddy - P.yc0) * P.rdy) + FT(1);
+    FT xi, yi;
+    const int i0 = lag_interpolator(fi, xi), j0 = lag_interpolator(fj, yi);
+    double imm, ilm;
+    if (!P.stretched) {
+        double zi;
+        const int k0 = lag_interpolator(lag_frac_z(P, z - ddz), zi);
+        imm = lag_trilinear<FT, double>(P.jmm_prev, g, i0, j0, k0, xi, yi, zi);
+        ilm = lag_trilinear<FT, double>(P.jlm_prev, g, i0, j0, k0, xi, yi, zi);
+    } else {
+        FT zi;
+        const int k0 = lag_interpolator(FT(lag_frac_z(P, z - ddz)), zi);
+        imm = (double)lag_trilinear<FT, FT>(P.jmm_prev, g, i0, j0, k0, xi, yi, zi);
+        ilm = (double)lag_trilinear<FT, FT>(P.jlm_prev, g, i0, j0, k0, xi, yi, zi);
+    }
     P.jmm[idx] = FT(eps * (double)MM + (1 - eps) * imm);
     const double lms = eps * (double)LM + (1 - eps) * jl_max(ilm, (double)P.lm_min);
     P.jlm[idx] = FT(jl_max(lms, (double)P.lm_min));

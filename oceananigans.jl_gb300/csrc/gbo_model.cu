@@ -656,7 +656,8 @@ struct ModelImpl : gbo_model {
         if (lagrangian) {
             for (DBuf<FT>* b : {&lag_jlm, &lag_jmm, &lag_jlm_prev, &lag_jmm_prev}) b->alloc(N);
             std::vector<double> zc(Nz);
-            for (int k = 0; k < Nz; ++k) zc[k] = (double)Z.at(Z.zc, k + 1);
+            // the grid's FT nodes (the reference interpolates on eltype(grid) coordinates)
+            for (int k = 0; k < Nz; ++k) zc[k] = (double)(FT)Z.at(Z.zc, k + 1);
             lag_zc.upload(zc);
             lag_x0 = gd->x[0];
             lag_y0 = gd->y[0];
@@ -1219,12 +1220,13 @@ struct ModelImpl : gbo_model {
         L.y0 = lag_y0;
         L.dx = (grid.x[1] - grid.x[0]) / Nx;
         L.dy = (grid.y[1] - grid.y[0]) / Ny;
-        L.xc0 = L.x0 + 0.5 * L.dx;
-        L.yc0 = L.y0 + 0.5 * L.dy;
-        L.rdx = 1.0 / L.dx;
-        L.rdy = 1.0 / L.dy;
+        // the grid's FT first centres and spacings, promoted
+        L.xc0 = (double)(FT)(L.x0 + 0.5 * L.dx);
+        L.yc0 = (double)(FT)(L.y0 + 0.5 * L.dy);
+        L.rdx = 1.0 / (double)(FT)L.dx;
+        L.rdy = 1.0 / (double)(FT)L.dy;
         L.zc = lag_zc.p;
-        L.dz1 = (double)Z.at(Z.dzc, 1);
+        L.dz1 = (double)(FT)Z.at(Z.dzc, 1);
         L.rdz1 = 1.0 / L.dz1;
         L.stretched = stretched_z ? 1 : 0;
         L.clock = lag_s.p;

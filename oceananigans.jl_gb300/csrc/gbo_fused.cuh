@@ -12,9 +12,9 @@
 //     south values with its neighbours through shared memory, and carries the
 //     top value to the next level as the bottom value.
 // The extra faces on the tile's east column and north row are evaluated by
-// warps 0 and 1 after their own work, by a separately compiled form of the face code
-// that takes the vertical windows of those columns from a small shared-memory ring,
-// prefetched two levels ahead.
+// warps 0 and 1 after their own work, taking the vertical windows of those columns from
+// a small shared-memory ring prefetched two levels ahead; off an immersed grid by a
+// separately compiled form of the face code (on an immersed grid one copy serves both).
 #pragma once
 #include <initializer_list>
 #include <type_traits>

@@ -1,9 +1,9 @@
 """Ensembles: members of different sizes and physics advanced by one graph launch
-per step must match the same models stepped one by one (bit for bit where the
-step is deterministic; CG dot products accumulate with atomics in a varying
-order, so the CG member, solved to a 1e-12 relative residual, within 1e-10),
-and each FP32 member must match its own FP64 oracle run
-within the FP32 bar of the parity tests (1e-4 relative L2)."""
+per step must match the same models stepped one by one (bit for bit for the spectral
+members; the CG member, solved to a 1e-12 relative residual, within 1e-10), and each
+FP32 member must match its own FP64 oracle run within the FP32 bar of the parity tests
+(1e-4 relative L2): two mixed members, and one member of every size class of the
+64-member benchmark ensemble (Nx = Ny in {64, 96, 128}, Nz in {32, 48, 64})."""
 import numpy as np
 import pytest
 
@@ -54,3 +54,17 @@ def test_ensemble_fp32_members_against_fp64_oracle():
         r.time_step(2.0, 5)
         for name in ("u", "v", "w", "b"):
             assert cases.rel_l2(m.get(name), r.get(name)) <= 1e-4, name
+
+
+def test_ensemble_every_size_class_against_fp64_oracle():
+    sizes = [(n, n, nz) for n in (64, 96, 128) for nz in (32, 48, 64)]
+    specs = [cases.convection_3d(sz, float_type=np.float32, seed=10 + q) for q, sz in enumerate(sizes)]
+    ens = og.Ensemble([(c.grid, c.physics) for c in specs])
+    for m, c in zip(ens.members, specs):
+        og.set_(m, **c.init)
+    ens.time_step(2.0, 5)
+    for q, (m, c) in enumerate(zip(ens.members, specs)):
+        r = cases.convection_3d(sizes[q], seed=10 + q).start_oracle()
+        r.time_step(2.0, 5)
+        for name in ("u", "v", "w", "b"):
+            assert cases.rel_l2(m.get(name), r.get(name)) <= 1e-4, (sizes[q], name)

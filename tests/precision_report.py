@@ -1,7 +1,8 @@
 """FP32 against FP64 on the GPU for the benchmark configurations: relative L2 per
 field after 1, 10, 50 and 100 steps, the floor set by FP32 initial fields (FP64 run
 from the FP32-rounded initial state), and the worst of the 64 ensemble members.
-Writes gpurun_out/precision_report.json.  Usage: python tests/precision_report.py
+Writes the JSON report to the path in PRECISION_REPORT (default precision_report.json
+in the working directory).  Usage: python tests/precision_report.py
 [conv] [conv_fp32init] [stretched] [seamount] [ensemble]  (all by default).
 A GPU script, not a pytest module; the bars it reports are asserted by
 tests/test_gpu_parity.py, test_gpu_precision.py and test_gpu_horizons.py."""
@@ -72,6 +73,8 @@ if "ensemble" in which:
     worst = {n: max(e[n] for e in errs) for n in ("u", "v", "w", "b")}
     out["ensemble"] = {"members": errs, "worst": worst}
     print("ensemble 64 members 100 steps %.1f s" % (time.time() - t0), json.dumps(worst), flush=True)
-os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-with open(os.path.join(ROOT, "gpurun_out", "precision_report.json"), "w") as f:
+path = os.environ.get("PRECISION_REPORT", "precision_report.json")
+if os.path.dirname(path):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+with open(path, "w") as f:
     json.dump(out, f, indent=1, default=str)

@@ -90,7 +90,8 @@ typedef struct gbo_grid_desc {
  * coriolis, tracers, boundary_conditions, pressure_solver)
  * (src/Models/NonhydrostaticModels/nonhydrostatic_model.jl:124-313). */
 typedef struct gbo_model_desc {
-    int32_t advection;               /* gbo_advection */
+    int32_t advection;               /* gbo_advection: only GBO_ADVECTION_WENO5 is implemented (the
+                                        default here; the reference's own default is Centered()) */
     int32_t closure;                 /* gbo_closure */
     double  closure_C;               /* Smagorinsky C (0.16) or AMD C (1/3) */
     double  closure_Cb;              /* Lilly reduction factor Cb (1.0); 0 gives the constant-coefficient

@@ -102,6 +102,12 @@ one_value(x::NamedTuple) = Float64(first(values(x)))   # one Pr / κ for every t
 padded4(x::Number) = ntuple(_ -> Float64(x), 4)
 padded4(x::NamedTuple) = ntuple(n -> n ≤ length(x) ? Float64(values(x)[n]) : 0.0, 4)
 
+# WENO(order=5) is the only advection scheme of the library (the reference's default,
+# Centered(), and bounded or lower-order WENO are refused rather than replaced)
+advection_desc(a::WENO{3}) = isnothing(a.bounds) ? (; advection = Int32(5)) :
+    throw(ArgumentError("bounded WENO advection is not available on GB300"))
+advection_desc(a) = throw(ArgumentError("advection $(summary(a)) is not available on GB300: use WENO(order=5)"))
+
 closure_desc(::Nothing) = (; closure = Int32(0))
 # a constant coefficient is the Lilly form with Cb = 0 (smagorinsky.jl:47,106)
 closure_desc(c::Smagorinsky{<:Any, <:Number}) =
@@ -150,7 +156,8 @@ function describe(model, md::ModelDesc)
          (; timestepper = Int32(1), ab2_chi = Float64(model.timestepper.χ)) : (; timestepper = Int32(0))
     return with(md; ntracers = Int32(length(tracers)), buoyancy_tracer = Int32(b),
                 tracer_flux_top = tops, tracer_flux_bottom = bots,
-                closure_desc(model.closure)..., solver_desc(model.pressure_solver)..., f..., ts...)
+                advection_desc(model.advection)..., closure_desc(model.closure)..., solver_desc(model.pressure_solver)...,
+                f..., ts...)
 end
 
 check(rc, h=C_NULL) = rc == 0 ||

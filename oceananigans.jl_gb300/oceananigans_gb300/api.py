@@ -294,10 +294,11 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
                      boundary_conditions=None, pressure_solver=None, timestepper="RungeKutta3"):
     """Translate NonhydrostaticModel keyword arguments into the C ABI's gbo_model_desc.
 
-    Follows the reference constructor's choices: default advection WENO(), the
-    pressure solver picked from the grid (nonhydrostatic_pressure_solver,
-    src/Models/NonhydrostaticModels/NonhydrostaticModels.jl:30-76), and
-    ArgumentError-style failures raised as ValueError.
+    Follows the reference constructor's choices: the pressure solver picked from the grid
+    (nonhydrostatic_pressure_solver, src/Models/NonhydrostaticModels/NonhydrostaticModels.jl:
+    30-76), and ArgumentError-style failures raised as ValueError.  The reference's default
+    advection, Centered() (nonhydrostatic_model.jl:126), is not implemented here, so
+    `advection` must be given: WENO() (order 5).
     """
     if isinstance(timestepper, QuasiAdamsBashforth2TimeStepper):
         ab2_chi, timestepper = timestepper.chi, "QuasiAdamsBashforth2"
@@ -305,7 +306,8 @@ def model_descriptor(grid, advection=None, closure=None, buoyancy=None, coriolis
         ab2_chi = 0.1
     if timestepper not in ("RungeKutta3", "QuasiAdamsBashforth2"):
         raise ValueError("timestepper = :%s is not supported; use :RungeKutta3 or :QuasiAdamsBashforth2" % timestepper)
-    advection = advection if advection is not None else WENO()
+    if advection is None:
+        raise ValueError("advection: the reference's default Centered() is not implemented; pass advection=WENO()")
     if not isinstance(advection, WENO):
         raise ValueError("advection must be WENO(order=5)")
     if isinstance(tracers, str):

@@ -64,6 +64,7 @@ def test_invalid_extent_rejected_before_device():
 
 
 def _create(grid, **kw):
+    kw.setdefault("advection", og.WENO())
     d, _ = og.api.model_descriptor(grid, **kw)
     g = grid.descriptor()
     h = ctypes.c_void_p()
@@ -80,7 +81,7 @@ def test_validation_messages():
     with pytest.raises(ValueError, match="Periodic"):
         og.RectilinearGrid(size=(16, 16, 8), topology=("Bounded", "Periodic", "Bounded"))
     with pytest.raises(ValueError, match="BuoyancyTracer"):
-        og.api.model_descriptor(grid, buoyancy=og.BuoyancyTracer(), tracers=("c",))
+        og.api.model_descriptor(grid, advection=og.WENO(), buoyancy=og.BuoyancyTracer(), tracers=("c",))
     stretched = og.RectilinearGrid(size=(16, 16, 8), z=np.linspace(-1, 0, 9) ** 3)
     with pytest.raises(ValueError, match="regular"):
         _create(stretched, pressure_solver=og.FFTBasedPoissonSolver())
@@ -108,7 +109,7 @@ def test_ensemble_arguments_rejected_before_device():
         og.Ensemble([(c.grid, c.physics), (c.grid, qab2)])
     flat = og.RectilinearGrid(size=(16, 16), x=(0, 1), y=(0, 1), topology=("Periodic", "Periodic", "Flat"))
     with pytest.raises(ValueError, match="member 0: DynamicSmagorinsky requires"):
-        og.Ensemble([(flat, dict(closure=og.DynamicSmagorinsky(averaging=(1, 2))))])
+        og.Ensemble([(flat, dict(advection=og.WENO(), closure=og.DynamicSmagorinsky(averaging=(1, 2))))])
     with pytest.raises(ValueError, match="invalid ensemble arguments"):
         og.Ensemble([])
 

@@ -169,10 +169,11 @@ def test_unsupported_averaging_and_grids_rejected():
     flat = og.RectilinearGrid(size=(16, 16), x=(0, 1), y=(0, 1), topology=("Periodic", "Periodic", "Flat"))
     # invalid configurations are rejected on the host, before any device work
     with pytest.raises(ValueError, match="Bounded z"):
-        og.NonhydrostaticModel(flat, closure=og.DynamicSmagorinsky())
+        og.NonhydrostaticModel(flat, advection=og.WENO(), closure=og.DynamicSmagorinsky())
     c = cases.seamount((16, 16, 8), solver="cg")
     with pytest.raises(ValueError, match="ImmersedBoundaryGrid"):
-        og.NonhydrostaticModel(c.grid, closure=og.DynamicSmagorinsky(), pressure_solver=og.ConjugateGradientPoissonSolver())
+        og.NonhydrostaticModel(c.grid, advection=og.WENO(), closure=og.DynamicSmagorinsky(),
+                               pressure_solver=og.ConjugateGradientPoissonSolver())
 
 
 # ---- LagrangianAveraging (dynamic_coefficient.jl:322-487): the oracle's restatement ----
@@ -350,7 +351,7 @@ def test_closure_defaults_and_descriptor():
     assert og.DynamicSmagorinsky(averaging=[2, 1]).averaging == (1, 2)
     for closure, avg in ((d0, L.GBO_AVERAGING_LAGRANGIAN),
                          (og.DynamicSmagorinsky(averaging=(1, 2), Pr=0.5, minimum_numerator=1e-20), L.GBO_AVERAGING_XY)):
-        d, _ = model_descriptor(c.grid, closure=closure, tracers=("b",), buoyancy=og.BuoyancyTracer())
+        d, _ = model_descriptor(c.grid, advection=og.WENO(), closure=closure, tracers=("b",), buoyancy=og.BuoyancyTracer())
         assert d.closure == L.GBO_CLOSURE_DYNAMIC_SMAGORINSKY and d.closure_averaging == avg
         assert d.closure_Pr == closure.Pr and d.closure_min_numerator == closure.minimum_numerator
 

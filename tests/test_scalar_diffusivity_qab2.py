@@ -66,6 +66,6 @@ def test_scalar_diffusivity_descriptor():
     m_desc = c.oracle_model().desc
     assert m_desc.closure == 3 and m_desc.closure_nu == 1.0 and m_desc.closure_kappa[0] == 1.0
     with pytest.raises(ValueError, match="tracer"):
-        og.api.model_descriptor(c.grid, closure=og.ScalarDiffusivity(nu=1, kappa={"d": 1.0}), tracers=("c",))
+        og.api.model_descriptor(c.grid, advection=og.WENO(), closure=og.ScalarDiffusivity(nu=1, kappa={"d": 1.0}), tracers=("c",))
     with pytest.raises(ValueError, match="timestepper"):
-        og.api.model_descriptor(c.grid, timestepper="SplitRungeKutta3")
+        og.api.model_descriptor(c.grid, advection=og.WENO(), timestepper="SplitRungeKutta3")

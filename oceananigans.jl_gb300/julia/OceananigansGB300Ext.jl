@@ -86,7 +86,7 @@ using Oceananigans.BuoyancyFormulations: BuoyancyTracer
 using Oceananigans.Coriolis: FPlane
 using Oceananigans.BoundaryConditions: BoundaryCondition, Flux
 using Oceananigans.Solvers: FFTBasedPoissonSolver, FourierTridiagonalPoissonSolver, ConjugateGradientPoissonSolver
-using Oceananigans.TimeSteppers: QuasiAdamsBashforth2TimeStepper
+using Oceananigans.TimeSteppers: QuasiAdamsBashforth2TimeStepper, RungeKutta3TimeStepper
 
 # a copy of d with the named fields replaced
 function with(d::ModelDesc; kw...)
@@ -153,7 +153,9 @@ function describe(model, md::ModelDesc)
         model.coriolis isa Nothing ? (; has_coriolis = Int32(0)) :
         throw(ArgumentError("only FPlane Coriolis is available on GB300"))
     ts = model.timestepper isa QuasiAdamsBashforth2TimeStepper ?
-         (; timestepper = Int32(1), ab2_chi = Float64(model.timestepper.χ)) : (; timestepper = Int32(0))
+         (; timestepper = Int32(1), ab2_chi = Float64(model.timestepper.χ)) :
+         model.timestepper isa RungeKutta3TimeStepper ? (; timestepper = Int32(0)) :
+         throw(ArgumentError("timestepper $(summary(model.timestepper)) is not available on GB300"))
     return with(md; ntracers = Int32(length(tracers)), buoyancy_tracer = Int32(b),
                 tracer_flux_top = tops, tracer_flux_bottom = bots,
                 advection_desc(model.advection)..., closure_desc(model.closure)..., solver_desc(model.pressure_solver)...,

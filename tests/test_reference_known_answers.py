@@ -1,0 +1,83 @@
+"""Known-answer tests of the reference's own suite (test/test_dynamics.jl), run on the FP64
+oracle with the reference's tolerances.  They anchor the oracle, which the GPU parity
+tests compare the library against, to the reference's own expectations at the level of
+whole time steps.  Differences from the reference's setups: WENO(order=5) advection in
+place of the default Centered() (the only scheme of this path), Periodic x and y with
+a Bounded z (the path's topology), and no SeawaterBuoyancy (not in the path: the
+advected tracer is passive)."""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+import oceananigans_gb300 as og
+
+TIMESTEPPERS = ("RungeKutta3", "QuasiAdamsBashforth2")
+
+
+def _case(size, extent, init, ophys, **physics):
+    gkw = dict(size=size, x=(0, extent[0]), y=(0, extent[1]), z=(-extent[2], 0),
+               topology=("Periodic", "Periodic", "Bounded"))
+    return cases.Case(og.RectilinearGrid(**gkw), init, gkw, ophys, advection=og.WENO(), **physics)
+
+
+def _diffusive(size, init, timestepper, nu=1.0, kappa=1.0):
+    ophys = dict(closure=("ScalarDiffusivity", {"nu": nu, "kappa": kappa}), tracers=("c",), timestepper=timestepper)
+    return _case(size, (1, 1, 1), init, ophys, closure=og.ScalarDiffusivity(nu=nu, kappa=kappa), tracers=("c",),
+                 timestepper=timestepper)
+
+
+@pytest.mark.parametrize("timestepper", TIMESTEPPERS)
+@pytest.mark.parametrize("fieldname", ["u", "v", "c"])
+def test_diffusion_simple(fieldname, timestepper):
+    # test_diffusion_simple (test_dynamics.jl:15-30): a constant field under
+    # ScalarDiffusivity(ν=1, κ=1) stays that constant through 10 steps of Δt = 1
+    size = (8, 8, 16)
+    c = _diffusive(size, {fieldname: np.full(size, math.pi)}, timestepper)
+    r = c.start_oracle()
+    r.time_step(1.0, 10)
+    assert np.allclose(r.get(fieldname), math.pi, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("timestepper", TIMESTEPPERS)
+@pytest.mark.parametrize("fieldname", ["u", "v", "c"])
+def test_scalar_diffusivity_budget(fieldname, timestepper):
+    # test_diffusion_budget / test_ScalarDiffusivity_budget (test_dynamics.jl:32-54): the
+    # mean of a random field is conserved by 10 steps of Δt = 1e-4 Δz² / κ
+    # (isapprox's default relative tolerance, √eps)
+    size = (8, 8, 8)
+    rng = np.random.default_rng(7)
+    c = _diffusive(size, {fieldname: rng.uniform(0, 1, size)}, timestepper)
+    r = c.start_oracle()
+    before = r.get(fieldname).mean()
+    dz = 1.0 / size[2]
+    r.time_step(1e-4 * dz ** 2 / 1.0, 10)
+    assert r.get(fieldname).mean() == pytest.approx(before, rel=math.sqrt(np.finfo(float).eps))
+
+
+@pytest.mark.parametrize("timestepper", TIMESTEPPERS)
+def test_passive_tracer_advection(timestepper):
+    # passive_tracer_advection_test (test_dynamics.jl:175-207): a Gaussian advected by a
+    # uniform (U, V) for 100 steps of Δt = 0.05 Δx / |U|, ν = κ = 1e-12;
+    # mean((T - T_exact)²) / mean(T_exact²) < 1e-4
+    N, L, U, V = 128, 1.0, 0.5, 0.8
+    delta, x0, y0 = L / 15, L / 2, L / 2
+    dt = 0.05 * L / N / math.sqrt(U ** 2 + V ** 2)
+    xc = (np.arange(N) + 0.5) * L / N
+
+    def exact(t):
+        X, Y = np.meshgrid(xc, xc, indexing="ij")
+        T = np.exp(-((X - U * t - x0) ** 2 + (Y - V * t - y0) ** 2) / (2 * delta ** 2))
+        return np.broadcast_to(T[:, :, None], (N, N, 2)).copy()
+
+    size = (N, N, 2)
+    init = {"u": np.full(size, U), "v": np.full(size, V), "T": exact(0.0)}
+    ophys = dict(closure=("ScalarDiffusivity", {"nu": 1e-12, "kappa": 1e-12}), tracers=("T",), timestepper=timestepper)
+    c = _case(size, (L, L, L), init, ophys, closure=og.ScalarDiffusivity(nu=1e-12, kappa=1e-12), tracers=("T",),
+              timestepper=timestepper)
+    r = c.start_oracle()
+    r.time_step(dt, 100)
+    t, _ = r.clock()
+    num, ex = r.get("T"), exact(t)
+    assert np.mean((num - ex) ** 2) / np.mean(ex ** 2) < 1e-4

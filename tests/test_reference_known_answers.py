@@ -115,3 +115,24 @@ def test_immersed_diffusion():
     assert np.allclose(cb, ca, rtol=math.sqrt(np.finfo(float).eps), atol=0)
     # the profile has diffused: the check compares evolved values
     assert np.max(np.abs(ca - init["c"][:, :, half:])) > 1e-2
+
+
+@pytest.mark.parametrize("side", ["top", "bottom"])
+def test_tracer_flux_budget(side):
+    # test_nonhydrostatic_flux_budget (test_boundary_conditions_integration.jl:32-56,
+    # 671-722): a tracer starting at zero under a Flux boundary condition of magnitude π
+    # into the domain (−π on the top, +π on the bottom: the flux is positive upward), no
+    # closure, one step of Δt = 1: the domain mean is flux t / Lz.  The reference's
+    # 2 x 2 x 2 box of (0, 0.3) x (0, 0.4) x (0, 0.5) becomes 8 x 8 x 8 cells of the same box
+    # (the budget does not depend on the resolution) with Periodic x and y.
+    size, Lz = (8, 8, 8), 0.5
+    flux = math.pi * (-1 if side == "top" else 1)
+    gkw = dict(size=size, x=(0, 0.3), y=(0, 0.4), z=(0, Lz), topology=("Periodic", "Periodic", "Bounded"))
+    ophys = dict(tracers=("c",), **{"flux_" + side: {"c": flux}})
+    bc = og.FieldBoundaryConditions(**{side: og.FluxBoundaryCondition(flux)})
+    c = cases.Case(og.RectilinearGrid(**gkw), {"c": np.zeros(size)}, gkw, ophys, advection=og.WENO(), tracers=("c",),
+                   boundary_conditions={"c": bc})
+    r = c.start_oracle()
+    r.time_step(1.0, 1)
+    t, _ = r.clock()
+    assert r.get("c").mean() == pytest.approx(math.pi * t / Lz, rel=math.sqrt(np.finfo(float).eps))

@@ -162,3 +162,28 @@ def test_fft_poisson_solver_second_order_convergence(sizes, mode):
     e1, e2 = _analytic_poisson_l1(n1, mode), _analytic_poisson_l1(n2, mode)
     rate = math.log(e1 / e2) / math.log(n2 / n1)
     assert rate == pytest.approx(2, rel=5e-3), rate
+
+
+def test_inertial_oscillation():
+    # inertial_oscillations_work_with_rotation_in_different_axis (test_dynamics.jl:354-396),
+    # its FPlane half: a uniform u = 1 under FPlane(f = 1), no buoyancy, tracers or closure,
+    # RungeKutta3 with Δt = 1e-3 to t = π (half an inertial period, the last step shortened
+    # to land on it, as run! with a stop_time does): w stays exactly 0 and the speed stays
+    # 1 (isapprox, √eps); the velocity has turned to (u, v) = (cos t, -sin t) = (-1, 0)
+    # within the RK3 error.  The reference's grid has no points (Flat x, y, z); here a
+    # uniform flow on 8 x 8 x 8 Periodic, Periodic, Bounded cells.
+    size = (8, 8, 8)
+    gkw = dict(size=size, x=(0, 1), y=(0, 1), z=(-1, 0), topology=("Periodic", "Periodic", "Bounded"))
+    c = cases.Case(og.RectilinearGrid(**gkw), {"u": np.ones(size)}, gkw, dict(coriolis=1.0),
+                   advection=og.WENO(), coriolis=og.FPlane(1.0))
+    r = c.start_oracle()
+    dt, stop = 1e-3, math.pi
+    n = int(stop / dt)
+    r.time_step(dt, n)
+    r.time_step(stop - n * dt)
+    t, _ = r.clock()
+    assert t == pytest.approx(stop, rel=1e-15)
+    u, v, w = r.get("u"), r.get("v"), r.get("w")
+    assert np.all(w == 0.0)
+    assert np.allclose(np.hypot(u, v), 1.0, rtol=math.sqrt(np.finfo(float).eps), atol=0)
+    assert np.allclose(u, math.cos(t), atol=1e-7) and np.allclose(v, -math.sin(t), atol=1e-7)
